@@ -1,0 +1,394 @@
+#!/usr/bin/env python3
+"""Benchmark: DoF/s of assembly + solve at <= 1e-10 relative error against
+FP64, mixed-precision versus plain FP64 on the GPU, with p50/p99 latency.
+
+Workload (default): 3D Poisson, unit cube 64^3 Kuhn tetrahedra (1,572,864
+cells), H1P2 (2,146,689 DoFs), per-cell kappa = exp(N(0,1)) (seed 0),
+f = 8 seeded Fourier modes, homogeneous Dirichlet.  One step = FP64 (+ FP32)
+assembly of the matrix, the right-hand side, Dirichlet elimination and the
+solve; inputs (mesh, pattern, kappa) are resident in HBM when a timed step
+starts.  The matrix (~490 MB FP64) and its FP32 copy exceed the 129 MB L2, so
+no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 64]
+
+Under torchrun (N > 1) every rank solves its own replica (the path does not
+shard: replicas only, weak scaling); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "gradientrobustmultiphysics.jl_gb300")
+METRIC = "DoF/s assembly+solve at 1e-10 rel err vs FP64: mixed vs plain GPU; p50/p99 latency"
+
+
+def _package():
+    if "grmp_gb300" in sys.modules:
+        return sys.modules["grmp_gb300"]
+    spec = importlib.util.spec_from_file_location("grmp_gb300", os.path.join(PKG_DIR, "__init__.py"),
+                                                  submodule_search_locations=[PKG_DIR])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["grmp_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"grmp_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], p[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle port)
+def cpu_port_step(n_cpu: int, reltol: float, seed: int = 0):
+    """One bounded sample of the same workload on the host cores: the oracle's
+    single-threaded assembly (the reference's item loop) + OpenMP FP64 CG.
+    Returns (dofs, seconds, assembly_s, solve_s, iterations)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from grmp_gb300 import problems as P
+    prob = P.poisson3d(n_cpu, seed=seed)
+    FES = prob.FES
+    g = FES.xgrid
+    t0 = time.perf_counter()
+    M = O.Matrix(FES.ndofs)
+    op = prob.operators[0]
+    M.add_bilinear(g.coords, g.cells, 2, 1, FES.celldofs, O.OP_GRADIENT, True, 1.0, O.ACT_CELLSCALE, op.cell_coef)
+    b = np.zeros(FES.ndofs)
+    f = prob.rhs.f
+    O.assemble_linear(b, g.coords, g.cells, 2, 1, FES.celldofs, f.kind, f.params)
+    M.penalize(prob.fixed)
+    A = M.csr()
+    bb = O.penalized_rhs(b, prob.fixed)
+    t1 = time.perf_counter()
+    x, it, rr = O.solve_cg(A, bb, reltol)
+    t2 = time.perf_counter()
+    return FES.ndofs, t2 - t0, t1 - t0, t2 - t1, it
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    for _ in range(args.warmup):
+        cpu_port_step(args.cpu_n, args.reltol)
+    times, dofs = [], 0
+    for _ in range(args.steps):
+        dofs, dt, _, _, _ = cpu_port_step(args.cpu_n, args.reltol)
+        times.append(dt)
+    v = dofs / statistics.mean(times)
+    line = {"metric": METRIC, "value": v, "unit": "DoF/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": f"poisson3d_P2_kuhn{args.n}_lognormal_kappa (sample: {args.cpu_n}^3 cubes)",
+                       "sample_dofs": dofs},
+            "cpu_baseline": {"value": v, "unit": "DoF/s", "cores": cores, "kind": "port",
+                             "sample": f"3D P2 Poisson on {args.cpu_n}^3 Kuhn cubes ({dofs} DoFs): single-thread "
+                                       f"assembly (reference item loop) + {cores}-thread FP64 Jacobi-CG to "
+                                       f"relative residual {args.reltol:g} (Julia reference not runnable here)"},
+            "e2e": {"value": v, "unit": "DoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool) -> float:
+    """Algorithmic DRAM bytes of one persistent PCG launch."""
+    it, outer = stats["iterations"], stats["outer_iterations"]
+    if mixed:
+        per_it = 8.0 * nnz + 56.0 * n
+        per_outer = 12.0 * nnz + 64.0 * n
+        return it * per_it + (outer + 1) * per_outer
+    return it * (12.0 * nnz + 108.0 * n) + 2 * (12.0 * nnz + 36.0 * n)
+
+
+def run_ours(args):
+    dist = Dist()
+    G = _package()
+    from grmp_gb300 import build as B
+    from grmp_gb300 import problems as P
+    from grmp_gb300 import _lib as L
+    B.build()
+    import torch
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    ctx = G.GB300Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    prob = P.poisson3d(args.n, seed=args.seed + dist.rank)
+    FES = prob.FES
+    ndofs = FES.ndofs
+    op = prob.operators[0]
+    # resident inputs: kappa in a device vector (coefficient read in place)
+    kdev = G.FEVector.__new__(G.FEVector)
+    kdev.ctx = ctx
+    kdev.h = ctypes.c_void_p()
+    ctx.check(ctx.lib.grmp_vector_create(ctx.h, FES.xgrid.ncells, ctypes.byref(kdev.h)))
+    kap = np.ascontiguousarray(op.cell_coef, dtype=np.float64)
+    ctx.check(ctx.lib.grmp_vector_upload(kdev.h, kap.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    kptr = ctypes.c_void_p()
+    ctx.check(ctx.lib.grmp_vector_device_ptr(kdev.h, ctypes.byref(kptr)))
+
+    def dev_term():
+        t = L.BilinearTerm()
+        t.op_kind = L.OP_LAPLACE
+        t.symmetric = 1
+        t.factor = 1.0
+        t.cell_coef = ctypes.cast(kptr, ctypes.POINTER(ctypes.c_double))
+        t.bonus_quadorder = 0
+        t.coef_on_device = 1
+        return t
+
+    dev_terms = (L.BilinearTerm * 1)(dev_term())
+    A = G.FEMatrix(ctx, FES, prob.operators)
+    b = G.FEVector(ctx, FES)
+    x = G.FEVector(ctx, FES)
+    nnz = A.nnz
+
+    def step(mode: str, host_inputs: bool = False):
+        if host_inputs:
+            G.assemble(A, prob.operators, G.FP64)
+            if mode == "mixed":
+                G.assemble(A, prob.operators, G.FP32)
+        else:
+            ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP64))
+            if mode == "mixed":
+                ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP32))
+        b.fill(0.0)
+        G.assemble(b, prob.rhs)
+        G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)
+        s = G.GB300PCG(mode=mode, reltol=args.reltol, abstol=0.0, inner_reltol=args.inner_reltol)
+        st = s.solve(A, b, x)
+        out = x.entries if host_inputs else None
+        return st, out
+
+    # FP64 reference solution of this system (tight tolerance, untimed)
+    G.assemble(A, prob.operators, G.FP64)
+    b.fill(0.0)
+    G.assemble(b, prob.rhs)
+    G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)
+    ref = G.GB300PCG(mode="fp64", reltol=args.ref_reltol, abstol=0.0, maxiter=200000)
+    ref_st = ref.solve(A, b, x, raise_on_error=False)
+    uref = x.entries
+
+    results = {}
+    for mode in ("fp64", "mixed"):
+        for _ in range(max(3, args.warmup)):
+            step(mode)
+        dist.barrier()
+        torch.cuda.synchronize()
+        clk = ClockSampler(dev) if mode == "mixed" else None
+        if clk:
+            clk.start()
+        l0 = ctypes.c_uint64()
+        ctx.check(ctx.lib.grmp_context_launches(ctx.h, ctypes.byref(l0)))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        stats = []
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            st, _ = step(mode)
+            ev[k][1].record(stream)
+            stats.append(st)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        dist.barrier()
+        l1 = ctypes.c_uint64()
+        ctx.check(ctx.lib.grmp_context_launches(ctx.h, ctypes.byref(l1)))
+        clocks = clk.stop() if clk else None
+        ms = [e[0].elapsed_time(e[1]) for e in ev]
+        u = x.entries
+        err = float(np.linalg.norm(u - uref) / np.linalg.norm(uref))
+        tot = dist.max(sum(ms) / 1e3)
+        results[mode] = {"ms": ms, "total_s": tot, "wall_s": wall, "stats": stats, "err": err,
+                         "launches": int(l1.value - l0.value), "clocks": clocks}
+    # end-to-end through the host-buffer API (kappa from host, solution back to host)
+    for _ in range(max(3, args.warmup)):
+        step("mixed", host_inputs=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step("mixed", host_inputs=True)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_tot = dist.max(sum(e2e_ms) / 1e3)
+    dist.barrier()
+
+    mixed, plain = results["mixed"], results["fp64"]
+    world_dofs = ndofs * dist.ws * args.steps
+    value = world_dofs / mixed["total_s"]
+    plain_value = world_dofs / plain["total_s"]
+    # roofline of the dominant kernel (persistent mixed PCG)
+    st_last = mixed["stats"][-1]
+    kb = pcg_bytes(st_last, ndofs, nnz, True)
+    kms = statistics.mean([s["solve_ms"] for s in mixed["stats"]])
+    achieved = kb / (kms / 1e3) / 1e9
+    pk = peaks()
+    peak = float(pk["hbm_gbs"]) if pk else 6800.0
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        d, dt, ta, ts, it = cpu_port_step(args.cpu_n, args.reltol)
+        cores = os.cpu_count() or 1
+        cpu = {"value": d / dt, "unit": "DoF/s", "cores": cores, "kind": "port",
+               "sample": f"3D P2 Poisson {args.cpu_n}^3 Kuhn cubes, {d} DoFs: single-thread assembly "
+                         f"{ta:.2f}s + {cores}-thread FP64 Jacobi-CG {ts:.2f}s ({it} it)"}
+    p = sorted(mixed["ms"])
+    line = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": dist.ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(mixed["ms"]), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-outer", "data": "synthetic (seeded)",
+            "config": {"workload": f"poisson3d_P2_kuhn{args.n}_lognormal_kappa", "ndofs": ndofs, "nnz": nnz,
+                       "ncells": FES.xgrid.ncells, "global_batch": dist.ws, "parallelism": f"replicas{dist.ws}",
+                       "l2": "inputs larger than L2 (matrix FP64+FP32 > 129 MB)", "reltol": args.reltol,
+                       "inner_reltol": args.inner_reltol},
+            "latency_ms": {"p50": p[len(p) // 2], "p99": p[min(len(p) - 1, int(0.99 * len(p)))]},
+            "rel_err_vs_fp64": {"mixed": mixed["err"], "plain": plain["err"],
+                                "reference": f"GPU FP64 PCG to relres {ref_st['final_relres']:.1e}"},
+            "plain_fp64": {"value": plain_value, "ms_per_step": statistics.mean(plain["ms"]),
+                           "iterations": plain["stats"][-1]["iterations"]},
+            "mixed_vs_plain": value / plain_value,
+            "solver": {"iterations": st_last["iterations"], "outer": st_last["outer_iterations"],
+                       "threads_per_row": st_last["threads_per_row"], "grid_blocks": st_last["grid_blocks"]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "k_pcg_mixed (persistent)",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world_dofs / e2e_tot, "unit": "DoF/s",
+                    "h2d_bytes_per_step": int(FES.xgrid.ncells * 8 + prob.rhs.f.params.size * 8),
+                    "d2h_bytes_per_step": int(ndofs * 8)},
+            "gpu_launches": mixed["launches"],
+            "clocks": mixed["clocks"]}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    dist.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--reltol", type=float, default=1e-11)
+    ap.add_argument("--ref-reltol", type=float, default=1e-14)
+    ap.add_argument("--inner-reltol", type=float, default=0.1)
+    ap.add_argument("--cpu-n", type=int, default=24)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,443 @@
+"""Host-side mirror of the reference's assembly / solve interface over the C-ABI.
+
+Names and argument meanings follow GradientRobustMultiPhysics.jl:
+``LaplaceOperator(kappa)`` (src/pdeoperators.jl:154-169),
+``ReactionOperator(alpha)`` (:176-203), ``HookStiffnessOperator2D(mu, lambda)``
+(:256-273), ``BilinearForm([Gradient, Gradient], action)`` (:355-396),
+``LinearForm(Identity, f)`` (:659-755), ``FEMatrix`` / ``FEVector``
+(src/fematrix.jl, src/fevector.jl), ``assemble!`` (src/assemblypatterns/
+bilinearform.jl:92, linearform.jl:47) and ``solve!`` with a ``linsolver``
+(src/solvers.jl:55, :622-686).  Every compute call goes through
+libgrmp_gpu.so; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .fespace import FESpace, FE_H1BR
+from .mesh import SimplexMesh
+
+# operator tags of src/functionoperators.jl
+Identity = "Identity"
+Gradient = "Gradient"
+SymmetricGradient = "SymmetricGradient"
+Divergence = "Divergence"
+ReconstructionIdentity = "ReconstructionIdentity"
+ReconstructionDivergence = "ReconstructionDivergence"
+
+APT_BilinearForm = "APT_BilinearForm"
+APT_SymmetricBilinearForm = "APT_SymmetricBilinearForm"
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+# ----------------------------------------------------------------------- context
+class GB300Context:
+    """One GPU, one CUDA stream, an HBM budget.  Owns every device handle."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.grmp_create_context(device, hbm_budget_bytes, ctypes.byref(h))
+        if rc != L.OK:
+            raise L.GrmpError(rc, "could not create a context (is a CUDA device visible?)")
+        self.h = h
+        self._meshes = {}
+        self._spaces = {}
+
+    def check(self, rc: int):
+        L.check(rc, self.h)
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self.check(self.lib.grmp_context_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def synchronize(self):
+        self.check(self.lib.grmp_synchronize(self.h))
+
+    def memory_in_use(self) -> int:
+        v = ctypes.c_size_t()
+        self.check(self.lib.grmp_context_memory(self.h, ctypes.byref(v)))
+        return v.value
+
+    # -- handles ------------------------------------------------------------
+    def mesh(self, grid: SimplexMesh, with_faces: bool = False):
+        key = id(grid)
+        ent = self._meshes.get(key)
+        if ent is None:
+            h = ctypes.c_void_p()
+            coords = np.ascontiguousarray(grid.coords, dtype=np.float64)
+            cells = np.ascontiguousarray(grid.cells, dtype=np.int32)
+            self.check(self.lib.grmp_mesh_upload(self.h, grid.dim, grid.nverts, _dp(coords), grid.ncells, _ip(cells),
+                                                 ctypes.byref(h)))
+            ent = {"h": h, "grid": grid, "faces": False}
+            self._meshes[key] = ent
+        if with_faces and not ent["faces"]:
+            fnodes, cfaces = grid.faces()
+            normals, vols, signs = grid.face_geometry()
+            cf = np.ascontiguousarray(cfaces, dtype=np.int32)
+            nr = np.ascontiguousarray(normals, dtype=np.float64)
+            fv = np.ascontiguousarray(vols, dtype=np.float64)
+            sg = np.ascontiguousarray(signs, dtype=np.int8)
+            self.check(self.lib.grmp_mesh_set_faces(ent["h"], fnodes.shape[0], _ip(cf), _dp(nr), _dp(fv),
+                                                    sg.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+            ent["faces"] = True
+        return ent["h"]
+
+    def space(self, FES: FESpace):
+        key = id(FES)
+        h = self._spaces.get(key)
+        if h is None:
+            mh = self.mesh(FES.xgrid, with_faces=(FES.FEType.kind == FE_H1BR))
+            h = ctypes.c_void_p()
+            cd = np.ascontiguousarray(FES.celldofs, dtype=np.int32)
+            self.check(self.lib.grmp_space_create(mh, FES.FEType.kind, FES.FEType.ncomponents, _ip(cd), FES.ndofs,
+                                                  ctypes.byref(h)))
+            self._spaces[key] = h
+        return h
+
+    def close(self):
+        if getattr(self, "h", None):
+            for h in self._spaces.values():
+                self.lib.grmp_space_destroy(h)
+            for ent in self._meshes.values():
+                self.lib.grmp_mesh_destroy(ent["h"])
+            self.lib.grmp_destroy_context(self.h)
+            self.h = None
+            self._spaces.clear()
+            self._meshes.clear()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------------- operators
+@dataclass
+class Operator:
+    """One bilinear-form term (a PDEOperator with an APT)."""
+    op_kind: int
+    symmetric: bool
+    factor: float = 1.0
+    cell_coef: Optional[np.ndarray] = None
+    params: tuple = (0.0, 0.0, 0.0, 0.0)
+    bonus_quadorder: int = 0
+    name: str = ""
+
+    def term(self) -> L.BilinearTerm:
+        t = L.BilinearTerm()
+        t.op_kind = self.op_kind
+        t.symmetric = 1 if self.symmetric else 0
+        t.factor = float(self.factor)
+        if self.cell_coef is not None:
+            self._cc = np.ascontiguousarray(self.cell_coef, dtype=np.float64)
+            t.cell_coef = _dp(self._cc)
+        else:
+            t.cell_coef = ctypes.POINTER(ctypes.c_double)()
+        for i, v in enumerate(self.params[:4]):
+            t.param[i] = float(v)
+        t.bonus_quadorder = int(self.bonus_quadorder)
+        return t
+
+
+@dataclass
+class CellCoefficient:
+    """An Action with "I" dependency: result = coef[cell] * input
+    (the reference's Action(kernel, [d, d]; dependencies = "I"))."""
+    values: np.ndarray
+    bonus_quadorder: int = 0
+
+
+def LaplaceOperator(kappa: float = 1.0, *, name: str = "auto") -> Operator:
+    """a(u,v) = kappa (grad u, grad v), APT_SymmetricBilinearForm."""
+    return Operator(L.OP_LAPLACE, True, float(kappa), name=name)
+
+
+def ReactionOperator(alpha=1.0, *, name: str = "auto") -> Operator:
+    """a(u,v) = (alpha u, v).  A number gives APT_SymmetricBilinearForm with
+    factor alpha; a CellCoefficient gives the Action form (APT_BilinearForm),
+    as in src/pdeoperators.jl:186-202."""
+    if isinstance(alpha, CellCoefficient):
+        return Operator(L.OP_MASS, False, 1.0, cell_coef=alpha.values, bonus_quadorder=alpha.bonus_quadorder,
+                        name=name)
+    return Operator(L.OP_MASS, True, float(alpha), name=name)
+
+
+def HookStiffnessOperator2D(mu: float, lam: float, *, name: str = "auto") -> Operator:
+    """a(u,v) = (C eps(u), eps(v)) with SymmetricGradient{1}, APT_BilinearForm."""
+    return Operator(L.OP_HOOKE, False, 1.0, params=(mu, lam, 0.0, 0.0), name=name)
+
+
+def HookStiffnessOperator3D(mu: float, lam: float, *, name: str = "auto") -> Operator:
+    return Operator(L.OP_HOOKE, False, 1.0, params=(mu, lam, 0.0, 0.0), name=name)
+
+
+def BilinearForm(operators: Sequence[str], action=None, *, APT: str = APT_BilinearForm, factor: float = 1.0,
+                 name: str = "auto") -> Operator:
+    """BilinearForm([op, op], action) for the operator pairs on the hot path."""
+    ops = tuple(operators)
+    sym = APT == APT_SymmetricBilinearForm
+    cc = action.values if isinstance(action, CellCoefficient) else None
+    bonus = action.bonus_quadorder if isinstance(action, CellCoefficient) else 0
+    if action is not None and not isinstance(action, CellCoefficient):
+        raise ValueError("supported actions: CellCoefficient")
+    if ops == (Gradient, Gradient):
+        return Operator(L.OP_LAPLACE, sym, factor, cell_coef=cc, bonus_quadorder=bonus, name=name)
+    if ops == (Identity, Identity):
+        return Operator(L.OP_MASS, sym, factor, cell_coef=cc, bonus_quadorder=bonus, name=name)
+    if ops == (ReconstructionDivergence, ReconstructionDivergence):
+        return Operator(L.OP_RDIVRDIV, sym, factor, cell_coef=cc, bonus_quadorder=bonus, name=name)
+    raise ValueError(f"BilinearForm{ops} is not on the GPU path")
+
+
+# ----------------------------------------------------------------------- data functions
+@dataclass
+class DataFunction:
+    """Right-hand side data of the kinds the library evaluates on device."""
+    kind: int
+    ncomponents: int
+    params: np.ndarray
+    bonus_quadorder: int = 0
+
+    @staticmethod
+    def constant(values, bonus_quadorder: int = 0) -> "DataFunction":
+        v = np.atleast_1d(np.asarray(values, dtype=np.float64))
+        return DataFunction(L.RHS_CONST, v.size, v, bonus_quadorder)
+
+    @staticmethod
+    def cellwise(values: np.ndarray, bonus_quadorder: int = 0) -> "DataFunction":
+        v = np.asarray(values, dtype=np.float64)
+        nc = 1 if v.ndim == 1 else v.shape[1]
+        return DataFunction(L.RHS_CELL, nc, v.reshape(-1), bonus_quadorder)
+
+    @staticmethod
+    def fourier(amplitudes, wavevectors, bonus_quadorder: int = 0) -> "DataFunction":
+        a = np.asarray(amplitudes, dtype=np.float64).reshape(-1, 1)
+        k = np.asarray(wavevectors, dtype=np.float64)
+        return DataFunction(L.RHS_FOURIER, 1, np.concatenate([a, k], axis=1).reshape(-1), bonus_quadorder)
+
+    @staticmethod
+    def polynomial(terms, ncomponents: int, bonus_quadorder: int = 0) -> "DataFunction":
+        """terms: iterable of (component, coefficient, e1, e2, e3)."""
+        t = np.asarray(terms, dtype=np.float64).reshape(-1, 5)
+        return DataFunction(L.RHS_POLY, ncomponents, t.reshape(-1), bonus_quadorder)
+
+
+@dataclass
+class LinearFormOp:
+    test_operator: str
+    f: DataFunction
+    factor: float = 1.0
+
+    def rhs(self) -> L.Rhs:
+        r = L.Rhs()
+        r.kind = self.f.kind
+        r.ncomponents = self.f.ncomponents
+        self._p = np.ascontiguousarray(self.f.params, dtype=np.float64)
+        r.params = _dp(self._p)
+        r.nparams = self._p.size
+        r.factor = float(self.factor)
+        r.bonus_quadorder = int(self.f.bonus_quadorder)
+        r.test_operator = 1 if self.test_operator == ReconstructionIdentity else 0
+        return r
+
+
+def LinearForm(operator: str, f: DataFunction, *, factor: float = 1.0) -> LinearFormOp:
+    return LinearFormOp(operator, f, factor)
+
+
+# ----------------------------------------------------------------------- containers
+class FEVector:
+    """Device-resident FP64 vector over an FESpace (FEVector, src/fevector.jl)."""
+
+    def __init__(self, ctx: GB300Context, FES: FESpace, name: str = ""):
+        self.ctx = ctx
+        self.FES = FES
+        self.name = name
+        self.h = ctypes.c_void_p()
+        ctx.check(ctx.lib.grmp_vector_create(ctx.h, FES.ndofs, ctypes.byref(self.h)))
+
+    @property
+    def n(self) -> int:
+        return self.FES.ndofs
+
+    @property
+    def entries(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grmp_vector_download(self.h, _dp(out)))
+        return out
+
+    def upload(self, values: np.ndarray):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        assert v.size == self.n
+        self.ctx.check(self.ctx.lib.grmp_vector_upload(self.h, _dp(v)))
+
+    def fill(self, value: float = 0.0):
+        self.ctx.check(self.ctx.lib.grmp_vector_fill(self.h, float(value)))
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.grmp_vector_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            if self.ctx.h:
+                self.free()
+        except Exception:
+            pass
+
+
+def _terms(ops: Sequence[Operator]):
+    arr = (L.BilinearTerm * len(ops))()
+    for i, o in enumerate(ops):
+        arr[i] = o.term()
+    return arr
+
+
+class FEMatrix:
+    """Device CSR matrix over FES x FES whose sparsity pattern is the union of
+    the nonzero local contributions of `operators` (drop-exact-zero rule of
+    _addnz).  Built once; values assembled with assemble()."""
+
+    def __init__(self, ctx: GB300Context, FES: FESpace, operators: Sequence[Operator], name: str = ""):
+        self.ctx = ctx
+        self.FES = FES
+        self.operators = list(operators)
+        self.name = name
+        sh = ctx.space(FES)
+        self.h = ctypes.c_void_p()
+        ctx.check(ctx.lib.grmp_pattern_build(sh, len(self.operators), _terms(self.operators), ctypes.byref(self.h)))
+
+    def info(self):
+        n = ctypes.c_int32()
+        nnz = ctypes.c_int64()
+        mx = ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.grmp_matrix_info(self.h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(mx)))
+        return n.value, nnz.value, mx.value
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[1]
+
+    def pattern(self):
+        n, nnz, _ = self.info()
+        rp = np.empty(n + 1, dtype=np.int64)
+        ci = np.empty(nnz, dtype=np.int32)
+        self.ctx.check(self.ctx.lib.grmp_matrix_download(self.h, L.FP64, rp.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int64)), _ip(ci), ctypes.POINTER(ctypes.c_double)()))
+        return rp, ci
+
+    def download(self, precision: int = L.FP64):
+        import scipy.sparse as sp
+        n, nnz, _ = self.info()
+        rp = np.empty(n + 1, dtype=np.int64)
+        ci = np.empty(nnz, dtype=np.int32)
+        v = np.empty(nnz, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grmp_matrix_download(self.h, precision, rp.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int64)), _ip(ci), _dp(v)))
+        return sp.csr_matrix((v, ci, rp), shape=(n, n))
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.grmp_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            if self.ctx.h:
+                self.free()
+        except Exception:
+            pass
+
+
+def assemble(target, operators, precision: int = L.FP64):
+    """assemble!(A, operators) / assemble!(b, LinearForm): device assembly.
+
+    For an FEMatrix the values of the given precision are overwritten with the
+    sum of `operators` (a list of Operator).  For an FEVector the LinearForm is
+    added to the vector's current entries."""
+    if isinstance(target, FEMatrix):
+        ops = list(operators) if isinstance(operators, (list, tuple)) else [operators]
+        target.ctx.check(target.ctx.lib.grmp_assemble_bilinear(target.h, len(ops), _terms(ops), precision))
+        return target
+    if isinstance(target, FEVector):
+        lf = operators
+        r = lf.rhs()
+        sh = target.ctx.space(target.FES)
+        target.ctx.check(target.ctx.lib.grmp_assemble_linear(sh, ctypes.byref(r), target.h))
+        return target
+    raise TypeError("assemble target must be an FEMatrix or FEVector")
+
+
+def apply_dirichlet(A: FEMatrix, b: Optional[FEVector], fixed_dofs: np.ndarray, values=None,
+                    mode: int = L.DIRICHLET_ELIMINATE, penalty: float = 1e60):
+    """Dirichlet treatment of fixed DoFs: the reference's penalty form
+    (fixed_penalty = 1e60, src/solvers.jl:640-652) or symmetric elimination."""
+    f = np.ascontiguousarray(fixed_dofs, dtype=np.int32)
+    vals = None if values is None else np.ascontiguousarray(values, dtype=np.float64)
+    A.ctx.check(A.ctx.lib.grmp_apply_dirichlet(A.h, b.h if b is not None else None, f.size, _ip(f),
+                                               _dp(vals) if vals is not None else ctypes.POINTER(ctypes.c_double)(),
+                                               mode, float(penalty)))
+
+
+@dataclass
+class GB300PCG:
+    """The linear solver handed to solve! as `linsolver` (the LinearSolve
+    algorithm slot of default_solver_kwargs, src/solvers.jl:55).
+
+    mode "fp64": Jacobi-PCG in FP64.  mode "mixed": FP32 Jacobi-PCG inside an
+    FP64 refinement loop (FP64 residual b - A x and solution update)."""
+    mode: str = "fp64"
+    abstol: float = 1e-12
+    reltol: float = 1e-12
+    maxiter: int = 100000
+    inner_reltol: float = 0.1
+    max_outer: int = 1000
+    threads_per_row: int = 0
+    grid_blocks: int = 0
+    use_initial_guess: bool = False
+    last_stats: dict = field(default_factory=dict)
+
+    def params(self) -> L.SolveParams:
+        p = L.SolveParams()
+        p.abstol = self.abstol
+        p.reltol = self.reltol
+        p.maxiter = self.maxiter
+        p.mode = L.SOLVE_MIXED if self.mode == "mixed" else L.SOLVE_FP64
+        p.inner_reltol = self.inner_reltol
+        p.max_outer = self.max_outer
+        p.threads_per_row = self.threads_per_row
+        p.grid_blocks = self.grid_blocks
+        p.use_initial_guess = 1 if self.use_initial_guess else 0
+        return p
+
+    def solve(self, A: FEMatrix, b: FEVector, x: FEVector, raise_on_error: bool = True) -> dict:
+        st = L.SolveStats()
+        p = self.params()
+        rc = A.ctx.lib.grmp_solve(A.h, b.h, x.h, ctypes.byref(p), ctypes.byref(st))
+        self.last_stats = {"status": st.status, "iterations": st.iterations, "outer_iterations": st.outer_iterations,
+                           "threads_per_row": st.threads_per_row, "grid_blocks": st.grid_blocks,
+                           "final_relres": st.final_relres, "solve_ms": st.solve_ms, "rc": rc}
+        if raise_on_error:
+            A.ctx.check(rc)
+        return self.last_stats
+
+
+def spmv(A: FEMatrix, x: FEVector, y: FEVector, precision: int = L.FP64):
+    A.ctx.check(A.ctx.lib.grmp_spmv(A.h, precision, x.h, y.h))

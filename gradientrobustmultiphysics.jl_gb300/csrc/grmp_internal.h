@@ -1,0 +1,184 @@
+// Internal declarations of libgrmp_gpu.so (not part of the C-ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/grmp.h"
+
+// ---------------------------------------------------------------- limits
+constexpr int GRMP_MAX_LDOFS = 32;      // local DoFs per cell (mask width)
+constexpr int GRMP_MAX_ROW_NNZ = 512;   // pattern build: per-row column list
+constexpr int GRMP_MAXQ = 128;          // quadrature points
+constexpr int GRMP_MAX_TERMS = 4;       // operator terms per assembly call
+constexpr long long GRMP_SPIN_LIMIT = 1LL << 24;   // bounded device waits
+
+// ---------------------------------------------------------------- handles
+struct grmp_context_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t budget = 0;       // 0 = unlimited
+    size_t in_use = 0;
+    int num_sms = 0;
+    std::atomic<unsigned long long> launches{0};
+    std::string last_error;
+    std::mutex mu;
+};
+
+struct grmp_mesh_s {
+    grmp_context ctx = nullptr;
+    int dim = 0;
+    int32_t nverts = 0, ncells = 0;
+    double *d_coords = nullptr;     // [nverts][dim]
+    int32_t *d_cells = nullptr;     // [ncells][dim+1]
+    // optional face data (H1BR / reconstruction)
+    int32_t nfaces = 0;
+    int32_t *d_cell_faces = nullptr;
+    double *d_face_normals = nullptr;
+    double *d_face_volumes = nullptr;
+    int8_t *d_cell_face_signs = nullptr;
+};
+
+struct grmp_space_s {
+    grmp_mesh mesh = nullptr;
+    int fe = 0;
+    int ncomp = 1;
+    int ldofs = 0;          // local dofs per cell
+    int nb = 0;             // scalar basis size of the H1 part
+    int32_t ndofs = 0;
+    int32_t *d_celldofs = nullptr;  // [ncells][ldofs]
+    // DoF -> (cell, local) incidence, ascending cell per DoF
+    int32_t *d_inc_ptr = nullptr;   // [ndofs+1]
+    int32_t *d_inc_cell = nullptr;  // [ncells*ldofs]
+    uint8_t *d_inc_loc = nullptr;   // [ncells*ldofs]
+    double *d_locbuf = nullptr;     // [ncells][ldofs] linear-form cell vectors
+};
+
+struct grmp_matrix_s {
+    grmp_space space = nullptr;
+    int32_t nrows = 0;
+    int64_t nnz = 0;
+    int32_t max_row_nnz = 0;
+    int32_t *d_rowptr = nullptr;    // [nrows+1]
+    int32_t *d_cols = nullptr;      // [nnz]
+    void *d_slot = nullptr;         // [ninc][ldofs] uint8 or uint16 (row-relative slot, all-ones = dropped)
+    int slot_bytes = 1;
+    double *d_vals64 = nullptr;     // [nnz]
+    float *d_vals32 = nullptr;      // [nnz]
+    bool has64 = false, has32 = false;
+    uint8_t *d_fixed = nullptr;     // [nrows] Dirichlet flags (eliminated rows)
+    bool eliminated = false;
+    // cached workspace for solves
+    void *d_work = nullptr;
+    size_t work_bytes = 0;
+    int tuned_tpr = 0;              // autotuned SpMV lanes per row (0 = not tuned)
+    // per-cell geometric factors (scratch for assembly)
+    void *d_cellfac = nullptr;
+    size_t cellfac_bytes = 0;
+};
+
+struct grmp_vector_s {
+    grmp_context ctx = nullptr;
+    int32_t n = 0;
+    double *d = nullptr;
+};
+
+// ---------------------------------------------------------------- errors
+int grmp_fail(grmp_context ctx, int code, const char *fmt, ...);
+int grmp_cuda_fail(grmp_context ctx, cudaError_t e, const char *what);
+
+#define GRMP_CUDA(ctx, call)                                  \
+    do {                                                      \
+        cudaError_t e__ = (call);                             \
+        if (e__ != cudaSuccess) return grmp_cuda_fail((ctx), e__, #call); \
+    } while (0)
+
+// count one kernel launch of a context
+#define GRMP_LAUNCHED(ctx) ((ctx)->launches.fetch_add(1, std::memory_order_relaxed))
+
+// device memory accounted against the context budget
+int grmp_alloc(grmp_context ctx, void **p, size_t bytes);
+void grmp_free(grmp_context ctx, void *p, size_t bytes);
+
+// ---------------------------------------------------------------- tables
+// Reference tables for one element and quadrature order (host).
+struct RefTables {
+    int dim = 0, nq = 0, nb = 0;
+    double xref[GRMP_MAXQ][3];
+    double w[GRMP_MAXQ];
+    double vals[GRMP_MAXQ][GRMP_MAX_LDOFS];            // scalar basis values
+    double derivs[GRMP_MAXQ][GRMP_MAX_LDOFS][3];       // d/dxref_j
+};
+int grmp_quadrature(int dim, int order, double (*xref)[3], double *w);   // returns nq (0 = unavailable)
+int grmp_tables(int dim, int fe, int order, RefTables *t);              // returns 0 on success
+int grmp_fe_polyorder(int fe, int dim);
+int grmp_fe_nb(int fe, int dim);          // scalar H1 basis size per component
+int grmp_fe_ldofs(int fe, int dim, int ncomp);
+
+// ---------------------------------------------------------------- internal entry points
+int grmp_build_incidence(grmp_space s);
+int grmp_scan_i32(grmp_context ctx, const int32_t *d_in, int32_t *d_out_excl, int32_t n, int32_t *total);
+
+// pattern / assembly / solve implementations (pattern.cu, assemble.cu, solve.cu)
+int grmp_pattern_build_impl(grmp_space space, int nterms, const grmp_bilinear_term *terms, grmp_matrix *out);
+int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
+int grmp_assemble_linear_impl(grmp_space space, const grmp_rhs *rhs, grmp_vector b);
+int grmp_apply_dirichlet_impl(grmp_matrix A, grmp_vector b, int32_t nfixed, const int32_t *fixed,
+                              const double *values, int mode, double penalty);
+int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st);
+int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y);
+
+// upload a host array into a freshly allocated device array
+template <typename T>
+int grmp_upload(grmp_context ctx, T **dst, const T *src, size_t count) {
+    int rc = grmp_alloc(ctx, (void **)dst, count * sizeof(T));
+    if (rc) return rc;
+    if (count) GRMP_CUDA(ctx, cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return GRMP_OK;
+}
+
+// ---------------------------------------------------------------- device helpers
+#ifdef __CUDACC__
+// Grid-wide barrier for a cooperative (co-resident) launch.  Every wait is
+// bounded: after GRMP_SPIN_LIMIT polls the waiting block records
+// GRMP_ERR_TIMEOUT in *status and leaves; callers check the return value
+// and exit their loops.
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+};
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nblocks, int *status) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &gb->gen;
+        unsigned int g = *vgen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&gb->count, 1u) + 1u;
+        if (arrived == nblocks) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (++spins > GRMP_SPIN_LIMIT) {
+                    atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)status == 0;
+}
+#endif

@@ -1,0 +1,574 @@
+// Sparse solve: CSR SpMV and a persistent Jacobi-preconditioned CG.
+//
+// Stands in for the LinearSolve.jl call of solve_direct! (src/solvers.jl:
+// 89-101, :658-668).  Two modes:
+//  * FP64: plain Jacobi-PCG in FP64.
+//  * MIXED: Jacobi-PCG in FP32 (FP32 matrix values, FP32 vectors, FP32
+//    accumulation) inside an FP64 refinement loop.  The correction is
+//    accumulated in FP32 and folded into the FP64 solution whenever the FP32
+//    recurrence residual has dropped by `inner_reltol` since the last
+//    refinement; then the true residual b - A x is recomputed with the FP64
+//    matrix and replaces the FP32 residual ("reliable updates"), keeping the
+//    FP32 search direction.  Convergence is decided on the FP64 residual only.
+//
+// The whole iteration runs in one cooperative launch: three grid barriers per
+// iteration (bounded waits, see grid_barrier), dot products reduced through
+// per-block partials summed in a fixed order by every block, so all blocks
+// take identical decisions and results are reproducible run to run.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+#include "grmp_internal.h"
+
+namespace {
+
+constexpr int PTPB = 256;   // threads per block of the persistent kernel
+inline int nblk(long long n, int tpb = 256) { return (int)((n + tpb - 1) / tpb); }
+
+struct WorkLayout {
+    size_t vec, off_r64, off_part;
+};
+
+struct SolveState {
+    GridBarrier bar;
+    int status;
+    int iters;
+    int outer;
+    int pad;
+    double relres;
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum NV values over the block; result valid in all threads.
+template <int NV>
+__device__ __forceinline__ void block_sum(double *v, double *sh /* [32*NV] */) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < NV; k++) sh[wid * NV + k] = v[k];
+    __syncthreads();
+    for (int k = 0; k < NV; k++) {
+        double s = 0;
+        for (int w = 0; w < nw; w++) s += sh[w * NV + k];   // fixed order
+        v[k] = s;
+    }
+    __syncthreads();
+}
+
+// Write this block's partial sums, pass a grid barrier, then every block sums
+// all partials in the same fixed order.  Returns false on a barrier timeout.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh, SolveState *st) {
+    block_sum<NV>(v, sh);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NV; k++) partial[blockIdx.x * 4 + k] = v[k];
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return false;
+    double acc[NV];
+    for (int k = 0; k < NV; k++) acc[k] = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int k = 0; k < NV; k++) acc[k] += __ldcg(&partial[b * 4 + k]);
+    block_sum<NV>(acc, sh);
+    for (int k = 0; k < NV; k++) v[k] = acc[k];
+    return true;
+}
+
+// y = A x over the rows of this grid; groups of TPR lanes per row.  If DOT,
+// returns this thread's share of sum_r w[r]*y[r].  If RESID, y = b - A x.
+template <int TPR, typename V, typename X, typename Y, bool DOT, bool RESID>
+__device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                                            const V *__restrict__ vals, const X *x, Y *y, const Y *w,
+                                            const double *b) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & (TPR - 1);
+    const int warp = gtid >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    constexpr int RPW = 32 / TPR;   // rows per warp per step
+    const int gin = (threadIdx.x & 31) / TPR;
+    double dot = 0;
+    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
+        int r = base + gin;
+        using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
+        A s = 0;
+        if (r < n) {
+            int e = rowptr[r + 1];
+            for (int k = rowptr[r] + lane; k < e; k += TPR) s += (A)vals[k] * (A)x[cols[k]];
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (r < n && lane == 0) {
+            if (RESID) {
+                double v = b[r] - (double)s;
+                y[r] = (Y)v;
+                if (DOT) dot += v * v;
+            } else {
+                y[r] = (Y)s;
+                if (DOT) dot += (double)w[r] * (double)s;
+            }
+        }
+    }
+    return dot;
+}
+
+// ------------------------------------------------------------------ FP64 PCG
+template <int TPR>
+__global__ void __launch_bounds__(PTPB) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
+                                                const double *vals, const double *b, double *x, const double *dinv,
+                                                double *r, double *z, double *p, double *q, double *partial,
+                                                SolveState *st, double abstol, double reltol, int maxit, int guess) {
+    __shared__ double sh[32 * 4];
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsz = gridDim.x * blockDim.x;
+    // r = b - A x  (or b)
+    if (guess) spmv_grid<TPR, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+    double v[3] = {0, 0, 0};
+    for (int i = gtid; i < n; i += gsz) {
+        double ri = guess ? r[i] : b[i];
+        if (!guess) { r[i] = ri; x[i] = 0.0; }
+        double zi = dinv[i] * ri;
+        z[i] = zi;
+        p[i] = zi;
+        v[0] += ri * zi;
+        v[1] += ri * ri;
+        v[2] += b[i] * b[i];
+    }
+    if (!grid_sum<3>(v, partial, sh, st)) return;
+    double rz = v[0], rr = v[1];
+    const double bn = sqrt(v[2]);
+    const double tol = fmax(abstol, reltol * bn);
+    int it = 0;
+    bool conv = sqrt(rr) <= tol;
+    while (!conv && it < maxit) {
+        double d[1];
+        d[0] = spmv_grid<TPR, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
+        if (!grid_sum<1>(d, partial, sh, st)) return;
+        const double pq = d[0];
+        if (!(pq > 0) || !isfinite(pq)) {
+            if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
+            break;
+        }
+        const double alpha = rz / pq;
+        double w[2] = {0, 0};
+        for (int i = gtid; i < n; i += gsz) {
+            x[i] += alpha * p[i];
+            double ri = r[i] - alpha * q[i];
+            r[i] = ri;
+            double zi = dinv[i] * ri;
+            z[i] = zi;
+            w[0] += ri * zi;
+            w[1] += ri * ri;
+        }
+        if (!grid_sum<2>(w, partial, sh, st)) return;
+        it++;
+        rr = w[1];
+        conv = sqrt(rr) <= tol;
+        if (conv) break;
+        const double beta = w[0] / rz;
+        rz = w[0];
+        for (int i = gtid; i < n; i += gsz) p[i] = z[i] + beta * p[i];
+        if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+    }
+    // true residual in FP64
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+    double t[1];
+    t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    if (!grid_sum<1>(t, partial, sh, st)) return;
+    if (gtid == 0) {
+        st->iters = it;
+        st->outer = 0;
+        st->relres = sqrt(t[0]) / (bn > 0 ? bn : 1.0);
+        if (st->status == 0 && !(sqrt(t[0]) <= fmax(tol, 0.0) || conv)) st->status = GRMP_ERR_NOT_CONVERGED;
+    }
+}
+
+// ------------------------------------------------------------------ mixed PCG
+template <int TPR>
+__global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+                                                    const double *vals64, const float *vals32, const double *b,
+                                                    double *x, const float *dinv, float *r, float *z, float *p,
+                                                    float *q, float *xc, double *r64, double *partial,
+                                                    SolveState *st, double abstol, double reltol, double delta,
+                                                    int maxit, int maxouter, int guess) {
+    __shared__ double sh[32 * 4];
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsz = gridDim.x * blockDim.x;
+    // FP64 residual of the initial guess
+    double v[2] = {0, 0};
+    if (guess) {
+        v[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+    } else {
+        for (int i = gtid; i < n; i += gsz) {
+            x[i] = 0.0;
+            r64[i] = b[i];
+            v[0] += b[i] * b[i];
+        }
+    }
+    for (int i = gtid; i < n; i += gsz) v[1] += b[i] * b[i];
+    if (!grid_sum<2>(v, partial, sh, st)) return;
+    const double bn = sqrt(v[1]);
+    const double tol = fmax(abstol, reltol * bn);
+    double rn64 = sqrt(v[0]);
+    int it = 0, outer = 0;
+    bool conv = rn64 <= tol;
+    // FP32 state from the FP64 residual
+    double w[2] = {0, 0};
+    for (int i = gtid; i < n; i += gsz) {
+        float ri = (float)r64[i];
+        float zi = dinv[i] * ri;
+        r[i] = ri;
+        z[i] = zi;
+        p[i] = zi;
+        xc[i] = 0.0f;
+        w[0] += (double)(ri * zi);
+        w[1] += (double)(ri * ri);
+    }
+    if (!grid_sum<2>(w, partial, sh, st)) return;
+    double rz = w[0];
+    double rmax = sqrt(w[1]);
+    while (!conv && it < maxit && outer < maxouter) {
+        double d[1];
+        d[0] = spmv_grid<TPR, float, float, float, true, false>(n, rowptr, cols, vals32, p, q, p, nullptr);
+        if (!grid_sum<1>(d, partial, sh, st)) return;
+        const double pq = d[0];
+        if (!(pq > 0) || !isfinite(pq)) {
+            if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
+            break;
+        }
+        const float alpha = (float)(rz / pq);
+        double u[2] = {0, 0};
+        for (int i = gtid; i < n; i += gsz) {
+            xc[i] += alpha * p[i];
+            float ri = r[i] - alpha * q[i];
+            r[i] = ri;
+            float zi = dinv[i] * ri;
+            z[i] = zi;
+            u[0] += (double)(ri * zi);
+            u[1] += (double)(ri * ri);
+        }
+        if (!grid_sum<2>(u, partial, sh, st)) return;
+        it++;
+        double rz_new = u[0];
+        const double rn32 = sqrt(u[1]);
+        if (rn32 <= delta * rmax || rn32 <= tol || it >= maxit) {
+            // refinement: fold the FP32 correction into x, recompute b - A x in FP64
+            for (int i = gtid; i < n; i += gsz) {
+                x[i] += (double)xc[i];
+                xc[i] = 0.0f;
+            }
+            if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+            double t[1];
+            t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+            if (!grid_sum<1>(t, partial, sh, st)) return;
+            outer++;
+            rn64 = sqrt(t[0]);
+            conv = rn64 <= tol;
+            if (conv || it >= maxit) break;
+            double y[2] = {0, 0};
+            for (int i = gtid; i < n; i += gsz) {
+                float ri = (float)r64[i];
+                float zi = dinv[i] * ri;
+                r[i] = ri;
+                z[i] = zi;
+                y[0] += (double)(ri * zi);
+                y[1] += (double)(ri * ri);
+            }
+            if (!grid_sum<2>(y, partial, sh, st)) return;
+            rz_new = y[0];
+            rmax = sqrt(y[1]);
+        }
+        const float beta = (float)(rz_new / rz);
+        rz = rz_new;
+        for (int i = gtid; i < n; i += gsz) p[i] = z[i] + beta * p[i];
+        if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+    }
+    if (gtid == 0) {
+        st->iters = it;
+        st->outer = outer;
+        st->relres = rn64 / (bn > 0 ? bn : 1.0);
+        if (st->status == 0 && !conv) st->status = GRMP_ERR_NOT_CONVERGED;
+    }
+}
+
+// ------------------------------------------------------------------ helpers
+template <typename V>
+__global__ void k_dinv(int n, const int32_t *rowptr, const int32_t *cols, const V *vals, V *dinv, int *bad) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V d = 0;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++)
+        if (cols[k] == i) d = vals[k];
+    if (!(d > 0) || !isfinite((double)d)) {
+        atomicExch(bad, 1);
+        dinv[i] = V(1);
+    } else {
+        dinv[i] = V(1) / d;
+    }
+}
+
+template <int TPR, typename V, typename X>
+__global__ void __launch_bounds__(256) k_spmv(int n, const int32_t *rowptr, const int32_t *cols, const V *vals,
+                                              const X *x, X *y) {
+    spmv_grid<TPR, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr);
+}
+
+__global__ void k_f64_to_f32(const double *a, float *b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+__global__ void k_f32_to_f64v(const float *a, double *b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (double)a[i];
+}
+
+template <typename V, typename X>
+void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, const int32_t *ci, const V *v, const X *x,
+                 X *y) {
+    switch (tpr) {
+        case 1: k_spmv<1, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 2: k_spmv<2, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 4: k_spmv<4, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 8: k_spmv<8, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 16: k_spmv<16, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        default: k_spmv<32, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+    }
+}
+
+int heuristic_tpr(grmp_matrix A) {
+    double avg = (double)A->nnz / (double)std::max(1, A->nrows);
+    if (avg <= 3) return 2;
+    if (avg <= 6) return 4;
+    if (avg <= 14) return 8;
+    if (avg <= 40) return 16;
+    return 32;
+}
+
+// Autotuner: time the standalone SpMV for each lane count on this matrix
+// (values of `precision`) and keep the fastest.
+int autotune_tpr(grmp_matrix A, int precision) {
+    grmp_context ctx = A->space->mesh->ctx;
+    int n = A->nrows;
+    void *xb = nullptr, *yb = nullptr;
+    size_t es = precision == GRMP_FP64 ? 8 : 4;
+    if (grmp_alloc(ctx, &xb, (size_t)n * es) || grmp_alloc(ctx, &yb, (size_t)n * es)) {
+        grmp_free(ctx, xb, (size_t)n * es);
+        return heuristic_tpr(A);
+    }
+    cudaMemsetAsync(xb, 0, (size_t)n * es, ctx->stream);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = heuristic_tpr(A);
+    float bt = 1e30f;
+    const int cand[5] = {2, 4, 8, 16, 32};
+    for (int c : cand) {
+        int rows_per_block = 256 / c;
+        int grid = std::min(nblk(n, rows_per_block), ctx->num_sms * 16);
+        float tot = 0;
+        for (int rep = 0; rep < 4; rep++) {
+            cudaEventRecord(e0, ctx->stream);
+            if (precision == GRMP_FP64)
+                launch_spmv<double, double>(c, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals64,
+                                            (const double *)xb, (double *)yb);
+            else
+                launch_spmv<float, float>(c, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals32,
+                                          (const float *)xb, (float *)yb);
+            GRMP_LAUNCHED(ctx);
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) tot += ms;
+        }
+        if (tot < bt) {
+            bt = tot;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    grmp_free(ctx, xb, (size_t)n * es);
+    grmp_free(ctx, yb, (size_t)n * es);
+    cudaGetLastError();
+    return best;
+}
+
+template <typename K>
+int coop_grid(grmp_context ctx, K kern, int n, int want) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PTPB, 0);
+    int maxg = std::max(1, per_sm) * ctx->num_sms;
+    int need = std::max(1, nblk(n, PTPB));
+    int g = want > 0 ? std::min(want, maxg) : std::min(maxg, need);
+    return std::max(1, g);
+}
+
+template <int TPR>
+int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *out,
+               char *work, SolveState *dst, WorkLayout lay) {
+    grmp_context ctx = A->space->mesh->ctx;
+    int n = A->nrows;
+    bool mixed = p->mode == GRMP_SOLVE_MIXED;
+    int guess = p->use_initial_guess ? 1 : 0;
+    int grid;
+    cudaError_t e;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    if (!mixed) {
+        auto kern = k_pcg64<TPR>;
+        grid = coop_grid(ctx, kern, n, p->grid_blocks);
+        double *dinv = (double *)work, *r = (double *)(work + lay.vec), *z = (double *)(work + 2 * lay.vec);
+        double *pp = (double *)(work + 3 * lay.vec), *q = (double *)(work + 4 * lay.vec);
+        double *part = (double *)(work + lay.off_part);
+        int nn = n, mi = p->maxiter;
+        double at = p->abstol, rt = p->reltol;
+        const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+        const double *vv = A->d_vals64, *bb = b->d;
+        double *xx = x->d;
+        void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess};
+        cudaEventRecord(e0, ctx->stream);
+        e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+        GRMP_LAUNCHED(ctx);
+        cudaEventRecord(e1, ctx->stream);
+    } else {
+        auto kern = k_pcg_mixed<TPR>;
+        grid = coop_grid(ctx, kern, n, p->grid_blocks);
+        float *dinv = (float *)work, *r = (float *)(work + lay.vec), *z = (float *)(work + 2 * lay.vec);
+        float *pp = (float *)(work + 3 * lay.vec), *q = (float *)(work + 4 * lay.vec), *xc = (float *)(work + 5 * lay.vec);
+        double *r64 = (double *)(work + lay.off_r64);
+        double *part = (double *)(work + lay.off_part);
+        int nn = n, mi = p->maxiter, mo = p->max_outer > 0 ? p->max_outer : 1000;
+        double at = p->abstol, rt = p->reltol, dl = p->inner_reltol > 0 && p->inner_reltol < 1 ? p->inner_reltol : 0.1;
+        const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+        const double *v64 = A->d_vals64, *bb = b->d;
+        const float *v32 = A->d_vals32;
+        double *xx = x->d;
+        void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &z, &pp, &q, &xc, &r64, &part, &dst,
+                        &at, &rt, &dl, &mi, &mo, &guess};
+        cudaEventRecord(e0, ctx->stream);
+        e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+        GRMP_LAUNCHED(ctx);
+        cudaEventRecord(e1, ctx->stream);
+    }
+    SolveState hs;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "persistent PCG launch");
+    out->status = hs.status;
+    out->iterations = hs.iters;
+    out->outer_iterations = hs.outer;
+    out->final_relres = hs.relres;
+    out->threads_per_row = TPR;
+    out->grid_blocks = grid;
+    out->solve_ms = ms;
+    if (hs.status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, GRMP_ERR_NOT_CONVERGED, "PCG: %d iterations, relative residual %.3e", hs.iters, hs.relres);
+    if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a grid barrier wait timed out");
+    if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
+    return hs.status;
+}
+
+}  // namespace
+
+int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st) {
+    grmp_context ctx = A->space->mesh->ctx;
+    std::memset(st, 0, sizeof(*st));
+    bool mixed = p->mode == GRMP_SOLVE_MIXED;
+    if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: FP64 values not assembled");
+    if (mixed && !A->has32) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: MIXED needs FP32 values too");
+    int n = A->nrows;
+    // workspace, each array 256-byte aligned:
+    //   FP64 : dinv r z p q (double)                  | partials | state
+    //   MIXED: dinv r z p q xc (float) | r64 (double)  | partials | state
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    size_t pbytes = (size_t)4 * 8 * 4096;
+    size_t vec = mixed ? al((size_t)n * 4) : al((size_t)n * 8);
+    size_t nvec = mixed ? 6 : 5;
+    size_t off_r64 = nvec * vec;
+    size_t off_part = off_r64 + (mixed ? al((size_t)n * 8) : 0);
+    size_t off_state = off_part + al(pbytes);
+    size_t need = off_state + al(sizeof(SolveState));
+    if (A->work_bytes < need) {
+        grmp_free(ctx, A->d_work, A->work_bytes);
+        A->work_bytes = 0;
+        int rc = grmp_alloc(ctx, &A->d_work, need);
+        if (rc) return rc;
+        A->work_bytes = need;
+    }
+    char *work = (char *)A->d_work;
+    SolveState *dst = (SolveState *)(work + off_state);
+    WorkLayout lay{vec, off_r64, off_part};
+    cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
+    // Jacobi preconditioner
+    int *bad = nullptr;
+    int rc = grmp_alloc(ctx, (void **)&bad, 4);
+    if (rc) return rc;
+    cudaMemsetAsync(bad, 0, 4, ctx->stream);
+    if (mixed)
+        k_dinv<float><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals32, (float *)work, bad);
+    else
+        k_dinv<double><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, (double *)work, bad);
+    GRMP_LAUNCHED(ctx);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    grmp_free(ctx, bad, 4);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
+    if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
+    int tpr = p->threads_per_row;
+    if (tpr <= 0) {
+        if (!A->tuned_tpr) A->tuned_tpr = autotune_tpr(A, mixed ? GRMP_FP32 : GRMP_FP64);
+        tpr = A->tuned_tpr;
+    }
+    switch (tpr) {
+        case 2: return launch_pcg<2>(A, b, x, p, st, work, dst, lay);
+        case 4: return launch_pcg<4>(A, b, x, p, st, work, dst, lay);
+        case 8: return launch_pcg<8>(A, b, x, p, st, work, dst, lay);
+        case 16: return launch_pcg<16>(A, b, x, p, st, work, dst, lay);
+        case 32: return launch_pcg<32>(A, b, x, p, st, work, dst, lay);
+    }
+    return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "threads_per_row must be 2, 4, 8, 16 or 32");
+}
+
+int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
+    grmp_context ctx = A->space->mesh->ctx;
+    int n = A->nrows;
+    int tpr = A->tuned_tpr ? A->tuned_tpr : heuristic_tpr(A);
+    int grid = std::min(nblk(n, 256 / tpr), ctx->num_sms * 16);
+    if (precision == GRMP_FP64) {
+        if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv: no FP64 values");
+        launch_spmv<double, double>(tpr, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals64, x->d, y->d);
+        GRMP_LAUNCHED(ctx);
+    } else {
+        if (!A->has32) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv: no FP32 values");
+        float *xf = nullptr, *yf = nullptr;
+        int rc = grmp_alloc(ctx, (void **)&xf, (size_t)n * 4);
+        if (!rc) rc = grmp_alloc(ctx, (void **)&yf, (size_t)n * 4);
+        if (rc) {
+            grmp_free(ctx, xf, (size_t)n * 4);
+            return rc;
+        }
+        k_f64_to_f32<<<nblk(n), 256, 0, ctx->stream>>>(x->d, xf, n); GRMP_LAUNCHED(ctx);
+        launch_spmv<float, float>(tpr, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals32, xf, yf);
+        GRMP_LAUNCHED(ctx);
+        k_f32_to_f64v<<<nblk(n), 256, 0, ctx->stream>>>(yf, y->d, n); GRMP_LAUNCHED(ctx);
+        grmp_free(ctx, xf, (size_t)n * 4);
+        grmp_free(ctx, yf, (size_t)n * 4);
+    }
+    GRMP_CUDA(ctx, cudaGetLastError());
+    GRMP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GRMP_OK;
+}

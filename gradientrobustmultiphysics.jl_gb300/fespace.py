@@ -1,0 +1,179 @@
+"""Finite element spaces and their DoF maps (the reference's FESpace layer).
+
+Element types mirror the reference's parametric types: ``H1P1(ncomponents)``
+(src/fedefs/h1_p1.jl), ``H1P2(ncomponents, edim)`` (src/fedefs/h1_p2.jl),
+``H1BR(edim)`` (src/fedefs/h1v_br.jl), ``L2P0(ncomponents)``
+(src/fedefs/l2_p0.jl), ``HDIVRT0(edim)`` / ``HDIVBDM1(edim)`` as
+reconstruction targets.
+
+Global numbering follows ``init_dofmap_from_pattern!``
+(src/dofmaps.jl:201-330): components are blocked with a per-component offset
+``coffset`` (the number of DoFs of one component); within a component the
+pattern order is nodes, then faces ("N1F1", 2D P2) or edges ("N1E1", 3D P2);
+the BR face bubbles ("f1", not per component) follow all node DoFs.  Local
+cell DoFs are component-major in the same pattern order, which is the row
+order of the reference bases.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .mesh import SimplexMesh, TRI_LOCAL_FACES, TET_LOCAL_EDGES, TET_LOCAL_FACES
+
+# element kind codes shared with the C-ABI (include/grmp.h)
+FE_H1P1 = 1
+FE_H1P2 = 2
+FE_H1BR = 3
+FE_HDIVRT0 = 4
+FE_HDIVBDM1 = 5
+FE_L2P0 = 6
+
+
+@dataclass(frozen=True)
+class FEType:
+    kind: int
+    ncomponents: int
+    name: str
+
+    def __repr__(self) -> str:
+        return self.name
+
+
+def H1P1(ncomponents: int = 1) -> FEType:
+    return FEType(FE_H1P1, ncomponents, f"H1P1{{{ncomponents}}}")
+
+
+def H1P2(ncomponents: int = 1, edim: int = 2) -> FEType:
+    return FEType(FE_H1P2, ncomponents, f"H1P2{{{ncomponents},{edim}}}")
+
+
+def H1BR(edim: int = 2) -> FEType:
+    return FEType(FE_H1BR, edim, f"H1BR{{{edim}}}")
+
+
+def L2P0(ncomponents: int = 1) -> FEType:
+    return FEType(FE_L2P0, ncomponents, f"L2P0{{{ncomponents}}}")
+
+
+def HDIVRT0(edim: int = 2) -> FEType:
+    return FEType(FE_HDIVRT0, edim, f"HDIVRT0{{{edim}}}")
+
+
+def HDIVBDM1(edim: int = 2) -> FEType:
+    return FEType(FE_HDIVBDM1, edim, f"HDIVBDM1{{{edim}}}")
+
+
+def polynomial_order(fe: FEType, dim: int) -> int:
+    """get_polynomialorder for the element on a simplex of dimension dim."""
+    if fe.kind == FE_H1P1:
+        return 1
+    if fe.kind == FE_H1P2:
+        return 2
+    if fe.kind == FE_H1BR:
+        return 2 if dim == 2 else 3          # src/fedefs/h1v_br.jl:23-29
+    if fe.kind == FE_L2P0:
+        return 0
+    if fe.kind == FE_HDIVRT0:
+        return 1
+    if fe.kind == FE_HDIVBDM1:
+        return 1
+    raise ValueError(fe)
+
+
+class FESpace:
+    """FESpace{FEType}(grid): holds the cell DoF map and boundary DoFs."""
+
+    def __init__(self, fetype: FEType, grid: SimplexMesh, name: str = ""):
+        self.FEType = fetype
+        self.xgrid = grid
+        self.name = name or repr(fetype)
+        self._build()
+
+    def _build(self):
+        g = self.xgrid
+        fe = self.FEType
+        nn = g.nverts
+        nc = fe.ncomponents
+        if fe.kind == FE_H1P1:
+            self.coffset = nn
+            self.ndofs = nn * nc
+            per = [g.cells.astype(np.int64) + c * nn for c in range(nc)]
+            self.celldofs = np.concatenate(per, axis=1).astype(np.int32)
+        elif fe.kind == FE_H1P2:
+            if g.dim == 2:
+                ent, cent = g.faces()[0].shape[0], g.faces()[1]
+            else:
+                ent, cent = g.edges()[0].shape[0], g.edges()[1]
+            self.coffset = nn + ent
+            self.ndofs = self.coffset * nc
+            per = []
+            for c in range(nc):
+                off = c * self.coffset
+                per.append(g.cells.astype(np.int64) + off)
+                per.append(cent.astype(np.int64) + off + nn)
+            self.celldofs = np.concatenate(per, axis=1).astype(np.int32)
+        elif fe.kind == FE_H1BR:
+            fnodes, cfaces = g.faces()
+            self.coffset = nn
+            self.ndofs = nn * nc + fnodes.shape[0]
+            per = [g.cells.astype(np.int64) + c * nn for c in range(nc)]
+            per.append(cfaces.astype(np.int64) + nc * nn)
+            self.celldofs = np.concatenate(per, axis=1).astype(np.int32)
+        elif fe.kind == FE_L2P0:
+            self.coffset = g.ncells
+            self.ndofs = g.ncells * nc
+            self.celldofs = np.stack([np.arange(g.ncells) + c * g.ncells for c in range(nc)], axis=1).astype(np.int32)
+        elif fe.kind in (FE_HDIVRT0,):
+            fnodes, cfaces = g.faces()
+            self.coffset = fnodes.shape[0]
+            self.ndofs = fnodes.shape[0]
+            self.celldofs = cfaces.astype(np.int32)
+        else:
+            raise ValueError(f"unsupported element {fe}")
+        self.celldofs = np.ascontiguousarray(self.celldofs)
+
+    @property
+    def ndofs4cell(self) -> int:
+        return self.celldofs.shape[1]
+
+    def boundary_dofs(self, regions=None) -> np.ndarray:
+        """Sorted unique DoFs on boundary faces of the given regions (all if
+        None): the BFaceDofs collection of the homogeneous-Dirichlet branch of
+        boundarydata! (src/boundarydata.jl:200-260)."""
+        g = self.xgrid
+        fe = self.FEType
+        bf, reg = g.boundary_faces()
+        if regions is not None:
+            bf = bf[np.isin(reg, np.asarray(regions))]
+        fnodes = g.faces()[0][bf]                          # (nb, dim)
+        nn = g.nverts
+        out = []
+        if fe.kind in (FE_H1P1, FE_H1P2, FE_H1BR):
+            for c in range(fe.ncomponents):
+                out.append(fnodes.ravel().astype(np.int64) + c * self.coffset)
+            if fe.kind == FE_H1P2:
+                if g.dim == 2:
+                    for c in range(fe.ncomponents):
+                        out.append(bf.astype(np.int64) + nn + c * self.coffset)
+                else:
+                    # edges of the boundary faces
+                    enodes = g.edges()[0]
+                    key = enodes[:, 0].astype(np.int64) * (nn + 1) + enodes[:, 1]
+                    order = np.argsort(key)
+                    pairs = np.concatenate([fnodes[:, [0, 1]], fnodes[:, [0, 2]], fnodes[:, [1, 2]]])
+                    pairs = np.sort(pairs, axis=1)
+                    pk = pairs[:, 0].astype(np.int64) * (nn + 1) + pairs[:, 1]
+                    eid = order[np.searchsorted(key[order], pk)]
+                    for c in range(fe.ncomponents):
+                        out.append(eid.astype(np.int64) + nn + c * self.coffset)
+            if fe.kind == FE_H1BR:
+                out.append(bf.astype(np.int64) + fe.ncomponents * nn)
+        elif fe.kind == FE_L2P0:
+            pass
+        else:
+            raise ValueError(fe)
+        if not out:
+            return np.zeros(0, dtype=np.int32)
+        return np.unique(np.concatenate(out)).astype(np.int32)

@@ -1,0 +1,267 @@
+/*
+ * grmp.h -- C-ABI of the GB300 finite-element assembly + solve library
+ * (libgrmp_gpu.so).
+ *
+ * The library replaces, for one GPU, the hot path of GradientRobustMultiPhysics.jl
+ * v0.12.0: global assembly of BilinearForm / LinearForm operators and the sparse
+ * linear solve behind solve!(Solution, Problem).  Each entry point cites the
+ * reference interface it stands in for (paths are relative to the reference
+ * project root).
+ *
+ * Conventions
+ *  - Every function returns an int status (grmp_status); nothing throws.
+ *    The text of the last error of a context is returned by grmp_last_error.
+ *  - Handles are opaque and owned by the library; free them with the matching
+ *    *_destroy call.  Host arrays passed in are copied before the call returns
+ *    (a garbage-collected caller may move or free them afterwards).  Output
+ *    host arrays are allocated by the caller.
+ *  - Indices are 0-based int32.  The reference is 1-based: a Julia caller
+ *    subtracts 1 (see the integration notes).
+ *  - One context owns one CUDA stream; all work of a context is ordered on it.
+ *    Handles of one context may be used from one host thread at a time.
+ */
+#ifndef GRMP_H
+#define GRMP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef enum {
+    GRMP_OK = 0,
+    GRMP_ERR_INVALID_ARG = 1,    /* bad handle, size, index or option          */
+    GRMP_ERR_OUT_OF_MEMORY = 2,  /* device allocation failed                  */
+    GRMP_ERR_DEVICE = 3,         /* CUDA runtime error                        */
+    GRMP_ERR_NOT_CONVERGED = 4,  /* iteration cap hit before the tolerance    */
+    GRMP_ERR_UNSUPPORTED = 5,    /* element / operator combination not built  */
+    GRMP_ERR_BUDGET = 6,         /* request exceeds the context's HBM budget  */
+    GRMP_ERR_TIMEOUT = 7,        /* a bounded device-side wait gave up        */
+    GRMP_ERR_NAN = 8,            /* non-finite value in an input or iterate   */
+    GRMP_ERR_NO_DEVICE = 9       /* no CUDA device / library built without one */
+} grmp_status;
+
+typedef struct grmp_context_s *grmp_context;
+typedef struct grmp_mesh_s *grmp_mesh;
+typedef struct grmp_space_s *grmp_space;
+typedef struct grmp_matrix_s *grmp_matrix;
+typedef struct grmp_vector_s *grmp_vector;
+
+/* --------------------------------------------------------------- context */
+
+/* Library version as major*10000 + minor*100 + patch. */
+int grmp_version(void);
+
+/* Create a context on CUDA device `device`.  `hbm_budget_bytes` caps the
+ * device memory the context may hold (0 = no cap); allocations beyond it fail
+ * with GRMP_ERR_BUDGET.  No reference counterpart (the reference is CPU-only);
+ * it is the state a LinearSolve algorithm cache holds (src/solvers.jl:89-101). */
+int grmp_create_context(int device, size_t hbm_budget_bytes, grmp_context *out);
+int grmp_destroy_context(grmp_context ctx);
+const char *grmp_last_error(grmp_context ctx);
+/* cudaStream_t of the context, as void*, for callers that time or order work. */
+int grmp_context_stream(grmp_context ctx, void **stream);
+int grmp_synchronize(grmp_context ctx);
+/* Bytes of device memory currently held by the context's handles. */
+int grmp_context_memory(grmp_context ctx, size_t *bytes_in_use);
+/* Number of kernels this context has launched so far (instrumentation). */
+int grmp_context_launches(grmp_context ctx, uint64_t *launches);
+/* Device address of a vector's FP64 data (for coef_on_device inputs). */
+int grmp_vector_device_ptr(grmp_vector v, void **dptr);
+
+/* ------------------------------------------------------------------ mesh */
+
+/* Upload a simplex mesh: coords [nverts][dim] (FP64), cell_verts
+ * [ncells][dim+1].  Replaces the ExtendableGrids arrays Coordinates /
+ * CellNodes read by L2GTransformer (src/feevaluator.jl:38). */
+int grmp_mesh_upload(grmp_context ctx, int dim, int32_t nverts, const double *coords, int32_t ncells,
+                     const int32_t *cell_verts, grmp_mesh *out);
+
+/* Face data needed by the H1BR element and the RT0 / BDM1 reconstruction
+ * (FaceNormals, FaceVolumes, CellFaces, CellFaceSigns of ExtendableGrids, read
+ * in src/fedefs/h1v_br.jl:150-162 and src/reconstructions.jl:381-403):
+ * cell_faces [ncells][dim+1], face_normals [nfaces][dim] (unit, globally
+ * oriented), face_volumes [nfaces], cell_face_signs [ncells][dim+1] (+1/-1). */
+int grmp_mesh_set_faces(grmp_mesh mesh, int32_t nfaces, const int32_t *cell_faces, const double *face_normals,
+                        const double *face_volumes, const int8_t *cell_face_signs);
+int grmp_mesh_destroy(grmp_mesh mesh);
+
+/* ----------------------------------------------------------------- space */
+
+typedef enum {
+    GRMP_FE_H1P1 = 1,     /* src/fedefs/h1_p1.jl                    */
+    GRMP_FE_H1P2 = 2,     /* src/fedefs/h1_p2.jl                    */
+    GRMP_FE_H1BR = 3,     /* src/fedefs/h1v_br.jl (2D)              */
+    GRMP_FE_HDIVRT0 = 4,  /* reconstruction target only            */
+    GRMP_FE_HDIVBDM1 = 5, /* reconstruction target only            */
+    GRMP_FE_L2P0 = 6      /* src/fedefs/l2_p0.jl                    */
+} grmp_fe_kind;
+
+/* FESpace{FEType}(xgrid) (src/finiteelements.jl:72-119) with the cell DoF
+ * map FES[CellDofs] (src/dofmaps.jl:201-330) supplied by the caller:
+ * celldofs [ncells][ndofs4cell], component-major in the element's pattern
+ * order. */
+int grmp_space_create(grmp_mesh mesh, int fe_kind, int ncomponents, const int32_t *celldofs, int32_t ndofs,
+                      grmp_space *out);
+int grmp_space_destroy(grmp_space space);
+/* Number of local DoFs per cell for the space. */
+int grmp_space_ndofs4cell(grmp_space space, int *out);
+
+/* Reference tables of the space's element for the quadrature rule of `order`
+ * (QuadratureRule{Float64,EG}(order), src/quadrature.jl:173-325, and the
+ * reference basis / ForwardDiff derivative tables, src/feevaluator.jl:93-131,
+ * :235-293).  Host-only query.  xref [nq][3], w [nq], vals [nq][nb],
+ * derivs [nq][nb][dim] where nb = scalar basis size; pass NULL to only get
+ * sizes.  Returns nq in *nq and nb in *nb. */
+int grmp_reference_tables(int dim, int fe_kind, int order, int *nq, int *nb, double *xref, double *w, double *vals,
+                          double *derivs);
+
+/* ------------------------------------------------------- bilinear forms */
+
+typedef enum {
+    GRMP_OP_LAPLACE = 1,   /* (Gradient u, Gradient v): LaplaceOperator / BilinearForm([Gradient,Gradient])
+                              src/pdeoperators.jl:154-169, :355-396                                     */
+    GRMP_OP_MASS = 2,      /* (Identity u, Identity v): ReactionOperator, src/pdeoperators.jl:176-203     */
+    GRMP_OP_HOOKE = 3,     /* (C eps(u), eps(v)) with SymmetricGradient{1}: HookStiffnessOperator2D/3D
+                              src/pdeoperators.jl:256-315; param[0] = mu, param[1] = lambda            */
+    GRMP_OP_RDIVRDIV = 4   /* (div R u, div R v), R = BR -> RT0 reconstruction (ReconstructionDivergence,
+                              src/feevaluator_h1.jl:409-437); iterated-penalty term                  */
+} grmp_op_kind;
+
+/* One operator term.  Assembly of a list of terms adds them into one matrix,
+ * as the reference adds several PDE operators into one FEMatrix block. */
+typedef struct {
+    int op_kind;             /* grmp_op_kind                                                        */
+    int symmetric;           /* 1: APT_SymmetricBilinearForm, 0: APT_BilinearForm                   */
+    double factor;           /* operator factor (e.g. kappa of LaplaceOperator(kappa))              */
+    const double *cell_coef; /* optional [ncells] per-cell scalar (an Action with "I" dependency:
+                                result = coef[cell] * input); NULL if absent                          */
+    double param[4];         /* op-specific parameters (Hooke: mu, lambda)                           */
+    int bonus_quadorder;     /* added to the quadrature order (src/assemblypatterns.jl:559-565)     */
+    int coef_on_device;      /* 1: cell_coef is a device pointer of this context's GPU (e.g. the
+                                data of a grmp_vector), read in place; 0: a host array, copied     */
+} grmp_bilinear_term;
+
+typedef enum { GRMP_FP64 = 0, GRMP_FP32 = 1 } grmp_precision;
+
+/* Build the sparsity pattern of the sum of `terms` on `space` x `space`:
+ * the union of the nonzero local contributions, an entry being dropped when
+ * every local contribution to it is exactly 0.0 in the reference's operation
+ * order (_addnz, src/fematrix.jl:54-65).  Also builds the DoF->cell
+ * incidence lists and the cell-to-CSR slot map used by assembly.  Replaces
+ * FEMatrix{T}(FEs) + the ExtendableSparse LNK build (src/fematrix.jl:186-213). */
+int grmp_pattern_build(grmp_space space, int nterms, const grmp_bilinear_term *terms, grmp_matrix *out);
+int grmp_matrix_destroy(grmp_matrix A);
+/* nrows, nnz and the maximum number of nonzeros of a row. */
+int grmp_matrix_info(grmp_matrix A, int32_t *nrows, int64_t *nnz, int32_t *max_row_nnz);
+
+/* Assemble the sum of `terms` into the matrix values in the given precision
+ * (FP64 values and/or FP32 values are held separately in the handle).
+ * Stands in for assemble!(A::FEMatrixBlock, AP::AssemblyPattern{<:APT_BilinearForm})
+ * (src/assemblypatterns/bilinearform.jl:92-400).  Deterministic: each
+ * nonzero is the sum of its cell contributions in ascending cell order. */
+int grmp_assemble_bilinear(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
+
+/* Copy the CSR arrays (rowptr [nrows+1] int64, cols [nnz], vals [nnz] FP64)
+ * to host memory; any pointer may be NULL.  `precision` selects which values. */
+int grmp_matrix_download(grmp_matrix A, int precision, int64_t *rowptr, int32_t *cols, double *vals);
+
+/* --------------------------------------------------------- linear forms */
+
+typedef enum {
+    GRMP_RHS_CONST = 0,   /* f = const vector: params[ncomp]                                    */
+    GRMP_RHS_CELL = 1,    /* f = per-cell vector: params[ncells][ncomp] ("I" dependency)         */
+    GRMP_RHS_FOURIER = 2, /* f = sum_m a_m sin(pi k_m . x): params[nmodes][1+dim] = (a_m, k_m)   */
+    GRMP_RHS_POLY = 3     /* f_c = sum_t coef_t x^e1 y^e2 z^e3: params[nterms][5]
+                             = (component, coef, e1, e2, e3)                                   */
+} grmp_rhs_kind;
+
+typedef struct {
+    int kind;               /* grmp_rhs_kind                                       */
+    int ncomponents;        /* components of f                                     */
+    const double *params;   /* see grmp_rhs_kind                                    */
+    int64_t nparams;        /* number of doubles in params                           */
+    double factor;          /* LinearForm factor                                     */
+    int bonus_quadorder;    /* DataFunction bonus_quadorder                          */
+    int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0}
+                               (BR only, src/feevaluator_h1.jl:342-381)              */
+} grmp_rhs;
+
+/* b += LinearForm(test_operator, f) over the space (src/assemblypatterns/
+ * linearform.jl:47-237).  FP64, deterministic (ascending cell order). */
+int grmp_assemble_linear(grmp_space space, const grmp_rhs *rhs, grmp_vector b);
+
+/* -------------------------------------------------------------- vectors */
+
+int grmp_vector_create(grmp_context ctx, int32_t n, grmp_vector *out);
+int grmp_vector_destroy(grmp_vector v);
+int grmp_vector_upload(grmp_vector v, const double *host);
+int grmp_vector_download(grmp_vector v, double *host);
+int grmp_vector_fill(grmp_vector v, double value);
+
+/* ------------------------------------------------------------- Dirichlet */
+
+typedef enum { GRMP_DIRICHLET_PENALTY = 0, GRMP_DIRICHLET_ELIMINATE = 1 } grmp_dirichlet_mode;
+
+/* Fix DoFs `fixed[nfixed]` to `values` (NULL = homogeneous).  PENALTY is the
+ * reference's treatment: A[d,d] = penalty, b[d] = penalty * u_D[d]
+ * (src/solvers.jl:640-652, src/fematrix.jl:349-355; default penalty 1e60).
+ * ELIMINATE zeroes row and column d (b -= A[:,d] u_D), sets A[d,d] = 1 and
+ * b[d] = u_D[d]; it gives the same free-DoF solution up to O(1/penalty) and is
+ * the form the FP32 path needs (1e60 overflows FP32).  Applied to both the
+ * FP64 and FP32 values present in A. */
+int grmp_apply_dirichlet(grmp_matrix A, grmp_vector b, int32_t nfixed, const int32_t *fixed, const double *values,
+                         int mode, double penalty);
+
+/* ------------------------------------------------------------------ solve */
+
+typedef enum {
+    GRMP_SOLVE_FP64 = 0,   /* plain: FP64 Jacobi-PCG                                                 */
+    GRMP_SOLVE_MIXED = 1   /* FP32 Jacobi-PCG inside FP64 refinement (outer residual, update in FP64) */
+} grmp_solve_mode;
+
+typedef struct {
+    double abstol;          /* stop when ||b - A x||_2 <= max(abstol, reltol*||b||_2)   */
+    double reltol;
+    int32_t maxiter;        /* cap on inner iterations                                   */
+    int32_t mode;           /* grmp_solve_mode                                           */
+    double inner_reltol;    /* MIXED: residual reduction per refinement (reliable update) */
+    int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
+    int32_t threads_per_row;/* SpMV lanes per row: 0 = autotuned                         */
+    int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
+    int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
+} grmp_solve_params;
+
+typedef struct {
+    int32_t status;          /* grmp_status of the solve                     */
+    int32_t iterations;      /* inner (or plain) iterations                  */
+    int32_t outer_iterations;/* FP64 refinement steps (MIXED)                */
+    int32_t threads_per_row; /* SpMV configuration used                      */
+    int32_t grid_blocks;
+    double final_relres;     /* ||b - A x|| / ||b|| in FP64 at exit          */
+    double solve_ms;         /* device time of the solve                     */
+} grmp_solve_stats;
+
+/* Fill params with defaults mirroring default_solver_kwargs
+ * (src/solvers.jl:38-59): abstol = reltol = 1e-12. */
+int grmp_solve_params_default(grmp_solve_params *p);
+
+/* Solve A x = b.  Stands in for init(LinearProblem(A, b), alg; abstol, reltol)
+ * + LinearSolve.solve(cache) (src/solvers.jl:89-101, :658-661).  `x` is
+ * overwritten.  Returns GRMP_ERR_NOT_CONVERGED (with x = the last iterate)
+ * when the caps are hit; device-side waits are bounded (GRMP_ERR_TIMEOUT). */
+int grmp_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *params,
+               grmp_solve_stats *stats);
+
+/* y = A x in the given precision (diagnostic / residual check,
+ * src/solvers.jl:664-668). */
+int grmp_spmv(grmp_matrix A, int precision, grmp_vector x, grmp_vector y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRMP_H */

@@ -1,0 +1,729 @@
+/*
+ * grmp_oracle.c -- CPU restatement of GradientRobustMultiPhysics.jl (v0.12.0)
+ * global assembly for the finite-element hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA library is
+ * compared against; it is loaded by the tests, by __graft_entry__.smoke() and by
+ * bench.py's CPU-baseline leg.  Nothing in the product links or calls it.
+ *
+ * Parity status: the reference is Julia and cannot run here (no julia binary,
+ * and ExtendableGrids / ExtendableSparse / LinearSolve are not vendored).  This
+ * restatement is pinned against the reference's own known-answer tests
+ * (test/runtests.jl quadrature exactness, polynomial reproduction of the
+ * elements, Stokes / pressure-robustness exactness) which the pytest suite
+ * re-implements.  Mesh numbering, the affine-map inverse and face orientation
+ * come from ExtendableGrids and are conventions of this build (see the
+ * mesh module and the design notes); they are "parity unpinned".
+ *
+ * Every routine follows the operation order of the reference file it cites so
+ * that the drop-exact-zero sparsity rule (src/fematrix.jl:54-65) sees the same
+ * floating-point zeros.  Build with -ffp-contract=off (no fused multiply-add),
+ * which is what Julia does for plain `a*b + c`.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OR_MAXQ 128
+#define OR_MAXD 32
+
+/* ------------------------------------------------------------------------- */
+/* Quadrature (src/quadrature.jl)                                            */
+/* ------------------------------------------------------------------------- */
+
+/* Symmetric tridiagonal eigen-decomposition by cyclic Jacobi rotations;
+ * returns ascending eigenvalues and the first component of each normalised
+ * eigenvector (all that Golub-Welsch needs).  The reference uses Julia's
+ * `eigen` (LAPACK); results agree to rounding. */
+static void sym_eig_first(int n, const double *diag, const double *off,
+                          double *evals, double *v1)
+{
+    double a[16][16], v[16][16];
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) { a[i][j] = 0.0; v[i][j] = (i == j) ? 1.0 : 0.0; }
+    for (int i = 0; i < n; i++) a[i][i] = diag[i];
+    for (int i = 0; i + 1 < n; i++) { a[i][i + 1] = off[i]; a[i + 1][i] = off[i]; }
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double offn = 0.0;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) offn += a[p][q] * a[p][q];
+        if (offn < 1e-300) break;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) {
+                if (fabs(a[p][q]) < 1e-300) continue;
+                double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; k++) {
+                    double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; k++) {
+                    double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; k++) {
+                    double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int idx[16];
+    for (int i = 0; i < n; i++) idx[i] = i;
+    for (int i = 0; i < n; i++)
+        for (int j = i + 1; j < n; j++)
+            if (a[idx[j]][idx[j]] < a[idx[i]][idx[i]]) { int t = idx[i]; idx[i] = idx[j]; idx[j] = t; }
+    for (int i = 0; i < n; i++) {
+        evals[i] = a[idx[i]][idx[i]];
+        double nrm = 0.0;
+        for (int k = 0; k < n; k++) nrm += v[k][idx[i]] * v[k][idx[i]];
+        v1[i] = v[0][idx[i]] / sqrt(nrm);
+    }
+}
+
+/* Gauss-Legendre on [0,1] (src/quadrature.jl:506-525). */
+static int gauss01(int order, double *x, double *w)
+{
+    int n = order / 2 + 1;
+    double diag[16] = {0}, off[16], ev[16], v1[16];
+    for (int i = 1; i <= n - 1; i++) off[i - 1] = i / sqrt(4.0 * i * i - 1.0);
+    sym_eig_first(n, diag, off, ev, v1);
+    for (int i = 0; i < n; i++) { x[i] = 0.5 * ev[i] + 0.5; w[i] = 0.5 * (2.0 * v1[i] * v1[i]); }
+    return n;
+}
+
+/* Stroud conical product rule on the reference triangle
+ * (src/quadrature.jl:528-562): points [s_j, r_i (1 - s_j)], weights a_i b_j,
+ * point index (j-1)*n + i. */
+static int stroud_tri(int order, double (*xref)[3], double *w)
+{
+    int n = order / 2 + 1;
+    double diag[16] = {0}, off[16], r[16], a[16], s[16], b[16], v1[16];
+    for (int i = 1; i <= n - 1; i++) off[i - 1] = i / sqrt(4.0 * i * i - 1.0);
+    sym_eig_first(n, diag, off, r, v1);
+    for (int i = 0; i < n; i++) a[i] = 2.0 * v1[i] * v1[i];
+    for (int i = 1; i <= n; i++) diag[i - 1] = -1.0 / (4.0 * i * i - 1.0);
+    for (int i = 1; i <= n - 1; i++) off[i - 1] = sqrt((double)(i + 1) * i) / (2.0 * (i + 1) - 1.0);
+    sym_eig_first(n, diag, off, s, v1);
+    for (int i = 0; i < n; i++) b[i] = 2.0 * v1[i] * v1[i];
+    for (int i = 0; i < n; i++) {
+        r[i] = 0.5 * r[i] + 0.5; s[i] = 0.5 * s[i] + 0.5;
+        a[i] = 0.5 * a[i]; b[i] = 0.5 * b[i];
+    }
+    int q = 0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            xref[q][0] = s[j] * 1.0 - r[i] * (s[j] - 1.0) * 0.0;
+            xref[q][1] = s[j] * 0.0 - r[i] * (s[j] - 1.0) * 1.0;
+            xref[q][2] = 0.0;
+            w[q] = a[i] * b[j];
+            q++;
+        }
+    return q;
+}
+
+/* Quadrature rule for a simplex of dimension dim (2 = Triangle2D,
+ * 3 = Tetrahedron3D) and the given order; src/quadrature.jl:173-194 (tri),
+ * :268-325 (tet).  Orders served: tri 0..20 except the symmetric-table orders
+ * 8 and 12..14 (for which the Stroud rule of the same order is returned and
+ * flagged by a negative count), tet 0..4.  Returns npoints, or 0 if the order
+ * is not available. */
+int oracle_qrule(int dim, int order, double *xref_out, double *w_out)
+{
+    double xr[OR_MAXQ][3];
+    double w[OR_MAXQ];
+    int n = 0, flag = 1;
+    memset(xr, 0, sizeof(xr));
+    if (dim == 1) {
+        if (order <= 1) { xr[0][0] = 0.5; w[0] = 1.0; n = 1; }
+        else if (order == 2) {
+            xr[0][0] = 0.0; xr[1][0] = 0.5; xr[2][0] = 1.0;
+            w[0] = 1.0 / 6.0; w[1] = 2.0 / 3.0; w[2] = 1.0 / 6.0; n = 3;
+        } else {
+            double x[16], ww[16];
+            n = gauss01(order, x, ww);
+            for (int i = 0; i < n; i++) { xr[i][0] = x[i]; w[i] = ww[i]; }
+        }
+    } else if (dim == 2) {
+        if (order <= 1) { xr[0][0] = 1.0 / 3.0; xr[0][1] = 1.0 / 3.0; w[0] = 1.0; n = 1; }
+        else if (order == 2) {
+            xr[0][0] = 0.5; xr[0][1] = 0.5;
+            xr[1][0] = 0.0; xr[1][1] = 0.5;
+            xr[2][0] = 0.5; xr[2][1] = 0.0;
+            w[0] = w[1] = w[2] = 1.0 / 3.0; n = 3;
+        } else if (order <= 20) {
+            if (order == 8 || (order >= 12 && order <= 14)) flag = -1;
+            n = stroud_tri(order, xr, w);
+        } else return 0;
+    } else if (dim == 3) {
+        if (order <= 1) { xr[0][0] = xr[0][1] = xr[0][2] = 0.25; w[0] = 1.0; n = 1; }
+        else if (order == 2) {
+            const double a = 0.1381966011250105, b = 0.5854101966249685;
+            double p[4][3] = {{a, a, a}, {b, a, a}, {a, b, a}, {a, a, b}};
+            for (int i = 0; i < 4; i++) { for (int k = 0; k < 3; k++) xr[i][k] = p[i][k]; w[i] = 0.25; }
+            n = 4;
+        } else if (order == 3) {
+            double p[5][3] = {{1.0 / 4, 1.0 / 4, 1.0 / 4}, {1.0 / 2, 1.0 / 6, 1.0 / 6}, {1.0 / 6, 1.0 / 6, 1.0 / 6},
+                              {1.0 / 6, 1.0 / 6, 1.0 / 2}, {1.0 / 6, 1.0 / 2, 1.0 / 6}};
+            double ww[5] = {-4.0 / 5, 9.0 / 20, 9.0 / 20, 9.0 / 20, 9.0 / 20};
+            for (int i = 0; i < 5; i++) { for (int k = 0; k < 3; k++) xr[i][k] = p[i][k]; w[i] = ww[i]; }
+            n = 5;
+        } else if (order == 4) {
+            const double c = 0.2500000000000000, d = 0.7857142857142857, e = 0.0714285714285714,
+                         f = 0.1005964238332008, g = 0.3994035761667992;
+            double p[11][3] = {{c, c, c}, {d, e, e}, {e, e, e}, {e, e, d}, {e, d, e},
+                               {f, g, g}, {g, f, g}, {g, g, f}, {g, f, f}, {f, g, f}, {f, f, g}};
+            double ww[11] = {-0.0789333333333333, 0.0457333333333333, 0.0457333333333333, 0.0457333333333333,
+                             0.0457333333333333, 0.1493333333333333, 0.1493333333333333, 0.1493333333333333,
+                             0.1493333333333333, 0.1493333333333333, 0.1493333333333333};
+            for (int i = 0; i < 11; i++) { for (int k = 0; k < 3; k++) xr[i][k] = p[i][k]; w[i] = ww[i]; }
+            n = 11;
+        } else return 0;
+    } else return 0;
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < 3; k++) xref_out[3 * i + k] = xr[i][k];
+        w_out[i] = w[i];
+    }
+    return flag * n;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Reference bases with ForwardDiff-ordered derivatives                      */
+/* ------------------------------------------------------------------------- */
+
+/* Dual number with up to 3 partials; products follow ForwardDiff's
+ * `vy*px + vx*py`, scalar*dual scales value and partials. */
+typedef struct { double v, d[3]; } dual;
+
+static dual dvar(double x, int j) { dual r = {x, {0, 0, 0}}; r.d[j] = 1.0; return r; }
+static dual dconst(double c) { dual r = {c, {0, 0, 0}}; return r; }
+static dual dmul(dual x, dual y)
+{
+    dual r; r.v = x.v * y.v;
+    for (int i = 0; i < 3; i++) r.d[i] = y.v * x.d[i] + x.v * y.d[i];
+    return r;
+}
+static dual dscale(double c, dual x)
+{
+    dual r; r.v = c * x.v;
+    for (int i = 0; i < 3; i++) r.d[i] = c * x.d[i];
+    return r;
+}
+static dual dsubc(dual x, double c) { dual r = x; r.v = x.v - c; return r; }
+static dual dcsub(double c, dual x)
+{
+    dual r; r.v = c - x.v;
+    for (int i = 0; i < 3; i++) r.d[i] = -x.d[i];
+    return r;
+}
+static dual dsub(dual x, dual y)
+{
+    dual r; r.v = x.v - y.v;
+    for (int i = 0; i < 3; i++) r.d[i] = x.d[i] - y.d[i];
+    return r;
+}
+
+enum { OR_FE_P1 = 1, OR_FE_P2 = 2, OR_FE_BR = 3, OR_FE_RT0 = 4, OR_FE_BDM1 = 5, OR_FE_P0 = 6 };
+
+/* Scalar reference basis (one component) of H1P1 / H1P2 on the simplex of
+ * dimension dim, evaluated on duals.  src/fedefs/h1_p1.jl:64-75,
+ * src/fedefs/h1_p2.jl:134-165.  Returns number of basis functions. */
+static int h1_scalar_basis(int fe, int dim, const dual *x, dual *out)
+{
+    if (fe == OR_FE_P1) {
+        dual r = dcsub(1.0, x[0]);
+        for (int j = 1; j < dim; j++) r = dsub(r, x[j]);
+        out[0] = r;
+        for (int j = 0; j < dim; j++) out[1 + j] = x[j];
+        return dim + 1;
+    }
+    if (fe == OR_FE_P2 && dim == 2) {
+        dual r = dsub(dcsub(1.0, x[0]), x[1]);
+        out[0] = dmul(dscale(2.0, r), dsubc(r, 0.5));
+        out[1] = dmul(dscale(2.0, x[0]), dsubc(x[0], 0.5));
+        out[2] = dmul(dscale(2.0, x[1]), dsubc(x[1], 0.5));
+        out[3] = dmul(dscale(4.0, r), x[0]);
+        out[4] = dmul(dscale(4.0, x[0]), x[1]);
+        out[5] = dmul(dscale(4.0, x[1]), r);
+        return 6;
+    }
+    if (fe == OR_FE_P2 && dim == 3) {
+        dual r = dsub(dsub(dcsub(1.0, x[0]), x[1]), x[2]);
+        out[0] = dmul(dscale(2.0, r), dsubc(r, 0.5));
+        out[1] = dmul(dscale(2.0, x[0]), dsubc(x[0], 0.5));
+        out[2] = dmul(dscale(2.0, x[1]), dsubc(x[1], 0.5));
+        out[3] = dmul(dscale(2.0, x[2]), dsubc(x[2], 0.5));
+        out[4] = dmul(dscale(4.0, r), x[0]);
+        out[5] = dmul(dscale(4.0, r), x[1]);
+        out[6] = dmul(dscale(4.0, r), x[2]);
+        out[7] = dmul(dscale(4.0, x[0]), x[1]);
+        out[8] = dmul(dscale(4.0, x[0]), x[2]);
+        out[9] = dmul(dscale(4.0, x[1]), x[2]);
+        return 10;
+    }
+    return 0;
+}
+
+/* Tabulate the scalar reference basis at the quadrature points:
+ * vals[q*nb + a], derivs[(q*nb + a)*dim + j] = d/dxref_j. */
+int oracle_basis_tables(int fe, int dim, int nq, const double *xref, double *vals, double *derivs)
+{
+    int nb = 0;
+    for (int q = 0; q < nq; q++) {
+        dual x[3], out[OR_MAXD];
+        for (int j = 0; j < dim; j++) x[j] = dvar(xref[3 * q + j], j);
+        nb = h1_scalar_basis(fe, dim, x, out);
+        for (int a = 0; a < nb; a++) {
+            vals[q * nb + a] = out[a].v;
+            for (int j = 0; j < dim; j++) derivs[(q * nb + a) * dim + j] = out[a].d[j];
+        }
+    }
+    return nb;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Geometry (ExtendableGrids L2GTransformer role; convention of this build)  */
+/* ------------------------------------------------------------------------- */
+
+/* A = [x1-x0, x2-x0(, x3-x0)] (columns).  G = A^{-T} = cof(A)/det(A), the
+ * matrix `L2GAinv` with cvals[k] = sum_j G[k][j] dref_j
+ * (src/feevaluator_h1.jl:61-74).  vol = |det|/2 or |det|/6. */
+void oracle_geometry(int dim, const double *X, double A[3][3], double G[3][3], double *det, double *vol)
+{
+    for (int k = 0; k < dim; k++)
+        for (int j = 0; j < dim; j++) A[k][j] = X[(j + 1) * dim + k] - X[k];
+    if (dim == 2) {
+        double d = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+        G[0][0] = A[1][1] / d;  G[0][1] = -A[1][0] / d;
+        G[1][0] = -A[0][1] / d; G[1][1] = A[0][0] / d;
+        *det = d; *vol = fabs(d) / 2.0;
+    } else {
+        double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+        double c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+        double c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+        double c10 = A[0][2] * A[2][1] - A[0][1] * A[2][2];
+        double c11 = A[0][0] * A[2][2] - A[0][2] * A[2][0];
+        double c12 = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+        double c20 = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+        double c21 = A[0][2] * A[1][0] - A[0][0] * A[1][2];
+        double c22 = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+        double d = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
+        G[0][0] = c00 / d; G[0][1] = c01 / d; G[0][2] = c02 / d;
+        G[1][0] = c10 / d; G[1][1] = c11 / d; G[1][2] = c12 / d;
+        G[2][0] = c20 / d; G[2][1] = c21 / d; G[2][2] = c22 / d;
+        *det = d; *vol = fabs(d) / 6.0;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Sparse accumulator with the reference's accumulation order                */
+/* ------------------------------------------------------------------------- */
+
+typedef struct { int n, cap; int *col; double *val; } orow;
+typedef struct { int nrows; orow *rows; } omat;
+
+static omat *omat_new(int n)
+{
+    omat *m = (omat *)calloc(1, sizeof(omat));
+    m->nrows = n;
+    m->rows = (orow *)calloc((size_t)n, sizeof(orow));
+    return m;
+}
+
+/* _addnz (src/fematrix.jl:54-58): skip exact zeros, otherwise
+ * rawupdateindex!(+): accumulate in call order. */
+static void omat_addnz(omat *m, int i, int j, double v, double fac)
+{
+    if (v == 0.0) return;
+    orow *r = &m->rows[i];
+    for (int k = 0; k < r->n; k++)
+        if (r->col[k] == j) { r->val[k] += v * fac; return; }
+    if (r->n == r->cap) {
+        r->cap = r->cap ? 2 * r->cap : 8;
+        r->col = (int *)realloc(r->col, sizeof(int) * (size_t)r->cap);
+        r->val = (double *)realloc(r->val, sizeof(double) * (size_t)r->cap);
+    }
+    r->col[r->n] = j; r->val[r->n] = v * fac; r->n++;
+}
+
+static void omat_set(omat *m, int i, int j, double v)
+{
+    orow *r = &m->rows[i];
+    for (int k = 0; k < r->n; k++)
+        if (r->col[k] == j) { r->val[k] = v; return; }
+    omat_addnz(m, i, j, v, 1.0);
+    for (int k = 0; k < r->n; k++)
+        if (r->col[k] == j) { r->val[k] = v; return; }
+}
+
+void *oracle_mat_new(int n) { return omat_new(n); }
+
+void oracle_mat_free(void *h)
+{
+    omat *m = (omat *)h;
+    if (!m) return;
+    for (int i = 0; i < m->nrows; i++) { free(m->rows[i].col); free(m->rows[i].val); }
+    free(m->rows); free(m);
+}
+
+long long oracle_mat_nnz(void *h)
+{
+    omat *m = (omat *)h;
+    long long nnz = 0;
+    for (int i = 0; i < m->nrows; i++) nnz += m->rows[i].n;
+    return nnz;
+}
+
+static int cmp_colval(const void *a, const void *b)
+{
+    const int ca = *(const int *)a, cb = *(const int *)b;
+    return (ca > cb) - (ca < cb);
+}
+
+/* Export as CSR with columns ascending. */
+void oracle_mat_csr(void *h, long long *rowptr, int *cols, double *vals)
+{
+    omat *m = (omat *)h;
+    long long p = 0;
+    typedef struct { int c; double v; } cv;
+    cv *buf = NULL; int bcap = 0;
+    for (int i = 0; i < m->nrows; i++) {
+        orow *r = &m->rows[i];
+        rowptr[i] = p;
+        if (r->n > bcap) { bcap = r->n; buf = (cv *)realloc(buf, sizeof(cv) * (size_t)bcap); }
+        for (int k = 0; k < r->n; k++) { buf[k].c = r->col[k]; buf[k].v = r->val[k]; }
+        qsort(buf, (size_t)r->n, sizeof(cv), cmp_colval);
+        for (int k = 0; k < r->n; k++) { cols[p] = buf[k].c; vals[p] = buf[k].v; p++; }
+    }
+    rowptr[m->nrows] = p;
+    free(buf);
+}
+
+/* apply_penalties! (src/fematrix.jl:349-355): A[d,d] = penalty. */
+void oracle_mat_penalize(void *h, int nfixed, const int *fixed, double penalty)
+{
+    omat *m = (omat *)h;
+    for (int k = 0; k < nfixed; k++) omat_set(m, fixed[k], fixed[k], penalty);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Operator evaluation at quadrature points (cvals)                          */
+/* ------------------------------------------------------------------------- */
+
+enum {
+    OR_OP_IDENTITY = 0,     /* Identity                          */
+    OR_OP_GRADIENT = 1,     /* Gradient                          */
+    OR_OP_SYMGRAD = 2,      /* SymmetricGradient{1} (Voigt)      */
+    OR_OP_DIVERGENCE = 3    /* Divergence                        */
+};
+
+/* cvals[(q*nd + dof)*rdim + k] for H1P1/H1P2 with ncomp components,
+ * local dof = c*nb + a.  Loop orders follow src/feevaluator_h1.jl:61-74
+ * (Gradient), :97-116 (SymmetricGradient), :119-131 (Divergence); the
+ * Identity values are the reference values (src/feevaluator.jl:107-115). */
+static int h1_cvals(int op, int dim, int ncomp, int nb, int nq, const double *vals, const double *derivs,
+                    double G[3][3], double *cv)
+{
+    int nd = nb * ncomp;
+    int rdim;
+    if (op == OR_OP_IDENTITY) rdim = ncomp;
+    else if (op == OR_OP_GRADIENT) rdim = dim * ncomp;
+    else if (op == OR_OP_SYMGRAD) rdim = (dim == 2) ? 3 : 6;
+    else rdim = 1;
+    memset(cv, 0, sizeof(double) * (size_t)nq * nd * rdim);
+    static const int comp2[4] = {0, 2, 2, 1};
+    static const int comp3[9] = {0, 5, 4, 5, 1, 3, 4, 3, 2};
+    for (int q = 0; q < nq; q++) {
+        if (op == OR_OP_IDENTITY) {
+            for (int dof = 0; dof < nd; dof++)
+                for (int k = 0; k < ncomp; k++) {
+                    int c = dof / nb, a = dof % nb;
+                    cv[(q * nd + dof) * rdim + k] = (c == k) ? vals[q * nb + a] : 0.0;
+                }
+        } else if (op == OR_OP_GRADIENT) {
+            /* for i, c, j, k, dof: cvals[k+off_c, dof] += G[k,j]*dref[dof+off2_c, j] */
+            for (int c = 0; c < ncomp; c++)
+                for (int j = 0; j < dim; j++)
+                    for (int k = 0; k < dim; k++)
+                        for (int dof = 0; dof < nd; dof++) {
+                            int cd = dof / nb, a = dof % nb;
+                            double d = (cd == c) ? derivs[(q * nb + a) * dim + j] : 0.0;
+                            cv[(q * nd + dof) * rdim + k + c * dim] += G[k][j] * d;
+                        }
+        } else if (op == OR_OP_SYMGRAD) {
+            const int *comp = (dim == 2) ? comp2 : comp3;
+            for (int dof = 0; dof < nd; dof++)
+                for (int c = 0; c < ncomp; c++)
+                    for (int k = 0; k < dim; k++)
+                        for (int j = 0; j < dim; j++) {
+                            int cd = dof / nb, a = dof % nb;
+                            double d = (cd == c) ? derivs[(q * nb + a) * dim + j] : 0.0;
+                            int t = comp[k + c * dim];
+                            if (k != c) cv[(q * nd + dof) * rdim + t] += 1.0 * G[k][j] * d;
+                            else cv[(q * nd + dof) * rdim + t] += G[k][j] * d;
+                        }
+        } else { /* divergence */
+            for (int dof = 0; dof < nd; dof++)
+                for (int k = 0; k < dim; k++)
+                    for (int j = 0; j < dim; j++) {
+                        int cd = dof / nb, a = dof % nb;
+                        double d = (cd == k) ? derivs[(q * nb + a) * dim + j] : 0.0;
+                        cv[(q * nd + dof) * rdim] += G[k][j] * d;
+                    }
+        }
+    }
+    return rdim;
+}
+
+/* ------------------------------------------------------------------------- */
+/* BilinearForm assembly (src/assemblypatterns/bilinearform.jl:92-380)       */
+/* ------------------------------------------------------------------------- */
+
+enum {
+    OR_ACT_NONE = 0,       /* NoAction: result = input                     */
+    OR_ACT_CELLSCALE = 1,  /* result = coef[cell] * input ("I" dependency)  */
+    OR_ACT_HOOKE2D = 2,    /* tensor_apply_2d, src/pdeoperators.jl:265-270 */
+    OR_ACT_HOOKE3D = 3     /* tensor_apply_3d                               */
+};
+
+typedef struct {
+    int dim;            /* 2 or 3                                  */
+    int nverts;
+    const double *coords;   /* [nverts][dim]                       */
+    int ncells;
+    const int *cellnodes;   /* [ncells][dim+1]                     */
+    int fe;             /* OR_FE_P1 / OR_FE_P2                     */
+    int ncomp;
+    int ldofs;          /* local dofs per cell = nb*ncomp          */
+    const int *celldofs;    /* [ncells][ldofs], 0-based            */
+} or_space;
+
+/* Assemble one BilinearForm with operator `op` on both arguments into the
+ * accumulator `h` (which may already hold other operators).  `symmetric`
+ * selects APT_SymmetricBilinearForm (upper triangle computed once and
+ * scattered twice, :196-210, :329-346) versus APT_BilinearForm (full block,
+ * :180-192, :347-367).  The local matrix is built qp-outer, dof_i, dof_j as in
+ * basismul!; the scatter value is local[i,j] * (volume * factor) and exact
+ * zeros are dropped by _addnz. */
+int oracle_assemble_bilinear(void *h, int dim, int nverts, const double *coords, int ncells, const int *cellnodes,
+                             int fe, int ncomp, const int *celldofs, int op, int symmetric, double factor,
+                             int action, const double *cellcoef, double mu, double lambda, int bonus_quadorder)
+{
+    omat *m = (omat *)h;
+    int nb = (fe == OR_FE_P1) ? dim + 1 : (dim == 2 ? 6 : 10);
+    int nd = nb * ncomp;
+    int polyorder = (fe == OR_FE_P1) ? 1 : 2;
+    int derivorder = (op == OR_OP_IDENTITY) ? 0 : 1;
+    int order = bonus_quadorder + 2 * (polyorder - derivorder);
+    if (order < 0) order = 0;
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(dim, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    double *vals = (double *)malloc(sizeof(double) * (size_t)nq * nb);
+    double *derivs = (double *)malloc(sizeof(double) * (size_t)nq * nb * dim);
+    oracle_basis_tables(fe, dim, nq, xref, vals, derivs);
+    double *cv = (double *)malloc(sizeof(double) * (size_t)nq * nd * 6 * 3);
+    double *loc = (double *)malloc(sizeof(double) * (size_t)nd * nd);
+    double X[4 * 3];
+    for (int cell = 0; cell < ncells; cell++) {
+        for (int v = 0; v <= dim; v++)
+            for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cellnodes[(size_t)cell * (dim + 1) + v] * dim + k];
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(dim, X, A, G, &det, &vol);
+        int rdim = h1_cvals(op, dim, ncomp, nb, nq, vals, derivs, G, cv);
+        memset(loc, 0, sizeof(double) * (size_t)nd * nd);
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < nd; i++) {
+                double res[6];
+                const double *in = &cv[(q * nd + i) * rdim];
+                if (action == OR_ACT_NONE) for (int k = 0; k < rdim; k++) res[k] = in[k];
+                else if (action == OR_ACT_CELLSCALE) for (int k = 0; k < rdim; k++) res[k] = cellcoef[cell] * in[k];
+                else if (action == OR_ACT_HOOKE2D) {
+                    res[0] = (lambda + 2 * mu) * in[0] + lambda * in[1];
+                    res[1] = (lambda + 2 * mu) * in[1] + lambda * in[0];
+                    res[2] = mu * in[2];
+                } else {
+                    /* tensor_apply_3d, src/pdeoperators.jl:304-312 */
+                    res[0] = (lambda + 2 * mu) * in[0] + lambda * (in[1] + in[2]);
+                    res[1] = (lambda + 2 * mu) * in[1] + lambda * (in[0] + in[2]);
+                    res[2] = (lambda + 2 * mu) * in[2] + lambda * (in[0] + in[1]);
+                    res[3] = mu * in[3]; res[4] = mu * in[4]; res[5] = mu * in[5];
+                }
+                int j0 = symmetric ? i : 0;
+                for (int j = j0; j < nd; j++) {
+                    double t = 0;
+                    for (int k = 0; k < rdim; k++) t += res[k] * cv[(q * nd + j) * rdim + k];
+                    loc[i * nd + j] += w[q] * t;
+                }
+            }
+        double itemfactor = vol * factor;
+        const int *dofs = &celldofs[(size_t)cell * nd];
+        if (symmetric) {
+            for (int i = 0; i < nd; i++)
+                for (int j = i + 1; j < nd; j++) {
+                    omat_addnz(m, dofs[i], dofs[j], loc[i * nd + j] * itemfactor, 1.0);
+                    omat_addnz(m, dofs[j], dofs[i], loc[i * nd + j] * itemfactor, 1.0);
+                }
+            for (int i = 0; i < nd; i++) omat_addnz(m, dofs[i], dofs[i], loc[i * nd + i] * itemfactor, 1.0);
+        } else {
+            for (int i = 0; i < nd; i++)
+                for (int j = 0; j < nd; j++) omat_addnz(m, dofs[i], dofs[j], loc[i * nd + j] * itemfactor, 1.0);
+        }
+    }
+    free(vals); free(derivs); free(cv); free(loc);
+    return nq;
+}
+
+/* ------------------------------------------------------------------------- */
+/* LinearForm assembly (src/assemblypatterns/linearform.jl:47-237)           */
+/* ------------------------------------------------------------------------- */
+
+enum {
+    OR_RHS_CONST = 0,    /* f = const vector (ncomp values)                     */
+    OR_RHS_CELL = 1,     /* f = per-cell vector [ncells][ncomp] ("I")            */
+    OR_RHS_FOURIER = 2,  /* f = sum_m a_m sin(pi k_m . x) (scalar, "X")          */
+    OR_RHS_POLY = 3      /* f_c = sum_t coef_t x^e1 y^e2 z^e3 (vector, "X")      */
+};
+
+/* Evaluate f at a physical point: eval_trafo! gives x = x0 + A xref. */
+static void rhs_eval(int kind, int dim, int ncomp, const double *par, int npar, int cell, const double *x, double *f)
+{
+    if (kind == OR_RHS_CONST) { for (int c = 0; c < ncomp; c++) f[c] = par[c]; return; }
+    if (kind == OR_RHS_CELL) { for (int c = 0; c < ncomp; c++) f[c] = par[(size_t)cell * ncomp + c]; return; }
+    if (kind == OR_RHS_FOURIER) {
+        /* par = [a_m, k_m1, k_m2, (k_m3)] per mode */
+        int stride = 1 + dim, nm = npar / stride;
+        double s = 0;
+        for (int mm = 0; mm < nm; mm++) {
+            double arg = 0;
+            for (int j = 0; j < dim; j++) arg += par[mm * stride + 1 + j] * x[j];
+            s += par[mm * stride] * sin(M_PI * arg);
+        }
+        f[0] = s;
+        for (int c = 1; c < ncomp; c++) f[c] = 0;
+        return;
+    }
+    /* polynomial: par = [comp, coef, e1, e2, e3] per term */
+    for (int c = 0; c < ncomp; c++) f[c] = 0;
+    int nt = npar / 5;
+    for (int t = 0; t < nt; t++) {
+        int c = (int)par[5 * t];
+        double v = par[5 * t + 1];
+        for (int j = 0; j < dim; j++) v *= pow(x[j], par[5 * t + 2 + j]);
+        f[c] += v;
+    }
+}
+
+/* b[dof] += (factor*vol) * sum_q w_q sum_k f_k(x_q) cvals[k,dof,q] with the
+ * Identity test operator; quadrature order polyorder + bonus. */
+int oracle_assemble_linear(double *b, int dim, int nverts, const double *coords, int ncells, const int *cellnodes,
+                           int fe, int ncomp, const int *celldofs, int rhs_kind, const double *par, int npar,
+                           double factor, int bonus_quadorder)
+{
+    int nb = (fe == OR_FE_P1) ? dim + 1 : (dim == 2 ? 6 : 10);
+    int nd = nb * ncomp;
+    int polyorder = (fe == OR_FE_P1) ? 1 : 2;
+    int order = polyorder + bonus_quadorder;
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(dim, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    double *vals = (double *)malloc(sizeof(double) * (size_t)nq * nb);
+    double *derivs = (double *)malloc(sizeof(double) * (size_t)nq * nb * dim);
+    oracle_basis_tables(fe, dim, nq, xref, vals, derivs);
+    double G[3][3];
+    double *cv = (double *)malloc(sizeof(double) * (size_t)nq * nd * 6);
+    double *locb = (double *)malloc(sizeof(double) * (size_t)nd);
+    double X[12];
+    for (int cell = 0; cell < ncells; cell++) {
+        for (int v = 0; v <= dim; v++)
+            for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cellnodes[(size_t)cell * (dim + 1) + v] * dim + k];
+        double A[3][3], det, vol;
+        oracle_geometry(dim, X, A, G, &det, &vol);
+        h1_cvals(OR_OP_IDENTITY, dim, ncomp, nb, nq, vals, derivs, G, cv);
+        memset(locb, 0, sizeof(double) * (size_t)nd);
+        for (int q = 0; q < nq; q++) {
+            double x[3] = {0, 0, 0}, f[3];
+            for (int k = 0; k < dim; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < dim; j++) x[k] += A[k][j] * xref[3 * q + j];
+            }
+            rhs_eval(rhs_kind, dim, ncomp, par, npar, cell, x, f);
+            for (int i = 0; i < nd; i++) {
+                double t = 0;
+                for (int k = 0; k < ncomp; k++) t += f[k] * cv[(q * nd + i) * ncomp + k];
+                locb[i] += t * w[q];
+            }
+        }
+        double itemfactor = factor * vol;
+        for (int i = 0; i < nd; i++) b[celldofs[(size_t)cell * nd + i]] += locb[i] * itemfactor;
+    }
+    free(vals); free(derivs); free(cv); free(locb);
+    return nq;
+}
+
+/* ------------------------------------------------------------------------- */
+/* FP64 CG (Jacobi) on CSR -- used for sizes where a sparse-direct           */
+/* factorisation does not fit, and as the multi-threaded CPU baseline solve. */
+/* ------------------------------------------------------------------------- */
+
+static void csr_mv(int n, const long long *rp, const int *ci, const double *v, const double *x, double *y)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        double s = 0;
+        for (long long p = rp[i]; p < rp[i + 1]; p++) s += v[p] * x[ci[p]];
+        y[i] = s;
+    }
+}
+
+static double dotp(int n, const double *a, const double *b)
+{
+    double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+/* Returns iterations; stops when ||r|| <= reltol*||b|| or maxit. */
+int oracle_cg(int n, const long long *rp, const int *ci, const double *v, const double *b, double *x, double reltol,
+              int maxit, double *final_relres)
+{
+    double *r = (double *)malloc(sizeof(double) * (size_t)n), *z = (double *)malloc(sizeof(double) * (size_t)n);
+    double *p = (double *)malloc(sizeof(double) * (size_t)n), *q = (double *)malloc(sizeof(double) * (size_t)n);
+    double *dinv = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        double d = 1.0;
+        for (long long k = rp[i]; k < rp[i + 1]; k++) if (ci[k] == i) d = v[k];
+        dinv[i] = 1.0 / d;
+    }
+    csr_mv(n, rp, ci, v, x, q);
+#pragma omp parallel for
+    for (int i = 0; i < n; i++) { r[i] = b[i] - q[i]; z[i] = dinv[i] * r[i]; p[i] = z[i]; }
+    double bn = sqrt(dotp(n, b, b));
+    if (bn == 0) bn = 1;
+    double rz = dotp(n, r, z);
+    int it = 0;
+    double rn = sqrt(dotp(n, r, r));
+    while (it < maxit && rn > reltol * bn) {
+        csr_mv(n, rp, ci, v, p, q);
+        double alpha = rz / dotp(n, p, q);
+#pragma omp parallel for
+        for (int i = 0; i < n; i++) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; z[i] = dinv[i] * r[i]; }
+        double rz2 = dotp(n, r, z);
+        double beta = rz2 / rz;
+        rz = rz2;
+#pragma omp parallel for
+        for (int i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
+        rn = sqrt(dotp(n, r, r));
+        it++;
+    }
+    if (final_relres) *final_relres = rn / bn;
+    free(r); free(z); free(p); free(q); free(dinv);
+    return it;
+}

@@ -1,0 +1,245 @@
+"""Python harness of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline
+leg.  The product never imports this module.
+
+It wraps ``grmp_oracle.c`` (a restatement of GradientRobustMultiPhysics.jl's
+assembly, see that file's header), restates the DoF-map construction of
+``init_dofmap_from_pattern!`` (src/dofmaps.jl:201-330) independently of the
+library's own, and performs the reference's FP64 solve: penalised system
+(src/solvers.jl:640-652) and a sparse-direct factorisation.  The reference's
+default is UMFPACK via LinearSolve.jl (src/solvers.jl:55); scipy's SuperLU is
+the sparse-direct solver available here and stands in for it.  For systems
+too large for a direct factorisation the FP64 CG of grmp_oracle.c is used with
+a stated tolerance.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+SO = os.path.join(BUILD, "libgrmp_oracle.so")
+
+FE_P1, FE_P2, FE_BR, FE_RT0, FE_BDM1, FE_P0 = 1, 2, 3, 4, 5, 6
+OP_IDENTITY, OP_GRADIENT, OP_SYMGRAD, OP_DIVERGENCE = 0, 1, 2, 3
+ACT_NONE, ACT_CELLSCALE, ACT_HOOKE2D, ACT_HOOKE3D = 0, 1, 2, 3
+RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
+
+
+def build(force: bool = False) -> str:
+    """Compile grmp_oracle.c (no FMA contraction, OpenMP for the CG)."""
+    src = os.path.join(HERE, "grmp_oracle.c")
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(src):
+        cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-ffp-contract=off",
+               "-fno-fast-math", "-fopenmp", src, "-o", SO, "-lm"]
+        subprocess.check_call(cmd)
+    return SO
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        L = _lib
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        llp = ctypes.POINTER(ctypes.c_longlong)
+        L.oracle_qrule.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp]
+        L.oracle_qrule.restype = ctypes.c_int
+        L.oracle_basis_tables.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
+        L.oracle_basis_tables.restype = ctypes.c_int
+        L.oracle_mat_new.argtypes = [ctypes.c_int]
+        L.oracle_mat_new.restype = ctypes.c_void_p
+        L.oracle_mat_free.argtypes = [ctypes.c_void_p]
+        L.oracle_mat_nnz.argtypes = [ctypes.c_void_p]
+        L.oracle_mat_nnz.restype = ctypes.c_longlong
+        L.oracle_mat_csr.argtypes = [ctypes.c_void_p, llp, ip, dp]
+        L.oracle_mat_penalize.argtypes = [ctypes.c_void_p, ctypes.c_int, ip, ctypes.c_double]
+        L.oracle_assemble_bilinear.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ip,
+                                               ctypes.c_int, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_double, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_int]
+        L.oracle_assemble_bilinear.restype = ctypes.c_int
+        L.oracle_assemble_linear.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ip, ctypes.c_int,
+                                             ctypes.c_int, ip, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double,
+                                             ctypes.c_int]
+        L.oracle_assemble_linear.restype = ctypes.c_int
+        L.oracle_cg.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
+        L.oracle_cg.restype = ctypes.c_int
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _llp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+
+
+# --------------------------------------------------------------------------
+# quadrature and bases
+# --------------------------------------------------------------------------
+
+def qrule(dim: int, order: int):
+    """(xref (n, 3), w (n,), exact_reference_rule: bool)."""
+    x = np.zeros(3 * 128)
+    w = np.zeros(128)
+    n = lib().oracle_qrule(dim, order, _dp(x), _dp(w))
+    if n == 0:
+        raise ValueError(f"no quadrature rule dim={dim} order={order}")
+    return x[: 3 * abs(n)].reshape(-1, 3).copy(), w[: abs(n)].copy(), n > 0
+
+
+def basis_tables(fe: int, dim: int, xref: np.ndarray):
+    nq = xref.shape[0]
+    nb = (dim + 1) if fe == FE_P1 else (6 if dim == 2 else 10)
+    vals = np.zeros(nq * nb)
+    der = np.zeros(nq * nb * dim)
+    x3 = np.zeros((nq, 3))
+    x3[:, : xref.shape[1]] = xref
+    x = np.ascontiguousarray(x3, dtype=np.float64).ravel()
+    lib().oracle_basis_tables(fe, dim, nq, _dp(x), _dp(vals), _dp(der))
+    return vals.reshape(nq, nb), der.reshape(nq, nb, dim)
+
+
+# --------------------------------------------------------------------------
+# DoF maps, restated from src/dofmaps.jl:201-330 (patterns N1, N1F1, N1E1)
+# --------------------------------------------------------------------------
+
+def _enumerate_entities(cells: np.ndarray, local: np.ndarray):
+    loc = np.sort(cells[:, local], axis=2).reshape(-1, local.shape[1])
+    uniq, inv = np.unique(loc, axis=0, return_inverse=True)
+    return uniq, inv.reshape(cells.shape[0], local.shape[0])
+
+
+def celldofs(fe: int, ncomp: int, dim: int, nverts: int, cells: np.ndarray):
+    """(celldofs (ncells, ldofs) int32, ndofs, coffset) for H1P1 / H1P2."""
+    if fe == FE_P1:
+        coffset = nverts
+        items = [cells]
+    else:
+        if dim == 2:
+            local = np.array([[0, 1], [1, 2], [2, 0]])
+        else:
+            local = np.array([[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3]])
+        ents, cent = _enumerate_entities(cells, local)
+        coffset = nverts + ents.shape[0]
+        items = [cells, cent + nverts]
+    cols = []
+    for c in range(ncomp):
+        for it in items:
+            cols.append(it.astype(np.int64) + c * coffset)
+    return np.concatenate(cols, axis=1).astype(np.int32), coffset * ncomp, coffset
+
+
+# --------------------------------------------------------------------------
+# assembly
+# --------------------------------------------------------------------------
+
+class Matrix:
+    """Sparse accumulator with the reference's accumulation order and the
+    drop-exact-zero rule of _addnz."""
+
+    def __init__(self, n: int):
+        self.n = n
+        self.h = lib().oracle_mat_new(n)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_mat_free(self.h)
+            self.h = None
+
+    def add_bilinear(self, coords, cells, fe, ncomp, cdofs, op, symmetric, factor=1.0, action=ACT_NONE,
+                     cellcoef=None, mu=0.0, lam=0.0, bonus_quadorder=0):
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        cdofs = np.ascontiguousarray(cdofs, dtype=np.int32)
+        dim = coords.shape[1]
+        cc = np.ascontiguousarray(cellcoef if cellcoef is not None else np.zeros(1), dtype=np.float64)
+        nq = lib().oracle_assemble_bilinear(self.h, dim, coords.shape[0], _dp(coords), cells.shape[0], _ip(cells),
+                                            fe, ncomp, _ip(cdofs), op, int(symmetric), float(factor), action,
+                                            _dp(cc), float(mu), float(lam), int(bonus_quadorder))
+        if nq < 0:
+            raise RuntimeError("oracle bilinear assembly failed")
+        return nq
+
+    def penalize(self, fixed, penalty=1e60):
+        f = np.ascontiguousarray(fixed, dtype=np.int32)
+        lib().oracle_mat_penalize(self.h, f.shape[0], _ip(f), float(penalty))
+
+    def csr(self):
+        import scipy.sparse as sp
+        nnz = lib().oracle_mat_nnz(self.h)
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        ci = np.zeros(nnz, dtype=np.int32)
+        v = np.zeros(nnz)
+        lib().oracle_mat_csr(self.h, _llp(rp), _ip(ci), _dp(v))
+        return sp.csr_matrix((v, ci, rp), shape=(self.n, self.n))
+
+
+def assemble_linear(b, coords, cells, fe, ncomp, cdofs, rhs_kind, params, factor=1.0, bonus_quadorder=0):
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    cells = np.ascontiguousarray(cells, dtype=np.int32)
+    cdofs = np.ascontiguousarray(cdofs, dtype=np.int32)
+    par = np.ascontiguousarray(params, dtype=np.float64).ravel()
+    if par.size == 0:
+        par = np.zeros(1)
+    assert b.dtype == np.float64 and b.flags.c_contiguous
+    nq = lib().oracle_assemble_linear(_dp(b), coords.shape[1], coords.shape[0], _dp(coords), cells.shape[0],
+                                      _ip(cells), fe, ncomp, _ip(cdofs), rhs_kind, _dp(par), par.size,
+                                      float(factor), int(bonus_quadorder))
+    if nq < 0:
+        raise RuntimeError("oracle linear assembly failed")
+    return b
+
+
+# --------------------------------------------------------------------------
+# solve (src/solvers.jl:622-686)
+# --------------------------------------------------------------------------
+
+def penalized_rhs(b, fixed, values=None, penalty=1e60):
+    b = b.copy()
+    if values is None:
+        b[fixed] = 0.0
+    else:
+        b[fixed] = penalty * values
+    return b
+
+
+def solve_direct(A, b):
+    """FP64 sparse-direct solve (SuperLU standing in for UMFPACK)."""
+    import scipy.sparse.linalg as spla
+    return spla.spsolve(A.tocsc(), b)
+
+
+def solve_cg(A, b, reltol=1e-14, maxit=100000):
+    """FP64 Jacobi-CG of grmp_oracle.c (OpenMP); returns (x, iters, relres)."""
+    A = A.tocsr()
+    n = A.shape[0]
+    rp = np.ascontiguousarray(A.indptr, dtype=np.int64)
+    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+    v = np.ascontiguousarray(A.data, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    rr = ctypes.c_double(0)
+    it = lib().oracle_cg(n, _llp(rp), _ip(ci), _dp(v), _dp(bb), _dp(x), reltol, maxit, ctypes.byref(rr))
+    return x, it, rr.value
+
+
+if __name__ == "__main__":  # pragma: no cover - manual build helper
+    print(build(force="--force" in sys.argv))
