@@ -511,7 +511,7 @@ int grmp_pattern_build_impl(grmp_space s, int nterms, const grmp_bilinear_term *
         A->max_row_nnz = hmax;
         A->slot_bytes = hmax < 255 ? 1 : 2;
         rc = grmp_alloc(ctx, (void **)&A->d_cols, (size_t)total * 4);
-        if (!rc) rc = grmp_alloc(ctx, &A->d_slot, ncl * A->slot_bytes);
+        if (!rc) rc = grmp_alloc(ctx, &A->d_slot, ncl * ld * A->slot_bytes);   // ld slots per incidence
     }
     if (!rc) {
         if (A->slot_bytes == 1)
@@ -547,7 +547,7 @@ extern "C" int grmp_matrix_destroy(grmp_matrix A) {
     size_t ncl = (size_t)A->space->mesh->ncells * A->space->ldofs;
     grmp_free(ctx, A->d_rowptr, ((size_t)A->nrows + 1) * 4);
     grmp_free(ctx, A->d_cols, (size_t)A->nnz * 4);
-    grmp_free(ctx, A->d_slot, ncl * A->slot_bytes);
+    grmp_free(ctx, A->d_slot, ncl * A->space->ldofs * A->slot_bytes);
     grmp_free(ctx, A->d_vals64, (size_t)A->nnz * 8);
     grmp_free(ctx, A->d_vals32, (size_t)A->nnz * 4);
     grmp_free(ctx, A->d_fixed, (size_t)A->nrows);
