@@ -75,8 +75,12 @@ class GB300Context:
 
     # -- handles ------------------------------------------------------------
     def mesh(self, grid: SimplexMesh, with_faces: bool = False):
+        # entries keep a strong reference to the grid so that its id() cannot
+        # be reused by another object while the device copy exists
         key = id(grid)
         ent = self._meshes.get(key)
+        if ent is not None and ent["grid"] is not grid:
+            ent = None
         if ent is None:
             h = ctypes.c_void_p()
             coords = np.ascontiguousarray(grid.coords, dtype=np.float64)
@@ -99,19 +103,26 @@ class GB300Context:
 
     def space(self, FES: FESpace):
         key = id(FES)
-        h = self._spaces.get(key)
-        if h is None:
+        ent = self._spaces.get(key)
+        if ent is None or ent[0] is not FES:
             mh = self.mesh(FES.xgrid, with_faces=(FES.FEType.kind == FE_H1BR))
             h = ctypes.c_void_p()
             cd = np.ascontiguousarray(FES.celldofs, dtype=np.int32)
             self.check(self.lib.grmp_space_create(mh, FES.FEType.kind, FES.FEType.ncomponents, _ip(cd), FES.ndofs,
                                                   ctypes.byref(h)))
-            self._spaces[key] = h
-        return h
+            ent = (FES, h)
+            self._spaces[key] = ent
+        return ent[1]
+
+    def release(self, FES: FESpace):
+        """Free the device copy of a space (its mesh stays resident)."""
+        ent = self._spaces.pop(id(FES), None)
+        if ent is not None:
+            self.lib.grmp_space_destroy(ent[1])
 
     def close(self):
         if getattr(self, "h", None):
-            for h in self._spaces.values():
+            for _, h in self._spaces.values():
                 self.lib.grmp_space_destroy(h)
             for ent in self._meshes.values():
                 self.lib.grmp_mesh_destroy(ent["h"])

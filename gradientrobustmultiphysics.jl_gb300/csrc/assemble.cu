@@ -52,7 +52,9 @@ struct FastTerms {
     const double *coef[GRMP_MAX_TERMS];
 };
 
-// Per-cell factors: fac[cell*nf_total + foff + f].
+// Per-cell factors: fac[cell*nf_total + foff + f].  The factors are formed in
+// FP64 (a few dozen operations per cell) and rounded once to the storage
+// precision T, so FP32 element matrices carry no FP32 geometry error.
 template <int DIM, int NC, typename T>
 __global__ void k_cell_factors(int ncells, const double *coords, const int32_t *cells, FastTerms ft, T *fac) {
     int cell = blockIdx.x * blockDim.x + threadIdx.x;
@@ -60,27 +62,27 @@ __global__ void k_cell_factors(int ncells, const double *coords, const int32_t *
     double X[4 * 3];
     for (int v = 0; v <= DIM; v++)
         for (int k = 0; k < DIM; k++) X[v * DIM + k] = coords[(size_t)cells[(size_t)cell * (DIM + 1) + v] * DIM + k];
-    T G[3][3], A[3][3], vol;
-    simplex_geometry<DIM, T>(X, G, vol, A);
+    double G[3][3], A[3][3], vol;
+    simplex_geometry<DIM, double>(X, G, vol, A);
     T *out = fac + (size_t)cell * ft.nf_total;
     for (int ti = 0; ti < ft.n; ti++) {
         const FastTerm &t = ft.t[ti];
-        T scale = vol * (T)ft.factor[ti];
-        if (ft.coef[ti]) scale *= (T)ft.coef[ti][cell];
+        double scale = vol * ft.factor[ti];
+        if (ft.coef[ti]) scale *= ft.coef[ti][cell];
         if (t.op == GRMP_OP_LAPLACE) {
             int f = 0;
             for (int p = 0; p < DIM; p++)
                 for (int s = p; s < DIM; s++) {
-                    T m = 0;
+                    double m = 0;
                     for (int k = 0; k < DIM; k++) m += G[k][p] * G[k][s];
-                    out[t.foff + f++] = scale * m;
+                    out[t.foff + f++] = (T)(scale * m);
                 }
         } else if (t.op == GRMP_OP_MASS) {
-            out[t.foff] = scale;
+            out[t.foff] = (T)scale;
         } else {  // Hooke: C in Voigt form, V(c,k) = unit vector of the Voigt slot
-            const T l = (T)ft.lambda[ti], mu = (T)ft.mu[ti];
+            const double l = ft.lambda[ti], mu = ft.mu[ti];
             constexpr int NV = DIM == 2 ? 3 : 6;
-            T C[NV][NV];
+            double C[NV][NV];
             for (int i = 0; i < NV; i++)
                 for (int j = 0; j < NV; j++) C[i][j] = 0;
             for (int i = 0; i < DIM; i++)
@@ -90,11 +92,11 @@ __global__ void k_cell_factors(int ncells, const double *coords, const int32_t *
                 for (int c2 = 0; c2 < NC; c2++)
                     for (int p = 0; p < DIM; p++)
                         for (int s = 0; s < DIM; s++) {
-                            T acc = 0;
+                            double acc = 0;
                             for (int k1 = 0; k1 < DIM; k1++)
                                 for (int k2 = 0; k2 < DIM; k2++)
                                     acc += C[voigt_slot(DIM, c1, k1)][voigt_slot(DIM, c2, k2)] * G[k1][p] * G[k2][s];
-                            out[t.foff + ((c1 * NC + c2) * DIM + p) * DIM + s] = scale * acc;
+                            out[t.foff + ((c1 * NC + c2) * DIM + p) * DIM + s] = (T)(scale * acc);
                         }
         }
     }

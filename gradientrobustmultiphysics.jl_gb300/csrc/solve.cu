@@ -93,14 +93,32 @@ __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ r
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     constexpr int RPW = 32 / TPR;   // rows per warp per step
     const int gin = (threadIdx.x & 31) / TPR;
+    // Each lane keeps U independent (col, val) loads and U gathers in
+    // flight per pass: the SpMV is bound by memory-level parallelism, not
+    // arithmetic.  The matrix is read-only for the whole solve (non-coherent
+    // path); x is written by other blocks between barriers (coherent loads).
+    constexpr int U = TPR >= 16 ? 2 : 4;
+    using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
     double dot = 0;
+    A dacc = 0;
     for (int base = warp * RPW; base < n; base += nwarps * RPW) {
         int r = base + gin;
-        using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
         A s = 0;
         if (r < n) {
-            int e = rowptr[r + 1];
-            for (int k = rowptr[r] + lane; k < e; k += TPR) s += (A)vals[k] * (A)x[cols[k]];
+            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                A v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(cols + idx) : r;
+                    v[u] = ok ? (A)__ldg(vals + idx) : A(0);
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) s += v[u] * (A)x[c[u]];
+            }
         }
 #pragma unroll
         for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -111,11 +129,11 @@ __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ r
                 if (DOT) dot += v * v;
             } else {
                 y[r] = (Y)s;
-                if (DOT) dot += (double)w[r] * (double)s;
+                if (DOT) dacc += (A)w[r] * s;   // FP32 partial in the FP32 path
             }
         }
     }
-    return dot;
+    return dot + (double)dacc;
 }
 
 // ------------------------------------------------------------------ FP64 PCG
@@ -234,6 +252,8 @@ __global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr
     if (!grid_sum<2>(w, partial, sh, st)) return;
     double rz = w[0];
     double rmax = sqrt(w[1]);
+    double prev_rn64 = rn64;
+    int stall = 0;
     while (!conv && it < maxit && outer < maxouter) {
         double d[1];
         d[0] = spmv_grid<TPR, float, float, float, true, false>(n, rowptr, cols, vals32, p, q, p, nullptr);
@@ -244,20 +264,23 @@ __global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr
             break;
         }
         const float alpha = (float)(rz / pq);
-        double u[2] = {0, 0};
+        // per-thread partial sums in FP32 (a handful of terms each), combined in FP64
+        float uf0 = 0.f, uf1 = 0.f;
         for (int i = gtid; i < n; i += gsz) {
             xc[i] += alpha * p[i];
             float ri = r[i] - alpha * q[i];
             r[i] = ri;
             float zi = dinv[i] * ri;
             z[i] = zi;
-            u[0] += (double)(ri * zi);
-            u[1] += (double)(ri * ri);
+            uf0 += ri * zi;
+            uf1 += ri * ri;
         }
+        double u[2] = {(double)uf0, (double)uf1};
         if (!grid_sum<2>(u, partial, sh, st)) return;
         it++;
         double rz_new = u[0];
         const double rn32 = sqrt(u[1]);
+        bool restart = false;
         if (rn32 <= delta * rmax || rn32 <= tol || it >= maxit) {
             // refinement: fold the FP32 correction into x, recompute b - A x in FP64
             for (int i = gtid; i < n; i += gsz) {
@@ -272,20 +295,30 @@ __global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr
             rn64 = sqrt(t[0]);
             conv = rn64 <= tol;
             if (conv || it >= maxit) break;
-            double y[2] = {0, 0};
+            // Keeping the FP32 search direction across a refinement is exact only
+            // while the FP32 matrix is a uniform rounding of the FP64 one; when the
+            // true residual stops falling (FP32 element matrices of nearly
+            // incompressible elasticity lose the soft modes to cancellation),
+            // restart the inner CG: classical iterative refinement.
+            restart = rn64 > 0.5 * prev_rn64;
+            stall = (rn64 > 0.9 * prev_rn64) ? stall + 1 : 0;
+            prev_rn64 = rn64;
+            if (stall >= 16) break;   // no progress: report NOT_CONVERGED
+            float yf0 = 0.f, yf1 = 0.f;
             for (int i = gtid; i < n; i += gsz) {
                 float ri = (float)r64[i];
                 float zi = dinv[i] * ri;
                 r[i] = ri;
                 z[i] = zi;
-                y[0] += (double)(ri * zi);
-                y[1] += (double)(ri * ri);
+                yf0 += ri * zi;
+                yf1 += ri * ri;
             }
+            double y[2] = {(double)yf0, (double)yf1};
             if (!grid_sum<2>(y, partial, sh, st)) return;
             rz_new = y[0];
             rmax = sqrt(y[1]);
         }
-        const float beta = (float)(rz_new / rz);
+        const float beta = restart ? 0.0f : (float)(rz_new / rz);
         rz = rz_new;
         for (int i = gtid; i < n; i += gsz) p[i] = z[i] + beta * p[i];
         if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;

@@ -727,3 +727,252 @@ int oracle_cg(int n, const long long *rp, const int *ci, const double *v, const 
     free(r); free(z); free(p); free(q); free(dinv);
     return it;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Bernardi-Raugel (H1BR{2}) with the RT0 reconstruction, 2D triangles       */
+/* ------------------------------------------------------------------------- */
+
+/* Local DoFs of a cell: 0-2 P1 component 1 (nodes), 3-5 P1 component 2,
+ * 6-8 face bubbles (src/fedefs/h1v_br.jl:33 "N1f1").  Scalar basis table:
+ * 0-2 P1 functions, 3-5 bubbles (:117-130).  Coefficients (:150-162):
+ * 1 for P1 DoFs, the global unit normal of face f for bubble f. */
+static void br_component_derivs(int dof, int c, int q, int nb, const double *derivs, double *d)
+{
+    int s;
+    if (dof < 3) s = (c == 0) ? dof : -1;
+    else if (dof < 6) s = (c == 1) ? dof - 3 : -1;
+    else s = 3 + (dof - 6);
+    for (int j = 0; j < 2; j++) d[j] = (s >= 0) ? derivs[(q * nb + s) * 2 + j] : 0.0;
+}
+
+static double br_coef(int dof, int c, const double *nrm /* [3][2] of the cell's faces */)
+{
+    if (dof < 6) return 1.0;
+    return nrm[(dof - 6) * 2 + c];
+}
+
+/* RT0 reconstruction coefficients R[9][3] of one cell
+ * (src/reconstructions.jl:381-403): R[(k)*3+node][f] = (1/2 |F|) n_F[k] for
+ * the two nodes of face f, R[6+f][f] = |F|. */
+static void br_rt0_coeffs(const double *fvol, const double *nrm, double R[9][3])
+{
+    memset(R, 0, sizeof(double) * 27);
+    for (int f = 0; f < 3; f++) {
+        int nodes[2] = {f, (f + 1) % 3};
+        for (int n = 0; n < 2; n++)
+            for (int k = 0; k < 2; k++) R[3 * k + nodes[n]][f] = (0.5 * fvol[f]) * nrm[f * 2 + k];
+        R[6 + f][f] = fvol[f];
+    }
+}
+
+typedef struct {
+    const double *coords; const int *cells; const int *cell_faces; const double *fnormals;
+    const double *fvolumes; const signed char *signs; const int *celldofs;
+} br_mesh;
+
+static void br_cell(const br_mesh *m, int cell, double X[6], double nrm[6], double fv[3], double sg[3])
+{
+    for (int v = 0; v < 3; v++)
+        for (int k = 0; k < 2; k++) X[v * 2 + k] = m->coords[(size_t)m->cells[(size_t)cell * 3 + v] * 2 + k];
+    for (int f = 0; f < 3; f++) {
+        int F = m->cell_faces[(size_t)cell * 3 + f];
+        nrm[f * 2] = m->fnormals[(size_t)F * 2];
+        nrm[f * 2 + 1] = m->fnormals[(size_t)F * 2 + 1];
+        fv[f] = m->fvolumes[F];
+        sg[f] = (double)m->signs[(size_t)cell * 3 + f];
+    }
+}
+
+/* nu (grad u, grad v) on H1BR{2} (LaplaceOperator, APT_SymmetricBilinearForm;
+ * Gradient with coefficients, src/feevaluator_h1.jl:77-94) plus
+ * lambda (div R u, div R v) (BilinearForm([ReconstructionDivergence{HDIVRT0{2}}]^2),
+ * APT_BilinearForm; src/feevaluator_h1.jl:409-437).  cellnu (optional)
+ * replaces nu by a per-cell action coefficient. */
+int oracle_br_assemble(void *h, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                       const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                       double nu, const double *cellnu, double lambda)
+{
+    omat *M = (omat *)h;
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(2, 2, xref, w); /* order 2(2-1) = 2 for both terms */
+    double vals[OR_MAXQ * 6], derivs[OR_MAXQ * 6 * 2];
+    /* scalar basis: P1 then bubbles, with ForwardDiff-ordered derivatives */
+    for (int q = 0; q < nq; q++) {
+        dual x[2] = {dvar(xref[3 * q], 0), dvar(xref[3 * q + 1], 1)};
+        dual r = dsub(dcsub(1.0, x[0]), x[1]);
+        dual o[6] = {r, x[0], x[1], dmul(dscale(6.0, x[0]), r), dmul(dscale(6.0, x[1]), x[0]), dmul(dscale(6.0, r), x[1])};
+        for (int a = 0; a < 6; a++) {
+            vals[q * 6 + a] = o[a].v;
+            derivs[(q * 6 + a) * 2] = o[a].d[0];
+            derivs[(q * 6 + a) * 2 + 1] = o[a].d[1];
+        }
+    }
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], nrm[6], fv[3], sg[3];
+        br_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(2, X, A, G, &det, &vol);
+        const int *dofs = &celldofs[(size_t)cell * 9];
+        /* Laplace with coefficients: cv[q][dof][k + 2c] */
+        double cv[OR_MAXQ][9][4];
+        for (int q = 0; q < nq; q++)
+            for (int dof = 0; dof < 9; dof++)
+                for (int c = 0; c < 2; c++)
+                    for (int k = 0; k < 2; k++) {
+                        double d[2], s = 0;
+                        br_component_derivs(dof, c, q, 6, derivs, d);
+                        for (int j = 0; j < 2; j++) s += G[k][j] * d[j];
+                        s *= br_coef(dof, c, nrm);
+                        cv[q][dof][k + 2 * c] = s;
+                    }
+        double loc[9][9];
+        memset(loc, 0, sizeof(loc));
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < 9; i++) {
+                double res[4];
+                for (int k = 0; k < 4; k++) res[k] = cellnu ? cellnu[cell] * cv[q][i][k] : cv[q][i][k];
+                for (int j = i; j < 9; j++) {
+                    double t = 0;
+                    for (int k = 0; k < 4; k++) t += res[k] * cv[q][j][k];
+                    loc[i][j] += w[q] * t;
+                }
+            }
+        double itemfactor = vol * (cellnu ? 1.0 : nu);
+        for (int i = 0; i < 9; i++)
+            for (int j = i + 1; j < 9; j++) {
+                omat_addnz(M, dofs[i], dofs[j], loc[i][j] * itemfactor, 1.0);
+                omat_addnz(M, dofs[j], dofs[i], loc[i][j] * itemfactor, 1.0);
+            }
+        for (int i = 0; i < 9; i++) omat_addnz(M, dofs[i], dofs[i], loc[i][i] * itemfactor, 1.0);
+        if (lambda == 0.0) continue;
+        /* reconstruction divergence, constant per cell but evaluated per qp */
+        double R[9][3];
+        br_rt0_coeffs(fv, nrm, R);
+        double dv[OR_MAXQ][9];
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < 9; i++) {
+                double s = 0;
+                for (int j = 0; j < 3; j++)
+                    if (R[i][j] != 0)
+                        for (int jd = 0; jd < 2; jd++) s += R[i][j] * 1.0 * sg[j];
+                s /= det;
+                dv[q][i] = s;
+            }
+        double lp[9][9];
+        memset(lp, 0, sizeof(lp));
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < 9; i++)
+                for (int j = 0; j < 9; j++) {
+                    double t = 0;
+                    t += dv[q][i] * dv[q][j];
+                    lp[i][j] += w[q] * t;
+                }
+        double pf = vol * lambda;
+        for (int i = 0; i < 9; i++)
+            for (int j = 0; j < 9; j++) omat_addnz(M, dofs[i], dofs[j], lp[i][j] * pf, 1.0);
+    }
+    return nq;
+}
+
+/* b += factor * (f, R v), f polynomial (RHS_POLY params, 2 components), with
+ * the ReconstructionIdentity{HDIVRT0{2}} test operator
+ * (src/feevaluator_h1.jl:342-381, src/assemblypatterns/linearform.jl:181-220);
+ * quadrature order polyorder(H1BR{2}) = 2 plus bonus. */
+int oracle_br_rhs(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                  const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                  const double *par, int npar, double factor, int bonus_quadorder)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(2, 2 + bonus_quadorder, xref, w);
+    if (nq < 0) nq = -nq;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], nrm[6], fv[3], sg[3];
+        br_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(2, X, A, G, &det, &vol);
+        double R[9][3];
+        br_rt0_coeffs(fv, nrm, R);
+        double locb[9] = {0};
+        for (int q = 0; q < nq; q++) {
+            double xi = xref[3 * q], eta = xref[3 * q + 1];
+            double rt[3][2] = {{xi, eta - 1}, {xi, eta}, {xi - 1, eta}};
+            double te[3][2];
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < 2; k++) {
+                    double s = 0;
+                    for (int l = 0; l < 2; l++) s += A[k][l] * rt[j][l];
+                    s *= sg[j] / det;
+                    te[j][k] = s;
+                }
+            double x[2], f[2];
+            for (int k = 0; k < 2; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 2; j++) x[k] += A[k][j] * xref[3 * q + j];
+            }
+            rhs_eval(OR_RHS_POLY, 2, 2, par, npar, cell, x, f);
+            for (int i = 0; i < 9; i++) {
+                double cv[2] = {0, 0};
+                for (int j = 0; j < 3; j++)
+                    if (R[i][j] != 0)
+                        for (int k = 0; k < 2; k++) cv[k] += R[i][j] * te[j][k];
+                double t = 0;
+                for (int k = 0; k < 2; k++) t += f[k] * cv[k];
+                locb[i] += t * w[q];
+            }
+        }
+        double itemfactor = factor * vol;
+        for (int i = 0; i < 9; i++) b[celldofs[(size_t)cell * 9 + i]] += locb[i] * itemfactor;
+    }
+    return nq;
+}
+
+/* Divergence of H1BR{2} functions with coefficients
+ * (src/feevaluator_h1.jl:133-145) at the midpoint: per cell
+ * divu[cell] = (1/|T|) int_T div u  (the rule of order 1 is exact), and
+ * b[dof] += int_T p_T div phi_dof  (the (p, div v) term of the velocity
+ * update, BilinearForm([Divergence, Identity]; factor = -1) moved to the
+ * right-hand side).  Either output may be NULL. */
+void oracle_br_div(int ncells, const double *coords, const int *cells, const int *cell_faces, const double *fnormals,
+                   const double *fvolumes, const signed char *signs, const int *celldofs, const double *u,
+                   const double *p, double *divu, double *b)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(2, 1, xref, w);
+    double derivs[OR_MAXQ * 6 * 2];
+    for (int q = 0; q < nq; q++) {
+        dual x[2] = {dvar(xref[3 * q], 0), dvar(xref[3 * q + 1], 1)};
+        dual r = dsub(dcsub(1.0, x[0]), x[1]);
+        dual o[6] = {r, x[0], x[1], dmul(dscale(6.0, x[0]), r), dmul(dscale(6.0, x[1]), x[0]), dmul(dscale(6.0, r), x[1])};
+        for (int a = 0; a < 6; a++) { derivs[(q * 6 + a) * 2] = o[a].d[0]; derivs[(q * 6 + a) * 2 + 1] = o[a].d[1]; }
+    }
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], nrm[6], fv[3], sg[3];
+        br_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(2, X, A, G, &det, &vol);
+        const int *dofs = &celldofs[(size_t)cell * 9];
+        double dint = 0;
+        double lb[9] = {0};
+        for (int q = 0; q < nq; q++) {
+            double dq = 0;
+            for (int dof = 0; dof < 9; dof++) {
+                double cv = 0;
+                for (int k = 0; k < 2; k++)
+                    for (int j = 0; j < 2; j++) {
+                        double d[2];
+                        br_component_derivs(dof, k, q, 6, derivs, d);
+                        cv += G[k][j] * d[j] * br_coef(dof, k, nrm);
+                    }
+                if (u) dq += u[dofs[dof]] * cv;
+                if (b && p) lb[dof] += (p[cell] * cv) * w[q];
+            }
+            dint += dq * w[q];
+        }
+        if (divu) divu[cell] = dint;
+        if (b && p)
+            for (int i = 0; i < 9; i++) b[dofs[i]] += lb[i] * vol;
+    }
+}

@@ -76,6 +76,13 @@ def lib():
         L.oracle_assemble_linear.restype = ctypes.c_int
         L.oracle_cg.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
         L.oracle_cg.restype = ctypes.c_int
+        sp = ctypes.POINTER(ctypes.c_byte)
+        brm = [ctypes.c_int, dp, ip, ip, dp, dp, sp, ip]
+        L.oracle_br_assemble.argtypes = [ctypes.c_void_p] + brm + [ctypes.c_double, dp, ctypes.c_double]
+        L.oracle_br_assemble.restype = ctypes.c_int
+        L.oracle_br_rhs.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.oracle_br_rhs.restype = ctypes.c_int
+        L.oracle_br_div.argtypes = brm + [dp, dp, dp, dp]
     return _lib
 
 

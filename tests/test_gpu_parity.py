@@ -5,7 +5,9 @@ Tolerances:
 * FP64 matrix values: per nonzero |a - o| <= 1e-12 * max(|o|, 1e-3 * max|o_row|)
   (1e-12 relative per nonzero; the floor covers entries that are sums of
   cancelling cell contributions, whose relative error is undefined);
-* FP32 matrix values: same form with 2e-6;
+* FP32 matrix values: row-scaled, |a - o| <= 2e-6 * max|o_row| (FP32 element
+  matrices round each cell contribution; cancelling contributions make a
+  per-entry relative bound meaningless at FP32);
 * FP64 right-hand side: max |b - o| <= 1e-12 * max |o|;
 * solutions: ||u - u_oracle||_2 / ||u_oracle||_2 <= 1e-10 for the FP64 and
   the mixed-precision solver, u_oracle from the sparse-direct FP64 solve of
@@ -47,13 +49,13 @@ def oracle_system(G, O, prob, penalty=True):
     return A0, M.csr(), b, O.penalized_rhs(b, prob.fixed)
 
 
-def check_values(Ag, Ao, tol):
+def check_values(Ag, Ao, tol, rowscaled=False):
     assert np.array_equal(Ag.indptr, Ao.indptr)
     assert np.array_equal(Ag.indices, Ao.indices)
     o = Ao.data
     rowmax = np.maximum.reduceat(np.abs(o), Ao.indptr[:-1])
     rm = np.repeat(rowmax, np.diff(Ao.indptr))
-    scale = np.maximum(np.abs(o), 1e-3 * rm)
+    scale = rm if rowscaled else np.maximum(np.abs(o), 1e-3 * rm)
     err = np.abs(Ag.data - o) / scale
     assert err.max() <= tol, f"max scaled error {err.max():.3e}"
     return err.max()
@@ -76,7 +78,7 @@ def test_pattern_and_values_parity(G, O, ctx, idx):
     G.assemble(A, prob.operators, G.FP64)
     check_values(A.download(G.FP64), A0, 1e-12)
     G.assemble(A, prob.operators, G.FP32)
-    check_values(A.download(G.FP32), A0, 2e-6)
+    check_values(A.download(G.FP32), A0, 2e-6, rowscaled=True)
     b = G.FEVector(ctx, prob.FES)
     G.assemble(b, prob.rhs)
     bg = b.entries
@@ -127,7 +129,7 @@ def test_solve_parity(G, O, ctx, idx, mode):
     _, Apen, _, bpen = oracle_system(G, O, prob)
     uo = O.solve_direct(Apen, bpen)
     sysd = P.DeviceSystem(ctx, prob, mixed=(mode == "mixed"))
-    st = sysd.assemble_and_solve(G.GB300PCG(mode=mode, reltol=1e-13, abstol=0.0))
+    st = sysd.assemble_and_solve(G.GB300PCG(mode=mode, reltol=1e-12, abstol=0.0))
     u = sysd.x.entries
     err = np.linalg.norm(u - uo) / np.linalg.norm(uo)
     assert err <= 1e-10, (err, st)
@@ -140,7 +142,7 @@ def test_solve_penalty_form_fp64(G, O, ctx):
     _, Apen, _, bpen = oracle_system(G, O, prob)
     uo = O.solve_direct(Apen, bpen)
     sysd = P.DeviceSystem(ctx, prob, mixed=False)
-    sysd.assemble_and_solve(G.GB300PCG(mode="fp64", reltol=1e-13, abstol=0.0), dirichlet=G.DIRICHLET_PENALTY)
+    sysd.assemble_and_solve(G.GB300PCG(mode="fp64", reltol=1e-12, abstol=0.0), dirichlet=G.DIRICHLET_PENALTY)
     u = sysd.x.entries
     assert np.linalg.norm(u - uo) / np.linalg.norm(uo) <= 1e-10
 
@@ -152,7 +154,7 @@ def test_config1_full_size_solve(G, O, ctx, mode):
     _, Apen, _, bpen = oracle_system(G, O, prob)
     uo = O.solve_direct(Apen, bpen)
     sysd = P.DeviceSystem(ctx, prob, mixed=(mode == "mixed"))
-    st = sysd.assemble_and_solve(G.GB300PCG(mode=mode, reltol=1e-13, abstol=0.0))
+    st = sysd.assemble_and_solve(G.GB300PCG(mode=mode, reltol=1e-12, abstol=0.0))
     u = sysd.x.entries
     err = np.linalg.norm(u - uo) / np.linalg.norm(uo)
     assert err <= 1e-10, (err, st)
