@@ -209,11 +209,65 @@ __global__ void __launch_bounds__(PTPB) k_pcg64(int n, const int32_t *rowptr, co
 }
 
 // ------------------------------------------------------------------ mixed PCG
+// FP32 SpMV fused with the search-direction update.  The preconditioned
+// residual z and the search direction p are stored interleaved (float2) and
+// double-buffered: `cur` holds (z_k, p_{k-1}), the SpMV gathers
+// p_k = z_k + beta p_{k-1} on the fly (one 8-byte load per nonzero, the same
+// fmaf everywhere so all readers see identical values), the owner of row r
+// stores p_k(r) into nxt[r].y, and phase B stores z_{k+1} into nxt[r].x.
+// This removes the separate p-update pass and one grid barrier per iteration.
 template <int TPR>
-__global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+__device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr,
+                                               const int32_t *__restrict__ cols, const float *__restrict__ vals,
+                                               const float2 *cur, float *nxt_f, float *q, float beta) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & (TPR - 1);
+    const int warp = gtid >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    constexpr int RPW = 32 / TPR;
+    constexpr int U = TPR >= 16 ? 2 : 4;
+    const int gin = (threadIdx.x & 31) / TPR;
+    float dacc = 0.f;
+    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
+        const int r = base + gin;
+        float s = 0.f;
+        if (r < n) {
+            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                float v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(cols + idx) : r;
+                    v[u] = ok ? __ldg(vals + idx) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const float2 g = cur[c[u]];
+                    s += v[u] * __fmaf_rn(beta, g.y, g.x);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (r < n && lane == 0) {
+            const float2 me = cur[r];
+            const float pn = __fmaf_rn(beta, me.y, me.x);
+            nxt_f[2 * r + 1] = pn;
+            q[r] = s;
+            dacc += pn * s;
+        }
+    }
+    return dacc;
+}
+
+template <int TPR>
+__global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
                                                     const double *vals64, const float *vals32, const double *b,
-                                                    double *x, const float *dinv, float *r, float *z, float *p,
-                                                    float *q, float *xc, double *r64, double *partial,
+                                                    double *x, const float *dinv, float *r, float *q, float *xc,
+                                                    float2 *zp0, float2 *zp1, double *r64, double *partial,
                                                     SolveState *st, double abstol, double reltol, double delta,
                                                     int maxit, int maxouter, int guess) {
     __shared__ double sh[32 * 4];
@@ -237,46 +291,49 @@ __global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr
     double rn64 = sqrt(v[0]);
     int it = 0, outer = 0;
     bool conv = rn64 <= tol;
-    // FP32 state from the FP64 residual
-    double w[2] = {0, 0};
+    // FP32 state from the FP64 residual; p_{-1} = 0
+    float wf0 = 0.f, wf1 = 0.f;
     for (int i = gtid; i < n; i += gsz) {
         float ri = (float)r64[i];
         float zi = dinv[i] * ri;
         r[i] = ri;
-        z[i] = zi;
-        p[i] = zi;
+        zp0[i] = make_float2(zi, 0.f);
         xc[i] = 0.0f;
-        w[0] += (double)(ri * zi);
-        w[1] += (double)(ri * ri);
+        wf0 += ri * zi;
+        wf1 += ri * ri;
     }
+    double w[2] = {(double)wf0, (double)wf1};
     if (!grid_sum<2>(w, partial, sh, st)) return;
     double rz = w[0];
     double rmax = sqrt(w[1]);
     double prev_rn64 = rn64;
     int stall = 0;
+    float beta = 0.f;
+    float2 *cur = zp0, *nxt = zp1;
     while (!conv && it < maxit && outer < maxouter) {
+        float *nxt_f = reinterpret_cast<float *>(nxt);
         double d[1];
-        d[0] = spmv_grid<TPR, float, float, float, true, false>(n, rowptr, cols, vals32, p, q, p, nullptr);
-        if (!grid_sum<1>(d, partial, sh, st)) return;
+        d[0] = (double)spmv_fused_zp<TPR>(n, rowptr, cols, vals32, cur, nxt_f, q, beta);
+        if (!grid_sum<1>(d, partial, sh, st)) return;   // barrier 1
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
             break;
         }
         const float alpha = (float)(rz / pq);
-        // per-thread partial sums in FP32 (a handful of terms each), combined in FP64
         float uf0 = 0.f, uf1 = 0.f;
         for (int i = gtid; i < n; i += gsz) {
-            xc[i] += alpha * p[i];
+            const float pi = nxt_f[2 * i + 1];
+            xc[i] += alpha * pi;
             float ri = r[i] - alpha * q[i];
             r[i] = ri;
             float zi = dinv[i] * ri;
-            z[i] = zi;
+            nxt_f[2 * i] = zi;
             uf0 += ri * zi;
             uf1 += ri * ri;
         }
         double u[2] = {(double)uf0, (double)uf1};
-        if (!grid_sum<2>(u, partial, sh, st)) return;
+        if (!grid_sum<2>(u, partial, sh, st)) return;   // barrier 2
         it++;
         double rz_new = u[0];
         const double rn32 = sqrt(u[1]);
@@ -309,7 +366,7 @@ __global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr
                 float ri = (float)r64[i];
                 float zi = dinv[i] * ri;
                 r[i] = ri;
-                z[i] = zi;
+                nxt_f[2 * i] = zi;
                 yf0 += ri * zi;
                 yf1 += ri * ri;
             }
@@ -318,10 +375,11 @@ __global__ void __launch_bounds__(PTPB) k_pcg_mixed(int n, const int32_t *rowptr
             rz_new = y[0];
             rmax = sqrt(y[1]);
         }
-        const float beta = restart ? 0.0f : (float)(rz_new / rz);
+        beta = restart ? 0.0f : (float)(rz_new / rz);
         rz = rz_new;
-        for (int i = gtid; i < n; i += gsz) p[i] = z[i] + beta * p[i];
-        if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+        float2 *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
     }
     if (gtid == 0) {
         st->iters = it;
@@ -475,8 +533,9 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     } else {
         auto kern = k_pcg_mixed<TPR>;
         grid = coop_grid(ctx, kern, n, p->grid_blocks);
-        float *dinv = (float *)work, *r = (float *)(work + lay.vec), *z = (float *)(work + 2 * lay.vec);
-        float *pp = (float *)(work + 3 * lay.vec), *q = (float *)(work + 4 * lay.vec), *xc = (float *)(work + 5 * lay.vec);
+        float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
+        float *xc = (float *)(work + 3 * lay.vec);
+        float2 *zp0 = (float2 *)(work + 4 * lay.vec), *zp1 = (float2 *)(work + 6 * lay.vec);
         double *r64 = (double *)(work + lay.off_r64);
         double *part = (double *)(work + lay.off_part);
         int nn = n, mi = p->maxiter, mo = p->max_outer > 0 ? p->max_outer : 1000;
@@ -485,7 +544,7 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
         const double *v64 = A->d_vals64, *bb = b->d;
         const float *v32 = A->d_vals32;
         double *xx = x->d;
-        void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &z, &pp, &q, &xc, &r64, &part, &dst,
+        void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
                         &at, &rt, &dl, &mi, &mo, &guess};
         cudaEventRecord(e0, ctx->stream);
         e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
@@ -529,7 +588,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     size_t pbytes = (size_t)4 * 8 * 4096;
     size_t vec = mixed ? al((size_t)n * 4) : al((size_t)n * 8);
-    size_t nvec = mixed ? 6 : 5;
+    size_t nvec = mixed ? 8 : 5;   // MIXED: dinv r q xc (float) + two interleaved (z, p) float2 buffers
     size_t off_r64 = nvec * vec;
     size_t off_part = off_r64 + (mixed ? al((size_t)n * 8) : 0);
     size_t off_state = off_part + al(pbytes);
@@ -562,9 +621,10 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
     int tpr = p->threads_per_row;
-    if (tpr <= 0) {
-        if (!A->tuned_tpr) A->tuned_tpr = autotune_tpr(A, mixed ? GRMP_FP32 : GRMP_FP64);
-        tpr = A->tuned_tpr;
+    if (tpr <= 0) {   // autotuned once per matrix and precision of the inner operator
+        int &slot = mixed ? A->tuned_tpr32 : A->tuned_tpr;
+        if (!slot) slot = autotune_tpr(A, mixed ? GRMP_FP32 : GRMP_FP64);
+        tpr = slot;
     }
     switch (tpr) {
         case 2: return launch_pcg<2>(A, b, x, p, st, work, dst, lay);
