@@ -39,20 +39,35 @@ class BilinearTerm(ctypes.Structure):
 class Rhs(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("ncomponents", ctypes.c_int), ("params", ctypes.POINTER(ctypes.c_double)),
                 ("nparams", ctypes.c_int64), ("factor", ctypes.c_double), ("bonus_quadorder", ctypes.c_int),
-                ("test_operator", ctypes.c_int)]
+                ("test_operator", ctypes.c_int), ("cell_group", ctypes.POINTER(ctypes.c_int32)),
+                ("ngroups", ctypes.c_int32)]
 
 
 class SolveParams(ctypes.Structure):
     _fields_ = [("abstol", ctypes.c_double), ("reltol", ctypes.c_double), ("maxiter", ctypes.c_int32),
                 ("mode", ctypes.c_int32), ("inner_reltol", ctypes.c_double), ("max_outer", ctypes.c_int32),
-                ("threads_per_row", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
+                ("spmv_chunk", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
                 ("use_initial_guess", ctypes.c_int32)]
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("iterations", ctypes.c_int32), ("outer_iterations", ctypes.c_int32),
-                ("threads_per_row", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
+                ("spmv_chunk", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
                 ("final_relres", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+
+
+class StokesBatchParams(ctypes.Structure):
+    _fields_ = [("nproblems", ctypes.c_int32), ("row_offsets", ctypes.POINTER(ctypes.c_int32)),
+                ("cell_offsets", ctypes.POINTER(ctypes.c_int32)), ("lam", ctypes.c_double),
+                ("sweeps", ctypes.c_int32), ("sweep_tol", ctypes.c_double), ("mode", ctypes.c_int32),
+                ("reltol", ctypes.c_double), ("inner_reltol", ctypes.c_double), ("maxiter", ctypes.c_int32),
+                ("block_threads", ctypes.c_int32)]
+
+
+class StokesBatchStats(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("max_iterations", ctypes.c_int32), ("total_iterations", ctypes.c_int64),
+                ("max_sweeps", ctypes.c_int32), ("failed_problems", ctypes.c_int32), ("max_relres", ctypes.c_double),
+                ("solve_ms", ctypes.c_double)]
 
 
 # every symbol of include/grmp.h with (argtypes, restype)
@@ -93,6 +108,8 @@ SIGNATURES = {
     "grmp_solve_params_default": ([ctypes.POINTER(SolveParams)], ctypes.c_int),
     "grmp_solve": ([_vp, _vp, _vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveStats)], ctypes.c_int),
     "grmp_spmv": ([_vp, ctypes.c_int, _vp, _vp], ctypes.c_int),
+    "grmp_stokes_batch_solve": ([_vp, _vp, _vp, _vp, ctypes.POINTER(StokesBatchParams), _pi32,
+                                 ctypes.POINTER(StokesBatchStats)], ctypes.c_int),
 }
 
 _lib = None

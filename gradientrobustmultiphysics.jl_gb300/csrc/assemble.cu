@@ -348,9 +348,17 @@ __global__ void k_dirichlet_rows(int32_t nrows, const int32_t *rowptr, const int
 }  // namespace
 
 // ---------------------------------------------------------------------- bilinear
+int grmp_br_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
+int grmp_br_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b);
+
 int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision) {
     grmp_space s = A->space;
     grmp_context ctx = s->mesh->ctx;
+    if (s->fe == GRMP_FE_H1BR) {
+        int rc = grmp_br_assemble(A, nterms, terms, precision);
+        if (!rc) A->eliminated = false;
+        return rc;
+    }
     int dim = s->mesh->dim, nb = s->nb, nc = s->ncomp;
     TermsDev td;
     std::vector<std::pair<void *, size_t>> keep;
@@ -437,6 +445,11 @@ int grmp_assemble_linear_impl(grmp_space s, const grmp_rhs *rhs, grmp_vector b) 
     grmp_context ctx = s->mesh->ctx;
     grmp_mesh m = s->mesh;
     int dim = m->dim;
+    if (s->fe == GRMP_FE_H1BR) {
+        if (rhs->test_operator != 1)
+            return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR right-hand sides use the RT0 reconstruction test operator");
+        return grmp_br_rhs(s, rhs, b);
+    }
     if (rhs->test_operator != 0) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "reconstruction test operator needs H1BR");
     if (s->fe != GRMP_FE_H1P1 && s->fe != GRMP_FE_H1P2)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "linear form on element %d", s->fe);

@@ -1,0 +1,579 @@
+// Batched iterated-penalty Stokes solver: many independent Bernardi-Raugel /
+// P0 problems, one thread block per problem, all in one launch.
+//
+// Reference: solve_fixpoint_subiterations! (src/solvers.jl:1018-1250) with
+// subiterations [[1],[2]] on the operators of
+// examples/Example221_StokesIterated2D.jl:80-90 (without the convection term):
+//   velocity update  (nu grad u, grad v) + lambda (div R u, div R v)
+//                      = (f, R v) + (p, div v)            [R: BR -> RT0]
+//   pressure update  (p_new, q) = (p, q) - lambda (div u, q)  on P0
+//   FixedIntegralMean(2, 0): the pressure has zero mean (src/globalconstraints.jl:23-44).
+// The velocity system is solved by Jacobi-PCG (FP64, or FP32 inside FP64
+// refinement) warm-started from the previous sweep's velocity.
+//
+// Scheduling: a persistent grid of blocks pulls problems from a work queue
+// sorted by size (largest first).  A problem never spans blocks, all its
+// reductions are block reductions in a fixed order, so its result does not
+// depend on which block runs it or on the rest of the batch.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "grmp_internal.h"
+
+int grmp_br_divergence(grmp_space s, double **Dv, double **vol);
+
+namespace {
+
+struct BatchDev {
+    int nprob;
+    const int32_t *order, *row_off, *cell_off;
+    const int32_t *rowptr, *cols;
+    const double *v64;
+    const float *v32;
+    const int32_t *inc_ptr, *inc_cell;
+    const uint8_t *inc_loc;
+    const int32_t *celldofs;
+    const double *Dv, *vol;
+    const uint8_t *fixed;
+    const double *bf;
+    double *u, *p;
+    // workspace (per row / per cell)
+    double *rhs, *r64, *dinv64, *w64a, *w64b, *w64c;
+    float *dinv32, *r32, *q32, *xc32;
+    float2 *zp0, *zp1;
+    int *queue;
+    int *iters, *sweeps_done, *status;
+    double *relres;
+    double lambda, sweep_tol, reltol, delta;
+    int sweeps, maxit, mixed;
+};
+
+template <int NV>
+__device__ __forceinline__ void bsum(double *v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < NV; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < NV; k++) sh[wid * NV + k] = v[k];
+    __syncthreads();
+    for (int k = 0; k < NV; k++) {
+        double s = 0;
+        for (int w = 0; w < nw; w++) s += sh[w * NV + k];
+        v[k] = s;
+    }
+    __syncthreads();
+}
+
+// rows [r0, r1) of y = A x (or y = b - A x with RESID) by the block; returns
+// this thread's part of sum w.y (DOT) or of sum y^2 (RESID)
+template <int TPR, typename V, typename X, bool RESID>
+__device__ __forceinline__ double block_spmv(const BatchDev &d, int r0, int r1, const V *vals, const X *x, X *y,
+                                             const X *w, const double *b) {
+    constexpr int RPW = 32 / TPR;
+    constexpr int U = TPR >= 16 ? 2 : 4;
+    using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
+    const int lane = threadIdx.x & (TPR - 1), gin = (threadIdx.x & 31) / TPR;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    double dot = 0;
+    for (int base = r0 + warp * RPW; base < r1; base += nwarps * RPW) {
+        const int r = base + gin;
+        A s = 0;
+        if (r < r1) {
+            const int kb = __ldg(d.rowptr + r), e = __ldg(d.rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                A v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(d.cols + idx) : r;
+                    v[u] = ok ? (A)__ldg(vals + idx) : A(0);
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) s += v[u] * (A)x[c[u]];
+            }
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (r < r1 && lane == 0) {
+            if (RESID) {
+                const double v = b[r] - (double)s;
+                y[r] = (X)v;
+                dot += v * v;
+            } else {
+                y[r] = (X)s;
+                if (w) dot += (double)w[r] * (double)s;
+            }
+        }
+    }
+    return dot;
+}
+
+template <int TPR>
+__device__ __forceinline__ float block_spmv_zp(const BatchDev &d, int r0, int r1, const float2 *cur, float *nxt_f,
+                                               float *q, float beta) {
+    constexpr int RPW = 32 / TPR;
+    constexpr int U = TPR >= 16 ? 2 : 4;
+    const int lane = threadIdx.x & (TPR - 1), gin = (threadIdx.x & 31) / TPR;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    float dacc = 0.f;
+    for (int base = r0 + warp * RPW; base < r1; base += nwarps * RPW) {
+        const int r = base + gin;
+        float s = 0.f;
+        if (r < r1) {
+            const int kb = __ldg(d.rowptr + r), e = __ldg(d.rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                float v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(d.cols + idx) : r;
+                    v[u] = ok ? __ldg(d.v32 + idx) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const float2 g = cur[c[u]];
+                    s += v[u] * __fmaf_rn(beta, g.y, g.x);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (r < r1 && lane == 0) {
+            const float2 me = cur[r];
+            const float pn = __fmaf_rn(beta, me.y, me.x);
+            nxt_f[2 * r + 1] = pn;
+            q[r] = s;
+            dacc += pn * s;
+        }
+    }
+    return dacc;
+}
+
+// FP32 Jacobi-PCG inside FP64 refinement on rows [r0, r1); x (FP64) holds the
+// initial guess and the result.  Returns iterations; *relres = final FP64
+// relative residual; *ok = converged.
+template <int TPR>
+__device__ int block_pcg_mixed(const BatchDev &d, int r0, int r1, const double *rhs, double *x, double *sh,
+                               double *relres, bool *ok) {
+    const int tid = threadIdx.x, bs = blockDim.x;
+    double v[2] = {0, 0};
+    v[0] = block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, x, d.r64, nullptr, rhs);
+    for (int i = r0 + tid; i < r1; i += bs) v[1] += rhs[i] * rhs[i];
+    bsum<2>(v, sh);
+    const double bn = sqrt(v[1]);
+    const double tol = d.reltol * bn;
+    double rn64 = sqrt(v[0]);
+    bool conv = rn64 <= tol || bn == 0.0;
+    int it = 0;
+    float wf0 = 0.f, wf1 = 0.f;
+    for (int i = r0 + tid; i < r1; i += bs) {
+        const float ri = (float)d.r64[i];
+        const float zi = d.dinv32[i] * ri;
+        d.r32[i] = ri;
+        d.zp0[i] = make_float2(zi, 0.f);
+        d.xc32[i] = 0.f;
+        wf0 += ri * zi;
+        wf1 += ri * ri;
+    }
+    double w[2] = {(double)wf0, (double)wf1};
+    bsum<2>(w, sh);
+    double rz = w[0], rmax = sqrt(w[1]), prev = rn64;
+    int stall = 0;
+    float beta = 0.f;
+    float2 *cur = d.zp0, *nxt = d.zp1;
+    while (!conv && it < d.maxit) {
+        float *nxt_f = reinterpret_cast<float *>(nxt);
+        double pq[1] = {(double)block_spmv_zp<TPR>(d, r0, r1, cur, nxt_f, d.q32, beta)};
+        bsum<1>(pq, sh);
+        if (!(pq[0] > 0) || !isfinite(pq[0])) break;
+        const float alpha = (float)(rz / pq[0]);
+        float u0 = 0.f, u1 = 0.f;
+        for (int i = r0 + tid; i < r1; i += bs) {
+            const float pi = nxt_f[2 * i + 1];
+            d.xc32[i] += alpha * pi;
+            const float ri = d.r32[i] - alpha * d.q32[i];
+            d.r32[i] = ri;
+            const float zi = d.dinv32[i] * ri;
+            nxt_f[2 * i] = zi;
+            u0 += ri * zi;
+            u1 += ri * ri;
+        }
+        double u[2] = {(double)u0, (double)u1};
+        bsum<2>(u, sh);
+        it++;
+        double rz_new = u[0];
+        const double rn32 = sqrt(u[1]);
+        bool restart = false;
+        if (rn32 <= d.delta * rmax || rn32 <= tol || it >= d.maxit) {
+            for (int i = r0 + tid; i < r1; i += bs) {
+                x[i] += (double)d.xc32[i];
+                d.xc32[i] = 0.f;
+            }
+            __syncthreads();
+            double t[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, x, d.r64, nullptr, rhs)};
+            bsum<1>(t, sh);
+            rn64 = sqrt(t[0]);
+            conv = rn64 <= tol;
+            if (conv || it >= d.maxit) break;
+            restart = rn64 > 0.5 * prev;
+            stall = rn64 > 0.9 * prev ? stall + 1 : 0;
+            prev = rn64;
+            if (stall >= 16) break;
+            float y0 = 0.f, y1 = 0.f;
+            for (int i = r0 + tid; i < r1; i += bs) {
+                const float ri = (float)d.r64[i];
+                const float zi = d.dinv32[i] * ri;
+                d.r32[i] = ri;
+                nxt_f[2 * i] = zi;
+                y0 += ri * zi;
+                y1 += ri * ri;
+            }
+            double y[2] = {(double)y0, (double)y1};
+            bsum<2>(y, sh);
+            rz_new = y[0];
+            rmax = sqrt(y[1]);
+        }
+        beta = restart ? 0.f : (float)(rz_new / rz);
+        rz = rz_new;
+        float2 *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    *relres = bn > 0 ? rn64 / bn : 0.0;
+    *ok = conv;
+    return it;
+}
+
+// Plain FP64 Jacobi-PCG on rows [r0, r1); w64a = z, w64b = p, w64c = q.
+template <int TPR>
+__device__ int block_pcg64(const BatchDev &d, int r0, int r1, const double *rhs, double *x, double *sh,
+                           double *relres, bool *ok) {
+    const int tid = threadIdx.x, bs = blockDim.x;
+    double *z = d.w64a, *p = d.w64b, *q = d.w64c, *r = d.r64;
+    double v[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, x, r, nullptr, rhs)};
+    bsum<1>(v, sh);
+    double w[3] = {0, 0, 0};
+    for (int i = r0 + tid; i < r1; i += bs) {
+        const double zi = d.dinv64[i] * r[i];
+        z[i] = zi;
+        p[i] = zi;
+        w[0] += r[i] * zi;
+        w[1] += r[i] * r[i];
+        w[2] += rhs[i] * rhs[i];
+    }
+    bsum<3>(w, sh);
+    const double bn = sqrt(w[2]), tol = d.reltol * bn;
+    double rz = w[0], rr = w[1];
+    bool conv = sqrt(rr) <= tol || bn == 0.0;
+    int it = 0;
+    while (!conv && it < d.maxit) {
+        double pq[1] = {block_spmv<TPR, double, double, false>(d, r0, r1, d.v64, p, q, p, nullptr)};
+        bsum<1>(pq, sh);
+        if (!(pq[0] > 0) || !isfinite(pq[0])) break;
+        const double alpha = rz / pq[0];
+        double u[2] = {0, 0};
+        for (int i = r0 + tid; i < r1; i += bs) {
+            x[i] += alpha * p[i];
+            const double ri = r[i] - alpha * q[i];
+            r[i] = ri;
+            const double zi = d.dinv64[i] * ri;
+            z[i] = zi;
+            u[0] += ri * zi;
+            u[1] += ri * ri;
+        }
+        bsum<2>(u, sh);
+        it++;
+        rr = u[1];
+        conv = sqrt(rr) <= tol;
+        if (conv) break;
+        const double beta = u[0] / rz;
+        rz = u[0];
+        for (int i = r0 + tid; i < r1; i += bs) p[i] = z[i] + beta * p[i];
+        __syncthreads();
+    }
+    *relres = bn > 0 ? sqrt(rr) / bn : 0.0;
+    *ok = conv;
+    return it;
+}
+
+template <int TPR>
+__global__ void __launch_bounds__(512) k_stokes_batch(BatchDev d) {
+    __shared__ double sh[32 * 4];
+    __shared__ int slot;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    while (true) {
+        if (tid == 0) slot = atomicAdd(d.queue, 1);
+        __syncthreads();
+        const int k = slot;
+        __syncthreads();
+        if (k >= d.nprob) break;
+        const int pid = d.order[k];
+        const int r0 = d.row_off[pid], r1 = d.row_off[pid + 1];
+        const int c0 = d.cell_off[pid], c1 = d.cell_off[pid + 1];
+        // Jacobi diagonal, zero initial state
+        for (int i = r0 + tid; i < r1; i += bs) {
+            double dg = 1.0;
+            for (int kk = d.rowptr[i]; kk < d.rowptr[i + 1]; kk++)
+                if (d.cols[kk] == i) dg = d.v64[kk];
+            d.dinv64[i] = 1.0 / dg;
+            if (d.mixed) {
+                float df = 1.f;
+                for (int kk = d.rowptr[i]; kk < d.rowptr[i + 1]; kk++)
+                    if (d.cols[kk] == i) df = d.v32[kk];
+                d.dinv32[i] = 1.f / df;
+            }
+            d.u[i] = 0.0;
+        }
+        for (int c = c0 + tid; c < c1; c += bs) d.p[c] = 0.0;
+        __syncthreads();
+        int total_it = 0, sweep = 0;
+        double worst = 0.0;
+        bool all_ok = true;
+        for (sweep = 0; sweep < d.sweeps; sweep++) {
+            // rhs = (f, R v) + (p, div v) on the free rows
+            for (int i = r0 + tid; i < r1; i += bs) {
+                double acc = d.bf[i];
+                if (!d.fixed[i])
+                    for (int q = d.inc_ptr[i]; q < d.inc_ptr[i + 1]; q++) {
+                        const int cell = d.inc_cell[q];
+                        acc += d.Dv[(size_t)cell * 9 + d.inc_loc[q]] * d.p[cell];
+                    }
+                d.rhs[i] = acc;
+            }
+            __syncthreads();
+            double rr;
+            bool ok;
+            const int it = d.mixed ? block_pcg_mixed<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok)
+                                   : block_pcg64<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok);
+            total_it += it;
+            worst = fmax(worst, rr);
+            all_ok = all_ok && ok;
+            __syncthreads();
+            // pressure update and zero mean
+            double m[3] = {0, 0, 0};   // sum vol*p_new, sum vol, sum (dp)^2 vol
+            for (int c = c0 + tid; c < c1; c += bs) {
+                double dv = 0;
+                for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
+                const double dp = d.lambda * dv / d.vol[c];
+                const double pn = d.p[c] - dp;
+                d.p[c] = pn;
+                m[0] += d.vol[c] * pn;
+                m[1] += d.vol[c];
+            }
+            bsum<2>(m, sh);
+            const double mean = m[0] / m[1];
+            double cmp[2] = {0, 0};
+            for (int c = c0 + tid; c < c1; c += bs) {
+                const double pn = d.p[c] - mean;
+                d.p[c] = pn;
+                cmp[1] += d.vol[c] * pn * pn;
+            }
+            // change of the pressure in this sweep (after the mean shift) from the divergence
+            for (int c = c0 + tid; c < c1; c += bs) {
+                double dv = 0;
+                for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
+                const double dp = d.lambda * dv / d.vol[c];
+                cmp[0] += d.vol[c] * dp * dp;
+            }
+            bsum<2>(cmp, sh);
+            if (d.sweep_tol > 0 && sqrt(cmp[0]) <= d.sweep_tol * sqrt(cmp[1])) {
+                sweep++;
+                break;
+            }
+        }
+        if (tid == 0) {
+            d.iters[pid] = total_it;
+            d.sweeps_done[pid] = sweep;
+            d.relres[pid] = worst;
+            d.status[pid] = all_ok ? 0 : (int)GRMP_ERR_NOT_CONVERGED;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_check_blocks(int nprob, const int32_t *row_off, const int32_t *rowptr, const int32_t *cols,
+                               int *bad) {
+    int pid = blockIdx.x;
+    if (pid >= nprob) return;
+    const int r0 = row_off[pid], r1 = row_off[pid + 1];
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++)
+            if (cols[k] < r0 || cols[k] >= r1) atomicExch(bad, 1);
+}
+
+}  // namespace
+
+extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vector u, grmp_vector p,
+                                       const grmp_stokes_batch_params *prm, int32_t *iters_out,
+                                       grmp_stokes_batch_stats *stats) {
+    if (!A || !bf || !u || !p || !prm || !stats) return GRMP_ERR_INVALID_ARG;
+    grmp_space s = A->space;
+    grmp_mesh m = s->mesh;
+    grmp_context ctx = m->ctx;
+    std::memset(stats, 0, sizeof(*stats));
+    cudaSetDevice(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int np = prm->nproblems;
+    if (s->fe != GRMP_FE_H1BR) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batched Stokes needs an H1BR space");
+    if (np <= 0 || !prm->row_offsets || !prm->cell_offsets) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: offsets");
+    if (prm->row_offsets[0] != 0 || prm->row_offsets[np] != A->nrows || prm->cell_offsets[0] != 0 ||
+        prm->cell_offsets[np] != m->ncells)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: offsets must cover all rows and cells");
+    for (int k = 0; k < np; k++)
+        if (prm->row_offsets[k + 1] <= prm->row_offsets[k] || prm->cell_offsets[k + 1] <= prm->cell_offsets[k])
+            return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: empty or decreasing problem range");
+    if (bf->n != A->nrows || u->n != A->nrows || p->n != m->ncells)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: vector sizes");
+    if (!A->has64 || (prm->mode == GRMP_SOLVE_MIXED && !A->has32) || !A->d_fixed || !A->eliminated)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: assemble FP64 (and FP32 for MIXED) and eliminate Dirichlet rows first");
+    if (prm->sweeps <= 0 || prm->maxiter <= 0 || !(prm->reltol > 0))
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: sweeps, maxiter and reltol must be positive");
+    const int n = A->nrows, nc = m->ncells;
+    // problem order: largest first (longest processing time first)
+    std::vector<int32_t> order(np);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return prm->row_offsets[a + 1] - prm->row_offsets[a] > prm->row_offsets[b + 1] - prm->row_offsets[b];
+    });
+    // device buffers
+    std::vector<std::pair<void *, size_t>> bufs;
+    auto take = [&](size_t bytes) -> void * {
+        void *q = nullptr;
+        if (grmp_alloc(ctx, &q, bytes)) return nullptr;
+        bufs.push_back({q, bytes});
+        return q;
+    };
+    auto release = [&]() {
+        for (auto &b : bufs) grmp_free(ctx, b.first, b.second);
+        bufs.clear();
+    };
+    BatchDev d;
+    std::memset(&d, 0, sizeof(d));
+    int32_t *dorder = (int32_t *)take((size_t)np * 4), *drow = (int32_t *)take((size_t)(np + 1) * 4);
+    int32_t *dcell = (int32_t *)take((size_t)(np + 1) * 4);
+    d.rhs = (double *)take((size_t)n * 8);
+    d.r64 = (double *)take((size_t)n * 8);
+    d.dinv64 = (double *)take((size_t)n * 8);
+    d.w64a = (double *)take((size_t)n * 8);
+    d.w64b = (double *)take((size_t)n * 8);
+    d.w64c = (double *)take((size_t)n * 8);
+    d.dinv32 = (float *)take((size_t)n * 4);
+    d.r32 = (float *)take((size_t)n * 4);
+    d.q32 = (float *)take((size_t)n * 4);
+    d.xc32 = (float *)take((size_t)n * 4);
+    d.zp0 = (float2 *)take((size_t)n * 8);
+    d.zp1 = (float2 *)take((size_t)n * 8);
+    d.queue = (int *)take(64);
+    d.iters = (int *)take((size_t)np * 4);
+    d.sweeps_done = (int *)take((size_t)np * 4);
+    d.status = (int *)take((size_t)np * 4);
+    d.relres = (double *)take((size_t)np * 8);
+    int *bad = (int *)take(4);
+    double *Dv = nullptr, *vol = nullptr;
+    bool okalloc = dorder && drow && dcell && d.rhs && d.r64 && d.dinv64 && d.w64a && d.w64b && d.w64c && d.dinv32 &&
+                   d.r32 && d.q32 && d.xc32 && d.zp0 && d.zp1 && d.queue && d.iters && d.sweeps_done && d.status &&
+                   d.relres && bad;
+    int rc = okalloc ? GRMP_OK : GRMP_ERR_OUT_OF_MEMORY;
+    if (!rc) rc = grmp_br_divergence(s, &Dv, &vol);
+    if (rc) {
+        release();
+        grmp_free(ctx, Dv, (size_t)nc * 72);
+        grmp_free(ctx, vol, (size_t)nc * 8);
+        return rc;
+    }
+    cudaMemcpyAsync(dorder, order.data(), (size_t)np * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(drow, prm->row_offsets, (size_t)(np + 1) * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dcell, prm->cell_offsets, (size_t)(np + 1) * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(d.queue, 0, 64, ctx->stream);
+    cudaMemsetAsync(bad, 0, 4, ctx->stream);
+    // the problems must not couple (block-diagonal system)
+    k_check_blocks<<<np, 128, 0, ctx->stream>>>(np, drow, A->d_rowptr, A->d_cols, bad);
+    GRMP_LAUNCHED(ctx);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess || hbad) {
+        release();
+        grmp_free(ctx, Dv, (size_t)nc * 72);
+        grmp_free(ctx, vol, (size_t)nc * 8);
+        return e != cudaSuccess ? grmp_cuda_fail(ctx, e, "batch check")
+                                : grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: a row couples two problems");
+    }
+    d.nprob = np;
+    d.order = dorder;
+    d.row_off = drow;
+    d.cell_off = dcell;
+    d.rowptr = A->d_rowptr;
+    d.cols = A->d_cols;
+    d.v64 = A->d_vals64;
+    d.v32 = A->d_vals32;
+    d.inc_ptr = s->d_inc_ptr;
+    d.inc_cell = s->d_inc_cell;
+    d.inc_loc = s->d_inc_loc;
+    d.celldofs = s->d_celldofs;
+    d.Dv = Dv;
+    d.vol = vol;
+    d.fixed = A->d_fixed;
+    d.bf = bf->d;
+    d.u = u->d;
+    d.p = p->d;
+    d.lambda = prm->lambda;
+    d.sweep_tol = prm->sweep_tol;
+    d.reltol = prm->reltol;
+    d.delta = prm->inner_reltol > 0 && prm->inner_reltol < 1 ? prm->inner_reltol : 0.1;
+    d.sweeps = prm->sweeps;
+    d.maxit = prm->maxiter;
+    d.mixed = prm->mode == GRMP_SOLVE_MIXED ? 1 : 0;
+    int threads = prm->block_threads > 0 ? prm->block_threads : 512;
+    threads = std::max(64, std::min(512, threads / 32 * 32));
+    // lanes per row from the average row length
+    double avg = (double)A->nnz / std::max(1, n);
+    int tpr = avg <= 6 ? 4 : (avg <= 14 ? 8 : 16);
+    int per_sm = 0;
+    auto kern = tpr == 4 ? k_stokes_batch<4> : (tpr == 8 ? k_stokes_batch<8> : k_stokes_batch<16>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
+    int grid = std::max(1, std::min(np, std::max(1, per_sm) * ctx->num_sms));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    kern<<<grid, threads, 0, ctx->stream>>>(d);
+    GRMP_LAUNCHED(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    std::vector<int> it(np), sw(np), st(np);
+    std::vector<double> rr(np);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(it.data(), d.iters, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sw.data(), d.sweeps_done, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st.data(), d.status, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rr.data(), d.relres, (size_t)np * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    release();
+    grmp_free(ctx, Dv, (size_t)nc * 72);
+    grmp_free(ctx, vol, (size_t)nc * 8);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "batched Stokes");
+    stats->solve_ms = ms;
+    for (int k = 0; k < np; k++) {
+        stats->total_iterations += it[k];
+        stats->max_iterations = std::max(stats->max_iterations, it[k]);
+        stats->max_sweeps = std::max(stats->max_sweeps, sw[k]);
+        stats->max_relres = std::max(stats->max_relres, rr[k]);
+        if (st[k]) stats->failed_problems++;
+    }
+    if (iters_out) std::memcpy(iters_out, it.data(), (size_t)np * 4);
+    stats->status = stats->failed_problems ? GRMP_ERR_NOT_CONVERGED : GRMP_OK;
+    if (stats->status)
+        return grmp_fail(ctx, stats->status, "batch: %d of %d problems hit the iteration cap (worst relres %.2e)",
+                         stats->failed_problems, np, stats->max_relres);
+    return GRMP_OK;
+}

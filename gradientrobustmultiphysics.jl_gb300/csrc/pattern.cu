@@ -363,6 +363,8 @@ int grmp_build_incidence(grmp_space s) {
 }
 
 // ---------------------------------------------------------------------- terms
+int grmp_br_mask(grmp_space s, int nterms, const grmp_bilinear_term *terms, uint32_t *mask);
+
 // Host helper shared with assemble.cu: validate terms and upload the tables
 // they need.  Returns device tables in `keep` (freed by the caller).
 int grmp_prepare_terms(grmp_space s, int nterms, const grmp_bilinear_term *terms, TermsDev *td,
@@ -452,20 +454,27 @@ int grmp_pattern_build_impl(grmp_space s, int nterms, const grmp_bilinear_term *
     *out = nullptr;
     TermsDev td;
     std::vector<std::pair<void *, size_t>> keep;
-    int rc = grmp_prepare_terms(s, nterms, terms, &td, keep);
-    if (rc) {
-        grmp_release(ctx, keep);
-        return rc;
-    }
     size_t ncl = (size_t)s->mesh->ncells * ld;
     uint32_t *mask = nullptr;
-    rc = grmp_alloc(ctx, (void **)&mask, ncl * 4);
-    if (rc) {
-        grmp_release(ctx, keep);
-        return rc;
-    }
+    int rc = grmp_alloc(ctx, (void **)&mask, ncl * 4);
+    if (rc) return rc;
     bool launched = true;
-    if (dim == 2 && nb == 3 && nc == 1) launch_mask<2, 3, 1>(s, td, mask);
+    if (s->fe == GRMP_FE_H1BR) {
+        rc = grmp_br_mask(s, nterms, terms, mask);
+        if (rc) {
+            grmp_free(ctx, mask, ncl * 4);
+            return rc;
+        }
+    } else {
+        rc = grmp_prepare_terms(s, nterms, terms, &td, keep);
+        if (rc) {
+            grmp_free(ctx, mask, ncl * 4);
+            grmp_release(ctx, keep);
+            return rc;
+        }
+    }
+    if (s->fe == GRMP_FE_H1BR) launched = true;
+    else if (dim == 2 && nb == 3 && nc == 1) launch_mask<2, 3, 1>(s, td, mask);
     else if (dim == 2 && nb == 3 && nc == 2) launch_mask<2, 3, 2>(s, td, mask);
     else if (dim == 2 && nb == 6 && nc == 1) launch_mask<2, 6, 1>(s, td, mask);
     else if (dim == 2 && nb == 6 && nc == 2) launch_mask<2, 6, 2>(s, td, mask);

@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "grmp_internal.h"
+#include "spmv.cuh"
 
 namespace {
 
@@ -81,72 +82,46 @@ __device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh,
     return true;
 }
 
-// y = A x over the rows of this grid; groups of TPR lanes per row.  If DOT,
-// returns this thread's share of sum_r w[r]*y[r].  If RESID, y = b - A x.
-template <int TPR, typename V, typename X, typename Y, bool DOT, bool RESID>
+// y = A x over all rows with the warp-stream core (chunk CH).  If DOT,
+// returns this thread's share of sum_r w[r]*y[r]; if RESID, y = b - A x and
+// the share of sum_r y[r]^2.  `smem` holds 8 warps x CH accumulators.
+template <int CH, typename V, typename X, typename Y, bool DOT, bool RESID>
 __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
                                             const V *__restrict__ vals, const X *x, Y *y, const Y *w,
-                                            const double *b) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & (TPR - 1);
-    const int warp = gtid >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    constexpr int RPW = 32 / TPR;   // rows per warp per step
-    const int gin = (threadIdx.x & 31) / TPR;
-    // Each lane keeps U independent (col, val) loads and U gathers in
-    // flight per pass: the SpMV is bound by memory-level parallelism, not
-    // arithmetic.  The matrix is read-only for the whole solve (non-coherent
-    // path); x is written by other blocks between barriers (coherent loads).
-    constexpr int U = TPR >= 16 ? 2 : 4;
+                                            const double *b, void *smem) {
     using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
+    A *wb = reinterpret_cast<A *>(smem) + (threadIdx.x >> 5) * CH;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     double dot = 0;
     A dacc = 0;
-    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
-        int r = base + gin;
-        A s = 0;
-        if (r < n) {
-            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
-            for (int k = kb + lane; k < e; k += TPR * U) {
-                int c[U];
-                A v[U];
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int idx = k + u * TPR;
-                    const bool ok = idx < e;
-                    c[u] = ok ? __ldg(cols + idx) : r;
-                    v[u] = ok ? (A)__ldg(vals + idx) : A(0);
-                }
-#pragma unroll
-                for (int u = 0; u < U; u++) s += v[u] * (A)x[c[u]];
-            }
-        }
-#pragma unroll
-        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (r < n && lane == 0) {
+    spmv::warp_stream<CH, V, A>(
+        0, n, gw, nw, rowptr, cols, vals, wb, [&](int c) { return (A)x[c]; },
+        [&](int r, A s) {
             if (RESID) {
-                double v = b[r] - (double)s;
+                const double v = b[r] - (double)s;
                 y[r] = (Y)v;
                 if (DOT) dot += v * v;
             } else {
                 y[r] = (Y)s;
                 if (DOT) dacc += (A)w[r] * s;   // FP32 partial in the FP32 path
             }
-        }
-    }
+        });
     return dot + (double)dacc;
 }
 
 // ------------------------------------------------------------------ FP64 PCG
 template <int TPR>
-__global__ void __launch_bounds__(PTPB) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
+__global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
                                                 const double *vals, const double *b, double *x, const double *dinv,
                                                 double *r, double *z, double *p, double *q, double *partial,
                                                 SolveState *st, double abstol, double reltol, int maxit, int guess) {
     __shared__ double sh[32 * 4];
+    __shared__ __align__(16) double swb[8 * TPR];   // warp-stream accumulators (8 warps x chunk)
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // r = b - A x  (or b)
-    if (guess) spmv_grid<TPR, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    if (guess) spmv_grid<TPR, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b, swb);
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double v[3] = {0, 0, 0};
     for (int i = gtid; i < n; i += gsz) {
@@ -167,7 +142,7 @@ __global__ void __launch_bounds__(PTPB) k_pcg64(int n, const int32_t *rowptr, co
     bool conv = sqrt(rr) <= tol;
     while (!conv && it < maxit) {
         double d[1];
-        d[0] = spmv_grid<TPR, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
+        d[0] = spmv_grid<TPR, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr, swb);
         if (!grid_sum<1>(d, partial, sh, st)) return;
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -198,7 +173,7 @@ __global__ void __launch_bounds__(PTPB) k_pcg64(int n, const int32_t *rowptr, co
     // true residual in FP64
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double t[1];
-    t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b, swb);
     if (!grid_sum<1>(t, partial, sh, st)) return;
     if (gtid == 0) {
         st->iters = it;
@@ -216,50 +191,27 @@ __global__ void __launch_bounds__(PTPB) k_pcg64(int n, const int32_t *rowptr, co
 // fmaf everywhere so all readers see identical values), the owner of row r
 // stores p_k(r) into nxt[r].y, and phase B stores z_{k+1} into nxt[r].x.
 // This removes the separate p-update pass and one grid barrier per iteration.
-template <int TPR>
+template <int CH>
 __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr,
                                                const int32_t *__restrict__ cols, const float *__restrict__ vals,
-                                               const float2 *cur, float *nxt_f, float *q, float beta) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & (TPR - 1);
-    const int warp = gtid >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    constexpr int RPW = 32 / TPR;
-    constexpr int U = TPR >= 16 ? 2 : 4;
-    const int gin = (threadIdx.x & 31) / TPR;
+                                               const float2 *cur, float *nxt_f, float *q, float beta, void *smem) {
+    float *wb = reinterpret_cast<float *>(smem) + (threadIdx.x >> 5) * CH;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     float dacc = 0.f;
-    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
-        const int r = base + gin;
-        float s = 0.f;
-        if (r < n) {
-            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
-            for (int k = kb + lane; k < e; k += TPR * U) {
-                int c[U];
-                float v[U];
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int idx = k + u * TPR;
-                    const bool ok = idx < e;
-                    c[u] = ok ? __ldg(cols + idx) : r;
-                    v[u] = ok ? __ldg(vals + idx) : 0.f;
-                }
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const float2 g = cur[c[u]];
-                    s += v[u] * __fmaf_rn(beta, g.y, g.x);
-                }
-            }
-        }
-#pragma unroll
-        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (r < n && lane == 0) {
+    spmv::warp_stream<CH, float, float>(
+        0, n, gw, nw, rowptr, cols, vals, wb,
+        [&](int c) {
+            const float2 g = cur[c];
+            return __fmaf_rn(beta, g.y, g.x);
+        },
+        [&](int r, float s) {
             const float2 me = cur[r];
             const float pn = __fmaf_rn(beta, me.y, me.x);
             nxt_f[2 * r + 1] = pn;
             q[r] = s;
             dacc += pn * s;
-        }
-    }
+        });
     return dacc;
 }
 
@@ -271,12 +223,13 @@ __global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *row
                                                     SolveState *st, double abstol, double reltol, double delta,
                                                     int maxit, int maxouter, int guess) {
     __shared__ double sh[32 * 4];
+    __shared__ __align__(16) double swb[8 * TPR];   // warp-stream accumulators (8 warps x chunk)
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // FP64 residual of the initial guess
     double v[2] = {0, 0};
     if (guess) {
-        v[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+        v[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b, swb);
     } else {
         for (int i = gtid; i < n; i += gsz) {
             x[i] = 0.0;
@@ -313,7 +266,7 @@ __global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *row
     while (!conv && it < maxit && outer < maxouter) {
         float *nxt_f = reinterpret_cast<float *>(nxt);
         double d[1];
-        d[0] = (double)spmv_fused_zp<TPR>(n, rowptr, cols, vals32, cur, nxt_f, q, beta);
+        d[0] = (double)spmv_fused_zp<TPR>(n, rowptr, cols, vals32, cur, nxt_f, q, beta, swb);
         if (!grid_sum<1>(d, partial, sh, st)) return;   // barrier 1
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -346,7 +299,7 @@ __global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *row
             }
             if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
             double t[1];
-            t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+            t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b, swb);
             if (!grid_sum<1>(t, partial, sh, st)) return;
             outer++;
             rn64 = sqrt(t[0]);
@@ -408,7 +361,8 @@ __global__ void k_dinv(int n, const int32_t *rowptr, const int32_t *cols, const 
 template <int TPR, typename V, typename X>
 __global__ void __launch_bounds__(256) k_spmv(int n, const int32_t *rowptr, const int32_t *cols, const V *vals,
                                               const X *x, X *y) {
-    spmv_grid<TPR, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr);
+    __shared__ __align__(16) double swb[8 * TPR];
+    spmv_grid<TPR, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr, swb);
 }
 
 __global__ void k_f64_to_f32(const double *a, float *b, int n) {
@@ -421,25 +375,19 @@ __global__ void k_f32_to_f64v(const float *a, double *b, int n) {
 }
 
 template <typename V, typename X>
-void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, const int32_t *ci, const V *v, const X *x,
-                 X *y) {
-    switch (tpr) {
-        case 1: k_spmv<1, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        case 2: k_spmv<2, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        case 4: k_spmv<4, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        case 8: k_spmv<8, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        case 16: k_spmv<16, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        default: k_spmv<32, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+void launch_spmv(int chunk, int grid, cudaStream_t s, int n, const int32_t *rp, const int32_t *ci, const V *v,
+                 const X *x, X *y) {
+    switch (chunk) {
+        case 64: k_spmv<64, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 256: k_spmv<256, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        default: k_spmv<128, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
     }
 }
 
 int heuristic_tpr(grmp_matrix A) {
+    // warp-stream chunk: about one chunk per 8-row warp step
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
-    if (avg <= 3) return 2;
-    if (avg <= 6) return 4;
-    if (avg <= 14) return 8;
-    if (avg <= 40) return 16;
-    return 32;
+    return avg * 8 <= 96 ? 64 : (avg * 8 <= 192 ? 128 : 256);
 }
 
 // Autotuner: time the standalone SpMV for each lane count on this matrix
@@ -459,10 +407,9 @@ int autotune_tpr(grmp_matrix A, int precision) {
     cudaEventCreate(&e1);
     int best = heuristic_tpr(A);
     float bt = 1e30f;
-    const int cand[5] = {2, 4, 8, 16, 32};
+    const int cand[3] = {64, 128, 256};
     for (int c : cand) {
-        int rows_per_block = 256 / c;
-        int grid = std::min(nblk(n, rows_per_block), ctx->num_sms * 16);
+        int grid = std::min(nblk(n, 64), ctx->num_sms * 8);
         float tot = 0;
         for (int rep = 0; rep < 4; rep++) {
             cudaEventRecord(e0, ctx->stream);
@@ -563,7 +510,7 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     out->iterations = hs.iters;
     out->outer_iterations = hs.outer;
     out->final_relres = hs.relres;
-    out->threads_per_row = TPR;
+    out->spmv_chunk = TPR;
     out->grid_blocks = grid;
     out->solve_ms = ms;
     if (hs.status == GRMP_ERR_NOT_CONVERGED)
@@ -620,27 +567,25 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     grmp_free(ctx, bad, 4);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
-    int tpr = p->threads_per_row;
+    int tpr = p->spmv_chunk;
     if (tpr <= 0) {   // autotuned once per matrix and precision of the inner operator
         int &slot = mixed ? A->tuned_tpr32 : A->tuned_tpr;
         if (!slot) slot = autotune_tpr(A, mixed ? GRMP_FP32 : GRMP_FP64);
         tpr = slot;
     }
     switch (tpr) {
-        case 2: return launch_pcg<2>(A, b, x, p, st, work, dst, lay);
-        case 4: return launch_pcg<4>(A, b, x, p, st, work, dst, lay);
-        case 8: return launch_pcg<8>(A, b, x, p, st, work, dst, lay);
-        case 16: return launch_pcg<16>(A, b, x, p, st, work, dst, lay);
-        case 32: return launch_pcg<32>(A, b, x, p, st, work, dst, lay);
+        case 64: return launch_pcg<64>(A, b, x, p, st, work, dst, lay);
+        case 128: return launch_pcg<128>(A, b, x, p, st, work, dst, lay);
+        case 256: return launch_pcg<256>(A, b, x, p, st, work, dst, lay);
     }
-    return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "threads_per_row must be 2, 4, 8, 16 or 32");
+    return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_chunk must be 64, 128 or 256");
 }
 
 int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
     grmp_context ctx = A->space->mesh->ctx;
     int n = A->nrows;
     int tpr = A->tuned_tpr ? A->tuned_tpr : heuristic_tpr(A);
-    int grid = std::min(nblk(n, 256 / tpr), ctx->num_sms * 16);
+    int grid = std::min(nblk(n, 64), ctx->num_sms * 8);
     if (precision == GRMP_FP64) {
         if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv: no FP64 values");
         launch_spmv<double, double>(tpr, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals64, x->d, y->d);

@@ -188,6 +188,10 @@ typedef struct {
     int bonus_quadorder;    /* DataFunction bonus_quadorder                          */
     int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0}
                                (BR only, src/feevaluator_h1.jl:342-381)              */
+    const int32_t *cell_group; /* optional [ncells]: POLY data per cell group (one DataFunction
+                                  per independent problem of a batch); params then hold
+                                  [ngroups][nterms][5]                                 */
+    int32_t ngroups;
 } grmp_rhs;
 
 /* b += LinearForm(test_operator, f) over the space (src/assemblypatterns/
@@ -230,7 +234,7 @@ typedef struct {
     int32_t mode;           /* grmp_solve_mode                                           */
     double inner_reltol;    /* MIXED: residual reduction per refinement (reliable update) */
     int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
-    int32_t threads_per_row;/* SpMV lanes per row: 0 = autotuned                         */
+    int32_t spmv_chunk;     /* SpMV nonzeros streamed per warp pass (64/128/256): 0 = autotuned */
     int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
     int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
 } grmp_solve_params;
@@ -239,7 +243,7 @@ typedef struct {
     int32_t status;          /* grmp_status of the solve                     */
     int32_t iterations;      /* inner (or plain) iterations                  */
     int32_t outer_iterations;/* FP64 refinement steps (MIXED)                */
-    int32_t threads_per_row; /* SpMV configuration used                      */
+    int32_t spmv_chunk;      /* SpMV configuration used                      */
     int32_t grid_blocks;
     double final_relres;     /* ||b - A x|| / ||b|| in FP64 at exit          */
     double solve_ms;         /* device time of the solve                     */
@@ -259,6 +263,50 @@ int grmp_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
 /* y = A x in the given precision (diagnostic / residual check,
  * src/solvers.jl:664-668). */
 int grmp_spmv(grmp_matrix A, int precision, grmp_vector x, grmp_vector y);
+
+/* ------------------------------------------------- batched Stokes (BR/P0) */
+
+typedef struct {
+    int32_t nproblems;
+    const int32_t *row_offsets;  /* [nproblems+1] velocity rows of each problem (contiguous, disjoint) */
+    const int32_t *cell_offsets; /* [nproblems+1] cells (= P0 pressure DoFs) of each problem          */
+    double lambda;               /* iterated-penalty parameter                                        */
+    int32_t sweeps;              /* maximum iterated-penalty sweeps                                   */
+    double sweep_tol;            /* stop a problem when ||p_new - p|| <= sweep_tol ||p_new|| (0: all)  */
+    int32_t mode;                /* inner solver: GRMP_SOLVE_FP64 or GRMP_SOLVE_MIXED                 */
+    double reltol;               /* inner solve: ||rhs - A u|| <= reltol ||rhs|| per sweep             */
+    double inner_reltol;         /* MIXED: refinement trigger                                          */
+    int32_t maxiter;             /* inner iteration cap per sweep                                       */
+    int32_t block_threads;       /* threads per problem (0 = 512)                                       */
+} grmp_stokes_batch_params;
+
+typedef struct {
+    int32_t status;
+    int32_t max_iterations;      /* largest per-problem inner iteration total */
+    int64_t total_iterations;
+    int32_t max_sweeps;
+    int32_t failed_problems;     /* problems that hit a cap                   */
+    double max_relres;           /* worst final inner relative residual       */
+    double solve_ms;
+} grmp_stokes_batch_stats;
+
+/* Iterated-penalty Stokes solve of many independent Bernardi-Raugel / P0
+ * problems assembled into one block-diagonal system (the reference's
+ * solve_fixpoint_subiterations! with subiterations [[1],[2]],
+ * src/solvers.jl:1018-1250, on the operators of
+ * examples/Example221_StokesIterated2D.jl:80-90 without convection):
+ *   velocity:  (nu grad u, grad v) + lambda (div R u, div R v) = (f, R v) + (p, div v)
+ *   pressure:  p <- p - lambda * (1/|T|) int_T div u,  then mean(p) = 0
+ *              (FixedIntegralMean, src/globalconstraints.jl:23-44).
+ * A: the assembled velocity matrix over an H1BR space (terms LAPLACE and
+ * RDIVRDIV) with Dirichlet rows eliminated; bf: the reconstructed
+ * right-hand side (f, R v) with the same rows zeroed.  u (velocity, per row)
+ * and p (pressure, per cell) are overwritten.  One thread block owns one
+ * problem for the whole solve, so a problem's result is bit-identical alone
+ * and inside any batch.  iterations_per_problem (optional, [nproblems]). */
+int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vector u, grmp_vector p,
+                            const grmp_stokes_batch_params *params, int32_t *iterations_per_problem,
+                            grmp_stokes_batch_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -250,3 +250,82 @@ def solve_cg(A, b, reltol=1e-14, maxit=100000):
 
 if __name__ == "__main__":  # pragma: no cover - manual build helper
     print(build(force="--force" in sys.argv))
+
+
+# --------------------------------------------------------------------------
+# Bernardi-Raugel / P0 Stokes with the RT0 reconstruction (2D)
+# --------------------------------------------------------------------------
+
+def br_celldofs(nverts: int, cells: np.ndarray, cell_faces: np.ndarray):
+    """H1BR{2} cell DoFs, pattern "N1f1" (src/fedefs/h1v_br.jl:33) restated
+    from src/dofmaps.jl:201-330: component-1 nodes, component-2 nodes, faces."""
+    nf = int(cell_faces.max()) + 1
+    cd = np.concatenate([cells, cells + nverts, cell_faces + 2 * nverts], axis=1).astype(np.int32)
+    return np.ascontiguousarray(cd), 2 * nverts + nf
+
+
+def _br_args(g, cd):
+    fn, cf = g.faces()
+    nrm, fv, sg = g.face_geometry()
+    arrs = [np.ascontiguousarray(g.coords, dtype=np.float64), np.ascontiguousarray(g.cells, dtype=np.int32),
+            np.ascontiguousarray(cf, dtype=np.int32), np.ascontiguousarray(nrm, dtype=np.float64),
+            np.ascontiguousarray(fv, dtype=np.float64), np.ascontiguousarray(sg, dtype=np.int8),
+            np.ascontiguousarray(cd, dtype=np.int32)]
+    ptrs = [g.ncells, _dp(arrs[0]), _ip(arrs[1]), _ip(arrs[2]), _dp(arrs[3]), _dp(arrs[4]),
+            arrs[5].ctypes.data_as(ctypes.POINTER(ctypes.c_byte)), _ip(arrs[6])]
+    return arrs, ptrs
+
+
+def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, reconstruct: bool = True):
+    """(A (penalised), bf, fixed, celldofs) of the velocity update system:
+    nu (grad u, grad v) + lam (div R u, div R v) = (f, R v)."""
+    fn, cf = g.faces()
+    cd, nd = br_celldofs(g.nverts, g.cells, cf)
+    arrs, ptrs = _br_args(g, cd)
+    M = Matrix(nd)
+    lib().oracle_br_assemble(M.h, *ptrs, float(nu), None, float(lam))
+    bf = np.zeros(nd)
+    par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
+    lib().oracle_br_rhs(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder))
+    # homogeneous Dirichlet on all boundary faces: nodes (both components) and face bubbles
+    bf_ids = np.nonzero(np.bincount(cf.ravel(), minlength=fn.shape[0]) == 1)[0]
+    bnodes = np.unique(fn[bf_ids].ravel())
+    fixed = np.unique(np.concatenate([bnodes, bnodes + g.nverts, bf_ids + 2 * g.nverts])).astype(np.int32)
+    return M, bf, fixed, cd, (arrs, ptrs)
+
+
+def br_div(g, cd_args, u=None, p=None):
+    """(cell averages of div u, int p div phi as a vector)."""
+    arrs, ptrs = cd_args
+    nc = g.ncells
+    nd = int(arrs[6].max()) + 1
+    divu = np.zeros(nc) if u is not None else None
+    b = np.zeros(nd) if p is not None else None
+    uu = np.ascontiguousarray(u, dtype=np.float64) if u is not None else None
+    pp = np.ascontiguousarray(p, dtype=np.float64) if p is not None else None
+    lib().oracle_br_div(*ptrs, _dp(uu) if uu is not None else None, _dp(pp) if pp is not None else None,
+                        _dp(divu) if divu is not None else None, _dp(b) if b is not None else None)
+    return divu, b
+
+
+def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6):
+    """Iterated penalty (examples/Example221_StokesIterated2D.jl:61-95, no
+    convection): sparse-direct velocity solves of the penalised system,
+    P0 pressure update p <- p - lam * avg(div u), zero mean."""
+    import scipy.sparse.linalg as spla
+    M, bf, fixed, cd, args = br_stokes_system(g, nu, lam, terms)
+    M.penalize(fixed)
+    A = M.csr().tocsc()
+    lu = spla.splu(A)
+    vol = g.cell_volumes()
+    p = np.zeros(g.ncells)
+    u = None
+    for _ in range(sweeps):
+        _, bp = br_div(g, args, p=p)
+        b = bf + bp
+        b[fixed] = 0.0
+        u = lu.solve(b)
+        divu, _ = br_div(g, args, u=u)
+        p = p - lam * divu
+        p -= np.dot(vol, p) / vol.sum()
+    return u, p, fixed

@@ -1,0 +1,124 @@
+"""Bernardi-Raugel / P0 Stokes with the RT0 reconstruction (batched iterated penalty).
+
+CPU: the oracle reproduces the reference's pressure-robustness known answer
+(examples/Example222_PressureRobustness2D.jl:189-211, runtests.jl:684-723):
+a pure gradient force gives a zero discrete velocity with the reconstructed
+right-hand side.  GPU: pattern / matrix / rhs parity of the H1BR assembly,
+solution parity of the batched solver against the oracle's iterated penalty
+with sparse-direct solves, and bit-identical results alone and in a batch.
+"""
+import numpy as np
+import pytest
+
+
+def _poly_terms(rng):
+    from grmp_gb300 import stokes as S
+    return S.grad_plus_curl_terms(S.cubic_coefficients(rng), S.cubic_coefficients(rng))
+
+
+def test_oracle_hydrostatic_velocity_is_zero(G, O):
+    """f = grad(phi), phi = x^3 + y^3 - xy: the gradient-robust scheme gives
+    u_h = 0 and p_h = (cell means of phi) up to a constant."""
+    g = G.grid_unitsquare(6)
+    phi = {(3, 0): 1.0, (0, 3): 1.0, (1, 1): -1.0}
+    from grmp_gb300 import stokes as S
+    terms = S.grad_plus_curl_terms(phi, {})
+    for nu in (1.0, 1e-3):
+        u, p, _ = O.stokes_iterated_penalty(g, nu, 1e4, terms, sweeps=10)
+        assert np.max(np.abs(u)) < 1e-12, nu
+        # cell means of phi (order-6 rule is exact for cubics)
+        x, w, _ = O.qrule(2, 6)
+        X = g.coords[g.cells]
+        A = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))
+        pts = X[:, None, 0, :] + np.einsum("ckj,qj->cqk", A, x[:, :2])
+        ph = pts[..., 0] ** 3 + pts[..., 1] ** 3 - pts[..., 0] * pts[..., 1]
+        mean_phi = ph @ w
+        target = mean_phi - np.dot(g.cell_volumes(), mean_phi) / g.cell_volumes().sum()
+        assert np.max(np.abs(p - target)) < 1e-9 * np.max(np.abs(target)), nu
+
+
+def test_oracle_br_rhs_of_gradient_is_in_range_of_divergence(G, O):
+    """(grad phi, R v) = -(pi_0 phi, div v) for v vanishing on the boundary:
+    the reconstructed load of a gradient is annihilated by div-free
+    velocities -- the identity behind pressure robustness."""
+    g = G.grid_unitsquare(4)
+    from grmp_gb300 import stokes as S
+    phi = {(2, 1): 1.0, (0, 2): -2.0}
+    M, bf, fixed, cd, args = O.br_stokes_system(g, 1.0, 0.0, S.grad_plus_curl_terms(phi, {}))
+    x, w, _ = O.qrule(2, 6)
+    X = g.coords[g.cells]
+    A = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))
+    pts = X[:, None, 0, :] + np.einsum("ckj,qj->cqk", A, x[:, :2])
+    ph = pts[..., 0] ** 2 * pts[..., 1] - 2 * pts[..., 1] ** 2
+    _, bp = O.br_div(g, args, p=ph @ w)
+    free = np.setdiff1d(np.arange(bf.size), fixed)
+    assert np.max(np.abs(bf[free] + bp[free])) < 1e-13 * max(1.0, np.max(np.abs(bf)))
+
+
+def _small_batch(G, sizes, nus, seed=3):
+    from grmp_gb300 import stokes as S
+    return S.make_batch(sizes=np.array(sizes), nus=np.array(nus), seed=seed)
+
+
+@pytest.mark.gpu
+def test_br_assembly_parity(G, O, ctx):
+    from grmp_gb300 import stokes as S
+    prob = _small_batch(G, [7], [0.3])
+    sysd = S.StokesBatchSystem(ctx, prob, mixed=True)
+    g = prob.mesh.parts[0]
+    M, bf, fixed, cd, args = O.br_stokes_system(g, prob.nus[0], prob.lam, prob.terms[0])
+    A0 = M.csr()
+    rp, ci = sysd.A.pattern()
+    assert np.array_equal(rp, A0.indptr) and np.array_equal(ci, A0.indices)
+    api = __import__("grmp_gb300").api
+    api.assemble(sysd.A, sysd.ops, G.FP64)
+    Ag = sysd.A.download(G.FP64)
+    o = A0.data
+    rm = np.repeat(np.maximum.reduceat(np.abs(o), A0.indptr[:-1]), np.diff(A0.indptr))
+    assert np.max(np.abs(Ag.data - o) / np.maximum(np.abs(o), 1e-3 * rm)) <= 1e-12
+    sysd.assemble()
+    b = sysd.bf.entries
+    free = np.setdiff1d(np.arange(bf.size), fixed)
+    assert np.max(np.abs(b[free] - bf[free])) <= 1e-12 * np.max(np.abs(bf))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_batch_matches_oracle(G, O, ctx, mode):
+    from grmp_gb300 import stokes as S
+    sizes, nus = [5, 9, 6], [1.0, 0.2, 0.05]
+    prob = _small_batch(G, sizes, nus)
+    sysd = S.StokesBatchSystem(ctx, prob, mixed=(mode == "mixed"))
+    sysd.assemble()
+    st = sysd.solve(sweeps=8, reltol=1e-13 if mode == "fp64" else 1e-12)
+    u, p = sysd.velocity(), sysd.pressure()
+    for k, g in enumerate(prob.mesh.parts):
+        uo, po, _ = O.stokes_iterated_penalty(g, nus[k], prob.lam, prob.terms[k], sweeps=8)
+        r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
+        c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
+        eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
+        ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
+        assert eu < 1e-8 and ep < 1e-8, (k, eu, ep, st)
+
+
+@pytest.mark.gpu
+def test_batch_result_same_alone_and_in_the_mix(G, ctx):
+    """Each problem is owned by one thread block: its bits do not depend on
+    the other problems of the batch."""
+    from grmp_gb300 import stokes as S
+    sizes, nus = [6, 12, 4, 9], [1.0, 1e-2, 0.3, 1e-3]
+    big = _small_batch(G, sizes, nus, seed=11)
+    sb = S.StokesBatchSystem(ctx, big, mixed=True)
+    sb.assemble()
+    sb.solve(sweeps=5, reltol=1e-10)
+    u, p = sb.velocity(), sb.pressure()
+    k = 1
+    alone = S.make_batch(sizes=np.array([sizes[k]]), nus=np.array([nus[k]]), seed=11)
+    alone.terms = big.terms[k:k + 1].copy()
+    sa = S.StokesBatchSystem(ctx, alone, mixed=True)
+    sa.assemble()
+    sa.solve(sweeps=5, reltol=1e-10)
+    r0, r1 = big.V.row_offsets[k], big.V.row_offsets[k + 1]
+    c0, c1 = big.mesh.cell_offsets[k], big.mesh.cell_offsets[k + 1]
+    assert np.array_equal(sa.velocity(), u[r0:r1])
+    assert np.array_equal(sa.pressure(), p[c0:c1])
