@@ -362,7 +362,7 @@ def run_ours(args):
                            "iterations": plain["stats"][-1]["iterations"]},
             "mixed_vs_plain": value / plain_value,
             "solver": {"iterations": st_last["iterations"], "outer": st_last["outer_iterations"],
-                       "spmv_chunk": st_last["spmv_chunk"], "grid_blocks": st_last["grid_blocks"]},
+                       "spmv_config": st_last["spmv_config"], "grid_blocks": st_last["grid_blocks"]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "kernel": "k_pcg_mixed (persistent)",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"},

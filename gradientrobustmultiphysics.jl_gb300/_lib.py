@@ -46,13 +46,13 @@ class Rhs(ctypes.Structure):
 class SolveParams(ctypes.Structure):
     _fields_ = [("abstol", ctypes.c_double), ("reltol", ctypes.c_double), ("maxiter", ctypes.c_int32),
                 ("mode", ctypes.c_int32), ("inner_reltol", ctypes.c_double), ("max_outer", ctypes.c_int32),
-                ("spmv_chunk", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
+                ("spmv_config", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
                 ("use_initial_guess", ctypes.c_int32)]
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("iterations", ctypes.c_int32), ("outer_iterations", ctypes.c_int32),
-                ("spmv_chunk", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
+                ("spmv_config", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
                 ("final_relres", ctypes.c_double), ("solve_ms", ctypes.c_double)]
 
 
@@ -61,13 +61,28 @@ class StokesBatchParams(ctypes.Structure):
                 ("cell_offsets", ctypes.POINTER(ctypes.c_int32)), ("lam", ctypes.c_double),
                 ("sweeps", ctypes.c_int32), ("sweep_tol", ctypes.c_double), ("mode", ctypes.c_int32),
                 ("reltol", ctypes.c_double), ("inner_reltol", ctypes.c_double), ("maxiter", ctypes.c_int32),
-                ("block_threads", ctypes.c_int32)]
+                ("block_threads", ctypes.c_int32), ("split_penalty", ctypes.c_int32)]
 
 
 class StokesBatchStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("max_iterations", ctypes.c_int32), ("total_iterations", ctypes.c_int64),
                 ("max_sweeps", ctypes.c_int32), ("failed_problems", ctypes.c_int32), ("max_relres", ctypes.c_double),
-                ("solve_ms", ctypes.c_double)]
+                ("solve_ms", ctypes.c_double), ("fp64_fallbacks", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("nverts", ctypes.c_int32), ("coords", ctypes.POINTER(ctypes.c_double)),
+                ("ncells", ctypes.c_int32), ("cells", ctypes.POINTER(ctypes.c_int32)), ("fe_kind", ctypes.c_int),
+                ("ncomponents", ctypes.c_int), ("ndofs", ctypes.c_int32),
+                ("celldofs", ctypes.POINTER(ctypes.c_int32)), ("nterms", ctypes.c_int),
+                ("terms", ctypes.POINTER(BilinearTerm)), ("rhs", Rhs), ("nfixed", ctypes.c_int32),
+                ("fixed", ctypes.POINTER(ctypes.c_int32)), ("solve", SolveParams)]
+
+
+class RequestStats(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("slot", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("outer_iterations", ctypes.c_int32), ("final_relres", ctypes.c_double), ("queue_ms", ctypes.c_double),
+                ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("solve_ms", ctypes.c_double)]
 
 
 # every symbol of include/grmp.h with (argtypes, restype)
@@ -110,6 +125,10 @@ SIGNATURES = {
     "grmp_spmv": ([_vp, ctypes.c_int, _vp, _vp], ctypes.c_int),
     "grmp_stokes_batch_solve": ([_vp, _vp, _vp, _vp, ctypes.POINTER(StokesBatchParams), _pi32,
                                  ctypes.POINTER(StokesBatchStats)], ctypes.c_int),
+    "grmp_server_create": ([ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+    "grmp_server_submit": ([_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "grmp_server_wait": ([_vp, ctypes.c_int64, ctypes.c_double, _pd, ctypes.POINTER(RequestStats)], ctypes.c_int),
+    "grmp_server_destroy": ([_vp], ctypes.c_int),
 }
 
 _lib = None

@@ -420,7 +420,7 @@ class GB300PCG:
     maxiter: int = 100000
     inner_reltol: float = 0.1
     max_outer: int = 1000
-    spmv_chunk: int = 0
+    spmv_config: int = 0
     grid_blocks: int = 0
     use_initial_guess: bool = False
     last_stats: dict = field(default_factory=dict)
@@ -433,7 +433,7 @@ class GB300PCG:
         p.mode = L.SOLVE_MIXED if self.mode == "mixed" else L.SOLVE_FP64
         p.inner_reltol = self.inner_reltol
         p.max_outer = self.max_outer
-        p.spmv_chunk = self.spmv_chunk
+        p.spmv_config = self.spmv_config
         p.grid_blocks = self.grid_blocks
         p.use_initial_guess = 1 if self.use_initial_guess else 0
         return p
@@ -443,7 +443,7 @@ class GB300PCG:
         p = self.params()
         rc = A.ctx.lib.grmp_solve(A.h, b.h, x.h, ctypes.byref(p), ctypes.byref(st))
         self.last_stats = {"status": st.status, "iterations": st.iterations, "outer_iterations": st.outer_iterations,
-                           "spmv_chunk": st.spmv_chunk, "grid_blocks": st.grid_blocks,
+                           "spmv_config": st.spmv_config, "grid_blocks": st.grid_blocks,
                            "final_relres": st.final_relres, "solve_ms": st.solve_ms, "rc": rc}
         if raise_on_error:
             A.ctx.check(rc)

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgrmp_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cpp", "tables.cpp", "pattern.cu", "assemble.cu", "br.cu", "solve.cu", "batch.cu"]
+SOURCES = ["api.cpp", "tables.cpp", "server.cpp", "pattern.cu", "assemble.cu", "br.cu", "solve.cu", "batch.cu"]
 
 
 def nvcc() -> str:
@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
                 if verbose and out.strip():
                     print(out)
     if force or jobs or _stale(LIB, objs):
-        run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+        run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-Xcompiler", "-pthread"])
     return LIB
 
 

@@ -42,11 +42,13 @@ struct BatchDev {
     double *rhs, *r64, *dinv64, *w64a, *w64b, *w64c;
     float *dinv32, *r32, *q32, *xc32;
     float2 *zp0, *zp1;
+    // split-penalty inner operator (MIXED, split_penalty = 1)
+    float *z32, *p32, *s32, *Dv32, *w32;
     int *queue;
-    int *iters, *sweeps_done, *status;
+    int *iters, *sweeps_done, *status, *fallbacks;
     double *relres;
     double lambda, sweep_tol, reltol, delta;
-    int sweeps, maxit, mixed;
+    int sweeps, maxit, mixed, split;
 };
 
 template <int NV>
@@ -250,6 +252,152 @@ __device__ int block_pcg_mixed(const BatchDev &d, int r0, int r1, const double *
     return it;
 }
 
+// Inner FP32 operator with the penalty in factored form:
+//   q = L32 p + sum_T w_T D_T^T (D_T . p),   w_T = lambda / |T|,
+// L32 = FP32 values of (nu grad u, grad v) with Dirichlet rows eliminated,
+// D_T[I] = int_T div phi_I with the entries of Dirichlet DoFs zeroed.
+// Cells first (s_T = w_T D_T . p), then rows gather the matrix part and the
+// incident cells' D_T[loc] s_T.  Returns this thread's part of p.q.
+template <int TPR>
+__device__ __forceinline__ float block_apply_split(const BatchDev &d, int r0, int r1, int c0, int c1) {
+    constexpr int RPW = 32 / TPR;
+    constexpr int U = TPR >= 16 ? 2 : 4;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const float *p = d.p32;
+    for (int c = c0 + tid; c < c1; c += bs) {
+        float a = 0.f;
+#pragma unroll
+        for (int I = 0; I < 9; I++) a += d.Dv32[(size_t)c * 9 + I] * p[d.celldofs[(size_t)c * 9 + I]];
+        d.s32[c] = d.w32[c] * a;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & (TPR - 1), gin = (threadIdx.x & 31) / TPR;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    float dacc = 0.f;
+    for (int base = r0 + warp * RPW; base < r1; base += nwarps * RPW) {
+        const int r = base + gin;
+        float sm = 0.f;
+        if (r < r1) {
+            const int kb = __ldg(d.rowptr + r), e = __ldg(d.rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                float v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(d.cols + idx) : r;
+                    v[u] = ok ? __ldg(d.v32 + idx) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) sm += v[u] * p[c[u]];
+            }
+            const int qb = d.inc_ptr[r], qe = d.inc_ptr[r + 1];
+            for (int q = qb + lane; q < qe; q += TPR) {
+                const int cell = d.inc_cell[q];
+                sm += d.Dv32[(size_t)cell * 9 + d.inc_loc[q]] * d.s32[cell];
+            }
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
+        if (r < r1 && lane == 0) {
+            d.q32[r] = sm;
+            dacc += p[r] * sm;
+        }
+    }
+    return dacc;
+}
+
+// FP32 Jacobi-PCG on the split-penalty operator inside FP64 refinement
+// (outer residual rhs - A64 x with the assembled FP64 matrix).  Same
+// reliable-update and restart rules as block_pcg_mixed.
+template <int TPR>
+__device__ int block_pcg_mixed_split(const BatchDev &d, int r0, int r1, int c0, int c1, const double *rhs,
+                                     double *x, double *sh, double *relres, bool *ok) {
+    const int tid = threadIdx.x, bs = blockDim.x;
+    double v[2] = {0, 0};
+    v[0] = block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, x, d.r64, nullptr, rhs);
+    for (int i = r0 + tid; i < r1; i += bs) v[1] += rhs[i] * rhs[i];
+    bsum<2>(v, sh);
+    const double bn = sqrt(v[1]);
+    const double tol = d.reltol * bn;
+    double rn64 = sqrt(v[0]);
+    bool conv = rn64 <= tol || bn == 0.0;
+    int it = 0;
+    float wf0 = 0.f, wf1 = 0.f;
+    for (int i = r0 + tid; i < r1; i += bs) {
+        const float ri = (float)d.r64[i];
+        const float zi = d.dinv32[i] * ri;
+        d.r32[i] = ri;
+        d.p32[i] = zi;
+        d.xc32[i] = 0.f;
+        wf0 += ri * zi;
+        wf1 += ri * ri;
+    }
+    double w[2] = {(double)wf0, (double)wf1};
+    bsum<2>(w, sh);
+    double rz = w[0], rmax = sqrt(w[1]), prev = rn64;
+    int stall = 0;
+    while (!conv && it < d.maxit) {
+        double pq[1] = {(double)block_apply_split<TPR>(d, r0, r1, c0, c1)};
+        bsum<1>(pq, sh);
+        if (!(pq[0] > 0) || !isfinite(pq[0])) break;
+        const float alpha = (float)(rz / pq[0]);
+        float u0 = 0.f, u1 = 0.f;
+        for (int i = r0 + tid; i < r1; i += bs) {
+            d.xc32[i] += alpha * d.p32[i];
+            const float ri = d.r32[i] - alpha * d.q32[i];
+            d.r32[i] = ri;
+            const float zi = d.dinv32[i] * ri;
+            d.z32[i] = zi;
+            u0 += ri * zi;
+            u1 += ri * ri;
+        }
+        double u[2] = {(double)u0, (double)u1};
+        bsum<2>(u, sh);
+        it++;
+        double rz_new = u[0];
+        const double rn32 = sqrt(u[1]);
+        bool restart = false;
+        if (rn32 <= d.delta * rmax || rn32 <= tol || it >= d.maxit) {
+            for (int i = r0 + tid; i < r1; i += bs) {
+                x[i] += (double)d.xc32[i];
+                d.xc32[i] = 0.f;
+            }
+            __syncthreads();
+            double t[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, x, d.r64, nullptr, rhs)};
+            bsum<1>(t, sh);
+            rn64 = sqrt(t[0]);
+            conv = rn64 <= tol;
+            if (conv || it >= d.maxit) break;
+            restart = rn64 > 0.5 * prev;
+            stall = rn64 > 0.9 * prev ? stall + 1 : 0;
+            prev = rn64;
+            if (stall >= 16) break;
+            float y0 = 0.f, y1 = 0.f;
+            for (int i = r0 + tid; i < r1; i += bs) {
+                const float ri = (float)d.r64[i];
+                const float zi = d.dinv32[i] * ri;
+                d.r32[i] = ri;
+                d.z32[i] = zi;
+                y0 += ri * zi;
+                y1 += ri * ri;
+            }
+            double y[2] = {(double)y0, (double)y1};
+            bsum<2>(y, sh);
+            rz_new = y[0];
+            rmax = sqrt(y[1]);
+        }
+        const float beta = restart ? 0.f : (float)(rz_new / rz);
+        rz = rz_new;
+        for (int i = r0 + tid; i < r1; i += bs) d.p32[i] = __fmaf_rn(beta, d.p32[i], d.z32[i]);
+        __syncthreads();
+    }
+    *relres = bn > 0 ? rn64 / bn : 0.0;
+    *ok = conv;
+    return it;
+}
+
 // Plain FP64 Jacobi-PCG on rows [r0, r1); w64a = z, w64b = p, w64c = q.
 template <int TPR>
 __device__ int block_pcg64(const BatchDev &d, int r0, int r1, const double *rhs, double *x, double *sh,
@@ -303,7 +451,7 @@ __device__ int block_pcg64(const BatchDev &d, int r0, int r1, const double *rhs,
 }
 
 template <int TPR>
-__global__ void __launch_bounds__(512) k_stokes_batch(BatchDev d) {
+__global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
     __shared__ double sh[32 * 4];
     __shared__ int slot;
     const int tid = threadIdx.x, bs = blockDim.x;
@@ -322,7 +470,9 @@ __global__ void __launch_bounds__(512) k_stokes_batch(BatchDev d) {
             for (int kk = d.rowptr[i]; kk < d.rowptr[i + 1]; kk++)
                 if (d.cols[kk] == i) dg = d.v64[kk];
             d.dinv64[i] = 1.0 / dg;
-            if (d.mixed) {
+            if (d.mixed && d.split) {
+                d.dinv32[i] = (float)(1.0 / dg);   // diagonal of the whole operator
+            } else if (d.mixed) {
                 float df = 1.f;
                 for (int kk = d.rowptr[i]; kk < d.rowptr[i + 1]; kk++)
                     if (d.cols[kk] == i) df = d.v32[kk];
@@ -330,9 +480,18 @@ __global__ void __launch_bounds__(512) k_stokes_batch(BatchDev d) {
             }
             d.u[i] = 0.0;
         }
-        for (int c = c0 + tid; c < c1; c += bs) d.p[c] = 0.0;
+        for (int c = c0 + tid; c < c1; c += bs) {
+            d.p[c] = 0.0;
+            if (d.mixed && d.split) {
+                for (int I = 0; I < 9; I++) {
+                    const size_t k9 = (size_t)c * 9 + I;
+                    d.Dv32[k9] = d.fixed[d.celldofs[k9]] ? 0.f : (float)d.Dv[k9];
+                }
+                d.w32[c] = (float)(d.lambda / d.vol[c]);
+            }
+        }
         __syncthreads();
-        int total_it = 0, sweep = 0;
+        int total_it = 0, sweep = 0, nfall = 0;
         double worst = 0.0;
         bool all_ok = true;
         for (sweep = 0; sweep < d.sweeps; sweep++) {
@@ -349,8 +508,15 @@ __global__ void __launch_bounds__(512) k_stokes_batch(BatchDev d) {
             __syncthreads();
             double rr;
             bool ok;
-            const int it = d.mixed ? block_pcg_mixed<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok)
-                                   : block_pcg64<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok);
+            int it = !d.mixed ? block_pcg64<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok)
+                     : d.split ? block_pcg_mixed_split<TPR>(d, r0, r1, c0, c1, d.rhs, d.u, sh, &rr, &ok)
+                               : block_pcg_mixed<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok);
+            if (d.mixed && !ok) {
+                // FP32 stalled (or hit the cap): finish this sweep in FP64 from the same iterate
+                __syncthreads();
+                it += block_pcg64<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok);
+                nfall++;
+            }
             total_it += it;
             worst = fmax(worst, rr);
             all_ok = all_ok && ok;
@@ -391,6 +557,7 @@ __global__ void __launch_bounds__(512) k_stokes_batch(BatchDev d) {
             d.iters[pid] = total_it;
             d.sweeps_done[pid] = sweep;
             d.relres[pid] = worst;
+            d.fallbacks[pid] = nfall;
             d.status[pid] = all_ok ? 0 : (int)GRMP_ERR_NOT_CONVERGED;
         }
         __syncthreads();
@@ -469,7 +636,16 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     d.xc32 = (float *)take((size_t)n * 4);
     d.zp0 = (float2 *)take((size_t)n * 8);
     d.zp1 = (float2 *)take((size_t)n * 8);
+    const bool split = prm->mode == GRMP_SOLVE_MIXED && prm->split_penalty;
+    if (split) {
+        d.z32 = (float *)take((size_t)n * 4);
+        d.p32 = (float *)take((size_t)n * 4);
+        d.s32 = (float *)take((size_t)nc * 4);
+        d.Dv32 = (float *)take((size_t)nc * 36);
+        d.w32 = (float *)take((size_t)nc * 4);
+    }
     d.queue = (int *)take(64);
+    d.fallbacks = (int *)take((size_t)np * 4);
     d.iters = (int *)take((size_t)np * 4);
     d.sweeps_done = (int *)take((size_t)np * 4);
     d.status = (int *)take((size_t)np * 4);
@@ -478,7 +654,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     double *Dv = nullptr, *vol = nullptr;
     bool okalloc = dorder && drow && dcell && d.rhs && d.r64 && d.dinv64 && d.w64a && d.w64b && d.w64c && d.dinv32 &&
                    d.r32 && d.q32 && d.xc32 && d.zp0 && d.zp1 && d.queue && d.iters && d.sweeps_done && d.status &&
-                   d.relres && bad;
+                   d.relres && bad && d.fallbacks && (!split || (d.z32 && d.p32 && d.s32 && d.Dv32 && d.w32));
     int rc = okalloc ? GRMP_OK : GRMP_ERR_OUT_OF_MEMORY;
     if (!rc) rc = grmp_br_divergence(s, &Dv, &vol);
     if (rc) {
@@ -530,6 +706,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     d.sweeps = prm->sweeps;
     d.maxit = prm->maxiter;
     d.mixed = prm->mode == GRMP_SOLVE_MIXED ? 1 : 0;
+    d.split = split ? 1 : 0;
     int threads = prm->block_threads > 0 ? prm->block_threads : 512;
     threads = std::max(64, std::min(512, threads / 32 * 32));
     // lanes per row from the average row length
@@ -546,13 +723,14 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     kern<<<grid, threads, 0, ctx->stream>>>(d);
     GRMP_LAUNCHED(ctx);
     cudaEventRecord(e1, ctx->stream);
-    std::vector<int> it(np), sw(np), st(np);
+    std::vector<int> it(np), sw(np), st(np), fb(np);
     std::vector<double> rr(np);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(it.data(), d.iters, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sw.data(), d.sweeps_done, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(st.data(), d.status, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rr.data(), d.relres, (size_t)np * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fb.data(), d.fallbacks, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     float ms = 0;
     if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
@@ -568,6 +746,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
         stats->max_iterations = std::max(stats->max_iterations, it[k]);
         stats->max_sweeps = std::max(stats->max_sweeps, sw[k]);
         stats->max_relres = std::max(stats->max_relres, rr[k]);
+        stats->fp64_fallbacks += fb[k];
         if (st[k]) stats->failed_problems++;
     }
     if (iters_out) std::memcpy(iters_out, it.data(), (size_t)np * 4);

@@ -78,8 +78,8 @@ struct grmp_matrix_s {
     // cached workspace for solves
     void *d_work = nullptr;
     size_t work_bytes = 0;
-    int tuned_tpr = 0;              // autotuned SpMV lanes per row, FP64 values (0 = not tuned)
-    int tuned_tpr32 = 0;            // autotuned SpMV lanes per row, FP32 values
+    int tuned_cfg = 0;              // autotuned SpMV configuration, FP64 solves (0 = not tuned)
+    int tuned_cfg32 = 0;            // autotuned SpMV configuration (100*lanes + loads), mixed solves
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;

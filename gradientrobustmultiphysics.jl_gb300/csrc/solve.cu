@@ -22,7 +22,6 @@
 #include <type_traits>
 
 #include "grmp_internal.h"
-#include "spmv.cuh"
 
 namespace {
 
@@ -82,46 +81,71 @@ __device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh,
     return true;
 }
 
-// y = A x over all rows with the warp-stream core (chunk CH).  If DOT,
-// returns this thread's share of sum_r w[r]*y[r]; if RESID, y = b - A x and
-// the share of sum_r y[r]^2.  `smem` holds 8 warps x CH accumulators.
-template <int CH, typename V, typename X, typename Y, bool DOT, bool RESID>
+// y = A x over the rows of this grid; groups of TPR lanes per row.  If DOT,
+// returns this thread's share of sum_r w[r]*y[r].  If RESID, y = b - A x.
+template <int TPR, int U, typename V, typename X, typename Y, bool DOT, bool RESID>
 __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
                                             const V *__restrict__ vals, const X *x, Y *y, const Y *w,
-                                            const double *b, void *smem) {
+                                            const double *b) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & (TPR - 1);
+    const int warp = gtid >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    constexpr int RPW = 32 / TPR;   // rows per warp per step
+    const int gin = (threadIdx.x & 31) / TPR;
+    // Each lane keeps U independent (col, val) loads and U gathers in
+    // flight per pass: the SpMV is bound by memory-level parallelism, not
+    // arithmetic.  The matrix is read-only for the whole solve (non-coherent
+    // path); x is written by other blocks between barriers (coherent loads).
     using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
-    A *wb = reinterpret_cast<A *>(smem) + (threadIdx.x >> 5) * CH;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     double dot = 0;
     A dacc = 0;
-    spmv::warp_stream<CH, V, A>(
-        0, n, gw, nw, rowptr, cols, vals, wb, [&](int c) { return (A)x[c]; },
-        [&](int r, A s) {
+    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
+        int r = base + gin;
+        A s = 0;
+        if (r < n) {
+            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                A v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(cols + idx) : r;
+                    v[u] = ok ? (A)__ldg(vals + idx) : A(0);
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) s += v[u] * (A)x[c[u]];
+            }
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (r < n && lane == 0) {
             if (RESID) {
-                const double v = b[r] - (double)s;
+                double v = b[r] - (double)s;
                 y[r] = (Y)v;
                 if (DOT) dot += v * v;
             } else {
                 y[r] = (Y)s;
                 if (DOT) dacc += (A)w[r] * s;   // FP32 partial in the FP32 path
             }
-        });
+        }
+    }
     return dot + (double)dacc;
 }
 
 // ------------------------------------------------------------------ FP64 PCG
-template <int TPR>
+template <int TPR, int U>
 __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
                                                 const double *vals, const double *b, double *x, const double *dinv,
                                                 double *r, double *z, double *p, double *q, double *partial,
                                                 SolveState *st, double abstol, double reltol, int maxit, int guess) {
     __shared__ double sh[32 * 4];
-    __shared__ __align__(16) double swb[8 * TPR];   // warp-stream accumulators (8 warps x chunk)
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // r = b - A x  (or b)
-    if (guess) spmv_grid<TPR, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b, swb);
+    if (guess) spmv_grid<TPR, U, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double v[3] = {0, 0, 0};
     for (int i = gtid; i < n; i += gsz) {
@@ -142,7 +166,7 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
     bool conv = sqrt(rr) <= tol;
     while (!conv && it < maxit) {
         double d[1];
-        d[0] = spmv_grid<TPR, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr, swb);
+        d[0] = spmv_grid<TPR, U, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
         if (!grid_sum<1>(d, partial, sh, st)) return;
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -173,7 +197,7 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
     // true residual in FP64
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double t[1];
-    t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b, swb);
+    t[0] = spmv_grid<TPR, U, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
     if (!grid_sum<1>(t, partial, sh, st)) return;
     if (gtid == 0) {
         st->iters = it;
@@ -191,45 +215,66 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
 // fmaf everywhere so all readers see identical values), the owner of row r
 // stores p_k(r) into nxt[r].y, and phase B stores z_{k+1} into nxt[r].x.
 // This removes the separate p-update pass and one grid barrier per iteration.
-template <int CH>
+template <int TPR, int U>
 __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr,
                                                const int32_t *__restrict__ cols, const float *__restrict__ vals,
-                                               const float2 *cur, float *nxt_f, float *q, float beta, void *smem) {
-    float *wb = reinterpret_cast<float *>(smem) + (threadIdx.x >> 5) * CH;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
+                                               const float2 *cur, float *nxt_f, float *q, float beta) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & (TPR - 1);
+    const int warp = gtid >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    constexpr int RPW = 32 / TPR;
+    const int gin = (threadIdx.x & 31) / TPR;
     float dacc = 0.f;
-    spmv::warp_stream<CH, float, float>(
-        0, n, gw, nw, rowptr, cols, vals, wb,
-        [&](int c) {
-            const float2 g = cur[c];
-            return __fmaf_rn(beta, g.y, g.x);
-        },
-        [&](int r, float s) {
+    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
+        const int r = base + gin;
+        float s = 0.f;
+        if (r < n) {
+            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+            for (int k = kb + lane; k < e; k += TPR * U) {
+                int c[U];
+                float v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = k + u * TPR;
+                    const bool ok = idx < e;
+                    c[u] = ok ? __ldg(cols + idx) : r;
+                    v[u] = ok ? __ldg(vals + idx) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const float2 g = cur[c[u]];
+                    s += v[u] * __fmaf_rn(beta, g.y, g.x);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (r < n && lane == 0) {
             const float2 me = cur[r];
             const float pn = __fmaf_rn(beta, me.y, me.x);
             nxt_f[2 * r + 1] = pn;
             q[r] = s;
             dacc += pn * s;
-        });
+        }
+    }
     return dacc;
 }
 
-template <int TPR>
-__global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+template <int TPR, int U>
+__global__ void __launch_bounds__(PTPB, U >= 8 ? 4 : 5) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
                                                     const double *vals64, const float *vals32, const double *b,
                                                     double *x, const float *dinv, float *r, float *q, float *xc,
                                                     float2 *zp0, float2 *zp1, double *r64, double *partial,
                                                     SolveState *st, double abstol, double reltol, double delta,
                                                     int maxit, int maxouter, int guess) {
     __shared__ double sh[32 * 4];
-    __shared__ __align__(16) double swb[8 * TPR];   // warp-stream accumulators (8 warps x chunk)
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // FP64 residual of the initial guess
     double v[2] = {0, 0};
     if (guess) {
-        v[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b, swb);
+        v[0] = spmv_grid<TPR, U, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
     } else {
         for (int i = gtid; i < n; i += gsz) {
             x[i] = 0.0;
@@ -266,7 +311,7 @@ __global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *row
     while (!conv && it < maxit && outer < maxouter) {
         float *nxt_f = reinterpret_cast<float *>(nxt);
         double d[1];
-        d[0] = (double)spmv_fused_zp<TPR>(n, rowptr, cols, vals32, cur, nxt_f, q, beta, swb);
+        d[0] = (double)spmv_fused_zp<TPR, U>(n, rowptr, cols, vals32, cur, nxt_f, q, beta);
         if (!grid_sum<1>(d, partial, sh, st)) return;   // barrier 1
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -299,7 +344,7 @@ __global__ void __launch_bounds__(PTPB, 6) k_pcg_mixed(int n, const int32_t *row
             }
             if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
             double t[1];
-            t[0] = spmv_grid<TPR, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b, swb);
+            t[0] = spmv_grid<TPR, U, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
             if (!grid_sum<1>(t, partial, sh, st)) return;
             outer++;
             rn64 = sqrt(t[0]);
@@ -361,8 +406,7 @@ __global__ void k_dinv(int n, const int32_t *rowptr, const int32_t *cols, const 
 template <int TPR, typename V, typename X>
 __global__ void __launch_bounds__(256) k_spmv(int n, const int32_t *rowptr, const int32_t *cols, const V *vals,
                                               const X *x, X *y) {
-    __shared__ __align__(16) double swb[8 * TPR];
-    spmv_grid<TPR, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr, swb);
+    spmv_grid<TPR, TPR >= 16 ? 2 : 4, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr);
 }
 
 __global__ void k_f64_to_f32(const double *a, float *b, int n) {
@@ -375,68 +419,36 @@ __global__ void k_f32_to_f64v(const float *a, double *b, int n) {
 }
 
 template <typename V, typename X>
-void launch_spmv(int chunk, int grid, cudaStream_t s, int n, const int32_t *rp, const int32_t *ci, const V *v,
-                 const X *x, X *y) {
-    switch (chunk) {
-        case 64: k_spmv<64, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        case 256: k_spmv<256, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
-        default: k_spmv<128, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, const int32_t *ci, const V *v, const X *x,
+                 X *y) {
+    switch (tpr) {
+        case 1: k_spmv<1, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 2: k_spmv<2, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 4: k_spmv<4, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 8: k_spmv<8, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        case 16: k_spmv<16, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
+        default: k_spmv<32, V, X><<<grid, 256, 0, s>>>(n, rp, ci, v, x, y); break;
     }
 }
+
+// SpMV configurations of the persistent solvers: (lanes per row, loads in
+// flight per lane), encoded 100*TPR + U.
+constexpr int kConfigs[] = {208, 404, 408, 804, 1602};
 
 int heuristic_tpr(grmp_matrix A) {
-    // warp-stream chunk: about one chunk per 8-row warp step
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
-    return avg * 8 <= 96 ? 64 : (avg * 8 <= 192 ? 128 : 256);
+    if (avg <= 3) return 2;
+    if (avg <= 6) return 4;
+    if (avg <= 14) return 8;
+    if (avg <= 40) return 16;
+    return 32;
 }
 
-// Autotuner: time the standalone SpMV for each lane count on this matrix
-// (values of `precision`) and keep the fastest.
-int autotune_tpr(grmp_matrix A, int precision) {
-    grmp_context ctx = A->space->mesh->ctx;
-    int n = A->nrows;
-    void *xb = nullptr, *yb = nullptr;
-    size_t es = precision == GRMP_FP64 ? 8 : 4;
-    if (grmp_alloc(ctx, &xb, (size_t)n * es) || grmp_alloc(ctx, &yb, (size_t)n * es)) {
-        grmp_free(ctx, xb, (size_t)n * es);
-        return heuristic_tpr(A);
-    }
-    cudaMemsetAsync(xb, 0, (size_t)n * es, ctx->stream);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    int best = heuristic_tpr(A);
-    float bt = 1e30f;
-    const int cand[3] = {64, 128, 256};
-    for (int c : cand) {
-        int grid = std::min(nblk(n, 64), ctx->num_sms * 8);
-        float tot = 0;
-        for (int rep = 0; rep < 4; rep++) {
-            cudaEventRecord(e0, ctx->stream);
-            if (precision == GRMP_FP64)
-                launch_spmv<double, double>(c, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals64,
-                                            (const double *)xb, (double *)yb);
-            else
-                launch_spmv<float, float>(c, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals32,
-                                          (const float *)xb, (float *)yb);
-            GRMP_LAUNCHED(ctx);
-            cudaEventRecord(e1, ctx->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (rep > 0) tot += ms;
-        }
-        if (tot < bt) {
-            bt = tot;
-            best = c;
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    grmp_free(ctx, xb, (size_t)n * es);
-    grmp_free(ctx, yb, (size_t)n * es);
-    cudaGetLastError();
-    return best;
+int heuristic_config(grmp_matrix A) {
+    double avg = (double)A->nnz / (double)std::max(1, A->nrows);
+    if (avg <= 8) return 208;
+    if (avg <= 20) return 404;
+    return 408;
 }
 
 template <typename K>
@@ -449,8 +461,8 @@ int coop_grid(grmp_context ctx, K kern, int n, int want) {
     return std::max(1, g);
 }
 
-template <int TPR>
-int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *out,
+template <int TPR, int U>
+int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p, grmp_solve_stats *out,
                char *work, SolveState *dst, WorkLayout lay) {
     grmp_context ctx = A->space->mesh->ctx;
     int n = A->nrows;
@@ -461,8 +473,9 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
     if (!mixed) {
-        auto kern = k_pcg64<TPR>;
+        auto kern = k_pcg64<TPR, U>;
         grid = coop_grid(ctx, kern, n, p->grid_blocks);
         double *dinv = (double *)work, *r = (double *)(work + lay.vec), *z = (double *)(work + 2 * lay.vec);
         double *pp = (double *)(work + 3 * lay.vec), *q = (double *)(work + 4 * lay.vec);
@@ -470,15 +483,15 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
         int nn = n, mi = p->maxiter;
         double at = p->abstol, rt = p->reltol;
         const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
-        const double *vv = A->d_vals64, *bb = b->d;
-        double *xx = x->d;
+        const double *vv = A->d_vals64, *bb = bvec;
+        double *xx = xvec;
         void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess};
         cudaEventRecord(e0, ctx->stream);
         e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
         GRMP_LAUNCHED(ctx);
         cudaEventRecord(e1, ctx->stream);
     } else {
-        auto kern = k_pcg_mixed<TPR>;
+        auto kern = k_pcg_mixed<TPR, U>;
         grid = coop_grid(ctx, kern, n, p->grid_blocks);
         float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
         float *xc = (float *)(work + 3 * lay.vec);
@@ -488,9 +501,9 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
         int nn = n, mi = p->maxiter, mo = p->max_outer > 0 ? p->max_outer : 1000;
         double at = p->abstol, rt = p->reltol, dl = p->inner_reltol > 0 && p->inner_reltol < 1 ? p->inner_reltol : 0.1;
         const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
-        const double *v64 = A->d_vals64, *bb = b->d;
+        const double *v64 = A->d_vals64, *bb = bvec;
         const float *v32 = A->d_vals32;
-        double *xx = x->d;
+        double *xx = xvec;
         void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
                         &at, &rt, &dl, &mi, &mo, &guess};
         cudaEventRecord(e0, ctx->stream);
@@ -510,7 +523,7 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     out->iterations = hs.iters;
     out->outer_iterations = hs.outer;
     out->final_relres = hs.relres;
-    out->spmv_chunk = TPR;
+    out->spmv_config = 100 * TPR + U;
     out->grid_blocks = grid;
     out->solve_ms = ms;
     if (hs.status == GRMP_ERR_NOT_CONVERGED)
@@ -518,6 +531,53 @@ int launch_pcg(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a grid barrier wait timed out");
     if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
     return hs.status;
+}
+
+int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_solve_params *p, grmp_solve_stats *st,
+                 char *work, SolveState *dst, WorkLayout lay) {
+    switch (cfg) {
+        case 208: return launch_pcg<2, 8>(A, b, x, p, st, work, dst, lay);
+        case 404: return launch_pcg<4, 4>(A, b, x, p, st, work, dst, lay);
+        case 408: return launch_pcg<4, 8>(A, b, x, p, st, work, dst, lay);
+        case 804: return launch_pcg<8, 4>(A, b, x, p, st, work, dst, lay);
+        case 1602: return launch_pcg<16, 2>(A, b, x, p, st, work, dst, lay);
+    }
+    return grmp_fail(A->space->mesh->ctx, GRMP_ERR_INVALID_ARG, "spmv_config must be one of 208 404 408 804 1602");
+}
+
+// Autotuner: run each configuration for a few iterations of the real solve
+// on this matrix and right-hand side (into a scratch solution vector) and keep
+// the one with the lowest time per iteration.  The persistent kernel's
+// occupancy, barriers and vector phases are part of what is measured.
+int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_params *p, char *work, SolveState *dst,
+                    WorkLayout lay) {
+    grmp_context ctx = A->space->mesh->ctx;
+    if (A->nrows < 20000) return heuristic_config(A);
+    double *xs = nullptr;
+    if (grmp_alloc(ctx, (void **)&xs, (size_t)A->nrows * 8)) return heuristic_config(A);
+    grmp_solve_params q = *p;
+    q.maxiter = 24;
+    q.use_initial_guess = 0;
+    q.reltol = 0.0;
+    q.abstol = 0.0;
+    int best = heuristic_config(A);
+    double bt = 1e30;
+    for (int cfg : kConfigs) {
+        grmp_solve_stats s{};
+        dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);   // warm-up: first launch of this instantiation
+        s = grmp_solve_stats{};
+        dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);
+        if (s.iterations > 0) {
+            double per = s.solve_ms / s.iterations;
+            if (per < bt) {
+                bt = per;
+                best = cfg;
+            }
+        }
+    }
+    grmp_free(ctx, xs, (size_t)A->nrows * 8);
+    ctx->last_error.clear();
+    return best;
 }
 
 }  // namespace
@@ -567,25 +627,20 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     grmp_free(ctx, bad, 4);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
-    int tpr = p->spmv_chunk;
-    if (tpr <= 0) {   // autotuned once per matrix and precision of the inner operator
-        int &slot = mixed ? A->tuned_tpr32 : A->tuned_tpr;
-        if (!slot) slot = autotune_tpr(A, mixed ? GRMP_FP32 : GRMP_FP64);
-        tpr = slot;
+    int cfg = p->spmv_config;
+    if (cfg <= 0) {   // autotuned once per matrix and solver mode
+        int &slot = mixed ? A->tuned_cfg32 : A->tuned_cfg;
+        if (!slot) slot = autotune_config(A, b, p, work, dst, lay);
+        cfg = slot;
     }
-    switch (tpr) {
-        case 64: return launch_pcg<64>(A, b, x, p, st, work, dst, lay);
-        case 128: return launch_pcg<128>(A, b, x, p, st, work, dst, lay);
-        case 256: return launch_pcg<256>(A, b, x, p, st, work, dst, lay);
-    }
-    return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_chunk must be 64, 128 or 256");
+    return dispatch_pcg(cfg, A, b->d, x->d, p, st, work, dst, lay);
 }
 
 int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
     grmp_context ctx = A->space->mesh->ctx;
     int n = A->nrows;
-    int tpr = A->tuned_tpr ? A->tuned_tpr : heuristic_tpr(A);
-    int grid = std::min(nblk(n, 64), ctx->num_sms * 8);
+    int tpr = A->tuned_cfg ? A->tuned_cfg / 100 : heuristic_tpr(A);
+    int grid = std::min(nblk(n, 256 / tpr), ctx->num_sms * 16);
     if (precision == GRMP_FP64) {
         if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv: no FP64 values");
         launch_spmv<double, double>(tpr, grid, ctx->stream, n, A->d_rowptr, A->d_cols, A->d_vals64, x->d, y->d);

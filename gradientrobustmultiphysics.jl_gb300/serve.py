@@ -1,0 +1,201 @@
+"""Serving loop: Poisson-process arrivals of Poisson / reaction-diffusion solves.
+
+Request mix (seeded): dimension 2 or 3, element H1P1 or H1P2 (uniform), DoF
+count log-uniform in [1e3, 2e6], per-cell kappa = exp(N(0,1)) as
+BilinearForm([Gradient, Gradient], Action(kappa[cell] * input; "I")), with
+probability 1/2 a ReactionOperator(alpha), alpha uniform in [0, 10], an
+8-mode Fourier right-hand side and homogeneous Dirichlet data on the whole
+boundary.  Requests are served by the library's serving engine
+(grmp_server_*): slots with their own streams, admission by an HBM budget,
+mixed-precision solves to a relative residual that gives <= 1e-10 relative
+error against FP64.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from . import api
+from .fespace import FESpace, H1P1, H1P2
+from .mesh import grid_unitsquare, grid_unitcube_kuhn
+from .problems import fourier_modes
+
+
+@dataclass
+class ServeRequest:
+    dim: int
+    order: int
+    n: int
+    FES: FESpace
+    kappa: np.ndarray
+    alpha: float
+    amp: np.ndarray
+    k: np.ndarray
+    fixed: np.ndarray
+    arrival_s: float = 0.0
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def ndofs(self) -> int:
+        return self.FES.ndofs
+
+    def operators(self):
+        ops = [api.BilinearForm([api.Gradient, api.Gradient], api.CellCoefficient(self.kappa),
+                                APT=api.APT_SymmetricBilinearForm)]
+        if self.alpha > 0:
+            ops.append(api.ReactionOperator(self.alpha))
+        return ops
+
+    def rhs(self):
+        return api.LinearForm(api.Identity, api.DataFunction.fourier(self.amp, self.k))
+
+
+def mesh_size_for(dofs: float, dim: int, order: int) -> int:
+    """Number of subdivisions per axis whose DoF count is closest to `dofs`."""
+    side = dofs ** (1.0 / dim)                 # DoFs per axis ~ (order n + 1)
+    return max(2, int(round((side - 1) / order)))
+
+
+_grid_cache: dict = {}
+_space_cache: dict = {}
+
+
+def build_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=2e6, dim=None, order=None) -> ServeRequest:
+    dim = int(rng.integers(2, 4)) if dim is None else dim
+    order = int(rng.integers(1, 3)) if order is None else order
+    target = math.exp(rng.uniform(math.log(dofs_min), math.log(dofs_max)))
+    n = mesh_size_for(target, dim, order)
+    key = (dim, n)
+    if key not in _grid_cache:
+        _grid_cache[key] = grid_unitsquare(n) if dim == 2 else grid_unitcube_kuhn(n)
+    g = _grid_cache[key]
+    skey = (dim, n, order)
+    if skey not in _space_cache:
+        _space_cache[skey] = FESpace(H1P1(1) if order == 1 else H1P2(1, dim), g)
+    FES = _space_cache[skey]
+    kappa = np.exp(rng.standard_normal(g.ncells))
+    alpha = float(rng.uniform(0, 10)) if rng.random() < 0.5 else 0.0
+    amp, k = fourier_modes(rng, dim)
+    return ServeRequest(dim, order, n, FES, kappa, alpha, amp, k, FES.boundary_dofs())
+
+
+def make_workload(nrequests: int, seed: int = 0, mean_interarrival_s: float = 0.05, dofs_max=2e6):
+    """Requests with Poisson-process arrival times (exponential gaps)."""
+    rng = np.random.default_rng(seed)
+    reqs, t = [], 0.0
+    for _ in range(nrequests):
+        r = build_request(rng, dofs_max=dofs_max)
+        t += float(rng.exponential(mean_interarrival_s))
+        r.arrival_s = t
+        reqs.append(r)
+    return reqs
+
+
+class Server:
+    """The library's serving engine (grmp_server_*)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 150 << 30, nslots: int = 4):
+        self.lib = L.load()
+        self.h = ctypes.c_void_p()
+        rc = self.lib.grmp_server_create(device, hbm_budget_bytes, nslots, ctypes.byref(self.h))
+        if rc:
+            raise L.GrmpError(rc, "grmp_server_create")
+
+    def submit(self, r: ServeRequest, mode: str = "mixed", reltol: float = 1e-11) -> int:
+        FES, g = r.FES, r.FES.xgrid
+        q = L.Request()
+        keep = []
+
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt)))
+
+        q.dim = g.dim
+        q.nverts = g.nverts
+        q.coords = arr(g.coords, np.float64)
+        q.ncells = g.ncells
+        q.cells = arr(g.cells, np.int32)
+        q.fe_kind = FES.FEType.kind
+        q.ncomponents = FES.FEType.ncomponents
+        q.ndofs = FES.ndofs
+        q.celldofs = arr(FES.celldofs, np.int32)
+        ops = r.operators()
+        terms = (L.BilinearTerm * len(ops))()
+        for i, o in enumerate(ops):
+            terms[i] = o.term()
+        keep.append(ops)
+        q.nterms = len(ops)
+        q.terms = terms
+        lf = r.rhs()
+        q.rhs = lf.rhs()
+        keep.append(lf)
+        q.nfixed = r.fixed.size
+        q.fixed = arr(r.fixed, np.int32)
+        s = api.GB300PCG(mode=mode, reltol=reltol, abstol=0.0)
+        q.solve = s.params()
+        rid = ctypes.c_int64()
+        rc = self.lib.grmp_server_submit(self.h, ctypes.byref(q), ctypes.byref(rid))
+        if rc:
+            raise L.GrmpError(rc, "grmp_server_submit")
+        return rid.value
+
+    def wait(self, rid: int, ndofs: int, timeout_s: float = -1.0):
+        x = np.empty(ndofs)
+        st = L.RequestStats()
+        rc = self.lib.grmp_server_wait(self.h, rid, timeout_s, x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       ctypes.byref(st))
+        return rc, x, {"status": st.status, "slot": st.slot, "iterations": st.iterations,
+                       "outer": st.outer_iterations, "relres": st.final_relres, "queue_ms": st.queue_ms,
+                       "run_ms": st.run_ms, "latency_ms": st.latency_ms, "solve_ms": st.solve_ms}
+
+    def close(self):
+        if self.h:
+            self.lib.grmp_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run(reqs, nslots: int = 4, hbm_budget_bytes: int = 150 << 30, mode: str = "mixed", reltol: float = 1e-11,
+        realtime: bool = True):
+    """Submit the requests at their arrival times (realtime) or all at once;
+    returns (solutions, per-request stats, makespan seconds)."""
+    srv = Server(0, hbm_budget_bytes, nslots)
+    try:
+        t0 = time.perf_counter()
+        ids = []
+        for r in reqs:
+            if realtime:
+                dt = r.arrival_s - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+            ids.append(srv.submit(r, mode, reltol))
+        xs, sts = [], []
+        for r, rid in zip(reqs, ids):
+            rc, x, st = srv.wait(rid, r.ndofs)
+            st["rc"] = rc
+            xs.append(x)
+            sts.append(st)
+        makespan = time.perf_counter() - t0
+    finally:
+        srv.close()
+    return xs, sts, makespan
+
+
+def summarize(reqs, sts, makespan):
+    lat = np.array([s["latency_ms"] for s in sts])
+    dofs = sum(r.ndofs for r in reqs)
+    return {"requests": len(reqs), "dofs": int(dofs), "makespan_s": makespan, "dof_per_s": dofs / makespan,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max())},
+            "failed": int(sum(1 for s in sts if s["rc"] != 0))}

@@ -167,10 +167,15 @@ def velocity_operators(prob: StokesBatchProblem):
 class StokesBatchSystem:
     """Device-resident batched system: pattern, assembly, reconstructed rhs."""
 
-    def __init__(self, ctx: api.GB300Context, prob: StokesBatchProblem, mixed: bool = True):
+    def __init__(self, ctx: api.GB300Context, prob: StokesBatchProblem, mixed: bool = True,
+                 split_penalty: bool = True):
+        """mixed: FP32 inner solves inside FP64 refinement.  split_penalty
+        (mixed only): the FP32 matrix holds the viscous term alone and the
+        inner operator applies the penalty per cell in factored form."""
         self.ctx = ctx
         self.prob = prob
         self.mixed = mixed
+        self.split_penalty = bool(split_penalty and mixed)
         self.ops = velocity_operators(prob)
         t0 = time.perf_counter()
         self.A = api.FEMatrix(ctx, prob.V, self.ops)
@@ -182,7 +187,7 @@ class StokesBatchSystem:
     def assemble(self):
         api.assemble(self.A, self.ops, L.FP64)
         if self.mixed:
-            api.assemble(self.A, self.ops, L.FP32)
+            api.assemble(self.A, self.ops[:1] if self.split_penalty else self.ops, L.FP32)
         self.bf.fill(0.0)
         r = L.Rhs()
         r.kind = L.RHS_POLY
@@ -218,6 +223,7 @@ class StokesBatchSystem:
         P.inner_reltol = inner_reltol
         P.maxiter = maxiter
         P.block_threads = block_threads
+        P.split_penalty = 1 if self.split_penalty else 0
         st = L.StokesBatchStats()
         its = np.zeros(self.prob.nproblems, dtype=np.int32)
         rc = self.ctx.lib.grmp_stokes_batch_solve(self.A.h, self.bf.h, self.u.h, self.p.h, ctypes.byref(P),
@@ -226,7 +232,7 @@ class StokesBatchSystem:
         out = {"rc": rc, "status": st.status, "max_iterations": st.max_iterations,
                "total_iterations": st.total_iterations, "max_sweeps": st.max_sweeps,
                "failed": st.failed_problems, "max_relres": st.max_relres, "solve_ms": st.solve_ms,
-               "iterations": its}
+               "fp64_fallbacks": st.fp64_fallbacks, "iterations": its}
         if raise_on_error:
             self.ctx.check(rc)
         return out

@@ -234,7 +234,8 @@ typedef struct {
     int32_t mode;           /* grmp_solve_mode                                           */
     double inner_reltol;    /* MIXED: residual reduction per refinement (reliable update) */
     int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
-    int32_t spmv_chunk;     /* SpMV nonzeros streamed per warp pass (64/128/256): 0 = autotuned */
+    int32_t spmv_config;    /* SpMV lanes per row and loads in flight, coded 100*lanes + loads:
+                               208, 404, 408, 804 or 1602; 0 = autotuned per matrix and mode */
     int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
     int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
 } grmp_solve_params;
@@ -243,7 +244,7 @@ typedef struct {
     int32_t status;          /* grmp_status of the solve                     */
     int32_t iterations;      /* inner (or plain) iterations                  */
     int32_t outer_iterations;/* FP64 refinement steps (MIXED)                */
-    int32_t spmv_chunk;      /* SpMV configuration used                      */
+    int32_t spmv_config;     /* SpMV configuration used (100*lanes + loads)  */
     int32_t grid_blocks;
     double final_relres;     /* ||b - A x|| / ||b|| in FP64 at exit          */
     double solve_ms;         /* device time of the solve                     */
@@ -278,6 +279,13 @@ typedef struct {
     double inner_reltol;         /* MIXED: refinement trigger                                          */
     int32_t maxiter;             /* inner iteration cap per sweep                                       */
     int32_t block_threads;       /* threads per problem (0 = 512)                                       */
+    int32_t split_penalty;       /* MIXED: 0 = A's FP32 values hold the whole velocity operator;
+                                    1 = they hold (nu grad u, grad v) alone and the inner FP32 operator
+                                    applies lambda (div R u, div R v) per cell in factored form
+                                    sum_T lambda/|T| (D_T.u)(D_T.v), D_T[I] = int_T div phi_I, which
+                                    stays exact on divergence-free fields (needed when lambda/nu is
+                                    large: FP32 rounding of the assembled penalty swamps the viscous
+                                    term there)                                                      */
 } grmp_stokes_batch_params;
 
 typedef struct {
@@ -288,6 +296,8 @@ typedef struct {
     int32_t failed_problems;     /* problems that hit a cap                   */
     double max_relres;           /* worst final inner relative residual       */
     double solve_ms;
+    int32_t fp64_fallbacks;      /* MIXED: inner solves that stalled in FP32 and
+                                    were finished by FP64 PCG from the same iterate */
 } grmp_stokes_batch_stats;
 
 /* Iterated-penalty Stokes solve of many independent Bernardi-Raugel / P0
@@ -307,6 +317,56 @@ typedef struct {
 int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vector u, grmp_vector p,
                             const grmp_stokes_batch_params *params, int32_t *iterations_per_problem,
                             grmp_stokes_batch_stats *stats);
+
+/* ---------------------------------------------------------------- serving */
+
+typedef struct grmp_server_s *grmp_server;
+
+/* One assembly + solve request (a solve_direct! of a linear problem,
+ * src/solvers.jl:622-686).  All arrays are host arrays, copied at submit;
+ * term cell coefficients must be host arrays (coef_on_device = 0). */
+typedef struct {
+    int dim;
+    int32_t nverts;
+    const double *coords;       /* [nverts][dim]          */
+    int32_t ncells;
+    const int32_t *cells;       /* [ncells][dim+1]        */
+    int fe_kind;
+    int ncomponents;
+    int32_t ndofs;
+    const int32_t *celldofs;    /* [ncells][ndofs4cell]   */
+    int nterms;
+    const grmp_bilinear_term *terms;
+    grmp_rhs rhs;               /* cell_group not allowed */
+    int32_t nfixed;
+    const int32_t *fixed;       /* homogeneous Dirichlet DoFs (eliminated) */
+    grmp_solve_params solve;
+} grmp_request;
+
+typedef struct {
+    int32_t status;             /* grmp_status of the request               */
+    int32_t slot;               /* worker that ran it                       */
+    int32_t iterations, outer_iterations;
+    double final_relres;
+    double queue_ms;            /* submit -> admission                       */
+    double run_ms;              /* admission -> result                       */
+    double latency_ms;          /* submit -> result                          */
+    double solve_ms;            /* device time of the solve                  */
+} grmp_request_stats;
+
+/* A serving loop with `nslots` concurrent slots (one stream each) on device
+ * `device`, admitting requests while their estimated device footprint fits in
+ * `hbm_budget_bytes` (0 = unlimited).  No reference counterpart. */
+int grmp_server_create(int device, size_t hbm_budget_bytes, int nslots, grmp_server *out);
+/* Queue a request (copied); returns its id at once.  GRMP_ERR_BUDGET if it
+ * can never fit. */
+int grmp_server_submit(grmp_server srv, const grmp_request *req, int64_t *id);
+/* Wait for a request (timeout_s < 0: forever); x_out [ndofs] receives the
+ * solution.  Returns the request's status (GRMP_ERR_TIMEOUT if still
+ * running after timeout_s; it can be waited for again). */
+int grmp_server_wait(grmp_server srv, int64_t id, double timeout_s, double *x_out, grmp_request_stats *stats);
+/* Stop the workers (running requests finish first) and free the server. */
+int grmp_server_destroy(grmp_server srv);
 
 #ifdef __cplusplus
 }
