@@ -22,6 +22,7 @@ FP64, FP32 = 0, 1
 RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
 DIRICHLET_PENALTY, DIRICHLET_ELIMINATE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
+NOALLOC_MAX_ROWS = 262144   # GRMP_NOALLOC_MAX_ROWS
 
 
 class GrmpError(RuntimeError):
@@ -123,6 +124,8 @@ SIGNATURES = {
     "grmp_solve_params_default": ([ctypes.POINTER(SolveParams)], ctypes.c_int),
     "grmp_solve": ([_vp, _vp, _vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveStats)], ctypes.c_int),
     "grmp_spmv": ([_vp, ctypes.c_int, _vp, _vp], ctypes.c_int),
+    "grmp_solve_fp64_noalloc": ([_vp, _vp, _vp, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveStats)],
+                                ctypes.c_int),
     "grmp_stokes_batch_solve": ([_vp, _vp, _vp, _vp, ctypes.POINTER(StokesBatchParams), _pi32,
                                  ctypes.POINTER(StokesBatchStats)], ctypes.c_int),
     "grmp_server_create": ([ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),

@@ -17,6 +17,10 @@
 // take identical decisions and results are reproducible run to run.
 #include <cooperative_groups.h>
 
+#include <chrono>
+#include <cstring>
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <type_traits>
@@ -664,4 +668,133 @@ int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
     GRMP_CUDA(ctx, cudaGetLastError());
     GRMP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return GRMP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 PCG without device allocation (grmp_solve_fp64_noalloc).
+//
+// The work arrays are a file-scope device array sized for
+// GRMP_NOALLOC_MAX_ROWS rows, laid out like the FP64 workspace of
+// grmp_solve_impl:
+//   [0, 5V)           dinv r z p q   (V = GRMP_NOALLOC_MAX_ROWS doubles each)
+//   [5V, 5V+P)        per-block reduction partials (4 x 4096 doubles)
+//   [5V+P, +256)      SolveState: grid-barrier counters + status  (zeroed per call)
+//   [5V+P+256, +256)  diagonal check flag                          (zeroed per call)
+// The array's address is looked up once per device; the first call makes
+// that lookup with the context's device current.
+namespace {
+
+constexpr size_t kNaVec = (size_t)GRMP_NOALLOC_MAX_ROWS * 8;
+constexpr size_t kNaPart = (size_t)4 * 8 * 4096;
+constexpr size_t kNaState = 5 * kNaVec + kNaPart;
+constexpr size_t kNaFlag = kNaState + 256;
+constexpr size_t kNaBytes = kNaFlag + 256;
+static_assert(kNaVec % 256 == 0 && sizeof(SolveState) <= 256, "scratch layout");
+
+__device__ __align__(256) char g_noalloc_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mu;
+char *g_na_ptr[kNaMaxDevices] = {};
+
+int noalloc_scratch(grmp_context ctx, char **out) {
+    if (ctx->device < 0 || ctx->device >= kNaMaxDevices)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "noalloc solve: device ordinal %d out of range", ctx->device);
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_ptr[ctx->device]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) return grmp_cuda_fail(ctx, e, "noalloc solve: scratch address lookup");
+        g_na_ptr[ctx->device] = (char *)ptr;
+    }
+    *out = g_na_ptr[ctx->device];
+    return GRMP_OK;
+}
+
+template <int TPR, int U>
+cudaError_t launch_pcg64_static(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
+                                char *work, int *grid_out) {
+    grmp_context ctx = A->space->mesh->ctx;
+    auto kern = k_pcg64<TPR, U>;
+    int grid = coop_grid(ctx, kern, A->nrows, p->grid_blocks);
+    double *dinv = (double *)work, *r = (double *)(work + kNaVec), *z = (double *)(work + 2 * kNaVec);
+    double *pp = (double *)(work + 3 * kNaVec), *q = (double *)(work + 4 * kNaVec);
+    double *part = (double *)(work + 5 * kNaVec);
+    SolveState *dst = (SolveState *)(work + kNaState);
+    int nn = A->nrows, mi = p->maxiter, guess = p->use_initial_guess ? 1 : 0;
+    double at = p->abstol, rt = p->reltol;
+    const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+    const double *vv = A->d_vals64, *bb = bvec;
+    double *xx = xvec;
+    void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess};
+    *grid_out = grid;
+    cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+    GRMP_LAUNCHED(ctx);
+    return e;
+}
+
+}  // namespace
+
+extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p,
+                                       grmp_solve_stats *st) {
+    if (!A || !b || !x || !p) return GRMP_ERR_INVALID_ARG;
+    grmp_context ctx = A->space->mesh->ctx;
+    grmp_solve_stats local;
+    if (!st) st = &local;
+    std::memset(st, 0, sizeof(*st));
+    if (b->n != A->nrows || x->n != A->nrows) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: size mismatch");
+    if (p->mode != GRMP_SOLVE_FP64)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "noalloc solve: only mode GRMP_SOLVE_FP64");
+    if (!(p->reltol >= 0) || !(p->abstol >= 0) || p->maxiter <= 0) return GRMP_ERR_INVALID_ARG;
+    if (A->nrows > GRMP_NOALLOC_MAX_ROWS)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: %d rows exceed the fixed scratch limit of %d rows",
+                         A->nrows, GRMP_NOALLOC_MAX_ROWS);
+    if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: FP64 values not assembled");
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaSetDevice(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    char *work = nullptr;
+    int rc = noalloc_scratch(ctx, &work);
+    if (rc) return rc;
+    const int n = A->nrows;
+    SolveState *dst = (SolveState *)(work + kNaState);
+    int *bad = (int *)(work + kNaFlag);
+    cudaError_t e = cudaMemsetAsync(work + kNaState, 0, 512, ctx->stream);   // state + flag start at zero
+    if (e == cudaSuccess) {
+        k_dinv<double><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, (double *)work, bad);
+        GRMP_LAUNCHED(ctx);
+        e = cudaGetLastError();
+    }
+    int hbad = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "noalloc solve: jacobi diagonal");
+    if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: non-positive or non-finite diagonal entry");
+    int cfg = p->spmv_config > 0 ? p->spmv_config : (A->tuned_cfg ? A->tuned_cfg : heuristic_config(A));
+    int grid = 0;
+    switch (cfg) {
+        case 208: e = launch_pcg64_static<2, 8>(A, b->d, x->d, p, work, &grid); break;
+        case 404: e = launch_pcg64_static<4, 4>(A, b->d, x->d, p, work, &grid); break;
+        case 408: e = launch_pcg64_static<4, 8>(A, b->d, x->d, p, work, &grid); break;
+        case 804: e = launch_pcg64_static<8, 4>(A, b->d, x->d, p, work, &grid); break;
+        case 1602: e = launch_pcg64_static<16, 2>(A, b->d, x->d, p, work, &grid); break;
+        default: return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_config must be one of 208 404 408 804 1602");
+    }
+    SolveState hs;
+    std::memset(&hs, 0, sizeof(hs));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "noalloc solve: persistent PCG launch");
+    st->status = hs.status;
+    st->iterations = hs.iters;
+    st->outer_iterations = 0;
+    st->final_relres = hs.relres;
+    st->spmv_config = cfg;
+    st->grid_blocks = grid;
+    st->solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (hs.status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, GRMP_ERR_NOT_CONVERGED, "PCG: %d iterations, relative residual %.3e", hs.iters, hs.relres);
+    if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a grid barrier wait timed out");
+    if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
+    return hs.status;
 }

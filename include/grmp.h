@@ -265,6 +265,32 @@ int grmp_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
  * src/solvers.jl:664-668). */
 int grmp_spmv(grmp_matrix A, int precision, grmp_vector x, grmp_vector y);
 
+/* Largest system grmp_solve_fp64_noalloc accepts (rows). */
+#define GRMP_NOALLOC_MAX_ROWS 262144
+
+/* FP64 Jacobi-PCG like grmp_solve with mode GRMP_SOLVE_FP64, but without
+ * any device-memory allocation: its work arrays live in a fixed scratch
+ * area of about 10.6 MB that is part of the loaded library on each device.
+ * No counterpart in the reference (its solves allocate freely).
+ *   - For callers that must not allocate during a solve: hosts whose own
+ *     memory pool has taken the device's free memory, or time-stepping loops
+ *     that cannot afford an allocation failing or stalling mid-step.
+ *   - Systems up to GRMP_NOALLOC_MAX_ROWS rows; larger ones are rejected
+ *     with GRMP_ERR_INVALID_ARG.  params->mode must be GRMP_SOLVE_FP64
+ *     (GRMP_ERR_UNSUPPORTED otherwise).  spmv_config 0 uses the matrix's
+ *     tuned configuration if grmp_solve has tuned it, else a heuristic; no
+ *     tuning runs here.
+ *   - The first call on a device looks up the scratch address (set-up);
+ *     make it before any stream capture on that device begins.
+ *   - The grid-barrier counters, the status word and the diagonal check flag
+ *     in the scratch must start at zero; every call zeroes them itself.
+ *   - Calls that overlap in time on the same device (e.g. from two host
+ *     threads with two contexts) share the one scratch area and race: the
+ *     caller must serialise them.
+ *   - stats->solve_ms is host wall time of the whole call. */
+int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *params,
+                            grmp_solve_stats *stats);
+
 /* ------------------------------------------------- batched Stokes (BR/P0) */
 
 typedef struct {
