@@ -196,8 +196,16 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one
+# k_pcg_mixed launch on the 48^3 case divided by pcg_bytes() of the same
+# launch: 183.94 GB / 185.02 GB (summary under profiles/).
+TRAFFIC_PER_ALGORITHMIC_BYTE = 183.94 / 185.02
+
+
 def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool) -> float:
-    """Algorithmic DRAM bytes of one persistent PCG launch."""
+    """Algorithmic DRAM bytes of one persistent PCG launch: per inner
+    iteration the matrix once (values + column indices) and the vector
+    traffic of the update phase; per FP64 refinement one FP64 residual."""
     it, outer = stats["iterations"], stats["outer_iterations"]
     if mixed:
         per_it = 8.0 * nnz + 56.0 * n
@@ -277,8 +285,12 @@ def run_ours(args):
     results = {}
     if args.profile:
         # profiling run: the mixed path only, no host-side extras (for ncu)
-        for _ in range(max(3, args.warmup) + args.steps):
-            step("mixed")
+        for k in range(max(3, args.warmup) + args.steps):
+            st, _ = step("mixed")
+            # iteration counts let a capture's DRAM bytes be set against the algorithmic bytes
+            print(json.dumps({"profile_step": k, "ndofs": ndofs, "nnz": nnz, "iterations": st["iterations"],
+                              "outer": st["outer_iterations"], "spmv_config": st["spmv_config"],
+                              "algorithmic_bytes": pcg_bytes(st, ndofs, nnz, True)}), flush=True)
         torch.cuda.synchronize()
         ctx.close()
         dist.close()
@@ -364,7 +376,10 @@ def run_ours(args):
             "solver": {"iterations": st_last["iterations"], "outer": st_last["outer_iterations"],
                        "spmv_config": st_last["spmv_config"], "grid_blocks": st_last["grid_blocks"]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "k_pcg_mixed (persistent)",
+                         "frac": achieved / peak, "traffic": kb * TRAFFIC_PER_ALGORITHMIC_BYTE,
+                         "traffic_source": "ncu dram__bytes_read+write of k_pcg_mixed on the 48^3 case "
+                                           "(0.994 x its algorithmic bytes), scaled to this launch",
+                         "kernel": "k_pcg_mixed (persistent)",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"},
             "cpu_baseline": cpu,
             "e2e": {"value": world_dofs / e2e_tot, "unit": "DoF/s",

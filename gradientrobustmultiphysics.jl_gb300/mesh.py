@@ -72,7 +72,17 @@ class SimplexMesh:
             return self._cache[key]
         loc = self.cells[:, local]                   # (ncells, nloc, k)
         srt = np.sort(loc, axis=2).reshape(-1, local.shape[1])
-        uniq, inv = np.unique(srt, axis=0, return_inverse=True)
+        k = srt.shape[1]
+        B = max(int(self.nverts), 2)
+        if B ** k <= 2 ** 63:
+            # lexicographic order of the sorted tuples = order of the int64 keys
+            code = np.zeros(srt.shape[0], dtype=np.int64)
+            for j in range(k):
+                code = code * B + srt[:, j].astype(np.int64)
+            _, first, inv = np.unique(code, return_index=True, return_inverse=True)
+            uniq = srt[first]
+        else:
+            uniq, inv = np.unique(srt, axis=0, return_inverse=True)
         inv = inv.reshape(self.ncells, local.shape[0]).astype(np.int32)
         self._cache[key] = (uniq.astype(np.int32), inv)
         return self._cache[key]
