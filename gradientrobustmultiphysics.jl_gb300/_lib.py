@@ -21,7 +21,7 @@ OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV = 1, 2, 3, 4
 FP64, FP32 = 0, 1
 RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
 DIRICHLET_PENALTY, DIRICHLET_ELIMINATE = 0, 1
-SOLVE_FP64, SOLVE_MIXED = 0, 1
+SOLVE_FP64, SOLVE_MIXED, SOLVE_DIRECT = 0, 1, 2
 NOALLOC_MAX_ROWS = 262144   # GRMP_NOALLOC_MAX_ROWS
 
 
@@ -129,6 +129,7 @@ SIGNATURES = {
     "grmp_stokes_batch_solve": ([_vp, _vp, _vp, _vp, ctypes.POINTER(StokesBatchParams), _pi32,
                                  ctypes.POINTER(StokesBatchStats)], ctypes.c_int),
     "grmp_server_create": ([ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+    "grmp_server_request_bytes": ([ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "grmp_server_submit": ([_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "grmp_server_wait": ([_vp, ctypes.c_int64, ctypes.c_double, _pd, ctypes.POINTER(RequestStats)], ctypes.c_int),
     "grmp_server_destroy": ([_vp], ctypes.c_int),

@@ -16,10 +16,14 @@
 // reductions are block reductions in a fixed order, so its result does not
 // depend on which block runs it or on the rest of the batch.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <numeric>
+#include <thread>
+#include <tuple>
 
 #include "grmp_internal.h"
+#include "nd_symbolic.h"
 
 int grmp_br_divergence(grmp_space s, double **Dv, double **vol);
 
@@ -450,6 +454,54 @@ __device__ int block_pcg64(const BatchDev &d, int r0, int r1, const double *rhs,
     return it;
 }
 
+// rhs = (f, R v) + (p, div v) on the free rows of one problem
+__device__ __forceinline__ void block_sweep_rhs(const BatchDev &d, int r0, int r1) {
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        double acc = d.bf[i];
+        if (!d.fixed[i])
+            for (int q = d.inc_ptr[i]; q < d.inc_ptr[i + 1]; q++) {
+                const int cell = d.inc_cell[q];
+                acc += d.Dv[(size_t)cell * 9 + d.inc_loc[q]] * d.p[cell];
+            }
+        d.rhs[i] = acc;
+    }
+    __syncthreads();
+}
+
+// Pressure update p <- p - lambda (1/|T|) int_T div u, then zero mean.
+// Returns true when the sweep tolerance is met (change of p from the
+// divergence <= sweep_tol * |p|, both in the volume-weighted norm).
+__device__ __forceinline__ bool block_pressure_update(const BatchDev &d, int c0, int c1, double *sh) {
+    const int tid = threadIdx.x, bs = blockDim.x;
+    double m[3] = {0, 0, 0};   // sum vol*p_new, sum vol
+    for (int c = c0 + tid; c < c1; c += bs) {
+        double dv = 0;
+        for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
+        const double dp = d.lambda * dv / d.vol[c];
+        const double pn = d.p[c] - dp;
+        d.p[c] = pn;
+        m[0] += d.vol[c] * pn;
+        m[1] += d.vol[c];
+    }
+    bsum<2>(m, sh);
+    const double mean = m[0] / m[1];
+    double cmp[2] = {0, 0};
+    for (int c = c0 + tid; c < c1; c += bs) {
+        const double pn = d.p[c] - mean;
+        d.p[c] = pn;
+        cmp[1] += d.vol[c] * pn * pn;
+    }
+    // change of the pressure in this sweep (after the mean shift) from the divergence
+    for (int c = c0 + tid; c < c1; c += bs) {
+        double dv = 0;
+        for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
+        const double dp = d.lambda * dv / d.vol[c];
+        cmp[0] += d.vol[c] * dp * dp;
+    }
+    bsum<2>(cmp, sh);
+    return d.sweep_tol > 0 && sqrt(cmp[0]) <= d.sweep_tol * sqrt(cmp[1]);
+}
+
 template <int TPR>
 __global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
     __shared__ double sh[32 * 4];
@@ -495,17 +547,7 @@ __global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
         double worst = 0.0;
         bool all_ok = true;
         for (sweep = 0; sweep < d.sweeps; sweep++) {
-            // rhs = (f, R v) + (p, div v) on the free rows
-            for (int i = r0 + tid; i < r1; i += bs) {
-                double acc = d.bf[i];
-                if (!d.fixed[i])
-                    for (int q = d.inc_ptr[i]; q < d.inc_ptr[i + 1]; q++) {
-                        const int cell = d.inc_cell[q];
-                        acc += d.Dv[(size_t)cell * 9 + d.inc_loc[q]] * d.p[cell];
-                    }
-                d.rhs[i] = acc;
-            }
-            __syncthreads();
+            block_sweep_rhs(d, r0, r1);
             double rr;
             bool ok;
             int it = !d.mixed ? block_pcg64<TPR>(d, r0, r1, d.rhs, d.u, sh, &rr, &ok)
@@ -521,34 +563,7 @@ __global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
             worst = fmax(worst, rr);
             all_ok = all_ok && ok;
             __syncthreads();
-            // pressure update and zero mean
-            double m[3] = {0, 0, 0};   // sum vol*p_new, sum vol, sum (dp)^2 vol
-            for (int c = c0 + tid; c < c1; c += bs) {
-                double dv = 0;
-                for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
-                const double dp = d.lambda * dv / d.vol[c];
-                const double pn = d.p[c] - dp;
-                d.p[c] = pn;
-                m[0] += d.vol[c] * pn;
-                m[1] += d.vol[c];
-            }
-            bsum<2>(m, sh);
-            const double mean = m[0] / m[1];
-            double cmp[2] = {0, 0};
-            for (int c = c0 + tid; c < c1; c += bs) {
-                const double pn = d.p[c] - mean;
-                d.p[c] = pn;
-                cmp[1] += d.vol[c] * pn * pn;
-            }
-            // change of the pressure in this sweep (after the mean shift) from the divergence
-            for (int c = c0 + tid; c < c1; c += bs) {
-                double dv = 0;
-                for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
-                const double dp = d.lambda * dv / d.vol[c];
-                cmp[0] += d.vol[c] * dp * dp;
-            }
-            bsum<2>(cmp, sh);
-            if (d.sweep_tol > 0 && sqrt(cmp[0]) <= d.sweep_tol * sqrt(cmp[1])) {
+            if (block_pressure_update(d, c0, c1, sh)) {
                 sweep++;
                 break;
             }
@@ -564,6 +579,310 @@ __global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
     }
 }
 
+// ------------------------------------------------------------------------
+// Direct mode: one multifrontal Cholesky factorisation per problem (nested-
+// dissection assembly tree from nd_symbolic.cpp), reused by every sweep.
+
+struct DNode {
+    int s, f, front_off, child_off, nchild, entry_off, nentry, ext_off;
+    long long L_off, U_off;
+};
+
+// A sweep whose refined residual stagnates (FP64 rounding floor of the
+// system) counts as solved when the floor is at most this relative residual.
+constexpr double kDirectFloorMax = 1e-6;
+
+struct DirectDev {
+    const DNode *node;
+    const int32_t *front, *child, *ent_rel, *ent_pos, *ext;
+    const int32_t *prob_node0, *prob_nnodes;
+    double *work;                                   // per resident block: [F | U | L]
+    long long slot_doubles, F_doubles, U_doubles;
+    int max_f, max_s, max_solves;
+};
+
+__device__ __forceinline__ double warp_sum64(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Numeric factorisation of one problem: for every node in post-order,
+// assemble the front (original entries + children's update matrices),
+// eliminate its own DoFs (right-looking dense Cholesky), keep the factor
+// columns and the update matrix.  Returns false on a non-positive pivot.
+__device__ bool mf_factor(const BatchDev &d, const DirectDev &m, int nb, int ne, long long nnz0, double *F, double *U,
+                          double *L, double *colk) {
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    for (int t = nb; t < ne; t++) {
+        const DNode nd = m.node[t];
+        const int f = nd.f, s = nd.s;
+        for (long long q = tid; q < (long long)f * f; q += bs) F[q] = 0.0;
+        __syncthreads();
+        for (int e = tid; e < nd.nentry; e += bs)
+            F[m.ent_pos[nd.entry_off + e]] = d.v64[nnz0 + m.ent_rel[nd.entry_off + e]];
+        __syncthreads();
+        for (int q = 0; q < nd.nchild; q++) {
+            const DNode cn = m.node[m.child[nd.child_off + q]];
+            const int sc = cn.f - cn.s;
+            const double *Uc = U + cn.U_off;
+            const int32_t *ex = m.ext + cn.ext_off;
+            for (int a = warp; a < sc; a += nw) {
+                const long long pa = (long long)ex[a] * f;
+                for (int b = lane; b <= a; b += 32) F[pa + ex[b]] += Uc[(long long)a * sc + b];
+            }
+            __syncthreads();
+        }
+        for (int k = 0; k < s; k++) {
+            const double dkk = F[(long long)k * f + k];   // every thread reads the same value
+            if (!(dkk > 0.0) || !isfinite(dkk)) return false;
+            const double dk = sqrt(dkk);
+            for (int i = k + 1 + tid; i < f; i += bs) {
+                const double v = F[(long long)i * f + k] / dk;
+                F[(long long)i * f + k] = v;
+                colk[i] = v;
+            }
+            __syncthreads();
+            if (tid == 0) F[(long long)k * f + k] = dk;
+            for (int i = k + 1 + warp; i < f; i += nw) {
+                const double lik = colk[i];
+                double *Fi = F + (long long)i * f;
+                for (int j = k + 1 + lane; j <= i; j += 32) Fi[j] -= lik * colk[j];
+            }
+            __syncthreads();
+        }
+        double *Lt = L + nd.L_off;
+        for (long long q = tid; q < (long long)f * s; q += bs) {
+            const int i = (int)(q / s), j = (int)(q - (long long)i * s);
+            Lt[q] = j <= i ? F[(long long)i * f + j] : 0.0;
+        }
+        const int sc = f - s;
+        double *Ut = U + nd.U_off;
+        for (long long q = tid; q < (long long)sc * sc; q += bs) {
+            const int a = (int)(q / sc), b = (int)(q - (long long)a * sc);
+            if (b <= a) Ut[q] = F[(long long)(s + a) * f + s + b];
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// w <- A^{-1} w for one problem (w indexed by the problem's local DoF):
+// forward L y = w in post-order, backward L^T x = y in reverse order; the
+// dense triangles are solved in 32-row blocks (block rows by all warps, the
+// diagonal block by warp 0 from a shared-memory tile).
+__device__ void mf_solve(const DirectDev &m, int nb, int ne, double *w, const double *L, double *ys, double *xs,
+                         double *tile) {
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    for (int t = nb; t < ne; t++) {
+        const DNode nd = m.node[t];
+        const int f = nd.f, s = nd.s;
+        const int32_t *fr = m.front + nd.front_off;
+        const double *Lt = L + nd.L_off;
+        for (int k = tid; k < s; k += bs) ys[k] = w[fr[k]];
+        __syncthreads();
+        for (int kb = 0; kb < s; kb += 32) {
+            const int nbk = min(32, s - kb);
+            if (kb > 0)
+                for (int r = warp; r < nbk; r += nw) {
+                    const double *Li = Lt + (long long)(kb + r) * s;
+                    double acc = 0.0;
+                    for (int j = lane; j < kb; j += 32) acc += Li[j] * ys[j];
+                    acc = warp_sum64(acc);
+                    if (lane == 0) ys[kb + r] -= acc;
+                }
+            for (int q = tid; q < nbk * nbk; q += bs) {
+                const int r = q / nbk, c = q - r * nbk;
+                tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : 0.0;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                double v = lane < nbk ? ys[kb + lane] : 0.0;
+                for (int c = 0; c < nbk; c++) {
+                    const double yc = __shfl_sync(0xffffffffu, v, c) / tile[c * 33 + c];
+                    if (lane == c) v = yc;
+                    else if (lane > c && lane < nbk) v -= tile[lane * 33 + c] * yc;
+                }
+                if (lane < nbk) ys[kb + lane] = v;
+            }
+            __syncthreads();
+        }
+        for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+        for (int i = s + warp; i < f; i += nw) {
+            const double *Li = Lt + (long long)i * s;
+            double acc = 0.0;
+            for (int k = lane; k < s; k += 32) acc += Li[k] * ys[k];
+            acc = warp_sum64(acc);
+            if (lane == 0) w[fr[i]] -= acc;
+        }
+        __syncthreads();
+    }
+    for (int t = ne - 1; t >= nb; t--) {
+        const DNode nd = m.node[t];
+        const int f = nd.f, s = nd.s, sc = f - s;
+        const int32_t *fr = m.front + nd.front_off;
+        const double *Lt = L + nd.L_off;
+        for (int i = tid; i < sc; i += bs) xs[i] = w[fr[s + i]];
+        __syncthreads();
+        for (int k = tid; k < s; k += bs) {
+            double acc = w[fr[k]];
+            for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
+            ys[k] = acc;
+        }
+        __syncthreads();
+        for (int kb = ((s + 31) / 32 - 1) * 32; kb >= 0; kb -= 32) {
+            const int nbk = min(32, s - kb);
+            for (int q = tid; q < nbk * nbk; q += bs) {
+                const int r = q / nbk, c = q - r * nbk;
+                tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : 0.0;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                double v = lane < nbk ? ys[kb + lane] : 0.0;
+                for (int c = nbk - 1; c >= 0; c--) {
+                    const double xc = __shfl_sync(0xffffffffu, v, c) / tile[c * 33 + c];
+                    if (lane == c) v = xc;
+                    else if (lane < c) v -= tile[c * 33 + lane] * xc;
+                }
+                if (lane < nbk) ys[kb + lane] = v;
+            }
+            __syncthreads();
+            for (int k = tid; k < kb; k += bs) {
+                double acc = 0.0;
+                for (int r = 0; r < nbk; r++) acc += Lt[(long long)(kb + r) * s + k] * ys[kb + r];
+                ys[k] -= acc;
+            }
+            __syncthreads();
+        }
+        for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+        __syncthreads();
+    }
+}
+
+template <int TPR>
+__global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev m) {
+    extern __shared__ double dsm[];
+    __shared__ double sh[32 * 4];
+    __shared__ int slot;
+    double *colk = dsm;                 // factor: column k of the front; solve: structure values
+    double *ys = dsm + m.max_f;
+    double *tile = ys + m.max_s;
+    double *F = m.work + (long long)blockIdx.x * m.slot_doubles;
+    double *U = F + m.F_doubles, *L = U + m.U_doubles;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    while (true) {
+        if (tid == 0) slot = atomicAdd(d.queue, 1);
+        __syncthreads();
+        const int k = slot;
+        __syncthreads();
+        if (k >= d.nprob) break;
+        const int pid = d.order[k];
+        const int r0 = d.row_off[pid], r1 = d.row_off[pid + 1];
+        const int c0 = d.cell_off[pid], c1 = d.cell_off[pid + 1];
+        const int nb = m.prob_node0[pid], ne = nb + m.prob_nnodes[pid];
+        for (int i = r0 + tid; i < r1; i += bs) d.u[i] = 0.0;
+        for (int c = c0 + tid; c < c1; c += bs) d.p[c] = 0.0;
+        __syncthreads();
+        const bool fact_ok = mf_factor(d, m, nb, ne, (long long)d.rowptr[r0], F, U, L, colk);
+        __syncthreads();
+        int nsolve = 0, sweep = 0;
+        double worst = 0.0;
+        bool all_ok = fact_ok;
+        if (fact_ok)
+            for (sweep = 0; sweep < d.sweeps; sweep++) {
+                block_sweep_rhs(d, r0, r1);
+                double bb[1] = {0.0};
+                for (int i = r0 + tid; i < r1; i += bs) bb[0] += d.rhs[i] * d.rhs[i];
+                bsum<1>(bb, sh);
+                const double bn = sqrt(bb[0]);
+                double rel = 0.0, prev = INFINITY;
+                bool floor = false;
+                for (int ref = 0;; ref++) {
+                    // r = rhs - A u (FP64, assembled matrix); stop at reltol or when the
+                    // residual stops falling (the FP64 floor of an ill-conditioned
+                    // system), else u += A^{-1} r
+                    double v[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, d.r64, nullptr, d.rhs)};
+                    bsum<1>(v, sh);
+                    rel = bn > 0 ? sqrt(v[0]) / bn : 0.0;
+                    if (rel <= d.reltol) break;
+                    if (ref > 0 && rel > 0.5 * prev) {
+                        floor = true;
+                        break;
+                    }
+                    if (ref >= m.max_solves) break;
+                    prev = rel;
+                    mf_solve(m, nb, ne, d.r64 + r0, L, ys, colk, tile);
+                    for (int i = r0 + tid; i < r1; i += bs) d.u[i] += d.r64[i];
+                    __syncthreads();
+                    nsolve++;
+                }
+                worst = fmax(worst, rel);
+                all_ok = all_ok && (rel <= d.reltol || (floor && rel <= kDirectFloorMax));
+                if (block_pressure_update(d, c0, c1, sh)) {
+                    sweep++;
+                    break;
+                }
+            }
+        if (tid == 0) {
+            d.iters[pid] = nsolve;
+            d.sweeps_done[pid] = sweep;
+            d.relres[pid] = fact_ok ? worst : INFINITY;
+            d.fallbacks[pid] = 0;
+            d.status[pid] = !fact_ok ? (int)GRMP_ERR_NAN : (all_ok ? 0 : (int)GRMP_ERR_NOT_CONVERGED);
+        }
+        __syncthreads();
+    }
+}
+
+// 64-bit fingerprint of each problem's local pattern (row lengths and
+// row-relative columns), summed over nonzeros so the reduction order does
+// not matter.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+__global__ void k_pattern_hash(int nprob, const int32_t *row_off, const int32_t *rowptr, const int32_t *cols,
+                               unsigned long long *hash) {
+    const int pid = blockIdx.x;
+    if (pid >= nprob) return;
+    const int r0 = row_off[pid], r1 = row_off[pid + 1];
+    const long long nnz0 = rowptr[r0];
+    unsigned long long h = 0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++)
+            h += mix64(((unsigned long long)(k - nnz0) << 32) ^ (unsigned long long)(uint32_t)(cols[k] - r0) ^
+                       ((unsigned long long)(i - r0) << 52));
+    atomicAdd(hash + pid, h);
+}
+
+// bad[p] = 1 when problem p's local pattern differs from problem rep[p]'s
+__global__ void k_pattern_equal(int nprob, const int32_t *row_off, const int32_t *rowptr, const int32_t *cols,
+                                const int32_t *rep, int *bad) {
+    const int pid = blockIdx.x;
+    if (pid >= nprob) return;
+    const int q = rep[pid];
+    if (q == pid) return;
+    const int r0 = row_off[pid], s0 = row_off[q];
+    const int n = row_off[pid + 1] - r0;
+    if (n != row_off[q + 1] - s0) {
+        if (threadIdx.x == 0) bad[pid] = 1;
+        return;
+    }
+    const long long a0 = rowptr[r0], b0 = rowptr[s0];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int ka = rowptr[r0 + i], kb = rowptr[s0 + i];
+        const int la = rowptr[r0 + i + 1] - ka, lb = rowptr[s0 + i + 1] - kb;
+        if (la != lb || ka - a0 != kb - b0) {
+            bad[pid] = 1;
+            continue;
+        }
+        for (int j = 0; j < la; j++)
+            if (cols[ka + j] - r0 != cols[kb + j] - s0) bad[pid] = 1;
+    }
+}
+
 __global__ void k_check_blocks(int nprob, const int32_t *row_off, const int32_t *rowptr, const int32_t *cols,
                                int *bad) {
     int pid = blockIdx.x;
@@ -575,6 +894,203 @@ __global__ void k_check_blocks(int nprob, const int32_t *row_off, const int32_t 
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------- direct-mode symbolic cache
+
+struct DirectCache {
+    std::vector<int32_t> row_offsets;
+    std::vector<std::pair<void *, size_t>> bufs;
+    const DNode *node = nullptr;
+    const int32_t *front = nullptr, *child = nullptr, *ent_rel = nullptr, *ent_pos = nullptr, *ext = nullptr;
+    const int32_t *prob_node0 = nullptr, *prob_nnodes = nullptr;
+    long long max_U = 0, max_L = 0;
+    int max_f = 0, max_s = 0, groups = 0;
+};
+
+namespace {
+
+template <typename T>
+int upload_vec(grmp_context ctx, DirectCache &C, const std::vector<T> &v, const T **out) {
+    T *p = nullptr;
+    const size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+    int rc = grmp_alloc(ctx, (void **)&p, bytes);
+    if (rc) return rc;
+    C.bufs.push_back({p, bytes});
+    if (!v.empty()) {
+        cudaError_t e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "direct cache upload");
+    }
+    *out = p;
+    return GRMP_OK;
+}
+
+// Group problems by local pattern (device fingerprint, then a device
+// comparison against the group's first problem), analyse one pattern per
+// group on the host cores, upload the concatenated trees.
+int build_direct_cache(grmp_matrix A, int np, const int32_t *row_off, const int32_t *drow) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int n = A->nrows;
+    std::vector<int32_t> rowptr(n + 1);
+    cudaError_t e = cudaMemcpyAsync(rowptr.data(), A->d_rowptr, (size_t)(n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    unsigned long long *dh = nullptr;
+    int32_t *drep = nullptr;
+    int *dbad = nullptr;
+    int rc = grmp_alloc(ctx, (void **)&dh, (size_t)np * 8);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&drep, (size_t)np * 4);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&dbad, (size_t)np * 4);
+    auto cleanup = [&]() {
+        grmp_free(ctx, dh, (size_t)np * 8);
+        grmp_free(ctx, drep, (size_t)np * 4);
+        grmp_free(ctx, dbad, (size_t)np * 4);
+    };
+    if (rc) {
+        cleanup();
+        return rc;
+    }
+    std::vector<unsigned long long> h(np);
+    cudaMemsetAsync(dh, 0, (size_t)np * 8, ctx->stream);
+    k_pattern_hash<<<np, 256, 0, ctx->stream>>>(np, drow, A->d_rowptr, A->d_cols, dh);
+    GRMP_LAUNCHED(ctx);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), dh, (size_t)np * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cleanup();
+        return grmp_cuda_fail(ctx, e, "direct: pattern fingerprints");
+    }
+    std::vector<int32_t> rep(np);
+    {
+        std::vector<std::pair<std::pair<long long, long long>, unsigned long long>> keys;
+        std::vector<std::tuple<long long, long long, unsigned long long, int>> seen;
+        for (int k = 0; k < np; k++) {
+            const long long nk = row_off[k + 1] - row_off[k];
+            const long long zk = (long long)rowptr[row_off[k + 1]] - rowptr[row_off[k]];
+            int r = k;
+            for (auto &t : seen)
+                if (std::get<0>(t) == nk && std::get<1>(t) == zk && std::get<2>(t) == h[k]) {
+                    r = std::get<3>(t);
+                    break;
+                }
+            if (r == k) seen.emplace_back(nk, zk, h[k], k);
+            rep[k] = r;
+        }
+    }
+    std::vector<int> bad(np, 0);
+    cudaMemcpyAsync(drep, rep.data(), (size_t)np * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(dbad, 0, (size_t)np * 4, ctx->stream);
+    k_pattern_equal<<<np, 256, 0, ctx->stream>>>(np, drow, A->d_rowptr, A->d_cols, drep, dbad);
+    GRMP_LAUNCHED(ctx);
+    e = cudaMemcpyAsync(bad.data(), dbad, (size_t)np * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "direct: pattern comparison");
+    for (int k = 0; k < np; k++)
+        if (bad[k]) rep[k] = k;   // fingerprint collision: own analysis
+    std::vector<int> reps;
+    std::vector<int> group_of(np, -1);
+    for (int k = 0; k < np; k++)
+        if (rep[k] == k) {
+            group_of[k] = (int)reps.size();
+            reps.push_back(k);
+        }
+    for (int k = 0; k < np; k++) group_of[k] = group_of[rep[k]];
+    // local patterns of the representatives
+    const int ng = (int)reps.size();
+    std::vector<std::vector<int32_t>> lrp(ng), lci(ng);
+    for (int g = 0; g < ng; g++) {
+        const int r0 = row_off[reps[g]], r1 = row_off[reps[g] + 1];
+        const long long z0 = rowptr[r0], z1 = rowptr[r1];
+        lrp[g].resize(r1 - r0 + 1);
+        for (int i = 0; i <= r1 - r0; i++) lrp[g][i] = (int32_t)(rowptr[r0 + i] - z0);
+        lci[g].resize(z1 - z0);
+        e = cudaMemcpyAsync(lci[g].data(), A->d_cols + z0, (size_t)(z1 - z0) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "direct: pattern download");
+    }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "direct: pattern download");
+    for (int g = 0; g < ng; g++) {
+        const int r0 = row_off[reps[g]];
+        for (auto &c : lci[g]) c -= r0;
+    }
+    std::vector<NdSymbolic> S(ng);
+    std::vector<int> src(ng, 0);
+    {
+        const int nthr = std::max(1, std::min<int>(ng, (int)std::thread::hardware_concurrency()));
+        std::atomic<int> next{0};
+        std::vector<std::thread> pool;
+        for (int w = 0; w < nthr; w++)
+            pool.emplace_back([&]() {
+                for (int g = next++; g < ng; g = next++)
+                    src[g] = nd_symbolic_build((int)lrp[g].size() - 1, lrp[g].data(), lci[g].data(), &S[g]);
+            });
+        for (auto &t : pool) t.join();
+    }
+    for (int g = 0; g < ng; g++)
+        if (src[g]) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "direct: symbolic analysis failed (%d)", src[g]);
+    // concatenate
+    DirectCache *C = new DirectCache;
+    C->row_offsets.assign(row_off, row_off + np + 1);
+    C->groups = ng;
+    std::vector<DNode> node;
+    std::vector<int32_t> front, child, ent_rel, ent_pos, ext, gnode0(ng), pn0(np), pnn(np);
+    for (int g = 0; g < ng; g++) {
+        const NdSymbolic &Sg = S[g];
+        const int nbase = (int)node.size(), fbase = (int)front.size(), cbase = (int)child.size();
+        const int ebase = (int)ent_rel.size(), xbase = (int)ext.size();
+        gnode0[g] = nbase;
+        for (const NdNode &q : Sg.node) {
+            DNode dn;
+            dn.s = q.s;
+            dn.f = q.f;
+            dn.front_off = q.front_off + fbase;
+            dn.child_off = q.child_off + cbase;
+            dn.nchild = q.nchild;
+            dn.entry_off = q.entry_off + ebase;
+            dn.nentry = q.nentry;
+            dn.ext_off = q.ext_off + xbase;
+            dn.L_off = q.L_off;
+            dn.U_off = q.U_off;
+            node.push_back(dn);
+        }
+        front.insert(front.end(), Sg.front.begin(), Sg.front.end());
+        for (int c : Sg.child) child.push_back(c + nbase);
+        ent_rel.insert(ent_rel.end(), Sg.ent_rel.begin(), Sg.ent_rel.end());
+        ent_pos.insert(ent_pos.end(), Sg.ent_pos.begin(), Sg.ent_pos.end());
+        ext.insert(ext.end(), Sg.ext.begin(), Sg.ext.end());
+        C->max_f = std::max(C->max_f, Sg.max_f);
+        C->max_s = std::max(C->max_s, Sg.max_s);
+        C->max_U = std::max<long long>(C->max_U, Sg.U_size);
+        C->max_L = std::max<long long>(C->max_L, Sg.L_size);
+    }
+    for (int k = 0; k < np; k++) {
+        pn0[k] = gnode0[group_of[k]];
+        pnn[k] = S[group_of[k]].nnodes;
+    }
+    A->direct = C;
+    rc = upload_vec(ctx, *C, node, &C->node);
+    if (!rc) rc = upload_vec(ctx, *C, front, &C->front);
+    if (!rc) rc = upload_vec(ctx, *C, child, &C->child);
+    if (!rc) rc = upload_vec(ctx, *C, ent_rel, &C->ent_rel);
+    if (!rc) rc = upload_vec(ctx, *C, ent_pos, &C->ent_pos);
+    if (!rc) rc = upload_vec(ctx, *C, ext, &C->ext);
+    if (!rc) rc = upload_vec(ctx, *C, pn0, &C->prob_node0);
+    if (!rc) rc = upload_vec(ctx, *C, pnn, &C->prob_nnodes);
+    if (!rc) {
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "direct cache upload");
+    }
+    if (rc) grmp_direct_cache_free(A);
+    return rc;
+}
+
+}  // namespace
+
+void grmp_direct_cache_free(grmp_matrix A) {
+    if (!A || !A->direct) return;
+    grmp_context ctx = A->space->mesh->ctx;
+    for (auto &b : A->direct->bufs) grmp_free(ctx, b.first, b.second);
+    delete A->direct;
+    A->direct = nullptr;
+}
 
 extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vector u, grmp_vector p,
                                        const grmp_stokes_batch_params *prm, int32_t *iters_out,
@@ -713,16 +1229,78 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     double avg = (double)A->nnz / std::max(1, n);
     int tpr = avg <= 6 ? 4 : (avg <= 14 ? 8 : 16);
     int per_sm = 0;
-    auto kern = tpr == 4 ? k_stokes_batch<4> : (tpr == 8 ? k_stokes_batch<8> : k_stokes_batch<16>);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
-    int grid = std::max(1, std::min(np, std::max(1, per_sm) * ctx->num_sms));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaEventRecord(e0, ctx->stream);
-    kern<<<grid, threads, 0, ctx->stream>>>(d);
-    GRMP_LAUNCHED(ctx);
-    cudaEventRecord(e1, ctx->stream);
+    void *dwork = nullptr;
+    size_t dwork_bytes = 0;
+    if (prm->mode == GRMP_SOLVE_DIRECT) {
+        // symbolic analysis once per distinct local pattern, cached in the matrix
+        if (!A->direct || A->direct->row_offsets != std::vector<int32_t>(prm->row_offsets, prm->row_offsets + np + 1)) {
+            grmp_direct_cache_free(A);
+            rc = build_direct_cache(A, np, prm->row_offsets, drow);
+        }
+        DirectDev m;
+        std::memset(&m, 0, sizeof(m));
+        if (!rc) {
+            DirectCache &C = *A->direct;
+            m.node = C.node;
+            m.front = C.front;
+            m.child = C.child;
+            m.ent_rel = C.ent_rel;
+            m.ent_pos = C.ent_pos;
+            m.ext = C.ext;
+            m.prob_node0 = C.prob_node0;
+            m.prob_nnodes = C.prob_nnodes;
+            m.F_doubles = (long long)C.max_f * C.max_f;
+            m.U_doubles = C.max_U;
+            m.slot_doubles = m.F_doubles + m.U_doubles + C.max_L;
+            m.max_f = C.max_f;
+            m.max_s = C.max_s;
+            m.max_solves = 4;
+        }
+        const size_t smem = ((size_t)m.max_f + m.max_s + 32 * 33) * 8;
+        auto kern = tpr == 4 ? k_stokes_direct<4> : (tpr == 8 ? k_stokes_direct<8> : k_stokes_direct<16>);
+        if (!rc && smem > 200 * 1024)
+            rc = grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batch direct: front of %d DoFs too large", m.max_f);
+        if (!rc) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 512, smem);
+            int grid = std::max(1, std::min(np, std::max(1, per_sm) * ctx->num_sms));
+            // one workspace slot per resident block; fewer blocks when memory is short
+            size_t freeb = 0, totalb = 0;
+            cudaMemGetInfo(&freeb, &totalb);
+            size_t allow = (size_t)(0.8 * (double)freeb);
+            if (ctx->budget) allow = std::min(allow, ctx->budget > ctx->in_use ? ctx->budget - ctx->in_use : (size_t)0);
+            const size_t slot_bytes = (size_t)m.slot_doubles * 8;
+            grid = (int)std::min<size_t>((size_t)grid, std::max<size_t>(1, allow / std::max<size_t>(1, slot_bytes)));
+            dwork_bytes = (size_t)grid * slot_bytes;
+            rc = grmp_alloc(ctx, &dwork, dwork_bytes);
+            if (!rc) {
+                m.work = (double *)dwork;
+                cudaEventRecord(e0, ctx->stream);
+                kern<<<grid, 512, smem, ctx->stream>>>(d, m);
+                GRMP_LAUNCHED(ctx);
+                cudaEventRecord(e1, ctx->stream);
+            }
+        }
+        if (rc) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            release();
+            grmp_free(ctx, Dv, (size_t)nc * 72);
+            grmp_free(ctx, vol, (size_t)nc * 8);
+            return rc;
+        }
+    } else {
+        auto kern = tpr == 4 ? k_stokes_batch<4> : (tpr == 8 ? k_stokes_batch<8> : k_stokes_batch<16>);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
+        int grid = std::max(1, std::min(np, std::max(1, per_sm) * ctx->num_sms));
+        cudaEventRecord(e0, ctx->stream);
+        kern<<<grid, threads, 0, ctx->stream>>>(d);
+        GRMP_LAUNCHED(ctx);
+        cudaEventRecord(e1, ctx->stream);
+    }
     std::vector<int> it(np), sw(np), st(np), fb(np);
     std::vector<double> rr(np);
     e = cudaGetLastError();
@@ -737,6 +1315,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     release();
+    grmp_free(ctx, dwork, dwork_bytes);
     grmp_free(ctx, Dv, (size_t)nc * 72);
     grmp_free(ctx, vol, (size_t)nc * 8);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "batched Stokes");
@@ -752,7 +1331,10 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     if (iters_out) std::memcpy(iters_out, it.data(), (size_t)np * 4);
     stats->status = stats->failed_problems ? GRMP_ERR_NOT_CONVERGED : GRMP_OK;
     if (stats->status)
-        return grmp_fail(ctx, stats->status, "batch: %d of %d problems hit the iteration cap (worst relres %.2e)",
+        return grmp_fail(ctx, stats->status,
+                         prm->mode == GRMP_SOLVE_DIRECT
+                             ? "batch: %d of %d problems failed (non-positive pivot or residual above reltol, worst %.2e)"
+                             : "batch: %d of %d problems hit the iteration cap (worst relres %.2e)",
                          stats->failed_problems, np, stats->max_relres);
     return GRMP_OK;
 }

@@ -83,7 +83,11 @@ struct grmp_matrix_s {
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;
+    // batched direct solver: symbolic analysis per distinct problem pattern
+    struct DirectCache *direct = nullptr;
 };
+
+void grmp_direct_cache_free(grmp_matrix A);
 
 struct grmp_vector_s {
     grmp_context ctx = nullptr;

@@ -562,6 +562,7 @@ extern "C" int grmp_matrix_destroy(grmp_matrix A) {
     grmp_free(ctx, A->d_fixed, (size_t)A->nrows);
     grmp_free(ctx, A->d_work, A->work_bytes);
     grmp_free(ctx, A->d_cellfac, A->cellfac_bytes);
+    grmp_direct_cache_free(A);
     cudaStreamSynchronize(ctx->stream);
     delete A;
     return GRMP_OK;

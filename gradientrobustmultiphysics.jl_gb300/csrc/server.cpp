@@ -107,6 +107,9 @@ int run_request(grmp_context ctx, Request &r) {
         rc = grmp_apply_dirichlet(A, b, (int32_t)r.fixed.size(), r.fixed.empty() ? nullptr : r.fixed.data(), nullptr,
                                   GRMP_DIRICHLET_ELIMINATE, 1e60);
     grmp_solve_stats st{};
+    // the SpMV configuration comes from the request's own sizes, never from
+    // timings taken while other requests share the GPU
+    if (r.solve.spmv_config == 0) r.solve.spmv_config = -1;
     if (!rc) rc = grmp_solve(A, b, x, &r.solve, &st);
     if (!rc || rc == GRMP_ERR_NOT_CONVERGED) {
         r.x.resize(r.ndofs);
@@ -204,6 +207,21 @@ int grmp_server_create(int device, size_t hbm_budget_bytes, int nslots, grmp_ser
     for (int w = 0; w < nslots; w++) srv->workers[w].th = std::thread(worker_loop, srv, w);
     srv->admitter = std::thread(admit_loop, srv);
     *out = srv;
+    return GRMP_OK;
+}
+
+int grmp_server_request_bytes(const grmp_request *q, size_t *bytes) {
+    if (!q || !bytes) return GRMP_ERR_INVALID_ARG;
+    if ((q->dim != 2 && q->dim != 3) || q->nverts <= 0 || q->ncells <= 0 || q->ndofs <= 0) return GRMP_ERR_INVALID_ARG;
+    if (grmp_fe_ldofs(q->fe_kind, q->dim, q->ncomponents) <= 0) return GRMP_ERR_UNSUPPORTED;
+    Request r;
+    r.dim = q->dim;
+    r.fe = q->fe_kind;
+    r.ncomp = q->ncomponents;
+    r.nverts = q->nverts;
+    r.ncells = q->ncells;
+    r.ndofs = q->ndofs;
+    *bytes = estimate_bytes(r);
     return GRMP_OK;
 }
 

@@ -632,10 +632,12 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
     int cfg = p->spmv_config;
-    if (cfg <= 0) {   // autotuned once per matrix and solver mode
+    if (cfg == 0) {   // autotuned once per matrix and solver mode
         int &slot = mixed ? A->tuned_cfg32 : A->tuned_cfg;
         if (!slot) slot = autotune_config(A, b, p, work, dst, lay);
         cfg = slot;
+    } else if (cfg < 0) {   // heuristic from the row length: no timing, independent of other work on the GPU
+        cfg = heuristic_config(A);
     }
     return dispatch_pcg(cfg, A, b->d, x->d, p, st, work, dst, lay);
 }

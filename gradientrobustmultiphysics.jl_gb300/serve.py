@@ -107,38 +107,7 @@ class Server:
             raise L.GrmpError(rc, "grmp_server_create")
 
     def submit(self, r: ServeRequest, mode: str = "mixed", reltol: float = 1e-11) -> int:
-        FES, g = r.FES, r.FES.xgrid
-        q = L.Request()
-        keep = []
-
-        def arr(a, dt):
-            a = np.ascontiguousarray(a, dtype=dt)
-            keep.append(a)
-            return a.ctypes.data_as(ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt)))
-
-        q.dim = g.dim
-        q.nverts = g.nverts
-        q.coords = arr(g.coords, np.float64)
-        q.ncells = g.ncells
-        q.cells = arr(g.cells, np.int32)
-        q.fe_kind = FES.FEType.kind
-        q.ncomponents = FES.FEType.ncomponents
-        q.ndofs = FES.ndofs
-        q.celldofs = arr(FES.celldofs, np.int32)
-        ops = r.operators()
-        terms = (L.BilinearTerm * len(ops))()
-        for i, o in enumerate(ops):
-            terms[i] = o.term()
-        keep.append(ops)
-        q.nterms = len(ops)
-        q.terms = terms
-        lf = r.rhs()
-        q.rhs = lf.rhs()
-        keep.append(lf)
-        q.nfixed = r.fixed.size
-        q.fixed = arr(r.fixed, np.int32)
-        s = api.GB300PCG(mode=mode, reltol=reltol, abstol=0.0)
-        q.solve = s.params()
+        q, keep = make_request(r, mode, reltol)
         rid = ctypes.c_int64()
         rc = self.lib.grmp_server_submit(self.h, ctypes.byref(q), ctypes.byref(rid))
         if rc:
@@ -164,6 +133,54 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def estimate_bytes(r: ServeRequest) -> int:
+    """The server's admission estimate for request r (grmp_server_request_bytes)."""
+    lib = L.load()
+    q, keep = make_request(r)
+    v = ctypes.c_size_t()
+    rc = lib.grmp_server_request_bytes(ctypes.byref(q), ctypes.byref(v))
+    if rc:
+        raise L.GrmpError(rc, "grmp_server_request_bytes")
+    return v.value
+
+
+def make_request(r: ServeRequest, mode: str = "mixed", reltol: float = 1e-11):
+    """grmp_request for r; returns (request, arrays it points into)."""
+    FES, g = r.FES, r.FES.xgrid
+    q = L.Request()
+    keep = []
+
+    def arr(a, dt):
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data_as(ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt)))
+
+    q.dim = g.dim
+    q.nverts = g.nverts
+    q.coords = arr(g.coords, np.float64)
+    q.ncells = g.ncells
+    q.cells = arr(g.cells, np.int32)
+    q.fe_kind = FES.FEType.kind
+    q.ncomponents = FES.FEType.ncomponents
+    q.ndofs = FES.ndofs
+    q.celldofs = arr(FES.celldofs, np.int32)
+    ops = r.operators()
+    terms = (L.BilinearTerm * len(ops))()
+    for i, o in enumerate(ops):
+        terms[i] = o.term()
+    keep.append(ops)
+    q.nterms = len(ops)
+    q.terms = terms
+    lf = r.rhs()
+    q.rhs = lf.rhs()
+    keep.append(lf)
+    q.nfixed = r.fixed.size
+    q.fixed = arr(r.fixed, np.int32)
+    s = api.GB300PCG(mode=mode, reltol=reltol, abstol=0.0)
+    q.solve = s.params()
+    return q, keep
 
 
 def run(reqs, nslots: int = 4, hbm_budget_bytes: int = 150 << 30, mode: str = "mixed", reltol: float = 1e-11,

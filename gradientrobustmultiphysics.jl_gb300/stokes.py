@@ -168,12 +168,16 @@ class StokesBatchSystem:
     """Device-resident batched system: pattern, assembly, reconstructed rhs."""
 
     def __init__(self, ctx: api.GB300Context, prob: StokesBatchProblem, mixed: bool = True,
-                 split_penalty: bool = True):
+                 split_penalty: bool = True, direct: bool = False):
         """mixed: FP32 inner solves inside FP64 refinement.  split_penalty
         (mixed only): the FP32 matrix holds the viscous term alone and the
-        inner operator applies the penalty per cell in factored form."""
+        inner operator applies the penalty per cell in factored form.
+        direct: FP64 multifrontal Cholesky per problem (the reference's
+        sparse-direct sweep solves), factored once for all sweeps."""
         self.ctx = ctx
         self.prob = prob
+        self.direct = bool(direct)
+        mixed = mixed and not self.direct
         self.mixed = mixed
         self.split_penalty = bool(split_penalty and mixed)
         self.ops = velocity_operators(prob)
@@ -218,7 +222,7 @@ class StokesBatchSystem:
         P.lam = self.prob.lam
         P.sweeps = sweeps
         P.sweep_tol = sweep_tol
-        P.mode = L.SOLVE_MIXED if self.mixed else L.SOLVE_FP64
+        P.mode = L.SOLVE_DIRECT if self.direct else (L.SOLVE_MIXED if self.mixed else L.SOLVE_FP64)
         P.reltol = reltol
         P.inner_reltol = inner_reltol
         P.maxiter = maxiter

@@ -224,7 +224,10 @@ int grmp_apply_dirichlet(grmp_matrix A, grmp_vector b, int32_t nfixed, const int
 
 typedef enum {
     GRMP_SOLVE_FP64 = 0,   /* plain: FP64 Jacobi-PCG                                                 */
-    GRMP_SOLVE_MIXED = 1   /* FP32 Jacobi-PCG inside FP64 refinement (outer residual, update in FP64) */
+    GRMP_SOLVE_MIXED = 1,  /* FP32 Jacobi-PCG inside FP64 refinement (outer residual, update in FP64) */
+    GRMP_SOLVE_DIRECT = 2  /* grmp_stokes_batch_solve only: FP64 multifrontal Cholesky per problem
+                              (nested-dissection order), factored once and reused by every sweep,
+                              with residual refinement against the assembled FP64 matrix          */
 } grmp_solve_mode;
 
 typedef struct {
@@ -235,7 +238,9 @@ typedef struct {
     double inner_reltol;    /* MIXED: residual reduction per refinement (reliable update) */
     int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
     int32_t spmv_config;    /* SpMV lanes per row and loads in flight, coded 100*lanes + loads:
-                               208, 404, 408, 804 or 1602; 0 = autotuned per matrix and mode */
+                               208, 404, 408, 804 or 1602; 0 = autotuned per matrix and mode
+                               (timed trial solves); -1 = chosen from the mean row length (no
+                               timing, so the choice does not depend on concurrent GPU work) */
     int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
     int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
 } grmp_solve_params;
@@ -384,6 +389,11 @@ typedef struct {
  * `device`, admitting requests while their estimated device footprint fits in
  * `hbm_budget_bytes` (0 = unlimited).  No reference counterpart. */
 int grmp_server_create(int device, size_t hbm_budget_bytes, int nslots, grmp_server *out);
+/* Device bytes the server reserves against its budget while running request
+ * q (its admission estimate: matrix in both precisions, pattern, slot map,
+ * incidence, mesh, vectors and solver workspace, with 25% margin). */
+int grmp_server_request_bytes(const grmp_request *q, size_t *bytes);
+
 /* Queue a request (copied); returns its id at once.  GRMP_ERR_BUDGET if it
  * can never fit. */
 int grmp_server_submit(grmp_server srv, const grmp_request *req, int64_t *id);
