@@ -168,6 +168,7 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    _package()   # host-side mesh / DoF-map code (pure Python; nothing runs on the GPU)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
