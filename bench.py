@@ -138,23 +138,54 @@ def peaks():
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)
-def cpu_port_step(n_cpu: int, reltol: float, seed: int = 0):
+WORKLOADS = {
+    # name: (description, default size n, CPU sample size)
+    "poisson3d": ("poisson3d_P2_kuhn{n}_lognormal_kappa", 64, 24),
+    "poisson2d": ("poisson2d_P2_{n}x{n}_kappa1e-3", 128, 128),
+    "elasticity2d": ("elasticity2d_P2vec_{n}x{n}_mu1_lambda1e3", 256, 32),
+}
+
+
+def make_problem(P, args, seed: int, n: int = None):
+    """The workload's LinearProblem at size n (default: the workload's)."""
+    n = n or args.n or WORKLOADS[args.workload][1]
+    if args.workload == "poisson2d":
+        return P.poisson2d(n)
+    if args.workload == "elasticity2d":
+        return P.elasticity2d(n, seed=seed)
+    return P.poisson3d(n, seed=seed)
+
+
+def cpu_port_step(args, n_cpu: int, reltol: float, seed: int = 0):
     """One bounded sample of the same workload on the host cores: the oracle's
     single-threaded assembly (the reference's item loop) + OpenMP FP64 CG.
     Returns (dofs, seconds, assembly_s, solve_s, iterations)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from grmp_gb300 import problems as P
-    prob = P.poisson3d(n_cpu, seed=seed)
+    prob = make_problem(P, args, seed, n_cpu)
     FES = prob.FES
     g = FES.xgrid
+    fe = 1 if FES.FEType.kind == 1 else 2
+    nc = FES.FEType.ncomponents
     t0 = time.perf_counter()
     M = O.Matrix(FES.ndofs)
-    op = prob.operators[0]
-    M.add_bilinear(g.coords, g.cells, 2, 1, FES.celldofs, O.OP_GRADIENT, True, 1.0, O.ACT_CELLSCALE, op.cell_coef)
+    for op in prob.operators:
+        if op.op_kind == 1:
+            act = O.ACT_CELLSCALE if op.cell_coef is not None else O.ACT_NONE
+            M.add_bilinear(g.coords, g.cells, fe, nc, FES.celldofs, O.OP_GRADIENT, op.symmetric, op.factor, act,
+                           op.cell_coef)
+        elif op.op_kind == 2:
+            act = O.ACT_CELLSCALE if op.cell_coef is not None else O.ACT_NONE
+            M.add_bilinear(g.coords, g.cells, fe, nc, FES.celldofs, O.OP_IDENTITY, op.symmetric, op.factor, act,
+                           op.cell_coef)
+        else:
+            M.add_bilinear(g.coords, g.cells, fe, nc, FES.celldofs, O.OP_SYMGRAD, op.symmetric, op.factor,
+                           O.ACT_HOOKE2D if g.dim == 2 else O.ACT_HOOKE3D, mu=op.params[0], lam=op.params[1])
     b = np.zeros(FES.ndofs)
     f = prob.rhs.f
-    O.assemble_linear(b, g.coords, g.cells, 2, 1, FES.celldofs, f.kind, f.params)
+    O.assemble_linear(b, g.coords, g.cells, fe, nc, FES.celldofs, f.kind, f.params, prob.rhs.factor,
+                      f.bonus_quadorder)
     M.penalize(prob.fixed)
     A = M.csr()
     bb = O.penalized_rhs(b, prob.fixed)
@@ -175,20 +206,20 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     for _ in range(args.warmup):
-        cpu_port_step(args.cpu_n, args.reltol)
+        cpu_port_step(args, args.cpu_n, args.reltol)
     times, dofs = [], 0
     for _ in range(args.steps):
-        dofs, dt, _, _, _ = cpu_port_step(args.cpu_n, args.reltol)
+        dofs, dt, _, _, _ = cpu_port_step(args, args.cpu_n, args.reltol)
         times.append(dt)
     v = dofs / statistics.mean(times)
     line = {"metric": METRIC, "value": v, "unit": "DoF/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference",
-            "config": {"workload": f"poisson3d_P2_kuhn{args.n}_lognormal_kappa (sample: {args.cpu_n}^3 cubes)",
+            "config": {"workload": f"{workload_name(args)} (sample: n = {args.cpu_n})",
                        "sample_dofs": dofs},
             "cpu_baseline": {"value": v, "unit": "DoF/s", "cores": cores, "kind": "port",
-                             "sample": f"3D P2 Poisson on {args.cpu_n}^3 Kuhn cubes ({dofs} DoFs): single-thread "
+                             "sample": f"{WORKLOADS[args.workload][0].format(n=args.cpu_n)} ({dofs} DoFs): single-thread "
                                        f"assembly (reference item loop) + {cores}-thread FP64 Jacobi-CG to "
                                        f"relative residual {args.reltol:g} (Julia reference not runnable here)"},
             "e2e": {"value": v, "unit": "DoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -215,6 +246,10 @@ def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool) -> float:
     return it * (12.0 * nnz + 108.0 * n) + 2 * (12.0 * nnz + 36.0 * n)
 
 
+def workload_name(args) -> str:
+    return WORKLOADS[args.workload][0].format(n=args.n)
+
+
 def run_ours(args):
     dist = Dist()
     G = _package()
@@ -227,31 +262,25 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     ctx = G.GB300Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
-    prob = P.poisson3d(args.n, seed=args.seed + dist.rank)
+    prob = make_problem(P, args, args.seed + dist.rank)
     FES = prob.FES
     ndofs = FES.ndofs
     op = prob.operators[0]
-    # resident inputs: kappa in a device vector (coefficient read in place)
-    kdev = G.FEVector.__new__(G.FEVector)
-    kdev.ctx = ctx
-    kdev.h = ctypes.c_void_p()
-    ctx.check(ctx.lib.grmp_vector_create(ctx.h, FES.xgrid.ncells, ctypes.byref(kdev.h)))
-    kap = np.ascontiguousarray(op.cell_coef, dtype=np.float64)
-    ctx.check(ctx.lib.grmp_vector_upload(kdev.h, kap.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
-    kptr = ctypes.c_void_p()
-    ctx.check(ctx.lib.grmp_vector_device_ptr(kdev.h, ctypes.byref(kptr)))
-
-    def dev_term():
-        t = L.BilinearTerm()
-        t.op_kind = L.OP_LAPLACE
-        t.symmetric = 1
-        t.factor = 1.0
+    dev_terms = None
+    if op.cell_coef is not None:
+        # resident inputs: the per-cell coefficient in a device vector (read in place)
+        kdev = G.FEVector.__new__(G.FEVector)
+        kdev.ctx = ctx
+        kdev.h = ctypes.c_void_p()
+        ctx.check(ctx.lib.grmp_vector_create(ctx.h, FES.xgrid.ncells, ctypes.byref(kdev.h)))
+        kap = np.ascontiguousarray(op.cell_coef, dtype=np.float64)
+        ctx.check(ctx.lib.grmp_vector_upload(kdev.h, kap.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        kptr = ctypes.c_void_p()
+        ctx.check(ctx.lib.grmp_vector_device_ptr(kdev.h, ctypes.byref(kptr)))
+        t = op.term()
         t.cell_coef = ctypes.cast(kptr, ctypes.POINTER(ctypes.c_double))
-        t.bonus_quadorder = 0
         t.coef_on_device = 1
-        return t
-
-    dev_terms = (L.BilinearTerm * 1)(dev_term())
+        dev_terms = (L.BilinearTerm * 1)(t)
     A = G.FEMatrix(ctx, FES, prob.operators)
     b = G.FEVector(ctx, FES)
     x = G.FEVector(ctx, FES)
@@ -262,10 +291,14 @@ def run_ours(args):
             G.assemble(A, prob.operators, G.FP64)
             if mode == "mixed":
                 G.assemble(A, prob.operators, G.FP32)
-        else:
+        elif dev_terms is not None:
             ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP64))
             if mode == "mixed":
                 ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP32))
+        else:   # scalar operator parameters: nothing per cell to upload
+            G.assemble(A, prob.operators, G.FP64)
+            if mode == "mixed":
+                G.assemble(A, prob.operators, G.FP32)
         b.fill(0.0)
         G.assemble(b, prob.rhs)
         G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)
@@ -355,16 +388,16 @@ def run_ours(args):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         O.build()
-        d, dt, ta, ts, it = cpu_port_step(args.cpu_n, args.reltol)
+        d, dt, ta, ts, it = cpu_port_step(args, args.cpu_n, args.reltol)
         cores = os.cpu_count() or 1
         cpu = {"value": d / dt, "unit": "DoF/s", "cores": cores, "kind": "port",
-               "sample": f"3D P2 Poisson {args.cpu_n}^3 Kuhn cubes, {d} DoFs: single-thread assembly "
+               "sample": f"{WORKLOADS[args.workload][0].format(n=args.cpu_n)}, {d} DoFs: single-thread assembly "
                          f"{ta:.2f}s + {cores}-thread FP64 Jacobi-CG {ts:.2f}s ({it} it)"}
     p = sorted(mixed["ms"])
     line = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": dist.ws, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(mixed["ms"]), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-outer", "data": "synthetic (seeded)",
-            "config": {"workload": f"poisson3d_P2_kuhn{args.n}_lognormal_kappa", "ndofs": ndofs, "nnz": nnz,
+            "config": {"workload": workload_name(args), "ndofs": ndofs, "nnz": nnz,
                        "ncells": FES.xgrid.ncells, "global_batch": dist.ws, "parallelism": f"replicas{dist.ws}",
                        "l2": "inputs larger than L2 (matrix FP64+FP32 > 129 MB)", "reltol": args.reltol,
                        "inner_reltol": args.inner_reltol},
@@ -384,7 +417,8 @@ def run_ours(args):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"},
             "cpu_baseline": cpu,
             "e2e": {"value": world_dofs / e2e_tot, "unit": "DoF/s",
-                    "h2d_bytes_per_step": int(FES.xgrid.ncells * 8 + prob.rhs.f.params.size * 8),
+                    "h2d_bytes_per_step": int(sum(o.cell_coef.size * 8 for o in prob.operators
+                                                  if o.cell_coef is not None) + prob.rhs.f.params.size * 8),
                     "d2h_bytes_per_step": int(ndofs * 8)},
             "gpu_launches": mixed["launches"],
             "clocks": mixed["clocks"]}
@@ -507,16 +541,17 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--n", type=int, default=0, help="mesh size (0: the workload's own)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--reltol", type=float, default=1e-11)
     ap.add_argument("--ref-reltol", type=float, default=1e-14)
     ap.add_argument("--inner-reltol", type=float, default=0.1)
-    ap.add_argument("--cpu-n", type=int, default=24)
+    ap.add_argument("--cpu-n", type=int, default=0, help="CPU sample mesh size (0: the workload's own)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true", help="mixed path only, no timing output (for ncu)")
-    ap.add_argument("--workload", default="poisson3d", choices=["poisson3d", "stokes-batch", "serve"],
-                    help="poisson3d: the headline line; stokes-batch and serve print their own lines")
+    ap.add_argument("--workload", default="poisson3d",
+                    choices=["poisson3d", "poisson2d", "elasticity2d", "stokes-batch", "serve"],
+                    help="poisson3d: the headline line; the others print their own lines")
     ap.add_argument("--nprob", type=int, default=2048)
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--stokes-reltol", type=float, default=1e-12)
@@ -524,6 +559,9 @@ def main():
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--interarrival", type=float, default=0.05)
     args = ap.parse_args()
+    if args.workload in WORKLOADS:
+        args.n = args.n or WORKLOADS[args.workload][1]
+        args.cpu_n = args.cpu_n or WORKLOADS[args.workload][2]
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "stokes-batch":

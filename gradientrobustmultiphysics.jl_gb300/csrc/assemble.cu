@@ -446,8 +446,9 @@ int grmp_assemble_linear_impl(grmp_space s, const grmp_rhs *rhs, grmp_vector b) 
     grmp_mesh m = s->mesh;
     int dim = m->dim;
     if (s->fe == GRMP_FE_H1BR) {
-        if (rhs->test_operator != 1)
-            return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR right-hand sides use the RT0 reconstruction test operator");
+        if (rhs->test_operator != 1 && rhs->test_operator != 2)
+            return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED,
+                             "H1BR right-hand sides use a reconstruction test operator (1 = RT0, 2 = BDM1)");
         return grmp_br_rhs(s, rhs, b);
     }
     if (rhs->test_operator != 0) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "reconstruction test operator needs H1BR");

@@ -72,6 +72,18 @@ __device__ __forceinline__ void bsum(double *v, double *sh) {
     __syncthreads();
 }
 
+__device__ __forceinline__ void bmax1(double *v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v[0] = fmax(v[0], __shfl_xor_sync(0xffffffffu, v[0], o));
+    __syncthreads();
+    if (lane == 0) sh[wid] = v[0];
+    __syncthreads();
+    double mx = 0.0;
+    for (int w = 0; w < nw; w++) mx = fmax(mx, sh[w]);
+    v[0] = mx;
+    __syncthreads();
+}
+
 // rows [r0, r1) of y = A x (or y = b - A x with RESID) by the block; returns
 // this thread's part of sum w.y (DOT) or of sum y^2 (RESID)
 template <int TPR, typename V, typename X, bool RESID>
@@ -588,9 +600,11 @@ struct DNode {
     long long L_off, U_off;
 };
 
-// A sweep whose refined residual stagnates (FP64 rounding floor of the
-// system) counts as solved when the floor is at most this relative residual.
-constexpr double kDirectFloorMax = 1e-6;
+// A sweep whose refined residual stagnates (FP64 rounding floor of an
+// ill-conditioned system) counts as solved when the normwise backward error
+// ||r|| / (||A||_inf ||u|| + ||rhs||) is at most this: the computed velocity
+// is then the exact solution of a system within this relative distance.
+constexpr double kDirectBackwardMax = 1e-13;
 
 struct DirectDev {
     const DNode *node;
@@ -606,12 +620,99 @@ __device__ __forceinline__ double warp_sum64(double v) {
     return v;
 }
 
+// Partial Cholesky of a front F (f x f, lower part, row-major): eliminate
+// its first s columns.  Blocked right-looking: a panel of kPanel columns
+// (all rows from the panel's diagonal down) is copied to shared memory P and
+// factored there column by column, written back, and the trailing lower
+// triangle receives one rank-kPanel update per panel from 4x4 register
+// tiles reading the panel from P, so F is read and written once per panel
+// instead of once per column.  Returns false on a non-positive pivot.
+constexpr int kPanel = 16;
+constexpr int kPanelStride = kPanel + 1;   // shared-memory row stride (bank spread)
+
+__device__ bool front_cholesky(double *F, int f, int s, double *colk, double *P) {
+    const int tid = threadIdx.x, bs = blockDim.x;
+    for (int k0 = 0; k0 < s; k0 += kPanel) {
+        const int kw = min(kPanel, s - k0), k1 = k0 + kw, mp = f - k0;
+        // panel: rows k0..f-1, columns k0..k1-1, factored in shared memory
+        for (int q = tid; q < mp * kw; q += bs) {
+            const int i = q / kw, t = q - i * kw;
+            P[i * kPanelStride + t] = F[(long long)(k0 + i) * f + k0 + t];
+        }
+        __syncthreads();
+        for (int c = 0; c < kw; c++) {
+            const double dcc = P[c * kPanelStride + c];
+            if (!(dcc > 0.0) || !isfinite(dcc)) return false;   // uniform: same value in every thread
+            const double dk = sqrt(dcc);
+            for (int i = c + 1 + tid; i < mp; i += bs) {
+                const double v = P[i * kPanelStride + c] / dk;
+                P[i * kPanelStride + c] = v;
+                colk[i] = v;
+            }
+            __syncthreads();
+            if (tid == 0) P[c * kPanelStride + c] = dk;
+            for (int i = c + 1 + tid; i < mp; i += bs) {
+                const double lic = colk[i];
+                const int jmax = min(i, kw - 1);
+                for (int j = c + 1; j <= jmax; j++) P[i * kPanelStride + j] -= lic * colk[j];
+            }
+            __syncthreads();
+        }
+        for (int q = tid; q < mp * kw; q += bs) {
+            const int i = q / kw, t = q - i * kw;
+            if (t <= i) F[(long long)(k0 + i) * f + k0 + t] = P[i * kPanelStride + t];
+        }
+        // trailing lower triangle: rank-kw update from 4x4 register tiles
+        const int m = f - k1;
+        const double *Pt = P + kw * kPanelStride;   // panel rows k1..f-1
+        const int nt = (m + 3) >> 2;
+        const long long ntiles = (long long)nt * (nt + 1) / 2;
+        for (long long q = tid; q < ntiles; q += bs) {
+            int bi = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+            while ((long long)(bi + 1) * (bi + 2) / 2 <= q) bi++;
+            while ((long long)bi * (bi + 1) / 2 > q) bi--;
+            const int bj = (int)(q - (long long)bi * (bi + 1) / 2);
+            const int i0 = bi * 4, j0 = bj * 4;
+            double acc[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
+            for (int t = 0; t < kw; t++) {
+                double x[4], y[4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    x[a] = i0 + a < m ? Pt[(i0 + a) * kPanelStride + t] : 0.0;
+                    y[a] = j0 + a < m ? Pt[(j0 + a) * kPanelStride + t] : 0.0;
+                }
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[a][b] += x[a] * y[b];
+            }
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int i = i0 + a;
+                if (i >= m) break;
+                double *Fi = F + (long long)(k1 + i) * f + k1;
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int j = j0 + b;
+                    if (j <= i) Fi[j] -= acc[a][b];
+                }
+            }
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
 // Numeric factorisation of one problem: for every node in post-order,
 // assemble the front (original entries + children's update matrices),
 // eliminate its own DoFs (right-looking dense Cholesky), keep the factor
 // columns and the update matrix.  Returns false on a non-positive pivot.
 __device__ bool mf_factor(const BatchDev &d, const DirectDev &m, int nb, int ne, long long nnz0, double *F, double *U,
-                          double *L, double *colk) {
+                          double *L, double *colk, double *P) {
     const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
     for (int t = nb; t < ne; t++) {
         const DNode nd = m.node[t];
@@ -632,24 +733,7 @@ __device__ bool mf_factor(const BatchDev &d, const DirectDev &m, int nb, int ne,
             }
             __syncthreads();
         }
-        for (int k = 0; k < s; k++) {
-            const double dkk = F[(long long)k * f + k];   // every thread reads the same value
-            if (!(dkk > 0.0) || !isfinite(dkk)) return false;
-            const double dk = sqrt(dkk);
-            for (int i = k + 1 + tid; i < f; i += bs) {
-                const double v = F[(long long)i * f + k] / dk;
-                F[(long long)i * f + k] = v;
-                colk[i] = v;
-            }
-            __syncthreads();
-            if (tid == 0) F[(long long)k * f + k] = dk;
-            for (int i = k + 1 + warp; i < f; i += nw) {
-                const double lik = colk[i];
-                double *Fi = F + (long long)i * f;
-                for (int j = k + 1 + lane; j <= i; j += 32) Fi[j] -= lik * colk[j];
-            }
-            __syncthreads();
-        }
+        if (!front_cholesky(F, f, s, colk, P)) return false;
         double *Lt = L + nd.L_off;
         for (long long q = tid; q < (long long)f * s; q += bs) {
             const int i = (int)(q / s), j = (int)(q - (long long)i * s);
@@ -766,6 +850,7 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
     double *colk = dsm;                 // factor: column k of the front; solve: structure values
     double *ys = dsm + m.max_f;
     double *tile = ys + m.max_s;
+    double *P = tile + 32 * 33;         // factor: the current panel's rows below it
     double *F = m.work + (long long)blockIdx.x * m.slot_doubles;
     double *U = F + m.F_doubles, *L = U + m.U_doubles;
     const int tid = threadIdx.x, bs = blockDim.x;
@@ -782,8 +867,17 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
         for (int i = r0 + tid; i < r1; i += bs) d.u[i] = 0.0;
         for (int c = c0 + tid; c < c1; c += bs) d.p[c] = 0.0;
         __syncthreads();
-        const bool fact_ok = mf_factor(d, m, nb, ne, (long long)d.rowptr[r0], F, U, L, colk);
+        const bool fact_ok = mf_factor(d, m, nb, ne, (long long)d.rowptr[r0], F, U, L, colk, P);
         __syncthreads();
+        // ||A||_inf of the problem (for the normwise backward error of a solve)
+        double an[1] = {0.0};
+        for (int i = r0 + tid; i < r1; i += bs) {
+            double rs = 0.0;
+            for (int kk = d.rowptr[i]; kk < d.rowptr[i + 1]; kk++) rs += fabs(d.v64[kk]);
+            an[0] = fmax(an[0], rs);
+        }
+        bmax1(an, sh);
+        const double anorm = an[0];
         int nsolve = 0, sweep = 0;
         double worst = 0.0;
         bool all_ok = fact_ok;
@@ -794,15 +888,18 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
                 for (int i = r0 + tid; i < r1; i += bs) bb[0] += d.rhs[i] * d.rhs[i];
                 bsum<1>(bb, sh);
                 const double bn = sqrt(bb[0]);
-                double rel = 0.0, prev = INFINITY;
+                double rel = 0.0, prev = INFINITY, eta = 0.0;
                 bool floor = false;
                 for (int ref = 0;; ref++) {
                     // r = rhs - A u (FP64, assembled matrix); stop at reltol or when the
                     // residual stops falling (the FP64 floor of an ill-conditioned
                     // system), else u += A^{-1} r
-                    double v[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, d.r64, nullptr, d.rhs)};
-                    bsum<1>(v, sh);
+                    double v[2] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, d.r64, nullptr, d.rhs),
+                                   0.0};
+                    for (int i = r0 + tid; i < r1; i += bs) v[1] += d.u[i] * d.u[i];
+                    bsum<2>(v, sh);
                     rel = bn > 0 ? sqrt(v[0]) / bn : 0.0;
+                    eta = sqrt(v[0]) / (anorm * sqrt(v[1]) + bn + 1e-300);   // normwise backward error
                     if (rel <= d.reltol) break;
                     if (ref > 0 && rel > 0.5 * prev) {
                         floor = true;
@@ -816,7 +913,7 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
                     nsolve++;
                 }
                 worst = fmax(worst, rel);
-                all_ok = all_ok && (rel <= d.reltol || (floor && rel <= kDirectFloorMax));
+                all_ok = all_ok && (rel <= d.reltol || (floor && eta <= kDirectBackwardMax));
                 if (block_pressure_update(d, c0, c1, sh)) {
                     sweep++;
                     break;
@@ -1259,9 +1356,9 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
             m.max_s = C.max_s;
             m.max_solves = 4;
         }
-        const size_t smem = ((size_t)m.max_f + m.max_s + 32 * 33) * 8;
+        const size_t smem = ((size_t)m.max_f + m.max_s + 32 * 33 + (size_t)m.max_f * kPanelStride) * 8;
         auto kern = tpr == 4 ? k_stokes_direct<4> : (tpr == 8 ? k_stokes_direct<8> : k_stokes_direct<16>);
-        if (!rc && smem > 200 * 1024)
+        if (!rc && smem > 220 * 1024)
             rc = grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batch direct: front of %d DoFs too large", m.max_f);
         if (!rc) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -257,6 +257,29 @@ struct BrRhs {
 
 // loc[cell][I] = factor*vol * sum_q w_q f(x_q) . (R Piola RT0)_I (x_q)
 // (src/feevaluator_h1.jl:342-381; src/assemblypatterns/linearform.jl:181-220)
+// BR -> BDM1 reconstruction coefficients (src/reconstructions.jl:351-379):
+// column 2f = RT0 function of face f, 2f+1 = its linear-moment BDM1 function.
+__device__ __forceinline__ void br_bdm1(const double fv[3], const double nrm[3][2], const double sg[3], double R[9][6]) {
+    const double c[2] = {-1.0 / 12.0, 1.0 / 12.0};
+    for (int i = 0; i < 9; i++)
+        for (int j = 0; j < 6; j++) R[i][j] = 0.0;
+    for (int f = 0; f < 3; f++) {
+        const int nodes[2] = {f, (f + 1) % 3};
+        for (int n = 0; n < 2; n++)
+            for (int k = 0; k < 2; k++) {
+                R[3 * k + nodes[n]][2 * f] = 0.5 * fv[f] * nrm[f][k];
+                R[3 * k + nodes[n]][2 * f + 1] = c[n] * fv[f] * nrm[f][k] * sg[f];
+            }
+        R[6 + f][2 * f] = fv[f];
+    }
+}
+
+// b += factor (f, R v) with R = BR -> RT0 (NR = 3) or BR -> BDM1 (NR = 6):
+// ReconstructionIdentity (src/feevaluator_h1.jl:342-381) with the Piola
+// transform of the H(div) basis (RT0: src/fedefs/hdiv_rt0.jl:67-116,
+// BDM1: src/fedefs/hdiv_bdm1.jl:81-92, 160-172; cell-face signs on the RT0
+// functions only).
+template <int NR>
 __global__ void k_br_rhs_cells(int ncells, BrMeshDev m, BrRhs r, double *loc) {
     int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= ncells) return;
@@ -267,17 +290,35 @@ __global__ void k_br_rhs_cells(int ncells, BrMeshDev m, BrRhs r, double *loc) {
         for (int j = 0; j < 2; j++) A[k][j] = X[(j + 1) * 2 + k] - X[k];
     const double det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
     const double vol = fabs(det) / 2.0;
-    double R[9][3];
-    br_rt0(fv, nrm, R, false);
+    double R[9][NR];
+    if constexpr (NR == 3) {
+        br_rt0(fv, nrm, R, false);
+    } else {
+        br_bdm1(fv, nrm, sg, R);
+    }
     const double *par = r.par + (size_t)(r.group ? r.group[cell] : 0) * r.nt * 5;
     double lb[9];
     for (int i = 0; i < 9; i++) lb[i] = 0;
     for (int q = 0; q < r.nq; q++) {
         const double xi = r.xref[q][0], eta = r.xref[q][1];
-        const double rt[3][2] = {{xi, eta - 1}, {xi, eta}, {xi - 1, eta}};
-        double te[3][2];
-        for (int j = 0; j < 3; j++)
-            for (int k = 0; k < 2; k++) te[j][k] = (A[k][0] * rt[j][0] + A[k][1] * rt[j][1]) * (sg[j] / det);
+        double rt[NR][2], cf[NR];
+        if constexpr (NR == 3) {
+            rt[0][0] = xi, rt[0][1] = eta - 1;
+            rt[1][0] = xi, rt[1][1] = eta;
+            rt[2][0] = xi - 1, rt[2][1] = eta;
+            for (int j = 0; j < NR; j++) cf[j] = sg[j];
+        } else {
+            rt[0][0] = xi, rt[0][1] = eta - 1;
+            rt[1][0] = 6 * xi, rt[1][1] = 6 - 12 * xi - 6 * eta;
+            rt[2][0] = xi, rt[2][1] = eta;
+            rt[3][0] = -6 * xi, rt[3][1] = 6 * eta;
+            rt[4][0] = xi - 1, rt[4][1] = eta;
+            rt[5][0] = 6 * (xi - 1) + 12 * eta, rt[5][1] = -6 * eta;
+            for (int j = 0; j < NR; j++) cf[j] = (j % 2 == 0) ? sg[j / 2] : 1.0;   // signs on RT0 only
+        }
+        double te[NR][2];
+        for (int j = 0; j < NR; j++)
+            for (int k = 0; k < 2; k++) te[j][k] = (A[k][0] * rt[j][0] + A[k][1] * rt[j][1]) * (cf[j] / det);
         double x[2];
         for (int k = 0; k < 2; k++) x[k] = X[k] + A[k][0] * xi + A[k][1] * eta;
         double f[2] = {0, 0};
@@ -290,7 +331,7 @@ __global__ void k_br_rhs_cells(int ncells, BrMeshDev m, BrRhs r, double *loc) {
         }
         for (int i = 0; i < 9; i++) {
             double cv0 = 0, cv1 = 0;
-            for (int j = 0; j < 3; j++) {
+            for (int j = 0; j < NR; j++) {
                 cv0 += R[i][j] * te[j][0];
                 cv1 += R[i][j] * te[j][1];
             }
@@ -515,7 +556,10 @@ int grmp_br_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
     if (!rc) {
         r.par = dpar;
         r.group = dgrp;
-        k_br_rhs_cells<<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, br_mesh(m), r, s->d_locbuf);
+        if (rhs->test_operator == 2)
+            k_br_rhs_cells<6><<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, br_mesh(m), r, s->d_locbuf);
+        else
+            k_br_rhs_cells<3><<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, br_mesh(m), r, s->d_locbuf);
         GRMP_LAUNCHED(ctx);
         k_gather_rows_br<<<nblk(s->ndofs), TPB, 0, ctx->stream>>>(s->ndofs, s->d_inc_ptr, s->d_inc_cell,
                                                                   s->d_inc_loc, s->d_locbuf, b->d);

@@ -85,47 +85,121 @@ __device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh,
     return true;
 }
 
-// y = A x over the rows of this grid; groups of TPR lanes per row.  If DOT,
-// returns this thread's share of sum_r w[r]*y[r].  If RESID, y = b - A x.
-template <int TPR, int U, typename V, typename X, typename Y, bool DOT, bool RESID>
-__device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
-                                            const V *__restrict__ vals, const X *x, Y *y, const Y *w,
-                                            const double *b) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & (TPR - 1);
-    const int warp = gtid >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+// Row loop shared by the SpMV variants: groups of TPR lanes per row, each
+// lane with U independent (column, value) loads per chunk.  With PIPE the
+// loop is software pipelined over the grid-strided rows: while the gathers `x[col]` of the
+// current row are in flight, the first chunk of the next row and the bounds
+// of the row after it are already being loaded, so a warp keeps the matrix
+// stream busy across the dependent gather.  Per-row summation order (chunk
+// by chunk, u = 0..U-1 within a chunk, then the lane reduction) does not
+// depend on the pipelining.  gather(c) returns x[c]; epi(r, s) consumes the
+// row sum (lane 0 of the group).
+template <int U, int TPR, typename A, typename V>
+__device__ __forceinline__ void load_chunk(const int32_t *__restrict__ cols, const V *__restrict__ vals, int k, int e,
+                                           int *c, A *v) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int idx = k + u * TPR;
+        const bool ok = idx < e;
+        c[u] = ok ? __ldg(cols + idx) : 0;
+        v[u] = ok ? (A)__ldg(vals + idx) : A(0);
+    }
+}
+
+template <int TPR, int U, bool PIPE, typename A, typename V, typename G, typename E>
+__device__ __forceinline__ void spmv_rows(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                                          const V *__restrict__ vals, G gather, E epi) {
     constexpr int RPW = 32 / TPR;   // rows per warp per step
+    constexpr int CH = TPR * U;
+    const int lane = threadIdx.x & (TPR - 1);
     const int gin = (threadIdx.x & 31) / TPR;
-    // Each lane keeps U independent (col, val) loads and U gathers in
-    // flight per pass: the SpMV is bound by memory-level parallelism, not
-    // arithmetic.  The matrix is read-only for the whole solve (non-coherent
-    // path); x is written by other blocks between barriers (coherent loads).
-    using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
-    double dot = 0;
-    A dacc = 0;
-    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
-        int r = base + gin;
-        A s = 0;
-        if (r < n) {
-            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
-            for (int k = kb + lane; k < e; k += TPR * U) {
-                int c[U];
-                A v[U];
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int stride = ((gridDim.x * blockDim.x) >> 5) * RPW;
+    if (!PIPE) {
+        // plain: bounds, chunk loads and gathers of one row after another
+        for (int base = warp * RPW; base < n; base += stride) {
+            const int r = base + gin;
+            A s = 0;
+            if (r < n) {
+                const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+                for (int k = kb + lane; k < e; k += CH) {
+                    int c[U];
+                    A v[U];
+                    load_chunk<U, TPR>(cols, vals, k, e, c, v);
 #pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int idx = k + u * TPR;
-                    const bool ok = idx < e;
-                    c[u] = ok ? __ldg(cols + idx) : r;
-                    v[u] = ok ? (A)__ldg(vals + idx) : A(0);
+                    for (int u = 0; u < U; u++) s += v[u] * gather(c[u]);
                 }
-#pragma unroll
-                for (int u = 0; u < U; u++) s += v[u] * (A)x[c[u]];
             }
+#pragma unroll
+            for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (r < n && lane == 0) epi(r, s);
+        }
+        return;
+    }
+    int r = warp * RPW + gin;
+    int kb = 0, e = 0, kbn = 0, en = 0;
+    if (r < n) {
+        kb = __ldg(rowptr + r);
+        e = __ldg(rowptr + r + 1);
+    }
+    if (r + stride < n) {
+        kbn = __ldg(rowptr + r + stride);
+        en = __ldg(rowptr + r + stride + 1);
+    }
+    int c[U];
+    A v[U];
+    load_chunk<U, TPR>(cols, vals, kb + lane, e, c, v);
+    for (int base = warp * RPW; base < n; base += stride) {
+        // next row: first chunk; the row after: bounds
+        int cn[U];
+        A vn[U];
+        load_chunk<U, TPR>(cols, vals, kbn + lane, en, cn, vn);
+        const int r2 = r + 2 * stride;
+        int kb2 = 0, e2 = 0;
+        if (r2 < n) {
+            kb2 = __ldg(rowptr + r2);
+            e2 = __ldg(rowptr + r2 + 1);
+        }
+        A s = 0;
+#pragma unroll
+        for (int u = 0; u < U; u++) s += v[u] * gather(c[u]);
+        for (int k = kb + lane + CH; k < e; k += CH) {   // rows longer than one chunk
+            int c2[U];
+            A v2[U];
+            load_chunk<U, TPR>(cols, vals, k, e, c2, v2);
+#pragma unroll
+            for (int u = 0; u < U; u++) s += v2[u] * gather(c2[u]);
         }
 #pragma unroll
         for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (r < n && lane == 0) {
+        if (r < n && lane == 0) epi(r, s);
+        r += stride;
+        kb = kbn;
+        e = en;
+        kbn = kb2;
+        en = e2;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            c[u] = cn[u];
+            v[u] = vn[u];
+        }
+    }
+}
+
+// y = A x over the rows of this grid.  If DOT, returns this thread's share
+// of sum_r w[r]*y[r].  If RESID, y = b - A x (and DOT gives sum y^2).  The
+// matrix is read-only for the whole solve (non-coherent path); x is written
+// by other blocks between barriers (coherent loads).
+template <int TPR, int U, bool PIPE, typename V, typename X, typename Y, bool DOT, bool RESID>
+__device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                                            const V *__restrict__ vals, const X *x, Y *y, const Y *w,
+                                            const double *b) {
+    using A = typename std::conditional<sizeof(V) == 8, double, float>::type;
+    double dot = 0;
+    A dacc = 0;
+    spmv_rows<TPR, U, PIPE, A>(
+        n, rowptr, cols, vals, [&](int c) { return (A)x[c]; },
+        [&](int r, A s) {
             if (RESID) {
                 double v = b[r] - (double)s;
                 y[r] = (Y)v;
@@ -134,14 +208,13 @@ __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ r
                 y[r] = (Y)s;
                 if (DOT) dacc += (A)w[r] * s;   // FP32 partial in the FP32 path
             }
-        }
-    }
+        });
     return dot + (double)dacc;
 }
 
 // ------------------------------------------------------------------ FP64 PCG
-template <int TPR, int U>
-__global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
+template <int TPR, int U, bool PIPE>
+__global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
                                                 const double *vals, const double *b, double *x, const double *dinv,
                                                 double *r, double *z, double *p, double *q, double *partial,
                                                 SolveState *st, double abstol, double reltol, int maxit, int guess) {
@@ -149,7 +222,7 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // r = b - A x  (or b)
-    if (guess) spmv_grid<TPR, U, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    if (guess) spmv_grid<TPR, U, PIPE, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double v[3] = {0, 0, 0};
     for (int i = gtid; i < n; i += gsz) {
@@ -170,7 +243,7 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
     bool conv = sqrt(rr) <= tol;
     while (!conv && it < maxit) {
         double d[1];
-        d[0] = spmv_grid<TPR, U, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
+        d[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
         if (!grid_sum<1>(d, partial, sh, st)) return;
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -201,7 +274,7 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
     // true residual in FP64
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double t[1];
-    t[0] = spmv_grid<TPR, U, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
     if (!grid_sum<1>(t, partial, sh, st)) return;
     if (gtid == 0) {
         st->iters = it;
@@ -219,54 +292,29 @@ __global__ void __launch_bounds__(PTPB, 4) k_pcg64(int n, const int32_t *rowptr,
 // fmaf everywhere so all readers see identical values), the owner of row r
 // stores p_k(r) into nxt[r].y, and phase B stores z_{k+1} into nxt[r].x.
 // This removes the separate p-update pass and one grid barrier per iteration.
-template <int TPR, int U>
+template <int TPR, int U, bool PIPE>
 __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr,
                                                const int32_t *__restrict__ cols, const float *__restrict__ vals,
                                                const float2 *cur, float *nxt_f, float *q, float beta) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & (TPR - 1);
-    const int warp = gtid >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    constexpr int RPW = 32 / TPR;
-    const int gin = (threadIdx.x & 31) / TPR;
     float dacc = 0.f;
-    for (int base = warp * RPW; base < n; base += nwarps * RPW) {
-        const int r = base + gin;
-        float s = 0.f;
-        if (r < n) {
-            const int kb = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
-            for (int k = kb + lane; k < e; k += TPR * U) {
-                int c[U];
-                float v[U];
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int idx = k + u * TPR;
-                    const bool ok = idx < e;
-                    c[u] = ok ? __ldg(cols + idx) : r;
-                    v[u] = ok ? __ldg(vals + idx) : 0.f;
-                }
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const float2 g = cur[c[u]];
-                    s += v[u] * __fmaf_rn(beta, g.y, g.x);
-                }
-            }
-        }
-#pragma unroll
-        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (r < n && lane == 0) {
+    spmv_rows<TPR, U, PIPE, float>(
+        n, rowptr, cols, vals,
+        [&](int c) {
+            const float2 g = cur[c];
+            return __fmaf_rn(beta, g.y, g.x);
+        },
+        [&](int r, float s) {
             const float2 me = cur[r];
             const float pn = __fmaf_rn(beta, me.y, me.x);
             nxt_f[2 * r + 1] = pn;
             q[r] = s;
             dacc += pn * s;
-        }
-    }
+        });
     return dacc;
 }
 
-template <int TPR, int U>
-__global__ void __launch_bounds__(PTPB, U >= 8 ? 4 : 5) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+template <int TPR, int U, bool PIPE>
+__global__ void __launch_bounds__(PTPB, U >= 8 ? (PIPE ? 3 : 4) : 5) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
                                                     const double *vals64, const float *vals32, const double *b,
                                                     double *x, const float *dinv, float *r, float *q, float *xc,
                                                     float2 *zp0, float2 *zp1, double *r64, double *partial,
@@ -278,7 +326,7 @@ __global__ void __launch_bounds__(PTPB, U >= 8 ? 4 : 5) k_pcg_mixed(int n, const
     // FP64 residual of the initial guess
     double v[2] = {0, 0};
     if (guess) {
-        v[0] = spmv_grid<TPR, U, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+        v[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
     } else {
         for (int i = gtid; i < n; i += gsz) {
             x[i] = 0.0;
@@ -315,7 +363,7 @@ __global__ void __launch_bounds__(PTPB, U >= 8 ? 4 : 5) k_pcg_mixed(int n, const
     while (!conv && it < maxit && outer < maxouter) {
         float *nxt_f = reinterpret_cast<float *>(nxt);
         double d[1];
-        d[0] = (double)spmv_fused_zp<TPR, U>(n, rowptr, cols, vals32, cur, nxt_f, q, beta);
+        d[0] = (double)spmv_fused_zp<TPR, U, PIPE>(n, rowptr, cols, vals32, cur, nxt_f, q, beta);
         if (!grid_sum<1>(d, partial, sh, st)) return;   // barrier 1
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -348,7 +396,7 @@ __global__ void __launch_bounds__(PTPB, U >= 8 ? 4 : 5) k_pcg_mixed(int n, const
             }
             if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
             double t[1];
-            t[0] = spmv_grid<TPR, U, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+            t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
             if (!grid_sum<1>(t, partial, sh, st)) return;
             outer++;
             rn64 = sqrt(t[0]);
@@ -410,7 +458,7 @@ __global__ void k_dinv(int n, const int32_t *rowptr, const int32_t *cols, const 
 template <int TPR, typename V, typename X>
 __global__ void __launch_bounds__(256) k_spmv(int n, const int32_t *rowptr, const int32_t *cols, const V *vals,
                                               const X *x, X *y) {
-    spmv_grid<TPR, TPR >= 16 ? 2 : 4, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr);
+    spmv_grid<TPR, TPR >= 16 ? 2 : 4, false, V, X, X, false, false>(n, rowptr, cols, vals, x, y, nullptr, nullptr);
 }
 
 __global__ void k_f64_to_f32(const double *a, float *b, int n) {
@@ -437,7 +485,7 @@ void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, co
 
 // SpMV configurations of the persistent solvers: (lanes per row, loads in
 // flight per lane), encoded 100*TPR + U.
-constexpr int kConfigs[] = {208, 404, 408, 804, 1602};
+constexpr int kConfigs[] = {208, 404, 408, 804, 1602, 10204, 10404, 10408, 10804};
 
 int heuristic_tpr(grmp_matrix A) {
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
@@ -465,7 +513,7 @@ int coop_grid(grmp_context ctx, K kern, int n, int want) {
     return std::max(1, g);
 }
 
-template <int TPR, int U>
+template <int TPR, int U, bool PIPE>
 int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p, grmp_solve_stats *out,
                char *work, SolveState *dst, WorkLayout lay) {
     grmp_context ctx = A->space->mesh->ctx;
@@ -479,7 +527,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
     cudaEventCreate(&e1);
     cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
     if (!mixed) {
-        auto kern = k_pcg64<TPR, U>;
+        auto kern = k_pcg64<TPR, U, PIPE>;
         grid = coop_grid(ctx, kern, n, p->grid_blocks);
         double *dinv = (double *)work, *r = (double *)(work + lay.vec), *z = (double *)(work + 2 * lay.vec);
         double *pp = (double *)(work + 3 * lay.vec), *q = (double *)(work + 4 * lay.vec);
@@ -495,7 +543,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         GRMP_LAUNCHED(ctx);
         cudaEventRecord(e1, ctx->stream);
     } else {
-        auto kern = k_pcg_mixed<TPR, U>;
+        auto kern = k_pcg_mixed<TPR, U, PIPE>;
         grid = coop_grid(ctx, kern, n, p->grid_blocks);
         float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
         float *xc = (float *)(work + 3 * lay.vec);
@@ -527,7 +575,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
     out->iterations = hs.iters;
     out->outer_iterations = hs.outer;
     out->final_relres = hs.relres;
-    out->spmv_config = 100 * TPR + U;
+    out->spmv_config = 100 * TPR + U + (PIPE ? 10000 : 0);
     out->grid_blocks = grid;
     out->solve_ms = ms;
     if (hs.status == GRMP_ERR_NOT_CONVERGED)
@@ -540,13 +588,17 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
 int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_solve_params *p, grmp_solve_stats *st,
                  char *work, SolveState *dst, WorkLayout lay) {
     switch (cfg) {
-        case 208: return launch_pcg<2, 8>(A, b, x, p, st, work, dst, lay);
-        case 404: return launch_pcg<4, 4>(A, b, x, p, st, work, dst, lay);
-        case 408: return launch_pcg<4, 8>(A, b, x, p, st, work, dst, lay);
-        case 804: return launch_pcg<8, 4>(A, b, x, p, st, work, dst, lay);
-        case 1602: return launch_pcg<16, 2>(A, b, x, p, st, work, dst, lay);
+        case 208: return launch_pcg<2, 8, false>(A, b, x, p, st, work, dst, lay);
+        case 404: return launch_pcg<4, 4, false>(A, b, x, p, st, work, dst, lay);
+        case 408: return launch_pcg<4, 8, false>(A, b, x, p, st, work, dst, lay);
+        case 804: return launch_pcg<8, 4, false>(A, b, x, p, st, work, dst, lay);
+        case 1602: return launch_pcg<16, 2, false>(A, b, x, p, st, work, dst, lay);
+        case 10204: return launch_pcg<2, 4, true>(A, b, x, p, st, work, dst, lay);
+        case 10404: return launch_pcg<4, 4, true>(A, b, x, p, st, work, dst, lay);
+        case 10408: return launch_pcg<4, 8, true>(A, b, x, p, st, work, dst, lay);
+        case 10804: return launch_pcg<8, 4, true>(A, b, x, p, st, work, dst, lay);
     }
-    return grmp_fail(A->space->mesh->ctx, GRMP_ERR_INVALID_ARG, "spmv_config must be one of 208 404 408 804 1602");
+    return grmp_fail(A->space->mesh->ctx, GRMP_ERR_INVALID_ARG, "spmv_config: unknown configuration %d", cfg);
 }
 
 // Autotuner: run each configuration for a few iterations of the real solve
@@ -713,11 +765,11 @@ int noalloc_scratch(grmp_context ctx, char **out) {
     return GRMP_OK;
 }
 
-template <int TPR, int U>
+template <int TPR, int U, bool PIPE>
 cudaError_t launch_pcg64_static(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
                                 char *work, int *grid_out) {
     grmp_context ctx = A->space->mesh->ctx;
-    auto kern = k_pcg64<TPR, U>;
+    auto kern = k_pcg64<TPR, U, PIPE>;
     int grid = coop_grid(ctx, kern, A->nrows, p->grid_blocks);
     double *dinv = (double *)work, *r = (double *)(work + kNaVec), *z = (double *)(work + 2 * kNaVec);
     double *pp = (double *)(work + 3 * kNaVec), *q = (double *)(work + 4 * kNaVec);
@@ -775,12 +827,16 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
     int cfg = p->spmv_config > 0 ? p->spmv_config : (A->tuned_cfg ? A->tuned_cfg : heuristic_config(A));
     int grid = 0;
     switch (cfg) {
-        case 208: e = launch_pcg64_static<2, 8>(A, b->d, x->d, p, work, &grid); break;
-        case 404: e = launch_pcg64_static<4, 4>(A, b->d, x->d, p, work, &grid); break;
-        case 408: e = launch_pcg64_static<4, 8>(A, b->d, x->d, p, work, &grid); break;
-        case 804: e = launch_pcg64_static<8, 4>(A, b->d, x->d, p, work, &grid); break;
-        case 1602: e = launch_pcg64_static<16, 2>(A, b->d, x->d, p, work, &grid); break;
-        default: return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_config must be one of 208 404 408 804 1602");
+        case 208: e = launch_pcg64_static<2, 8, false>(A, b->d, x->d, p, work, &grid); break;
+        case 404: e = launch_pcg64_static<4, 4, false>(A, b->d, x->d, p, work, &grid); break;
+        case 408: e = launch_pcg64_static<4, 8, false>(A, b->d, x->d, p, work, &grid); break;
+        case 804: e = launch_pcg64_static<8, 4, false>(A, b->d, x->d, p, work, &grid); break;
+        case 1602: e = launch_pcg64_static<16, 2, false>(A, b->d, x->d, p, work, &grid); break;
+        case 10204: e = launch_pcg64_static<2, 4, true>(A, b->d, x->d, p, work, &grid); break;
+        case 10404: e = launch_pcg64_static<4, 4, true>(A, b->d, x->d, p, work, &grid); break;
+        case 10408: e = launch_pcg64_static<4, 8, true>(A, b->d, x->d, p, work, &grid); break;
+        case 10804: e = launch_pcg64_static<8, 4, true>(A, b->d, x->d, p, work, &grid); break;
+        default: return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_config: unknown configuration %d", cfg);
     }
     SolveState hs;
     std::memset(&hs, 0, sizeof(hs));

@@ -168,12 +168,17 @@ class StokesBatchSystem:
     """Device-resident batched system: pattern, assembly, reconstructed rhs."""
 
     def __init__(self, ctx: api.GB300Context, prob: StokesBatchProblem, mixed: bool = True,
-                 split_penalty: bool = True, direct: bool = False):
+                 split_penalty: bool = True, direct: bool = False, reconstruction: str = "RT0"):
         """mixed: FP32 inner solves inside FP64 refinement.  split_penalty
         (mixed only): the FP32 matrix holds the viscous term alone and the
         inner operator applies the penalty per cell in factored form.
         direct: FP64 multifrontal Cholesky per problem (the reference's
-        sparse-direct sweep solves), factored once for all sweeps."""
+        sparse-direct sweep solves), factored once for all sweeps.
+        reconstruction: "RT0" or "BDM1", the H(div) space of the
+        right-hand side's ReconstructionIdentity test operator."""
+        if reconstruction not in ("RT0", "BDM1"):
+            raise ValueError("reconstruction must be RT0 or BDM1")
+        self.reconstruction = reconstruction
         self.ctx = ctx
         self.prob = prob
         self.direct = bool(direct)
@@ -204,7 +209,7 @@ class StokesBatchSystem:
         r.nparams = par.size
         r.factor = 1.0
         r.bonus_quadorder = 2
-        r.test_operator = 1
+        r.test_operator = 2 if self.reconstruction == "BDM1" else 1
         r.cell_group = grp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
         r.ngroups = self.prob.nproblems
         sh = self.ctx.space(self.prob.V)

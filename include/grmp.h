@@ -186,8 +186,9 @@ typedef struct {
     int64_t nparams;        /* number of doubles in params                           */
     double factor;          /* LinearForm factor                                     */
     int bonus_quadorder;    /* DataFunction bonus_quadorder                          */
-    int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0}
-                               (BR only, src/feevaluator_h1.jl:342-381)              */
+    int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0{2}};
+                               2 = ReconstructionIdentity{HDIVBDM1{2}} (1, 2: H1BR only,
+                               src/feevaluator_h1.jl:342-381, src/reconstructions.jl:351-403) */
     const int32_t *cell_group; /* optional [ncells]: POLY data per cell group (one DataFunction
                                   per independent problem of a batch); params then hold
                                   [ngroups][nterms][5]                                 */
@@ -237,10 +238,11 @@ typedef struct {
     int32_t mode;           /* grmp_solve_mode                                           */
     double inner_reltol;    /* MIXED: residual reduction per refinement (reliable update) */
     int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
-    int32_t spmv_config;    /* SpMV lanes per row and loads in flight, coded 100*lanes + loads:
-                               208, 404, 408, 804 or 1602; 0 = autotuned per matrix and mode
-                               (timed trial solves); -1 = chosen from the mean row length (no
-                               timing, so the choice does not depend on concurrent GPU work) */
+    int32_t spmv_config;    /* SpMV lanes per row and loads in flight, coded 100*lanes + loads,
+                               +10000 for the software-pipelined row loop: 208, 404, 408, 804,
+                               1602, 10204, 10404, 10408, 10804; 0 = autotuned per matrix and
+                               mode (timed trial solves); -1 = chosen from the mean row length
+                               (no timing, so the choice does not depend on concurrent GPU work) */
     int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
     int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
 } grmp_solve_params;

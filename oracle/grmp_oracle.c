@@ -765,6 +765,38 @@ static void br_rt0_coeffs(const double *fvol, const double *nrm, double R[9][3])
     }
 }
 
+/* BDM1 reconstruction coefficients R[9][6] of one cell
+ * (src/reconstructions.jl:351-379): columns 2f (RT0 function of face f) and
+ * 2f+1 (linear-moment BDM1 function of face f); for the two nodes of face f,
+ * R[3k+node][2f] = (1/2 |F|) n_F[k], R[3k+node][2f+1] = c_n |F| n_F[k] s_f
+ * with c = (-1/12, 1/12) and s_f the cell-face sign; R[6+f][2f] = |F|. */
+static void br_bdm1_coeffs(const double *fvol, const double *nrm, const double *sg, double R[9][6])
+{
+    const double c[2] = {-1.0 / 12.0, 1.0 / 12.0};
+    memset(R, 0, sizeof(double) * 54);
+    for (int f = 0; f < 3; f++) {
+        int nodes[2] = {f, (f + 1) % 3};
+        for (int n = 0; n < 2; n++)
+            for (int k = 0; k < 2; k++) {
+                R[3 * k + nodes[n]][2 * f] = (0.5 * fvol[f]) * nrm[f * 2 + k];
+                R[3 * k + nodes[n]][2 * f + 1] = ((c[n] * fvol[f]) * nrm[f * 2 + k]) * sg[f];
+            }
+        R[6 + f][2 * f] = fvol[f];
+    }
+}
+
+/* Reference HDIVBDM1{2} basis on the triangle (src/fedefs/hdiv_bdm1.jl:81-92),
+ * rows in the reference order: RT0 of face 1, BDM1 of face 1, RT0 of face 2, ... */
+static void bdm1_ref_basis(double xi, double eta, double out[6][2])
+{
+    out[0][0] = xi; out[0][1] = eta - 1;
+    out[1][0] = 6 * xi; out[1][1] = 6 - 12 * xi - 6 * eta;
+    out[2][0] = xi; out[2][1] = eta;
+    out[3][0] = -6 * xi; out[3][1] = 6 * eta;
+    out[4][0] = xi - 1; out[4][1] = eta;
+    out[5][0] = 6 * (xi - 1) + 12 * eta; out[5][1] = -6 * eta;
+}
+
 typedef struct {
     const double *coords; const int *cells; const int *cell_faces; const double *fnormals;
     const double *fvolumes; const signed char *signs; const int *celldofs;
@@ -876,34 +908,50 @@ int oracle_br_assemble(void *h, int ncells, const double *coords, const int *cel
 }
 
 /* b += factor * (f, R v), f polynomial (RHS_POLY params, 2 components), with
- * the ReconstructionIdentity{HDIVRT0{2}} test operator
+ * the ReconstructionIdentity{HDIVRT0{2}} (recon 1) or
+ * ReconstructionIdentity{HDIVBDM1{2}} (recon 2) test operator
  * (src/feevaluator_h1.jl:342-381, src/assemblypatterns/linearform.jl:181-220);
  * quadrature order polyorder(H1BR{2}) = 2 plus bonus. */
-int oracle_br_rhs(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
-                  const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
-                  const double *par, int npar, double factor, int bonus_quadorder)
+int oracle_br_rhs_recon(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                        const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                        const double *par, int npar, double factor, int bonus_quadorder, int recon)
 {
     br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
     double xref[3 * OR_MAXQ], w[OR_MAXQ];
     int nq = oracle_qrule(2, 2 + bonus_quadorder, xref, w);
     if (nq < 0) nq = -nq;
+    const int nr = recon == 2 ? 6 : 3;
     for (int cell = 0; cell < ncells; cell++) {
         double X[6], nrm[6], fv[3], sg[3];
         br_cell(&m, cell, X, nrm, fv, sg);
         double A[3][3], G[3][3], det, vol;
         oracle_geometry(2, X, A, G, &det, &vol);
-        double R[9][3];
-        br_rt0_coeffs(fv, nrm, R);
+        double R[9][6];
+        if (recon == 2) {
+            br_bdm1_coeffs(fv, nrm, sg, R);
+        } else {
+            double R3[9][3];
+            br_rt0_coeffs(fv, nrm, R3);
+            for (int i = 0; i < 9; i++)
+                for (int j = 0; j < 3; j++) R[i][j] = R3[i][j];
+        }
         double locb[9] = {0};
         for (int q = 0; q < nq; q++) {
             double xi = xref[3 * q], eta = xref[3 * q + 1];
-            double rt[3][2] = {{xi, eta - 1}, {xi, eta}, {xi - 1, eta}};
-            double te[3][2];
-            for (int j = 0; j < 3; j++)
+            double rt[6][2], coef[6];
+            if (recon == 2) {
+                bdm1_ref_basis(xi, eta, rt);
+                for (int j = 0; j < 6; j++) coef[j] = (j % 2 == 0) ? sg[j / 2] : 1.0;   /* signs on RT0 only */
+            } else {
+                double r3[3][2] = {{xi, eta - 1}, {xi, eta}, {xi - 1, eta}};
+                for (int j = 0; j < 3; j++) { rt[j][0] = r3[j][0]; rt[j][1] = r3[j][1]; coef[j] = sg[j]; }
+            }
+            double te[6][2];
+            for (int j = 0; j < nr; j++)
                 for (int k = 0; k < 2; k++) {
                     double s = 0;
                     for (int l = 0; l < 2; l++) s += A[k][l] * rt[j][l];
-                    s *= sg[j] / det;
+                    s *= coef[j] / det;
                     te[j][k] = s;
                 }
             double x[2], f[2];
@@ -914,7 +962,7 @@ int oracle_br_rhs(double *b, int ncells, const double *coords, const int *cells,
             rhs_eval(OR_RHS_POLY, 2, 2, par, npar, cell, x, f);
             for (int i = 0; i < 9; i++) {
                 double cv[2] = {0, 0};
-                for (int j = 0; j < 3; j++)
+                for (int j = 0; j < nr; j++)
                     if (R[i][j] != 0)
                         for (int k = 0; k < 2; k++) cv[k] += R[i][j] * te[j][k];
                 double t = 0;
@@ -926,6 +974,14 @@ int oracle_br_rhs(double *b, int ncells, const double *coords, const int *cells,
         for (int i = 0; i < 9; i++) b[celldofs[(size_t)cell * 9 + i]] += locb[i] * itemfactor;
     }
     return nq;
+}
+
+int oracle_br_rhs(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                  const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                  const double *par, int npar, double factor, int bonus_quadorder)
+{
+    return oracle_br_rhs_recon(b, ncells, coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs, par, npar,
+                               factor, bonus_quadorder, 1);
 }
 
 /* Divergence of H1BR{2} functions with coefficients

@@ -82,6 +82,8 @@ def lib():
         L.oracle_br_assemble.restype = ctypes.c_int
         L.oracle_br_rhs.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.oracle_br_rhs.restype = ctypes.c_int
+        L.oracle_br_rhs_recon.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.oracle_br_rhs_recon.restype = ctypes.c_int
         L.oracle_br_div.argtypes = brm + [dp, dp, dp, dp]
     return _lib
 
@@ -276,9 +278,13 @@ def _br_args(g, cd):
     return arrs, ptrs
 
 
-def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, reconstruct: bool = True):
+RECON_RT0, RECON_BDM1 = 1, 2
+
+
+def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, recon: int = RECON_RT0):
     """(A (penalised), bf, fixed, celldofs) of the velocity update system:
-    nu (grad u, grad v) + lam (div R u, div R v) = (f, R v)."""
+    nu (grad u, grad v) + lam (div R u, div R v) = (f, R_rhs v), R_rhs the
+    BR->RT0 (recon 1) or BR->BDM1 (recon 2) reconstruction."""
     fn, cf = g.faces()
     cd, nd = br_celldofs(g.nverts, g.cells, cf)
     arrs, ptrs = _br_args(g, cd)
@@ -286,7 +292,7 @@ def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, 
     lib().oracle_br_assemble(M.h, *ptrs, float(nu), None, float(lam))
     bf = np.zeros(nd)
     par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
-    lib().oracle_br_rhs(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder))
+    lib().oracle_br_rhs_recon(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder), int(recon))
     # homogeneous Dirichlet on all boundary faces: nodes (both components) and face bubbles
     bf_ids = np.nonzero(np.bincount(cf.ravel(), minlength=fn.shape[0]) == 1)[0]
     bnodes = np.unique(fn[bf_ids].ravel())
@@ -308,12 +314,12 @@ def br_div(g, cd_args, u=None, p=None):
     return divu, b
 
 
-def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6):
+def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6, recon: int = RECON_RT0):
     """Iterated penalty (examples/Example221_StokesIterated2D.jl:61-95, no
     convection): sparse-direct velocity solves of the penalised system,
     P0 pressure update p <- p - lam * avg(div u), zero mean."""
     import scipy.sparse.linalg as spla
-    M, bf, fixed, cd, args = br_stokes_system(g, nu, lam, terms)
+    M, bf, fixed, cd, args = br_stokes_system(g, nu, lam, terms, recon=recon)
     M.penalize(fixed)
     A = M.csr().tocsc()
     lu = spla.splu(A)

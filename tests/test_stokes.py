@@ -16,15 +16,17 @@ def _poly_terms(rng):
     return S.grad_plus_curl_terms(S.cubic_coefficients(rng), S.cubic_coefficients(rng))
 
 
-def test_oracle_hydrostatic_velocity_is_zero(G, O):
+@pytest.mark.parametrize("recon", [1, 2])   # BR->RT0, BR->BDM1
+def test_oracle_hydrostatic_velocity_is_zero(G, O, recon):
     """f = grad(phi), phi = x^3 + y^3 - xy: the gradient-robust scheme gives
-    u_h = 0 and p_h = (cell means of phi) up to a constant."""
+    u_h = 0 and p_h = (cell means of phi) up to a constant
+    (examples/Example222_PressureRobustness2D.jl:189-211)."""
     g = G.grid_unitsquare(6)
     phi = {(3, 0): 1.0, (0, 3): 1.0, (1, 1): -1.0}
     from grmp_gb300 import stokes as S
     terms = S.grad_plus_curl_terms(phi, {})
     for nu in (1.0, 1e-3):
-        u, p, _ = O.stokes_iterated_penalty(g, nu, 1e4, terms, sweeps=10)
+        u, p, _ = O.stokes_iterated_penalty(g, nu, 1e4, terms, sweeps=10, recon=recon)
         assert np.max(np.abs(u)) < 1e-12, nu
         # cell means of phi (order-6 rule is exact for cubics)
         x, w, _ = O.qrule(2, 6)
@@ -37,14 +39,15 @@ def test_oracle_hydrostatic_velocity_is_zero(G, O):
         assert np.max(np.abs(p - target)) < 1e-9 * np.max(np.abs(target)), nu
 
 
-def test_oracle_br_rhs_of_gradient_is_in_range_of_divergence(G, O):
+@pytest.mark.parametrize("recon", [1, 2])   # BR->RT0, BR->BDM1
+def test_oracle_br_rhs_of_gradient_is_in_range_of_divergence(G, O, recon):
     """(grad phi, R v) = -(pi_0 phi, div v) for v vanishing on the boundary:
     the reconstructed load of a gradient is annihilated by div-free
     velocities -- the identity behind pressure robustness."""
     g = G.grid_unitsquare(4)
     from grmp_gb300 import stokes as S
     phi = {(2, 1): 1.0, (0, 2): -2.0}
-    M, bf, fixed, cd, args = O.br_stokes_system(g, 1.0, 0.0, S.grad_plus_curl_terms(phi, {}))
+    M, bf, fixed, cd, args = O.br_stokes_system(g, 1.0, 0.0, S.grad_plus_curl_terms(phi, {}), recon=recon)
     x, w, _ = O.qrule(2, 6)
     X = g.coords[g.cells]
     A = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))
@@ -61,12 +64,14 @@ def _small_batch(G, sizes, nus, seed=3):
 
 
 @pytest.mark.gpu
-def test_br_assembly_parity(G, O, ctx):
+@pytest.mark.parametrize("recon", ["RT0", "BDM1"])
+def test_br_assembly_parity(G, O, ctx, recon):
     from grmp_gb300 import stokes as S
     prob = _small_batch(G, [7], [0.3])
-    sysd = S.StokesBatchSystem(ctx, prob, mixed=True)
+    sysd = S.StokesBatchSystem(ctx, prob, mixed=True, reconstruction=recon)
     g = prob.mesh.parts[0]
-    M, bf, fixed, cd, args = O.br_stokes_system(g, prob.nus[0], prob.lam, prob.terms[0])
+    M, bf, fixed, cd, args = O.br_stokes_system(g, prob.nus[0], prob.lam, prob.terms[0],
+                                                recon=2 if recon == "BDM1" else 1)
     A0 = M.csr()
     rp, ci = sysd.A.pattern()
     assert np.array_equal(rp, A0.indptr) and np.array_equal(ci, A0.indices)
@@ -98,6 +103,25 @@ def test_batch_matches_oracle(G, O, ctx, mode):
     u, p = sysd.velocity(), sysd.pressure()
     for k, g in enumerate(prob.mesh.parts):
         uo, po, _ = O.stokes_iterated_penalty(g, nus[k], prob.lam, prob.terms[k], sweeps=8)
+        r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
+        c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
+        eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
+        ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
+        assert eu < 1e-8 and ep < 1e-8, (k, eu, ep, st)
+
+
+@pytest.mark.gpu
+def test_batch_bdm1_matches_oracle(G, O, ctx):
+    """Direct batch with the BR -> BDM1 reconstructed right-hand side."""
+    from grmp_gb300 import stokes as S
+    sizes, nus = [6, 8], [1.0, 1e-3]
+    prob = _small_batch(G, sizes, nus, seed=5)
+    sysd = S.StokesBatchSystem(ctx, prob, direct=True, reconstruction="BDM1")
+    sysd.assemble()
+    st = sysd.solve(sweeps=8, reltol=1e-13)
+    u, p = sysd.velocity(), sysd.pressure()
+    for k, g in enumerate(prob.mesh.parts):
+        uo, po, _ = O.stokes_iterated_penalty(g, nus[k], prob.lam, prob.terms[k], sweeps=8, recon=2)
         r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
         c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
         eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
