@@ -286,23 +286,28 @@ def run_ours(args):
     x = G.FEVector(ctx, FES)
     nnz = A.nnz
 
+    direct = args.solver == "direct"
+
     def step(mode: str, host_inputs: bool = False):
+        # FP32 element matrices feed the FP32 PCG; the FP32 factorisation reads the FP64 values
+        needs32 = mode == "mixed" and not direct
         if host_inputs:
             G.assemble(A, prob.operators, G.FP64)
-            if mode == "mixed":
+            if needs32:
                 G.assemble(A, prob.operators, G.FP32)
         elif dev_terms is not None:
             ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP64))
-            if mode == "mixed":
+            if needs32:
                 ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP32))
         else:   # scalar operator parameters: nothing per cell to upload
             G.assemble(A, prob.operators, G.FP64)
-            if mode == "mixed":
+            if needs32:
                 G.assemble(A, prob.operators, G.FP32)
         b.fill(0.0)
         G.assemble(b, prob.rhs)
         G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)
-        s = G.GB300PCG(mode=mode, reltol=args.reltol, abstol=0.0, inner_reltol=args.inner_reltol)
+        smode = {"fp64": "direct", "mixed": "mixed_direct"}[mode] if direct else mode
+        s = G.GB300PCG(mode=smode, reltol=args.reltol, abstol=0.0, inner_reltol=args.inner_reltol)
         st = s.solve(A, b, x)
         out = x.entries if host_inputs else None
         return st, out
@@ -312,7 +317,7 @@ def run_ours(args):
     b.fill(0.0)
     G.assemble(b, prob.rhs)
     G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)
-    ref = G.GB300PCG(mode="fp64", reltol=args.ref_reltol, abstol=0.0, maxiter=200000)
+    ref = G.GB300PCG(mode="direct" if direct else "fp64", reltol=args.ref_reltol, abstol=0.0, maxiter=200000)
     ref_st = ref.solve(A, b, x, raise_on_error=False)
     uref = x.entries
 
@@ -383,6 +388,14 @@ def run_ours(args):
     achieved = kb / (kms / 1e3) / 1e9
     pk = peaks()
     peak = float(pk["hbm_gbs"]) if pk else 6800.0
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": kb * TRAFFIC_PER_ALGORITHMIC_BYTE,
+                "traffic_source": "ncu dram__bytes_read+write of k_pcg_mixed on the 48^3 case "
+                                  "(0.994 x its algorithmic bytes), scaled to this launch",
+                "kernel": "k_pcg_mixed (persistent)",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"}
+    if direct:
+        roofline = None   # factorisation-bound (FP32 / FP64 pipes), no HBM roofline line for this solver
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -400,21 +413,16 @@ def run_ours(args):
             "config": {"workload": workload_name(args), "ndofs": ndofs, "nnz": nnz,
                        "ncells": FES.xgrid.ncells, "global_batch": dist.ws, "parallelism": f"replicas{dist.ws}",
                        "l2": "inputs larger than L2 (matrix FP64+FP32 > 129 MB)", "reltol": args.reltol,
-                       "inner_reltol": args.inner_reltol},
+                       "inner_reltol": args.inner_reltol, "solver": args.solver},
             "latency_ms": {"p50": p[len(p) // 2], "p99": p[min(len(p) - 1, int(0.99 * len(p)))]},
             "rel_err_vs_fp64": {"mixed": mixed["err"], "plain": plain["err"],
-                                "reference": f"GPU FP64 PCG to relres {ref_st['final_relres']:.1e}"},
+                                "reference": f"GPU FP64 {'direct' if direct else 'PCG'} to relres {ref_st['final_relres']:.1e}"},
             "plain_fp64": {"value": plain_value, "ms_per_step": statistics.mean(plain["ms"]),
                            "iterations": plain["stats"][-1]["iterations"]},
             "mixed_vs_plain": value / plain_value,
             "solver": {"iterations": st_last["iterations"], "outer": st_last["outer_iterations"],
                        "spmv_config": st_last["spmv_config"], "grid_blocks": st_last["grid_blocks"]},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": kb * TRAFFIC_PER_ALGORITHMIC_BYTE,
-                         "traffic_source": "ncu dram__bytes_read+write of k_pcg_mixed on the 48^3 case "
-                                           "(0.994 x its algorithmic bytes), scaled to this launch",
-                         "kernel": "k_pcg_mixed (persistent)",
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"},
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": world_dofs / e2e_tot, "unit": "DoF/s",
                     "h2d_bytes_per_step": int(sum(o.cell_coef.size * 8 for o in prob.operators
@@ -552,6 +560,9 @@ def main():
     ap.add_argument("--workload", default="poisson3d",
                     choices=["poisson3d", "poisson2d", "elasticity2d", "stokes-batch", "serve"],
                     help="poisson3d: the headline line; the others print their own lines")
+    ap.add_argument("--solver", default="", choices=["", "pcg", "direct"],
+                    help="pcg: Jacobi-PCG (plain FP64 / mixed FP32-inner); direct: multifrontal Cholesky "
+                         "(plain FP64 / FP32 factor preconditioning FP64 CG); default per workload")
     ap.add_argument("--nprob", type=int, default=2048)
     ap.add_argument("--sweeps", type=int, default=6)
     ap.add_argument("--stokes-reltol", type=float, default=1e-12)
@@ -562,6 +573,7 @@ def main():
     if args.workload in WORKLOADS:
         args.n = args.n or WORKLOADS[args.workload][1]
         args.cpu_n = args.cpu_n or WORKLOADS[args.workload][2]
+        args.solver = args.solver or ("direct" if args.workload == "elasticity2d" else "pcg")
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "stokes-batch":

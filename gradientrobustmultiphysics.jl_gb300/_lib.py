@@ -21,7 +21,7 @@ OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV = 1, 2, 3, 4
 FP64, FP32 = 0, 1
 RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
 DIRICHLET_PENALTY, DIRICHLET_ELIMINATE = 0, 1
-SOLVE_FP64, SOLVE_MIXED, SOLVE_DIRECT = 0, 1, 2
+SOLVE_FP64, SOLVE_MIXED, SOLVE_DIRECT, SOLVE_MIXED_DIRECT = 0, 1, 2, 3
 NOALLOC_MAX_ROWS = 262144   # GRMP_NOALLOC_MAX_ROWS
 
 

@@ -413,7 +413,11 @@ class GB300PCG:
     algorithm slot of default_solver_kwargs, src/solvers.jl:55).
 
     mode "fp64": Jacobi-PCG in FP64.  mode "mixed": FP32 Jacobi-PCG inside an
-    FP64 refinement loop (FP64 residual b - A x and solution update)."""
+    FP64 refinement loop (FP64 residual b - A x and solution update).
+    mode "direct": FP64 multifrontal Cholesky + residual refinement (the
+    counterpart of the reference's sparse-direct default).  mode
+    "mixed_direct": FP32 multifrontal Cholesky as the preconditioner of FP64
+    conjugate gradients."""
     mode: str = "fp64"
     abstol: float = 1e-12
     reltol: float = 1e-12
@@ -430,7 +434,8 @@ class GB300PCG:
         p.abstol = self.abstol
         p.reltol = self.reltol
         p.maxiter = self.maxiter
-        p.mode = L.SOLVE_MIXED if self.mode == "mixed" else L.SOLVE_FP64
+        p.mode = {"fp64": L.SOLVE_FP64, "mixed": L.SOLVE_MIXED, "direct": L.SOLVE_DIRECT,
+                  "mixed_direct": L.SOLVE_MIXED_DIRECT}[self.mode]
         p.inner_reltol = self.inner_reltol
         p.max_outer = self.max_outer
         p.spmv_config = self.spmv_config

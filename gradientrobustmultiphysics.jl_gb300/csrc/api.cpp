@@ -354,12 +354,15 @@ int grmp_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     if (!A || !b || !x || !p) return GRMP_ERR_INVALID_ARG;
     grmp_context ctx = A->space->mesh->ctx;
     if (b->n != A->nrows || x->n != A->nrows) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: size mismatch");
-    if (p->mode != GRMP_SOLVE_FP64 && p->mode != GRMP_SOLVE_MIXED) return GRMP_ERR_INVALID_ARG;
+    if (p->mode < GRMP_SOLVE_FP64 || p->mode > GRMP_SOLVE_MIXED_DIRECT) return GRMP_ERR_INVALID_ARG;
     if (!(p->reltol >= 0) || !(p->abstol >= 0) || p->maxiter <= 0) return GRMP_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     std::lock_guard<std::mutex> lk(ctx->mu);
     grmp_solve_stats local;
-    return grmp_solve_impl(A, b, x, p, st ? st : &local);
+    if (!st) st = &local;
+    std::memset(st, 0, sizeof(*st));
+    if (p->mode == GRMP_SOLVE_DIRECT || p->mode == GRMP_SOLVE_MIXED_DIRECT) return grmp_mf_solve(A, b, x, p, st);
+    return grmp_solve_impl(A, b, x, p, st);
 }
 
 int grmp_spmv(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {

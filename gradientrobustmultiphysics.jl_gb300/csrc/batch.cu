@@ -23,6 +23,7 @@
 #include <tuple>
 
 #include "grmp_internal.h"
+#include "mf_device.cuh"
 #include "nd_symbolic.h"
 
 int grmp_br_divergence(grmp_space s, double **Dv, double **vol);
@@ -620,93 +621,6 @@ __device__ __forceinline__ double warp_sum64(double v) {
     return v;
 }
 
-// Partial Cholesky of a front F (f x f, lower part, row-major): eliminate
-// its first s columns.  Blocked right-looking: a panel of kPanel columns
-// (all rows from the panel's diagonal down) is copied to shared memory P and
-// factored there column by column, written back, and the trailing lower
-// triangle receives one rank-kPanel update per panel from 4x4 register
-// tiles reading the panel from P, so F is read and written once per panel
-// instead of once per column.  Returns false on a non-positive pivot.
-constexpr int kPanel = 16;
-constexpr int kPanelStride = kPanel + 1;   // shared-memory row stride (bank spread)
-
-__device__ bool front_cholesky(double *F, int f, int s, double *colk, double *P) {
-    const int tid = threadIdx.x, bs = blockDim.x;
-    for (int k0 = 0; k0 < s; k0 += kPanel) {
-        const int kw = min(kPanel, s - k0), k1 = k0 + kw, mp = f - k0;
-        // panel: rows k0..f-1, columns k0..k1-1, factored in shared memory
-        for (int q = tid; q < mp * kw; q += bs) {
-            const int i = q / kw, t = q - i * kw;
-            P[i * kPanelStride + t] = F[(long long)(k0 + i) * f + k0 + t];
-        }
-        __syncthreads();
-        for (int c = 0; c < kw; c++) {
-            const double dcc = P[c * kPanelStride + c];
-            if (!(dcc > 0.0) || !isfinite(dcc)) return false;   // uniform: same value in every thread
-            const double dk = sqrt(dcc);
-            for (int i = c + 1 + tid; i < mp; i += bs) {
-                const double v = P[i * kPanelStride + c] / dk;
-                P[i * kPanelStride + c] = v;
-                colk[i] = v;
-            }
-            __syncthreads();
-            if (tid == 0) P[c * kPanelStride + c] = dk;
-            for (int i = c + 1 + tid; i < mp; i += bs) {
-                const double lic = colk[i];
-                const int jmax = min(i, kw - 1);
-                for (int j = c + 1; j <= jmax; j++) P[i * kPanelStride + j] -= lic * colk[j];
-            }
-            __syncthreads();
-        }
-        for (int q = tid; q < mp * kw; q += bs) {
-            const int i = q / kw, t = q - i * kw;
-            if (t <= i) F[(long long)(k0 + i) * f + k0 + t] = P[i * kPanelStride + t];
-        }
-        // trailing lower triangle: rank-kw update from 4x4 register tiles
-        const int m = f - k1;
-        const double *Pt = P + kw * kPanelStride;   // panel rows k1..f-1
-        const int nt = (m + 3) >> 2;
-        const long long ntiles = (long long)nt * (nt + 1) / 2;
-        for (long long q = tid; q < ntiles; q += bs) {
-            int bi = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
-            while ((long long)(bi + 1) * (bi + 2) / 2 <= q) bi++;
-            while ((long long)bi * (bi + 1) / 2 > q) bi--;
-            const int bj = (int)(q - (long long)bi * (bi + 1) / 2);
-            const int i0 = bi * 4, j0 = bj * 4;
-            double acc[4][4];
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
-            for (int t = 0; t < kw; t++) {
-                double x[4], y[4];
-#pragma unroll
-                for (int a = 0; a < 4; a++) {
-                    x[a] = i0 + a < m ? Pt[(i0 + a) * kPanelStride + t] : 0.0;
-                    y[a] = j0 + a < m ? Pt[(j0 + a) * kPanelStride + t] : 0.0;
-                }
-#pragma unroll
-                for (int a = 0; a < 4; a++)
-#pragma unroll
-                    for (int b = 0; b < 4; b++) acc[a][b] += x[a] * y[b];
-            }
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-                const int i = i0 + a;
-                if (i >= m) break;
-                double *Fi = F + (long long)(k1 + i) * f + k1;
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const int j = j0 + b;
-                    if (j <= i) Fi[j] -= acc[a][b];
-                }
-            }
-        }
-        __syncthreads();
-    }
-    return true;
-}
-
 // Numeric factorisation of one problem: for every node in post-order,
 // assemble the front (original entries + children's update matrices),
 // eliminate its own DoFs (right-looking dense Cholesky), keep the factor
@@ -733,7 +647,7 @@ __device__ bool mf_factor(const BatchDev &d, const DirectDev &m, int nb, int ne,
             }
             __syncthreads();
         }
-        if (!front_cholesky(F, f, s, colk, P)) return false;
+        if (!front_cholesky<double>(F, f, s, colk, P, kPanelStride)) return false;
         double *Lt = L + nd.L_off;
         for (long long q = tid; q < (long long)f * s; q += bs) {
             const int i = (int)(q / s), j = (int)(q - (long long)i * s);

@@ -72,6 +72,7 @@ struct grmp_matrix_s {
     int slot_bytes = 1;
     double *d_vals64 = nullptr;     // [nnz]
     float *d_vals32 = nullptr;      // [nnz]
+    void *d_pack32 = nullptr;       // [nnz] int2 (column, FP32 value bits), built by mixed solves
     bool has64 = false, has32 = false;
     uint8_t *d_fixed = nullptr;     // [nrows] Dirichlet flags (eliminated rows)
     bool eliminated = false;
@@ -85,9 +86,13 @@ struct grmp_matrix_s {
     size_t cellfac_bytes = 0;
     // batched direct solver: symbolic analysis per distinct problem pattern
     struct DirectCache *direct = nullptr;
+    // single-problem direct solvers: symbolic analysis + factor storage
+    struct MfCache *mf = nullptr;
 };
 
 void grmp_direct_cache_free(grmp_matrix A);
+void grmp_mf_cache_free(grmp_matrix A);
+int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st);
 
 struct grmp_vector_s {
     grmp_context ctx = nullptr;

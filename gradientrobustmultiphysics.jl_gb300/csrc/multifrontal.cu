@@ -1,0 +1,731 @@
+// Single-problem sparse direct solvers on the device (grmp_solve with
+// mode GRMP_SOLVE_DIRECT or GRMP_SOLVE_MIXED_DIRECT).
+//
+// The reference solves every linear system with a sparse direct solver
+// (UMFPACK through LinearSolve.jl, src/solvers.jl:89-101).  Here the matrix
+// gets a multifrontal Cholesky factorisation over a nested-dissection tree
+// (symbolic analysis: nd_symbolic.cpp, once per pattern, cached in the
+// matrix).  The tree is processed level by level (a node's children are in
+// lower levels), one kernel launch per level, one thread block per front, so
+// the many small fronts near the leaves run in parallel across the GPU.
+//  * DIRECT: FP64 factorisation, forward/backward solves, residual
+//    refinement against the assembled FP64 matrix.
+//  * MIXED_DIRECT: the factorisation and the triangular solves run in FP32
+//    (the GB300 FP32 pipe is about 64x the FP64 rate) and precondition an
+//    FP64 conjugate-gradient iteration on the assembled FP64 matrix, whose
+//    residual decides convergence.
+// Forward solves pass each front's contribution to its ancestors as an update
+// vector read by the parent (no scatter, no atomics): results are
+// reproducible run to run.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "grmp_internal.h"
+#include "mf_device.cuh"
+#include "nd_symbolic.h"
+
+namespace {
+
+constexpr int kTB = 256;   // threads per block of the level kernels
+
+struct MfNode {
+    int s, f, front_off, child_off, nchild, entry_off, nentry, ext_off;
+    long long L_off, U_off, uv_off;
+};
+
+struct MfDev {
+    const MfNode *node;
+    const int32_t *front, *child, *ent_rel, *ent_pos, *ext, *lvl_nodes;
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) { return warp_sum_t<double>(v); }
+
+// ---------------------------------------------------------------- factor
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_factor_level(MfDev m, int lb, int count, const double *vals, T *L, T *U,
+                                                         T *Fpool, long long fslot, T *Ppool, long long pslot,
+                                                         int *err) {
+    extern __shared__ unsigned char mf_smem[];
+    T *colk = reinterpret_cast<T *>(mf_smem);
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    T *F = Fpool + (long long)blockIdx.x * fslot;
+    T *P = Ppool + (long long)blockIdx.x * pslot;
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const int t = m.lvl_nodes[lb + q];
+        const MfNode nd = m.node[t];
+        const int f = nd.f, s = nd.s;
+        for (long long k = tid; k < (long long)f * f; k += bs) F[k] = T(0);
+        __syncthreads();
+        for (int e = tid; e < nd.nentry; e += bs) F[m.ent_pos[nd.entry_off + e]] = (T)vals[m.ent_rel[nd.entry_off + e]];
+        __syncthreads();
+        for (int c = 0; c < nd.nchild; c++) {
+            const MfNode cn = m.node[m.child[nd.child_off + c]];
+            const int sc = cn.f - cn.s;
+            const T *Uc = U + cn.U_off;
+            const int32_t *ex = m.ext + cn.ext_off;
+            for (int a = warp; a < sc; a += nw) {
+                const long long pa = (long long)ex[a] * f;
+                for (int b = lane; b <= a; b += 32) F[pa + ex[b]] += Uc[(long long)a * sc + b];
+            }
+            __syncthreads();
+        }
+        if (!front_cholesky<T>(F, f, s, colk, P, kPanelStride)) {
+            if (tid == 0) atomicCAS(err, 0, t + 1);
+            __syncthreads();
+            continue;
+        }
+        T *Lt = L + nd.L_off;
+        for (long long k = tid; k < (long long)f * s; k += bs) {
+            const int i = (int)(k / s), j = (int)(k - (long long)i * s);
+            Lt[k] = j <= i ? F[(long long)i * f + j] : T(0);
+        }
+        const int sc = f - s;
+        T *Ut = U + nd.U_off;
+        for (long long k = tid; k < (long long)sc * sc; k += bs) {
+            const int a = (int)(k / sc), b = (int)(k - (long long)a * sc);
+            if (b <= a) Ut[k] = F[(long long)(s + a) * f + s + b];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- solves
+// Forward: ys = w[own] minus the children's update entries for own DoFs,
+// L11 y = ys, and the node's update vector = children's entries for its
+// structure + L21 y.
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_forward_level(MfDev m, int lb, int count, const T *L, T *uv, T *w,
+                                                          int maxs) {
+    extern __shared__ unsigned char mf_smem[];
+    T *ys = reinterpret_cast<T *>(mf_smem);
+    T *tile = ys + maxs;   // 32 x 33
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const int t = m.lvl_nodes[lb + q];
+        const MfNode nd = m.node[t];
+        const int f = nd.f, s = nd.s, sc = f - s;
+        const int32_t *fr = m.front + nd.front_off;
+        const T *Lt = L + nd.L_off;
+        T *ut = uv + nd.uv_off;
+        for (int k = tid; k < s; k += bs) ys[k] = w[fr[k]];
+        for (int i = tid; i < sc; i += bs) ut[i] = T(0);
+        __syncthreads();
+        for (int c = 0; c < nd.nchild; c++) {
+            const MfNode cn = m.node[m.child[nd.child_off + c]];
+            const int scc = cn.f - cn.s;
+            const T *uc = uv + cn.uv_off;
+            const int32_t *ex = m.ext + cn.ext_off;
+            for (int a = tid; a < scc; a += bs) {
+                const int pos = ex[a];
+                if (pos < s) ys[pos] -= uc[a];
+                else ut[pos - s] += uc[a];
+            }
+            __syncthreads();
+        }
+        for (int kb = 0; kb < s; kb += 32) {
+            const int nbk = min(32, s - kb);
+            if (kb > 0)
+                for (int r = warp; r < nbk; r += nw) {
+                    const T *Li = Lt + (long long)(kb + r) * s;
+                    T acc = T(0);
+                    for (int j = lane; j < kb; j += 32) acc += Li[j] * ys[j];
+                    acc = warp_sum_t<T>(acc);
+                    if (lane == 0) ys[kb + r] -= acc;
+                }
+            for (int k = tid; k < nbk * nbk; k += bs) {
+                const int r = k / nbk, c = k - r * nbk;
+                tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : T(0);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                T v = lane < nbk ? ys[kb + lane] : T(0);
+                for (int c = 0; c < nbk; c++) {
+                    const T yc = __shfl_sync(0xffffffffu, v, c) / tile[c * 33 + c];
+                    if (lane == c) v = yc;
+                    else if (lane > c && lane < nbk) v -= tile[lane * 33 + c] * yc;
+                }
+                if (lane < nbk) ys[kb + lane] = v;
+            }
+            __syncthreads();
+        }
+        for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+        for (int i = warp; i < sc; i += nw) {
+            const T *Li = Lt + (long long)(s + i) * s;
+            T acc = T(0);
+            for (int k = lane; k < s; k += 32) acc += Li[k] * ys[k];
+            acc = warp_sum_t<T>(acc);
+            if (lane == 0) ut[i] += acc;
+        }
+        __syncthreads();
+    }
+}
+
+// Backward: z = y_own - L21^T x_struct (ancestors already final), L11^T x = z.
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_backward_level(MfDev m, int lb, int count, const T *L, T *w, int maxs) {
+    extern __shared__ unsigned char mf_smem[];
+    T *ys = reinterpret_cast<T *>(mf_smem);
+    T *tile = ys + maxs;
+    T *xs = tile + 32 * 33;
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const int t = m.lvl_nodes[lb + q];
+        const MfNode nd = m.node[t];
+        const int f = nd.f, s = nd.s, sc = f - s;
+        const int32_t *fr = m.front + nd.front_off;
+        const T *Lt = L + nd.L_off;
+        for (int i = tid; i < sc; i += bs) xs[i] = w[fr[s + i]];
+        __syncthreads();
+        for (int k = tid; k < s; k += bs) {
+            T acc = w[fr[k]];
+            for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
+            ys[k] = acc;
+        }
+        __syncthreads();
+        for (int kb = ((s + 31) / 32 - 1) * 32; kb >= 0; kb -= 32) {
+            const int nbk = min(32, s - kb);
+            for (int k = tid; k < nbk * nbk; k += bs) {
+                const int r = k / nbk, c = k - r * nbk;
+                tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : T(0);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                T v = lane < nbk ? ys[kb + lane] : T(0);
+                for (int c = nbk - 1; c >= 0; c--) {
+                    const T xc = __shfl_sync(0xffffffffu, v, c) / tile[c * 33 + c];
+                    if (lane == c) v = xc;
+                    else if (lane < c) v -= tile[c * 33 + lane] * xc;
+                }
+                if (lane < nbk) ys[kb + lane] = v;
+            }
+            __syncthreads();
+            for (int k = tid; k < kb; k += bs) {
+                T acc = T(0);
+                for (int r = 0; r < nbk; r++) acc += Lt[(long long)(kb + r) * s + k] * ys[kb + r];
+                ys[k] -= acc;
+            }
+            __syncthreads();
+        }
+        for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- vector kernels
+// r = b - A x (FP64), per-block partial sums of r^2 (fixed order)
+__global__ void k_resid(int n, const int32_t *rowptr, const int32_t *cols, const double *vals, const double *x,
+                        const double *b, double *r, double *part) {
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double acc2 = 0.0;
+    for (int row = blockIdx.x * nw + warp; row < n; row += gridDim.x * nw) {
+        double s = 0.0;
+        for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) s += vals[k] * x[cols[k]];
+        s = warp_sum_d(s);
+        if (lane == 0) {
+            const double v = b[row] - s;
+            r[row] = v;
+            acc2 += v * v;
+        }
+    }
+    if (lane == 0) sh[warp] = acc2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; w++) t += sh[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// q = A p (FP64) and partial sums of p.q
+__global__ void k_apply_dot(int n, const int32_t *rowptr, const int32_t *cols, const double *vals, const double *p,
+                            double *q, double *part) {
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double acc = 0.0;
+    for (int row = blockIdx.x * nw + warp; row < n; row += gridDim.x * nw) {
+        double s = 0.0;
+        for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) s += vals[k] * p[cols[k]];
+        s = warp_sum_d(s);
+        if (lane == 0) {
+            q[row] = s;
+            acc += p[row] * s;
+        }
+    }
+    if (lane == 0) sh[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; w++) t += sh[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+template <typename T>
+__global__ void k_to(int n, const double *a, T *b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (T)a[i];
+}
+
+// x += alpha p, r -= alpha q, partial sums of r^2
+__global__ void k_cg_update(int n, double alpha, const double *p, const double *q, double *x, double *r,
+                            double *part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        acc += ri * ri;
+    }
+    acc = warp_sum_d(acc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// z = (double) zf, partial sums of r.z
+template <typename T>
+__global__ void k_from_dot(int n, const T *zf, const double *r, double *z, double *part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double zi = (double)zf[i];
+        z[i] = zi;
+        acc += r[i] * zi;
+    }
+    acc = warp_sum_d(acc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// partial sums of a.b
+__global__ void k_dot(int n, const double *a, const double *b, double *part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += a[i] * b[i];
+    acc = warp_sum_d(acc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// per-block maxima of the row sums of |A| (||A||_inf)
+__global__ void k_rownorm(int n, const int32_t *rowptr, const double *vals, double *part) {
+    __shared__ double sh[32];
+    double mx = 0.0;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = rowptr[row]; k < rowptr[row + 1]; k++) s += fabs(vals[k]);
+        mx = fmax(mx, s);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmax(t, sh[w]);
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_xpby(int n, const double *z, double beta, double *p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = z[i] + beta * p[i];
+}
+
+template <typename T>
+__global__ void k_add_from(int n, const T *w, double *x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += (double)w[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+
+struct MfCache {
+    std::vector<std::pair<void *, size_t>> bufs;   // symbolic arrays
+    MfDev dev{};
+    std::vector<int32_t> level_ptr, level_maxf, level_count;
+    int nnodes = 0, max_f = 0, max_s = 0;
+    long long L_size = 0, U_size = 0, uv_size = 0;
+    long long fpool = 0, ppool = 0;   // elements of the per-launch front / panel pools
+    // numeric storage of the current precision (sizeof(T) = esize)
+    int esize = 0;
+    void *L = nullptr, *U = nullptr, *uv = nullptr, *F = nullptr, *P = nullptr, *w = nullptr;
+    size_t Lb = 0, Ub = 0, uvb = 0, Fb = 0, Pb = 0, wb = 0;
+};
+
+namespace {
+
+constexpr int kMaxGrid = 2 * 152;
+
+template <typename V>
+int mf_upload(grmp_context ctx, MfCache &C, const std::vector<V> &v, const V **out) {
+    V *p = nullptr;
+    const size_t bytes = std::max<size_t>(1, v.size()) * sizeof(V);
+    int rc = grmp_alloc(ctx, (void **)&p, bytes);
+    if (rc) return rc;
+    C.bufs.push_back({p, bytes});
+    if (!v.empty()) {
+        cudaError_t e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "multifrontal upload");
+    }
+    *out = p;
+    return GRMP_OK;
+}
+
+void mf_free_numeric(grmp_context ctx, MfCache &C) {
+    grmp_free(ctx, C.L, C.Lb);
+    grmp_free(ctx, C.U, C.Ub);
+    grmp_free(ctx, C.uv, C.uvb);
+    grmp_free(ctx, C.F, C.Fb);
+    grmp_free(ctx, C.P, C.Pb);
+    grmp_free(ctx, C.w, C.wb);
+    C.L = C.U = C.uv = C.F = C.P = C.w = nullptr;
+    C.Lb = C.Ub = C.uvb = C.Fb = C.Pb = C.wb = 0;
+    C.esize = 0;
+}
+
+int mf_build(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int n = A->nrows;
+    std::vector<int32_t> rp(n + 1), ci((size_t)A->nnz);
+    cudaError_t e = cudaMemcpyAsync(rp.data(), A->d_rowptr, (size_t)(n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ci.data(), A->d_cols, (size_t)A->nnz * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "multifrontal: pattern download");
+    NdSymbolic S;
+    int src = nd_symbolic_build(n, rp.data(), ci.data(), &S);
+    if (src) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "multifrontal: symbolic analysis failed (%d)", src);
+    MfCache *C = new MfCache;
+    std::vector<MfNode> node(S.nnodes);
+    for (int t = 0; t < S.nnodes; t++) {
+        const NdNode &q = S.node[t];
+        node[t] = MfNode{q.s, q.f, q.front_off, q.child_off, q.nchild, q.entry_off, q.nentry, q.ext_off,
+                         (long long)q.L_off, (long long)q.U_off, (long long)S.uv_off[t]};
+    }
+    C->nnodes = S.nnodes;
+    C->max_f = S.max_f;
+    C->max_s = S.max_s;
+    C->L_size = S.L_size;
+    C->U_size = S.U_size;
+    C->uv_size = S.uv_size;
+    C->level_ptr = S.level_ptr;
+    C->level_maxf = S.level_maxf;
+    const int nl = (int)S.level_ptr.size() - 1;
+    for (int l = 0; l < nl; l++) {
+        const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
+        const long long g = std::min(cnt, kMaxGrid);
+        const long long mf = S.level_maxf[l];
+        C->fpool = std::max(C->fpool, g * mf * mf);
+        C->ppool = std::max(C->ppool, g * mf * kPanelStride);
+    }
+    A->mf = C;
+    int rc = mf_upload(ctx, *C, node, &C->dev.node);
+    if (!rc) rc = mf_upload(ctx, *C, S.front, &C->dev.front);
+    if (!rc) rc = mf_upload(ctx, *C, S.child, &C->dev.child);
+    if (!rc) rc = mf_upload(ctx, *C, S.ent_rel, &C->dev.ent_rel);
+    if (!rc) rc = mf_upload(ctx, *C, S.ent_pos, &C->dev.ent_pos);
+    if (!rc) rc = mf_upload(ctx, *C, S.ext, &C->dev.ext);
+    if (!rc) rc = mf_upload(ctx, *C, S.level_nodes, &C->dev.lvl_nodes);
+    if (!rc) {
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "multifrontal upload");
+    }
+    if (rc) grmp_mf_cache_free(A);
+    return rc;
+}
+
+template <typename T>
+int mf_numeric(grmp_matrix A, int *grid_out) {
+    grmp_context ctx = A->space->mesh->ctx;
+    MfCache &C = *A->mf;
+    // shared memory of the solve kernels: own values, a 32x33 tile and the structure values
+    if (((size_t)C.max_s + 32 * 33 + C.max_f) * sizeof(T) > 220 * 1024)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "direct solve: front of %d DoFs exceeds shared memory", C.max_f);
+    if (C.esize != (int)sizeof(T)) {
+        mf_free_numeric(ctx, C);
+        C.Lb = std::max<size_t>(1, C.L_size) * sizeof(T);
+        C.Ub = std::max<size_t>(1, C.U_size) * sizeof(T);
+        C.uvb = std::max<size_t>(1, C.uv_size) * sizeof(T);
+        C.Fb = std::max<size_t>(1, C.fpool) * sizeof(T);
+        C.Pb = std::max<size_t>(1, C.ppool) * sizeof(T);
+        C.wb = (size_t)A->nrows * sizeof(T);
+        int rc = grmp_alloc(ctx, &C.L, C.Lb);
+        if (!rc) rc = grmp_alloc(ctx, &C.U, C.Ub);
+        if (!rc) rc = grmp_alloc(ctx, &C.uv, C.uvb);
+        if (!rc) rc = grmp_alloc(ctx, &C.F, C.Fb);
+        if (!rc) rc = grmp_alloc(ctx, &C.P, C.Pb);
+        if (!rc) rc = grmp_alloc(ctx, &C.w, C.wb);
+        if (rc) {
+            mf_free_numeric(ctx, C);
+            return rc;
+        }
+        C.esize = sizeof(T);
+    }
+    int *derr = nullptr;
+    int rc = grmp_alloc(ctx, (void **)&derr, 4);
+    if (rc) return rc;
+    cudaMemsetAsync(derr, 0, 4, ctx->stream);
+    const size_t smem = (size_t)C.max_f * sizeof(T);
+    cudaFuncSetAttribute(k_mf_factor_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int nl = (int)C.level_ptr.size() - 1;
+    int gmax = 0;
+    for (int l = 0; l < nl; l++) {
+        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
+        const int g = std::min(cnt, kMaxGrid);
+        const long long mf = C.level_maxf[l];
+        gmax = std::max(gmax, g);
+        k_mf_factor_level<T><<<g, kTB, smem, ctx->stream>>>(C.dev, lb, cnt, A->d_vals64, (T *)C.L, (T *)C.U,
+                                                            (T *)C.F, mf * mf, (T *)C.P, mf * kPanelStride, derr);
+        GRMP_LAUNCHED(ctx);
+    }
+    int herr = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    grmp_free(ctx, derr, 4);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "multifrontal factorisation");
+    if (herr)
+        return grmp_fail(ctx, GRMP_ERR_NAN, "multifrontal %s factorisation: non-positive pivot in front %d",
+                         sizeof(T) == 4 ? "FP32" : "FP64", herr - 1);
+    *grid_out = gmax;
+    return GRMP_OK;
+}
+
+// w <- A^{-1} w with the current factor (level launches)
+template <typename T>
+void mf_apply(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    MfCache &C = *A->mf;
+    const int nl = (int)C.level_ptr.size() - 1;
+    const size_t smem_f = ((size_t)C.max_s + 32 * 33) * sizeof(T);
+    const size_t smem_b = ((size_t)C.max_s + 32 * 33 + C.max_f) * sizeof(T);
+    cudaFuncSetAttribute(k_mf_forward_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
+    cudaFuncSetAttribute(k_mf_backward_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+    for (int l = 0; l < nl; l++) {
+        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
+        k_mf_forward_level<T><<<std::min(cnt, kMaxGrid), kTB, smem_f, ctx->stream>>>(C.dev, lb, cnt, (const T *)C.L,
+                                                                                     (T *)C.uv, (T *)C.w, C.max_s);
+        GRMP_LAUNCHED(ctx);
+    }
+    for (int l = nl - 1; l >= 0; l--) {
+        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
+        k_mf_backward_level<T><<<std::min(cnt, kMaxGrid), kTB, smem_b, ctx->stream>>>(C.dev, lb, cnt,
+                                                                                      (const T *)C.L, (T *)C.w,
+                                                                                      C.max_s);
+        GRMP_LAUNCHED(ctx);
+    }
+}
+
+double host_sum(grmp_context ctx, const double *dpart, int nb, cudaError_t *e) {
+    std::vector<double> h(nb);
+    *e = cudaMemcpyAsync(h.data(), dpart, (size_t)nb * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (*e == cudaSuccess) *e = cudaStreamSynchronize(ctx->stream);
+    double s = 0.0;
+    for (double v : h) s += v;   // fixed order
+    return s;
+}
+
+}  // namespace
+
+void grmp_mf_cache_free(grmp_matrix A) {
+    if (!A || !A->mf) return;
+    grmp_context ctx = A->space->mesh->ctx;
+    mf_free_numeric(ctx, *A->mf);
+    for (auto &b : A->mf->bufs) grmp_free(ctx, b.first, b.second);
+    delete A->mf;
+    A->mf = nullptr;
+}
+
+// grmp_solve for the direct modes; called with the context locked.
+int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int n = A->nrows;
+    const bool mixed = p->mode == GRMP_SOLVE_MIXED_DIRECT;
+    if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: FP64 values not assembled");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    int rc = A->mf ? GRMP_OK : mf_build(A);
+    int grid = 0;
+    if (!rc) rc = mixed ? mf_numeric<float>(A, &grid) : mf_numeric<double>(A, &grid);
+    const int nb = 2 * ctx->num_sms, tb = 256;
+    double *r = nullptr, *z = nullptr, *pp = nullptr, *q = nullptr, *part = nullptr;
+    const size_t vb = (size_t)n * 8;
+    if (!rc) rc = grmp_alloc(ctx, (void **)&r, vb);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&z, vb);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&pp, vb);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&q, vb);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&part, (size_t)nb * 8);
+    auto cleanup = [&]() {
+        grmp_free(ctx, r, vb);
+        grmp_free(ctx, z, vb);
+        grmp_free(ctx, pp, vb);
+        grmp_free(ctx, q, vb);
+        grmp_free(ctx, part, (size_t)nb * 8);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    };
+    if (rc) {
+        cleanup();
+        return rc;
+    }
+    MfCache &C = *A->mf;
+    cudaError_t e = cudaSuccess;
+    const int gv = (n + tb - 1) / tb;
+    if (!p->use_initial_guess) cudaMemsetAsync(x->d, 0, vb, ctx->stream);
+    k_dot<<<nb, tb, 0, ctx->stream>>>(n, b->d, b->d, part);
+    GRMP_LAUNCHED(ctx);
+    const double bn = sqrt(host_sum(ctx, part, nb, &e));
+    const double tol = std::max(p->abstol, p->reltol * bn);
+    int it = 0, status = GRMP_ERR_NOT_CONVERGED;
+    double rn = 0.0;
+    if (!mixed) {
+        // FP64 factor: x += A^{-1} (b - A x) until reltol or the residual stops falling
+        double prev = INFINITY;
+        for (;; it++) {
+            k_resid<<<nb, tb, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, x->d, b->d, r, part);
+            GRMP_LAUNCHED(ctx);
+            rn = sqrt(host_sum(ctx, part, nb, &e));
+            if (e != cudaSuccess) break;
+            if (rn <= tol || bn == 0.0) {
+                status = GRMP_OK;
+                break;
+            }
+            if ((it > 0 && rn > 0.5 * prev) || it >= std::min(p->maxiter, 8)) {
+                // the residual stopped falling (FP64 floor of an ill-conditioned system):
+                // accept when the normwise backward error ||r|| / (||A|| ||x|| + ||b||) is at rounding level
+                k_rownorm<<<nb, tb, 0, ctx->stream>>>(n, A->d_rowptr, A->d_vals64, part);
+                GRMP_LAUNCHED(ctx);
+                std::vector<double> hm(nb);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(hm.data(), part, (size_t)nb * 8, cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                double anorm = 0.0;
+                for (double v : hm) anorm = std::max(anorm, v);
+                k_dot<<<nb, tb, 0, ctx->stream>>>(n, x->d, x->d, part);
+                GRMP_LAUNCHED(ctx);
+                const double xn = sqrt(host_sum(ctx, part, nb, &e));
+                const double eta = rn / (anorm * xn + bn + 1e-300);
+                status = (it > 0 && rn > 0.5 * prev && eta <= 1e-13) ? GRMP_OK : GRMP_ERR_NOT_CONVERGED;
+                break;
+            }
+            prev = rn;
+            cudaMemcpyAsync(C.w, r, vb, cudaMemcpyDeviceToDevice, ctx->stream);
+            mf_apply<double>(A);
+            k_add_from<double><<<gv, tb, 0, ctx->stream>>>(n, (const double *)C.w, x->d);
+            GRMP_LAUNCHED(ctx);
+        }
+    } else {
+        // FP64 conjugate gradients preconditioned by the FP32 factorisation
+        k_resid<<<nb, tb, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, x->d, b->d, r, part);
+        GRMP_LAUNCHED(ctx);
+        rn = sqrt(host_sum(ctx, part, nb, &e));
+        auto precond = [&]() -> double {   // z = M^{-1} r, returns r.z
+            k_to<float><<<gv, tb, 0, ctx->stream>>>(n, r, (float *)C.w);
+            GRMP_LAUNCHED(ctx);
+            mf_apply<float>(A);
+            k_from_dot<float><<<nb, tb, 0, ctx->stream>>>(n, (const float *)C.w, r, z, part);
+            GRMP_LAUNCHED(ctx);
+            return host_sum(ctx, part, nb, &e);
+        };
+        // CG with restarts from the true FP64 residual: when the recurrence
+        // residual has converged but b - A x has not, restart from x (at most
+        // 3 times); a residual that no longer falls is accepted when its
+        // normwise backward error is at FP64 rounding level.
+        double prev_true = INFINITY;
+        for (int restart = 0; restart < 4 && e == cudaSuccess; restart++) {
+            double rz = rn <= tol ? 0.0 : precond();
+            cudaMemcpyAsync(pp, z, vb, cudaMemcpyDeviceToDevice, ctx->stream);
+            status = GRMP_ERR_NOT_CONVERGED;
+            while (e == cudaSuccess) {
+                if (rn <= tol || bn == 0.0) {
+                    status = GRMP_OK;
+                    break;
+                }
+                if (it >= p->maxiter) break;
+                k_apply_dot<<<nb, tb, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, pp, q, part);
+                GRMP_LAUNCHED(ctx);
+                const double pq = host_sum(ctx, part, nb, &e);
+                if (!(pq > 0.0) || !std::isfinite(pq)) {
+                    status = GRMP_ERR_NAN;
+                    break;
+                }
+                const double alpha = rz / pq;
+                k_cg_update<<<nb, tb, 0, ctx->stream>>>(n, alpha, pp, q, x->d, r, part);
+                GRMP_LAUNCHED(ctx);
+                rn = sqrt(host_sum(ctx, part, nb, &e));
+                it++;
+                if (rn <= tol) continue;
+                const double rz_new = precond();
+                k_xpby<<<gv, tb, 0, ctx->stream>>>(n, z, rz_new / rz, pp);
+                GRMP_LAUNCHED(ctx);
+                rz = rz_new;
+            }
+            if (e != cudaSuccess || status == GRMP_ERR_NAN) break;
+            // the true FP64 residual of the iterate (r becomes b - A x)
+            k_resid<<<nb, tb, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, x->d, b->d, r, part);
+            GRMP_LAUNCHED(ctx);
+            rn = sqrt(host_sum(ctx, part, nb, &e));
+            if (rn <= 2.0 * tol) {
+                status = GRMP_OK;
+                break;
+            }
+            if (rn > 0.5 * prev_true || it >= p->maxiter) {
+                k_rownorm<<<nb, tb, 0, ctx->stream>>>(n, A->d_rowptr, A->d_vals64, part);
+                GRMP_LAUNCHED(ctx);
+                std::vector<double> hm(nb);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(hm.data(), part, (size_t)nb * 8, cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                double anorm = 0.0;
+                for (double v : hm) anorm = std::max(anorm, v);
+                k_dot<<<nb, tb, 0, ctx->stream>>>(n, x->d, x->d, part);
+                GRMP_LAUNCHED(ctx);
+                const double xn = sqrt(host_sum(ctx, part, nb, &e));
+                status = rn / (anorm * xn + bn + 1e-300) <= 1e-13 ? GRMP_OK : GRMP_ERR_NOT_CONVERGED;
+                break;
+            }
+            prev_true = rn;
+            status = GRMP_ERR_NOT_CONVERGED;
+        }
+    }
+    cudaEventRecord(e1, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cleanup();
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "multifrontal solve");
+    st->status = status;
+    st->iterations = it;
+    st->outer_iterations = 0;
+    st->spmv_config = 0;
+    st->grid_blocks = grid;
+    st->final_relres = bn > 0 ? rn / bn : 0.0;
+    st->solve_ms = ms;
+    if (status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, status, "direct solve: relative residual %.3e after %d steps", st->final_relres, it);
+    if (status == GRMP_ERR_NAN) return grmp_fail(ctx, status, "direct solve: breakdown of the preconditioned CG");
+    return status;
+}

@@ -229,5 +229,29 @@ int nd_symbolic_build(int n, const int32_t *rowptr, const int32_t *cols, NdSymbo
     }
     S->L_size = Loff;
     S->U_size = Uoff;
+    // level schedule (height above the leaves) and update-vector offsets
+    std::vector<int> height(nn, 0);
+    int maxh = 0;
+    for (int t = 0; t < nn; t++) {
+        for (int c : B.kids[t]) height[t] = std::max(height[t], height[c] + 1);
+        maxh = std::max(maxh, height[t]);
+    }
+    S->level_ptr.assign(maxh + 2, 0);
+    for (int t = 0; t < nn; t++) S->level_ptr[height[t] + 1]++;
+    for (int l = 0; l <= maxh; l++) S->level_ptr[l + 1] += S->level_ptr[l];
+    S->level_nodes.resize(nn);
+    S->level_maxf.assign(maxh + 1, 0);
+    std::vector<int> fill(S->level_ptr.begin(), S->level_ptr.end() - 1);
+    for (int t = 0; t < nn; t++) {
+        S->level_nodes[fill[height[t]]++] = t;
+        S->level_maxf[height[t]] = std::max(S->level_maxf[height[t]], S->node[t].f);
+    }
+    S->uv_off.resize(nn);
+    int64_t uo = 0;
+    for (int t = 0; t < nn; t++) {
+        S->uv_off[t] = uo;
+        uo += S->node[t].f - S->node[t].s;
+    }
+    S->uv_size = uo;
     return 0;
 }

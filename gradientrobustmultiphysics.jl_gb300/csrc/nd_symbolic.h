@@ -22,6 +22,11 @@ struct NdSymbolic {
     std::vector<NdNode> node;       // post-order
     std::vector<int32_t> front, child, ent_rel, ent_pos, ext;
     int64_t L_size = 0, U_size = 0;
+    // level schedule: nodes grouped by height above the leaves (children
+    // always in a lower level), level_nodes[level_ptr[l] .. level_ptr[l+1])
+    std::vector<int32_t> level_ptr, level_nodes, level_maxf;
+    std::vector<int64_t> uv_off;    // per node: offset of its update vector (f - s values)
+    int64_t uv_size = 0;
 };
 
 // rowptr/cols: the local pattern (cols local to the problem, diagonal

@@ -559,10 +559,12 @@ extern "C" int grmp_matrix_destroy(grmp_matrix A) {
     grmp_free(ctx, A->d_slot, ncl * A->space->ldofs * A->slot_bytes);
     grmp_free(ctx, A->d_vals64, (size_t)A->nnz * 8);
     grmp_free(ctx, A->d_vals32, (size_t)A->nnz * 4);
+    grmp_free(ctx, A->d_pack32, (size_t)A->nnz * 8);
     grmp_free(ctx, A->d_fixed, (size_t)A->nrows);
     grmp_free(ctx, A->d_work, A->work_bytes);
     grmp_free(ctx, A->d_cellfac, A->cellfac_bytes);
     grmp_direct_cache_free(A);
+    grmp_mf_cache_free(A);
     cudaStreamSynchronize(ctx->stream);
     delete A;
     return GRMP_OK;

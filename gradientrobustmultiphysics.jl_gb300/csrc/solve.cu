@@ -94,21 +94,44 @@ __device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh,
 // by chunk, u = 0..U-1 within a chunk, then the lane reduction) does not
 // depend on the pipelining.  gather(c) returns x[c]; epi(r, s) consumes the
 // row sum (lane 0 of the group).
-template <int U, int TPR, typename A, typename V>
-__device__ __forceinline__ void load_chunk(const int32_t *__restrict__ cols, const V *__restrict__ vals, int k, int e,
-                                           int *c, A *v) {
+// Matrix entry sources: CSR arrays (column indices and values apart), or
+// the FP32 copy packed as (column, value bits) pairs, one 8-byte load each.
+template <typename V>
+struct CsrSource {
+    const int32_t *__restrict__ cols;
+    const V *__restrict__ vals;
+    template <typename A>
+    __device__ __forceinline__ void get(int idx, int &c, A &v) const {
+        c = __ldg(cols + idx);
+        v = (A)__ldg(vals + idx);
+    }
+};
+
+struct PackedSource {
+    const int2 *__restrict__ pack;
+    __device__ __forceinline__ void get(int idx, int &c, float &v) const {
+        const int2 p = __ldg(pack + idx);
+        c = p.x;
+        v = __int_as_float(p.y);
+    }
+};
+
+template <int U, int TPR, typename A, typename S>
+__device__ __forceinline__ void load_chunk(const S &src, int k, int e, int *c, A *v) {
 #pragma unroll
     for (int u = 0; u < U; u++) {
         const int idx = k + u * TPR;
-        const bool ok = idx < e;
-        c[u] = ok ? __ldg(cols + idx) : 0;
-        v[u] = ok ? (A)__ldg(vals + idx) : A(0);
+        if (idx < e) {
+            src.get(idx, c[u], v[u]);
+        } else {
+            c[u] = 0;
+            v[u] = A(0);
+        }
     }
 }
 
-template <int TPR, int U, bool PIPE, typename A, typename V, typename G, typename E>
-__device__ __forceinline__ void spmv_rows(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
-                                          const V *__restrict__ vals, G gather, E epi) {
+template <int TPR, int U, bool PIPE, typename A, typename S, typename G, typename E>
+__device__ __forceinline__ void spmv_rows(int n, const int32_t *__restrict__ rowptr, const S src, G gather, E epi) {
     constexpr int RPW = 32 / TPR;   // rows per warp per step
     constexpr int CH = TPR * U;
     const int lane = threadIdx.x & (TPR - 1);
@@ -125,7 +148,7 @@ __device__ __forceinline__ void spmv_rows(int n, const int32_t *__restrict__ row
                 for (int k = kb + lane; k < e; k += CH) {
                     int c[U];
                     A v[U];
-                    load_chunk<U, TPR>(cols, vals, k, e, c, v);
+                    load_chunk<U, TPR>(src, k, e, c, v);
 #pragma unroll
                     for (int u = 0; u < U; u++) s += v[u] * gather(c[u]);
                 }
@@ -148,12 +171,12 @@ __device__ __forceinline__ void spmv_rows(int n, const int32_t *__restrict__ row
     }
     int c[U];
     A v[U];
-    load_chunk<U, TPR>(cols, vals, kb + lane, e, c, v);
+    load_chunk<U, TPR>(src, kb + lane, e, c, v);
     for (int base = warp * RPW; base < n; base += stride) {
         // next row: first chunk; the row after: bounds
         int cn[U];
         A vn[U];
-        load_chunk<U, TPR>(cols, vals, kbn + lane, en, cn, vn);
+        load_chunk<U, TPR>(src, kbn + lane, en, cn, vn);
         const int r2 = r + 2 * stride;
         int kb2 = 0, e2 = 0;
         if (r2 < n) {
@@ -166,7 +189,7 @@ __device__ __forceinline__ void spmv_rows(int n, const int32_t *__restrict__ row
         for (int k = kb + lane + CH; k < e; k += CH) {   // rows longer than one chunk
             int c2[U];
             A v2[U];
-            load_chunk<U, TPR>(cols, vals, k, e, c2, v2);
+            load_chunk<U, TPR>(src, k, e, c2, v2);
 #pragma unroll
             for (int u = 0; u < U; u++) s += v2[u] * gather(c2[u]);
         }
@@ -198,7 +221,7 @@ __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ r
     double dot = 0;
     A dacc = 0;
     spmv_rows<TPR, U, PIPE, A>(
-        n, rowptr, cols, vals, [&](int c) { return (A)x[c]; },
+        n, rowptr, CsrSource<V>{cols, vals}, [&](int c) { return (A)x[c]; },
         [&](int r, A s) {
             if (RESID) {
                 double v = b[r] - (double)s;
@@ -293,12 +316,11 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
 // stores p_k(r) into nxt[r].y, and phase B stores z_{k+1} into nxt[r].x.
 // This removes the separate p-update pass and one grid barrier per iteration.
 template <int TPR, int U, bool PIPE>
-__device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr,
-                                               const int32_t *__restrict__ cols, const float *__restrict__ vals,
+__device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr, const int2 *__restrict__ pack,
                                                const float2 *cur, float *nxt_f, float *q, float beta) {
     float dacc = 0.f;
     spmv_rows<TPR, U, PIPE, float>(
-        n, rowptr, cols, vals,
+        n, rowptr, PackedSource{pack},
         [&](int c) {
             const float2 g = cur[c];
             return __fmaf_rn(beta, g.y, g.x);
@@ -314,8 +336,8 @@ __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict_
 }
 
 template <int TPR, int U, bool PIPE>
-__global__ void __launch_bounds__(PTPB, U >= 8 ? (PIPE ? 3 : 4) : 5) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
-                                                    const double *vals64, const float *vals32, const double *b,
+__global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 5)) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+                                                    const double *vals64, const int2 *pack32, const double *b,
                                                     double *x, const float *dinv, float *r, float *q, float *xc,
                                                     float2 *zp0, float2 *zp1, double *r64, double *partial,
                                                     SolveState *st, double abstol, double reltol, double delta,
@@ -363,7 +385,7 @@ __global__ void __launch_bounds__(PTPB, U >= 8 ? (PIPE ? 3 : 4) : 5) k_pcg_mixed
     while (!conv && it < maxit && outer < maxouter) {
         float *nxt_f = reinterpret_cast<float *>(nxt);
         double d[1];
-        d[0] = (double)spmv_fused_zp<TPR, U, PIPE>(n, rowptr, cols, vals32, cur, nxt_f, q, beta);
+        d[0] = (double)spmv_fused_zp<TPR, U, PIPE>(n, rowptr, pack32, cur, nxt_f, q, beta);
         if (!grid_sum<1>(d, partial, sh, st)) return;   // barrier 1
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
@@ -440,6 +462,13 @@ __global__ void __launch_bounds__(PTPB, U >= 8 ? (PIPE ? 3 : 4) : 5) k_pcg_mixed
 }
 
 // ------------------------------------------------------------------ helpers
+// FP32 copy of the matrix packed as (column, value bits) pairs for the mixed
+// solver's SpMV (one 8-byte load per nonzero instead of two 4-byte loads).
+__global__ void k_pack32(long long nnz, const int32_t *cols, const float *vals, int2 *pack) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz) pack[k] = make_int2(cols[k], __float_as_int(vals[k]));
+}
+
 template <typename V>
 __global__ void k_dinv(int n, const int32_t *rowptr, const int32_t *cols, const V *vals, V *dinv, int *bad) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -554,7 +583,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         double at = p->abstol, rt = p->reltol, dl = p->inner_reltol > 0 && p->inner_reltol < 1 ? p->inner_reltol : 0.1;
         const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
         const double *v64 = A->d_vals64, *bb = bvec;
-        const float *v32 = A->d_vals32;
+        const int2 *v32 = (const int2 *)A->d_pack32;
         double *xx = xvec;
         void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
                         &at, &rt, &dl, &mi, &mo, &guess};
@@ -683,6 +712,16 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     grmp_free(ctx, bad, 4);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
+    if (mixed) {   // refresh the packed FP32 copy (values may have been reassembled)
+        const size_t pb = (size_t)A->nnz * 8;
+        if (!A->d_pack32) {
+            int prc = grmp_alloc(ctx, &A->d_pack32, pb);
+            if (prc) return prc;
+        }
+        k_pack32<<<(unsigned)((A->nnz + 255) / 256), 256, 0, ctx->stream>>>(A->nnz, A->d_cols, A->d_vals32,
+                                                                           (int2 *)A->d_pack32);
+        GRMP_LAUNCHED(ctx);
+    }
     int cfg = p->spmv_config;
     if (cfg == 0) {   // autotuned once per matrix and solver mode
         int &slot = mixed ? A->tuned_cfg32 : A->tuned_cfg;

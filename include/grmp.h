@@ -226,9 +226,13 @@ int grmp_apply_dirichlet(grmp_matrix A, grmp_vector b, int32_t nfixed, const int
 typedef enum {
     GRMP_SOLVE_FP64 = 0,   /* plain: FP64 Jacobi-PCG                                                 */
     GRMP_SOLVE_MIXED = 1,  /* FP32 Jacobi-PCG inside FP64 refinement (outer residual, update in FP64) */
-    GRMP_SOLVE_DIRECT = 2  /* grmp_stokes_batch_solve only: FP64 multifrontal Cholesky per problem
-                              (nested-dissection order), factored once and reused by every sweep,
-                              with residual refinement against the assembled FP64 matrix          */
+    GRMP_SOLVE_DIRECT = 2, /* FP64 multifrontal Cholesky (nested-dissection order) + residual
+                              refinement against the assembled FP64 matrix; in
+                              grmp_stokes_batch_solve one factorisation per problem, reused by
+                              every sweep.  SPD matrices (Dirichlet eliminated or penalised).     */
+    GRMP_SOLVE_MIXED_DIRECT = 3 /* grmp_solve only: FP32 multifrontal Cholesky used as the
+                              preconditioner of FP64 conjugate gradients on the FP64 matrix
+                              (Dirichlet rows must be eliminated: 1e60 overflows FP32)           */
 } grmp_solve_mode;
 
 typedef struct {
