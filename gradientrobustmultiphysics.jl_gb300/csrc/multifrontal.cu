@@ -95,6 +95,185 @@ __global__ void __launch_bounds__(kTB) k_mf_factor_level(MfDev m, int lb, int co
     }
 }
 
+// One large front by the whole grid (cooperative launch, bounded grid
+// barriers): assembly, then per panel of kPanel columns (a) block 0 factors
+// the diagonal block, (b) every thread solves rows below it against the
+// diagonal block (L21 = A21 L11^-T, also staged into the panel buffer P),
+// (c) the trailing lower triangle gets the rank-kPanel update from 4x4
+// register tiles spread over all blocks.  Same arithmetic per entry as
+// front_cholesky, spread over the GPU instead of one block.
+struct CoopState {
+    GridBarrier bar;
+    int status;   // GRMP_ERR_TIMEOUT if a barrier wait gave up
+    int abort;    // non-positive pivot found
+};
+
+// Body of the grouped large-front factorisation: `grank` = this
+// block's rank in the group, `gblocks` = blocks in the group, `sync()` = the
+// group's barrier (returns false when a bounded wait gave up), `abort` = the
+// group's pivot-failure flag (global memory, zero on entry).
+template <typename T, typename Sync>
+__device__ void group_factor(MfDev m, int t, const double *vals, T *L, T *U, T *F, T *P, int grank, int gblocks,
+                             Sync sync, int *abort, int *err) {
+    __shared__ T dt[kPanel][kPanel + 1];
+    const long long gtid = (long long)grank * blockDim.x + threadIdx.x, gsz = (long long)gblocks * blockDim.x;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const long long gwarp = gtid >> 5, nwarps = gsz >> 5;
+    const MfNode nd = m.node[t];
+    const int f = nd.f, s = nd.s;
+    for (long long k = gtid; k < (long long)f * f; k += gsz) F[k] = T(0);
+    if (!sync()) return;
+    for (long long e = gtid; e < nd.nentry; e += gsz) F[m.ent_pos[nd.entry_off + e]] = (T)vals[m.ent_rel[nd.entry_off + e]];
+    if (!sync()) return;
+    for (int c = 0; c < nd.nchild; c++) {
+        const MfNode cn = m.node[m.child[nd.child_off + c]];
+        const int sc = cn.f - cn.s;
+        const T *Uc = U + cn.U_off;
+        const int32_t *ex = m.ext + cn.ext_off;
+        for (long long a = gwarp; a < sc; a += nwarps) {
+            const long long pa = (long long)ex[a] * f;
+            for (int b = lane; b <= a; b += 32) F[pa + ex[b]] += Uc[a * sc + b];
+        }
+        if (!sync()) return;
+    }
+    for (int k0 = 0; k0 < s; k0 += kPanel) {
+        const int kw = min(kPanel, s - k0), k1 = k0 + kw, mrows = f - k1;
+        if (grank == 0) {   // (a) diagonal block
+            for (int q = tid; q < kw * kw; q += blockDim.x) {
+                const int r = q / kw, c = q - r * kw;
+                dt[r][c] = c <= r ? F[(long long)(k0 + r) * f + k0 + c] : T(0);
+            }
+            __syncthreads();
+            bool bad = false;
+            for (int c = 0; c < kw; c++) {
+                const T dcc = dt[c][c];
+                if (!(dcc > T(0)) || !isfinite((double)dcc)) {
+                    bad = true;
+                    break;
+                }
+                const T dk = sqrt(dcc);
+                __syncthreads();
+                if (tid > c && tid < kw) dt[tid][c] /= dk;
+                if (tid == 0) dt[c][c] = dk;
+                __syncthreads();
+                const int r = c + 1 + tid / kw, cc = c + 1 + tid % kw;
+                if (tid < kw * kw && r < kw && cc <= r) dt[r][cc] -= dt[r][c] * dt[cc][c];
+                __syncthreads();
+            }
+            if (bad) {
+                if (tid == 0) {
+                    *(volatile int *)abort = 1;
+                    atomicCAS(err, 0, t + 1);
+                }
+            } else {
+                for (int q = tid; q < kw * kw; q += blockDim.x) {
+                    const int r = q / kw, c = q - r * kw;
+                    if (c <= r) F[(long long)(k0 + r) * f + k0 + c] = dt[r][c];
+                }
+            }
+        }
+        if (!sync()) return;
+        if (*(volatile int *)abort) return;
+        // (b) rows below the diagonal block
+        for (int q = tid; q < kw * kw; q += blockDim.x) {
+            const int r = q / kw, c = q - r * kw;
+            dt[r][c] = c <= r ? F[(long long)(k0 + r) * f + k0 + c] : T(0);
+        }
+        __syncthreads();
+        for (long long i = k1 + gtid; i < f; i += gsz) {
+            T xr[kPanel];
+            T *Fi = F + i * f + k0;
+#pragma unroll
+            for (int j = 0; j < kPanel; j++) {
+                if (j < kw) {
+                    T a = Fi[j];
+                    for (int l = 0; l < j; l++) a -= xr[l] * dt[j][l];
+                    xr[j] = a / dt[j][j];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kPanel; j++)
+                if (j < kw) {
+                    Fi[j] = xr[j];
+                    P[(i - k1) * kPanelStride + j] = xr[j];
+                }
+        }
+        if (!sync()) return;
+        // (c) trailing update
+        const int nt = (mrows + 3) >> 2;
+        const long long ntiles = (long long)nt * (nt + 1) / 2;
+        for (long long q = gtid; q < ntiles; q += gsz) {
+            int bi = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+            while ((long long)(bi + 1) * (bi + 2) / 2 <= q) bi++;
+            while ((long long)bi * (bi + 1) / 2 > q) bi--;
+            const int bj = (int)(q - (long long)bi * (bi + 1) / 2);
+            const int i0 = bi * 4, j0 = bj * 4;
+            T acc[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+            for (int tt = 0; tt < kw; tt++) {
+                T x[4], y[4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    x[a] = i0 + a < mrows ? P[(long long)(i0 + a) * kPanelStride + tt] : T(0);
+                    y[a] = j0 + a < mrows ? P[(long long)(j0 + a) * kPanelStride + tt] : T(0);
+                }
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[a][b] += x[a] * y[b];
+            }
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int i = i0 + a;
+                if (i >= mrows) break;
+                T *Fi = F + (long long)(k1 + i) * f + k1;
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int j = j0 + b;
+                    if (j <= i) Fi[j] -= acc[a][b];
+                }
+            }
+        }
+        if (!sync()) return;
+    }
+    T *Lt = L + nd.L_off;
+    for (long long k = gtid; k < (long long)f * s; k += gsz) {
+        const int i = (int)(k / s), j = (int)(k - (long long)i * s);
+        Lt[k] = j <= i ? F[(long long)i * f + j] : T(0);
+    }
+    const int sc = f - s;
+    T *Ut = U + nd.U_off;
+    for (long long k = gtid; k < (long long)sc * sc; k += gsz) {
+        const int a = (int)(k / sc), b = (int)(k - (long long)a * sc);
+        if (b <= a) Ut[k] = F[(long long)(s + a) * f + s + b];
+    }
+}
+
+
+// The large fronts of one level by the whole grid split into `ngroups`
+// groups (block b belongs to group b % ngroups, so every group spans all
+// SMs evenly); group g factors fronts g, g + ngroups, ... of the level, each
+// group with its own bounded barrier, front and panel buffers.  One
+// cooperative launch per level.
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_group_factor(MfDev m, int lb, int count, int ngroups, const double *vals,
+                                                         T *L, T *U, T *Fpool, long long fslot, T *Ppool,
+                                                         long long pslot, CoopState *cs, int *err) {
+    const int g = blockIdx.x % ngroups, grank = blockIdx.x / ngroups;
+    const int gblocks = (gridDim.x - g + ngroups - 1) / ngroups;
+    CoopState *c = cs + g;
+    auto sync = [&]() { return grid_barrier(&c->bar, gblocks, &c->status); };
+    for (int q = g; q < count; q += ngroups) {
+        group_factor<T>(m, m.lvl_nodes[lb + q], vals, L, U, Fpool + g * fslot, Ppool + g * pslot, grank, gblocks, sync,
+                        &c->abort, err);
+        if (*(volatile int *)&c->abort || *(volatile int *)&c->status) return;
+        if (!sync()) return;   // buffers reused by the group's next front
+    }
+}
+
 // ---------------------------------------------------------------- solves
 // Forward: ys = w[own] minus the children's update entries for own DoFs,
 // L11 y = ys, and the node's update vector = children's entries for its
@@ -213,6 +392,181 @@ __global__ void __launch_bounds__(kTB) k_mf_backward_level(MfDev m, int lb, int 
             __syncthreads();
         }
         for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- inverse-based solves
+// For the FP32 preconditioner, applied once per CG iteration, each front
+// keeps Q = [L11^-1 ; G] with G = L21 L11^-1 (same f x s layout as its
+// factor columns).  Forward:  y_own = L11^-1 b_own,  u_struct += G b_own;
+// backward: x_own = L11^-T y_own - G^T x_struct.  Every output is one dot
+// product: a level is one or two fully parallel launches, with no
+// sequential triangular chain inside a front.
+
+// index idx in [lo, hi) with pref[idx] <= item < pref[idx + 1]
+__device__ __forceinline__ int find_seg(const long long *pref, int lo, int hi, long long item) {
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pref[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// L11^-1 by 32 x 32 blocks: one thread block per (front, block column c).
+// X_cc solves L_cc X = I; for b > c, X_bc solves L_bb X = -sum_{m=c}^{b-1} L_bm X_mc
+// (the sum as a small GEMM by all threads, the 32-column triangular solve by
+// one warp, each lane a column).  Block columns are independent.
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_invert(MfDev m, const long long *bcol, int nn, const T *L, T *Q) {
+    __shared__ T Lbb[32][33];
+    __shared__ T Tb[32][33];
+    const long long item = blockIdx.x;
+    const int idx = find_seg(bcol, 0, nn, item);
+    const MfNode nd = m.node[m.lvl_nodes[idx]];
+    const int s = nd.s, c = (int)(item - bcol[idx]);
+    const T *Lt = L + nd.L_off;
+    T *Qt = Q + nd.L_off;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nbk = (s + 31) / 32;
+    const int c0 = c * 32, cw = min(32, s - c0);
+    for (int b = c; b < nbk; b++) {
+        const int b0 = b * 32, bw = min(32, s - b0);
+        // Tb = (b == c ? I : -sum_m L_bm X_mc), Lbb = L_bb
+        for (int q = tid; q < 32 * 32; q += blockDim.x) {
+            const int r = q >> 5, cc = q & 31;
+            T acc = T(0);
+            if (r < bw && cc < cw) {
+                if (b == c) {
+                    acc = r == cc ? T(1) : T(0);
+                } else {
+                    const T *Lr = Lt + (long long)(b0 + r) * s;
+                    for (int k = c0; k < b0; k++) acc -= Lr[k] * Qt[(long long)k * s + c0 + cc];
+                }
+            }
+            Tb[r][cc] = acc;
+            Lbb[r][cc] = (r < bw && cc <= r) ? Lt[(long long)(b0 + r) * s + b0 + cc] : T(0);
+        }
+        __syncthreads();
+        if (warp == 0 && lane < cw) {   // forward substitution, column `lane`
+            for (int r = 0; r < bw; r++) {
+                T v = Tb[r][lane];
+                for (int k = 0; k < r; k++) v -= Lbb[r][k] * Tb[k][lane];
+                Tb[r][lane] = v / Lbb[r][r];
+            }
+        }
+        __syncthreads();
+        for (int q = tid; q < bw * cw; q += blockDim.x) {
+            const int r = q / cw, cc = q - r * cw;
+            Qt[(long long)(b0 + r) * s + c0 + cc] = Tb[r][cc];
+        }
+        __syncthreads();
+    }
+}
+
+// G = L21 L11^-1, one thread per entry (i, k)
+template <typename T>
+__global__ void k_mf_gmat(MfDev m, const long long *gpref, int nn, long long total, const T *L, T *Q) {
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= total) return;
+    const int idx = find_seg(gpref, 0, nn, item);
+    const MfNode nd = m.node[m.lvl_nodes[idx]];
+    const int s = nd.s;
+    const long long e = item - gpref[idx];
+    const int i = (int)(e / s), k = (int)(e - (long long)i * s);
+    const T *Lr = L + nd.L_off + (long long)(s + i) * s;
+    const T *Qt = Q + nd.L_off;
+    T acc = T(0);
+    for (int mm = k; mm < s; mm++) acc += Lr[mm] * Qt[(long long)mm * s + k];
+    Q[nd.L_off + (long long)(s + i) * s + k] = acc;
+}
+
+// forward, part 1 (block per front): the children's update entries, own ones
+// subtracted from w in place, structure ones summed into the front's update vector
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_gather_level(MfDev m, int lb, int count, T *uv, T *w) {
+    const int tid = threadIdx.x, bs = blockDim.x;
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const MfNode nd = m.node[m.lvl_nodes[lb + q]];
+        const int s = nd.s, sc = nd.f - nd.s;
+        const int32_t *fr = m.front + nd.front_off;
+        T *ut = uv + nd.uv_off;
+        for (int i = tid; i < sc; i += bs) ut[i] = T(0);
+        __syncthreads();
+        for (int c = 0; c < nd.nchild; c++) {
+            const MfNode cn = m.node[m.child[nd.child_off + c]];
+            const int scc = cn.f - cn.s;
+            const T *uc = uv + cn.uv_off;
+            const int32_t *ex = m.ext + cn.ext_off;
+            for (int a = tid; a < scc; a += bs) {
+                const int pos = ex[a];
+                if (pos < s) w[fr[pos]] -= uc[a];
+                else ut[pos - s] += uc[a];
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// forward, part 2 (warp per row of Q over the level): y_own, update vector
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_qmul_level(MfDev m, const long long *qrow, int lb, int cnt, const T *Q,
+                                                       T *uv, const T *w, T *wy) {
+    const long long r0 = qrow[lb], nrows = qrow[lb + cnt] - r0;
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarp = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long it = gw; it < nrows; it += nwarp) {
+        const int idx = find_seg(qrow, lb, lb + cnt, r0 + it);
+        const MfNode nd = m.node[m.lvl_nodes[idx]];
+        const int s = nd.s, r = (int)(r0 + it - qrow[idx]);
+        const int32_t *fr = m.front + nd.front_off;
+        const T *Qr = Q + nd.L_off + (long long)r * s;
+        const int kend = r < s ? r + 1 : s;
+        T acc = T(0);
+        for (int k = lane; k < kend; k += 32) acc += Qr[k] * w[fr[k]];
+        acc = warp_sum_t<T>(acc);
+        if (lane == 0) {
+            if (r < s) wy[fr[r]] = acc;
+            else uv[nd.uv_off + r - s] += acc;
+        }
+    }
+}
+
+// backward: x_k = sum_j Q[j][k] y_j - sum_i G[i][k] x_struct_i.  A block
+// takes 32 consecutive own columns of the level (tx = column) and splits
+// the rows over 8 groups (ty); the 8 partial sums are added in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(kTB) k_mf_qtmul_level(MfDev m, const long long *scol, int lb, int cnt, const T *Q,
+                                                        const T *wy, T *wx) {
+    __shared__ T part[8][33];
+    const long long c0 = scol[lb], ncols = scol[lb + cnt] - c0;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (long long base = (long long)blockIdx.x * 32; base < ncols; base += (long long)gridDim.x * 32) {
+        const long long it = base + tx;
+        T acc = T(0);
+        int k = 0, idx = lb;
+        if (it < ncols) {
+            idx = find_seg(scol, lb, lb + cnt, c0 + it);
+            const MfNode nd = m.node[m.lvl_nodes[idx]];
+            const int s = nd.s, f = nd.f;
+            k = (int)(c0 + it - scol[idx]);
+            const int32_t *fr = m.front + nd.front_off;
+            const T *Qt = Q + nd.L_off;
+            for (int j = k + ty; j < f; j += 8) {
+                const T v = j < s ? wy[fr[j]] : -wx[fr[j]];
+                acc += Qt[(long long)j * s + k] * v;
+            }
+        }
+        part[ty][tx] = acc;
+        __syncthreads();
+        if (ty == 0 && it < ncols) {
+            T sum = T(0);
+            for (int g = 0; g < 8; g++) sum += part[g][tx];
+            const MfNode nd = m.node[m.lvl_nodes[idx]];
+            wx[m.front[nd.front_off + k]] = sum;
+        }
         __syncthreads();
     }
 }
@@ -366,7 +720,8 @@ __global__ void k_add_from(int n, const T *w, double *x) {
 struct MfCache {
     std::vector<std::pair<void *, size_t>> bufs;   // symbolic arrays
     MfDev dev{};
-    std::vector<int32_t> level_ptr, level_maxf, level_count;
+    std::vector<int32_t> level_ptr, level_maxf, level_small;   // level_small[l]: fronts below kBigFront first
+    std::vector<int32_t> level_nodes_host;                     // same order as dev.lvl_nodes
     int nnodes = 0, max_f = 0, max_s = 0;
     long long L_size = 0, U_size = 0, uv_size = 0;
     long long fpool = 0, ppool = 0;   // elements of the per-launch front / panel pools
@@ -374,11 +729,22 @@ struct MfCache {
     int esize = 0;
     void *L = nullptr, *U = nullptr, *uv = nullptr, *F = nullptr, *P = nullptr, *w = nullptr;
     size_t Lb = 0, Ub = 0, uvb = 0, Fb = 0, Pb = 0, wb = 0;
+    // inverse-based FP32 preconditioner: Q = [L11^-1; L21 L11^-1] per front, two more vectors
+    void *Q = nullptr, *wy = nullptr, *wx = nullptr;
+    size_t Qb = 0;
+    // prefixes over fronts in level order: rows (f), own columns (s), G entries (sc * s)
+    const long long *qrow = nullptr, *scol = nullptr, *gpref = nullptr, *bcol = nullptr;
+    long long total_cols = 0, total_g = 0, total_bcols = 0;
 };
 
 namespace {
 
 constexpr int kMaxGrid = 2 * 152;
+constexpr int kBigFront = 1024;   // fronts from this size up are factored by the whole grid
+constexpr int kCoopFront = 256;   // ... and from this size up in levels with fewer than kFillLevel fronts
+constexpr int kFillLevel = 152;
+constexpr int kGroups64 = 4;      // concurrent large fronts per level launch, FP64 (FP64 pipe bound: many SMs each)
+constexpr int kGroups32 = 16;     // ... FP32
 
 template <typename V>
 int mf_upload(grmp_context ctx, MfCache &C, const std::vector<V> &v, const V **out) {
@@ -402,8 +768,11 @@ void mf_free_numeric(grmp_context ctx, MfCache &C) {
     grmp_free(ctx, C.F, C.Fb);
     grmp_free(ctx, C.P, C.Pb);
     grmp_free(ctx, C.w, C.wb);
-    C.L = C.U = C.uv = C.F = C.P = C.w = nullptr;
-    C.Lb = C.Ub = C.uvb = C.Fb = C.Pb = C.wb = 0;
+    grmp_free(ctx, C.Q, C.Qb);
+    grmp_free(ctx, C.wy, C.wb);
+    grmp_free(ctx, C.wx, C.wb);
+    C.L = C.U = C.uv = C.F = C.P = C.w = C.Q = C.wy = C.wx = nullptr;
+    C.Lb = C.Ub = C.uvb = C.Fb = C.Pb = C.wb = C.Qb = 0;
     C.esize = 0;
 }
 
@@ -434,13 +803,39 @@ int mf_build(grmp_matrix A) {
     C->level_ptr = S.level_ptr;
     C->level_maxf = S.level_maxf;
     const int nl = (int)S.level_ptr.size() - 1;
+    // within each level: fronts below kBigFront first (one block each), then the big ones
+    // (one cooperative launch each, the whole grid on one front)
+    std::vector<int32_t> order = S.level_nodes;
+    C->level_small.assign(nl, 0);
     for (int l = 0; l < nl; l++) {
-        const int cnt = S.level_ptr[l + 1] - S.level_ptr[l];
-        const long long g = std::min(cnt, kMaxGrid);
-        const long long mf = S.level_maxf[l];
+        auto b0 = order.begin() + S.level_ptr[l], b1 = order.begin() + S.level_ptr[l + 1];
+        // a level too sparse to fill the GPU with one front per block sends its
+        // mid-size and large fronts to the whole grid
+        const bool sparse = S.level_ptr[l + 1] - S.level_ptr[l] < kFillLevel;
+        auto mid = std::stable_partition(b0, b1, [&](int32_t t) {
+            return S.node[t].f < (sparse ? kCoopFront : kBigFront);
+        });
+        C->level_small[l] = (int)(mid - b0);
+        const long long nbig = (long long)(b1 - mid);
+        const long long g = std::max<long long>(std::min<long long>(std::max(1, C->level_small[l]), kMaxGrid), nbig);
+        long long mf = 0;
+        for (auto it2 = b0; it2 != b1; ++it2) mf = std::max<long long>(mf, S.node[*it2].f);
         C->fpool = std::max(C->fpool, g * mf * mf);
         C->ppool = std::max(C->ppool, g * mf * kPanelStride);
     }
+    C->level_nodes_host = order;
+    std::vector<long long> qrow(S.nnodes + 1, 0), scol(S.nnodes + 1, 0), gpref(S.nnodes + 1, 0),
+        bcol(S.nnodes + 1, 0);
+    for (int i = 0; i < S.nnodes; i++) {
+        const NdNode &q = S.node[order[i]];
+        qrow[i + 1] = qrow[i] + q.f;
+        scol[i + 1] = scol[i] + q.s;
+        gpref[i + 1] = gpref[i] + (long long)(q.f - q.s) * q.s;
+        bcol[i + 1] = bcol[i] + (q.s + 31) / 32;
+    }
+    C->total_cols = scol[S.nnodes];
+    C->total_g = gpref[S.nnodes];
+    C->total_bcols = bcol[S.nnodes];
     A->mf = C;
     int rc = mf_upload(ctx, *C, node, &C->dev.node);
     if (!rc) rc = mf_upload(ctx, *C, S.front, &C->dev.front);
@@ -448,7 +843,11 @@ int mf_build(grmp_matrix A) {
     if (!rc) rc = mf_upload(ctx, *C, S.ent_rel, &C->dev.ent_rel);
     if (!rc) rc = mf_upload(ctx, *C, S.ent_pos, &C->dev.ent_pos);
     if (!rc) rc = mf_upload(ctx, *C, S.ext, &C->dev.ext);
-    if (!rc) rc = mf_upload(ctx, *C, S.level_nodes, &C->dev.lvl_nodes);
+    if (!rc) rc = mf_upload(ctx, *C, order, &C->dev.lvl_nodes);
+    if (!rc) rc = mf_upload(ctx, *C, qrow, &C->qrow);
+    if (!rc) rc = mf_upload(ctx, *C, scol, &C->scol);
+    if (!rc) rc = mf_upload(ctx, *C, gpref, &C->gpref);
+    if (!rc) rc = mf_upload(ctx, *C, bcol, &C->bcol);
     if (!rc) {
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "multifrontal upload");
@@ -491,27 +890,120 @@ int mf_numeric(grmp_matrix A, int *grid_out) {
     const size_t smem = (size_t)C.max_f * sizeof(T);
     cudaFuncSetAttribute(k_mf_factor_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int nl = (int)C.level_ptr.size() - 1;
-    int gmax = 0;
+    int gmax = 0, coop_grid = 0, ncs = 0;
+    bool timed_out = false;
+    CoopState *cs = nullptr;
+    cudaError_t e = cudaSuccess;
     for (int l = 0; l < nl; l++) {
-        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
-        const int g = std::min(cnt, kMaxGrid);
-        const long long mf = C.level_maxf[l];
-        gmax = std::max(gmax, g);
-        k_mf_factor_level<T><<<g, kTB, smem, ctx->stream>>>(C.dev, lb, cnt, A->d_vals64, (T *)C.L, (T *)C.U,
-                                                            (T *)C.F, mf * mf, (T *)C.P, mf * kPanelStride, derr);
-        GRMP_LAUNCHED(ctx);
+        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb, nsmall = C.level_small[l];
+        if (nsmall > 0) {
+            const int g = std::min(nsmall, kMaxGrid);
+            const long long mf = C.level_maxf[l];
+            gmax = std::max(gmax, g);
+            k_mf_factor_level<T><<<g, kTB, smem, ctx->stream>>>(C.dev, lb, nsmall, A->d_vals64, (T *)C.L, (T *)C.U,
+                                                                (T *)C.F, mf * mf, (T *)C.P, mf * kPanelStride, derr);
+            GRMP_LAUNCHED(ctx);
+        }
+        const int nbig = cnt - nsmall;
+        if (nbig > 0) {
+            // one cooperative launch for the level's large fronts; FP64 fronts get more SMs each
+            const int ng = std::min(nbig, sizeof(T) == 8 ? kGroups64 : kGroups32);
+            if (!cs || ng > ncs) {
+                grmp_free(ctx, cs, (size_t)ncs * sizeof(CoopState));
+                ncs = std::max(ng, kGroups32);
+                rc = grmp_alloc(ctx, (void **)&cs, (size_t)ncs * sizeof(CoopState));
+                if (rc) break;
+            }
+            if (!coop_grid) {
+                int per_sm = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_group_factor<T>, kTB, 0);
+                coop_grid = std::max(1, std::min(per_sm, 4)) * ctx->num_sms;
+            }
+            cudaMemsetAsync(cs, 0, (size_t)ng * sizeof(CoopState), ctx->stream);
+            MfDev dv = C.dev;
+            int lbb = lb + nsmall, cntb = nbig, ngv = ng;
+            const double *vv = A->d_vals64;
+            T *Lp = (T *)C.L, *Up = (T *)C.U, *Fp = (T *)C.F, *Pp = (T *)C.P;
+            long long mf = C.level_maxf[l], fs = mf * mf, ps = mf * kPanelStride;
+            void *args[] = {&dv, &lbb, &cntb, &ngv, &vv, &Lp, &Up, &Fp, &fs, &Pp, &ps, &cs, &derr};
+            e = cudaLaunchCooperativeKernel((void *)k_mf_group_factor<T>, coop_grid, kTB, args, 0, ctx->stream);
+            GRMP_LAUNCHED(ctx);
+            gmax = std::max(gmax, coop_grid);
+            if (e == cudaSuccess) {   // a timed-out barrier of any group fails the factorisation
+                std::vector<CoopState> hc(ng);
+                e = cudaMemcpyAsync(hc.data(), cs, (size_t)ng * sizeof(CoopState), cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                for (auto &h : hc) timed_out = timed_out || h.status != 0;
+            }
+        }
+        if (rc || e != cudaSuccess) break;
     }
     int herr = 0;
-    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     grmp_free(ctx, derr, 4);
+    grmp_free(ctx, cs, (size_t)ncs * sizeof(CoopState));
+    if (rc) return rc;
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "multifrontal factorisation");
+    if (timed_out) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "multifrontal factorisation: a grid barrier wait timed out");
     if (herr)
         return grmp_fail(ctx, GRMP_ERR_NAN, "multifrontal %s factorisation: non-positive pivot in front %d",
                          sizeof(T) == 4 ? "FP32" : "FP64", herr - 1);
     *grid_out = gmax;
     return GRMP_OK;
+}
+
+// Q = [L11^-1; L21 L11^-1] of every front from the current factor (FP32 preconditioner)
+template <typename T>
+int mf_build_inverse(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    MfCache &C = *A->mf;
+    if (!C.Q) {
+        C.Qb = std::max<size_t>(1, C.L_size) * sizeof(T);
+        int rc = grmp_alloc(ctx, &C.Q, C.Qb);
+        if (!rc) rc = grmp_alloc(ctx, &C.wy, C.wb);
+        if (!rc) rc = grmp_alloc(ctx, &C.wx, C.wb);
+        if (rc) return rc;
+    }
+    const int tb = 256;
+    if (C.total_bcols > 0) {
+        k_mf_invert<T><<<(unsigned)C.total_bcols, kTB, 0, ctx->stream>>>(C.dev, C.bcol, C.nnodes, (const T *)C.L,
+                                                                        (T *)C.Q);
+        GRMP_LAUNCHED(ctx);
+    }
+    if (C.total_g > 0) {
+        k_mf_gmat<T><<<(unsigned)((C.total_g + tb - 1) / tb), tb, 0, ctx->stream>>>(C.dev, C.gpref, C.nnodes,
+                                                                                   C.total_g, (const T *)C.L,
+                                                                                   (T *)C.Q);
+        GRMP_LAUNCHED(ctx);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "multifrontal inverse");
+    return GRMP_OK;
+}
+
+// wx <- A^{-1} w with the inverse-based factor (w is overwritten)
+template <typename T>
+void mf_apply_inverse(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    MfCache &C = *A->mf;
+    const int nl = (int)C.level_ptr.size() - 1;
+    const int grid = 4 * ctx->num_sms;
+    for (int l = 0; l < nl; l++) {
+        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
+        k_mf_gather_level<T><<<std::min(cnt, kMaxGrid), kTB, 0, ctx->stream>>>(C.dev, lb, cnt, (T *)C.uv, (T *)C.w);
+        GRMP_LAUNCHED(ctx);
+        k_mf_qmul_level<T><<<grid, kTB, 0, ctx->stream>>>(C.dev, C.qrow, lb, cnt, (const T *)C.Q, (T *)C.uv,
+                                                         (const T *)C.w, (T *)C.wy);
+        GRMP_LAUNCHED(ctx);
+    }
+    for (int l = nl - 1; l >= 0; l--) {
+        const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
+        k_mf_qtmul_level<T><<<grid, kTB, 0, ctx->stream>>>(C.dev, C.scol, lb, cnt, (const T *)C.Q, (const T *)C.wy,
+                                                          (T *)C.wx);
+        GRMP_LAUNCHED(ctx);
+    }
 }
 
 // w <- A^{-1} w with the current factor (level launches)
@@ -572,6 +1064,7 @@ int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_
     int rc = A->mf ? GRMP_OK : mf_build(A);
     int grid = 0;
     if (!rc) rc = mixed ? mf_numeric<float>(A, &grid) : mf_numeric<double>(A, &grid);
+    if (!rc && mixed) rc = mf_build_inverse<float>(A);
     const int nb = 2 * ctx->num_sms, tb = 256;
     double *r = nullptr, *z = nullptr, *pp = nullptr, *q = nullptr, *part = nullptr;
     const size_t vb = (size_t)n * 8;
@@ -646,8 +1139,8 @@ int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_
         auto precond = [&]() -> double {   // z = M^{-1} r, returns r.z
             k_to<float><<<gv, tb, 0, ctx->stream>>>(n, r, (float *)C.w);
             GRMP_LAUNCHED(ctx);
-            mf_apply<float>(A);
-            k_from_dot<float><<<nb, tb, 0, ctx->stream>>>(n, (const float *)C.w, r, z, part);
+            mf_apply_inverse<float>(A);
+            k_from_dot<float><<<nb, tb, 0, ctx->stream>>>(n, (const float *)C.wx, r, z, part);
             GRMP_LAUNCHED(ctx);
             return host_sum(ctx, part, nb, &e);
         };
