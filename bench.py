@@ -139,10 +139,10 @@ def peaks():
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)
 WORKLOADS = {
-    # name: (description, default size n, CPU sample size)
-    "poisson3d": ("poisson3d_P2_kuhn{n}_lognormal_kappa", 64, 24),
-    "poisson2d": ("poisson2d_P2_{n}x{n}_kappa1e-3", 128, 128),
-    "elasticity2d": ("elasticity2d_P2vec_{n}x{n}_mu1_lambda1e3", 256, 32),
+    # name: (description, default size n, CPU sample size, solve tolerance for <= 1e-10 error vs FP64)
+    "poisson3d": ("poisson3d_P2_kuhn{n}_lognormal_kappa", 64, 24, 1e-11),
+    "poisson2d": ("poisson2d_P2_{n}x{n}_kappa1e-3", 128, 128, 1e-11),
+    "elasticity2d": ("elasticity2d_P2vec_{n}x{n}_mu1_lambda1e3", 256, 32, 1e-12),
 }
 
 
@@ -551,7 +551,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="mesh size (0: the workload's own)")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--reltol", type=float, default=1e-11)
+    ap.add_argument("--reltol", type=float, default=0.0, help="solve tolerance (0: the workload's own)")
     ap.add_argument("--ref-reltol", type=float, default=1e-14)
     ap.add_argument("--inner-reltol", type=float, default=0.1)
     ap.add_argument("--cpu-n", type=int, default=0, help="CPU sample mesh size (0: the workload's own)")
@@ -574,6 +574,8 @@ def main():
         args.n = args.n or WORKLOADS[args.workload][1]
         args.cpu_n = args.cpu_n or WORKLOADS[args.workload][2]
         args.solver = args.solver or ("direct" if args.workload == "elasticity2d" else "pcg")
+        args.reltol = args.reltol or WORKLOADS[args.workload][3]
+    args.reltol = args.reltol or 1e-11
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "stokes-batch":

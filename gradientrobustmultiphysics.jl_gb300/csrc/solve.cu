@@ -70,8 +70,16 @@ __device__ __forceinline__ void block_sum(double *v, double *sh /* [32*NV] */) {
 
 // Write this block's partial sums, pass a grid barrier, then every block sums
 // all partials in the same fixed order.  Returns false on a barrier timeout.
+// The partial-sum area holds two buffers used alternately by successive
+// reductions (`round` counts them): a block may start writing the next
+// reduction's partials while a slower block still reads the previous ones,
+// but it cannot reach the reduction after that before every block has left
+// this one.
+constexpr int kPartStride = 4 * 4096;   // doubles per buffer (4 values x up to 4096 blocks)
+
 template <int NV>
-__device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh, SolveState *st) {
+__device__ __forceinline__ bool grid_sum(double *v, double *partial_area, double *sh, SolveState *st, int &round) {
+    double *partial = partial_area + (round++ & 1) * kPartStride;
     block_sum<NV>(v, sh);
     if (threadIdx.x == 0)
         for (int k = 0; k < NV; k++) partial[blockIdx.x * 4 + k] = v[k];
@@ -81,6 +89,42 @@ __device__ __forceinline__ bool grid_sum(double *v, double *partial, double *sh,
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
         for (int k = 0; k < NV; k++) acc[k] += __ldcg(&partial[b * 4 + k]);
     block_sum<NV>(acc, sh);
+    for (int k = 0; k < NV; k++) v[k] = acc[k];
+    return true;
+}
+
+// FP32 versions for the inner iteration of the mixed solver: on GB300 the
+// FP64 pipe issues about 2 operations per clock per SM, so double-precision
+// shuffles and sums in every reduction of every iteration are not free.  The
+// summation order is fixed as in the FP64 versions.
+template <int NV>
+__device__ __forceinline__ void block_sum_f(float *v, float *sh /* [32*NV] */) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < NV; k++) sh[wid * NV + k] = v[k];
+    __syncthreads();
+    for (int k = 0; k < NV; k++) {
+        float s = 0.f;
+        for (int w = 0; w < nw; w++) s += sh[w * NV + k];
+        v[k] = s;
+    }
+    __syncthreads();
+}
+
+template <int NV>
+__device__ __forceinline__ bool grid_sum_f(float *v, double *partial_area, float *sh, SolveState *st, int &round) {
+    float *partial = reinterpret_cast<float *>(partial_area + (round++ & 1) * kPartStride);
+    block_sum_f<NV>(v, sh);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NV; k++) partial[blockIdx.x * 4 + k] = v[k];
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return false;
+    float acc[NV];
+    for (int k = 0; k < NV; k++) acc[k] = 0.f;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int k = 0; k < NV; k++) acc[k] += __ldcg(&partial[b * 4 + k]);
+    block_sum_f<NV>(acc, sh);
     for (int k = 0; k < NV; k++) v[k] = acc[k];
     return true;
 }
@@ -242,6 +286,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
                                                 double *r, double *z, double *p, double *q, double *partial,
                                                 SolveState *st, double abstol, double reltol, int maxit, int guess) {
     __shared__ double sh[32 * 4];
+    int round = 0;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // r = b - A x  (or b)
@@ -258,7 +303,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
         v[1] += ri * ri;
         v[2] += b[i] * b[i];
     }
-    if (!grid_sum<3>(v, partial, sh, st)) return;
+    if (!grid_sum<3>(v, partial, sh, st, round)) return;
     double rz = v[0], rr = v[1];
     const double bn = sqrt(v[2]);
     const double tol = fmax(abstol, reltol * bn);
@@ -267,7 +312,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
     while (!conv && it < maxit) {
         double d[1];
         d[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
-        if (!grid_sum<1>(d, partial, sh, st)) return;
+        if (!grid_sum<1>(d, partial, sh, st, round)) return;
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
@@ -284,7 +329,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
             w[0] += ri * zi;
             w[1] += ri * ri;
         }
-        if (!grid_sum<2>(w, partial, sh, st)) return;
+        if (!grid_sum<2>(w, partial, sh, st, round)) return;
         it++;
         rr = w[1];
         conv = sqrt(rr) <= tol;
@@ -298,7 +343,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
     if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
     double t[1];
     t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
-    if (!grid_sum<1>(t, partial, sh, st)) return;
+    if (!grid_sum<1>(t, partial, sh, st, round)) return;
     if (gtid == 0) {
         st->iters = it;
         st->outer = 0;
@@ -343,6 +388,8 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 
                                                     SolveState *st, double abstol, double reltol, double delta,
                                                     int maxit, int maxouter, int guess) {
     __shared__ double sh[32 * 4];
+    __shared__ float shf[32 * 4];
+    int round = 0;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // FP64 residual of the initial guess
@@ -357,7 +404,7 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 
         }
     }
     for (int i = gtid; i < n; i += gsz) v[1] += b[i] * b[i];
-    if (!grid_sum<2>(v, partial, sh, st)) return;
+    if (!grid_sum<2>(v, partial, sh, st, round)) return;
     const double bn = sqrt(v[1]);
     const double tol = fmax(abstol, reltol * bn);
     double rn64 = sqrt(v[0]);
@@ -375,24 +422,26 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 
         wf1 += ri * ri;
     }
     double w[2] = {(double)wf0, (double)wf1};
-    if (!grid_sum<2>(w, partial, sh, st)) return;
-    double rz = w[0];
-    double rmax = sqrt(w[1]);
+    if (!grid_sum<2>(w, partial, sh, st, round)) return;
+    // inner-iteration scalars in FP32 (every thread computes them; the FP64
+    // pipe is scarce): rz, the FP32 residual norms, alpha, beta
+    float rz = (float)w[0];
+    float rmax = sqrtf((float)w[1]);
+    const float tolf = (float)tol, deltaf = (float)delta;
     double prev_rn64 = rn64;
     int stall = 0;
     float beta = 0.f;
     float2 *cur = zp0, *nxt = zp1;
     while (!conv && it < maxit && outer < maxouter) {
         float *nxt_f = reinterpret_cast<float *>(nxt);
-        double d[1];
-        d[0] = (double)spmv_fused_zp<TPR, U, PIPE>(n, rowptr, pack32, cur, nxt_f, q, beta);
-        if (!grid_sum<1>(d, partial, sh, st)) return;   // barrier 1
-        const double pq = d[0];
-        if (!(pq > 0) || !isfinite(pq)) {
+        float d[1] = {spmv_fused_zp<TPR, U, PIPE>(n, rowptr, pack32, cur, nxt_f, q, beta)};
+        if (!grid_sum_f<1>(d, partial, shf, st, round)) return;   // barrier 1
+        const float pq = d[0];
+        if (!(pq > 0.f) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
             break;
         }
-        const float alpha = (float)(rz / pq);
+        const float alpha = rz / pq;
         float uf0 = 0.f, uf1 = 0.f;
         for (int i = gtid; i < n; i += gsz) {
             const float pi = nxt_f[2 * i + 1];
@@ -404,13 +453,13 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 
             uf0 += ri * zi;
             uf1 += ri * ri;
         }
-        double u[2] = {(double)uf0, (double)uf1};
-        if (!grid_sum<2>(u, partial, sh, st)) return;   // barrier 2
+        float u[2] = {uf0, uf1};
+        if (!grid_sum_f<2>(u, partial, shf, st, round)) return;   // barrier 2
         it++;
-        double rz_new = u[0];
-        const double rn32 = sqrt(u[1]);
+        float rz_new = u[0];
+        const float rn32 = sqrtf(u[1]);
         bool restart = false;
-        if (rn32 <= delta * rmax || rn32 <= tol || it >= maxit) {
+        if (rn32 <= deltaf * rmax || rn32 <= tolf || it >= maxit) {
             // refinement: fold the FP32 correction into x, recompute b - A x in FP64
             for (int i = gtid; i < n; i += gsz) {
                 x[i] += (double)xc[i];
@@ -419,7 +468,7 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 
             if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
             double t[1];
             t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
-            if (!grid_sum<1>(t, partial, sh, st)) return;
+            if (!grid_sum<1>(t, partial, sh, st, round)) return;
             outer++;
             rn64 = sqrt(t[0]);
             conv = rn64 <= tol;
@@ -442,12 +491,12 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 
                 yf0 += ri * zi;
                 yf1 += ri * ri;
             }
-            double y[2] = {(double)yf0, (double)yf1};
-            if (!grid_sum<2>(y, partial, sh, st)) return;
+            float y[2] = {yf0, yf1};
+            if (!grid_sum_f<2>(y, partial, shf, st, round)) return;
             rz_new = y[0];
-            rmax = sqrt(y[1]);
+            rmax = sqrtf(y[1]);
         }
-        beta = restart ? 0.0f : (float)(rz_new / rz);
+        beta = restart ? 0.0f : rz_new / rz;
         rz = rz_new;
         float2 *tmp = cur;
         cur = nxt;
@@ -678,7 +727,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     //   FP64 : dinv r z p q (double)                  | partials | state
     //   MIXED: dinv r z p q xc (float) | r64 (double)  | partials | state
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    size_t pbytes = (size_t)4 * 8 * 4096;
+    size_t pbytes = (size_t)2 * kPartStride * 8;   // two alternating partial-sum buffers
     size_t vec = mixed ? al((size_t)n * 4) : al((size_t)n * 8);
     size_t nvec = mixed ? 8 : 5;   // MIXED: dinv r q xc (float) + two interleaved (z, p) float2 buffers
     size_t off_r64 = nvec * vec;
@@ -770,7 +819,7 @@ int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
 // GRMP_NOALLOC_MAX_ROWS rows, laid out like the FP64 workspace of
 // grmp_solve_impl:
 //   [0, 5V)           dinv r z p q   (V = GRMP_NOALLOC_MAX_ROWS doubles each)
-//   [5V, 5V+P)        per-block reduction partials (4 x 4096 doubles)
+//   [5V, 5V+P)        per-block reduction partials (two buffers of 4 x 4096 doubles)
 //   [5V+P, +256)      SolveState: grid-barrier counters + status  (zeroed per call)
 //   [5V+P+256, +256)  diagonal check flag                          (zeroed per call)
 // The array's address is looked up once per device; the first call makes
@@ -778,7 +827,7 @@ int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
 namespace {
 
 constexpr size_t kNaVec = (size_t)GRMP_NOALLOC_MAX_ROWS * 8;
-constexpr size_t kNaPart = (size_t)4 * 8 * 4096;
+constexpr size_t kNaPart = (size_t)2 * kPartStride * 8;
 constexpr size_t kNaState = 5 * kNaVec + kNaPart;
 constexpr size_t kNaFlag = kNaState + 256;
 constexpr size_t kNaBytes = kNaFlag + 256;

@@ -281,7 +281,7 @@ int grmp_spmv(grmp_matrix A, int precision, grmp_vector x, grmp_vector y);
 
 /* FP64 Jacobi-PCG like grmp_solve with mode GRMP_SOLVE_FP64, but without
  * any device-memory allocation: its work arrays live in a fixed scratch
- * area of about 10.6 MB that is part of the loaded library on each device.
+ * area of about 10.8 MB that is part of the loaded library on each device.
  * No counterpart in the reference (its solves allocate freely).
  *   - For callers that must not allocate during a solve: hosts whose own
  *     memory pool has taken the device's free memory, or time-stepping loops
