@@ -735,6 +735,9 @@ struct MfCache {
     // prefixes over fronts in level order: rows (f), own columns (s), G entries (sc * s)
     const long long *qrow = nullptr, *scol = nullptr, *gpref = nullptr, *bcol = nullptr;
     long long total_cols = 0, total_g = 0, total_bcols = 0;
+    // the preconditioner's level launches (w -> wx), captured once per numeric storage
+    cudaGraphExec_t apply_graph = nullptr;
+    int apply_kernels = 0;
 };
 
 namespace {
@@ -762,6 +765,8 @@ int mf_upload(grmp_context ctx, MfCache &C, const std::vector<V> &v, const V **o
 }
 
 void mf_free_numeric(grmp_context ctx, MfCache &C) {
+    if (C.apply_graph) cudaGraphExecDestroy(C.apply_graph);
+    C.apply_graph = nullptr;
     grmp_free(ctx, C.L, C.Lb);
     grmp_free(ctx, C.U, C.Ub);
     grmp_free(ctx, C.uv, C.uvb);
@@ -983,27 +988,56 @@ int mf_build_inverse(grmp_matrix A) {
     return GRMP_OK;
 }
 
-// wx <- A^{-1} w with the inverse-based factor (w is overwritten)
+// wx <- A^{-1} w with the inverse-based factor (w is overwritten): the level
+// launches, in order
 template <typename T>
-void mf_apply_inverse(grmp_matrix A) {
+int mf_enqueue_inverse(grmp_matrix A) {
     grmp_context ctx = A->space->mesh->ctx;
     MfCache &C = *A->mf;
     const int nl = (int)C.level_ptr.size() - 1;
     const int grid = 4 * ctx->num_sms;
+    int k = 0;
     for (int l = 0; l < nl; l++) {
         const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
         k_mf_gather_level<T><<<std::min(cnt, kMaxGrid), kTB, 0, ctx->stream>>>(C.dev, lb, cnt, (T *)C.uv, (T *)C.w);
-        GRMP_LAUNCHED(ctx);
         k_mf_qmul_level<T><<<grid, kTB, 0, ctx->stream>>>(C.dev, C.qrow, lb, cnt, (const T *)C.Q, (T *)C.uv,
                                                          (const T *)C.w, (T *)C.wy);
-        GRMP_LAUNCHED(ctx);
+        k += 2;
     }
     for (int l = nl - 1; l >= 0; l--) {
         const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
         k_mf_qtmul_level<T><<<grid, kTB, 0, ctx->stream>>>(C.dev, C.scol, lb, cnt, (const T *)C.Q, (const T *)C.wy,
                                                           (T *)C.wx);
-        GRMP_LAUNCHED(ctx);
+        k++;
     }
+    return k;
+}
+
+// The sequence is replayed once per CG iteration with the same buffers, so it
+// is captured into a CUDA graph at the first application after the numeric
+// storage was (re)allocated and replayed from then on.
+template <typename T>
+int mf_apply_inverse(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    MfCache &C = *A->mf;
+    if (!C.apply_graph) {
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            C.apply_kernels = mf_enqueue_inverse<T>(A);
+            e = cudaStreamEndCapture(ctx->stream, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&C.apply_graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            C.apply_graph = nullptr;
+            return grmp_cuda_fail(ctx, e, "preconditioner graph capture");
+        }
+    }
+    cudaError_t e = cudaGraphLaunch(C.apply_graph, ctx->stream);
+    ctx->launches += (uint64_t)C.apply_kernels;
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "preconditioner graph launch");
+    return GRMP_OK;
 }
 
 // w <- A^{-1} w with the current factor (level launches)
@@ -1139,7 +1173,7 @@ int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_
         auto precond = [&]() -> double {   // z = M^{-1} r, returns r.z
             k_to<float><<<gv, tb, 0, ctx->stream>>>(n, r, (float *)C.w);
             GRMP_LAUNCHED(ctx);
-            mf_apply_inverse<float>(A);
+            if (mf_apply_inverse<float>(A)) e = cudaErrorUnknown;
             k_from_dot<float><<<nb, tb, 0, ctx->stream>>>(n, (const float *)C.wx, r, z, part);
             GRMP_LAUNCHED(ctx);
             return host_sum(ctx, part, nb, &e);

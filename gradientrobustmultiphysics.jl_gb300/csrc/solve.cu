@@ -381,7 +381,7 @@ __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict_
 }
 
 template <int TPR, int U, bool PIPE>
-__global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : 4) : (U >= 8 ? 4 : 5)) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+__global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) : (U >= 8 ? 4 : 5)) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
                                                     const double *vals64, const int2 *pack32, const double *b,
                                                     double *x, const float *dinv, float *r, float *q, float *xc,
                                                     float2 *zp0, float2 *zp1, double *r64, double *partial,
@@ -563,7 +563,7 @@ void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, co
 
 // SpMV configurations of the persistent solvers: (lanes per row, loads in
 // flight per lane), encoded 100*TPR + U.
-constexpr int kConfigs[] = {208, 404, 408, 804, 1602, 10204, 10404, 10408, 10804};
+constexpr int kConfigs[] = {208, 404, 408, 804, 1602, 10204, 10404, 10408, 10804, 10402, 10802};
 
 int heuristic_tpr(grmp_matrix A) {
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
@@ -675,6 +675,8 @@ int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_
         case 10404: return launch_pcg<4, 4, true>(A, b, x, p, st, work, dst, lay);
         case 10408: return launch_pcg<4, 8, true>(A, b, x, p, st, work, dst, lay);
         case 10804: return launch_pcg<8, 4, true>(A, b, x, p, st, work, dst, lay);
+        case 10402: return launch_pcg<4, 2, true>(A, b, x, p, st, work, dst, lay);
+        case 10802: return launch_pcg<8, 2, true>(A, b, x, p, st, work, dst, lay);
     }
     return grmp_fail(A->space->mesh->ctx, GRMP_ERR_INVALID_ARG, "spmv_config: unknown configuration %d", cfg);
 }
@@ -924,6 +926,8 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
         case 10404: e = launch_pcg64_static<4, 4, true>(A, b->d, x->d, p, work, &grid); break;
         case 10408: e = launch_pcg64_static<4, 8, true>(A, b->d, x->d, p, work, &grid); break;
         case 10804: e = launch_pcg64_static<8, 4, true>(A, b->d, x->d, p, work, &grid); break;
+        case 10402: e = launch_pcg64_static<4, 2, true>(A, b->d, x->d, p, work, &grid); break;
+        case 10802: e = launch_pcg64_static<8, 2, true>(A, b->d, x->d, p, work, &grid); break;
         default: return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_config: unknown configuration %d", cfg);
     }
     SolveState hs;

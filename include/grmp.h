@@ -244,8 +244,9 @@ typedef struct {
     int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
     int32_t spmv_config;    /* SpMV lanes per row and loads in flight, coded 100*lanes + loads,
                                +10000 for the software-pipelined row loop: 208, 404, 408, 804,
-                               1602, 10204, 10404, 10408, 10804; 0 = autotuned per matrix and
-                               mode (timed trial solves); -1 = chosen from the mean row length
+                               1602, 10204, 10404, 10408, 10804, 10402, 10802; 0 = autotuned
+                               per matrix and mode (timed trial solves); -1 = chosen from the
+                               mean row length
                                (no timing, so the choice does not depend on concurrent GPU work) */
     int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
     int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
