@@ -307,7 +307,8 @@ def run_ours(args):
         G.assemble(b, prob.rhs)
         G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)
         smode = {"fp64": "direct", "mixed": "mixed_direct"}[mode] if direct else mode
-        s = G.GB300PCG(mode=smode, reltol=args.reltol, abstol=0.0, inner_reltol=args.inner_reltol)
+        s = G.GB300PCG(mode=smode, reltol=args.reltol, abstol=0.0, inner_reltol=args.inner_reltol,
+                       spmv_config=args.spmv_config if smode == "mixed" else 0)
         st = s.solve(A, b, x)
         out = x.entries if host_inputs else None
         return st, out
@@ -554,6 +555,8 @@ def main():
     ap.add_argument("--reltol", type=float, default=0.0, help="solve tolerance (0: the workload's own)")
     ap.add_argument("--ref-reltol", type=float, default=1e-14)
     ap.add_argument("--inner-reltol", type=float, default=0.1)
+    ap.add_argument("--spmv-config", type=int, default=0,
+                    help="SpMV configuration of the mixed solver (0: autotuned per matrix)")
     ap.add_argument("--cpu-n", type=int, default=0, help="CPU sample mesh size (0: the workload's own)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true", help="mixed path only, no timing output (for ncu)")

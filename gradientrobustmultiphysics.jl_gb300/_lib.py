@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libgrmp_gpu.so")
 # status codes (grmp_status)
 OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_DEVICE, ERR_NOT_CONVERGED = 0, 1, 2, 3, 4
 ERR_UNSUPPORTED, ERR_BUDGET, ERR_TIMEOUT, ERR_NAN, ERR_NO_DEVICE = 5, 6, 7, 8, 9
+ITEM_IDENTITY, ITEM_GRADIENT = 0, 1
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "DEVICE", 4: "NOT_CONVERGED",
                 5: "UNSUPPORTED", 6: "BUDGET", 7: "TIMEOUT", 8: "NAN", 9: "NO_DEVICE"}
 
@@ -115,6 +116,8 @@ SIGNATURES = {
     "grmp_assemble_bilinear": ([_vp, ctypes.c_int, ctypes.POINTER(BilinearTerm), ctypes.c_int], ctypes.c_int),
     "grmp_matrix_download": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64), _pi32, _pd], ctypes.c_int),
     "grmp_assemble_linear": ([_vp, ctypes.POINTER(Rhs), _vp], ctypes.c_int),
+    "grmp_item_l2error": ([_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(Rhs), ctypes.c_double, ctypes.c_int, _pd, _pd],
+                          ctypes.c_int),
     "grmp_vector_create": ([_vp, _i32, ctypes.POINTER(_vp)], ctypes.c_int),
     "grmp_vector_destroy": ([_vp], ctypes.c_int),
     "grmp_vector_upload": ([_vp, _pd], ctypes.c_int),

@@ -396,6 +396,64 @@ def assemble(target, operators, precision: int = L.FP64):
     raise TypeError("assemble target must be an FEMatrix or FEVector")
 
 
+# ----------------------------------------------------------------------- item integrators
+@dataclass
+class ItemIntegrator:
+    """L2ErrorIntegrator / L2NormIntegrator / L2DifferenceIntegrator of
+    src/assemblypatterns/itemintegrator.jl (:40-158) over all cells;
+    `evaluate` / `evaluate_cells` mirror evaluate (:314-330) / evaluate!
+    (:173-300) and run on the device (grmp_item_l2error)."""
+    operator: str
+    data: Optional[DataFunction] = None
+    factor: float = 1.0
+    quadorder: int = -1          # -1: the reference's "auto"
+    difference: bool = False
+
+    def _call(self, u: FEVector, v: Optional[FEVector], cells: bool):
+        if self.difference != (v is not None):
+            raise ValueError("L2DifferenceIntegrator takes two FEVectors, the other integrators one")
+        op = {Identity: L.ITEM_IDENTITY, Gradient: L.ITEM_GRADIENT}[self.operator]
+        rp = None
+        if self.data is not None:
+            r = L.Rhs()
+            r.kind = self.data.kind
+            r.ncomponents = self.data.ncomponents
+            par = np.ascontiguousarray(self.data.params, dtype=np.float64)
+            r.params = _dp(par)
+            r.nparams = par.size
+            r.factor = 1.0
+            r.bonus_quadorder = int(self.data.bonus_quadorder)
+            rp = ctypes.byref(r)
+        out = np.empty(u.FES.xgrid.ncells) if cells else None
+        tot = ctypes.c_double(0.0)
+        sh = u.ctx.space(u.FES)
+        u.ctx.check(u.ctx.lib.grmp_item_l2error(sh, u.h, v.h if v is not None else None, op, rp, float(self.factor),
+                                                int(self.quadorder), _dp(out) if cells else None,
+                                                ctypes.byref(tot)))
+        return out if cells else tot.value
+
+    def evaluate(self, u: FEVector, v: Optional[FEVector] = None) -> float:
+        """Sum over all cells (the squared error / norm / difference)."""
+        return self._call(u, v, False)
+
+    def evaluate_cells(self, u: FEVector, v: Optional[FEVector] = None) -> np.ndarray:
+        """Per-cell values (evaluate! into a [1, ncells] array)."""
+        return self._call(u, v, True)
+
+
+def L2ErrorIntegrator(data: DataFunction, operator: str = Identity, *, quadorder="auto",
+                      factor: float = 1.0) -> ItemIntegrator:
+    return ItemIntegrator(operator, data, factor, -1 if quadorder == "auto" else int(quadorder))
+
+
+def L2NormIntegrator(operator: str = Identity, *, quadorder: int = 2) -> ItemIntegrator:
+    return ItemIntegrator(operator, None, 1.0, int(quadorder))
+
+
+def L2DifferenceIntegrator(operator: str = Identity, *, quadorder: int = 2) -> ItemIntegrator:
+    return ItemIntegrator(operator, None, 1.0, int(quadorder), difference=True)
+
+
 def apply_dirichlet(A: FEMatrix, b: Optional[FEVector], fixed_dofs: np.ndarray, values=None,
                     mode: int = L.DIRICHLET_ELIMINATE, penalty: float = 1e60):
     """Dirichlet treatment of fixed DoFs: the reference's penalty form

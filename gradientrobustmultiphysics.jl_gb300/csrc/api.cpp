@@ -324,6 +324,15 @@ int grmp_assemble_linear(grmp_space space, const grmp_rhs *rhs, grmp_vector b) {
     return grmp_assemble_linear_impl(space, rhs, b);
 }
 
+int grmp_item_l2error(grmp_space space, grmp_vector u, grmp_vector v, int op, const grmp_rhs *data, double factor,
+                      int quadorder, double *cell_values, double *total) {
+    if (!space || !u) return GRMP_ERR_INVALID_ARG;
+    if (u->ctx != space->mesh->ctx || (v && v->ctx != space->mesh->ctx)) return GRMP_ERR_INVALID_ARG;
+    cudaSetDevice(space->mesh->ctx->device);
+    std::lock_guard<std::mutex> lk(space->mesh->ctx->mu);
+    return grmp_item_l2error_impl(space, u, v, op, data, factor, quadorder, cell_values, total);
+}
+
 int grmp_apply_dirichlet(grmp_matrix A, grmp_vector b, int32_t nfixed, const int32_t *fixed, const double *values,
                          int mode, double penalty) {
     if (!A || nfixed < 0 || (nfixed > 0 && !fixed)) return GRMP_ERR_INVALID_ARG;

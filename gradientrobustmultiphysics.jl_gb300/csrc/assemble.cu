@@ -220,45 +220,6 @@ int dispatch_precision(grmp_matrix A, const FastTerms &ft, const std::vector<dou
 }
 
 // ------------------------------------------------------------------ linear forms
-struct RhsDev {
-    int kind, ncomp;
-    const double *par;
-    long long npar;
-    double factor;
-    int nq, nb;
-    const double *w, *xref, *vals;
-};
-
-__device__ __forceinline__ void rhs_eval(const RhsDev &r, int dim, int cell, const double *x, double *f) {
-    if (r.kind == GRMP_RHS_CONST) {
-        for (int c = 0; c < r.ncomp; c++) f[c] = r.par[c];
-    } else if (r.kind == GRMP_RHS_CELL) {
-        for (int c = 0; c < r.ncomp; c++) f[c] = r.par[(size_t)cell * r.ncomp + c];
-    } else if (r.kind == GRMP_RHS_FOURIER) {
-        int stride = 1 + dim, nm = (int)(r.npar / stride);
-        double s = 0;
-        for (int m = 0; m < nm; m++) {
-            double arg = 0;
-            for (int j = 0; j < dim; j++) arg += r.par[m * stride + 1 + j] * x[j];
-            s += r.par[m * stride] * sin(M_PI * arg);
-        }
-        f[0] = s;
-        for (int c = 1; c < r.ncomp; c++) f[c] = 0;
-    } else {
-        for (int c = 0; c < r.ncomp; c++) f[c] = 0;
-        int nt = (int)(r.npar / 5);
-        for (int t = 0; t < nt; t++) {
-            int c = (int)r.par[5 * t];
-            double v = r.par[5 * t + 1];
-            for (int j = 0; j < dim; j++) {
-                double e = r.par[5 * t + 2 + j];
-                if (e != 0) v *= pow(x[j], e);
-            }
-            f[c] += v;
-        }
-    }
-}
-
 // Cell-local vectors  loc[cell][(c,a)] = (factor*vol) * sum_q (f_c(x_q) phi_a(q)) w_q
 // (src/assemblypatterns/linearform.jl:181-220; x_q = x0 + A xref_q).
 template <int DIM>

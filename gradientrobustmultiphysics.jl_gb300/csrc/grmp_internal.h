@@ -81,6 +81,13 @@ struct grmp_matrix_s {
     size_t work_bytes = 0;
     int tuned_cfg = 0;              // autotuned SpMV configuration, FP64 solves (0 = not tuned)
     int tuned_cfg32 = 0;            // autotuned SpMV configuration (100*lanes + loads), mixed solves
+    // staged SpMV of mixed solves: the FP32 pairs re-laid out in fixed-size row
+    // windows (state 0 = not built, 1 = built, -1 = a row does not fit a window)
+    int stg_state = 0;
+    int stg_nwin = 0;
+    int32_t *d_stg_row0 = nullptr;  // [nwin+1] first row of each window
+    char *d_stg_rec = nullptr;      // [nwin] window records
+    size_t stg_rec_bytes = 0;
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;
@@ -140,6 +147,8 @@ int grmp_scan_i32(grmp_context ctx, const int32_t *d_in, int32_t *d_out_excl, in
 int grmp_pattern_build_impl(grmp_space space, int nterms, const grmp_bilinear_term *terms, grmp_matrix *out);
 int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
 int grmp_assemble_linear_impl(grmp_space space, const grmp_rhs *rhs, grmp_vector b);
+int grmp_item_l2error_impl(grmp_space s, grmp_vector u, grmp_vector v, int op, const grmp_rhs *data, double factor,
+                           int quadorder, double *cell_values, double *total);
 int grmp_apply_dirichlet_impl(grmp_matrix A, grmp_vector b, int32_t nfixed, const int32_t *fixed,
                               const double *values, int mode, double penalty);
 int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st);
@@ -166,6 +175,7 @@ struct GridBarrier {
 };
 
 __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nblocks, int *status) {
+    __shared__ int ok;   // one answer for the whole block, so its threads leave together
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int *vgen = &gb->gen;
@@ -187,8 +197,9 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nbloc
             }
         }
         __threadfence();
+        ok = *(volatile int *)status == 0;
     }
     __syncthreads();
-    return *(volatile int *)status == 0;
+    return ok != 0;
 }
 #endif

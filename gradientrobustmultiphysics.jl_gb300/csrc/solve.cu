@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
 // This removes the separate p-update pass and one grid barrier per iteration.
 template <int TPR, int U, bool PIPE>
 __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict__ rowptr, const int2 *__restrict__ pack,
-                                               const float2 *cur, float *nxt_f, float *q, float beta) {
+                                               const float2 *cur, float2 *nxt, float *q, float beta) {
     float dacc = 0.f;
     spmv_rows<TPR, U, PIPE, float>(
         n, rowptr, PackedSource{pack},
@@ -373,20 +373,42 @@ __device__ __forceinline__ float spmv_fused_zp(int n, const int32_t *__restrict_
         [&](int r, float s) {
             const float2 me = cur[r];
             const float pn = __fmaf_rn(beta, me.y, me.x);
-            nxt_f[2 * r + 1] = pn;
+            nxt[r] = make_float2(me.x, pn);
             q[r] = s;
             dacc += pn * s;
         });
     return dacc;
 }
 
+// SpMV policy of the mixed solver: the grid-strided row loop over the packed
+// FP32 pairs (fused_zp) and the FP64 residual b - A x (resid64).
 template <int TPR, int U, bool PIPE>
-__global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) : (U >= 8 ? 4 : 5)) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
-                                                    const double *vals64, const int2 *pack32, const double *b,
-                                                    double *x, const float *dinv, float *r, float *q, float *xc,
-                                                    float2 *zp0, float2 *zp1, double *r64, double *partial,
-                                                    SolveState *st, double abstol, double reltol, double delta,
-                                                    int maxit, int maxouter, int guess) {
+struct RowsSpmv {
+    int n;
+    const int32_t *rowptr, *cols;
+    const double *vals64;
+    const int2 *pack32;
+    __device__ __forceinline__ float fused_zp(const float2 *cur, float2 *nxt, float *q, float beta) {
+        return spmv_fused_zp<TPR, U, PIPE>(n, rowptr, pack32, cur, nxt, q, beta);
+    }
+    __device__ __forceinline__ double resid64(const double *x, double *r64, const double *b) {
+        return spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+    }
+};
+
+// The mixed PCG iteration; `sp` supplies the two SpMV forms.  Returns early
+// (every thread of a block alike) when a grid barrier fails.
+//
+// (preconditioned residual, search direction) pairs are double-buffered:
+// `cur` holds (z_k, p_{k-1}); the SpMV gathers p_k = z_k + beta p_{k-1} on
+// the fly, the owner of row i stores the pair (z_k, p_k) into nxt[i]; the
+// vector phase (four rows per thread, 16-byte loads) reads p_k from nxt[i],
+// updates x, r and writes z_{k+1} over the pair's first half.
+template <class SP>
+__device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, double *x, const float *dinv, float *r,
+                                               float *q, float *xc, float2 *zp0, float2 *zp1, double *r64,
+                                               double *partial, SolveState *st, double abstol, double reltol,
+                                               double delta, int maxit, int maxouter, int guess) {
     __shared__ double sh[32 * 4];
     __shared__ float shf[32 * 4];
     int round = 0;
@@ -395,7 +417,7 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
     // FP64 residual of the initial guess
     double v[2] = {0, 0};
     if (guess) {
-        v[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+        v[0] = sp.resid64(x, r64, b);
     } else {
         for (int i = gtid; i < n; i += gsz) {
             x[i] = 0.0;
@@ -411,30 +433,28 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
     int it = 0, outer = 0;
     bool conv = rn64 <= tol;
     // FP32 state from the FP64 residual; p_{-1} = 0
-    float wf0 = 0.f, wf1 = 0.f;
+    float wf = 0.f;
     for (int i = gtid; i < n; i += gsz) {
-        float ri = (float)r64[i];
-        float zi = dinv[i] * ri;
+        const float ri = (float)r64[i];
+        const float zi = dinv[i] * ri;
         r[i] = ri;
         zp0[i] = make_float2(zi, 0.f);
         xc[i] = 0.0f;
-        wf0 += ri * zi;
-        wf1 += ri * ri;
+        wf += ri * zi;
     }
-    double w[2] = {(double)wf0, (double)wf1};
-    if (!grid_sum<2>(w, partial, sh, st, round)) return;
-    // inner-iteration scalars in FP32 (every thread computes them; the FP64
-    // pipe is scarce): rz, the FP32 residual norms, alpha, beta
-    float rz = (float)w[0];
-    float rmax = sqrtf((float)w[1]);
+    float w[1] = {wf};
+    if (!grid_sum_f<1>(w, partial, shf, st, round)) return;
+    // inner-iteration scalars in FP32 (the FP64 pipe is scarce)
+    float rz = w[0];
+    float rmax = (float)rn64;
     const float tolf = (float)tol, deltaf = (float)delta;
     double prev_rn64 = rn64;
     int stall = 0;
     float beta = 0.f;
     float2 *cur = zp0, *nxt = zp1;
+    const int n4 = n >> 2;
     while (!conv && it < maxit && outer < maxouter) {
-        float *nxt_f = reinterpret_cast<float *>(nxt);
-        float d[1] = {spmv_fused_zp<TPR, U, PIPE>(n, rowptr, pack32, cur, nxt_f, q, beta)};
+        float d[1] = {sp.fused_zp(cur, nxt, q, beta)};
         if (!grid_sum_f<1>(d, partial, shf, st, round)) return;   // barrier 1
         const float pq = d[0];
         if (!(pq > 0.f) || !isfinite(pq)) {
@@ -442,16 +462,47 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
             break;
         }
         const float alpha = rz / pq;
+        // vector phase, four rows per thread: two (z, p) pairs per 16-byte load
         float uf0 = 0.f, uf1 = 0.f;
-        for (int i = gtid; i < n; i += gsz) {
-            const float pi = nxt_f[2 * i + 1];
-            xc[i] += alpha * pi;
-            float ri = r[i] - alpha * q[i];
-            r[i] = ri;
-            float zi = dinv[i] * ri;
-            nxt_f[2 * i] = zi;
-            uf0 += ri * zi;
-            uf1 += ri * ri;
+        {
+            float4 *nx4 = reinterpret_cast<float4 *>(nxt);
+            float4 *xc4 = reinterpret_cast<float4 *>(xc);
+            float4 *r4 = reinterpret_cast<float4 *>(r);
+            const float4 *q4 = reinterpret_cast<const float4 *>(q);
+            const float4 *di4 = reinterpret_cast<const float4 *>(dinv);
+            for (int i = gtid; i < n4; i += gsz) {
+                float4 a = nx4[2 * i], c = nx4[2 * i + 1];
+                const float4 qq = q4[i], dd = di4[i];
+                float4 rr = r4[i], xx = xc4[i];
+                xx.x += alpha * a.y;
+                xx.y += alpha * a.w;
+                xx.z += alpha * c.y;
+                xx.w += alpha * c.w;
+                rr.x -= alpha * qq.x;
+                rr.y -= alpha * qq.y;
+                rr.z -= alpha * qq.z;
+                rr.w -= alpha * qq.w;
+                a.x = dd.x * rr.x;
+                a.z = dd.y * rr.y;
+                c.x = dd.z * rr.z;
+                c.z = dd.w * rr.w;
+                xc4[i] = xx;
+                r4[i] = rr;
+                nx4[2 * i] = a;
+                nx4[2 * i + 1] = c;
+                uf0 += rr.x * a.x + rr.y * a.z + rr.z * c.x + rr.w * c.z;
+                uf1 += rr.x * rr.x + rr.y * rr.y + rr.z * rr.z + rr.w * rr.w;
+            }
+            for (int i = 4 * n4 + gtid; i < n; i += gsz) {
+                float2 e = nxt[i];
+                xc[i] += alpha * e.y;
+                const float ri = r[i] - alpha * q[i];
+                r[i] = ri;
+                e.x = dinv[i] * ri;
+                nxt[i] = e;
+                uf0 += ri * e.x;
+                uf1 += ri * ri;
+            }
         }
         float u[2] = {uf0, uf1};
         if (!grid_sum_f<2>(u, partial, shf, st, round)) return;   // barrier 2
@@ -467,7 +518,7 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
             }
             if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
             double t[1];
-            t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+            t[0] = sp.resid64(x, r64, b);
             if (!grid_sum<1>(t, partial, sh, st, round)) return;
             outer++;
             rn64 = sqrt(t[0]);
@@ -482,19 +533,18 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
             stall = (rn64 > 0.9 * prev_rn64) ? stall + 1 : 0;
             prev_rn64 = rn64;
             if (stall >= 16) break;   // no progress: report NOT_CONVERGED
-            float yf0 = 0.f, yf1 = 0.f;
+            float yf = 0.f;
             for (int i = gtid; i < n; i += gsz) {
-                float ri = (float)r64[i];
-                float zi = dinv[i] * ri;
+                const float ri = (float)r64[i];
+                const float zi = dinv[i] * ri;
                 r[i] = ri;
-                nxt_f[2 * i] = zi;
-                yf0 += ri * zi;
-                yf1 += ri * ri;
+                nxt[i].x = zi;
+                yf += ri * zi;
             }
-            float y[2] = {yf0, yf1};
-            if (!grid_sum_f<2>(y, partial, shf, st, round)) return;
+            float y[1] = {yf};
+            if (!grid_sum_f<1>(y, partial, shf, st, round)) return;
             rz_new = y[0];
-            rmax = sqrtf(y[1]);
+            rmax = (float)rn64;
         }
         beta = restart ? 0.0f : rz_new / rz;
         rz = rz_new;
@@ -508,6 +558,256 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
         st->relres = rn64 / (bn > 0 ? bn : 1.0);
         if (st->status == 0 && !conv) st->status = GRMP_ERR_NOT_CONVERGED;
     }
+}
+
+template <int TPR, int U, bool PIPE>
+__global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) : (U >= 8 ? 4 : 5)) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+                                                    const double *vals64, const int2 *pack32, const double *b,
+                                                    double *x, const float *dinv, float *r, float *q, float *xc,
+                                                    float2 *zp0, float2 *zp1, double *r64, double *partial,
+                                                    SolveState *st, double abstol, double reltol, double delta,
+                                                    int maxit, int maxouter, int guess) {
+    RowsSpmv<TPR, U, PIPE> sp{n, rowptr, cols, vals64, pack32};
+    pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
+                   guess);
+}
+
+// ------------------------------------------------------------ staged mixed PCG
+// The FP32 matrix re-laid out in fixed-size row windows (kStgRec bytes each):
+//   int row0, int nrows | uint16 local row offsets [nrows + 1] | pad to 16 B |
+//   int2 (column, FP32 value bits) entries of rows row0 .. row0 + nrows - 1.
+// Windows are packed greedily with whole rows.  Each block of the staged
+// kernel owns a contiguous range of windows and streams them, iteration after
+// iteration, through a ring of S shared-memory stages with one bulk async
+// copy per window (cp.async.bulk, completion counted on an mbarrier): warp 0
+// issues the copies, the other warps compute rows out of shared memory, so
+// the only global loads left on the compute warps are the gathers of the
+// search direction, which hit L1/L2.  The stream never stops at iteration
+// boundaries: the copies of the next iteration's first windows are issued as
+// soon as their stages are released, and land during the vector phase and
+// the grid barriers.
+constexpr int kStgRec = 32768;
+
+__host__ __device__ __forceinline__ int stg_header_bytes(int nrows) { return (8 + 2 * (nrows + 1) + 15) & ~15; }
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    for (long long spins = 0; spins < GRMP_SPIN_LIMIT; spins++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+template <int TPR, int U, int NT, int S>
+struct StagedSpmv {
+    static constexpr int NC = NT / 32 - 1;   // compute warps
+    static constexpr int RPW = 32 / TPR;
+    // FP64 residual: plain grid-strided rows from the CSR arrays
+    int n;
+    const int32_t *rowptr, *cols;
+    const double *vals64;
+    // window stream
+    const char *rec;
+    char *stage;            // S x kStgRec bytes of shared memory
+    uint64_t *full, *empty;
+    int jb, cnt;            // this block's windows
+    unsigned consumed;      // windows consumed so far (all threads)
+    unsigned issued;        // windows issued so far (issuing thread only)
+    int *status;
+
+    __device__ __forceinline__ bool issue_one() {
+        const unsigned qn = issued, s = qn % S;
+        if (qn >= (unsigned)S && !mbar_wait(&empty[s], (qn / S - 1) & 1)) return false;
+        mbar_arrive_expect_tx(&full[s], kStgRec);
+        bulk_load(stage + (size_t)s * kStgRec, rec + (size_t)(jb + (int)(qn % (unsigned)cnt)) * kStgRec, kStgRec,
+                  &full[s]);
+        issued = qn + 1;
+        return true;
+    }
+    // first S windows, before the first SpMV
+    __device__ __forceinline__ void prologue() {
+        if (threadIdx.x == 0 && cnt > 0)
+            for (int m = 0; m < S; m++)
+                if (!issue_one()) {
+                    atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
+                    break;
+                }
+    }
+    // wait (bounded) for the copies still in flight before the block exits:
+    // the last copy issued into each stage (copies into one stage are
+    // serialised by its release barrier)
+    __device__ __forceinline__ void drain() {
+        if (threadIdx.x == 0 && cnt > 0)
+            for (unsigned qn = issued > (unsigned)S ? issued - S : 0u; qn < issued; qn++)
+                if (!mbar_wait(&full[qn % S], (qn / S) & 1)) break;
+        __syncthreads();
+    }
+
+    __device__ __forceinline__ float fused_zp(const float2 *cur, float2 *nxt, float *q, float beta) {
+        float dacc = 0.f;
+        const int warp = threadIdx.x >> 5;
+        if (cnt <= 0) return dacc;
+        if (warp == 0) {
+            if (threadIdx.x == 0) {
+                for (int m = 0; m < cnt; m++)
+                    if (!issue_one()) {
+                        atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
+                        break;
+                    }
+            }
+            __syncwarp();
+        } else {
+            const int cw = warp - 1;
+            const int lane = threadIdx.x & (TPR - 1);
+            const int gin = (threadIdx.x & 31) / TPR;
+            int T = 0;   // row steps of the windows before this one
+            for (int m = 0; m < cnt; m++) {
+                const unsigned qn = consumed + m, s = qn % S;
+                if (!mbar_wait(&full[s], (qn / S) & 1)) {
+                    atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
+                    break;
+                }
+                const char *w = stage + (size_t)s * kStgRec;
+                const int row0 = reinterpret_cast<const int *>(w)[0];
+                const int nr = reinterpret_cast<const int *>(w)[1];
+                const uint16_t *lrp = reinterpret_cast<const uint16_t *>(w + 8);
+                const int2 *ent = reinterpret_cast<const int2 *>(w + stg_header_bytes(nr));
+                const int steps = (nr + RPW - 1) / RPW;
+                int j = cw - T % NC;
+                if (j < 0) j += NC;
+                for (; j < steps; j += NC) {
+                    const int i = j * RPW + gin;
+                    float sum = 0.f;
+                    if (i < nr) {
+                        const int kb = lrp[i], e = lrp[i + 1];
+                        for (int k = kb + lane; k < e; k += TPR * U) {
+                            int c[U];
+                            float v[U];
+#pragma unroll
+                            for (int u = 0; u < U; u++) {
+                                const int idx = k + u * TPR;
+                                if (idx < e) {
+                                    const int2 pe = ent[idx];
+                                    c[u] = pe.x;
+                                    v[u] = __int_as_float(pe.y);
+                                } else {
+                                    c[u] = 0;
+                                    v[u] = 0.f;
+                                }
+                            }
+#pragma unroll
+                            for (int u = 0; u < U; u++) {
+                                const float2 g = cur[c[u]];
+                                sum += v[u] * __fmaf_rn(beta, g.y, g.x);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int o = TPR / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                    if (i < nr && lane == 0) {
+                        const int r = row0 + i;
+                        const float2 me = cur[r];
+                        const float pn = __fmaf_rn(beta, me.y, me.x);
+                        nxt[r] = make_float2(me.x, pn);
+                        q[r] = sum;
+                        dacc += pn * sum;
+                    }
+                }
+                T += steps;
+                __syncwarp();
+                if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
+            }
+        }
+        consumed += cnt;
+        return dacc;
+    }
+    __device__ __forceinline__ double resid64(const double *x, double *r64, const double *b) {
+        return spmv_grid<TPR, 4, false, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+    }
+};
+
+template <int TPR, int U, int NT, int S>
+__global__ void __launch_bounds__(NT, 2048 / NT / 2) k_pcg_mixed_staged(int n, const int32_t *rowptr, const int32_t *cols,
+                                                            const double *vals64, const char *rec, int nwin,
+                                                            const double *b, double *x, const float *dinv,
+                                                            float *r, float *q, float *xc, float2 *zp0,
+                                                            float2 *zp1, double *r64,
+                                                            double *partial, SolveState *st, double abstol,
+                                                            double reltol, double delta, int maxit, int maxouter,
+                                                            int guess) {
+    extern __shared__ __align__(128) char stage_smem[];
+    __shared__ __align__(8) uint64_t bars[2 * S];
+    using SP = StagedSpmv<TPR, U, NT, S>;
+    SP sp;
+    sp.n = n;
+    sp.rowptr = rowptr;
+    sp.cols = cols;
+    sp.vals64 = vals64;
+    sp.rec = rec;
+    sp.stage = stage_smem;
+    sp.full = bars;
+    sp.empty = bars + S;
+    sp.jb = (int)((long long)blockIdx.x * nwin / gridDim.x);
+    sp.cnt = (int)((long long)(blockIdx.x + 1) * nwin / gridDim.x) - sp.jb;
+    sp.consumed = 0;
+    sp.issued = 0;
+    sp.status = &st->status;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&sp.full[s], 1);
+            mbar_init(&sp.empty[s], SP::NC);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    sp.prologue();
+    pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
+                   guess);
+    sp.drain();
+}
+
+// fills the window records from the packed FP32 pairs (one block per window)
+__global__ void k_stage_fill(const int32_t *win_row0, const int32_t *rowptr, const int2 *pack, char *rec) {
+    const int j = blockIdx.x;
+    const int r0 = win_row0[j], nr = win_row0[j + 1] - r0;
+    char *w = rec + (size_t)j * kStgRec;
+    const int base = rowptr[r0];
+    if (threadIdx.x == 0) {
+        reinterpret_cast<int *>(w)[0] = r0;
+        reinterpret_cast<int *>(w)[1] = nr;
+    }
+    uint16_t *lrp = reinterpret_cast<uint16_t *>(w + 8);
+    for (int i = threadIdx.x; i <= nr; i += blockDim.x) lrp[i] = (uint16_t)(rowptr[r0 + i] - base);
+    const int ne = rowptr[r0 + nr] - base;
+    int2 *ent = reinterpret_cast<int2 *>(w + stg_header_bytes(nr));
+    for (int k = threadIdx.x; k < ne; k += blockDim.x) ent[k] = pack[base + k];
 }
 
 // ------------------------------------------------------------------ helpers
@@ -562,8 +862,76 @@ void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, co
 }
 
 // SpMV configurations of the persistent solvers: (lanes per row, loads in
-// flight per lane), encoded 100*TPR + U.
-constexpr int kConfigs[] = {208, 404, 408, 804, 1602, 10204, 10404, 10408, 10804, 10402, 10802};
+// flight per lane), encoded 100*TPR + U; + 10000: software-pipelined row
+// loop; + 20000: staged windows, 512 threads x 3 stages per block; + 30000:
+// staged windows, 1024 threads x 6 stages (the staged ones: mixed solves only).
+constexpr int kConfigs[] = {208,   404,   408,   804,   1602,  10204, 10404, 10408,
+                            10804, 10402, 10802, 20204, 20408, 20804, 30408, 30804};
+
+inline bool staged_config(int cfg) { return cfg >= 20000; }
+
+// Window layout of the staged SpMV, built once per matrix pattern from the
+// row pointers (greedy: whole rows while header + entries fit one record).
+int stage_build(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int n = A->nrows;
+    std::vector<int32_t> rp((size_t)n + 1);
+    cudaError_t e = cudaMemcpyAsync(rp.data(), A->d_rowptr, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "staged SpMV: row pointer download");
+    std::vector<int32_t> row0;
+    int r = 0;
+    while (r < n) {
+        const int start = r;
+        long long ne = 0;
+        while (r < n) {
+            const int len = rp[r + 1] - rp[r];
+            if (stg_header_bytes(r - start + 1) + 8 * (ne + len) > kStgRec) break;
+            ne += len;
+            r++;
+        }
+        if (r == start) {
+            A->stg_state = -1;
+            return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "staged SpMV: row %d has %d entries, more than a window holds",
+                             r, rp[r + 1] - rp[r]);
+        }
+        row0.push_back(start);
+    }
+    row0.push_back(n);
+    const int nwin = (int)row0.size() - 1;
+    int32_t *d_row0 = nullptr;
+    char *d_rec = nullptr;
+    const size_t rec_bytes = std::max<size_t>(1, (size_t)nwin) * kStgRec;
+    int rc = grmp_alloc(ctx, (void **)&d_row0, row0.size() * 4);
+    if (rc) return rc;
+    rc = grmp_alloc(ctx, (void **)&d_rec, rec_bytes);
+    if (rc) {
+        grmp_free(ctx, d_row0, row0.size() * 4);
+        return rc;
+    }
+    e = cudaMemcpyAsync(d_row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_rec, 0, rec_bytes, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // row0 is a host vector
+    if (e != cudaSuccess) {
+        grmp_free(ctx, d_row0, row0.size() * 4);
+        grmp_free(ctx, d_rec, rec_bytes);
+        return grmp_cuda_fail(ctx, e, "staged SpMV: window upload");
+    }
+    A->d_stg_row0 = d_row0;
+    A->d_stg_rec = d_rec;
+    A->stg_rec_bytes = rec_bytes;
+    A->stg_nwin = nwin;
+    A->stg_state = 1;
+    return GRMP_OK;
+}
+
+void stage_fill(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    if (A->stg_nwin <= 0) return;
+    k_stage_fill<<<A->stg_nwin, 256, 0, ctx->stream>>>(A->d_stg_row0, A->d_rowptr, (const int2 *)A->d_pack32,
+                                                       A->d_stg_rec);
+    GRMP_LAUNCHED(ctx);
+}
 
 int heuristic_tpr(grmp_matrix A) {
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
@@ -663,9 +1031,84 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
     return hs.status;
 }
 
+template <int TPR, int U, int NT, int S>
+int launch_pcg_staged(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
+                      grmp_solve_stats *out, char *work, SolveState *dst, WorkLayout lay) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int cfg = (NT == 512 ? 20000 : 30000) + 100 * TPR + U;
+    if (p->mode != GRMP_SOLVE_MIXED)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: staged configurations are for mixed solves", cfg);
+    if (A->stg_state == 0) {
+        int rc = stage_build(A);
+        if (rc) return rc;
+        stage_fill(A);
+    }
+    if (A->stg_state < 0)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: a row does not fit a staged window", cfg);
+    const int n = A->nrows;
+    auto kern = k_pcg_mixed_staged<TPR, U, NT, S>;
+    const int dyn = S * kStgRec;
+    cudaError_t e = cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, dyn);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "staged PCG: occupancy");
+    if (per_sm < 1) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: does not fit an SM", cfg);
+    const int maxg = std::min(per_sm * ctx->num_sms, kPartStride / 4);
+    int grid = std::min(maxg, std::max(A->stg_nwin, nblk(n, NT)));
+    if (p->grid_blocks > 0) grid = std::min(grid, p->grid_blocks);
+    grid = std::max(1, grid);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
+    float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
+    float *xc = (float *)(work + 3 * lay.vec);
+    float2 *zp0 = (float2 *)(work + 4 * lay.vec), *zp1 = (float2 *)(work + 6 * lay.vec);
+    double *r64 = (double *)(work + lay.off_r64);
+    double *part = (double *)(work + lay.off_part);
+    int nn = n, nw = A->stg_nwin, mi = p->maxiter, mo = p->max_outer > 0 ? p->max_outer : 1000;
+    int guess = p->use_initial_guess ? 1 : 0;
+    double at = p->abstol, rt = p->reltol, dl = p->inner_reltol > 0 && p->inner_reltol < 1 ? p->inner_reltol : 0.1;
+    const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+    const double *v64 = A->d_vals64, *bb = bvec;
+    const char *rec = A->d_stg_rec;
+    double *xx = xvec;
+    void *args[] = {&nn, &rp, &ci, &v64, &rec, &nw, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
+                    &at, &rt, &dl, &mi, &mo, &guess};
+    cudaEventRecord(e0, ctx->stream);
+    e = cudaLaunchCooperativeKernel((void *)kern, grid, NT, args, (size_t)dyn, ctx->stream);
+    GRMP_LAUNCHED(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    SolveState hs;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "staged PCG launch");
+    out->status = hs.status;
+    out->iterations = hs.iters;
+    out->outer_iterations = hs.outer;
+    out->final_relres = hs.relres;
+    out->spmv_config = cfg;
+    out->grid_blocks = grid;
+    out->solve_ms = ms;
+    if (hs.status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, GRMP_ERR_NOT_CONVERGED, "PCG: %d iterations, relative residual %.3e", hs.iters, hs.relres);
+    if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a barrier wait timed out");
+    if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
+    return hs.status;
+}
+
 int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_solve_params *p, grmp_solve_stats *st,
                  char *work, SolveState *dst, WorkLayout lay) {
     switch (cfg) {
+        case 20204: return launch_pcg_staged<2, 4, 512, 3>(A, b, x, p, st, work, dst, lay);
+        case 20408: return launch_pcg_staged<4, 8, 512, 3>(A, b, x, p, st, work, dst, lay);
+        case 20804: return launch_pcg_staged<8, 4, 512, 3>(A, b, x, p, st, work, dst, lay);
+        case 30408: return launch_pcg_staged<4, 8, 1024, 6>(A, b, x, p, st, work, dst, lay);
+        case 30804: return launch_pcg_staged<8, 4, 1024, 6>(A, b, x, p, st, work, dst, lay);
         case 208: return launch_pcg<2, 8, false>(A, b, x, p, st, work, dst, lay);
         case 404: return launch_pcg<4, 4, false>(A, b, x, p, st, work, dst, lay);
         case 408: return launch_pcg<4, 8, false>(A, b, x, p, st, work, dst, lay);
@@ -699,6 +1142,7 @@ int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_para
     int best = heuristic_config(A);
     double bt = 1e30;
     for (int cfg : kConfigs) {
+        if (staged_config(cfg) && (p->mode != GRMP_SOLVE_MIXED || A->stg_state < 0)) continue;
         grmp_solve_stats s{};
         dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);   // warm-up: first launch of this instantiation
         s = grmp_solve_stats{};
@@ -727,11 +1171,11 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     int n = A->nrows;
     // workspace, each array 256-byte aligned:
     //   FP64 : dinv r z p q (double)                  | partials | state
-    //   MIXED: dinv r z p q xc (float) | r64 (double)  | partials | state
+    //   MIXED: dinv r q xc (float), (z, p) pairs x2 | r64 (double) | partials | state
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     size_t pbytes = (size_t)2 * kPartStride * 8;   // two alternating partial-sum buffers
     size_t vec = mixed ? al((size_t)n * 4) : al((size_t)n * 8);
-    size_t nvec = mixed ? 8 : 5;   // MIXED: dinv r q xc (float) + two interleaved (z, p) float2 buffers
+    size_t nvec = mixed ? 8 : 5;   // MIXED: dinv, r, q, xc (float) + two (z, p) float2 pair buffers
     size_t off_r64 = nvec * vec;
     size_t off_part = off_r64 + (mixed ? al((size_t)n * 8) : 0);
     size_t off_state = off_part + al(pbytes);
@@ -772,6 +1216,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
         k_pack32<<<(unsigned)((A->nnz + 255) / 256), 256, 0, ctx->stream>>>(A->nnz, A->d_cols, A->d_vals32,
                                                                            (int2 *)A->d_pack32);
         GRMP_LAUNCHED(ctx);
+        if (A->stg_state == 1) stage_fill(A);   // the staged windows hold a copy of the pairs
     }
     int cfg = p->spmv_config;
     if (cfg == 0) {   // autotuned once per matrix and solver mode
@@ -787,7 +1232,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
 int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
     grmp_context ctx = A->space->mesh->ctx;
     int n = A->nrows;
-    int tpr = A->tuned_cfg ? A->tuned_cfg / 100 : heuristic_tpr(A);
+    int tpr = A->tuned_cfg ? (A->tuned_cfg % 10000) / 100 : heuristic_tpr(A);
     int grid = std::min(nblk(n, 256 / tpr), ctx->num_sms * 16);
     if (precision == GRMP_FP64) {
         if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv: no FP64 values");

@@ -177,3 +177,49 @@ class FESpace:
         if not out:
             return np.zeros(0, dtype=np.int32)
         return np.unique(np.concatenate(out)).astype(np.int32)
+
+
+# local P2 edge DoFs: the two local vertices of each edge, in the basis order of
+# src/fedefs/h1_p2.jl (edge functions 4 lambda_a lambda_b)
+_P2_EDGES = {2: [(0, 1), (1, 2), (2, 0)], 3: [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]}
+
+
+def interpolate(FES: FESpace, f, edge_points: int = 5) -> np.ndarray:
+    """interpolate!(Target, FES, f) for H1P1 and H1P2 (scalar or vector):
+    vertex DoFs by point evaluation (point_evaluation!, src/fedefs/h1_p2.jl:
+    47-59), P2 edge DoFs so that the interpolant keeps the mean of f on every
+    edge (ensure_moments!, :61-71, :73-92), the mean taken with a Gauss rule of
+    `edge_points` points.  Along an edge (a, b) the vertex functions integrate
+    to |E|/6 and the edge function to 2|E|/3, so the edge DoF is
+    3/2 mean_E(f) - (f(a) + f(b))/4.  f maps points (m, dim) to values
+    (m, ncomponents) or (m,).  Host-side, like the reference's."""
+    g = FES.xgrid
+    fe = FES.FEType
+    if fe.kind not in (FE_H1P1, FE_H1P2):
+        raise ValueError(f"interpolate: element {fe} not supported")
+    dim, nc = g.dim, fe.ncomponents
+    nv = dim + 1
+    nb = nv if fe.kind == FE_H1P1 else (6 if dim == 2 else 10)
+
+    def ev(x):
+        y = np.asarray(f(x), dtype=np.float64)
+        return y.reshape(x.shape[0], nc)
+
+    X = g.coords[g.cells]                       # (ncells, dim+1, dim)
+    out = np.zeros(FES.ndofs)
+    cd = FES.celldofs
+    vals_v = [ev(X[:, a, :]) for a in range(nv)]
+    for c in range(nc):
+        for a in range(nv):
+            out[cd[:, c * nb + a]] = vals_v[a][:, c]
+    if fe.kind == FE_H1P2:
+        t, w = np.polynomial.legendre.leggauss(edge_points)
+        t, w = 0.5 * (t + 1.0), 0.5 * w
+        for e, (a, b) in enumerate(_P2_EDGES[dim]):
+            mean = np.zeros((X.shape[0], nc))
+            for tk, wk in zip(t, w):
+                mean += wk * ev((1.0 - tk) * X[:, a, :] + tk * X[:, b, :])
+            dofv = 1.5 * mean - 0.25 * (vals_v[a] + vals_v[b])
+            for c in range(nc):
+                out[cd[:, c * nb + nv + e]] = dofv[:, c]
+    return out

@@ -199,6 +199,31 @@ typedef struct {
  * linearform.jl:47-237).  FP64, deterministic (ascending cell order). */
 int grmp_assemble_linear(grmp_space space, const grmp_rhs *rhs, grmp_vector b);
 
+/* ------------------------------------------------------- item integrators */
+
+typedef enum { GRMP_ITEM_IDENTITY = 0, GRMP_ITEM_GRADIENT = 1 } grmp_item_operator;
+
+/* ItemIntegrator over all cells of an H1P1 / H1P2 space (scalar or vector),
+ * replacing evaluate / evaluate! of src/assemblypatterns/itemintegrator.jl
+ * (:173-330) for the three error/norm integrators of that file:
+ *   L2ErrorIntegrator(data, op; factor)  (:40-94):  data != NULL, v == NULL
+ *       integrand sum_j (data_j(x) - factor * (op u)_j)^2
+ *   L2NormIntegrator(op)                 (:96-130): data == NULL, v == NULL
+ *       integrand sum_j (factor * (op u)_j)^2
+ *   L2DifferenceIntegrator(op)           (:132-158): v != NULL (data must be NULL)
+ *       integrand sum_j ((op u)_j - (op v)_j)^2
+ * op: GRMP_ITEM_IDENTITY (components u_c) or GRMP_ITEM_GRADIENT (component-major
+ * [du_1/dx_1 .. du_1/dx_d, du_2/dx_1 ..]); data->ncomponents must equal the
+ * operator's length (data->factor, test_operator and cell_group are ignored).
+ * quadorder: the integrator's bonus order (>= 0), or -1 for the reference's
+ * "auto" (2 * data->bonus_quadorder; 2 without data); the rule has order
+ * polyorder - (op == GRADIENT) + bonus (src/assemblypatterns.jl:559-565).
+ * cell_values (optional, host, [ncells]) receives the per-cell integrals, total
+ * (optional, host) their sum; sqrt(total) is the error/norm.  FP64;
+ * reproducible run to run (fixed summation order). */
+int grmp_item_l2error(grmp_space space, grmp_vector u, grmp_vector v, int op, const grmp_rhs *data, double factor,
+                      int quadorder, double *cell_values, double *total);
+
 /* -------------------------------------------------------------- vectors */
 
 int grmp_vector_create(grmp_context ctx, int32_t n, grmp_vector *out);
@@ -244,7 +269,10 @@ typedef struct {
     int32_t max_outer;      /* MIXED: cap on FP64 refinement steps                        */
     int32_t spmv_config;    /* SpMV lanes per row and loads in flight, coded 100*lanes + loads,
                                +10000 for the software-pipelined row loop: 208, 404, 408, 804,
-                               1602, 10204, 10404, 10408, 10804, 10402, 10802; 0 = autotuned
+                               1602, 10204, 10404, 10408, 10804, 10402, 10802; MIXED only,
+                               rows streamed through shared memory in 32 KB windows by bulk
+                               async copies: 20204, 20408, 20804 (512 threads, 3 stages per
+                               block), 30408, 30804 (1024 threads, 6 stages); 0 = autotuned
                                per matrix and mode (timed trial solves); -1 = chosen from the
                                mean row length
                                (no timing, so the choice does not depend on concurrent GPU work) */

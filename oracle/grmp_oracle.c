@@ -668,6 +668,90 @@ int oracle_assemble_linear(double *b, int dim, int nverts, const double *coords,
 }
 
 /* ------------------------------------------------------------------------- */
+/* ItemIntegrator over cells (src/assemblypatterns/itemintegrator.jl)        */
+/* ------------------------------------------------------------------------- */
+
+/* L2ErrorIntegrator (:40-94), L2NormIntegrator (:96-130) and
+ * L2DifferenceIntegrator (:132-158) evaluated by evaluate! (:173-300):
+ * per cell in ascending order and per quadrature point,
+ *   input_k = sum_dof u[dof] cvals[k,dof,q]            (eval_febe!, dof ascending)
+ *   result  = sum_j (f_j(x_q) - factor*input_j)^2       (error; f = 0: norm)
+ *           = sum_j (input_j - input2_j)^2              (difference, v given)
+ *   cellv[cell] += result * w_q * vol,  total += result * w_q * vol
+ * (the AccumulatingVector of evaluate, :314-330, sums in the same order).
+ * Quadrature order: polyorder + shift(op) + quadorder
+ * (src/assemblypatterns.jl:559-565; Gradient shifts by -1).
+ * Returns the number of quadrature points, or -1. */
+int oracle_item_l2error(double *cellv, double *total, int dim, int nverts, const double *coords, int ncells,
+                        const int *cellnodes, int fe, int ncomp, const int *celldofs, const double *u,
+                        const double *v, int op, int data_kind, const double *par, int npar, double factor,
+                        int quadorder)
+{
+    (void)nverts;
+    if (op != OR_OP_IDENTITY && op != OR_OP_GRADIENT) return -1;
+    int nb = (fe == OR_FE_P1) ? dim + 1 : (dim == 2 ? 6 : 10);
+    int nd = nb * ncomp;
+    int polyorder = (fe == OR_FE_P1) ? 1 : 2;
+    int order = polyorder + (op == OR_OP_GRADIENT ? -1 : 0) + quadorder;
+    if (order < 0) order = 0;
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(dim, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    double *vals = (double *)malloc(sizeof(double) * (size_t)nq * nb);
+    double *derivs = (double *)malloc(sizeof(double) * (size_t)nq * nb * dim);
+    oracle_basis_tables(fe, dim, nq, xref, vals, derivs);
+    double G[3][3];
+    double *cv = (double *)malloc(sizeof(double) * (size_t)nq * nd * 9);
+    double X[12];
+    double acc = 0.0;
+    for (int cell = 0; cell < ncells; cell++) {
+        for (int vv = 0; vv <= dim; vv++)
+            for (int k = 0; k < dim; k++) X[vv * dim + k] = coords[(size_t)cellnodes[(size_t)cell * (dim + 1) + vv] * dim + k];
+        double A[3][3], det, vol;
+        oracle_geometry(dim, X, A, G, &det, &vol);
+        int rdim = h1_cvals(op, dim, ncomp, nb, nq, vals, derivs, G, cv);
+        double cellacc = 0.0;
+        for (int q = 0; q < nq; q++) {
+            double in1[9] = {0}, in2[9] = {0}, f[9] = {0};
+            for (int dof = 0; dof < nd; dof++) {
+                double c1 = u[celldofs[(size_t)cell * nd + dof]];
+                for (int k = 0; k < rdim; k++) in1[k] += c1 * cv[(q * nd + dof) * rdim + k];
+            }
+            if (v)
+                for (int dof = 0; dof < nd; dof++) {
+                    double c2 = v[celldofs[(size_t)cell * nd + dof]];
+                    for (int k = 0; k < rdim; k++) in2[k] += c2 * cv[(q * nd + dof) * rdim + k];
+                }
+            double result = 0.0;
+            if (v) {
+                for (int j = 0; j < rdim; j++) result += (in1[j] - in2[j]) * (in1[j] - in2[j]);
+            } else {
+                if (data_kind >= 0) {
+                    double x[3] = {0, 0, 0};
+                    for (int k = 0; k < dim; k++) {
+                        x[k] = X[k];
+                        for (int j = 0; j < dim; j++) x[k] += A[k][j] * xref[3 * q + j];
+                    }
+                    rhs_eval(data_kind, dim, rdim, par, npar, cell, x, f);
+                }
+                for (int j = 0; j < rdim; j++) {
+                    double e = f[j] - in1[j] * factor;
+                    result += e * e;
+                }
+            }
+            double contrib = result * w[q] * vol;
+            cellacc += contrib;
+            acc += contrib;
+        }
+        if (cellv) cellv[cell] = cellacc;
+    }
+    if (total) *total = acc;
+    free(vals); free(derivs); free(cv);
+    return nq;
+}
+
+/* ------------------------------------------------------------------------- */
 /* FP64 CG (Jacobi) on CSR -- used for sizes where a sparse-direct           */
 /* factorisation does not fit, and as the multi-threaded CPU baseline solve. */
 /* ------------------------------------------------------------------------- */

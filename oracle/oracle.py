@@ -74,6 +74,10 @@ def lib():
                                              ctypes.c_int, ip, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double,
                                              ctypes.c_int]
         L.oracle_assemble_linear.restype = ctypes.c_int
+        L.oracle_item_l2error.argtypes = [dp, dp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ip, ctypes.c_int,
+                                          ctypes.c_int, ip, dp, dp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_int]
+        L.oracle_item_l2error.restype = ctypes.c_int
         L.oracle_cg.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
         L.oracle_cg.restype = ctypes.c_int
         sp = ctypes.POINTER(ctypes.c_byte)
@@ -215,6 +219,38 @@ def assemble_linear(b, coords, cells, fe, ncomp, cdofs, rhs_kind, params, factor
     if nq < 0:
         raise RuntimeError("oracle linear assembly failed")
     return b
+
+
+# --------------------------------------------------------------------------
+# ItemIntegrator (src/assemblypatterns/itemintegrator.jl)
+# --------------------------------------------------------------------------
+
+OP_IDENTITY, OP_GRADIENT = 0, 1
+
+
+def item_l2error(coords, cells, fe, ncomp, cdofs, u, op=OP_IDENTITY, data_kind=-1, params=None, factor=1.0,
+                 quadorder=0, v=None):
+    """L2ErrorIntegrator / L2NormIntegrator (data_kind -1) / L2DifferenceIntegrator (v given) over all
+    cells; returns (per-cell values, total), the total summed in the reference's order."""
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    cells = np.ascontiguousarray(cells, dtype=np.int32)
+    cdofs = np.ascontiguousarray(cdofs, dtype=np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    par = np.zeros(1) if params is None else np.ascontiguousarray(params, dtype=np.float64).ravel()
+    if par.size == 0:
+        par = np.zeros(1)
+    cellv = np.zeros(cells.shape[0])
+    total = np.zeros(1)
+    vp = None
+    if v is not None:
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        vp = _dp(v)
+    nq = lib().oracle_item_l2error(_dp(cellv), _dp(total), coords.shape[1], coords.shape[0], _dp(coords),
+                                   cells.shape[0], _ip(cells), fe, ncomp, _ip(cdofs), _dp(u), vp, op, data_kind,
+                                   _dp(par), par.size, float(factor), int(quadorder))
+    if nq < 0:
+        raise RuntimeError("oracle item integrator failed")
+    return cellv, float(total[0])
 
 
 # --------------------------------------------------------------------------
