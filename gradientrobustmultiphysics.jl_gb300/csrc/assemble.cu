@@ -102,7 +102,10 @@ __global__ void k_cell_factors(int ncells, const double *coords, const int32_t *
     }
 }
 
-// Row-centric assembly.  S = slot index type (uint8_t / uint16_t).
+// Row-centric assembly.  S = slot index type (uint8_t / uint16_t).  A block
+// owns blockDim.x consecutive rows; their values (contiguous in the CSR) are
+// accumulated in shared memory, each thread adding its row's contributions in
+// incidence order, and written out once with coalesced stores.
 template <int DIM, int NB, int NC, typename T, typename S>
 __global__ void __launch_bounds__(128) k_assemble_rows(int32_t nrows, const int32_t *__restrict__ inc_ptr,
                                                        const int32_t *__restrict__ inc_cell,
@@ -111,46 +114,52 @@ __global__ void __launch_bounds__(128) k_assemble_rows(int32_t nrows, const int3
                                                        const T *__restrict__ fac, const T *__restrict__ gtens,
                                                        FastTerms ft, T *__restrict__ vals) {
     constexpr int LD = NB * NC;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tens = reinterpret_cast<T *>(smem_raw);
+    T *acc = tens + ((ft.tens_total + 1) & ~1);
+    const int row0 = blockIdx.x * blockDim.x;
+    const int row1 = min(row0 + (int)blockDim.x, nrows);
+    const int v0 = rowptr[row0], nv = rowptr[row1] - v0;
     for (int i = threadIdx.x; i < ft.tens_total; i += blockDim.x) tens[i] = gtens[i];
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) acc[i] = T(0);
     __syncthreads();
-    int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= nrows) return;
-    T *rv = vals + rowptr[row];
-    int nnz = rowptr[row + 1] - rowptr[row];
-    for (int k = 0; k < nnz; k++) rv[k] = T(0);
-    const S DROP = (S)~(S)0;
-    const int pe = inc_ptr[row + 1];
-    for (int p = inc_ptr[row]; p < pe; p++) {
-        const int cell = inc_cell[p];
-        const int A = inc_loc[p];
-        const int c1 = A / NB, a = A - c1 * NB;
-        const T *cf = fac + (size_t)cell * ft.nf_total;
-        const S *sl = slot + (size_t)p * LD;
-        T f[GRMP_MAX_TERMS * 16];
-        for (int i = 0; i < ft.nf_total && i < GRMP_MAX_TERMS * 16; i++) f[i] = cf[i];
+    const int row = row0 + threadIdx.x;
+    if (row < row1) {
+        T *rv = acc + (rowptr[row] - v0);
+        const S DROP = (S)~(S)0;
+        const int pe = inc_ptr[row + 1];
+        for (int p = inc_ptr[row]; p < pe; p++) {
+            const int cell = inc_cell[p];
+            const int A = inc_loc[p];
+            const int c1 = A / NB, a = A - c1 * NB;
+            const T *cf = fac + (size_t)cell * ft.nf_total;
+            const S *sl = slot + (size_t)p * LD;
+            T f[GRMP_MAX_TERMS * 16];
+            for (int i = 0; i < ft.nf_total && i < GRMP_MAX_TERMS * 16; i++) f[i] = cf[i];
 #pragma unroll
-        for (int B = 0; B < LD; B++) {
-            const S s = sl[B];
-            if (s == DROP) continue;
-            const int c2 = B / NB, b = B - c2 * NB;
-            T v = 0;
-            for (int ti = 0; ti < ft.n; ti++) {
-                const FastTerm &t = ft.t[ti];
-                const T *tt = tens + t.toff + a * NB + b;
-                if (t.op == GRMP_OP_HOOKE) {
-                    const T *ff = f + t.foff + (c1 * NC + c2) * DIM * DIM;
+            for (int B = 0; B < LD; B++) {
+                const S s = sl[B];
+                if (s == DROP) continue;
+                const int c2 = B / NB, b = B - c2 * NB;
+                T v = 0;
+                for (int ti = 0; ti < ft.n; ti++) {
+                    const FastTerm &t = ft.t[ti];
+                    const T *tt = tens + t.toff + a * NB + b;
+                    if (t.op == GRMP_OP_HOOKE) {
+                        const T *ff = f + t.foff + (c1 * NC + c2) * DIM * DIM;
 #pragma unroll
-                    for (int q = 0; q < DIM * DIM; q++) v += ff[q] * tt[q * NB * NB];
-                } else if (c1 == c2) {
-                    const T *ff = f + t.foff;
-                    for (int q = 0; q < t.ntens; q++) v += ff[q] * tt[q * NB * NB];
+                        for (int q = 0; q < DIM * DIM; q++) v += ff[q] * tt[q * NB * NB];
+                    } else if (c1 == c2) {
+                        const T *ff = f + t.foff;
+                        for (int q = 0; q < t.ntens; q++) v += ff[q] * tt[q * NB * NB];
+                    }
                 }
+                rv[s] += v;
             }
-            rv[s] += v;
         }
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) vals[v0 + i] = acc[i];
 }
 
 template <int DIM, int NB, int NC, typename T>
@@ -190,18 +199,22 @@ int run_assembly(grmp_matrix A, const FastTerms &ft, const std::vector<double> &
         }
         vals = (T *)A->d_vals32;
     }
-    size_t shm = tens.size() * sizeof(T);
-    if (shm > 200 * 1024) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "reference tensors too large for shared memory");
-    const int tpb = 128;
+    // rows per block: their values (at most rows x longest row) and the
+    // reference tensors in shared memory, at most ~100 KB so that two blocks fit an SM
+    const size_t tens_b = ((tens.size() + 1) & ~(size_t)1) * sizeof(T);
+    int tpb = 128;
+    while (tpb > 32 && tens_b + (size_t)tpb * A->max_row_nnz * sizeof(T) > 100 * 1024) tpb /= 2;
+    size_t shm = tens_b + (size_t)tpb * A->max_row_nnz * sizeof(T);
+    if (shm > 220 * 1024) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
     if (A->slot_bytes == 1) {
         auto kern = k_assemble_rows<DIM, NB, NC, T, uint8_t>;
-        if (shm > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
                                                             (const uint8_t *)A->d_slot, A->d_rowptr, fac, dtens, ft, vals);
         GRMP_LAUNCHED(ctx);
     } else {
         auto kern = k_assemble_rows<DIM, NB, NC, T, uint16_t>;
-        if (shm > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
                                                             (const uint16_t *)A->d_slot, A->d_rowptr, fac, dtens, ft, vals);
         GRMP_LAUNCHED(ctx);
