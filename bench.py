@@ -515,7 +515,10 @@ def run_stokes(args):
 def run_serve(args):
     """Serving loop: Poisson-process arrivals of 2D/3D Poisson and
     reaction-diffusion requests (H1P1/H1P2, 1e3..2e6 DoFs), 4 slots, HBM
-    budget 150 GB, mixed-precision solves; DoF/s and p50/p99 latency."""
+    budget 150 GB, mixed-precision solves; DoF/s and p50/p99 latency.  The
+    same requests are then submitted all at once in mixed and in plain FP64
+    mode (serving capacity of each, and the largest relative difference
+    between the two solutions of a request)."""
     dist = Dist()
     G = _package()
     from grmp_gb300 import build as B
@@ -529,6 +532,16 @@ def run_serve(args):
     xs, sts, makespan = SV.run(reqs, nslots=args.slots, hbm_budget_bytes=150 << 30, realtime=True)
     clocks = clk.stop()
     summ = SV.summarize(reqs, sts, makespan)
+    # capacity: the same requests submitted at once, mixed and plain FP64 serving
+    sat = {}
+    sols = {}
+    for mode in ("mixed", "fp64"):
+        xm, sm, mk = SV.run(reqs, nslots=args.slots, hbm_budget_bytes=150 << 30, mode=mode, realtime=False)
+        ss = SV.summarize(reqs, sm, mk)
+        sat[mode] = {"dof_per_s": ss["dof_per_s"], "makespan_s": mk, "failed": ss["failed"],
+                     "latency_ms": ss["latency_ms"]}
+        sols[mode] = xm
+    rel = [float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)) for a, b in zip(sols["mixed"], sols["fp64"])]
     line = {"metric": "serving DoF/s and p50/p99 latency (Poisson-process arrivals)", "value": summ["dof_per_s"],
             "unit": "DoF/s", "n_gpus": dist.ws, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * makespan,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-outer",
@@ -537,7 +550,9 @@ def run_serve(args):
                        "mean_interarrival_s": args.interarrival, "dofs": summ["dofs"]},
             "latency_ms": summ["latency_ms"], "failed": summ["failed"],
             "run_ms_p50": float(np.percentile([s["run_ms"] for s in sts], 50)),
-            "queue_ms_p50": float(np.percentile([s["queue_ms"] for s in sts], 50)), "clocks": clocks}
+            "queue_ms_p50": float(np.percentile([s["queue_ms"] for s in sts], 50)),
+            "saturated": sat, "mixed_vs_plain": sat["mixed"]["dof_per_s"] / sat["fp64"]["dof_per_s"],
+            "max_rel_diff_mixed_vs_fp64": max(rel), "clocks": clocks}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()

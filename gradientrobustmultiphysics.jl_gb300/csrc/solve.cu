@@ -942,8 +942,16 @@ int heuristic_tpr(grmp_matrix A) {
     return 32;
 }
 
-int heuristic_config(grmp_matrix A) {
+// Configuration from the mean row length alone (no timing): the autotuner's
+// usual choices on FEM matrices -- plain row loops for FP64 (FP64-pipe bound,
+// more loads in flight do not help), the pipelined row loop for FP32.
+int heuristic_config(grmp_matrix A, bool mixed) {
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
+    if (mixed) {
+        if (avg <= 8) return 10204;
+        if (avg <= 20) return 10404;
+        return 10408;
+    }
     if (avg <= 8) return 208;
     if (avg <= 20) return 404;
     return 408;
@@ -1131,15 +1139,16 @@ int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_
 int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_params *p, char *work, SolveState *dst,
                     WorkLayout lay) {
     grmp_context ctx = A->space->mesh->ctx;
-    if (A->nrows < 20000) return heuristic_config(A);
+    const bool mixed = p->mode == GRMP_SOLVE_MIXED;
+    if (A->nrows < 20000) return heuristic_config(A, mixed);
     double *xs = nullptr;
-    if (grmp_alloc(ctx, (void **)&xs, (size_t)A->nrows * 8)) return heuristic_config(A);
+    if (grmp_alloc(ctx, (void **)&xs, (size_t)A->nrows * 8)) return heuristic_config(A, mixed);
     grmp_solve_params q = *p;
     q.maxiter = 24;
     q.use_initial_guess = 0;
     q.reltol = 0.0;
     q.abstol = 0.0;
-    int best = heuristic_config(A);
+    int best = heuristic_config(A, mixed);
     double bt = 1e30;
     for (int cfg : kConfigs) {
         if (staged_config(cfg) && (p->mode != GRMP_SOLVE_MIXED || A->stg_state < 0)) continue;
@@ -1224,7 +1233,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
         if (!slot) slot = autotune_config(A, b, p, work, dst, lay);
         cfg = slot;
     } else if (cfg < 0) {   // heuristic from the row length: no timing, independent of other work on the GPU
-        cfg = heuristic_config(A);
+        cfg = heuristic_config(A, mixed);
     }
     return dispatch_pcg(cfg, A, b->d, x->d, p, st, work, dst, lay);
 }
@@ -1359,7 +1368,7 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "noalloc solve: jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: non-positive or non-finite diagonal entry");
-    int cfg = p->spmv_config > 0 ? p->spmv_config : (A->tuned_cfg ? A->tuned_cfg : heuristic_config(A));
+    int cfg = p->spmv_config > 0 ? p->spmv_config : (A->tuned_cfg ? A->tuned_cfg : heuristic_config(A, false));
     int grid = 0;
     switch (cfg) {
         case 208: e = launch_pcg64_static<2, 8, false>(A, b->d, x->d, p, work, &grid); break;
