@@ -230,8 +230,8 @@ def run_reference(args):
 # ------------------------------------------------------------------ GPU arm
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one
 # k_pcg_mixed launch on the 48^3 case divided by pcg_bytes() of the same
-# launch: 183.94 GB / 185.02 GB (summary under profiles/).
-TRAFFIC_PER_ALGORITHMIC_BYTE = 183.94 / 185.02
+# launch: 180.78 GB / 185.73 GB (summary under profiles/).
+TRAFFIC_PER_ALGORITHMIC_BYTE = (163.612 + 17.166) / 185.732
 
 
 def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool) -> float:
@@ -392,7 +392,7 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": kb * TRAFFIC_PER_ALGORITHMIC_BYTE,
                 "traffic_source": "ncu dram__bytes_read+write of k_pcg_mixed on the 48^3 case "
-                                  "(0.994 x its algorithmic bytes), scaled to this launch",
+                                  "(0.973 x its algorithmic bytes), scaled to this launch",
                 "kernel": "k_pcg_mixed (persistent)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"}
     if direct:
