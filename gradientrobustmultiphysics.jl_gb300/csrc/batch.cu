@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
 
 struct DNode {
     int s, f, front_off, child_off, nchild, entry_off, nentry, ext_off;
-    long long L_off, U_off;
+    long long L_off, U_off, uv_off;
 };
 
 // A sweep whose refined residual stagnates (FP64 rounding floor of an
@@ -611,10 +611,16 @@ struct DirectDev {
     const DNode *node;
     const int32_t *front, *child, *ent_rel, *ent_pos, *ext;
     const int32_t *prob_node0, *prob_nnodes;
-    double *work;                                   // per resident block: [F | U | L]
-    long long slot_doubles, F_doubles, U_doubles;
+    // level schedule of each problem's tree: levels lvl_ptr[prob_lvl0 + l ..
+    // + l + 1) index lvl_nodes (node ids, children always in lower levels)
+    const int32_t *lvl_ptr, *lvl_nodes, *prob_lvl0, *prob_nlev;
+    double *work;                                   // per resident block: [F | U | L | uv]
+    long long slot_doubles, F_doubles, U_doubles, L_doubles;
     int max_f, max_s, max_solves;
 };
+
+// fronts up to this size are solved by one warp (forward and backward)
+constexpr int kWarpFront = 96;
 
 __device__ __forceinline__ double warp_sum64(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -664,94 +670,190 @@ __device__ bool mf_factor(const BatchDev &d, const DirectDev &m, int nb, int ne,
     return true;
 }
 
-// w <- A^{-1} w for one problem (w indexed by the problem's local DoF):
-// forward L y = w in post-order, backward L^T x = y in reverse order; the
-// dense triangles are solved in 32-row blocks (block rows by all warps, the
-// diagonal block by warp 0 from a shared-memory tile).
-__device__ void mf_solve(const DirectDev &m, int nb, int ne, double *w, const double *L, double *ys, double *xs,
-                         double *tile) {
+// Level-scheduled solve w <- A^{-1} w.  Forward (leaves up): every node
+// forms its front vector from its own entries of w and its children's update
+// vectors (extend-add, children in tree order), eliminates its s pivots
+// (y into w), and leaves the remaining f - s entries as its own update
+// vector; backward (root down): every node solves its pivots from its
+// ancestors' values already in w.  Nodes of one level are independent, so
+// fronts of at most kWarpFront rows go one per warp in parallel and the
+// larger ones through the whole block; one block barrier per level.  Fixed
+// order everywhere, no atomics: bit-reproducible.
+__device__ void mf_fwd_warp(const DirectDev &m, const DNode &nd, double *w, const double *L, double *uv, double *v,
+                            int lane) {
+    const int f = nd.f, s = nd.s;
+    const int32_t *fr = m.front + nd.front_off;
+    const double *Lt = L + nd.L_off;
+    for (int k = lane; k < f; k += 32) v[k] = k < s ? w[fr[k]] : 0.0;
+    __syncwarp();
+    for (int q = 0; q < nd.nchild; q++) {
+        const DNode cn = m.node[m.child[nd.child_off + q]];
+        const int sc = cn.f - cn.s;
+        const int32_t *ex = m.ext + cn.ext_off;
+        const double *uc = uv + cn.uv_off;
+        for (int a = lane; a < sc; a += 32) v[ex[a]] += uc[a];
+        __syncwarp();
+    }
+    for (int k = 0; k < s; k++) {
+        const double yk = v[k] / Lt[(long long)k * s + k];
+        for (int j = k + 1 + lane; j < f; j += 32) v[j] -= Lt[(long long)j * s + k] * yk;
+        __syncwarp();
+        if (lane == 0) v[k] = yk;
+        __syncwarp();
+    }
+    for (int k = lane; k < s; k += 32) w[fr[k]] = v[k];
+    double *uo = uv + nd.uv_off;
+    for (int j = lane; j < f - s; j += 32) uo[j] = v[s + j];
+    __syncwarp();
+}
+
+__device__ void mf_bwd_warp(const DirectDev &m, const DNode &nd, double *w, const double *L, double *v, int lane) {
+    const int f = nd.f, s = nd.s, sc = f - s;
+    const int32_t *fr = m.front + nd.front_off;
+    const double *Lt = L + nd.L_off;
+    double *xs = v + s;
+    for (int i = lane; i < sc; i += 32) xs[i] = w[fr[s + i]];
+    __syncwarp();
+    for (int k = lane; k < s; k += 32) {
+        double acc = w[fr[k]];
+        for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
+        v[k] = acc;
+    }
+    __syncwarp();
+    for (int k = s - 1; k >= 0; k--) {
+        const double xk = v[k] / Lt[(long long)k * s + k];
+        for (int j = lane; j < k; j += 32) v[j] -= Lt[(long long)k * s + j] * xk;
+        __syncwarp();
+        if (lane == 0) v[k] = xk;
+        __syncwarp();
+    }
+    for (int k = lane; k < s; k += 32) w[fr[k]] = v[k];
+    __syncwarp();
+}
+
+// one large front by the whole block (fv: shared front vector, max_f)
+__device__ void mf_fwd_block(const DirectDev &m, const DNode &nd, double *w, const double *L, double *uv, double *fv,
+                             double *tile) {
     const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
-    for (int t = nb; t < ne; t++) {
-        const DNode nd = m.node[t];
-        const int f = nd.f, s = nd.s;
-        const int32_t *fr = m.front + nd.front_off;
-        const double *Lt = L + nd.L_off;
-        for (int k = tid; k < s; k += bs) ys[k] = w[fr[k]];
+    const int f = nd.f, s = nd.s;
+    const int32_t *fr = m.front + nd.front_off;
+    const double *Lt = L + nd.L_off;
+    for (int k = tid; k < f; k += bs) fv[k] = k < s ? w[fr[k]] : 0.0;
+    __syncthreads();
+    for (int q = 0; q < nd.nchild; q++) {
+        const DNode cn = m.node[m.child[nd.child_off + q]];
+        const int sc = cn.f - cn.s;
+        const int32_t *ex = m.ext + cn.ext_off;
+        const double *uc = uv + cn.uv_off;
+        for (int a = tid; a < sc; a += bs) fv[ex[a]] += uc[a];
         __syncthreads();
-        for (int kb = 0; kb < s; kb += 32) {
-            const int nbk = min(32, s - kb);
-            if (kb > 0)
-                for (int r = warp; r < nbk; r += nw) {
-                    const double *Li = Lt + (long long)(kb + r) * s;
-                    double acc = 0.0;
-                    for (int j = lane; j < kb; j += 32) acc += Li[j] * ys[j];
-                    acc = warp_sum64(acc);
-                    if (lane == 0) ys[kb + r] -= acc;
-                }
-            for (int q = tid; q < nbk * nbk; q += bs) {
-                const int r = q / nbk, c = q - r * nbk;
-                tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : 0.0;
+    }
+    for (int kb = 0; kb < s; kb += 32) {
+        const int nbk = min(32, s - kb);
+        if (kb > 0)
+            for (int r = warp; r < nbk; r += nw) {
+                const double *Li = Lt + (long long)(kb + r) * s;
+                double acc = 0.0;
+                for (int j = lane; j < kb; j += 32) acc += Li[j] * fv[j];
+                acc = warp_sum64(acc);
+                if (lane == 0) fv[kb + r] -= acc;
             }
-            __syncthreads();
-            if (warp == 0) {
-                double v = lane < nbk ? ys[kb + lane] : 0.0;
-                for (int c = 0; c < nbk; c++) {
-                    const double yc = __shfl_sync(0xffffffffu, v, c) / tile[c * 33 + c];
-                    if (lane == c) v = yc;
-                    else if (lane > c && lane < nbk) v -= tile[lane * 33 + c] * yc;
-                }
-                if (lane < nbk) ys[kb + lane] = v;
-            }
-            __syncthreads();
+        for (int q = tid; q < nbk * nbk; q += bs) {
+            const int r = q / nbk, c = q - r * nbk;
+            tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : 0.0;
         }
-        for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
-        for (int i = s + warp; i < f; i += nw) {
-            const double *Li = Lt + (long long)i * s;
-            double acc = 0.0;
-            for (int k = lane; k < s; k += 32) acc += Li[k] * ys[k];
-            acc = warp_sum64(acc);
-            if (lane == 0) w[fr[i]] -= acc;
+        __syncthreads();
+        if (warp == 0) {
+            double vv = lane < nbk ? fv[kb + lane] : 0.0;
+            for (int c = 0; c < nbk; c++) {
+                const double yc = __shfl_sync(0xffffffffu, vv, c) / tile[c * 33 + c];
+                if (lane == c) vv = yc;
+                else if (lane > c && lane < nbk) vv -= tile[lane * 33 + c] * yc;
+            }
+            if (lane < nbk) fv[kb + lane] = vv;
         }
         __syncthreads();
     }
-    for (int t = ne - 1; t >= nb; t--) {
-        const DNode nd = m.node[t];
-        const int f = nd.f, s = nd.s, sc = f - s;
-        const int32_t *fr = m.front + nd.front_off;
-        const double *Lt = L + nd.L_off;
-        for (int i = tid; i < sc; i += bs) xs[i] = w[fr[s + i]];
-        __syncthreads();
-        for (int k = tid; k < s; k += bs) {
-            double acc = w[fr[k]];
-            for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
-            ys[k] = acc;
+    for (int k = tid; k < s; k += bs) w[fr[k]] = fv[k];
+    double *uo = uv + nd.uv_off;
+    for (int i = s + warp; i < f; i += nw) {
+        const double *Li = Lt + (long long)i * s;
+        double acc = 0.0;
+        for (int k = lane; k < s; k += 32) acc += Li[k] * fv[k];
+        acc = warp_sum64(acc);
+        if (lane == 0) uo[i - s] = fv[i] - acc;
+    }
+    __syncthreads();
+}
+
+__device__ void mf_bwd_block(const DirectDev &m, const DNode &nd, double *w, const double *L, double *ys, double *xs,
+                             double *tile) {
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int f = nd.f, s = nd.s, sc = f - s;
+    const int32_t *fr = m.front + nd.front_off;
+    const double *Lt = L + nd.L_off;
+    for (int i = tid; i < sc; i += bs) xs[i] = w[fr[s + i]];
+    __syncthreads();
+    for (int k = tid; k < s; k += bs) {
+        double acc = w[fr[k]];
+        for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
+        ys[k] = acc;
+    }
+    __syncthreads();
+    for (int kb = ((s + 31) / 32 - 1) * 32; kb >= 0; kb -= 32) {
+        const int nbk = min(32, s - kb);
+        for (int q = tid; q < nbk * nbk; q += bs) {
+            const int r = q / nbk, c = q - r * nbk;
+            tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : 0.0;
         }
         __syncthreads();
-        for (int kb = ((s + 31) / 32 - 1) * 32; kb >= 0; kb -= 32) {
-            const int nbk = min(32, s - kb);
-            for (int q = tid; q < nbk * nbk; q += bs) {
-                const int r = q / nbk, c = q - r * nbk;
-                tile[r * 33 + c] = c <= r ? Lt[(long long)(kb + r) * s + kb + c] : 0.0;
+        if (warp == 0) {
+            double vv = lane < nbk ? ys[kb + lane] : 0.0;
+            for (int c = nbk - 1; c >= 0; c--) {
+                const double xc = __shfl_sync(0xffffffffu, vv, c) / tile[c * 33 + c];
+                if (lane == c) vv = xc;
+                else if (lane < c) vv -= tile[c * 33 + lane] * xc;
             }
-            __syncthreads();
-            if (warp == 0) {
-                double v = lane < nbk ? ys[kb + lane] : 0.0;
-                for (int c = nbk - 1; c >= 0; c--) {
-                    const double xc = __shfl_sync(0xffffffffu, v, c) / tile[c * 33 + c];
-                    if (lane == c) v = xc;
-                    else if (lane < c) v -= tile[c * 33 + lane] * xc;
-                }
-                if (lane < nbk) ys[kb + lane] = v;
-            }
-            __syncthreads();
-            for (int k = tid; k < kb; k += bs) {
-                double acc = 0.0;
-                for (int r = 0; r < nbk; r++) acc += Lt[(long long)(kb + r) * s + k] * ys[kb + r];
-                ys[k] -= acc;
-            }
-            __syncthreads();
+            if (lane < nbk) ys[kb + lane] = vv;
         }
-        for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+        __syncthreads();
+        for (int k = tid; k < kb; k += bs) {
+            double acc = 0.0;
+            for (int r = 0; r < nbk; r++) acc += Lt[(long long)(kb + r) * s + k] * ys[kb + r];
+            ys[k] -= acc;
+        }
+        __syncthreads();
+    }
+    for (int k = tid; k < s; k += bs) w[fr[k]] = ys[k];
+    __syncthreads();
+}
+
+__device__ void mf_solve_lv(const DirectDev &m, int lv0, int nlev, double *w, const double *L, double *uv,
+                            double *fv, double *ys, double *xs, double *tile, double *wbuf) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    double *v = wbuf + warp * kWarpFront;
+    for (int l = 0; l < nlev; l++) {
+        const int a = m.lvl_ptr[lv0 + l], b = m.lvl_ptr[lv0 + l + 1];
+        for (int i = a + warp; i < b; i += nw) {
+            const DNode nd = m.node[m.lvl_nodes[i]];
+            if (nd.f <= kWarpFront) mf_fwd_warp(m, nd, w, L, uv, v, lane);
+        }
+        __syncthreads();
+        for (int i = a; i < b; i++) {
+            const DNode nd = m.node[m.lvl_nodes[i]];
+            if (nd.f > kWarpFront) mf_fwd_block(m, nd, w, L, uv, fv, tile);
+        }
+    }
+    for (int l = nlev - 1; l >= 0; l--) {
+        const int a = m.lvl_ptr[lv0 + l], b = m.lvl_ptr[lv0 + l + 1];
+        for (int i = a; i < b; i++) {
+            const DNode nd = m.node[m.lvl_nodes[i]];
+            if (nd.f > kWarpFront) mf_bwd_block(m, nd, w, L, ys, xs, tile);
+        }
+        for (int i = a + warp; i < b; i += nw) {
+            const DNode nd = m.node[m.lvl_nodes[i]];
+            if (nd.f <= kWarpFront) mf_bwd_warp(m, nd, w, L, v, lane);
+        }
         __syncthreads();
     }
 }
@@ -761,12 +863,13 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
     extern __shared__ double dsm[];
     __shared__ double sh[32 * 4];
     __shared__ int slot;
-    double *colk = dsm;                 // factor: column k of the front; solve: structure values
+    double *colk = dsm;                 // factor: column k of the front; solve: a large front's vector
     double *ys = dsm + m.max_f;
     double *tile = ys + m.max_s;
-    double *P = tile + 32 * 33;         // factor: the current panel's rows below it
+    double *P = tile + 32 * 33;         // factor: the current panel's rows below it; solve: structure values
+    double *wbuf = P + (long long)m.max_f * kPanelStride;   // solve: one small front per warp
     double *F = m.work + (long long)blockIdx.x * m.slot_doubles;
-    double *U = F + m.F_doubles, *L = U + m.U_doubles;
+    double *U = F + m.F_doubles, *L = U + m.U_doubles, *uvw = L + m.L_doubles;
     const int tid = threadIdx.x, bs = blockDim.x;
     while (true) {
         if (tid == 0) slot = atomicAdd(d.queue, 1);
@@ -821,7 +924,7 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
                     }
                     if (ref >= m.max_solves) break;
                     prev = rel;
-                    mf_solve(m, nb, ne, d.r64 + r0, L, ys, colk, tile);
+                    mf_solve_lv(m, m.prob_lvl0[pid], m.prob_nlev[pid], d.r64 + r0, L, uvw, colk, ys, P, tile, wbuf);
                     for (int i = r0 + tid; i < r1; i += bs) d.u[i] += d.r64[i];
                     __syncthreads();
                     nsolve++;
@@ -914,7 +1017,8 @@ struct DirectCache {
     const DNode *node = nullptr;
     const int32_t *front = nullptr, *child = nullptr, *ent_rel = nullptr, *ent_pos = nullptr, *ext = nullptr;
     const int32_t *prob_node0 = nullptr, *prob_nnodes = nullptr;
-    long long max_U = 0, max_L = 0;
+    const int32_t *lvl_ptr = nullptr, *lvl_nodes = nullptr, *prob_lvl0 = nullptr, *prob_nlev = nullptr;
+    long long max_U = 0, max_L = 0, max_uv = 0;
     int max_f = 0, max_s = 0, groups = 0;
 };
 
@@ -1043,11 +1147,18 @@ int build_direct_cache(grmp_matrix A, int np, const int32_t *row_off, const int3
     C->groups = ng;
     std::vector<DNode> node;
     std::vector<int32_t> front, child, ent_rel, ent_pos, ext, gnode0(ng), pn0(np), pnn(np);
+    std::vector<int32_t> lvl_ptr, lvl_nodes, glvl0(ng), gnlev(ng), pl0(np), pnl(np);
     for (int g = 0; g < ng; g++) {
         const NdSymbolic &Sg = S[g];
         const int nbase = (int)node.size(), fbase = (int)front.size(), cbase = (int)child.size();
         const int ebase = (int)ent_rel.size(), xbase = (int)ext.size();
         gnode0[g] = nbase;
+        const int lbase = (int)lvl_nodes.size();
+        glvl0[g] = (int)lvl_ptr.size();
+        gnlev[g] = (int)Sg.level_ptr.size() - 1;
+        for (int32_t lp : Sg.level_ptr) lvl_ptr.push_back(lbase + lp);
+        for (int32_t t : Sg.level_nodes) lvl_nodes.push_back(t + nbase);
+        C->max_uv = std::max<long long>(C->max_uv, Sg.uv_size);
         for (const NdNode &q : Sg.node) {
             DNode dn;
             dn.s = q.s;
@@ -1060,6 +1171,7 @@ int build_direct_cache(grmp_matrix A, int np, const int32_t *row_off, const int3
             dn.ext_off = q.ext_off + xbase;
             dn.L_off = q.L_off;
             dn.U_off = q.U_off;
+            dn.uv_off = Sg.uv_off[&q - Sg.node.data()];
             node.push_back(dn);
         }
         front.insert(front.end(), Sg.front.begin(), Sg.front.end());
@@ -1075,6 +1187,8 @@ int build_direct_cache(grmp_matrix A, int np, const int32_t *row_off, const int3
     for (int k = 0; k < np; k++) {
         pn0[k] = gnode0[group_of[k]];
         pnn[k] = S[group_of[k]].nnodes;
+        pl0[k] = glvl0[group_of[k]];
+        pnl[k] = gnlev[group_of[k]];
     }
     A->direct = C;
     rc = upload_vec(ctx, *C, node, &C->node);
@@ -1085,6 +1199,10 @@ int build_direct_cache(grmp_matrix A, int np, const int32_t *row_off, const int3
     if (!rc) rc = upload_vec(ctx, *C, ext, &C->ext);
     if (!rc) rc = upload_vec(ctx, *C, pn0, &C->prob_node0);
     if (!rc) rc = upload_vec(ctx, *C, pnn, &C->prob_nnodes);
+    if (!rc) rc = upload_vec(ctx, *C, lvl_ptr, &C->lvl_ptr);
+    if (!rc) rc = upload_vec(ctx, *C, lvl_nodes, &C->lvl_nodes);
+    if (!rc) rc = upload_vec(ctx, *C, pl0, &C->prob_lvl0);
+    if (!rc) rc = upload_vec(ctx, *C, pnl, &C->prob_nlev);
     if (!rc) {
         e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "direct cache upload");
@@ -1263,14 +1381,20 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
             m.ext = C.ext;
             m.prob_node0 = C.prob_node0;
             m.prob_nnodes = C.prob_nnodes;
+            m.lvl_ptr = C.lvl_ptr;
+            m.lvl_nodes = C.lvl_nodes;
+            m.prob_lvl0 = C.prob_lvl0;
+            m.prob_nlev = C.prob_nlev;
             m.F_doubles = (long long)C.max_f * C.max_f;
             m.U_doubles = C.max_U;
-            m.slot_doubles = m.F_doubles + m.U_doubles + C.max_L;
+            m.L_doubles = C.max_L;
+            m.slot_doubles = m.F_doubles + m.U_doubles + C.max_L + std::max<long long>(1, C.max_uv);
             m.max_f = C.max_f;
             m.max_s = C.max_s;
             m.max_solves = 4;
         }
-        const size_t smem = ((size_t)m.max_f + m.max_s + 32 * 33 + (size_t)m.max_f * kPanelStride) * 8;
+        const size_t smem =
+            ((size_t)m.max_f + m.max_s + 32 * 33 + (size_t)m.max_f * kPanelStride + 16 * (size_t)kWarpFront) * 8;
         auto kern = tpr == 4 ? k_stokes_direct<4> : (tpr == 8 ? k_stokes_direct<8> : k_stokes_direct<16>);
         if (!rc && smem > 220 * 1024)
             rc = grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batch direct: front of %d DoFs too large", m.max_f);
