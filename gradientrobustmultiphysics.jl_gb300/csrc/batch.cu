@@ -614,10 +614,15 @@ struct DirectDev {
     // level schedule of each problem's tree: levels lvl_ptr[prob_lvl0 + l ..
     // + l + 1) index lvl_nodes (node ids, children always in lower levels)
     const int32_t *lvl_ptr, *lvl_nodes, *prob_lvl0, *prob_nlev;
-    double *work;                                   // per resident block: [F | U | L | uv]
-    long long slot_doubles, F_doubles, U_doubles, L_doubles;
+    double *work;                                   // per resident block: [F | U | L | uv | group fronts]
+    long long slot_doubles, F_doubles, U_doubles, L_doubles, uv_doubles;
     int max_f, max_s, max_solves;
+    int fact_groups;                                // thread groups factoring small fronts concurrently
 };
+
+// fronts up to this size are factored by a group of warps (several groups
+// per block work on one tree level at the same time)
+constexpr int kGroupFront = 96;
 
 // fronts up to this size are solved by one warp (forward and backward)
 constexpr int kWarpFront = 96;
@@ -627,45 +632,76 @@ __device__ __forceinline__ double warp_sum64(double v) {
     return v;
 }
 
-// Numeric factorisation of one problem: for every node in post-order,
-// assemble the front (original entries + children's update matrices),
-// eliminate its own DoFs (right-looking dense Cholesky), keep the factor
-// columns and the update matrix.  Returns false on a non-positive pivot.
-__device__ bool mf_factor(const BatchDev &d, const DirectDev &m, int nb, int ne, long long nnz0, double *F, double *U,
-                          double *L, double *colk, double *P) {
-    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
-    for (int t = nb; t < ne; t++) {
-        const DNode nd = m.node[t];
-        const int f = nd.f, s = nd.s;
-        for (long long q = tid; q < (long long)f * f; q += bs) F[q] = 0.0;
-        __syncthreads();
-        for (int e = tid; e < nd.nentry; e += bs)
-            F[m.ent_pos[nd.entry_off + e]] = d.v64[nnz0 + m.ent_rel[nd.entry_off + e]];
-        __syncthreads();
-        for (int q = 0; q < nd.nchild; q++) {
-            const DNode cn = m.node[m.child[nd.child_off + q]];
-            const int sc = cn.f - cn.s;
-            const double *Uc = U + cn.U_off;
-            const int32_t *ex = m.ext + cn.ext_off;
-            for (int a = warp; a < sc; a += nw) {
-                const long long pa = (long long)ex[a] * f;
-                for (int b = lane; b <= a; b += 32) F[pa + ex[b]] += Uc[(long long)a * sc + b];
+// Numeric factorisation of one node by thread group g: assemble the front
+// F (original entries + the children's update matrices), eliminate its own
+// DoFs (blocked right-looking dense Cholesky), keep the factor columns and
+// the update matrix.  Returns false on a non-positive pivot.  Every entry's
+// arithmetic is independent of the group's size.
+__device__ bool mf_factor_node(const BatchDev &d, const DirectDev &m, const DNode &nd, long long nnz0, double *F,
+                               double *U, double *L, double *colk, double *P, ThreadGroup g) {
+    const int lane = threadIdx.x & 31, gw = g.tid >> 5, gnw = g.size >> 5;
+    const int f = nd.f, s = nd.s;
+    for (long long q = g.tid; q < (long long)f * f; q += g.size) F[q] = 0.0;
+    g.sync();
+    for (int e = g.tid; e < nd.nentry; e += g.size)
+        F[m.ent_pos[nd.entry_off + e]] = d.v64[nnz0 + m.ent_rel[nd.entry_off + e]];
+    g.sync();
+    for (int q = 0; q < nd.nchild; q++) {
+        const DNode cn = m.node[m.child[nd.child_off + q]];
+        const int sc = cn.f - cn.s;
+        const double *Uc = U + cn.U_off;
+        const int32_t *ex = m.ext + cn.ext_off;
+        for (int a = gw; a < sc; a += gnw) {
+            const long long pa = (long long)ex[a] * f;
+            for (int b = lane; b <= a; b += 32) F[pa + ex[b]] += Uc[(long long)a * sc + b];
+        }
+        g.sync();
+    }
+    if (!front_cholesky<double>(F, f, s, colk, P, kPanelStride, g)) return false;
+    double *Lt = L + nd.L_off;
+    for (long long q = g.tid; q < (long long)f * s; q += g.size) {
+        const int i = (int)(q / s), j = (int)(q - (long long)i * s);
+        Lt[q] = j <= i ? F[(long long)i * f + j] : 0.0;
+    }
+    const int sc = f - s;
+    double *Ut = U + nd.U_off;
+    for (long long q = g.tid; q < (long long)sc * sc; q += g.size) {
+        const int a = (int)(q / sc), b = (int)(q - (long long)a * sc);
+        if (b <= a) Ut[q] = F[(long long)(s + a) * f + s + b];
+    }
+    g.sync();
+    return true;
+}
+
+// Numeric factorisation of one problem, level by level from the leaves:
+// fronts of at most kGroupFront rows by m.fact_groups groups of warps in
+// parallel (each with its own front scratch Fg, pivot column and panel
+// shares of colk and P), larger fronts by the whole block one after another.
+__device__ bool mf_factor_lv(const BatchDev &d, const DirectDev &m, int lv0, int nlev, long long nnz0, double *F,
+                             double *U, double *L, double *colk, double *P, double *Fg, int *fail) {
+    const int ng = m.fact_groups;
+    const int gsize = blockDim.x / ng, gid = threadIdx.x / gsize;
+    const ThreadGroup grp{(int)threadIdx.x - gid * gsize, gsize, 1 + gid};
+    double *gF = Fg + (long long)gid * kGroupFront * kGroupFront;
+    double *gcolk = colk + gid * kGroupFront;
+    double *gP = P + (long long)gid * kGroupFront * kPanelStride;
+    if (threadIdx.x == 0) *fail = 0;
+    __syncthreads();
+    for (int l = 0; l < nlev; l++) {
+        const int a = m.lvl_ptr[lv0 + l], b = m.lvl_ptr[lv0 + l + 1];
+        if (ng > 1)
+            for (int i = a + gid; i < b; i += ng) {
+                const DNode nd = m.node[m.lvl_nodes[i]];
+                if (nd.f <= kGroupFront && !mf_factor_node(d, m, nd, nnz0, gF, U, L, gcolk, gP, grp) && grp.tid == 0)
+                    atomicOr(fail, 1);
             }
-            __syncthreads();
-        }
-        if (!front_cholesky<double>(F, f, s, colk, P, kPanelStride)) return false;
-        double *Lt = L + nd.L_off;
-        for (long long q = tid; q < (long long)f * s; q += bs) {
-            const int i = (int)(q / s), j = (int)(q - (long long)i * s);
-            Lt[q] = j <= i ? F[(long long)i * f + j] : 0.0;
-        }
-        const int sc = f - s;
-        double *Ut = U + nd.U_off;
-        for (long long q = tid; q < (long long)sc * sc; q += bs) {
-            const int a = (int)(q / sc), b = (int)(q - (long long)a * sc);
-            if (b <= a) Ut[q] = F[(long long)(s + a) * f + s + b];
-        }
         __syncthreads();
+        if (*(volatile int *)fail) return false;
+        for (int i = a; i < b; i++) {
+            const DNode nd = m.node[m.lvl_nodes[i]];
+            if ((ng == 1 || nd.f > kGroupFront) && !mf_factor_node(d, m, nd, nnz0, F, U, L, colk, P, whole_block()))
+                return false;
+        }
     }
     return true;
 }
@@ -869,7 +905,8 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
     double *P = tile + 32 * 33;         // factor: the current panel's rows below it; solve: structure values
     double *wbuf = P + (long long)m.max_f * kPanelStride;   // solve: one small front per warp
     double *F = m.work + (long long)blockIdx.x * m.slot_doubles;
-    double *U = F + m.F_doubles, *L = U + m.U_doubles, *uvw = L + m.L_doubles;
+    double *U = F + m.F_doubles, *L = U + m.U_doubles, *uvw = L + m.L_doubles, *Fg = uvw + m.uv_doubles;
+    __shared__ int fail_flag;
     const int tid = threadIdx.x, bs = blockDim.x;
     while (true) {
         if (tid == 0) slot = atomicAdd(d.queue, 1);
@@ -880,11 +917,11 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
         const int pid = d.order[k];
         const int r0 = d.row_off[pid], r1 = d.row_off[pid + 1];
         const int c0 = d.cell_off[pid], c1 = d.cell_off[pid + 1];
-        const int nb = m.prob_node0[pid], ne = nb + m.prob_nnodes[pid];
         for (int i = r0 + tid; i < r1; i += bs) d.u[i] = 0.0;
         for (int c = c0 + tid; c < c1; c += bs) d.p[c] = 0.0;
         __syncthreads();
-        const bool fact_ok = mf_factor(d, m, nb, ne, (long long)d.rowptr[r0], F, U, L, colk, P);
+        const bool fact_ok = mf_factor_lv(d, m, m.prob_lvl0[pid], m.prob_nlev[pid], (long long)d.rowptr[r0], F, U, L,
+                                          colk, P, Fg, &fail_flag);
         __syncthreads();
         // ||A||_inf of the problem (for the normwise backward error of a solve)
         double an[1] = {0.0};
@@ -1388,7 +1425,12 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
             m.F_doubles = (long long)C.max_f * C.max_f;
             m.U_doubles = C.max_U;
             m.L_doubles = C.max_L;
-            m.slot_doubles = m.F_doubles + m.U_doubles + C.max_L + std::max<long long>(1, C.max_uv);
+            m.uv_doubles = std::max<long long>(1, C.max_uv);
+            // groups of 128 threads factoring small fronts concurrently, as many as
+            // the pivot-column and panel buffers (sized for the largest front) hold
+            m.fact_groups = std::max(1, std::min(4, C.max_f / kGroupFront));
+            m.slot_doubles = m.F_doubles + m.U_doubles + C.max_L + m.uv_doubles +
+                             (m.fact_groups > 1 ? (long long)m.fact_groups * kGroupFront * kGroupFront : 0);
             m.max_f = C.max_f;
             m.max_s = C.max_s;
             m.max_solves = 4;

@@ -6,18 +6,31 @@
 constexpr int kPanel = 16;
 constexpr int kPanelStride = kPanel + 1;   // panel row stride (spreads shared-memory banks)
 
+// The threads that run one dense front operation: the whole block
+// (barrier 0 = __syncthreads) or a contiguous range of warps synchronised by
+// the named barrier `bar` (1..15).
+struct ThreadGroup {
+    int tid, size, bar;
+    __device__ __forceinline__ void sync() const {
+        if (bar == 0) __syncthreads();
+        else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(size) : "memory");
+    }
+};
+__device__ __forceinline__ ThreadGroup whole_block() { return ThreadGroup{(int)threadIdx.x, (int)blockDim.x, 0}; }
+
 // Partial Cholesky of a front F (f x f, lower part, row-major): eliminate
 // its first s columns.  Blocked right-looking: a panel of kPanel columns
 // (all rows from the panel's diagonal down) is copied to shared memory P and
 // factored there column by column, written back, and the trailing lower
 // triangle receives one rank-kPanel update per panel from 4x4 register
 // tiles reading the panel from P, so F is read and written once per panel
-// instead of once per column.  Returns false on a non-positive pivot.
+// instead of once per column.  Returns false on a non-positive pivot.  The
+// arithmetic of every entry is independent of the thread group's size.
 // P holds (f - k0) x kPanel values with row stride ps (shared or global memory).
 
 template <typename T>
-__device__ bool front_cholesky(T *F, int f, int s, T *colk, T *P, int ps) {
-    const int tid = threadIdx.x, bs = blockDim.x;
+__device__ bool front_cholesky(T *F, int f, int s, T *colk, T *P, int ps, ThreadGroup g = whole_block()) {
+    const int tid = g.tid, bs = g.size;
     for (int k0 = 0; k0 < s; k0 += kPanel) {
         const int kw = min(kPanel, s - k0), k1 = k0 + kw, mp = f - k0;
         // panel: rows k0..f-1, columns k0..k1-1, factored in shared memory
@@ -25,7 +38,7 @@ __device__ bool front_cholesky(T *F, int f, int s, T *colk, T *P, int ps) {
             const int i = q / kw, t = q - i * kw;
             P[i * ps + t] = F[(long long)(k0 + i) * f + k0 + t];
         }
-        __syncthreads();
+        g.sync();
         for (int c = 0; c < kw; c++) {
             const T dcc = P[c * ps + c];
             if (!(dcc > T(0)) || !isfinite((double)dcc)) return false;   // uniform: same value in every thread
@@ -35,14 +48,14 @@ __device__ bool front_cholesky(T *F, int f, int s, T *colk, T *P, int ps) {
                 P[i * ps + c] = v;
                 colk[i] = v;
             }
-            __syncthreads();
+            g.sync();
             if (tid == 0) P[c * ps + c] = dk;
             for (int i = c + 1 + tid; i < mp; i += bs) {
                 const T lic = colk[i];
                 const int jmax = min(i, kw - 1);
                 for (int j = c + 1; j <= jmax; j++) P[i * ps + j] -= lic * colk[j];
             }
-            __syncthreads();
+            g.sync();
         }
         for (int q = tid; q < mp * kw; q += bs) {
             const int i = q / kw, t = q - i * kw;
@@ -88,7 +101,7 @@ __device__ bool front_cholesky(T *F, int f, int s, T *colk, T *P, int ps) {
                 }
             }
         }
-        __syncthreads();
+        g.sync();
     }
     return true;
 }
