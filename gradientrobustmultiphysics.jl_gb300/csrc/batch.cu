@@ -730,12 +730,35 @@ __device__ void mf_fwd_warp(const DirectDev &m, const DNode &nd, double *w, cons
         for (int a = lane; a < sc; a += 32) v[ex[a]] += uc[a];
         __syncwarp();
     }
+    // column-oriented elimination; the next column of L (rows below its
+    // diagonal, up to three per lane) and its diagonal entry are loaded
+    // while the current column is applied
+    double lc[3], ln[3], dk = s > 0 ? Lt[0] : 1.0, dn = 1.0;
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+        const int j = 1 + lane + 32 * t;
+        lc[t] = (s > 0 && j < f) ? Lt[(long long)j * s] : 0.0;
+    }
     for (int k = 0; k < s; k++) {
-        const double yk = v[k] / Lt[(long long)k * s + k];
-        for (int j = k + 1 + lane; j < f; j += 32) v[j] -= Lt[(long long)j * s + k] * yk;
+        const bool more = k + 1 < s;
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+            const int j = k + 2 + lane + 32 * t;
+            ln[t] = (more && j < f) ? Lt[(long long)j * s + k + 1] : 0.0;
+        }
+        if (more) dn = Lt[(long long)(k + 1) * s + k + 1];
+        const double yk = v[k] / dk;
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+            const int j = k + 1 + lane + 32 * t;
+            if (j < f) v[j] -= lc[t] * yk;
+        }
         __syncwarp();
         if (lane == 0) v[k] = yk;
         __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 3; t++) lc[t] = ln[t];
+        dk = dn;
     }
     for (int k = lane; k < s; k += 32) w[fr[k]] = v[k];
     double *uo = uv + nd.uv_off;
@@ -756,12 +779,34 @@ __device__ void mf_bwd_warp(const DirectDev &m, const DNode &nd, double *w, cons
         v[k] = acc;
     }
     __syncwarp();
+    // row k of L11 (entries left of its diagonal, up to three per lane since
+    // s <= kWarpFront) and the next diagonal are loaded one step ahead
+    double rc[3], rn[3], dk = s > 0 ? Lt[(long long)(s - 1) * s + s - 1] : 1.0, dn = 1.0;
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+        const int j = lane + 32 * t;
+        rc[t] = (s > 0 && j < s - 1) ? Lt[(long long)(s - 1) * s + j] : 0.0;
+    }
     for (int k = s - 1; k >= 0; k--) {
-        const double xk = v[k] / Lt[(long long)k * s + k];
-        for (int j = lane; j < k; j += 32) v[j] -= Lt[(long long)k * s + j] * xk;
+        const bool more = k > 0;
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+            const int j = lane + 32 * t;
+            rn[t] = (more && j < k - 1) ? Lt[(long long)(k - 1) * s + j] : 0.0;
+        }
+        if (more) dn = Lt[(long long)(k - 1) * s + k - 1];
+        const double xk = v[k] / dk;
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+            const int j = lane + 32 * t;
+            if (j < k) v[j] -= rc[t] * xk;
+        }
         __syncwarp();
         if (lane == 0) v[k] = xk;
         __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 3; t++) rc[t] = rn[t];
+        dk = dn;
     }
     for (int k = lane; k < s; k += 32) w[fr[k]] = v[k];
     __syncwarp();
