@@ -291,18 +291,14 @@ def run_ours(args):
     def step(mode: str, host_inputs: bool = False):
         # FP32 element matrices feed the FP32 PCG; the FP32 factorisation reads the FP64 values
         needs32 = mode == "mixed" and not direct
+        # one walk of the incidence lists fills both precisions when both are needed
+        prec = G.FP64_FP32 if needs32 else G.FP64
         if host_inputs:
-            G.assemble(A, prob.operators, G.FP64)
-            if needs32:
-                G.assemble(A, prob.operators, G.FP32)
+            G.assemble(A, prob.operators, prec)
         elif dev_terms is not None:
-            ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP64))
-            if needs32:
-                ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, G.FP32))
+            ctx.check(ctx.lib.grmp_assemble_bilinear(A.h, 1, dev_terms, prec))
         else:   # scalar operator parameters: nothing per cell to upload
-            G.assemble(A, prob.operators, G.FP64)
-            if needs32:
-                G.assemble(A, prob.operators, G.FP32)
+            G.assemble(A, prob.operators, prec)
         b.fill(0.0)
         G.assemble(b, prob.rhs)
         G.apply_dirichlet(A, b, prob.fixed, None, G.DIRICHLET_ELIMINATE)

@@ -16,6 +16,6 @@ from .api import (GB300Context, Operator, CellCoefficient, LaplaceOperator, Reac
                   ReconstructionDivergence, APT_BilinearForm, APT_SymmetricBilinearForm,
                   ItemIntegrator, L2ErrorIntegrator, L2NormIntegrator, L2DifferenceIntegrator)
 from .fespace import interpolate  # noqa: F401
-from ._lib import FP64, FP32, DIRICHLET_PENALTY, DIRICHLET_ELIMINATE, GrmpError  # noqa: F401
+from ._lib import FP64, FP32, FP64_FP32, DIRICHLET_PENALTY, DIRICHLET_ELIMINATE, GrmpError  # noqa: F401
 
 __version__ = "0.1.0"

@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "DEVICE", 4: "
                 5: "UNSUPPORTED", 6: "BUDGET", 7: "TIMEOUT", 8: "NAN", 9: "NO_DEVICE"}
 
 OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV = 1, 2, 3, 4
-FP64, FP32 = 0, 1
+FP64, FP32, FP64_FP32 = 0, 1, 2
 RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
 DIRICHLET_PENALTY, DIRICHLET_ELIMINATE = 0, 1
 SOLVE_FP64, SOLVE_MIXED, SOLVE_DIRECT, SOLVE_MIXED_DIRECT = 0, 1, 2, 3

@@ -308,7 +308,7 @@ int grmp_pattern_build(grmp_space space, int nterms, const grmp_bilinear_term *t
 
 int grmp_assemble_bilinear(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision) {
     if (!A || nterms <= 0 || nterms > GRMP_MAX_TERMS || !terms) return GRMP_ERR_INVALID_ARG;
-    if (precision != GRMP_FP64 && precision != GRMP_FP32) return GRMP_ERR_INVALID_ARG;
+    if (precision != GRMP_FP64 && precision != GRMP_FP32 && precision != GRMP_FP64_FP32) return GRMP_ERR_INVALID_ARG;
     cudaSetDevice(A->space->mesh->ctx->device);
     std::lock_guard<std::mutex> lk(A->space->mesh->ctx->mu);
     return grmp_assemble_bilinear_impl(A, nterms, terms, precision);

@@ -162,6 +162,166 @@ __global__ void __launch_bounds__(128) k_assemble_rows(int32_t nrows, const int3
     for (int i = threadIdx.x; i < nv; i += blockDim.x) vals[v0 + i] = acc[i];
 }
 
+// Both precisions in one walk: the FP64 and the FP32 contribution of every
+// (row, cell, DoF) triple, each from its own factors and reference tensors in
+// its own arithmetic, accumulated into two shared-memory row blocks.
+template <int DIM, int NB, int NC, typename S>
+__global__ void __launch_bounds__(128) k_assemble_rows2(int32_t nrows, const int32_t *__restrict__ inc_ptr,
+                                                        const int32_t *__restrict__ inc_cell,
+                                                        const uint8_t *__restrict__ inc_loc,
+                                                        const S *__restrict__ slot, const int32_t *__restrict__ rowptr,
+                                                        const double *__restrict__ fac64, const float *__restrict__ fac32,
+                                                        const double *__restrict__ gtens64,
+                                                        const float *__restrict__ gtens32, FastTerms ft,
+                                                        double *__restrict__ vals64, float *__restrict__ vals32,
+                                                        int max_row_nnz) {
+    constexpr int LD = NB * NC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *tens64 = reinterpret_cast<double *>(smem_raw);
+    double *acc64 = tens64 + ft.tens_total;
+    float *tens32 = reinterpret_cast<float *>(acc64 + (size_t)blockDim.x * max_row_nnz);
+    float *acc32 = tens32 + ((ft.tens_total + 1) & ~1);
+    const int row0 = blockIdx.x * blockDim.x;
+    const int row1 = min(row0 + (int)blockDim.x, nrows);
+    const int v0 = rowptr[row0], nv = rowptr[row1] - v0;
+    for (int i = threadIdx.x; i < ft.tens_total; i += blockDim.x) {
+        tens64[i] = gtens64[i];
+        tens32[i] = gtens32[i];
+    }
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        acc64[i] = 0.0;
+        acc32[i] = 0.f;
+    }
+    __syncthreads();
+    const int row = row0 + threadIdx.x;
+    if (row < row1) {
+        double *rv64 = acc64 + (rowptr[row] - v0);
+        float *rv32 = acc32 + (rowptr[row] - v0);
+        const S DROP = (S)~(S)0;
+        const int pe = inc_ptr[row + 1];
+        for (int p = inc_ptr[row]; p < pe; p++) {
+            const int cell = inc_cell[p];
+            const int A = inc_loc[p];
+            const int c1 = A / NB, a = A - c1 * NB;
+            const double *cf64 = fac64 + (size_t)cell * ft.nf_total;
+            const float *cf32 = fac32 + (size_t)cell * ft.nf_total;
+            const S *sl = slot + (size_t)p * LD;
+            double f64[GRMP_MAX_TERMS * 16];
+            float f32[GRMP_MAX_TERMS * 16];
+            for (int i = 0; i < ft.nf_total && i < GRMP_MAX_TERMS * 16; i++) {
+                f64[i] = cf64[i];
+                f32[i] = cf32[i];
+            }
+#pragma unroll
+            for (int B = 0; B < LD; B++) {
+                const S s = sl[B];
+                if (s == DROP) continue;
+                const int c2 = B / NB, b = B - c2 * NB;
+                double v = 0;
+                float w = 0;
+                for (int ti = 0; ti < ft.n; ti++) {
+                    const FastTerm &t = ft.t[ti];
+                    const int to = t.toff + a * NB + b;
+                    if (t.op == GRMP_OP_HOOKE) {
+                        const int fo = t.foff + (c1 * NC + c2) * DIM * DIM;
+#pragma unroll
+                        for (int q = 0; q < DIM * DIM; q++) {
+                            v += f64[fo + q] * tens64[to + q * NB * NB];
+                            w += f32[fo + q] * tens32[to + q * NB * NB];
+                        }
+                    } else if (c1 == c2) {
+                        for (int q = 0; q < t.ntens; q++) {
+                            v += f64[t.foff + q] * tens64[to + q * NB * NB];
+                            w += f32[t.foff + q] * tens32[to + q * NB * NB];
+                        }
+                    }
+                }
+                rv64[s] += v;
+                rv32[s] += w;
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        vals64[v0 + i] = acc64[i];
+        vals32[v0 + i] = acc32[i];
+    }
+}
+
+template <int DIM, int NB, int NC>
+int run_assembly_dual(grmp_matrix A, const FastTerms &ft, const std::vector<double> &tens64) {
+    grmp_space s = A->space;
+    grmp_mesh m = s->mesh;
+    grmp_context ctx = m->ctx;
+    std::vector<float> tens32(tens64.begin(), tens64.end());
+    double *dt64 = nullptr;
+    float *dt32 = nullptr;
+    int rc = grmp_upload(ctx, &dt64, tens64.data(), tens64.size());
+    if (!rc) rc = grmp_upload(ctx, &dt32, tens32.data(), tens32.size());
+    auto release = [&]() {
+        grmp_free(ctx, dt64, tens64.size() * 8);
+        grmp_free(ctx, dt32, tens32.size() * 4);
+    };
+    if (rc) {
+        release();
+        return rc;
+    }
+    const size_t f64b = (size_t)m->ncells * ft.nf_total * 8, f32b = (size_t)m->ncells * ft.nf_total * 4;
+    const size_t fbytes = f64b + ((f32b + 255) & ~(size_t)255);
+    if (A->cellfac_bytes < fbytes) {
+        grmp_free(ctx, A->d_cellfac, A->cellfac_bytes);
+        A->cellfac_bytes = 0;
+        rc = grmp_alloc(ctx, &A->d_cellfac, fbytes);
+        if (rc) {
+            release();
+            return rc;
+        }
+        A->cellfac_bytes = fbytes;
+    }
+    double *fac64 = (double *)A->d_cellfac;
+    float *fac32 = (float *)((char *)A->d_cellfac + ((f64b + 255) & ~(size_t)255));
+    k_cell_factors<DIM, NC, double><<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, m->d_coords, m->d_cells, ft,
+                                                                              fac64);
+    GRMP_LAUNCHED(ctx);
+    k_cell_factors<DIM, NC, float><<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, m->d_coords, m->d_cells, ft,
+                                                                             fac32);
+    GRMP_LAUNCHED(ctx);
+    if (!A->d_vals64) rc = grmp_alloc(ctx, (void **)&A->d_vals64, (size_t)A->nnz * 8);
+    if (!rc && !A->d_vals32) rc = grmp_alloc(ctx, (void **)&A->d_vals32, (size_t)A->nnz * 4);
+    if (rc) {
+        release();
+        return rc;
+    }
+    const size_t tens_b = tens64.size() * 8 + ((tens32.size() + 1) & ~(size_t)1) * 4;
+    int tpb = 128;
+    while (tpb > 32 && tens_b + (size_t)tpb * A->max_row_nnz * 12 > 100 * 1024) tpb /= 2;
+    const size_t shm = tens_b + (size_t)tpb * A->max_row_nnz * 12 + 16;
+    if (shm > 220 * 1024) {
+        release();
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
+    }
+    if (A->slot_bytes == 1) {
+        auto kern = k_assemble_rows2<DIM, NB, NC, uint8_t>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
+                                                            (const uint8_t *)A->d_slot, A->d_rowptr, fac64, fac32,
+                                                            dt64, dt32, ft, A->d_vals64, A->d_vals32, A->max_row_nnz);
+    } else {
+        auto kern = k_assemble_rows2<DIM, NB, NC, uint16_t>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
+                                                            (const uint16_t *)A->d_slot, A->d_rowptr, fac64, fac32,
+                                                            dt64, dt32, ft, A->d_vals64, A->d_vals32, A->max_row_nnz);
+    }
+    GRMP_LAUNCHED(ctx);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // the tensor uploads are released next
+    release();
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "assembly kernels");
+    A->has64 = A->has32 = true;
+    return GRMP_OK;
+}
+
 template <int DIM, int NB, int NC, typename T>
 int run_assembly(grmp_matrix A, const FastTerms &ft, const std::vector<double> &tens64) {
     grmp_space s = A->space;
@@ -229,6 +389,7 @@ int run_assembly(grmp_matrix A, const FastTerms &ft, const std::vector<double> &
 template <int DIM, int NB, int NC>
 int dispatch_precision(grmp_matrix A, const FastTerms &ft, const std::vector<double> &tens, int precision) {
     if (precision == GRMP_FP64) return run_assembly<DIM, NB, NC, double>(A, ft, tens);
+    if (precision == GRMP_FP64_FP32) return run_assembly_dual<DIM, NB, NC>(A, ft, tens);
     return run_assembly<DIM, NB, NC, float>(A, ft, tens);
 }
 
@@ -329,7 +490,9 @@ int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_t
     grmp_space s = A->space;
     grmp_context ctx = s->mesh->ctx;
     if (s->fe == GRMP_FE_H1BR) {
-        int rc = grmp_br_assemble(A, nterms, terms, precision);
+        int rc = precision == GRMP_FP64_FP32 ? grmp_br_assemble(A, nterms, terms, GRMP_FP64)
+                                             : grmp_br_assemble(A, nterms, terms, precision);
+        if (!rc && precision == GRMP_FP64_FP32) rc = grmp_br_assemble(A, nterms, terms, GRMP_FP32);
         if (!rc) A->eliminated = false;
         return rc;
     }

@@ -130,7 +130,7 @@ __device__ __forceinline__ void rhs_eval(const RhsDev &r, int dim, int cell, con
         for (int m = 0; m < nm; m++) {
             double arg = 0;
             for (int j = 0; j < dim; j++) arg += r.par[m * stride + 1 + j] * x[j];
-            s += r.par[m * stride] * sin(M_PI * arg);
+            s += r.par[m * stride] * sinpi(arg);   // sin(pi arg), without rounding pi * arg first
         }
         f[0] = s;
         for (int c = 1; c < r.ncomp; c++) f[c] = 0;

@@ -91,9 +91,7 @@ class DeviceSystem:
     def assemble_and_solve(self, solver: api.GB300PCG, dirichlet: int = L.DIRICHLET_ELIMINATE) -> dict:
         """assembly (FP64, plus FP32 for the mixed mode) + Dirichlet + solve."""
         t0 = time.perf_counter()
-        api.assemble(self.A, self.prob.operators, L.FP64)
-        if self.mixed:
-            api.assemble(self.A, self.prob.operators, L.FP32)
+        api.assemble(self.A, self.prob.operators, L.FP64_FP32 if self.mixed else L.FP64)
         self.b.fill(0.0)
         api.assemble(self.b, self.prob.rhs)
         api.apply_dirichlet(self.A, self.b, self.prob.fixed, None, dirichlet)

@@ -145,7 +145,11 @@ typedef struct {
                                 data of a grmp_vector), read in place; 0: a host array, copied     */
 } grmp_bilinear_term;
 
-typedef enum { GRMP_FP64 = 0, GRMP_FP32 = 1 } grmp_precision;
+typedef enum {
+    GRMP_FP64 = 0,
+    GRMP_FP32 = 1,
+    GRMP_FP64_FP32 = 2   /* assembly only: FP64 and FP32 values in one pass (each in its own arithmetic) */
+} grmp_precision;
 
 /* Build the sparsity pattern of the sum of `terms` on `space` x `space`:
  * the union of the nonzero local contributions, an entry being dropped when
@@ -159,7 +163,9 @@ int grmp_matrix_destroy(grmp_matrix A);
 int grmp_matrix_info(grmp_matrix A, int32_t *nrows, int64_t *nnz, int32_t *max_row_nnz);
 
 /* Assemble the sum of `terms` into the matrix values in the given precision
- * (FP64 values and/or FP32 values are held separately in the handle).
+ * (FP64 values and/or FP32 values are held separately in the handle;
+ * GRMP_FP64_FP32 fills both from one walk of the incidence lists, the FP32
+ * values computed in FP32 arithmetic exactly as a GRMP_FP32 assembly would).
  * Stands in for assemble!(A::FEMatrixBlock, AP::AssemblyPattern{<:APT_BilinearForm})
  * (src/assemblypatterns/bilinearform.jl:92-400).  Deterministic: each
  * nonzero is the sum of its cell contributions in ascending cell order. */
