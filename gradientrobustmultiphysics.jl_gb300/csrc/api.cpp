@@ -199,7 +199,7 @@ int grmp_space_create(grmp_mesh mesh, int fe_kind, int ncomponents, const int32_
     int dim = mesh->dim;
     bool ok = (fe_kind == GRMP_FE_H1P1 && ncomponents >= 1 && ncomponents <= 3) ||
               (fe_kind == GRMP_FE_H1P2 && ncomponents >= 1 && ncomponents <= 3) ||
-              (fe_kind == GRMP_FE_H1BR && dim == 2 && ncomponents == 2) ||
+              (fe_kind == GRMP_FE_H1BR && ncomponents == dim) ||
               (fe_kind == GRMP_FE_L2P0 && ncomponents >= 1 && ncomponents <= 3);
     if (!ok)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "space: element %d with %d components in %dD is not built", fe_kind,

@@ -487,7 +487,12 @@ int br_assemble_t(grmp_matrix A, const BrTerms &bt) {
 }  // namespace
 
 // ---------------------------------------------------------------------- entry points used by pattern/assemble
+int grmp_br3_mask(grmp_space s, int nterms, const grmp_bilinear_term *terms, uint32_t *mask);
+int grmp_br3_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
+int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b);
+
 int grmp_br_mask(grmp_space s, int nterms, const grmp_bilinear_term *terms, uint32_t *mask) {
+    if (s->mesh->dim == 3) return grmp_br3_mask(s, nterms, terms, mask);
     grmp_context ctx = s->mesh->ctx;
     BrTerms bt;
     std::vector<std::pair<void *, size_t>> keep;
@@ -504,6 +509,7 @@ int grmp_br_mask(grmp_space s, int nterms, const grmp_bilinear_term *terms, uint
 }
 
 int grmp_br_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision) {
+    if (A->space->mesh->dim == 3) return grmp_br3_assemble(A, nterms, terms, precision);
     grmp_context ctx = A->space->mesh->ctx;
     BrTerms bt;
     std::vector<std::pair<void *, size_t>> keep;
@@ -516,6 +522,7 @@ int grmp_br_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms,
 
 // b += (f, R v) with f polynomial (optionally one polynomial per cell group)
 int grmp_br_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
+    if (s->mesh->dim == 3) return grmp_br3_rhs(s, rhs, b);
     grmp_mesh m = s->mesh;
     grmp_context ctx = m->ctx;
     if (rhs->kind != GRMP_RHS_POLY || rhs->ncomponents != 2)
@@ -577,6 +584,7 @@ int grmp_br_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
 int grmp_br_divergence(grmp_space s, double **Dv, double **vol) {
     grmp_mesh m = s->mesh;
     grmp_context ctx = m->ctx;
+    if (m->dim != 2) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batched Stokes: H1BR{2} only");
     int rc = grmp_alloc(ctx, (void **)Dv, (size_t)m->ncells * 9 * 8);
     if (!rc) rc = grmp_alloc(ctx, (void **)vol, (size_t)m->ncells * 8);
     if (rc) return rc;

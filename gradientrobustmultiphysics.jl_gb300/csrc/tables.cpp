@@ -142,7 +142,15 @@ int scalar_basis(int fe, int dim, const D *x, D *o) {
         o[0] = r;
         for (int j = 0; j < dim; j++) o[1 + j] = x[j];
         if (fe == GRMP_FE_H1P1) return dim + 1;
-        if (dim != 2) return 0;
+        if (dim == 3) {
+            // face bubbles of the faces [0,1,2], [0,1,3], [1,2,3], [0,2,3]
+            // (src/fedefs/h1v_br.jl:221-233), products left to right
+            o[4] = mul(mul(scal(60.0, x[0]), r), x[1]);
+            o[5] = mul(mul(scal(60.0, r), x[0]), x[2]);
+            o[6] = mul(mul(scal(60.0, x[0]), x[1]), x[2]);
+            o[7] = mul(mul(scal(60.0, r), x[1]), x[2]);
+            return 8;
+        }
         o[3] = mul(scal(6.0, x[0]), r);
         o[4] = mul(scal(6.0, x[1]), x[0]);
         o[5] = mul(scal(6.0, r), x[1]);
@@ -197,7 +205,7 @@ int grmp_fe_nb(int fe, int dim) {
     switch (fe) {
         case GRMP_FE_H1P1: return dim + 1;
         case GRMP_FE_H1P2: return dim == 2 ? 6 : 10;
-        case GRMP_FE_H1BR: return dim == 2 ? 6 : 0;
+        case GRMP_FE_H1BR: return dim == 2 ? 6 : 8;
         case GRMP_FE_L2P0: return 1;
     }
     return 0;
@@ -207,7 +215,7 @@ int grmp_fe_ldofs(int fe, int dim, int ncomp) {
     switch (fe) {
         case GRMP_FE_H1P1: return (dim + 1) * ncomp;
         case GRMP_FE_H1P2: return (dim == 2 ? 6 : 10) * ncomp;
-        case GRMP_FE_H1BR: return dim == 2 ? 9 : 0;
+        case GRMP_FE_H1BR: return dim == 2 ? 9 : 16;
         case GRMP_FE_L2P0: return ncomp;
         case GRMP_FE_HDIVRT0: return dim + 1;
     }

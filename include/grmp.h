@@ -94,7 +94,7 @@ int grmp_mesh_destroy(grmp_mesh mesh);
 typedef enum {
     GRMP_FE_H1P1 = 1,     /* src/fedefs/h1_p1.jl                    */
     GRMP_FE_H1P2 = 2,     /* src/fedefs/h1_p2.jl                    */
-    GRMP_FE_H1BR = 3,     /* src/fedefs/h1v_br.jl (2D)              */
+    GRMP_FE_H1BR = 3,     /* src/fedefs/h1v_br.jl (2D and 3D)       */
     GRMP_FE_HDIVRT0 = 4,  /* reconstruction target only            */
     GRMP_FE_HDIVBDM1 = 5, /* reconstruction target only            */
     GRMP_FE_L2P0 = 6      /* src/fedefs/l2_p0.jl                    */
@@ -192,9 +192,10 @@ typedef struct {
     int64_t nparams;        /* number of doubles in params                           */
     double factor;          /* LinearForm factor                                     */
     int bonus_quadorder;    /* DataFunction bonus_quadorder                          */
-    int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0{2}};
+    int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0{d}};
                                2 = ReconstructionIdentity{HDIVBDM1{2}} (1, 2: H1BR only,
-                               src/feevaluator_h1.jl:342-381, src/reconstructions.jl:351-403) */
+                               2 in 2D only; src/feevaluator_h1.jl:342-381,
+                               src/reconstructions.jl:351-491)                          */
     const int32_t *cell_group; /* optional [ncells]: POLY data per cell group (one DataFunction
                                   per independent problem of a batch); params then hold
                                   [ngroups][nterms][5]                                 */

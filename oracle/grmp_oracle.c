@@ -1068,6 +1068,252 @@ int oracle_br_rhs(double *b, int ncells, const double *coords, const int *cells,
                                factor, bonus_quadorder, 1);
 }
 
+/* ------------------------------------------------------------------------- */
+/* H1BR{3} on tetrahedra with the RT0 reconstruction                         */
+/* ------------------------------------------------------------------------- */
+
+/* Local faces of a tetrahedron (the reference's face_nodes of Tetrahedron3D):
+ * [0,1,2], [0,1,3], [1,2,3], [0,2,3]. */
+static const int BR3_FACES[4][3] = {{0, 1, 2}, {0, 1, 3}, {1, 2, 3}, {0, 2, 3}};
+
+/* Scalar basis of H1BR{3} (src/fedefs/h1v_br.jl:221-233): the four P1
+ * functions, then the face bubbles 60 x r y, 60 r x z, 60 x y z, 60 r y z
+ * (r = 1 - x - y - z), products in the reference's left-to-right order. */
+static void br3_basis(const double *xr, double vals[8], double derivs[8][3])
+{
+    dual x[3] = {dvar(xr[0], 0), dvar(xr[1], 1), dvar(xr[2], 2)};
+    dual r = dsub(dsub(dcsub(1.0, x[0]), x[1]), x[2]);
+    dual o[8] = {r, x[0], x[1], x[2],
+                 dmul(dmul(dscale(60.0, x[0]), r), x[1]),
+                 dmul(dmul(dscale(60.0, r), x[0]), x[2]),
+                 dmul(dmul(dscale(60.0, x[0]), x[1]), x[2]),
+                 dmul(dmul(dscale(60.0, r), x[1]), x[2])};
+    for (int a = 0; a < 8; a++) {
+        vals[a] = o[a].v;
+        for (int j = 0; j < 3; j++) derivs[a][j] = o[a].d[j];
+    }
+}
+
+/* local DoF layout (pattern "N1f1"): 0-11 P1, component-major (4 c + node),
+ * 12-15 the face bubbles (all three components, times n_F[c]) */
+static int br3_scalar(int dof, int c)
+{
+    if (dof < 12) return (dof / 4 == c) ? dof % 4 : -1;
+    return 4 + (dof - 12);
+}
+static double br3_coef(int dof, int c, const double *nrm /* [4][3] */)
+{
+    if (dof < 12) return 1.0;
+    return nrm[(dof - 12) * 3 + c];
+}
+
+/* RT0 reconstruction coefficients R[16][4] (src/reconstructions.jl:474-491):
+ * R[4k + node][f] = (1/3 |F|) n_F[k] for the three nodes of face f,
+ * R[12 + f][f] = |F|. */
+static void br3_rt0_coeffs(const double *fvol, const double *nrm, double R[16][4])
+{
+    memset(R, 0, sizeof(double) * 64);
+    for (int f = 0; f < 4; f++) {
+        for (int n = 0; n < 3; n++)
+            for (int k = 0; k < 3; k++) R[4 * k + BR3_FACES[f][n]][f] = ((1.0 / 3.0) * fvol[f]) * nrm[f * 3 + k];
+        R[12 + f][f] = fvol[f];
+    }
+}
+
+/* HDIVRT0{3} reference basis on the tetrahedron (src/fedefs/hdiv_rt0.jl:93-100) */
+static void rt03_ref_basis(double x, double y, double z, double out[4][3])
+{
+    out[0][0] = 2 * x; out[0][1] = 2 * y; out[0][2] = 2 * (z - 1);
+    out[1][0] = 2 * x; out[1][1] = 2 * (y - 1); out[1][2] = 2 * z;
+    out[2][0] = 2 * x; out[2][1] = 2 * y; out[2][2] = 2 * z;
+    out[3][0] = 2 * (x - 1); out[3][1] = 2 * y; out[3][2] = 2 * z;
+}
+
+static void br3_cell(const br_mesh *m, int cell, double X[12], double nrm[12], double fv[4], double sg[4])
+{
+    for (int v = 0; v < 4; v++)
+        for (int k = 0; k < 3; k++) X[v * 3 + k] = m->coords[(size_t)m->cells[(size_t)cell * 4 + v] * 3 + k];
+    for (int f = 0; f < 4; f++) {
+        int F = m->cell_faces[(size_t)cell * 4 + f];
+        for (int k = 0; k < 3; k++) nrm[f * 3 + k] = m->fnormals[(size_t)F * 3 + k];
+        fv[f] = m->fvolumes[F];
+        sg[f] = (double)m->signs[(size_t)cell * 4 + f];
+    }
+}
+
+/* nu (grad u, grad v) on H1BR{3} (Gradient with coefficients) plus
+ * lambda (div R u, div R v) with R the RT0 reconstruction; both on the rule of
+ * order 2 (polyorder 3 - 1) = 4.  The reconstructed divergence follows
+ * src/feevaluator_h1.jl:409-437: sum over faces and the three partial
+ * derivatives (2 each) of R * dphi * sign, divided by det A. */
+int oracle_br3_assemble(void *h, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                        const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                        double nu, const double *cellnu, double lambda)
+{
+    omat *M = (omat *)h;
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(3, 4, xref, w);
+    if (nq < 0) nq = -nq;
+    static double vals[OR_MAXQ][8], derivs[OR_MAXQ][8][3];
+    for (int q = 0; q < nq; q++) br3_basis(&xref[3 * q], vals[q], derivs[q]);
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], nrm[12], fv[4], sg[4];
+        br3_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(3, X, A, G, &det, &vol);
+        const int *dofs = &celldofs[(size_t)cell * 16];
+        static double cv[OR_MAXQ][16][9];
+        for (int q = 0; q < nq; q++)
+            for (int dof = 0; dof < 16; dof++)
+                for (int c = 0; c < 3; c++)
+                    for (int k = 0; k < 3; k++) {
+                        const int sidx = br3_scalar(dof, c);
+                        double s = 0;
+                        for (int j = 0; j < 3; j++) s += G[k][j] * (sidx >= 0 ? derivs[q][sidx][j] : 0.0);
+                        s *= br3_coef(dof, c, nrm);
+                        cv[q][dof][k + 3 * c] = s;
+                    }
+        double loc[16][16];
+        memset(loc, 0, sizeof(loc));
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < 16; i++) {
+                double res[9];
+                for (int k = 0; k < 9; k++) res[k] = cellnu ? cellnu[cell] * cv[q][i][k] : cv[q][i][k];
+                for (int j = i; j < 16; j++) {
+                    double t = 0;
+                    for (int k = 0; k < 9; k++) t += res[k] * cv[q][j][k];
+                    loc[i][j] += w[q] * t;
+                }
+            }
+        const double itemfactor = vol * (cellnu ? 1.0 : nu);
+        for (int i = 0; i < 16; i++)
+            for (int j = i + 1; j < 16; j++) {
+                omat_addnz(M, dofs[i], dofs[j], loc[i][j] * itemfactor, 1.0);
+                omat_addnz(M, dofs[j], dofs[i], loc[i][j] * itemfactor, 1.0);
+            }
+        for (int i = 0; i < 16; i++) omat_addnz(M, dofs[i], dofs[i], loc[i][i] * itemfactor, 1.0);
+        if (lambda == 0.0) continue;
+        double R[16][4];
+        br3_rt0_coeffs(fv, nrm, R);
+        double dv[16];
+        for (int i = 0; i < 16; i++) {
+            double s = 0;
+            for (int j = 0; j < 4; j++)
+                if (R[i][j] != 0)
+                    for (int jd = 0; jd < 3; jd++) s += R[i][j] * 2.0 * sg[j];
+            dv[i] = s / fabs(det);
+        }
+        double lp[16][16];
+        memset(lp, 0, sizeof(lp));
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < 16; i++)
+                for (int j = 0; j < 16; j++) {
+                    double t = 0;
+                    t += dv[i] * dv[j];
+                    lp[i][j] += w[q] * t;
+                }
+        const double pf = vol * lambda;
+        for (int i = 0; i < 16; i++)
+            for (int j = 0; j < 16; j++) omat_addnz(M, dofs[i], dofs[j], lp[i][j] * pf, 1.0);
+    }
+    return nq;
+}
+
+/* b += factor * (f, R v) on H1BR{3}, f polynomial (3 components), with the
+ * ReconstructionIdentity{HDIVRT0{3}} test operator (src/feevaluator_h1.jl:
+ * 342-381): Piola A phi_hat * sign / det; quadrature order 3 + bonus. */
+int oracle_br3_rhs(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                   const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                   const double *par, int npar, double factor, int bonus_quadorder)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(3, 3 + bonus_quadorder, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], nrm[12], fv[4], sg[4];
+        br3_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(3, X, A, G, &det, &vol);
+        double R[16][4];
+        br3_rt0_coeffs(fv, nrm, R);
+        double locb[16] = {0};
+        for (int q = 0; q < nq; q++) {
+            double rt[4][3];
+            rt03_ref_basis(xref[3 * q], xref[3 * q + 1], xref[3 * q + 2], rt);
+            double te[4][3];
+            for (int j = 0; j < 4; j++)
+                for (int k = 0; k < 3; k++) {
+                    double s = 0;
+                    for (int l = 0; l < 3; l++) s += A[k][l] * rt[j][l];
+                    s *= sg[j] / fabs(det);
+                    te[j][k] = s;
+                }
+            double x[3], f[3];
+            for (int k = 0; k < 3; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 3; j++) x[k] += A[k][j] * xref[3 * q + j];
+            }
+            rhs_eval(OR_RHS_POLY, 3, 3, par, npar, cell, x, f);
+            for (int i = 0; i < 16; i++) {
+                double cvv[3] = {0, 0, 0};
+                for (int j = 0; j < 4; j++)
+                    if (R[i][j] != 0)
+                        for (int k = 0; k < 3; k++) cvv[k] += R[i][j] * te[j][k];
+                double t = 0;
+                for (int k = 0; k < 3; k++) t += f[k] * cvv[k];
+                locb[i] += t * w[q];
+            }
+        }
+        const double itemfactor = factor * vol;
+        for (int i = 0; i < 16; i++) b[celldofs[(size_t)cell * 16 + i]] += locb[i] * itemfactor;
+    }
+    return nq;
+}
+
+/* Divergence of H1BR{3} functions with coefficients on the rule of order 2
+ * (polyorder 3 - 1 + 0 for (div u, q_P0); exact for the quadratic divergence
+ * of the bubbles): divu[cell] = (1/|T|) int_T div u and
+ * b[dof] += int_T p_T div phi_dof (either output may be NULL). */
+void oracle_br3_div(int ncells, const double *coords, const int *cells, const int *cell_faces, const double *fnormals,
+                    const double *fvolumes, const signed char *signs, const int *celldofs, const double *u,
+                    const double *p, double *divu, double *b)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(3, 2, xref, w);
+    double vals[OR_MAXQ][8], derivs[OR_MAXQ][8][3];
+    for (int q = 0; q < nq; q++) br3_basis(&xref[3 * q], vals[q], derivs[q]);
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], nrm[12], fv[4], sg[4];
+        br3_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(3, X, A, G, &det, &vol);
+        const int *dofs = &celldofs[(size_t)cell * 16];
+        double dint = 0;
+        double lb[16] = {0};
+        for (int q = 0; q < nq; q++) {
+            double dq = 0;
+            for (int dof = 0; dof < 16; dof++) {
+                double cv = 0;
+                for (int k = 0; k < 3; k++)
+                    for (int j = 0; j < 3; j++) {
+                        const int sidx = br3_scalar(dof, k);
+                        cv += G[k][j] * (sidx >= 0 ? derivs[q][sidx][j] : 0.0) * br3_coef(dof, k, nrm);
+                    }
+                if (u) dq += u[dofs[dof]] * cv;
+                if (b && p) lb[dof] += (p[cell] * cv) * w[q];
+            }
+            dint += dq * w[q];
+        }
+        if (divu) divu[cell] = dint;
+        if (b && p)
+            for (int dof = 0; dof < 16; dof++) b[dofs[dof]] += lb[dof] * vol;
+    }
+}
+
 /* Divergence of H1BR{2} functions with coefficients
  * (src/feevaluator_h1.jl:133-145) at the midpoint: per cell
  * divu[cell] = (1/|T|) int_T div u  (the rule of order 1 is exact), and

@@ -89,6 +89,11 @@ def lib():
         L.oracle_br_rhs_recon.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.oracle_br_rhs_recon.restype = ctypes.c_int
         L.oracle_br_div.argtypes = brm + [dp, dp, dp, dp]
+        L.oracle_br3_assemble.argtypes = [ctypes.c_void_p] + brm + [ctypes.c_double, dp, ctypes.c_double]
+        L.oracle_br3_assemble.restype = ctypes.c_int
+        L.oracle_br3_rhs.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.oracle_br3_rhs.restype = ctypes.c_int
+        L.oracle_br3_div.argtypes = brm + [dp, dp, dp, dp]
     return _lib
 
 
@@ -295,11 +300,12 @@ if __name__ == "__main__":  # pragma: no cover - manual build helper
 # --------------------------------------------------------------------------
 
 def br_celldofs(nverts: int, cells: np.ndarray, cell_faces: np.ndarray):
-    """H1BR{2} cell DoFs, pattern "N1f1" (src/fedefs/h1v_br.jl:33) restated
-    from src/dofmaps.jl:201-330: component-1 nodes, component-2 nodes, faces."""
+    """H1BR{d} cell DoFs, pattern "N1f1" (src/fedefs/h1v_br.jl:33) restated
+    from src/dofmaps.jl:201-330: the nodes of each component, then faces."""
     nf = int(cell_faces.max()) + 1
-    cd = np.concatenate([cells, cells + nverts, cell_faces + 2 * nverts], axis=1).astype(np.int32)
-    return np.ascontiguousarray(cd), 2 * nverts + nf
+    dim = cells.shape[1] - 1
+    cd = np.concatenate([cells + c * nverts for c in range(dim)] + [cell_faces + dim * nverts], axis=1).astype(np.int32)
+    return np.ascontiguousarray(cd), dim * nverts + nf
 
 
 def _br_args(g, cd):
@@ -318,6 +324,7 @@ RECON_RT0, RECON_BDM1 = 1, 2
 
 
 def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, recon: int = RECON_RT0):
+    # (2D: H1BR{2} with RT0 or BDM1; 3D: H1BR{3} with RT0)
     """(A (penalised), bf, fixed, celldofs) of the velocity update system:
     nu (grad u, grad v) + lam (div R u, div R v) = (f, R_rhs v), R_rhs the
     BR->RT0 (recon 1) or BR->BDM1 (recon 2) reconstruction."""
@@ -325,14 +332,22 @@ def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, 
     cd, nd = br_celldofs(g.nverts, g.cells, cf)
     arrs, ptrs = _br_args(g, cd)
     M = Matrix(nd)
-    lib().oracle_br_assemble(M.h, *ptrs, float(nu), None, float(lam))
     bf = np.zeros(nd)
     par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
-    lib().oracle_br_rhs_recon(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder), int(recon))
-    # homogeneous Dirichlet on all boundary faces: nodes (both components) and face bubbles
+    if g.dim == 3:
+        if recon != RECON_RT0:
+            raise ValueError("H1BR{3}: the RT0 reconstruction only")
+        lib().oracle_br3_assemble(M.h, *ptrs, float(nu), None, float(lam))
+        if lib().oracle_br3_rhs(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder)) < 0:
+            raise RuntimeError("oracle: no tetrahedral rule of that order")
+    else:
+        lib().oracle_br_assemble(M.h, *ptrs, float(nu), None, float(lam))
+        lib().oracle_br_rhs_recon(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder), int(recon))
+    # homogeneous Dirichlet on all boundary faces: nodes (every component) and face bubbles
     bf_ids = np.nonzero(np.bincount(cf.ravel(), minlength=fn.shape[0]) == 1)[0]
     bnodes = np.unique(fn[bf_ids].ravel())
-    fixed = np.unique(np.concatenate([bnodes, bnodes + g.nverts, bf_ids + 2 * g.nverts])).astype(np.int32)
+    fixed = np.unique(np.concatenate([bnodes + c * g.nverts for c in range(g.dim)] +
+                                     [bf_ids + g.dim * g.nverts])).astype(np.int32)
     return M, bf, fixed, cd, (arrs, ptrs)
 
 
@@ -345,17 +360,19 @@ def br_div(g, cd_args, u=None, p=None):
     b = np.zeros(nd) if p is not None else None
     uu = np.ascontiguousarray(u, dtype=np.float64) if u is not None else None
     pp = np.ascontiguousarray(p, dtype=np.float64) if p is not None else None
-    lib().oracle_br_div(*ptrs, _dp(uu) if uu is not None else None, _dp(pp) if pp is not None else None,
-                        _dp(divu) if divu is not None else None, _dp(b) if b is not None else None)
+    fn = lib().oracle_br3_div if arrs[1].shape[1] == 4 else lib().oracle_br_div
+    fn(*ptrs, _dp(uu) if uu is not None else None, _dp(pp) if pp is not None else None,
+       _dp(divu) if divu is not None else None, _dp(b) if b is not None else None)
     return divu, b
 
 
-def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6, recon: int = RECON_RT0):
+def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6, recon: int = RECON_RT0,
+                            bonus_quadorder: int = 2):
     """Iterated penalty (examples/Example221_StokesIterated2D.jl:61-95, no
     convection): sparse-direct velocity solves of the penalised system,
     P0 pressure update p <- p - lam * avg(div u), zero mean."""
     import scipy.sparse.linalg as spla
-    M, bf, fixed, cd, args = br_stokes_system(g, nu, lam, terms, recon=recon)
+    M, bf, fixed, cd, args = br_stokes_system(g, nu, lam, terms, bonus_quadorder=bonus_quadorder, recon=recon)
     M.penalize(fixed)
     A = M.csr().tocsc()
     lu = spla.splu(A)

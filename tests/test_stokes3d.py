@@ -1,0 +1,212 @@
+"""Bernardi-Raugel H1BR{3} / P0 Stokes with the BR -> RT0 reconstruction in 3D.
+
+CPU: the oracle's 3D element reproduces the reference's pressure-robustness
+known answer (examples/Example222_PressureRobustness2D.jl:189-211 restated on
+tetrahedra, the 3D element of src/fedefs/h1v_br.jl:23-29 with
+src/reconstructions.jl:404-470): a pure gradient force gives a zero discrete
+velocity and the cell means of the potential as pressure, and the
+reconstructed load of a gradient is annihilated by discretely div-free
+velocities.  GPU: DoF map, sparsity pattern (bit-exact), FP64 / FP32 / dual
+matrix values and the reconstructed right-hand side against the oracle, and
+the Dirichlet-eliminated velocity system solved on the device against a
+sparse-direct solve of the oracle's system.
+"""
+import numpy as np
+import pytest
+
+# phi = x^2 + 2 y^2 - z^2 + x y;  grad phi = (2x + y, x + 4y, -2z)
+GRAD_PHI = np.array([(0, 2.0, 1, 0, 0), (0, 1.0, 0, 1, 0), (1, 1.0, 1, 0, 0), (1, 4.0, 0, 1, 0),
+                     (2, -2.0, 0, 0, 1)], dtype=np.float64)
+
+
+def _phi(P):
+    x, y, z = P[..., 0], P[..., 1], P[..., 2]
+    return x * x + 2 * y * y - z * z + x * y
+
+
+def _cell_means(O, g, f):
+    x, w, _ = O.qrule(3, 2)                     # exact for the quadratic phi
+    X = g.coords[g.cells]
+    A = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))
+    pts = X[:, None, 0, :] + np.einsum("ckj,qj->cqk", A, x)
+    return f(pts) @ w
+
+
+def _random_quadratic_terms(rng, ncomp=3):
+    out = []
+    for c in range(ncomp):
+        for e in [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (1, 1, 0), (0, 1, 1), (1, 0, 1)]:
+            out.append((c, rng.standard_normal(), *e))
+    return np.array(out, dtype=np.float64)
+
+
+@pytest.mark.parametrize("bonus", [0, 1])
+def test_oracle_3d_hydrostatic_velocity_is_zero(G, O, bonus):
+    g = G.grid_unitcube_kuhn(2)
+    target = _cell_means(O, g, _phi)
+    vol = g.cell_volumes()
+    target = target - np.dot(vol, target) / vol.sum()
+    for nu in (1.0, 1e-3):
+        u, p, _ = O.stokes_iterated_penalty(g, nu, 1e4, GRAD_PHI, sweeps=10, bonus_quadorder=bonus)
+        assert np.max(np.abs(u)) < 1e-12, nu
+        assert np.max(np.abs(p - target)) < 1e-9 * np.max(np.abs(target)), nu
+
+
+def test_oracle_3d_rhs_of_gradient_is_in_range_of_divergence(G, O):
+    """(grad phi, R v) = -(pi_0 phi, div v) for every v vanishing on the boundary."""
+    g = G.grid_unitcube_kuhn(2)
+    M, bf, fixed, cd, args = O.br_stokes_system(g, 1.0, 0.0, GRAD_PHI, bonus_quadorder=1)
+    _, bp = O.br_div(g, args, p=_cell_means(O, g, _phi))
+    free = np.setdiff1d(np.arange(bf.size), fixed)
+    assert np.max(np.abs(bf[free] + bp[free])) < 1e-13 * max(1.0, np.max(np.abs(bf)))
+
+
+def test_oracle_3d_penalty_term_is_the_divergence_energy(G, O):
+    """u^T A_lam u = lam * sum_T |T| (avg_T div u)^2: the penalty matrix is the
+    Gram matrix of the piecewise-constant reconstructed divergence."""
+    g = G.grid_unitcube_kuhn(2)
+    M, _, _, cd, args = O.br_stokes_system(g, 0.0, 1.0, GRAD_PHI, bonus_quadorder=0)
+    A = M.csr()
+    u = np.random.default_rng(4).standard_normal(A.shape[0])
+    divu, _ = O.br_div(g, args, u=u)
+    e = np.dot(g.cell_volumes(), divu * divu)
+    assert abs(u @ (A @ u) - e) <= 1e-12 * e
+
+
+def test_fespace_h1br3_matches_oracle_dofmap(G, O):
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitcube_kuhn(3)
+    FES = F.FESpace(F.H1BR(3), g)
+    cd, nd = O.br_celldofs(g.nverts, g.cells, g.faces()[1])
+    assert FES.ndofs == nd and np.array_equal(FES.celldofs, cd)
+    _, _, fixed, _, _ = O.br_stokes_system(g, 1.0, 0.0, GRAD_PHI, bonus_quadorder=0)
+    assert np.array_equal(FES.boundary_dofs(), fixed)
+
+
+# ---------------------------------------------------------------------- GPU
+def _ops(nu_cell, lam):
+    from grmp_gb300 import _lib as L
+    from grmp_gb300 import api
+    lap = api.Operator(L.OP_LAPLACE, True, 1.0, cell_coef=nu_cell, name="nu (grad u, grad v)")
+    pen = api.Operator(L.OP_RDIVRDIV, False, lam, name="lambda (div R u, div R v)")
+    return [lap, pen]
+
+
+def _system(G, O, n, lam, seed=7):
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitcube_kuhn(n)
+    FES = F.FESpace(F.H1BR(3), g)
+    nu_cell = np.exp(0.5 * np.random.default_rng(seed).standard_normal(g.ncells))
+    return g, FES, nu_cell
+
+
+def _oracle_matrix(O, g, nu_cell, lam):
+    cd, nd = O.br_celldofs(g.nverts, g.cells, g.faces()[1])
+    arrs, ptrs = O._br_args(g, cd)
+    M = O.Matrix(nd)
+    nc = np.ascontiguousarray(nu_cell, dtype=np.float64)
+    O.lib().oracle_br3_assemble(M.h, *ptrs, 1.0, O._dp(nc), float(lam))
+    return M.csr()
+
+
+def _row_scaled_err(Ag, A0, floor=1e-3):
+    """max |a - o| / max(|o|, floor * max|o_row|); floor 1 gives the error
+    relative to the row maximum (the FP32 measure: cancelling sums make a
+    per-entry relative bound meaningless at FP32)."""
+    o = A0.data
+    rm = np.repeat(np.maximum.reduceat(np.abs(o), A0.indptr[:-1]), np.diff(A0.indptr))
+    return np.max(np.abs(Ag.data - o) / np.maximum(np.abs(o), floor * rm))
+
+
+@pytest.mark.gpu
+def test_br3_assembly_parity(G, O, ctx):
+    from grmp_gb300 import _lib as L
+    from grmp_gb300 import api
+    lam = 37.0
+    g, FES, nu_cell = _system(G, O, 3, lam)
+    A0 = _oracle_matrix(O, g, nu_cell, lam)
+    ops = _ops(nu_cell, lam)
+    A = api.FEMatrix(ctx, FES, ops)
+    rp, ci = A.pattern()
+    assert np.array_equal(rp, A0.indptr) and np.array_equal(ci, A0.indices)
+    api.assemble(A, ops, L.FP64)
+    A64 = A.download(L.FP64)
+    assert _row_scaled_err(A64, A0) <= 1e-12
+    api.assemble(A, ops, L.FP32)
+    A32 = A.download(L.FP32)
+    assert _row_scaled_err(A32, A0, floor=1.0) <= 2e-6
+    # the one-pass dual assembly writes exactly what the two single passes wrote
+    B = api.FEMatrix(ctx, FES, ops)
+    api.assemble(B, ops, L.FP64_FP32)
+    assert np.array_equal(B.download(L.FP64).data, A64.data)
+    assert np.array_equal(B.download(L.FP32).data, A32.data)
+    # repeat runs are bit-identical
+    api.assemble(A, ops, L.FP64)
+    assert np.array_equal(A.download(L.FP64).data, A64.data)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bonus", [0, 1])
+def test_br3_rhs_parity(G, O, ctx, bonus):
+    from grmp_gb300 import api
+    g = G.grid_unitcube_kuhn(3)
+    from grmp_gb300 import fespace as F
+    FES = F.FESpace(F.H1BR(3), g)
+    terms = _random_quadratic_terms(np.random.default_rng(9 + bonus))
+    _, bf, _, _, _ = O.br_stokes_system(g, 1.0, 0.0, terms, bonus_quadorder=bonus)
+    b = api.FEVector(ctx, FES)
+    b.fill(0.0)
+    api.assemble(b, api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(terms, 3, bonus)))
+    assert np.max(np.abs(b.entries - bf)) <= 1e-12 * np.max(np.abs(bf))
+
+
+@pytest.mark.gpu
+def test_br3_refusals(G, ctx):
+    from grmp_gb300 import _lib as L
+    from grmp_gb300 import api
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitcube_kuhn(2)
+    FES = F.FESpace(F.H1BR(3), g)
+    b = api.FEVector(ctx, FES)
+    with pytest.raises(G.GrmpError) as ei:   # BDM1 is the 2D reconstruction only
+        lf = api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(GRAD_PHI, 3))
+        r = lf.rhs()
+        r.test_operator = 2
+        import ctypes
+        ctx.check(ctx.lib.grmp_assemble_linear(ctx.space(FES), ctypes.byref(r), b.h))
+    assert ei.value.code == L.ERR_UNSUPPORTED
+    with pytest.raises(G.GrmpError) as ei:   # no tetrahedral rule of order 3 + 6
+        api.assemble(b, api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(GRAD_PHI, 3, 6)))
+    assert ei.value.code == L.ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "direct"])
+def test_br3_velocity_solve_matches_oracle(G, O, ctx, mode):
+    """One velocity solve of the iterated penalty (p = 0): the device's
+    eliminated system and solver against scipy's sparse LU of the oracle's."""
+    import scipy.sparse.linalg as spla
+    from grmp_gb300 import _lib as L
+    from grmp_gb300 import api
+    lam = 100.0
+    g, FES, nu_cell = _system(G, O, 4, lam, seed=2)
+    terms = _random_quadratic_terms(np.random.default_rng(3))
+    A0 = _oracle_matrix(O, g, nu_cell, lam)
+    _, bf, fixed, _, _ = O.br_stokes_system(g, 1.0, 0.0, terms, bonus_quadorder=1)
+    free = np.setdiff1d(np.arange(bf.size), fixed)
+    uref = np.zeros(bf.size)
+    uref[free] = spla.spsolve(A0[free][:, free].tocsc(), bf[free])
+    ops = _ops(nu_cell, lam)
+    A = api.FEMatrix(ctx, FES, ops)
+    api.assemble(A, ops, L.FP64_FP32 if mode == "mixed" else L.FP64)
+    b = api.FEVector(ctx, FES)
+    b.fill(0.0)
+    api.assemble(b, api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(terms, 3, 1)))
+    api.apply_dirichlet(A, b, FES.boundary_dofs(), None, L.DIRICHLET_ELIMINATE)
+    x = api.FEVector(ctx, FES)
+    x.fill(0.0)
+    st = api.GB300PCG(mode=mode, reltol=1e-13, abstol=0.0).solve(A, b, x)
+    assert st["status"] == 0, st
+    u = x.entries
+    assert np.max(np.abs(u[fixed])) == 0.0
+    assert np.linalg.norm(u - uref) <= 1e-9 * np.linalg.norm(uref), st
