@@ -93,6 +93,102 @@ int stroud(int order, double (*x)[3], double *w) {
     return q;
 }
 
+// Symmetric rules of Zhang, Cui and Liu ("A set of symmetric quadrature rules
+// on triangles and tetrahedra", J. Comput. Math. 27 (2009) 89-96) with the
+// orbit constants and the point order of src/quadrature.jl:332-499: the
+// reference takes them for triangles of order 8 and 12-14 and for
+// tetrahedra of order 5-8 (and, with a warning, above 8).
+int symmetric_triangle(int order, double (*x)[3], double *w) {
+    double w3;
+    const double *a21, *w21, (*a111)[2], *w111;
+    int n21, n111;
+    static const double a21_8[3] = {.1705693077517602066222935014914645, .0505472283170309754584235505965989,
+                                    .4592925882927231560288155144941693};
+    static const double w21_8[3] = {.1032173705347182502817915502921290, .0324584976231980803109259283417806,
+                                    .0950916342672846247938961043885843};
+    static const double a111_8[1][2] = {{.2631128296346381134217857862846436, .0083947774099576053372138345392944}};
+    static const double w111_8[1] = {.0272303141744349942648446900739089};
+    static const double a21_14[7] = {.0099797608064584324152935295820524, .4799778935211883898105528650883899,
+                                     .1538119591769669000000000000000000, .0740234771169878100000000000000000,
+                                     .1303546825033300000000000000000000, .2306172260266531342996053700983831,
+                                     .4223320834191478241144087137913939};
+    static const double w21_14[7] = {.0017351512297252675680618638808094, .0261637825586145217778288591819783,
+                                     .0039197292424018290965208275701454, .0122473597569408660972869899262505,
+                                     .0281996285032579601073663071515657, .0508870871859594852960348275454540,
+                                     .0504534399016035991910208971341189};
+    static const double a111_14[4][2] = {{.7862373859346610033296221140330900, .1906163600319009042461432828653034},
+                                         {.6305521436606074416224090755688129, .3623231377435471446183267343597729},
+                                         {.6265773298563063142335123137534265, .2907712058836674150248168174816732},
+                                         {.9142099849296254122399670993850469, .0711657108777507625475924502924336}};
+    static const double w111_14[4] = {.0170636442122334512900253993849472, .0096834664255066004075209630934194,
+                                      .0363857559284850056220113277642717, .0069646633735184124253997225042413};
+    if (order <= 8) {
+        w3 = .1443156076777871682510911104890646;
+        a21 = a21_8, w21 = w21_8, n21 = 3, a111 = a111_8, w111 = w111_8, n111 = 1;
+    } else {
+        w3 = .0585962852260285941278938063477560;
+        a21 = a21_14, w21 = w21_14, n21 = 7, a111 = a111_14, w111 = w111_14, n111 = 4;
+    }
+    int q = 0;
+    x[q][0] = x[q][1] = 1.0 / 3.0;
+    w[q++] = w3;
+    for (int j = 0; j < n21; j++) {       // orbit S21: three points
+        const double a = a21[j], c = 1.0 - 2.0 * a;
+        const double p[3][2] = {{a, a}, {a, c}, {c, a}};
+        for (int k = 0; k < 3; k++, q++) {
+            x[q][0] = p[k][0], x[q][1] = p[k][1];
+            w[q] = w21[j];
+        }
+    }
+    for (int j = 0; j < n111; j++) {      // orbit S111: six points
+        const double a = a111[j][0], b = a111[j][1], c = 1.0 - a - b;
+        const double p[6][2] = {{a, b}, {b, a}, {a, c}, {b, c}, {c, a}, {c, b}};
+        for (int k = 0; k < 6; k++, q++) {
+            x[q][0] = p[k][0], x[q][1] = p[k][1];
+            w[q] = w111[j];
+        }
+    }
+    return q;
+}
+
+int symmetric_tetrahedron(double (*x)[3], double *w) {   // order 8, 46 points
+    static const double a31[4] = {.0396754230703899012650713295393895, .3144878006980963137841605626971483,
+                                  .1019866930627033000000000000000000, .1842036969491915122759464173489092};
+    static const double w31[4] = {.0063971477799023213214514203351730, .0401904480209661724881611584798178,
+                                  .0243079755047703211748691087719226, .0548588924136974404669241239903914};
+    static const double a22 = .0634362877545398924051412387018983, w22 = .0357196122340991824649509689966176;
+    static const double a211[2][2] = {{.0216901620677280048026624826249302, .7199319220394659358894349533527348},
+                                      {.2044800806367957142413355748727453, .5805771901288092241753981713906204}};
+    static const double w211[2] = {.0071831906978525394094511052198038, .0163721819453191175409381397561191};
+    int q = 0;
+    for (int j = 0; j < 4; j++) {         // orbit S31: four points
+        const double a = a31[j], c = 1.0 - 3.0 * a;
+        const double p[4][3] = {{a, a, a}, {a, a, c}, {a, c, a}, {c, a, a}};
+        for (int k = 0; k < 4; k++, q++) {
+            for (int d = 0; d < 3; d++) x[q][d] = p[k][d];
+            w[q] = w31[j];
+        }
+    }
+    {                                     // orbit S22: six points
+        const double a = a22, c = 0.5 - a;
+        const double p[6][3] = {{a, a, c}, {a, c, a}, {c, a, a}, {c, a, c}, {c, c, a}, {a, c, c}};
+        for (int k = 0; k < 6; k++, q++) {
+            for (int d = 0; d < 3; d++) x[q][d] = p[k][d];
+            w[q] = w22;
+        }
+    }
+    for (int j = 0; j < 2; j++) {         // orbit S211: twelve points
+        const double a = a211[j][0], b = a211[j][1], c = 1.0 - 2.0 * a - b;
+        const double p[12][3] = {{a, a, b}, {a, b, a}, {b, a, a}, {a, a, c}, {a, c, a}, {c, a, a},
+                                 {a, b, c}, {a, c, b}, {c, a, b}, {b, a, c}, {b, c, a}, {c, b, a}};
+        for (int k = 0; k < 12; k++, q++) {
+            for (int d = 0; d < 3; d++) x[q][d] = p[k][d];
+            w[q] = w211[j];
+        }
+    }
+    return q;
+}
+
 // ------------------------------------------------------------------ duals
 struct D {
     double v, d[3];
@@ -238,7 +334,8 @@ int grmp_quadrature(int dim, int order, double (*x)[3], double *w) {
             w[0] = w[1] = w[2] = 1.0 / 3.0;
             return 3;
         }
-        if (order <= 20) return stroud(order, x, w);   // orders 8, 12-14 use the reference's symmetric tables
+        if (order == 8 || (order >= 12 && order <= 14)) return symmetric_triangle(order, x, w);
+        if (order <= 20) return stroud(order, x, w);
         return 0;
     }
     if (dim == 3) {
@@ -279,7 +376,7 @@ int grmp_quadrature(int dim, int order, double (*x)[3], double *w) {
             }
             return 11;
         }
-        return 0;
+        return symmetric_tetrahedron(x, w);   // orders above 8: the order-8 rule, as the reference
     }
     return 0;
 }

@@ -37,9 +37,8 @@ def _integrate(O, g, order, func):
 
 @pytest.mark.parametrize("order", list(range(1, 21)))
 def test_quadrature_triangle_exact(G, O, order):
-    """runtests.jl:81-137 on Triangle2D up to order 20 (Stroud and midpoint
-    rules; orders 8 and 12-14 use the reference's symmetric tables, replaced
-    here by the Stroud rule of the same order, which is also exact)."""
+    """runtests.jl:81-137 on Triangle2D up to order 20 (midpoint, edge
+    midpoint and Stroud rules; the symmetric rules at orders 8 and 12-14)."""
     g = G.grid_unitsquare(2)
     p = order
 
@@ -51,9 +50,10 @@ def test_quadrature_triangle_exact(G, O, order):
     assert np.allclose(val, exact, rtol=1e-13, atol=1e-13)
 
 
-@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("order", list(range(1, 9)))
 def test_quadrature_tetrahedron_exact(G, O, order):
-    """runtests.jl:81-137 on Tetrahedron3D (hard-coded rules, orders 1-4)."""
+    """runtests.jl:81-137 on Tetrahedron3D (hard-coded rules, orders 1-4;
+    the symmetric order-8 rule for 5-8)."""
     g = G.grid_unitcube_kuhn(2)
     p = order
 
@@ -65,6 +65,22 @@ def test_quadrature_tetrahedron_exact(G, O, order):
     exact = np.array([1 / (p + 1) - 1, 3 / (p + 1) + 1, 2 / (p + 1) - 1])
     # the reference's order-4 tet weights are 16-digit decimals
     assert np.allclose(val, exact, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("dim,order,npts", [(2, 8, 16), (2, 12, 46), (2, 13, 46), (2, 14, 46), (3, 5, 46),
+                                            (3, 8, 46), (3, 11, 46)])
+def test_symmetric_rules(G, O, dim, order, npts):
+    """The symmetric rules of src/quadrature.jl:332-499: point counts, points
+    inside the reference simplex, weights summing to one (to the digits the
+    reference tabulates), and the rule above order 8 on tetrahedra being the
+    order-8 rule (the reference warns and takes it)."""
+    x, w, exact = O.qrule(dim, order)
+    assert exact and x.shape[0] == npts
+    assert np.all(x[:, :dim] > 0) and np.all(x[:, :dim].sum(axis=1) < 1)
+    assert abs(w.sum() - 1.0) < 1e-4
+    if dim == 3 and order > 8:
+        x8, w8, _ = O.qrule(3, 8)
+        assert np.array_equal(x, x8) and np.array_equal(w, w8)
 
 
 # --------------------------------------------------------------------- bases

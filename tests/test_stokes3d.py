@@ -146,7 +146,7 @@ def test_br3_assembly_parity(G, O, ctx):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bonus", [0, 1])
+@pytest.mark.parametrize("bonus", [0, 1, 2])
 def test_br3_rhs_parity(G, O, ctx, bonus):
     from grmp_gb300 import api
     g = G.grid_unitcube_kuhn(3)
@@ -161,7 +161,7 @@ def test_br3_rhs_parity(G, O, ctx, bonus):
 
 
 @pytest.mark.gpu
-def test_br3_refusals(G, ctx):
+def test_br3_refusals_and_high_orders(G, ctx):
     from grmp_gb300 import _lib as L
     from grmp_gb300 import api
     from grmp_gb300 import fespace as F
@@ -175,9 +175,13 @@ def test_br3_refusals(G, ctx):
         import ctypes
         ctx.check(ctx.lib.grmp_assemble_linear(ctx.space(FES), ctypes.byref(r), b.h))
     assert ei.value.code == L.ERR_UNSUPPORTED
-    with pytest.raises(G.GrmpError) as ei:   # no tetrahedral rule of order 3 + 6
-        api.assemble(b, api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(GRAD_PHI, 3, 6)))
-    assert ei.value.code == L.ERR_UNSUPPORTED
+    # orders above 8 take the order-8 rule, as the reference does (with a warning)
+    vals = []
+    for bonus in (5, 6):
+        b.fill(0.0)
+        api.assemble(b, api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(GRAD_PHI, 3, bonus)))
+        vals.append(b.entries)
+    assert np.array_equal(vals[0], vals[1])
 
 
 @pytest.mark.gpu
