@@ -367,10 +367,13 @@ def br_div(g, cd_args, u=None, p=None):
 
 
 def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6, recon: int = RECON_RT0,
-                            bonus_quadorder: int = 2):
+                            bonus_quadorder: int = 2, u_boundary=None):
     """Iterated penalty (examples/Example221_StokesIterated2D.jl:61-95, no
     convection): sparse-direct velocity solves of the penalised system,
-    P0 pressure update p <- p - lam * avg(div u), zero mean."""
+    P0 pressure update p <- p - lam * avg(div u), zero mean.  u_boundary:
+    optional full-length vector whose entries at the boundary DoFs are the
+    Dirichlet values, imposed in the reference's penalty form (A[d,d] = 1e60,
+    b[d] = 1e60 u_D, src/solvers.jl:640-652); None = homogeneous."""
     import scipy.sparse.linalg as spla
     M, bf, fixed, cd, args = br_stokes_system(g, nu, lam, terms, bonus_quadorder=bonus_quadorder, recon=recon)
     M.penalize(fixed)
@@ -382,7 +385,7 @@ def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6, re
     for _ in range(sweeps):
         _, bp = br_div(g, args, p=p)
         b = bf + bp
-        b[fixed] = 0.0
+        b[fixed] = 0.0 if u_boundary is None else 1e60 * np.asarray(u_boundary, dtype=np.float64)[fixed]
         u = lu.solve(b)
         divu, _ = br_div(g, args, u=u)
         p = p - lam * divu

@@ -39,6 +39,31 @@ def test_oracle_hydrostatic_velocity_is_zero(G, O, recon):
         assert np.max(np.abs(p - target)) < 1e-9 * np.max(np.abs(target)), nu
 
 
+def br_linear_interpolant(g, field):
+    """BR DoF vector of a linear vector field: vertex values per component
+    (component-major), zero face bubbles (a linear field is its own P1 part)."""
+    vals = field(g.coords)                      # (nverts, dim)
+    nf = g.faces()[0].shape[0]
+    return np.concatenate([vals.T.ravel(), np.zeros(nf)])
+
+
+@pytest.mark.parametrize("recon,velocity", [(1, "const"), (2, "const"), (2, "linear")])
+def test_oracle_p_robust_exact_velocity(G, O, recon, velocity):
+    """The reference's p-robust Stokes test (test/runtests.jl:684-723,
+    exact_functions_stokes2D): velocity (y^k + 1, x^k - 1) of order k = 0
+    (BR + RT0, BR + BDM1) or 1 (BR + BDM1), pressure x^3 + y^3 - 1/2,
+    f = grad p, boundary data the exact velocity.  The discrete velocity is
+    exact (the reference checks its L2 error < 6e-12)."""
+    g = G.grid_unitsquare(4)
+    k = 0 if velocity == "const" else 1
+    exact = lambda X: np.stack([X[:, 1] ** k + 1, X[:, 0] ** k - 1], axis=1)   # noqa: E731
+    terms = np.array([(0, 3.0, 2, 0, 0), (1, 3.0, 0, 2, 0)])
+    ub = br_linear_interpolant(g, exact)
+    u, p, fixed = O.stokes_iterated_penalty(g, 1.0, 1e4, terms, sweeps=8, recon=recon, bonus_quadorder=2,
+                                            u_boundary=ub)
+    assert np.max(np.abs(u - ub)) < 1e-10
+
+
 @pytest.mark.parametrize("recon", [1, 2])   # BR->RT0, BR->BDM1
 def test_oracle_br_rhs_of_gradient_is_in_range_of_divergence(G, O, recon):
     """(grad phi, R v) = -(pi_0 phi, div v) for v vanishing on the boundary:

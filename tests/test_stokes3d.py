@@ -52,6 +52,30 @@ def test_oracle_3d_hydrostatic_velocity_is_zero(G, O, bonus):
         assert np.max(np.abs(p - target)) < 1e-9 * np.max(np.abs(target)), nu
 
 
+def test_oracle_3d_p_robust_exact_velocity(G, O):
+    """The reference's p-robust Stokes test in 3D (test/runtests.jl:684-723,
+    H1BR{3} + L2P0 + HDIVRT0{3}, exact_functions_stokes3D(0, 3)): velocity
+    (2, 0, 1), pressure x^3 + y^3 + z^3 - 3/4, f = grad p (rhs bonus 2:
+    order 5, the symmetric tetrahedral rule), boundary data the exact
+    velocity.  The discrete velocity is exact."""
+    g = G.grid_unitcube_kuhn(2)
+    terms = np.array([(0, 3.0, 2, 0, 0), (1, 3.0, 0, 2, 0), (2, 3.0, 0, 0, 2)])
+    nf = g.faces()[0].shape[0]
+    ub = np.concatenate([np.full(g.nverts, 2.0), np.zeros(g.nverts), np.ones(g.nverts), np.zeros(nf)])
+    u, p, fixed = O.stokes_iterated_penalty(g, 1.0, 1e4, terms, sweeps=8, bonus_quadorder=2, u_boundary=ub)
+    assert np.max(np.abs(u - ub)) < 1e-10
+    # the pressure is the cell mean of x^3 + y^3 + z^3 (up to the constant) -- order-3
+    # rule of the oracle, exact for cubics
+    x, w, _ = O.qrule(3, 3)
+    X = g.coords[g.cells]
+    A = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))
+    pts = X[:, None, 0, :] + np.einsum("ckj,qj->cqk", A, x)
+    pm = (pts ** 3).sum(axis=2) @ w
+    vol = g.cell_volumes()
+    pm -= np.dot(vol, pm) / vol.sum()
+    assert np.max(np.abs(p - pm)) < 1e-9 * np.max(np.abs(pm))
+
+
 def test_oracle_3d_rhs_of_gradient_is_in_range_of_divergence(G, O):
     """(grad phi, R v) = -(pi_0 phi, div v) for every v vanishing on the boundary."""
     g = G.grid_unitcube_kuhn(2)
