@@ -54,7 +54,22 @@ struct BatchDev {
     double *relres;
     double lambda, sweep_tol, reltol, delta;
     int sweeps, maxit, mixed, split;
+    int ld;   // local velocity DoFs per cell: 9 (H1BR{2}) or 16 (H1BR{3})
 };
+
+// sum_I Dv[c][I] u[celldofs[c][I]] in ascending I (int_T div u for the
+// cell's velocity DoFs)
+template <int LD, typename T, typename V>
+__device__ __forceinline__ T cell_div_t(const T *Dv, const int32_t *celldofs, const V *u, int c) {
+    T a = T(0);
+#pragma unroll
+    for (int I = 0; I < LD; I++) a += Dv[(size_t)c * LD + I] * u[celldofs[(size_t)c * LD + I]];
+    return a;
+}
+template <typename T, typename V>
+__device__ __forceinline__ T cell_div(const BatchDev &d, const T *Dv, const V *u, int c) {
+    return d.ld == 9 ? cell_div_t<9>(Dv, d.celldofs, u, c) : cell_div_t<16>(Dv, d.celldofs, u, c);
+}
 
 template <int NV>
 __device__ __forceinline__ void bsum(double *v, double *sh) {
@@ -282,9 +297,7 @@ __device__ __forceinline__ float block_apply_split(const BatchDev &d, int r0, in
     const int tid = threadIdx.x, bs = blockDim.x;
     const float *p = d.p32;
     for (int c = c0 + tid; c < c1; c += bs) {
-        float a = 0.f;
-#pragma unroll
-        for (int I = 0; I < 9; I++) a += d.Dv32[(size_t)c * 9 + I] * p[d.celldofs[(size_t)c * 9 + I]];
+        const float a = cell_div(d, (const float *)d.Dv32, p, c);
         d.s32[c] = d.w32[c] * a;
     }
     __syncthreads();
@@ -312,7 +325,7 @@ __device__ __forceinline__ float block_apply_split(const BatchDev &d, int r0, in
             const int qb = d.inc_ptr[r], qe = d.inc_ptr[r + 1];
             for (int q = qb + lane; q < qe; q += TPR) {
                 const int cell = d.inc_cell[q];
-                sm += d.Dv32[(size_t)cell * 9 + d.inc_loc[q]] * d.s32[cell];
+                sm += d.Dv32[(size_t)cell * d.ld + d.inc_loc[q]] * d.s32[cell];
             }
         }
 #pragma unroll
@@ -474,7 +487,7 @@ __device__ __forceinline__ void block_sweep_rhs(const BatchDev &d, int r0, int r
         if (!d.fixed[i])
             for (int q = d.inc_ptr[i]; q < d.inc_ptr[i + 1]; q++) {
                 const int cell = d.inc_cell[q];
-                acc += d.Dv[(size_t)cell * 9 + d.inc_loc[q]] * d.p[cell];
+                acc += d.Dv[(size_t)cell * d.ld + d.inc_loc[q]] * d.p[cell];
             }
         d.rhs[i] = acc;
     }
@@ -488,8 +501,7 @@ __device__ __forceinline__ bool block_pressure_update(const BatchDev &d, int c0,
     const int tid = threadIdx.x, bs = blockDim.x;
     double m[3] = {0, 0, 0};   // sum vol*p_new, sum vol
     for (int c = c0 + tid; c < c1; c += bs) {
-        double dv = 0;
-        for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
+        const double dv = cell_div(d, d.Dv, (const double *)d.u, c);
         const double dp = d.lambda * dv / d.vol[c];
         const double pn = d.p[c] - dp;
         d.p[c] = pn;
@@ -506,8 +518,7 @@ __device__ __forceinline__ bool block_pressure_update(const BatchDev &d, int c0,
     }
     // change of the pressure in this sweep (after the mean shift) from the divergence
     for (int c = c0 + tid; c < c1; c += bs) {
-        double dv = 0;
-        for (int I = 0; I < 9; I++) dv += d.Dv[(size_t)c * 9 + I] * d.u[d.celldofs[(size_t)c * 9 + I]];
+        const double dv = cell_div(d, d.Dv, (const double *)d.u, c);
         const double dp = d.lambda * dv / d.vol[c];
         cmp[0] += d.vol[c] * dp * dp;
     }
@@ -548,9 +559,9 @@ __global__ void __launch_bounds__(512, 2) k_stokes_batch(BatchDev d) {
         for (int c = c0 + tid; c < c1; c += bs) {
             d.p[c] = 0.0;
             if (d.mixed && d.split) {
-                for (int I = 0; I < 9; I++) {
-                    const size_t k9 = (size_t)c * 9 + I;
-                    d.Dv32[k9] = d.fixed[d.celldofs[k9]] ? 0.f : (float)d.Dv[k9];
+                for (int I = 0; I < d.ld; I++) {
+                    const size_t k = (size_t)c * d.ld + I;
+                    d.Dv32[k] = d.fixed[d.celldofs[k]] ? 0.f : (float)d.Dv[k];
                 }
                 d.w32[c] = (float)(d.lambda / d.vol[c]);
             }
@@ -1368,7 +1379,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
         d.z32 = (float *)take((size_t)n * 4);
         d.p32 = (float *)take((size_t)n * 4);
         d.s32 = (float *)take((size_t)nc * 4);
-        d.Dv32 = (float *)take((size_t)nc * 36);
+        d.Dv32 = (float *)take((size_t)nc * s->ldofs * 4);
         d.w32 = (float *)take((size_t)nc * 4);
     }
     d.queue = (int *)take(64);
@@ -1386,7 +1397,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     if (!rc) rc = grmp_br_divergence(s, &Dv, &vol);
     if (rc) {
         release();
-        grmp_free(ctx, Dv, (size_t)nc * 72);
+        grmp_free(ctx, Dv, (size_t)nc * s->ldofs * 8);
         grmp_free(ctx, vol, (size_t)nc * 8);
         return rc;
     }
@@ -1403,7 +1414,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess || hbad) {
         release();
-        grmp_free(ctx, Dv, (size_t)nc * 72);
+        grmp_free(ctx, Dv, (size_t)nc * s->ldofs * 8);
         grmp_free(ctx, vol, (size_t)nc * 8);
         return e != cudaSuccess ? grmp_cuda_fail(ctx, e, "batch check")
                                 : grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: a row couples two problems");
@@ -1420,6 +1431,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     d.inc_cell = s->d_inc_cell;
     d.inc_loc = s->d_inc_loc;
     d.celldofs = s->d_celldofs;
+    d.ld = s->ldofs;
     d.Dv = Dv;
     d.vol = vol;
     d.fixed = A->d_fixed;
@@ -1510,7 +1522,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             release();
-            grmp_free(ctx, Dv, (size_t)nc * 72);
+            grmp_free(ctx, Dv, (size_t)nc * s->ldofs * 8);
             grmp_free(ctx, vol, (size_t)nc * 8);
             return rc;
         }
@@ -1538,7 +1550,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     cudaEventDestroy(e1);
     release();
     grmp_free(ctx, dwork, dwork_bytes);
-    grmp_free(ctx, Dv, (size_t)nc * 72);
+    grmp_free(ctx, Dv, (size_t)nc * s->ldofs * 8);
     grmp_free(ctx, vol, (size_t)nc * 8);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "batched Stokes");
     stats->solve_ms = ms;

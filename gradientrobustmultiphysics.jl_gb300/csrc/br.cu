@@ -490,6 +490,7 @@ int br_assemble_t(grmp_matrix A, const BrTerms &bt) {
 int grmp_br3_mask(grmp_space s, int nterms, const grmp_bilinear_term *terms, uint32_t *mask);
 int grmp_br3_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
 int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b);
+int grmp_br3_divergence(grmp_space s, double **Dv, double **vol);
 
 int grmp_br_mask(grmp_space s, int nterms, const grmp_bilinear_term *terms, uint32_t *mask) {
     if (s->mesh->dim == 3) return grmp_br3_mask(s, nterms, terms, mask);
@@ -580,11 +581,11 @@ int grmp_br_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
     return rc;
 }
 
-// cell divergence table Dv [ncells][9] and cell volumes, allocated here
+// cell divergence table Dv [ncells][ldofs] and cell volumes, allocated here
 int grmp_br_divergence(grmp_space s, double **Dv, double **vol) {
     grmp_mesh m = s->mesh;
     grmp_context ctx = m->ctx;
-    if (m->dim != 2) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batched Stokes: H1BR{2} only");
+    if (m->dim == 3) return grmp_br3_divergence(s, Dv, vol);
     int rc = grmp_alloc(ctx, (void **)Dv, (size_t)m->ncells * 9 * 8);
     if (!rc) rc = grmp_alloc(ctx, (void **)vol, (size_t)m->ncells * 8);
     if (rc) return rc;

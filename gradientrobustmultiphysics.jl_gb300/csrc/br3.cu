@@ -266,7 +266,8 @@ __global__ void __launch_bounds__(128) k_br3_rows(int32_t nrows, const int32_t *
 
 // ------------------------------------------------------------------ reconstructed rhs (FP64)
 struct Br3Rhs {
-    const double *par;   // [nt][5] polynomial terms (component, coef, e1, e2, e3)
+    const double *par;   // [ngroups][nt][5] polynomial terms (component, coef, e1, e2, e3)
+    const int32_t *group;   // [ncells] group of each cell, or nullptr (one group)
     int nt;
     double factor;
     int nq;
@@ -305,8 +306,9 @@ __global__ void k_br3_rhs_cells(int ncells, Br3MeshDev m, Br3Rhs r, double *loc)
             for (int j = 0; j < 3; j++) x[k] += A[k][j] * r.xref[q][j];
         }
         double fq[3] = {0, 0, 0};
+        const double *gpar = r.par + (r.group ? (size_t)r.group[cell] * r.nt * 5 : 0);
         for (int t = 0; t < r.nt; t++) {
-            const double *pt = r.par + 5 * t;
+            const double *pt = gpar + 5 * t;
             double v = pt[1];
             for (int j = 0; j < 3; j++)
                 if (pt[2 + j] != 0) v *= pow(x[j], pt[2 + j]);
@@ -331,6 +333,36 @@ __global__ void k_gather_rows_br3(int32_t nrows, const int32_t *inc_ptr, const i
     double acc = b[row];
     for (int p = inc_ptr[row]; p < inc_ptr[row + 1]; p++) acc += loc[(size_t)inc_cell[p] * 16 + inc_loc[p]];
     b[row] = acc;
+}
+
+struct Br3DivTab {
+    int nq;
+    double w[4];
+    double dref[4][8][3];
+};
+
+__global__ void k_br3_div(int ncells, Br3MeshDev m, Br3DivTab t, double *Dv, double *vol_out) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= ncells) return;
+    double X[12], nrm[4][3], fv[4], sg[4];
+    br3_load(m, cell, X, nrm, fv, sg);
+    double A[3][3], G[3][3], vol;
+    simplex_geometry<3, double>(X, G, vol, A);
+    for (int I = 0; I < 16; I++) {
+        double s = 0;
+        for (int q = 0; q < t.nq; q++) {
+            double cv = 0;
+            for (int k = 0; k < 3; k++) {
+                const int si = br3_scalar(I, k);
+                if (si < 0) continue;
+                const double coef = br3_coef(I, k, nrm);
+                for (int j = 0; j < 3; j++) cv += G[k][j] * t.dref[q][si][j] * coef;
+            }
+            s += cv * t.w[q];
+        }
+        Dv[(size_t)cell * 16 + I] = s * vol;
+    }
+    vol_out[cell] = vol;
 }
 
 int br3_terms(grmp_space s, int nterms, const grmp_bilinear_term *terms, Br3Terms *bt,
@@ -474,14 +506,19 @@ int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
     grmp_context ctx = m->ctx;
     if (rhs->test_operator != 1)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR{3} right-hand sides: the RT0 reconstruction only");
-    if (rhs->kind != GRMP_RHS_POLY || rhs->ncomponents != 3 || rhs->cell_group)
+    if (rhs->kind != GRMP_RHS_POLY || rhs->ncomponents != 3)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR{3} reconstructed rhs: 3-component polynomial data only");
-    if (rhs->nparams % 5 || rhs->nparams <= 0 || !rhs->params)
+    const long long ng = rhs->cell_group ? rhs->ngroups : 1;
+    if (ng <= 0 || rhs->nparams <= 0 || rhs->nparams % (5 * ng) || !rhs->params)
         return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "rhs: parameter layout");
-    const int nt = (int)(rhs->nparams / 5);
-    for (int t = 0; t < nt; t++)
+    const int nt = (int)(rhs->nparams / (5 * ng));
+    for (long long t = 0; t < ng * nt; t++)
         if (rhs->params[5 * t] < 0 || rhs->params[5 * t] > 2)
             return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "rhs: polynomial component out of range");
+    if (rhs->cell_group)
+        for (int c = 0; c < m->ncells; c++)
+            if (rhs->cell_group[c] < 0 || rhs->cell_group[c] >= ng)
+                return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "rhs: cell group out of range");
     Br3Rhs r;
     std::memset(&r, 0, sizeof(r));
     RefTables *rt = new RefTables;
@@ -499,11 +536,14 @@ int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
     r.nt = nt;
     r.factor = rhs->factor;
     double *dpar = nullptr;
+    int32_t *dgrp = nullptr;
     rc = grmp_upload(ctx, &dpar, rhs->params, (size_t)rhs->nparams);
+    if (!rc && rhs->cell_group) rc = grmp_upload(ctx, &dgrp, rhs->cell_group, (size_t)m->ncells);
     const size_t ncl = (size_t)m->ncells * 16;
     if (!rc && !s->d_locbuf) rc = grmp_alloc(ctx, (void **)&s->d_locbuf, ncl * 8);
     if (!rc) {
         r.par = dpar;
+        r.group = dgrp;
         k_br3_rhs_cells<<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, br3_mesh(m), r, s->d_locbuf);
         GRMP_LAUNCHED(ctx);
         k_gather_rows_br3<<<nblk(s->ndofs), TPB, 0, ctx->stream>>>(s->ndofs, s->d_inc_ptr, s->d_inc_cell,
@@ -514,5 +554,36 @@ int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
         if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "H1BR{3} rhs");
     }
     grmp_free(ctx, dpar, (size_t)rhs->nparams * 8);
+    grmp_free(ctx, dgrp, (size_t)m->ncells * 4);
     return rc;
+}
+
+// Cell divergence table of the batched Stokes solver: Dv[cell][I] =
+// int_T div phi_I with the order-2 rule of the velocity-pressure coupling
+// (BilinearForm([Divergence, Identity]): polyorder 3 - 1 + 0), vol[cell] = |T|.
+int grmp_br3_divergence(grmp_space s, double **Dv, double **vol) {
+    grmp_mesh m = s->mesh;
+    grmp_context ctx = m->ctx;
+    Br3DivTab t;
+    std::memset(&t, 0, sizeof(t));
+    RefTables *rt = new RefTables;
+    int rc = grmp_tables(3, GRMP_FE_H1BR, 2, rt);
+    if (rc || rt->nq > 4 || rt->nb != 8) {
+        delete rt;
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR{3} divergence tables");
+    }
+    t.nq = rt->nq;
+    for (int q = 0; q < rt->nq; q++) {
+        t.w[q] = rt->w[q];
+        for (int a = 0; a < 8; a++)
+            for (int j = 0; j < 3; j++) t.dref[q][a][j] = rt->derivs[q][a][j];
+    }
+    delete rt;
+    rc = grmp_alloc(ctx, (void **)Dv, (size_t)m->ncells * 16 * 8);
+    if (!rc) rc = grmp_alloc(ctx, (void **)vol, (size_t)m->ncells * 8);
+    if (rc) return rc;
+    k_br3_div<<<nblk(m->ncells), TPB, 0, ctx->stream>>>(m->ncells, br3_mesh(m), t, *Dv, *vol);
+    GRMP_LAUNCHED(ctx);
+    GRMP_CUDA(ctx, cudaGetLastError());
+    return GRMP_OK;
 }

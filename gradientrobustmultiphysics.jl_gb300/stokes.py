@@ -22,12 +22,12 @@ import numpy as np
 from . import _lib as L
 from . import api
 from .fespace import FESpace, H1BR, FE_H1BR
-from .mesh import SimplexMesh, grid_unitsquare
+from .mesh import SimplexMesh, grid_unitcube_kuhn, grid_unitsquare
 
 
 class BatchedMesh(SimplexMesh):
-    """Disjoint union of 2D meshes with the faces of each part kept (face
-    numbering, normals and signs are those of the part)."""
+    """Disjoint union of meshes of one dimension with the faces of each part
+    kept (face numbering, normals and signs are those of the part)."""
 
     def __init__(self, parts):
         coords, cells, cfaces, normals, fvols, signs = [], [], [], [], [], []
@@ -51,7 +51,7 @@ class BatchedMesh(SimplexMesh):
             self.face_offsets.append(foff)
         super().__init__(np.concatenate(coords), np.concatenate(cells).astype(np.int32), name=f"batch{len(parts)}")
         self.parts = list(parts)
-        self._faces = (np.zeros((foff, 2), dtype=np.int32), np.concatenate(cfaces).astype(np.int32))
+        self._faces = (np.zeros((foff, self.dim), dtype=np.int32), np.concatenate(cfaces).astype(np.int32))
         self._facegeo = (np.concatenate(normals), np.concatenate(fvols), np.concatenate(signs))
 
     def faces(self):
@@ -62,17 +62,17 @@ class BatchedMesh(SimplexMesh):
 
 
 class BatchedBRSpace(FESpace):
-    """H1BR{2} over a BatchedMesh with per-problem contiguous DoF blocks."""
+    """H1BR{d} over a BatchedMesh with per-problem contiguous DoF blocks."""
 
     def __init__(self, bmesh: BatchedMesh):
-        self.FEType = H1BR(2)
+        self.FEType = H1BR(bmesh.dim)
         self.xgrid = bmesh
-        self.name = "H1BR{2} batch"
+        self.name = f"H1BR{{{bmesh.dim}}} batch"
         cds, fixed = [], []
         self.row_offsets = [0]
         off = 0
         for g in bmesh.parts:
-            S = FESpace(H1BR(2), g)
+            S = FESpace(H1BR(bmesh.dim), g)
             cds.append(S.celldofs.astype(np.int64) + off)
             fixed.append(S.boundary_dofs().astype(np.int64) + off)
             off += S.ndofs
@@ -118,6 +118,45 @@ def grad_plus_curl_terms(phi: dict, psi: dict):
     return np.array(out, dtype=np.float64)
 
 
+def cubic_coefficients_3d(rng: np.random.Generator):
+    """Coefficients a_ijk of a cubic sum_{i+j+k<=3} a_ijk x^i y^j z^k."""
+    return {(i, j, k): rng.standard_normal() for i in range(4) for j in range(4) for k in range(4) if i + j + k <= 3}
+
+
+def grad_plus_curl_terms_3d(phi: dict, psi):
+    """Polynomial records (component, coef, e1, e2, e3) of
+    f = grad(phi) + curl(psi) for a cubic phi and a cubic vector psi
+    (curl psi = (d2 psi3 - d3 psi2, d3 psi1 - d1 psi3, d1 psi2 - d2 psi1));
+    degree <= 2.  Always 30 records (the 10 monomials of degree <= 2 per
+    component)."""
+    acc = {}
+
+    def add(c, coef, e):
+        acc[(c, e)] = acc.get((c, e), 0.0) + coef
+
+    def deriv(poly, j):
+        for e, a in poly.items():
+            if e[j] > 0:
+                ee = list(e)
+                ee[j] -= 1
+                yield tuple(ee), e[j] * a
+
+    for c in range(3):
+        for e, a in deriv(phi, c):
+            add(c, a, e)
+    # (component, psi index, derivative direction, sign) of the curl
+    for c, m, j, sg in ((0, 2, 1, 1), (0, 1, 2, -1), (1, 0, 2, 1), (1, 2, 0, -1), (2, 1, 0, 1), (2, 0, 1, -1)):
+        for e, a in deriv(psi[m], j):
+            add(c, sg * a, e)
+    out = []
+    for c in range(3):
+        for i in range(3):
+            for j in range(3 - i):
+                for k in range(3 - i - j):
+                    out.append((c, acc.get((c, (i, j, k)), 0.0), i, j, k))
+    return np.array(out, dtype=np.float64)
+
+
 @dataclass
 class StokesBatchProblem:
     sizes: np.ndarray
@@ -132,22 +171,33 @@ class StokesBatchProblem:
     def nproblems(self) -> int:
         return len(self.sizes)
 
+    @property
+    def dim(self) -> int:
+        return self.mesh.dim
+
 
 def make_batch(nproblems: int = 2048, nmin: int = 8, nmax: int = 96, seed: int = 0, lam: float = 1e4,
-               sizes=None, nus=None) -> StokesBatchProblem:
-    """Seeded batch: n log-uniform in [nmin, nmax] (n x n squares, 2 n^2
-    triangles), nu log-uniform in [1e-4, 1], f = grad(cubic) + curl(cubic)."""
+               sizes=None, nus=None, dim: int = 2) -> StokesBatchProblem:
+    """Seeded batch: n log-uniform in [nmin, nmax] (2D: n x n squares, 2 n^2
+    triangles; 3D: n^3 cubes, 6 n^3 Kuhn tetrahedra), nu log-uniform in
+    [1e-4, 1], f = grad(cubic) + curl(cubic)."""
+    if dim not in (2, 3):
+        raise ValueError("dim must be 2 or 3")
     rng = np.random.default_rng(seed)
     if sizes is None:
         sizes = np.rint(np.exp(rng.uniform(np.log(nmin), np.log(nmax), nproblems))).astype(int)
     if nus is None:
         nus = np.exp(rng.uniform(np.log(1e-4), np.log(1.0), len(sizes)))
-    terms = np.stack([grad_plus_curl_terms(cubic_coefficients(rng), cubic_coefficients(rng)) for _ in sizes])
+    if dim == 2:
+        terms = np.stack([grad_plus_curl_terms(cubic_coefficients(rng), cubic_coefficients(rng)) for _ in sizes])
+    else:
+        terms = np.stack([grad_plus_curl_terms_3d(cubic_coefficients_3d(rng),
+                                                  [cubic_coefficients_3d(rng) for _ in range(3)]) for _ in sizes])
     cache = {}
     parts = []
     for n in sizes:
         if n not in cache:
-            cache[n] = grid_unitsquare(int(n))
+            cache[n] = grid_unitsquare(int(n)) if dim == 2 else grid_unitcube_kuhn(int(n))
         parts.append(cache[n])
     bm = BatchedMesh(parts)
     V = BatchedBRSpace(bm)
@@ -200,7 +250,7 @@ class StokesBatchSystem:
         self.bf.fill(0.0)
         r = L.Rhs()
         r.kind = L.RHS_POLY
-        r.ncomponents = 2
+        r.ncomponents = self.prob.dim
         par = np.ascontiguousarray(self.prob.terms, dtype=np.float64).ravel()
         grp = np.ascontiguousarray(np.repeat(np.arange(self.prob.nproblems, dtype=np.int32),
                                              np.diff(self.prob.mesh.cell_offsets)))

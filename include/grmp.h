@@ -381,8 +381,8 @@ typedef struct {
  *   velocity:  (nu grad u, grad v) + lambda (div R u, div R v) = (f, R v) + (p, div v)
  *   pressure:  p <- p - lambda * (1/|T|) int_T div u,  then mean(p) = 0
  *              (FixedIntegralMean, src/globalconstraints.jl:23-44).
- * A: the assembled velocity matrix over an H1BR space (terms LAPLACE and
- * RDIVRDIV) with Dirichlet rows eliminated; bf: the reconstructed
+ * A: the assembled velocity matrix over an H1BR{2} or H1BR{3} space (terms
+ * LAPLACE and RDIVRDIV) with Dirichlet rows eliminated; bf: the reconstructed
  * right-hand side (f, R v) with the same rows zeroed.  u (velocity, per row)
  * and p (pressure, per cell) are overwritten.  One thread block owns one
  * problem for the whole solve, so a problem's result is bit-identical alone

@@ -238,3 +238,80 @@ def test_br3_velocity_solve_matches_oracle(G, O, ctx, mode):
     u = x.entries
     assert np.max(np.abs(u[fixed])) == 0.0
     assert np.linalg.norm(u - uref) <= 1e-9 * np.linalg.norm(uref), st
+
+
+# ------------------------------------------------------------ batched, 3D
+def _field(terms, X):
+    f = np.zeros((X.shape[0], 3))
+    for c, a, e1, e2, e3 in terms:
+        f[:, int(c)] += a * X[:, 0] ** e1 * X[:, 1] ** e2 * X[:, 2] ** e3
+    return f
+
+
+def test_grad_plus_curl_terms_3d(G):
+    """The 3D load generator: 30 records; grad(phi) part matches finite
+    differences of phi, the curl part is divergence-free."""
+    from grmp_gb300 import stokes as S
+    rng = np.random.default_rng(1)
+    phi = S.cubic_coefficients_3d(rng)
+    psi = [S.cubic_coefficients_3d(rng) for _ in range(3)]
+    zero = {e: 0.0 for e in phi}
+    tg = S.grad_plus_curl_terms_3d(phi, [zero, zero, zero])
+    tc = S.grad_plus_curl_terms_3d(zero, psi)
+    assert tg.shape == (30, 5) and tc.shape == (30, 5)
+    X = rng.random((20, 3))
+    P = lambda Y: sum(a * Y[:, 0] ** i * Y[:, 1] ** j * Y[:, 2] ** k for (i, j, k), a in phi.items())  # noqa: E731
+    h = 1e-6
+    fd = np.stack([(P(X + h * np.eye(3)[j]) - P(X - h * np.eye(3)[j])) / (2 * h) for j in range(3)], axis=1)
+    assert np.max(np.abs(_field(tg, X) - fd)) < 1e-7
+    div = sum((_field(tc, X + h * np.eye(3)[j])[:, j] - _field(tc, X - h * np.eye(3)[j])[:, j]) / (2 * h)
+              for j in range(3))
+    assert np.max(np.abs(div)) < 1e-7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "direct"])
+def test_batch3d_matches_oracle(G, O, ctx, mode):
+    """3D batched iterated penalty (H1BR{3} / P0, RT0-reconstructed load of
+    order 3 + 2) against the oracle's sparse-direct sweeps per problem."""
+    from grmp_gb300 import stokes as S
+    sizes = [2, 3, 2]
+    nus = [1.0, 0.5, 0.3] if mode == "mixed" else [1.0, 0.2, 0.05]
+    prob = S.make_batch(sizes=np.array(sizes), nus=np.array(nus), seed=7, dim=3)
+    sysd = S.StokesBatchSystem(ctx, prob, mixed=(mode == "mixed"), direct=(mode == "direct"))
+    sysd.assemble()
+    st = sysd.solve(sweeps=8, reltol=1e-12 if mode == "mixed" else 1e-13)
+    u, p = sysd.velocity(), sysd.pressure()
+    for k, g in enumerate(prob.mesh.parts):
+        uo, po, _ = O.stokes_iterated_penalty(g, nus[k], prob.lam, prob.terms[k], sweeps=8)
+        r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
+        c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
+        eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
+        ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
+        assert eu < 1e-8 and ep < 1e-8, (k, eu, ep, st)
+
+
+@pytest.mark.gpu
+def test_batch3d_hydrostatic_and_alone_vs_mix(G, ctx):
+    """A gradient load gives a zero velocity (pressure robustness) through
+    the batched 3D solver; a problem's bits are the same alone and in the
+    batch."""
+    from grmp_gb300 import stokes as S
+    sizes, nus = [2, 3, 2], [1.0, 1e-3, 0.1]
+    big = S.make_batch(sizes=np.array(sizes), nus=np.array(nus), seed=3, dim=3)
+    big.terms[1] = S.grad_plus_curl_terms_3d(S.cubic_coefficients_3d(np.random.default_rng(2)),
+                                             [{(0, 0, 0): 0.0}] * 3)
+    sb = S.StokesBatchSystem(ctx, big, direct=True)
+    sb.assemble()
+    sb.solve(sweeps=8, reltol=1e-13)
+    u, p = sb.velocity(), sb.pressure()
+    r0, r1 = big.V.row_offsets[1], big.V.row_offsets[2]
+    assert np.max(np.abs(u[r0:r1])) < 1e-10
+    alone = S.make_batch(sizes=np.array([sizes[1]]), nus=np.array([nus[1]]), seed=3, dim=3)
+    alone.terms = big.terms[1:2].copy()
+    sa = S.StokesBatchSystem(ctx, alone, direct=True)
+    sa.assemble()
+    sa.solve(sweeps=8, reltol=1e-13)
+    c0, c1 = big.mesh.cell_offsets[1], big.mesh.cell_offsets[2]
+    assert np.array_equal(sa.velocity(), u[r0:r1])
+    assert np.array_equal(sa.pressure(), p[c0:c1])
