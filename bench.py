@@ -448,14 +448,21 @@ def run_stokes(args):
     torch.cuda.set_device(dist.local)
     ctx = G.GB300Context(dist.local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dist.local)
-    prob = S.make_batch(nproblems=args.nprob, seed=args.seed + dist.rank)
+    if args.dim == 3:
+        # n^3 Kuhn cubes, n log-uniform in [2, 6] (201 to 3,837 velocity DoFs per problem; the
+        # per-problem direct solver stages its largest front in shared memory, 969 DoFs at n = 6)
+        prob = S.make_batch(nproblems=args.nprob, nmin=2, nmax=6, seed=args.seed + dist.rank, dim=3)
+    else:
+        prob = S.make_batch(nproblems=args.nprob, seed=args.seed + dist.rank)
     sysd = S.StokesBatchSystem(ctx, prob, mixed=False, direct=True)
     ndofs = prob.V.ndofs + prob.mesh.ncells
 
     def step():
         sysd.assemble()
-        return sysd.solve(sweeps=args.sweeps, reltol=args.stokes_reltol, maxiter=1, sweep_tol=0.0,
-                          raise_on_error=False)
+        st = sysd.solve(sweeps=args.sweeps, reltol=args.stokes_reltol, maxiter=1, sweep_tol=0.0,
+                        raise_on_error=False)
+        ctx.check(st["rc"])   # a refused or failed solve ends the run, it is never timed
+        return st
 
     for _ in range(max(3, args.warmup)):
         st = step()
@@ -495,7 +502,8 @@ def run_stokes(args):
             "unit": "DoF/s", "n_gpus": dist.ws, "steps": args.steps, "warmup": max(3, args.warmup),
             "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"stokes_BR_P0_batch{args.nprob}", "velocity_dofs": prob.V.ndofs,
+            "config": {"workload": f"stokes_BR_P0_batch{args.nprob}" + ("_3d" if args.dim == 3 else ""),
+                       "velocity_dofs": prob.V.ndofs,
                        "cells": prob.mesh.ncells, "sweeps": args.sweeps, "reltol": args.stokes_reltol,
                        "solver": "FP64 multifrontal Cholesky per problem, factored once per step"},
             "latency_ms": {"p50": p[len(p) // 2], "p99": p[min(len(p) - 1, int(0.99 * len(p)))]},
@@ -579,6 +587,7 @@ def main():
                          "(plain FP64 / FP32 factor preconditioning FP64 CG); default per workload")
     ap.add_argument("--nprob", type=int, default=2048)
     ap.add_argument("--sweeps", type=int, default=6)
+    ap.add_argument("--dim", type=int, default=2, choices=[2, 3], help="stokes-batch: 2D or 3D problems")
     ap.add_argument("--stokes-reltol", type=float, default=1e-12)
     ap.add_argument("--nreq", type=int, default=64)
     ap.add_argument("--slots", type=int, default=4)

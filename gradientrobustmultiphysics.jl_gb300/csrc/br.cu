@@ -325,8 +325,8 @@ __global__ void k_br_rhs_cells(int ncells, BrMeshDev m, BrRhs r, double *loc) {
         for (int t = 0; t < r.nt; t++) {
             const int c = (int)par[5 * t];
             double v = par[5 * t + 1];
-            if (par[5 * t + 2] != 0) v *= pow(x[0], par[5 * t + 2]);
-            if (par[5 * t + 3] != 0) v *= pow(x[1], par[5 * t + 3]);
+            if (par[5 * t + 2] != 0) v *= poly_pow(x[0], par[5 * t + 2]);
+            if (par[5 * t + 3] != 0) v *= poly_pow(x[1], par[5 * t + 3]);
             f[c] += v;
         }
         for (int i = 0; i < 9; i++) {

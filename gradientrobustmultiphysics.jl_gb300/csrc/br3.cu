@@ -311,7 +311,7 @@ __global__ void k_br3_rhs_cells(int ncells, Br3MeshDev m, Br3Rhs r, double *loc)
             const double *pt = gpar + 5 * t;
             double v = pt[1];
             for (int j = 0; j < 3; j++)
-                if (pt[2 + j] != 0) v *= pow(x[j], pt[2 + j]);
+                if (pt[2 + j] != 0) v *= poly_pow(x[j], pt[2 + j]);
             fq[(int)pt[0]] += v;
         }
         for (int i = 0; i < 16; i++) {

@@ -107,6 +107,19 @@ __device__ __forceinline__ int voigt_slot(int dim, int c, int k) {
     return m[k + c * 3];
 }
 
+// x^e for the exponents of polynomial data: integer e in [1, 8] by
+// repeated multiplication left to right (x*x*x, as Julia's literal powers
+// x^2, x^3 of the reference's data functions evaluate), pow otherwise.
+__host__ __device__ __forceinline__ double poly_pow(double x, double e) {
+    const int k = (int)e;
+    if ((double)k == e && k >= 1 && k <= 8) {
+        double r = x;
+        for (int i = 1; i < k; i++) r = r * x;
+        return r;
+    }
+    return pow(x, e);
+}
+
 // Data functions of the linear forms and item integrators evaluated on device
 // (constant, per cell, Fourier series, polynomial; grmp_rhs_kind).  f gets
 // r.ncomp values.
@@ -142,7 +155,7 @@ __device__ __forceinline__ void rhs_eval(const RhsDev &r, int dim, int cell, con
             double v = r.par[5 * t + 1];
             for (int j = 0; j < dim; j++) {
                 double e = r.par[5 * t + 2 + j];
-                if (e != 0) v *= pow(x[j], e);
+                if (e != 0) v *= poly_pow(x[j], e);
             }
             f[c] += v;
         }

@@ -668,6 +668,22 @@ enum {
     OR_RHS_POLY = 3      /* f_c = sum_t coef_t x^e1 y^e2 z^e3 (vector, "X")      */
 };
 
+
+/* x^e of polynomial data: integer e in [1, 8] by repeated multiplication
+ * left to right (x*x*x: Julia's literal powers x^2, x^3 in the reference's
+ * data functions), e = 0 gives 1, other exponents pow. */
+static double or_pow(double x, double e)
+{
+    const int k = (int)e;
+    if (e == 0) return 1.0;
+    if ((double)k == e && k >= 1 && k <= 8) {
+        double r = x;
+        for (int i = 1; i < k; i++) r = r * x;
+        return r;
+    }
+    return pow(x, e);
+}
+
 /* Evaluate f at a physical point: eval_trafo! gives x = x0 + A xref. */
 static void rhs_eval(int kind, int dim, int ncomp, const double *par, int npar, int cell, const double *x, double *f)
 {
@@ -692,7 +708,7 @@ static void rhs_eval(int kind, int dim, int ncomp, const double *par, int npar, 
     for (int t = 0; t < nt; t++) {
         int c = (int)par[5 * t];
         double v = par[5 * t + 1];
-        for (int j = 0; j < dim; j++) v *= pow(x[j], par[5 * t + 2 + j]);
+        for (int j = 0; j < dim; j++) v *= or_pow(x[j], par[5 * t + 2 + j]);
         f[c] += v;
     }
 }
