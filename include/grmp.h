@@ -128,7 +128,9 @@ typedef enum {
     GRMP_OP_HOOKE = 3,     /* (C eps(u), eps(v)) with SymmetricGradient{1}: HookStiffnessOperator2D/3D
                               src/pdeoperators.jl:256-315; param[0] = mu, param[1] = lambda            */
     GRMP_OP_RDIVRDIV = 4   /* (div R u, div R v), R = BR -> RT0 reconstruction (ReconstructionDivergence,
-                              src/feevaluator_h1.jl:409-437); iterated-penalty term                  */
+                              src/feevaluator_h1.jl:409-437); iterated-penalty term.  In 3D the RT0
+                              basis is mapped with A phi / |det A| (times the cell-face sign), so
+                              div R u is the cell mean of div u on tetrahedra of either orientation */
 } grmp_op_kind;
 
 /* One operator term.  Assembly of a list of terms adds them into one matrix,
