@@ -250,6 +250,42 @@ def workload_name(args) -> str:
     return WORKLOADS[args.workload][0].format(n=args.n)
 
 
+def setup_timings(ctx, FES, prob) -> dict:
+    """One-time setup costs, reported beside the per-step numbers (which
+    exclude them): the host's mesh generation and dofmap + boundary DoFs
+    (the FESpace constructor's role) against the same dofmap and boundary
+    DoFs built on the device from the uploaded mesh (grmp_space_create_on_device,
+    grmp_space_boundary_dofs; results checked equal to the host's)."""
+    from grmp_gb300 import fespace as F
+    from grmp_gb300 import mesh as M
+    g = FES.xgrid
+    out = {}
+    n = getattr(prob, "meta", {}).get("n")
+    if n:
+        t0 = time.perf_counter()
+        g2 = M.grid_unitcube_kuhn(n) if g.dim == 3 else M.grid_unitsquare(n)
+        out["mesh_host"] = 1e3 * (time.perf_counter() - t0)
+    else:
+        g2 = type(g)(g.coords, g.cells, name="copy")
+    t0 = time.perf_counter()
+    H = F.FESpace(FES.FEType, g2)
+    fixed_h = H.boundary_dofs()
+    out["dofmap_boundary_host"] = 1e3 * (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    ctx.mesh(g2)
+    out["mesh_upload"] = 1e3 * (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    D = ctx.space_on_device(FES.FEType, g2, download=False)
+    fixed_d = ctx.boundary_dofs(D)
+    out["dofmap_boundary_device"] = 1e3 * (time.perf_counter() - t0)
+    cd = np.empty_like(H.celldofs)
+    ctx.check(ctx.lib.grmp_space_celldofs(ctx.space(D), cd.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+    if D.ndofs != H.ndofs or not np.array_equal(cd, H.celldofs) or not np.array_equal(fixed_d, fixed_h):
+        raise RuntimeError("device dofmap differs from the host's")
+    ctx.release(D)
+    return out
+
+
 def run_ours(args):
     dist = Dist()
     G = _package()
@@ -265,6 +301,7 @@ def run_ours(args):
     prob = make_problem(P, args, args.seed + dist.rank)
     FES = prob.FES
     ndofs = FES.ndofs
+    setup_ms = setup_timings(ctx, FES, prob)
     op = prob.operators[0]
     dev_terms = None
     if op.cell_coef is not None:
@@ -281,7 +318,9 @@ def run_ours(args):
         t.cell_coef = ctypes.cast(kptr, ctypes.POINTER(ctypes.c_double))
         t.coef_on_device = 1
         dev_terms = (L.BilinearTerm * 1)(t)
+    t0 = time.perf_counter()
     A = G.FEMatrix(ctx, FES, prob.operators)
+    setup_ms["pattern_device"] = 1e3 * (time.perf_counter() - t0)
     b = G.FEVector(ctx, FES)
     x = G.FEVector(ctx, FES)
     nnz = A.nnz
@@ -426,7 +465,8 @@ def run_ours(args):
                                                   if o.cell_coef is not None) + prob.rhs.f.params.size * 8),
                     "d2h_bytes_per_step": int(ndofs * 8)},
             "gpu_launches": mixed["launches"],
-            "clocks": mixed["clocks"]}
+            "clocks": mixed["clocks"],
+            "setup_ms": setup_ms}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

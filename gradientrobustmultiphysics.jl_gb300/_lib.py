@@ -108,6 +108,9 @@ SIGNATURES = {
     "grmp_space_create": ([_vp, ctypes.c_int, ctypes.c_int, _pi32, _i32, ctypes.POINTER(_vp)], ctypes.c_int),
     "grmp_space_destroy": ([_vp], ctypes.c_int),
     "grmp_space_ndofs4cell": ([_vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "grmp_space_create_on_device": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp), _pi32], ctypes.c_int),
+    "grmp_space_celldofs": ([_vp, _pi32], ctypes.c_int),
+    "grmp_space_boundary_dofs": ([_vp, _i32, _pi32, _pi32], ctypes.c_int),
     "grmp_reference_tables": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                ctypes.POINTER(ctypes.c_int), _pd, _pd, _pd, _pd], ctypes.c_int),
     "grmp_pattern_build": ([_vp, ctypes.c_int, ctypes.POINTER(BilinearTerm), ctypes.POINTER(_vp)], ctypes.c_int),

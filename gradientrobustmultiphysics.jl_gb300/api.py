@@ -114,6 +114,42 @@ class GB300Context:
             self._spaces[key] = ent
         return ent[1]
 
+    def space_on_device(self, fetype, grid: SimplexMesh, download: bool = True) -> FESpace:
+        """FESpace{FEType}(xgrid) with the dofmap built on the device
+        (grmp_space_create_on_device; H1P1 / H1P2).  The returned FESpace is
+        registered with this context (its device handle is reused by every
+        call); with download=True its host CellDofs are filled in too."""
+        mh = self.mesh(grid)
+        h = ctypes.c_void_p()
+        nd = ctypes.c_int32()
+        self.check(self.lib.grmp_space_create_on_device(mh, fetype.kind, fetype.ncomponents, ctypes.byref(h),
+                                                        ctypes.byref(nd)))
+        FES = FESpace.__new__(FESpace)
+        FES.FEType = fetype
+        FES.xgrid = grid
+        FES.name = repr(fetype)
+        FES.ndofs = nd.value
+        nv = grid.nverts
+        FES.coffset = nd.value // fetype.ncomponents if fetype.ncomponents else nv
+        ld = ctypes.c_int()
+        self.check(self.lib.grmp_space_ndofs4cell(h, ctypes.byref(ld)))
+        if download:
+            cd = np.empty((grid.ncells, ld.value), dtype=np.int32)
+            self.check(self.lib.grmp_space_celldofs(h, _ip(cd)))
+            FES.celldofs = cd
+        self._spaces[id(FES)] = (FES, h)
+        return FES
+
+    def boundary_dofs(self, FES: FESpace) -> np.ndarray:
+        """DoFs on all boundary faces, computed on the device
+        (grmp_space_boundary_dofs); equal to FES.boundary_dofs()."""
+        h = self.space(FES)
+        n = ctypes.c_int32()
+        self.check(self.lib.grmp_space_boundary_dofs(h, 0, None, ctypes.byref(n)))
+        out = np.empty(max(1, n.value), dtype=np.int32)
+        self.check(self.lib.grmp_space_boundary_dofs(h, out.size, _ip(out), ctypes.byref(n)))
+        return out[:n.value]
+
     def release(self, FES: FESpace):
         """Free the device copy of a space (its mesh stays resident)."""
         ent = self._spaces.pop(id(FES), None)

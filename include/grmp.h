@@ -107,6 +107,22 @@ typedef enum {
 int grmp_space_create(grmp_mesh mesh, int fe_kind, int ncomponents, const int32_t *celldofs, int32_t ndofs,
                       grmp_space *out);
 int grmp_space_destroy(grmp_space space);
+/* FESpace{FEType}(xgrid) built on the device from the mesh alone: the dofmap
+ * of src/dofmaps.jl:201-330 for H1P1 (pattern "N1") and H1P2 ("N1F1" in 2D,
+ * "N1E1" in 3D, src/fedefs/h1_p2.jl:33-35), components blocked.  Edges are
+ * numbered in the lexicographic order of their sorted vertex pairs (the
+ * host mesh module's numbering).  Replaces the host-side dofmap build of a
+ * caller; ndofs_out (optional) receives the DoF count. */
+int grmp_space_create_on_device(grmp_mesh mesh, int fe_kind, int ncomponents, grmp_space *out, int32_t *ndofs_out);
+/* The space's CellDofs into a host array [ncells][ndofs4cell]. */
+int grmp_space_celldofs(grmp_space space, int32_t *celldofs);
+/* DoFs on the boundary faces (faces of exactly one cell) of any H1P1 / H1P2
+ * / H1BR space, ascending: the BFaceDofs of the homogeneous Dirichlet branch
+ * of boundarydata! (src/boundarydata.jl:200-260) over all boundary regions,
+ * computed on the device.  fixed: host array of `capacity` entries, or NULL
+ * to count only; *nfixed receives the count (GRMP_ERR_INVALID_ARG when it
+ * exceeds a non-zero capacity). */
+int grmp_space_boundary_dofs(grmp_space space, int32_t capacity, int32_t *fixed, int32_t *nfixed);
 /* Number of local DoFs per cell for the space. */
 int grmp_space_ndofs4cell(grmp_space space, int *out);
 
