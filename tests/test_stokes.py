@@ -176,3 +176,28 @@ def test_batch_result_same_alone_and_in_the_mix(G, ctx, mode):
     c0, c1 = big.mesh.cell_offsets[k], big.mesh.cell_offsets[k + 1]
     assert np.array_equal(sa.velocity(), u[r0:r1])
     assert np.array_equal(sa.pressure(), p[c0:c1])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_divergence_coupling_recast(G, O, dim):
+    """The reference's recast test (test/test_operators.jl:15-82) on the
+    velocity-pressure coupling of the iterated penalty: on one cell, u = x
+    (div u = dim) and p = 0.75 give (div u, p) = dim * 0.75 * |T| both as the
+    cell mean of div u and as the assembled linear form (p, div v) applied to
+    u (the matrix-vector consistency of the recast)."""
+    from grmp_gb300 import mesh as M
+    if dim == 2:
+        g = M.SimplexMesh(np.array([[-1.0, 0.0], [1.0, 0.0], [0.0, 1.0]]), np.array([[0, 1, 2]], dtype=np.int32))
+    else:
+        g = M.SimplexMesh(np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]]),
+                          np.array([[0, 1, 2, 3]], dtype=np.int32))
+    _, _, _, cd, args = O.br_stokes_system(g, 1.0, 0.0, np.zeros((1, 5)), bonus_quadorder=0)
+    nf = g.faces()[0].shape[0]
+    u = np.concatenate([g.coords.T.ravel(), np.zeros(nf)])   # u = x: vertex values, no bubbles
+    vol = g.cell_volumes()[0]
+    divu, _ = O.br_div(g, args, u=u)
+    assert abs(divu[0] * 0.75 * vol - dim * 0.75 * vol) < 1e-14
+    _, bp = O.br_div(g, args, p=np.array([0.75]))
+    assert abs(bp @ u - dim * 0.75 * vol) < 1e-14
+    if dim == 2:
+        assert abs(bp @ u - 1.5) < 1e-14      # the reference's expected value on its triangle
