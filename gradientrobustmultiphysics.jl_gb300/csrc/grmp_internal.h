@@ -81,6 +81,8 @@ struct grmp_matrix_s {
     size_t work_bytes = 0;
     int tuned_cfg = 0;              // autotuned SpMV configuration, FP64 solves (0 = not tuned)
     int tuned_cfg32 = 0;            // autotuned SpMV configuration (100*lanes + loads), mixed solves
+    int tuned_grid = 0;             // autotuned persistent grid (blocks; 0 = as many as fit), FP64 solves
+    int tuned_grid32 = 0;           // the same, mixed solves
     // staged SpMV of mixed solves: the FP32 pairs re-laid out in fixed-size row
     // windows (state 0 = not built, 1 = built, -1 = a row does not fit a window)
     int stg_state = 0;

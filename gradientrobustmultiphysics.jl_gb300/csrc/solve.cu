@@ -1134,12 +1134,17 @@ int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_
 
 // Autotuner: run each configuration for a few iterations of the real solve
 // on this matrix and right-hand side (into a scratch solution vector) and keep
-// the one with the lowest time per iteration.  The persistent kernel's
-// occupancy, barriers and vector phases are part of what is measured.
+// the one with the lowest time per iteration; then, for that configuration,
+// the persistent grid: as many blocks as fit, one or two per SM (fewer
+// blocks make the grid barriers cheaper, which wins on problems whose
+// iteration is short).  The persistent kernel's occupancy, barriers and
+// vector phases are part of what is measured.  *grid_out: 0 = as many
+// blocks as fit.
 int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_params *p, char *work, SolveState *dst,
-                    WorkLayout lay) {
+                    WorkLayout lay, int *grid_out) {
     grmp_context ctx = A->space->mesh->ctx;
     const bool mixed = p->mode == GRMP_SOLVE_MIXED;
+    *grid_out = 0;
     if (A->nrows < 20000) return heuristic_config(A, mixed);
     double *xs = nullptr;
     if (grmp_alloc(ctx, (void **)&xs, (size_t)A->nrows * 8)) return heuristic_config(A, mixed);
@@ -1148,20 +1153,30 @@ int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_para
     q.use_initial_guess = 0;
     q.reltol = 0.0;
     q.abstol = 0.0;
-    int best = heuristic_config(A, mixed);
-    double bt = 1e30;
-    for (int cfg : kConfigs) {
-        if (staged_config(cfg) && (p->mode != GRMP_SOLVE_MIXED || A->stg_state < 0)) continue;
+    q.grid_blocks = 0;
+    auto trial = [&](int cfg) {
         grmp_solve_stats s{};
         dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);   // warm-up: first launch of this instantiation
         s = grmp_solve_stats{};
         dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);
-        if (s.iterations > 0) {
-            double per = s.solve_ms / s.iterations;
-            if (per < bt) {
-                bt = per;
-                best = cfg;
-            }
+        return s.iterations > 0 ? s.solve_ms / s.iterations : 1e30;
+    };
+    int best = heuristic_config(A, mixed);
+    double bt = 1e30;
+    for (int cfg : kConfigs) {
+        if (staged_config(cfg) && (p->mode != GRMP_SOLVE_MIXED || A->stg_state < 0)) continue;
+        const double per = trial(cfg);
+        if (per < bt) {
+            bt = per;
+            best = cfg;
+        }
+    }
+    for (int g : {ctx->num_sms, 2 * ctx->num_sms}) {
+        q.grid_blocks = g;
+        const double per = trial(best);
+        if (per < 0.97 * bt) {   // keep the default unless a smaller grid is clearly faster
+            bt = per;
+            *grid_out = g;
         }
     }
     grmp_free(ctx, xs, (size_t)A->nrows * 8);
@@ -1228,14 +1243,17 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
         if (A->stg_state == 1) stage_fill(A);   // the staged windows hold a copy of the pairs
     }
     int cfg = p->spmv_config;
-    if (cfg == 0) {   // autotuned once per matrix and solver mode
+    grmp_solve_params q = *p;
+    if (cfg == 0) {   // autotuned once per matrix and solver mode (configuration and grid)
         int &slot = mixed ? A->tuned_cfg32 : A->tuned_cfg;
-        if (!slot) slot = autotune_config(A, b, p, work, dst, lay);
+        int &gslot = mixed ? A->tuned_grid32 : A->tuned_grid;
+        if (!slot) slot = autotune_config(A, b, p, work, dst, lay, &gslot);
         cfg = slot;
+        if (q.grid_blocks <= 0) q.grid_blocks = gslot;
     } else if (cfg < 0) {   // heuristic from the row length: no timing, independent of other work on the GPU
         cfg = heuristic_config(A, mixed);
     }
-    return dispatch_pcg(cfg, A, b->d, x->d, p, st, work, dst, lay);
+    return dispatch_pcg(cfg, A, b->d, x->d, &q, st, work, dst, lay);
 }
 
 int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
