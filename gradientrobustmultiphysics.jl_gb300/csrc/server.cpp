@@ -98,8 +98,8 @@ int run_request(grmp_context ctx, Request &r) {
     r.rhs.cell_group = nullptr;
     if (!rc) rc = grmp_pattern_build(space, (int)r.terms.size(), r.terms.data(), &A);
     const bool mixed = r.solve.mode == GRMP_SOLVE_MIXED;
-    if (!rc) rc = grmp_assemble_bilinear(A, (int)r.terms.size(), r.terms.data(), GRMP_FP64);
-    if (!rc && mixed) rc = grmp_assemble_bilinear(A, (int)r.terms.size(), r.terms.data(), GRMP_FP32);
+    // one walk of the incidence lists fills both precisions (bit-identical to two passes)
+    if (!rc) rc = grmp_assemble_bilinear(A, (int)r.terms.size(), r.terms.data(), mixed ? GRMP_FP64_FP32 : GRMP_FP64);
     if (!rc) rc = grmp_vector_create(ctx, r.ndofs, &b);
     if (!rc) rc = grmp_vector_create(ctx, r.ndofs, &x);
     if (!rc) rc = grmp_assemble_linear(space, &r.rhs, b);
