@@ -109,6 +109,9 @@ SIGNATURES = {
     "grmp_space_destroy": ([_vp], ctypes.c_int),
     "grmp_space_ndofs4cell": ([_vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "grmp_space_create_on_device": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp), _pi32], ctypes.c_int),
+    "grmp_mesh_build_faces": ([_vp], ctypes.c_int),
+    "grmp_mesh_faces": ([_vp, _pi32, _pi32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                         ctypes.POINTER(ctypes.c_int8)], ctypes.c_int),
     "grmp_space_celldofs": ([_vp, _pi32], ctypes.c_int),
     "grmp_space_boundary_dofs": ([_vp, _i32, _pi32, _pi32], ctypes.c_int),
     "grmp_reference_tables": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),

@@ -130,7 +130,7 @@ class GB300Context:
         FES.name = repr(fetype)
         FES.ndofs = nd.value
         nv = grid.nverts
-        FES.coffset = nd.value // fetype.ncomponents if fetype.ncomponents else nv
+        FES.coffset = nv if fetype.kind == FE_H1BR else nd.value // fetype.ncomponents
         ld = ctypes.c_int()
         self.check(self.lib.grmp_space_ndofs4cell(h, ctypes.byref(ld)))
         if download:
@@ -139,6 +139,24 @@ class GB300Context:
             FES.celldofs = cd
         self._spaces[id(FES)] = (FES, h)
         return FES
+
+    def mesh_faces(self, grid: SimplexMesh, build: bool = True):
+        """(cell_faces, face_normals, face_volumes, cell_face_signs) of the
+        mesh on the device; build=True computes them there first
+        (grmp_mesh_build_faces), as SimplexMesh.faces / face_geometry do on
+        the host."""
+        mh = self.mesh(grid)
+        if build:
+            self.check(self.lib.grmp_mesh_build_faces(mh))
+        nf = ctypes.c_int32()
+        self.check(self.lib.grmp_mesh_faces(mh, ctypes.byref(nf), None, None, None, None))
+        cf = np.empty((grid.ncells, grid.dim + 1), dtype=np.int32)
+        nr = np.empty((nf.value, grid.dim))
+        fv = np.empty(nf.value)
+        sg = np.empty((grid.ncells, grid.dim + 1), dtype=np.int8)
+        self.check(self.lib.grmp_mesh_faces(mh, ctypes.byref(nf), _ip(cf), _dp(nr), _dp(fv),
+                                            sg.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+        return cf, nr, fv, sg
 
     def boundary_dofs(self, FES: FESpace) -> np.ndarray:
         """DoFs on all boundary faces, computed on the device

@@ -172,6 +172,103 @@ __global__ void k_mark_boundary(long long n, int dim, int fe, int ncomp, int ldo
     }
 }
 
+// outward unit normal and measure of local face l of cell c, as the host
+// mesh module builds them: 2D (t_y, -t_x) with t = P1 - P0, 3D
+// (P1 - P0) x (P2 - P0), normalised and turned away from the cell centroid
+__device__ void face_outward(const double *coords, const int32_t *cells, int dim, long long c, int l, double n[3],
+                             double &meas) {
+    const int32_t *cv = cells + c * (dim + 1);
+    double X[4][3], P[3][3];
+    for (int v = 0; v <= dim; v++)
+        for (int k = 0; k < dim; k++) X[v][k] = coords[(size_t)cv[v] * dim + k];
+    for (int j = 0; j < dim; j++)
+        for (int k = 0; k < dim; k++) P[j][k] = X[dim == 2 ? kTriEdges[l][j] : kTetFaces[l][j]][k];
+    double cc[3] = {0, 0, 0}, fm[3] = {0, 0, 0};
+    for (int k = 0; k < dim; k++) {
+        for (int v = 0; v <= dim; v++) cc[k] += X[v][k];
+        cc[k] /= (dim + 1);
+        for (int j = 0; j < dim; j++) fm[k] += P[j][k];
+        fm[k] /= dim;
+    }
+    // products rounded before they are subtracted or summed (no FMA
+    // contraction): an axis-aligned face then gets exactly zero normal
+    // components, as on the host, and the drop-zero pattern of a BR space
+    // built here is the host-built one's
+    double nr[3] = {0, 0, 0};
+    if (dim == 2) {
+        nr[0] = P[1][1] - P[0][1];
+        nr[1] = -(P[1][0] - P[0][0]);
+    } else {
+        double a[3], b[3];
+        for (int k = 0; k < 3; k++) {
+            a[k] = P[1][k] - P[0][k];
+            b[k] = P[2][k] - P[0][k];
+        }
+        nr[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
+        nr[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
+        nr[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+    }
+    double ln = 0;
+    for (int k = 0; k < dim; k++) ln = __dadd_rn(ln, __dmul_rn(nr[k], nr[k]));
+    ln = sqrt(ln);
+    double d = 0;
+    for (int k = 0; k < dim; k++) {
+        nr[k] /= ln;
+        d = __dadd_rn(d, __dmul_rn(nr[k], fm[k] - cc[k]));
+    }
+    const double sg = d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0);
+    for (int k = 0; k < 3; k++) n[k] = k < dim ? nr[k] * sg : 0.0;
+    meas = dim == 2 ? ln : 0.5 * ln;
+}
+
+// the owner of a face is the lowest-numbered cell that has it
+__global__ void k_face_owner(long long n, int nloc, const int32_t *cell_faces, int32_t *owner) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    atomicMin(&owner[cell_faces[i]], (int32_t)(i / nloc));
+}
+
+// the face normal is the owner's outward normal; the measure the owner's
+__global__ void k_face_geom(long long n, int dim, const double *coords, const int32_t *cells,
+                            const int32_t *cell_faces, const int32_t *owner, double *normals, double *vols) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int nloc = dim + 1;
+    const long long c = i / nloc;
+    const int f = cell_faces[i];
+    if (owner[f] != c) return;
+    double nn[3], meas;
+    face_outward(coords, cells, dim, c, (int)(i % nloc), nn, meas);
+    for (int k = 0; k < dim; k++) normals[(size_t)f * dim + k] = nn[k];
+    vols[f] = meas;
+}
+
+// +1 where the cell's outward normal agrees with the face normal, else -1
+__global__ void k_face_signs(long long n, int dim, const double *coords, const int32_t *cells,
+                             const int32_t *cell_faces, const double *normals, int8_t *signs) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int nloc = dim + 1;
+    double nn[3], meas;
+    face_outward(coords, cells, dim, i / nloc, (int)(i % nloc), nn, meas);
+    const int f = cell_faces[i];
+    double d = 0;
+    for (int k = 0; k < dim; k++) d += nn[k] * normals[(size_t)f * dim + k];
+    signs[i] = d > 0 ? 1 : -1;
+}
+
+// H1BR CellDofs: the vertex DoFs of each component, then the faces
+__global__ void k_celldofs_br(int ncells, const int32_t *cells, int dim, int nverts, const int32_t *cell_faces,
+                              int32_t *celldofs) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const int nv = dim + 1;
+    int32_t *out = celldofs + (size_t)c * (dim * nv + nv);
+    for (int k = 0; k < dim; k++)
+        for (int v = 0; v < nv; v++) out[k * nv + v] = cells[(size_t)c * nv + v] + k * nverts;
+    for (int l = 0; l < nv; l++) out[dim * nv + l] = dim * nverts + cell_faces[(size_t)c * nv + l];
+}
+
 struct DevBuf {
     grmp_context ctx;
     std::vector<std::pair<void *, size_t>> held;
@@ -234,15 +331,115 @@ EntKind face_kind(int dim) { return dim == 2 ? EntKind{2, 2, 3} : EntKind{3, 3, 
 
 }  // namespace
 
+int grmp_mesh_build_faces(grmp_mesh m) {
+    if (!m) return GRMP_ERR_INVALID_ARG;
+    grmp_context ctx = m->ctx;
+    cudaSetDevice(ctx->device);
+    const int dim = m->dim, nloc = dim + 1;
+    const long long n = (long long)m->ncells * nloc;
+    int32_t *cf = nullptr, *owner = nullptr;
+    double *nrm = nullptr, *vol = nullptr;
+    int8_t *sg = nullptr;
+    int32_t nf = 0;
+    int rc = grmp_alloc(ctx, (void **)&cf, (size_t)n * 4);
+    if (!rc) rc = enumerate(m, face_kind(dim), cf, nullptr, &nf);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&owner, (size_t)nf * 4);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&nrm, (size_t)nf * dim * 8);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&vol, (size_t)nf * 8);
+    if (!rc) rc = grmp_alloc(ctx, (void **)&sg, (size_t)n);
+    if (!rc) {
+        cudaMemsetAsync(owner, 0x7f, (size_t)nf * 4, ctx->stream);   // 0x7f7f7f7f: above every cell id
+        k_face_owner<<<nblk(n), TPB, 0, ctx->stream>>>(n, nloc, cf, owner);
+        GRMP_LAUNCHED(ctx);
+        k_face_geom<<<nblk(n), TPB, 0, ctx->stream>>>(n, dim, m->d_coords, m->d_cells, cf, owner, nrm, vol);
+        GRMP_LAUNCHED(ctx);
+        k_face_signs<<<nblk(n), TPB, 0, ctx->stream>>>(n, dim, m->d_coords, m->d_cells, cf, nrm, sg);
+        GRMP_LAUNCHED(ctx);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "mesh faces");
+    }
+    grmp_free(ctx, owner, (size_t)nf * 4);
+    if (rc) {
+        grmp_free(ctx, cf, (size_t)n * 4);
+        grmp_free(ctx, nrm, (size_t)nf * dim * 8);
+        grmp_free(ctx, vol, (size_t)nf * 8);
+        grmp_free(ctx, sg, (size_t)n);
+        return rc;
+    }
+    grmp_free(ctx, m->d_cell_faces, (size_t)n * 4);
+    grmp_free(ctx, m->d_face_normals, (size_t)m->nfaces * dim * 8);
+    grmp_free(ctx, m->d_face_volumes, (size_t)m->nfaces * 8);
+    grmp_free(ctx, m->d_cell_face_signs, (size_t)n);
+    m->nfaces = nf;
+    m->d_cell_faces = cf;
+    m->d_face_normals = nrm;
+    m->d_face_volumes = vol;
+    m->d_cell_face_signs = sg;
+    return GRMP_OK;
+}
+
+int grmp_mesh_faces(grmp_mesh m, int32_t *nfaces, int32_t *cell_faces, double *face_normals, double *face_volumes,
+                    int8_t *cell_face_signs) {
+    if (!m || !nfaces) return GRMP_ERR_INVALID_ARG;
+    grmp_context ctx = m->ctx;
+    cudaSetDevice(ctx->device);
+    *nfaces = m->nfaces;
+    if (m->nfaces == 0) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "mesh faces: none set or built");
+    const size_t nl = (size_t)m->ncells * (m->dim + 1);
+    if (cell_faces) GRMP_CUDA(ctx, cudaMemcpyAsync(cell_faces, m->d_cell_faces, nl * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (face_normals)
+        GRMP_CUDA(ctx, cudaMemcpyAsync(face_normals, m->d_face_normals, (size_t)m->nfaces * m->dim * 8,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    if (face_volumes)
+        GRMP_CUDA(ctx, cudaMemcpyAsync(face_volumes, m->d_face_volumes, (size_t)m->nfaces * 8, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    if (cell_face_signs)
+        GRMP_CUDA(ctx, cudaMemcpyAsync(cell_face_signs, m->d_cell_face_signs, nl, cudaMemcpyDeviceToHost, ctx->stream));
+    GRMP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GRMP_OK;
+}
+
 int grmp_space_create_on_device(grmp_mesh mesh, int fe_kind, int ncomponents, grmp_space *out, int32_t *ndofs_out) {
     if (!mesh || !out) return GRMP_ERR_INVALID_ARG;
     *out = nullptr;
     grmp_context ctx = mesh->ctx;
     const int dim = mesh->dim;
-    if (!((fe_kind == GRMP_FE_H1P1 || fe_kind == GRMP_FE_H1P2) && ncomponents >= 1 && ncomponents <= 3))
-        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "device dofmap: H1P1 / H1P2 with 1-3 components (got %d, %d)",
-                         fe_kind, ncomponents);
+    const bool br = fe_kind == GRMP_FE_H1BR && ncomponents == dim;
+    if (!(br || ((fe_kind == GRMP_FE_H1P1 || fe_kind == GRMP_FE_H1P2) && ncomponents >= 1 && ncomponents <= 3)))
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED,
+                         "device dofmap: H1P1 / H1P2 with 1-3 components or H1BR{dim} (got %d, %d)", fe_kind,
+                         ncomponents);
     cudaSetDevice(ctx->device);
+    if (br) {   // vertex DoFs per component, then one bubble per face (pattern "N1f1")
+        int rc = mesh->nfaces ? GRMP_OK : grmp_mesh_build_faces(mesh);
+        if (rc) return rc;
+        const long long nd = (long long)dim * mesh->nverts + mesh->nfaces;
+        if (nd >= (1LL << 31)) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "device dofmap: too many DoFs");
+        grmp_space s = new (std::nothrow) grmp_space_s();
+        if (!s) return GRMP_ERR_OUT_OF_MEMORY;
+        s->mesh = mesh;
+        s->fe = fe_kind;
+        s->ncomp = ncomponents;
+        s->ldofs = grmp_fe_ldofs(fe_kind, dim, ncomponents);
+        s->nb = grmp_fe_nb(fe_kind, dim);
+        s->ndofs = (int32_t)nd;
+        rc = grmp_alloc(ctx, (void **)&s->d_celldofs, (size_t)mesh->ncells * s->ldofs * 4);
+        if (!rc) {
+            k_celldofs_br<<<nblk(mesh->ncells), TPB, 0, ctx->stream>>>(mesh->ncells, mesh->d_cells, dim, mesh->nverts,
+                                                                        mesh->d_cell_faces, s->d_celldofs);
+            GRMP_LAUNCHED(ctx);
+            rc = grmp_build_incidence(s);
+        }
+        if (!rc) GRMP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (rc) {
+            grmp_space_destroy(s);
+            return rc;
+        }
+        *out = s;
+        if (ndofs_out) *ndofs_out = s->ndofs;
+        return GRMP_OK;
+    }
     const int nv = dim + 1;
     int ne = 0;
     int32_t nedges = 0;

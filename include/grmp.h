@@ -87,6 +87,17 @@ int grmp_mesh_upload(grmp_context ctx, int dim, int32_t nverts, const double *co
  * oriented), face_volumes [nfaces], cell_face_signs [ncells][dim+1] (+1/-1). */
 int grmp_mesh_set_faces(grmp_mesh mesh, int32_t nfaces, const int32_t *cell_faces, const double *face_normals,
                         const double *face_volumes, const int8_t *cell_face_signs);
+/* The same face data computed on the device from the mesh alone (faces
+ * numbered in the lexicographic order of their sorted vertex triples / pairs,
+ * the normal of a face the outward normal of the lowest-numbered cell that
+ * has it, cell_face_signs +1 where a cell's outward normal agrees with it,
+ * face_volumes the face areas / lengths), replacing a previous set. */
+int grmp_mesh_build_faces(grmp_mesh mesh);
+/* The mesh's face data into host arrays (any of them may be NULL):
+ * cell_faces [ncells][dim+1], face_normals [nfaces][dim], face_volumes
+ * [nfaces], cell_face_signs [ncells][dim+1]; *nfaces receives the count. */
+int grmp_mesh_faces(grmp_mesh mesh, int32_t *nfaces, int32_t *cell_faces, double *face_normals, double *face_volumes,
+                    int8_t *cell_face_signs);
 int grmp_mesh_destroy(grmp_mesh mesh);
 
 /* ----------------------------------------------------------------- space */
@@ -108,11 +119,13 @@ int grmp_space_create(grmp_mesh mesh, int fe_kind, int ncomponents, const int32_
                       grmp_space *out);
 int grmp_space_destroy(grmp_space space);
 /* FESpace{FEType}(xgrid) built on the device from the mesh alone: the dofmap
- * of src/dofmaps.jl:201-330 for H1P1 (pattern "N1") and H1P2 ("N1F1" in 2D,
- * "N1E1" in 3D, src/fedefs/h1_p2.jl:33-35), components blocked.  Edges are
- * numbered in the lexicographic order of their sorted vertex pairs (the
- * host mesh module's numbering).  Replaces the host-side dofmap build of a
- * caller; ndofs_out (optional) receives the DoF count. */
+ * of src/dofmaps.jl:201-330 for H1P1 (pattern "N1"), H1P2 ("N1F1" in 2D,
+ * "N1E1" in 3D, src/fedefs/h1_p2.jl:33-35) and H1BR{dim} ("N1f1",
+ * src/fedefs/h1v_br.jl:33; its face data are built with
+ * grmp_mesh_build_faces unless the mesh has some), components blocked.
+ * Edges and faces are numbered in the lexicographic order of their sorted
+ * vertex tuples (the host mesh module's numbering).  Replaces the host-side
+ * dofmap build of a caller; ndofs_out (optional) receives the DoF count. */
 int grmp_space_create_on_device(grmp_mesh mesh, int fe_kind, int ncomponents, grmp_space *out, int32_t *ndofs_out);
 /* The space's CellDofs into a host array [ncells][ndofs4cell]. */
 int grmp_space_celldofs(grmp_space space, int32_t *celldofs);

@@ -68,7 +68,10 @@ def test_refusals(G, ctx):
     from grmp_gb300 import _lib as L
     g = G.grid_unitsquare(3)
     with pytest.raises(G.GrmpError) as ei:
-        ctx.space_on_device(F.H1BR(2), g)
+        ctx.space_on_device(F.H1BR(3), g)          # BR{3} on a 2D mesh
+    assert ei.value.code == L.ERR_UNSUPPORTED
+    with pytest.raises(G.GrmpError) as ei:
+        ctx.space_on_device(F.L2P0(1), g)
     assert ei.value.code == L.ERR_UNSUPPORTED
     import ctypes
     S = F.FESpace(F.H1P2(1, 2), g)
@@ -101,3 +104,50 @@ def test_device_space_solves_like_host_space(G, ctx):
     assert np.array_equal(out[0][0].indices, out[1][0].indices)
     assert np.array_equal(out[0][0].data, out[1][0].data)
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("grid", ["square7", "cube3", "square6_shuffled", "cube3_shuffled", "one_tetrahedron"])
+def test_device_faces_equal_host(G, ctx, grid):
+    """grmp_mesh_build_faces against SimplexMesh.faces / face_geometry:
+    numbering and signs exact, normals and measures to rounding."""
+    g = _grids(G)[grid]
+    cf, nr, fv, sg = ctx.mesh_faces(g)
+    hfn, hcf = g.faces()
+    hnr, hfv, hsg = g.face_geometry()
+    assert np.array_equal(cf, hcf)
+    assert np.array_equal(sg, hsg)
+    assert nr.shape == hnr.shape and np.max(np.abs(nr - hnr)) <= 1e-15
+    assert np.max(np.abs(fv - hfv) / hfv) <= 1e-15
+
+
+@pytest.mark.parametrize("grid", ["square7", "cube3_shuffled"])
+def test_device_br_space_assembles_like_host(G, O, ctx, grid):
+    """An H1BR{d} space built on the device (DoF map and face data) gives the
+    host-built space's CellDofs and boundary DoFs, and the same penalised
+    Stokes matrix and reconstructed load to rounding of the face normals."""
+    from grmp_gb300 import fespace as F
+    from grmp_gb300 import _lib as L
+    from grmp_gb300 import api
+    g = _grids(G)[grid]
+    gd = type(g)(g.coords.copy(), g.cells.copy(), name="device copy")   # its own mesh handle
+    host = F.FESpace(F.H1BR(g.dim), g)
+    dev = ctx.space_on_device(F.H1BR(g.dim), gd)
+    assert dev.ndofs == host.ndofs and np.array_equal(dev.celldofs, host.celldofs)
+    assert np.array_equal(ctx.boundary_dofs(dev), host.boundary_dofs())
+    ops = [api.Operator(L.OP_LAPLACE, True, 0.7), api.Operator(L.OP_RDIVRDIV, False, 50.0)]
+    if g.dim == 2:
+        terms = np.array([(0, 1.0, 1, 0, 0), (1, -2.0, 0, 2, 0), (0, 0.5, 0, 0, 0)])
+    else:
+        terms = np.array([(0, 1.0, 1, 0, 0), (1, -2.0, 0, 2, 0), (2, 0.5, 0, 1, 1)])
+    out = []
+    for FES in (host, dev):
+        A = api.FEMatrix(ctx, FES, ops)
+        api.assemble(A, ops, L.FP64)
+        b = api.FEVector(ctx, FES)
+        b.fill(0.0)
+        api.assemble(b, api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(terms, g.dim, 1)))
+        out.append((A.download(L.FP64), b.entries))
+    (Ah, bh), (Ad, bd) = out
+    assert np.array_equal(Ah.indptr, Ad.indptr) and np.array_equal(Ah.indices, Ad.indices)
+    assert np.max(np.abs(Ad.data - Ah.data)) <= 1e-13 * np.max(np.abs(Ah.data))
+    assert np.max(np.abs(bd - bh)) <= 1e-13 * np.max(np.abs(bh))
