@@ -85,3 +85,12 @@ def test_invalid_handles_rejected(lib):
     p = __import__("grmp_gb300")._lib.SolveParams()
     assert lib.grmp_solve_params_default(ctypes.byref(p)) == 0
     assert p.reltol == 1e-12 and p.abstol == 1e-12
+
+
+def test_integration_notes_bind_every_symbol():
+    """The Julia-side bindings (the reference-side FFI a maintainer adds)
+    name every entry point the header declares."""
+    names = header_symbols()
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [n for n in names if n not in txt]
+    assert not missing, missing
