@@ -89,6 +89,84 @@ __global__ void __launch_bounds__(kTB) k_item_l2(int ncells, const double *coord
     cellv[cell] = acc;
 }
 
+// The same on an H1BR{DIM} function (Identity / Gradient "with
+// coefficients", src/feevaluator_h1.jl:77-94): local DoF I < DIM*(DIM+1) is
+// the P1 function I % (DIM+1) in component I / (DIM+1); the others are the
+// face bubbles (scalar function DIM+1+f) times the global unit normal n_F.
+template <int DIM>
+__global__ void __launch_bounds__(kTB) k_item_l2_br(int ncells, const double *coords, const int32_t *cells,
+                                                    const int32_t *cell_faces, const double *fnormals,
+                                                    const int32_t *celldofs, int nb, int op, const double *u,
+                                                    const double *v, RhsDev data, double factor, const double *tw,
+                                                    const double *txref, const double *tvals, const double *tderivs,
+                                                    int nq, double *cellv) {
+    constexpr int NV = DIM + 1, ND = DIM * NV + NV;
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= ncells) return;
+    double X[4 * 3], nrm[4][3];
+    for (int k = 0; k < NV; k++)
+        for (int j = 0; j < DIM; j++) X[k * DIM + j] = coords[(size_t)cells[(size_t)cell * NV + k] * DIM + j];
+    for (int f = 0; f < NV; f++)
+        for (int j = 0; j < DIM; j++) nrm[f][j] = fnormals[(size_t)cell_faces[(size_t)cell * NV + f] * DIM + j];
+    double G[3][3], A[3][3], vol;
+    simplex_geometry<DIM, double>(X, G, vol, A);
+    const int rdim = op == GRMP_ITEM_GRADIENT ? DIM * DIM : DIM;
+    double cu[ND], cvv[ND];
+    for (int i = 0; i < ND; i++) {
+        const int d = celldofs[(size_t)cell * ND + i];
+        cu[i] = u[d];
+        cvv[i] = v ? v[d] : 0.0;
+    }
+    double acc = 0.0;
+    for (int q = 0; q < nq; q++) {
+        double in1[kMaxIn], in2[kMaxIn];
+        for (int k = 0; k < rdim; k++) in1[k] = in2[k] = 0.0;
+        for (int dof = 0; dof < ND; dof++) {
+            double cv[kMaxIn];
+            for (int k = 0; k < rdim; k++) cv[k] = 0.0;
+            for (int c = 0; c < DIM; c++) {
+                const int si = dof < DIM * NV ? (dof / NV == c ? dof % NV : -1) : NV + (dof - DIM * NV);
+                if (si < 0) continue;
+                const double coef = dof < DIM * NV ? 1.0 : nrm[dof - DIM * NV][c];
+                if (op == GRMP_ITEM_GRADIENT) {
+                    for (int k = 0; k < DIM; k++) {
+                        double g = 0.0;
+                        for (int j = 0; j < DIM; j++) g += G[k][j] * tderivs[(q * nb + si) * DIM + j];
+                        cv[c * DIM + k] = g * coef;
+                    }
+                } else {
+                    cv[c] = tvals[q * nb + si] * coef;
+                }
+            }
+            for (int k = 0; k < rdim; k++) {
+                in1[k] += cu[dof] * cv[k];
+                in2[k] += cvv[dof] * cv[k];
+            }
+        }
+        double result = 0.0;
+        if (v) {
+            for (int j = 0; j < rdim; j++) result += (in1[j] - in2[j]) * (in1[j] - in2[j]);
+        } else {
+            double f[kMaxIn];
+            for (int j = 0; j < rdim; j++) f[j] = 0.0;
+            if (data.kind >= 0) {
+                double x[3] = {0, 0, 0};
+                for (int k = 0; k < DIM; k++) {
+                    x[k] = X[k];
+                    for (int j = 0; j < DIM; j++) x[k] += A[k][j] * txref[3 * q + j];
+                }
+                rhs_eval(data, DIM, cell, x, f);
+            }
+            for (int j = 0; j < rdim; j++) {
+                const double e = f[j] - in1[j] * factor;
+                result += e * e;
+            }
+        }
+        acc += result * tw[q] * vol;
+    }
+    cellv[cell] = acc;
+}
+
 // per-block sums of cellv in a fixed tree order
 __global__ void __launch_bounds__(256) k_block_sum(int n, const double *x, double *part) {
     __shared__ double sh[256];
@@ -109,8 +187,12 @@ int grmp_item_l2error_impl(grmp_space s, grmp_vector u, grmp_vector v, int op, c
     grmp_context ctx = s->mesh->ctx;
     grmp_mesh m = s->mesh;
     const int dim = m->dim;
-    if (s->fe != GRMP_FE_H1P1 && s->fe != GRMP_FE_H1P2)
-        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "item integrator: element %d (H1P1 and H1P2 are supported)", s->fe);
+    const bool br = s->fe == GRMP_FE_H1BR;
+    if (s->fe != GRMP_FE_H1P1 && s->fe != GRMP_FE_H1P2 && !br)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "item integrator: element %d (H1P1, H1P2 and H1BR are supported)",
+                         s->fe);
+    if (br && (m->nfaces == 0 || s->ncomp != dim))
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "item integrator: H1BR needs the mesh's face data");
     if (op != GRMP_ITEM_IDENTITY && op != GRMP_ITEM_GRADIENT)
         return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "item integrator: operator %d", op);
     if (u->n != s->ndofs || (v && v->n != s->ndofs))
@@ -175,7 +257,15 @@ int grmp_item_l2error_impl(grmp_space s, grmp_vector u, grmp_vector v, int op, c
         const double *dw = dtab, *dx = dtab + nq, *dv = dx + 3 * nq, *dd = dv + (size_t)nq * nb;
         RhsDev r{data ? data->kind : -1, rdim, dpar, data ? data->nparams : 0, 1.0, nq, nb, dw, dx, dv};
         const double *vd = v ? v->d : nullptr;
-        if (dim == 2)
+        if (br && dim == 2)
+            k_item_l2_br<2><<<(ncells + kTB - 1) / kTB, kTB, 0, ctx->stream>>>(
+                ncells, m->d_coords, m->d_cells, m->d_cell_faces, m->d_face_normals, s->d_celldofs, nb, op, u->d, vd, r,
+                factor, dw, dx, dv, dd, nq, dcell);
+        else if (br)
+            k_item_l2_br<3><<<(ncells + kTB - 1) / kTB, kTB, 0, ctx->stream>>>(
+                ncells, m->d_coords, m->d_cells, m->d_cell_faces, m->d_face_normals, s->d_celldofs, nb, op, u->d, vd, r,
+                factor, dw, dx, dv, dd, nq, dcell);
+        else if (dim == 2)
             k_item_l2<2><<<(ncells + kTB - 1) / kTB, kTB, 0, ctx->stream>>>(
                 ncells, m->d_coords, m->d_cells, s->d_celldofs, nb, s->ncomp, op, u->d, vd, r, factor, dw, dx, dv, dd,
                 nq, dcell);

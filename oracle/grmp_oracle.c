@@ -1235,6 +1235,106 @@ static void br3_cell(const br_mesh *m, int cell, double X[12], double nrm[12], d
     }
 }
 
+/* L2 error / norm / difference of an H1BR{dim} function: the ItemIntegrator
+ * (src/assemblypatterns/itemintegrator.jl:173-300) on the Bernardi-Raugel
+ * element with Identity or Gradient "with coefficients"
+ * (src/feevaluator_h1.jl:77-94): cvals[k][dof] = coef(dof, c) * (value or
+ * gradient of the scalar basis function s(dof, c)), the coefficient 1 for a
+ * vertex DoF and n_F[c] for the bubble of face F; summed DoF by DoF.  Rule
+ * order: polyorder(H1BR{dim}) = dim + shift(op) + quadorder. */
+int oracle_item_l2error_br(double *cellv, double *total, int dim, int ncells, const double *coords, const int *cells,
+                           const int *cell_faces, const double *fnormals, const int *celldofs, const double *u,
+                           const double *v, int op, int data_kind, const double *par, int npar, double factor,
+                           int quadorder)
+{
+    if (op != OR_OP_IDENTITY && op != OR_OP_GRADIENT) return -1;
+    if (dim != 2 && dim != 3) return -1;
+    const int nv = dim + 1, nb = 2 * nv, nd = dim * nv + nv;
+    int order = dim + (op == OR_OP_GRADIENT ? -1 : 0) + quadorder;
+    if (order < 0) order = 0;
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(dim, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    double vals[OR_MAXQ][8], derivs[OR_MAXQ][8][3];
+    for (int q = 0; q < nq; q++) {
+        if (dim == 3) {
+            br3_basis(&xref[3 * q], vals[q], derivs[q]);
+        } else {
+            dual x[2] = {dvar(xref[3 * q], 0), dvar(xref[3 * q + 1], 1)}, p1[OR_MAXD], p2[OR_MAXD];
+            h1_scalar_basis(OR_FE_P1, 2, x, p1);
+            h1_scalar_basis(OR_FE_P2, 2, x, p2);
+            for (int a = 0; a < 6; a++) {
+                const dual d = a < 3 ? p1[a] : p2[a];
+                vals[q][a] = d.v;
+                for (int j = 0; j < 2; j++) derivs[q][a][j] = d.d[j];
+            }
+        }
+    }
+    (void)nb;
+    const int rdim = op == OR_OP_GRADIENT ? dim * dim : dim;
+    double acc = 0.0;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], nrm[12];
+        for (int vv = 0; vv < nv; vv++)
+            for (int k = 0; k < dim; k++) X[vv * dim + k] = coords[(size_t)cells[(size_t)cell * nv + vv] * dim + k];
+        for (int f = 0; f < nv; f++)
+            for (int k = 0; k < dim; k++) nrm[f * dim + k] = fnormals[(size_t)cell_faces[(size_t)cell * nv + f] * dim + k];
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(dim, X, A, G, &det, &vol);
+        double cellacc = 0.0;
+        for (int q = 0; q < nq; q++) {
+            double in1[9] = {0}, in2[9] = {0}, f[9] = {0};
+            for (int dof = 0; dof < nd; dof++) {
+                double cv[9] = {0};
+                for (int c = 0; c < dim; c++) {
+                    const int sidx = dof < dim * nv ? (dof / nv == c ? dof % nv : -1) : nv + (dof - dim * nv);
+                    if (sidx < 0) continue;
+                    const double coef = dof < dim * nv ? 1.0 : nrm[(dof - dim * nv) * dim + c];
+                    if (op == OR_OP_IDENTITY) {
+                        cv[c] = vals[q][sidx] * coef;
+                    } else {
+                        for (int k = 0; k < dim; k++) {
+                            double g = 0.0;
+                            for (int j = 0; j < dim; j++) g += G[k][j] * derivs[q][sidx][j];
+                            cv[c * dim + k] = g * coef;
+                        }
+                    }
+                }
+                const double c1 = u[celldofs[(size_t)cell * nd + dof]];
+                const double c2 = v ? v[celldofs[(size_t)cell * nd + dof]] : 0.0;
+                for (int k = 0; k < rdim; k++) {
+                    in1[k] += c1 * cv[k];
+                    in2[k] += c2 * cv[k];
+                }
+            }
+            double result = 0.0;
+            if (v) {
+                for (int j = 0; j < rdim; j++) result += (in1[j] - in2[j]) * (in1[j] - in2[j]);
+            } else {
+                if (data_kind >= 0) {
+                    double x[3] = {0, 0, 0};
+                    for (int k = 0; k < dim; k++) {
+                        x[k] = X[k];
+                        for (int j = 0; j < dim; j++) x[k] += A[k][j] * xref[3 * q + j];
+                    }
+                    rhs_eval(data_kind, dim, rdim, par, npar, cell, x, f);
+                }
+                for (int j = 0; j < rdim; j++) {
+                    const double e = f[j] - in1[j] * factor;
+                    result += e * e;
+                }
+            }
+            const double contrib = result * w[q] * vol;
+            cellacc += contrib;
+            acc += contrib;
+        }
+        if (cellv) cellv[cell] = cellacc;
+    }
+    if (total) *total = acc;
+    return nq;
+}
+
 /* nu (grad u, grad v) on H1BR{3} (Gradient with coefficients) plus
  * lambda (div R u, div R v) with R the RT0 reconstruction; both on the rule of
  * order 2 (polyorder 3 - 1) = 4.  The reconstructed divergence follows
@@ -1249,7 +1349,7 @@ int oracle_br3_assemble(void *h, int ncells, const double *coords, const int *ce
     double xref[3 * OR_MAXQ], w[OR_MAXQ];
     int nq = oracle_qrule(3, 4, xref, w);
     if (nq < 0) nq = -nq;
-    static double vals[OR_MAXQ][8], derivs[OR_MAXQ][8][3];
+    double vals[OR_MAXQ][8], derivs[OR_MAXQ][8][3];
     for (int q = 0; q < nq; q++) br3_basis(&xref[3 * q], vals[q], derivs[q]);
     for (int cell = 0; cell < ncells; cell++) {
         double X[12], nrm[12], fv[4], sg[4];

@@ -78,6 +78,10 @@ def lib():
                                           ctypes.c_int, ip, dp, dp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_int]
         L.oracle_item_l2error.restype = ctypes.c_int
+        L.oracle_item_l2error_br.argtypes = [dp, dp, ctypes.c_int, ctypes.c_int, dp, ip, ip, dp, ip, dp, dp,
+                                             ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double,
+                                             ctypes.c_int]
+        L.oracle_item_l2error_br.restype = ctypes.c_int
         L.oracle_cg.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
         L.oracle_cg.restype = ctypes.c_int
         sp = ctypes.POINTER(ctypes.c_byte)
@@ -255,6 +259,34 @@ def item_l2error(coords, cells, fe, ncomp, cdofs, u, op=OP_IDENTITY, data_kind=-
                                    _dp(par), par.size, float(factor), int(quadorder))
     if nq < 0:
         raise RuntimeError("oracle item integrator failed")
+    return cellv, float(total[0])
+
+
+def item_l2error_br(g, cdofs, u, op=OP_IDENTITY, data_kind=-1, params=None, factor=1.0, quadorder=0, v=None):
+    """The same integrators on an H1BR{dim} function over the mesh g (its
+    faces and face normals as the host mesh module numbers them)."""
+    fn, cf = g.faces()
+    nrm, _, _ = g.face_geometry()
+    coords = np.ascontiguousarray(g.coords, dtype=np.float64)
+    cells = np.ascontiguousarray(g.cells, dtype=np.int32)
+    cf = np.ascontiguousarray(cf, dtype=np.int32)
+    nrm = np.ascontiguousarray(nrm, dtype=np.float64)
+    cdofs = np.ascontiguousarray(cdofs, dtype=np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    par = np.zeros(1) if params is None else np.ascontiguousarray(params, dtype=np.float64).ravel()
+    if par.size == 0:
+        par = np.zeros(1)
+    cellv = np.zeros(g.ncells)
+    total = np.zeros(1)
+    vp = None
+    if v is not None:
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        vp = _dp(v)
+    nq = lib().oracle_item_l2error_br(_dp(cellv), _dp(total), g.dim, g.ncells, _dp(coords), _ip(cells), _ip(cf),
+                                      _dp(nrm), _ip(cdofs), _dp(u), vp, op, data_kind, _dp(par), par.size,
+                                      float(factor), int(quadorder))
+    if nq < 0:
+        raise RuntimeError("oracle BR item integrator failed")
     return cellv, float(total[0])
 
 

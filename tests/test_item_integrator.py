@@ -104,11 +104,44 @@ def test_difference_integrator(G, O, ctx):
         assert abs(t - tn) <= 1e-12 * abs(tn)
 
 
+@pytest.mark.parametrize("dim,opname,kind", [(2, "Identity", "poly"), (2, "Gradient", None), (3, "Identity", None),
+                                             (3, "Gradient", "poly"), (2, "Gradient", "poly")])
+def test_br_parity_with_oracle(G, O, ctx, dim, opname, kind):
+    """Bernardi-Raugel functions (vertex parts and face bubbles times the face
+    normals) through the device integrator against the oracle."""
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitsquare(6) if dim == 2 else G.grid_unitcube_kuhn(3)
+    FES = F.FESpace(F.H1BR(dim), g)
+    rng = np.random.default_rng(21 + dim)
+    uvals = rng.standard_normal(FES.ndofs)
+    u = _vec(G, ctx, FES, uvals)
+    op = G.Identity if opname == "Identity" else G.Gradient
+    rdim = dim * (dim if opname == "Gradient" else 1)
+    if kind == "poly":
+        terms = [(c, rng.standard_normal(), *rng.integers(0, 3, size=3)) for c in range(rdim) for _ in range(2)]
+        data = G.DataFunction.polynomial(terms, rdim, bonus_quadorder=1)
+        integ = G.L2ErrorIntegrator(data, op, factor=0.5)
+        oc, ot = O.item_l2error_br(g, FES.celldofs, uvals, 0 if opname == "Identity" else 1, data.kind, data.params,
+                                   factor=0.5, quadorder=2 * data.bonus_quadorder)
+    else:
+        integ = G.L2NormIntegrator(op, quadorder=2)
+        oc, ot = O.item_l2error_br(g, FES.celldofs, uvals, 0 if opname == "Identity" else 1, quadorder=2)
+    cells = integ.evaluate_cells(u)
+    tot = integ.evaluate(u)
+    assert np.max(np.abs(cells - oc)) <= 1e-12 * np.max(np.abs(oc))
+    assert abs(tot - ot) <= 1e-13 * abs(ot)
+    # difference of two BR functions equals the norm of their difference
+    w = rng.standard_normal(FES.ndofs)
+    td = G.L2DifferenceIntegrator(op).evaluate(u, _vec(G, ctx, FES, w))
+    tn = G.L2NormIntegrator(op).evaluate(_vec(G, ctx, FES, uvals - w))
+    assert abs(td - tn) <= 1e-12 * abs(tn)
+
+
 def test_refusals(G, ctx):
     from grmp_gb300 import fespace as F
     from grmp_gb300 import _lib as L
     g = G.grid_unitsquare(4)
-    FES = F.FESpace(F.H1BR(2), g)
+    FES = F.FESpace(F.L2P0(1), g)
     u = _vec(G, ctx, FES, np.zeros(FES.ndofs))
     with pytest.raises(G.GrmpError) as ei:
         G.L2NormIntegrator(G.Identity).evaluate(u)

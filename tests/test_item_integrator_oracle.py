@@ -55,3 +55,54 @@ def test_closed_form_norms(G, O):
     _, t2 = O.item_l2error(g.coords, g.cells, 1, 1, FES.celldofs, u, OP_IDENTITY, RHS_POLY,
                            np.array([[0, 0.0, 0, 0, 0]]), factor=2.0, quadorder=2)
     assert abs(t2 - 4.0 / 3.0) < 1e-14
+
+
+def _br_linear(G, dim, seed=0):
+    """A linear vector field on a BR space: vertex values, zero bubbles, with
+    its polynomial records and those of its (constant) gradient."""
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitsquare(4) if dim == 2 else G.grid_unitcube_kuhn(2)
+    S = F.FESpace(F.H1BR(dim), g)
+    rng = np.random.default_rng(seed)
+    M, c0 = rng.standard_normal((dim, dim)), rng.standard_normal(dim)
+    vals = g.coords @ M.T + c0
+    u = np.concatenate([vals.T.ravel(), np.zeros(g.faces()[0].shape[0])])
+    terms = []
+    for c in range(dim):
+        terms.append((c, c0[c], 0, 0, 0))
+        for j in range(dim):
+            e = [0, 0, 0]
+            e[j] = 1
+            terms.append((c, M[c, j], *e))
+    gterms = [(c * dim + j, M[c, j], 0, 0, 0) for c in range(dim) for j in range(dim)]
+    return g, S, u, np.array(terms), np.array(gterms)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_br_linear_fields_are_exact(G, O, dim):
+    """H1BR{d} holds the linear vector fields (its P1 part): L2 and H1 errors
+    of such a field against its own formula vanish (the element-order
+    exactness of runtests.jl:170-330 for the BR element)."""
+    g, S, u, terms, gterms = _br_linear(G, dim)
+    _, l2 = O.item_l2error_br(g, S.celldofs, u, OP_IDENTITY, RHS_POLY, terms, quadorder=2)
+    _, h1 = O.item_l2error_br(g, S.celldofs, u, OP_GRADIENT, RHS_POLY, gterms, quadorder=0)
+    assert np.sqrt(l2) < 1e-14 and np.sqrt(h1) < 1e-13
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_br_bubble_norm_closed_form(G, O, dim):
+    """One face bubble with coefficient 1: ||phi_F||^2 = c (|T1| + |T2|) with
+    c = 16 * 2 * 2!2!/6! = 8/45 in 2D (4 l_a l_b) and 3600 * 6 * 2!2!2!/9! =
+    10/21 in 3D (60 l_a l_b l_c); the unit normal does not change the norm."""
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitsquare(3) if dim == 2 else G.grid_unitcube_kuhn(2)
+    S = F.FESpace(F.H1BR(dim), g)
+    fn, cf = g.faces()
+    cnt = np.bincount(cf.ravel(), minlength=fn.shape[0])
+    face = int(np.nonzero(cnt == 2)[0][0])
+    u = np.zeros(S.ndofs)
+    u[dim * g.nverts + face] = 1.0
+    cells = np.nonzero((cf == face).any(axis=1))[0]
+    c = 8.0 / 45.0 if dim == 2 else 10.0 / 21.0
+    _, n2 = O.item_l2error_br(g, S.celldofs, u, OP_IDENTITY, quadorder=2 if dim == 2 else 3)
+    assert abs(n2 - c * g.cell_volumes()[cells].sum()) < 1e-15
