@@ -1260,14 +1260,14 @@ int oracle_item_l2error_br(double *cellv, double *total, int dim, int ncells, co
     for (int q = 0; q < nq; q++) {
         if (dim == 3) {
             br3_basis(&xref[3 * q], vals[q], derivs[q]);
-        } else {
-            dual x[2] = {dvar(xref[3 * q], 0), dvar(xref[3 * q + 1], 1)}, p1[OR_MAXD], p2[OR_MAXD];
-            h1_scalar_basis(OR_FE_P1, 2, x, p1);
-            h1_scalar_basis(OR_FE_P2, 2, x, p2);
+        } else {   /* P1 functions and the bubbles 6 x r, 6 y x, 6 r y (src/fedefs/h1v_br.jl:117-130) */
+            dual x[2] = {dvar(xref[3 * q], 0), dvar(xref[3 * q + 1], 1)};
+            dual r = dsub(dcsub(1.0, x[0]), x[1]);
+            dual o[6] = {r, x[0], x[1], dmul(dscale(6.0, x[0]), r), dmul(dscale(6.0, x[1]), x[0]),
+                         dmul(dscale(6.0, r), x[1])};
             for (int a = 0; a < 6; a++) {
-                const dual d = a < 3 ? p1[a] : p2[a];
-                vals[q][a] = d.v;
-                for (int j = 0; j < 2; j++) derivs[q][a][j] = d.d[j];
+                vals[q][a] = o[a].v;
+                for (int j = 0; j < 2; j++) derivs[q][a][j] = o[a].d[j];
             }
         }
     }

@@ -92,8 +92,9 @@ def test_br_linear_fields_are_exact(G, O, dim):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_br_bubble_norm_closed_form(G, O, dim):
     """One face bubble with coefficient 1: ||phi_F||^2 = c (|T1| + |T2|) with
-    c = 16 * 2 * 2!2!/6! = 8/45 in 2D (4 l_a l_b) and 3600 * 6 * 2!2!2!/9! =
-    10/21 in 3D (60 l_a l_b l_c); the unit normal does not change the norm."""
+    c = 36 * 2 * 2!2!/6! = 2/5 in 2D (6 l_a l_b, src/fedefs/h1v_br.jl:117-130)
+    and 3600 * 6 * 2!2!2!/9! = 10/21 in 3D (60 l_a l_b l_c, :221-233); the
+    unit normal does not change the norm."""
     from grmp_gb300 import fespace as F
     g = G.grid_unitsquare(3) if dim == 2 else G.grid_unitcube_kuhn(2)
     S = F.FESpace(F.H1BR(dim), g)
@@ -103,6 +104,6 @@ def test_br_bubble_norm_closed_form(G, O, dim):
     u = np.zeros(S.ndofs)
     u[dim * g.nverts + face] = 1.0
     cells = np.nonzero((cf == face).any(axis=1))[0]
-    c = 8.0 / 45.0 if dim == 2 else 10.0 / 21.0
+    c = 2.0 / 5.0 if dim == 2 else 10.0 / 21.0
     _, n2 = O.item_l2error_br(g, S.celldofs, u, OP_IDENTITY, quadorder=2 if dim == 2 else 3)
     assert abs(n2 - c * g.cell_volumes()[cells].sum()) < 1e-15
