@@ -81,8 +81,10 @@ def _br_linear(G, dim, seed=0):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_br_linear_fields_are_exact(G, O, dim):
     """H1BR{d} holds the linear vector fields (its P1 part): L2 and H1 errors
-    of such a field against its own formula vanish (the element-order
-    exactness of runtests.jl:170-330 for the BR element)."""
+    of such a field against its own formula vanish -- the reference's
+    interpolation test for H1BR{2} / H1BR{3} with expected order 1
+    (test/runtests.jl:186-223, 224-260: for a linear function the
+    interpolant is its vertex values with zero bubble coefficients)."""
     g, S, u, terms, gterms = _br_linear(G, dim)
     _, l2 = O.item_l2error_br(g, S.celldofs, u, OP_IDENTITY, RHS_POLY, terms, quadorder=2)
     _, h1 = O.item_l2error_br(g, S.celldofs, u, OP_GRADIENT, RHS_POLY, gterms, quadorder=0)
