@@ -12,8 +12,8 @@
  * (test/runtests.jl quadrature exactness, polynomial reproduction of the
  * elements, Stokes / pressure-robustness exactness) which the pytest suite
  * re-implements.  Mesh numbering, the affine-map inverse and face orientation
- * come from ExtendableGrids and are conventions of this build (see the
- * mesh module and the design notes); they are "parity unpinned".
+ * come from ExtendableGrids and are restated here as conventions shared
+ * with the host mesh module; they are "parity unpinned".
  *
  * Every routine follows the operation order of the reference file it cites so
  * that the drop-exact-zero sparsity rule (src/fematrix.jl:54-65) sees the same
@@ -364,7 +364,7 @@ int oracle_basis_tables(int fe, int dim, int nq, const double *xref, double *val
 }
 
 /* ------------------------------------------------------------------------- */
-/* Geometry (ExtendableGrids L2GTransformer role; convention of this build)  */
+/* Geometry (ExtendableGrids L2GTransformer role; restated convention)      */
 /* ------------------------------------------------------------------------- */
 
 /* A = [x1-x0, x2-x0(, x3-x0)] (columns).  G = A^{-T} = cof(A)/det(A), the
