@@ -319,3 +319,24 @@ def test_batch3d_hydrostatic_and_alone_vs_mix(G, ctx):
     c0, c1 = big.mesh.cell_offsets[1], big.mesh.cell_offsets[2]
     assert np.array_equal(sa.velocity(), u[r0:r1])
     assert np.array_equal(sa.pressure(), p[c0:c1])
+
+
+def test_batch3d_layout(G, O):
+    """Host layout of a 3D batch: each problem's DoFs and cells are one
+    contiguous block, its CellDofs stay inside it and equal the single
+    problem's shifted by the block offset, and its boundary DoFs are the
+    single problem's, shifted."""
+    from grmp_gb300 import fespace as F
+    from grmp_gb300 import stokes as S
+    prob = S.make_batch(sizes=np.array([2, 3, 2]), nus=np.array([1.0, 0.5, 0.2]), seed=5, dim=3)
+    V, M = prob.V, prob.mesh
+    assert prob.terms.shape == (3, 30, 5)
+    fixed = V.boundary_dofs()
+    for k, g in enumerate(M.parts):
+        r0, r1 = V.row_offsets[k], V.row_offsets[k + 1]
+        c0, c1 = M.cell_offsets[k], M.cell_offsets[k + 1]
+        single = F.FESpace(F.H1BR(3), g)
+        assert r1 - r0 == single.ndofs and c1 - c0 == g.ncells
+        assert np.array_equal(V.celldofs[c0:c1], single.celldofs + r0)
+        mine = fixed[(fixed >= r0) & (fixed < r1)] - r0
+        assert np.array_equal(mine, single.boundary_dofs())
