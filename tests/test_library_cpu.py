@@ -94,3 +94,12 @@ def test_integration_notes_bind_every_symbol():
     txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     missing = [n for n in names if n not in txt]
     assert not missing, missing
+
+
+def test_build_compiles_every_source():
+    """Every translation unit under csrc/ is in the build list (a file left
+    out would not exist on a machine that builds from source)."""
+    import grmp_gb300.build as b
+    csrc = os.path.join(ROOT, "gradientrobustmultiphysics.jl_gb300", "csrc")
+    tus = sorted(f for f in os.listdir(csrc) if f.endswith((".cu", ".cpp")))
+    assert sorted(b.SOURCES) == tus
