@@ -103,3 +103,18 @@ def test_build_compiles_every_source():
     csrc = os.path.join(ROOT, "gradientrobustmultiphysics.jl_gb300", "csrc")
     tus = sorted(f for f in os.listdir(csrc) if f.endswith((".cu", ".cpp")))
     assert sorted(b.SOURCES) == tus
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/grmp.h is a C-ABI header: it compiles as strict C99 (what an
+    FFI generator or a C caller sees), not only as C++."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "h.c"
+    src.write_text('#include "grmp.h"\nint main(void) { return grmp_version() > 0 ? 0 : 1; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                        "-I" + os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
