@@ -314,7 +314,9 @@ typedef struct {
                                per matrix and mode (timed trial solves); -1 = chosen from the
                                mean row length
                                (no timing, so the choice does not depend on concurrent GPU work) */
-    int32_t grid_blocks;    /* persistent-kernel blocks: 0 = autotuned                   */
+    int32_t grid_blocks;    /* persistent-kernel blocks: 0 = as many as fit, or, with
+                               spmv_config 0, the autotuner's choice among that and one or
+                               two blocks per SM (cheaper grid barriers on small systems) */
     int32_t use_initial_guess; /* 1: start from x, 0: start from 0                      */
 } grmp_solve_params;
 
