@@ -340,3 +340,18 @@ def test_batch3d_layout(G, O):
         assert np.array_equal(V.celldofs[c0:c1], single.celldofs + r0)
         mine = fixed[(fixed >= r0) & (fixed < r1)] - r0
         assert np.array_equal(mine, single.boundary_dofs())
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_br_h1_bestapproximation_of_linear_fields(G, O, dim):
+    """The reference's H1 best-approximation test for H1BR{2} / H1BR{3}
+    (test/runtests.jl:425-470, expected order 1): the vector Laplace problem
+    of the BR element (nu = 1, no penalty, zero load) with a linear field
+    as boundary data returns that field (vertex values, zero bubbles)."""
+    g = G.grid_unitsquare(4) if dim == 2 else G.grid_unitcube_kuhn(2)
+    rng = np.random.default_rng(17)
+    M, c0 = rng.standard_normal((dim, dim)), rng.standard_normal(dim)
+    vals = g.coords @ M.T + c0
+    ub = np.concatenate([vals.T.ravel(), np.zeros(g.faces()[0].shape[0])])
+    u, p, _ = O.stokes_iterated_penalty(g, 1.0, 0.0, np.zeros((1, 5)), sweeps=1, bonus_quadorder=0, u_boundary=ub)
+    assert np.max(np.abs(u - ub)) < 1e-12
