@@ -185,7 +185,8 @@ _P2_EDGES = {2: [(0, 1), (1, 2), (2, 0)], 3: [(0, 1), (0, 2), (0, 3), (1, 2), (1
 
 
 def interpolate(FES: FESpace, f, edge_points: int = 5) -> np.ndarray:
-    """interpolate!(Target, FES, f) for H1P1 and H1P2 (scalar or vector):
+    """interpolate!(Target, FES, f) for H1P1 and H1P2 (scalar or vector) and
+    H1BR (see _interpolate_br):
     vertex DoFs by point evaluation (point_evaluation!, src/fedefs/h1_p2.jl:
     47-59), P2 edge DoFs so that the interpolant keeps the mean of f on every
     edge (ensure_moments!, :61-71, :73-92), the mean taken with a Gauss rule of
@@ -195,6 +196,8 @@ def interpolate(FES: FESpace, f, edge_points: int = 5) -> np.ndarray:
     (m, ncomponents) or (m,).  Host-side, like the reference's."""
     g = FES.xgrid
     fe = FES.FEType
+    if fe.kind == FE_H1BR:
+        return _interpolate_br(FES, f)
     if fe.kind not in (FE_H1P1, FE_H1P2):
         raise ValueError(f"interpolate: element {fe} not supported")
     dim, nc = g.dim, fe.ncomponents
@@ -223,3 +226,64 @@ def interpolate(FES: FESpace, f, edge_points: int = 5) -> np.ndarray:
             for c in range(nc):
                 out[cd[:, c * nb + nv + e]] = dofv[:, c]
     return out
+
+
+def _interpolate_br(FES: FESpace, f) -> np.ndarray:
+    """interpolate!(Target, FES, f) for H1BR{dim} (src/fedefs/h1v_br.jl:41-99):
+    vertex DoFs of every component by point evaluation, then the bubble of
+    face F set to (1/|F|) int_F (f - I_1 f) . n_F, with I_1 f the vertex
+    interpolant (its face integral |F| times the mean of the face's vertex
+    values) -- the bubbles have face mean 1, so the interpolant keeps every
+    face's normal flux of f.  The face integrals use a rule exact for
+    polynomials of degree 5 (Gauss on edges, Stroud's conical rule on
+    triangles)."""
+    g = FES.xgrid
+    dim = g.dim
+    fn, _ = g.faces()
+    nrm, fvol, _ = g.face_geometry()
+    nn = g.nverts
+
+    def ev(x):
+        return np.asarray(f(x), dtype=np.float64).reshape(x.shape[0], dim)
+
+    out = np.zeros(FES.ndofs)
+    vv = ev(g.coords)                                   # (nverts, dim)
+    for c in range(dim):
+        out[c * nn:(c + 1) * nn] = vv[:, c]
+    P = g.coords[fn]                                    # (nfaces, dim, dim): the faces' vertices
+    if dim == 2:
+        t, w = np.polynomial.legendre.leggauss(3)
+        t, w = 0.5 * (t + 1.0), 0.5 * w
+        pts = [((1.0 - tk) * P[:, 0] + tk * P[:, 1], wk) for tk, wk in zip(t, w)]
+    else:
+        s1, w1 = np.polynomial.legendre.leggauss(3)
+        s1, w1 = 0.5 * (s1 + 1.0), 0.5 * w1
+        s2, w2 = _gauss_jacobi_10(3)
+        pts = []
+        for a, wa in zip(s1, w1):            # conical product: (s, r (1 - s)) on the unit triangle
+            for b, wb in zip(s2, w2):
+                x1, x2 = b, a * (1.0 - b)
+                pts.append((P[:, 0] + x1 * (P[:, 1] - P[:, 0]) + x2 * (P[:, 2] - P[:, 0]), 2.0 * wa * wb))
+    mean = np.zeros((fn.shape[0], dim))
+    for x, wk in pts:
+        mean += wk * ev(x)
+    vmean = vv[fn].mean(axis=1)                         # mean of the vertex interpolant on the face
+    out[dim * nn:] = np.einsum("fc,fc->f", mean - vmean, nrm)
+    return out
+
+
+def _gauss_jacobi_10(n: int):
+    """n-point Gauss rule on [0, 1] for the weight (1 - s): nodes and weights
+    (the collapsed direction of the conical triangle rule), from the
+    eigenvalues of the Jacobi matrix of that weight."""
+    # monic recurrence of the Jacobi polynomials P^(1,0) mapped to [0, 1]
+    k = np.arange(n, dtype=np.float64)
+    a, b = 1.0, 0.0
+    alpha = (b * b - a * a) / ((2 * k + a + b) * (2 * k + a + b + 2))
+    kk = np.arange(1, n, dtype=np.float64)
+    beta = 4 * kk * (kk + a) * (kk + b) * (kk + a + b) / ((2 * kk + a + b) ** 2 * (2 * kk + a + b + 1) *
+                                                          (2 * kk + a + b - 1))
+    J = np.diag(alpha) + np.diag(np.sqrt(beta), 1) + np.diag(np.sqrt(beta), -1)
+    x, V = np.linalg.eigh(J)
+    w = 2.0 ** (a + b + 1) / (a + b + 1) * V[0] ** 2     # mu_0 = int_{-1}^{1} (1 - x) dx = 2
+    return 0.5 * (x + 1.0), 0.25 * w                     # to [0, 1]: int_0^1 (1 - s) ds = 1/2

@@ -355,3 +355,31 @@ def test_oracle_br_h1_bestapproximation_of_linear_fields(G, O, dim):
     ub = np.concatenate([vals.T.ravel(), np.zeros(g.faces()[0].shape[0])])
     u, p, _ = O.stokes_iterated_penalty(g, 1.0, 0.0, np.zeros((1, 5)), sweeps=1, bonus_quadorder=0, u_boundary=ub)
     assert np.max(np.abs(u - ub)) < 1e-12
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_br_interpolation_keeps_face_fluxes(G, O, dim):
+    """interpolate! for H1BR (src/fedefs/h1v_br.jl:41-99): linear fields give
+    their vertex values and zero bubbles, and for a quadratic field every
+    face's normal flux is kept, so each cell mean of div(I u), computed by
+    the oracle's BR divergence, equals the cell mean of div u."""
+    from grmp_gb300 import fespace as F
+    g = G.grid_unitsquare(4) if dim == 2 else G.grid_unitcube_kuhn(2)
+    S = F.FESpace(F.H1BR(dim), g)
+    rng = np.random.default_rng(8)
+    M, c0 = rng.standard_normal((dim, dim)), rng.standard_normal(dim)
+    lin = F.interpolate(S, lambda x: x @ M.T + c0)
+    assert np.max(np.abs(lin[dim * g.nverts:])) < 1e-13
+    assert np.max(np.abs(lin[:dim * g.nverts] - (g.coords @ M.T + c0).T.ravel())) < 1e-14
+    Q = rng.standard_normal((dim, dim, dim))        # u_c = sum_jk Q[c,j,k] x_j x_k
+
+    def u(x):
+        return np.einsum("cjk,mj,mk->mc", Q, x, x)
+
+    Iu = F.interpolate(S, u)
+    _, _, _, cd, args = O.br_stokes_system(g, 1.0, 0.0, np.zeros((1, 5)), bonus_quadorder=0)
+    divh, _ = O.br_div(g, args, u=Iu)
+    # div u = sum_c sum_k (Q[c,c,k] + Q[c,k,c]) x_k: linear, its cell mean is its value at the centroid
+    cen = g.coords[g.cells].mean(axis=1)
+    divx = np.einsum("ck,mk->m", np.stack([Q[c, c, :] + Q[c, :, c] for c in range(dim)]), cen)
+    assert np.max(np.abs(divh - divx)) < 1e-12 * max(1.0, np.max(np.abs(divx)))
