@@ -102,6 +102,8 @@ SIGNATURES = {
     "grmp_context_memory": ([_vp, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "grmp_context_launches": ([_vp, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "grmp_vector_device_ptr": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
+    "grmp_context_set_wait_limit": ([_vp, ctypes.c_int64], ctypes.c_int),
+    "grmp_selftest_wait_timeout": ([_vp, ctypes.c_int64, _pi32, _pi32], ctypes.c_int),
     "grmp_mesh_upload": ([_vp, ctypes.c_int, _i32, _pd, _i32, _pi32, ctypes.POINTER(_vp)], ctypes.c_int),
     "grmp_mesh_set_faces": ([_vp, _i32, _pi32, _pd, _pd, ctypes.POINTER(ctypes.c_int8)], ctypes.c_int),
     "grmp_mesh_destroy": ([_vp], ctypes.c_int),

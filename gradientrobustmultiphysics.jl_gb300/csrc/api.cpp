@@ -117,6 +117,13 @@ int grmp_context_launches(grmp_context ctx, uint64_t *launches) {
     return GRMP_OK;
 }
 
+int grmp_context_set_wait_limit(grmp_context ctx, int64_t polls) {
+    if (!valid_ctx(ctx) || polls < 0) return GRMP_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->wait_limit = polls > 0 ? (long long)polls : GRMP_SPIN_LIMIT;
+    return GRMP_OK;
+}
+
 int grmp_vector_device_ptr(grmp_vector v, void **dptr) {
     if (!v || !dptr) return GRMP_ERR_INVALID_ARG;
     *dptr = (void *)v->d;

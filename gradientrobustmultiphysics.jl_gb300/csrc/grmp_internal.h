@@ -18,7 +18,7 @@ constexpr int GRMP_MAX_LDOFS = 32;      // local DoFs per cell (mask width)
 constexpr int GRMP_MAX_ROW_NNZ = 512;   // pattern build: per-row column list
 constexpr int GRMP_MAXQ = 128;          // quadrature points
 constexpr int GRMP_MAX_TERMS = 4;       // operator terms per assembly call
-constexpr long long GRMP_SPIN_LIMIT = 1LL << 24;   // bounded device waits
+constexpr long long GRMP_SPIN_LIMIT = 1LL << 24;   // bounded device waits (default polls per wait)
 
 // ---------------------------------------------------------------- handles
 struct grmp_context_s {
@@ -27,6 +27,7 @@ struct grmp_context_s {
     size_t budget = 0;       // 0 = unlimited
     size_t in_use = 0;
     int num_sms = 0;
+    long long wait_limit = GRMP_SPIN_LIMIT;   // polls of a bounded device wait in this context's solves
     std::atomic<unsigned long long> launches{0};
     std::string last_error;
     std::mutex mu;
@@ -168,7 +169,7 @@ int grmp_upload(grmp_context ctx, T **dst, const T *src, size_t count) {
 // ---------------------------------------------------------------- device helpers
 #ifdef __CUDACC__
 // Grid-wide barrier for a cooperative (co-resident) launch.  Every wait is
-// bounded: after GRMP_SPIN_LIMIT polls the waiting block records
+// bounded: after `limit` polls (about 64 ns each) the waiting block records
 // GRMP_ERR_TIMEOUT in *status and leaves; callers check the return value
 // and exit their loops.
 struct GridBarrier {
@@ -176,7 +177,8 @@ struct GridBarrier {
     unsigned int gen;
 };
 
-__device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nblocks, int *status) {
+__device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nblocks, int *status,
+                                             long long limit = GRMP_SPIN_LIMIT) {
     __shared__ int ok;   // one answer for the whole block, so its threads leave together
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -191,7 +193,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nbloc
         } else {
             long long spins = 0;
             while (*vgen == g) {
-                if (++spins > GRMP_SPIN_LIMIT) {
+                if (++spins > limit) {
                     atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
                     break;
                 }

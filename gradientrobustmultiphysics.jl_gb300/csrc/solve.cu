@@ -78,12 +78,13 @@ __device__ __forceinline__ void block_sum(double *v, double *sh /* [32*NV] */) {
 constexpr int kPartStride = 4 * 4096;   // doubles per buffer (4 values x up to 4096 blocks)
 
 template <int NV>
-__device__ __forceinline__ bool grid_sum(double *v, double *partial_area, double *sh, SolveState *st, int &round) {
+__device__ __forceinline__ bool grid_sum(double *v, double *partial_area, double *sh, SolveState *st, int &round,
+                                         long long spin) {
     double *partial = partial_area + (round++ & 1) * kPartStride;
     block_sum<NV>(v, sh);
     if (threadIdx.x == 0)
         for (int k = 0; k < NV; k++) partial[blockIdx.x * 4 + k] = v[k];
-    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return false;
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return false;
     double acc[NV];
     for (int k = 0; k < NV; k++) acc[k] = 0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
@@ -114,12 +115,13 @@ __device__ __forceinline__ void block_sum_f(float *v, float *sh /* [32*NV] */) {
 }
 
 template <int NV>
-__device__ __forceinline__ bool grid_sum_f(float *v, double *partial_area, float *sh, SolveState *st, int &round) {
+__device__ __forceinline__ bool grid_sum_f(float *v, double *partial_area, float *sh, SolveState *st, int &round,
+                                           long long spin) {
     float *partial = reinterpret_cast<float *>(partial_area + (round++ & 1) * kPartStride);
     block_sum_f<NV>(v, sh);
     if (threadIdx.x == 0)
         for (int k = 0; k < NV; k++) partial[blockIdx.x * 4 + k] = v[k];
-    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return false;
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return false;
     float acc[NV];
     for (int k = 0; k < NV; k++) acc[k] = 0.f;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
@@ -284,14 +286,15 @@ template <int TPR, int U, bool PIPE>
 __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
                                                 const double *vals, const double *b, double *x, const double *dinv,
                                                 double *r, double *z, double *p, double *q, double *partial,
-                                                SolveState *st, double abstol, double reltol, int maxit, int guess) {
+                                                SolveState *st, double abstol, double reltol, int maxit, int guess,
+                                                long long spin) {
     __shared__ double sh[32 * 4];
     int round = 0;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // r = b - A x  (or b)
     if (guess) spmv_grid<TPR, U, PIPE, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
-    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
     double v[3] = {0, 0, 0};
     for (int i = gtid; i < n; i += gsz) {
         double ri = guess ? r[i] : b[i];
@@ -303,7 +306,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
         v[1] += ri * ri;
         v[2] += b[i] * b[i];
     }
-    if (!grid_sum<3>(v, partial, sh, st, round)) return;
+    if (!grid_sum<3>(v, partial, sh, st, round, spin)) return;
     double rz = v[0], rr = v[1];
     const double bn = sqrt(v[2]);
     const double tol = fmax(abstol, reltol * bn);
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
     while (!conv && it < maxit) {
         double d[1];
         d[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
-        if (!grid_sum<1>(d, partial, sh, st, round)) return;
+        if (!grid_sum<1>(d, partial, sh, st, round, spin)) return;
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
             w[0] += ri * zi;
             w[1] += ri * ri;
         }
-        if (!grid_sum<2>(w, partial, sh, st, round)) return;
+        if (!grid_sum<2>(w, partial, sh, st, round, spin)) return;
         it++;
         rr = w[1];
         conv = sqrt(rr) <= tol;
@@ -337,13 +340,13 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
         const double beta = w[0] / rz;
         rz = w[0];
         for (int i = gtid; i < n; i += gsz) p[i] = z[i] + beta * p[i];
-        if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+        if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
     }
     // true residual in FP64
-    if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
     double t[1];
     t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
-    if (!grid_sum<1>(t, partial, sh, st, round)) return;
+    if (!grid_sum<1>(t, partial, sh, st, round, spin)) return;
     if (gtid == 0) {
         st->iters = it;
         st->outer = 0;
@@ -408,7 +411,7 @@ template <class SP>
 __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, double *x, const float *dinv, float *r,
                                                float *q, float *xc, float2 *zp0, float2 *zp1, double *r64,
                                                double *partial, SolveState *st, double abstol, double reltol,
-                                               double delta, int maxit, int maxouter, int guess) {
+                                               double delta, int maxit, int maxouter, int guess, long long spin) {
     __shared__ double sh[32 * 4];
     __shared__ float shf[32 * 4];
     int round = 0;
@@ -426,7 +429,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
         }
     }
     for (int i = gtid; i < n; i += gsz) v[1] += b[i] * b[i];
-    if (!grid_sum<2>(v, partial, sh, st, round)) return;
+    if (!grid_sum<2>(v, partial, sh, st, round, spin)) return;
     const double bn = sqrt(v[1]);
     const double tol = fmax(abstol, reltol * bn);
     double rn64 = sqrt(v[0]);
@@ -443,7 +446,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
         wf += ri * zi;
     }
     float w[1] = {wf};
-    if (!grid_sum_f<1>(w, partial, shf, st, round)) return;
+    if (!grid_sum_f<1>(w, partial, shf, st, round, spin)) return;
     // inner-iteration scalars in FP32 (the FP64 pipe is scarce)
     float rz = w[0];
     float rmax = (float)rn64;
@@ -455,7 +458,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
     const int n4 = n >> 2;
     while (!conv && it < maxit && outer < maxouter) {
         float d[1] = {sp.fused_zp(cur, nxt, q, beta)};
-        if (!grid_sum_f<1>(d, partial, shf, st, round)) return;   // barrier 1
+        if (!grid_sum_f<1>(d, partial, shf, st, round, spin)) return;   // barrier 1
         const float pq = d[0];
         if (!(pq > 0.f) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
@@ -505,7 +508,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
             }
         }
         float u[2] = {uf0, uf1};
-        if (!grid_sum_f<2>(u, partial, shf, st, round)) return;   // barrier 2
+        if (!grid_sum_f<2>(u, partial, shf, st, round, spin)) return;   // barrier 2
         it++;
         float rz_new = u[0];
         const float rn32 = sqrtf(u[1]);
@@ -516,10 +519,10 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
                 x[i] += (double)xc[i];
                 xc[i] = 0.0f;
             }
-            if (!grid_barrier(&st->bar, gridDim.x, &st->status)) return;
+            if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
             double t[1];
             t[0] = sp.resid64(x, r64, b);
-            if (!grid_sum<1>(t, partial, sh, st, round)) return;
+            if (!grid_sum<1>(t, partial, sh, st, round, spin)) return;
             outer++;
             rn64 = sqrt(t[0]);
             conv = rn64 <= tol;
@@ -542,7 +545,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
                 yf += ri * zi;
             }
             float y[1] = {yf};
-            if (!grid_sum_f<1>(y, partial, shf, st, round)) return;
+            if (!grid_sum_f<1>(y, partial, shf, st, round, spin)) return;
             rz_new = y[0];
             rmax = (float)rn64;
         }
@@ -566,10 +569,10 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
                                                     double *x, const float *dinv, float *r, float *q, float *xc,
                                                     float2 *zp0, float2 *zp1, double *r64, double *partial,
                                                     SolveState *st, double abstol, double reltol, double delta,
-                                                    int maxit, int maxouter, int guess) {
+                                                    int maxit, int maxouter, int guess, long long spin) {
     RowsSpmv<TPR, U, PIPE> sp{n, rowptr, cols, vals64, pack32};
     pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
-                   guess);
+                   guess, spin);
 }
 
 // ------------------------------------------------------------ staged mixed PCG
@@ -613,8 +616,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
     return done != 0;
 }
 // bounded wait for the completion of the phase with the given parity
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-    for (long long spins = 0; spins < GRMP_SPIN_LIMIT; spins++)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long long limit) {
+    for (long long spins = 0; spins < limit; spins++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -641,10 +644,11 @@ struct StagedSpmv {
     unsigned consumed;      // windows consumed so far (all threads)
     unsigned issued;        // windows issued so far (issuing thread only)
     int *status;
+    long long spin;         // polls of a bounded mbarrier wait
 
     __device__ __forceinline__ bool issue_one() {
         const unsigned qn = issued, s = qn % S;
-        if (qn >= (unsigned)S && !mbar_wait(&empty[s], (qn / S - 1) & 1)) return false;
+        if (qn >= (unsigned)S && !mbar_wait(&empty[s], (qn / S - 1) & 1, spin)) return false;
         mbar_arrive_expect_tx(&full[s], kStgRec);
         bulk_load(stage + (size_t)s * kStgRec, rec + (size_t)(jb + (int)(qn % (unsigned)cnt)) * kStgRec, kStgRec,
                   &full[s]);
@@ -662,11 +666,13 @@ struct StagedSpmv {
     }
     // wait (bounded) for the copies still in flight before the block exits:
     // the last copy issued into each stage (copies into one stage are
-    // serialised by its release barrier)
+    // serialised by its release barrier).  This wait keeps the library's
+    // default bound even when the context's limit is lower: a copy in flight
+    // lands within microseconds, and the block must not leave before it does.
     __device__ __forceinline__ void drain() {
         if (threadIdx.x == 0 && cnt > 0)
             for (unsigned qn = issued > (unsigned)S ? issued - S : 0u; qn < issued; qn++)
-                if (!mbar_wait(&full[qn % S], (qn / S) & 1)) break;
+                if (!mbar_wait(&full[qn % S], (qn / S) & 1, spin > GRMP_SPIN_LIMIT ? spin : GRMP_SPIN_LIMIT)) break;
         __syncthreads();
     }
 
@@ -690,7 +696,7 @@ struct StagedSpmv {
             int T = 0;   // row steps of the windows before this one
             for (int m = 0; m < cnt; m++) {
                 const unsigned qn = consumed + m, s = qn % S;
-                if (!mbar_wait(&full[s], (qn / S) & 1)) {
+                if (!mbar_wait(&full[s], (qn / S) & 1, spin)) {
                     atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
                     break;
                 }
@@ -761,7 +767,7 @@ __global__ void __launch_bounds__(NT, 2048 / NT / 2) k_pcg_mixed_staged(int n, c
                                                             float2 *zp1, double *r64,
                                                             double *partial, SolveState *st, double abstol,
                                                             double reltol, double delta, int maxit, int maxouter,
-                                                            int guess) {
+                                                            int guess, long long spin) {
     extern __shared__ __align__(128) char stage_smem[];
     __shared__ __align__(8) uint64_t bars[2 * S];
     using SP = StagedSpmv<TPR, U, NT, S>;
@@ -779,6 +785,7 @@ __global__ void __launch_bounds__(NT, 2048 / NT / 2) k_pcg_mixed_staged(int n, c
     sp.consumed = 0;
     sp.issued = 0;
     sp.status = &st->status;
+    sp.spin = spin;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
             mbar_init(&sp.full[s], 1);
@@ -789,7 +796,7 @@ __global__ void __launch_bounds__(NT, 2048 / NT / 2) k_pcg_mixed_staged(int n, c
     __syncthreads();
     sp.prologue();
     pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
-                   guess);
+                   guess, spin);
     sp.drain();
 }
 
@@ -991,7 +998,8 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
         const double *vv = A->d_vals64, *bb = bvec;
         double *xx = xvec;
-        void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess};
+        long long spin = ctx->wait_limit;
+        void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess, &spin};
         cudaEventRecord(e0, ctx->stream);
         e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
         GRMP_LAUNCHED(ctx);
@@ -1010,8 +1018,9 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         const double *v64 = A->d_vals64, *bb = bvec;
         const int2 *v32 = (const int2 *)A->d_pack32;
         double *xx = xvec;
+        long long spin = ctx->wait_limit;
         void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
-                        &at, &rt, &dl, &mi, &mo, &guess};
+                        &at, &rt, &dl, &mi, &mo, &guess, &spin};
         cudaEventRecord(e0, ctx->stream);
         e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
         GRMP_LAUNCHED(ctx);
@@ -1081,8 +1090,9 @@ int launch_pcg_staged(grmp_matrix A, const double *bvec, double *xvec, const grm
     const double *v64 = A->d_vals64, *bb = bvec;
     const char *rec = A->d_stg_rec;
     double *xx = xvec;
+    long long spin = ctx->wait_limit;
     void *args[] = {&nn, &rp, &ci, &v64, &rec, &nw, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
-                    &at, &rt, &dl, &mi, &mo, &guess};
+                    &at, &rt, &dl, &mi, &mo, &guess, &spin};
     cudaEventRecord(e0, ctx->stream);
     e = cudaLaunchCooperativeKernel((void *)kern, grid, NT, args, (size_t)dyn, ctx->stream);
     GRMP_LAUNCHED(ctx);
@@ -1287,6 +1297,61 @@ int grmp_spmv_impl(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {
 }
 
 // ---------------------------------------------------------------------------
+// Failure-detection check of the bounded waits (grmp_selftest_wait_timeout):
+// every block waits on a shared-memory mbarrier that nothing completes, then
+// block 0 leaves while the others wait at a grid barrier it never reaches.
+// Both waits give up after `spin` polls and record GRMP_ERR_TIMEOUT; the
+// kernel then ends normally, so the context stays usable.
+namespace {
+__global__ void k_wait_selftest(GridBarrier *bar, int *grid_status, int *mbar_status, long long spin) {
+    __shared__ __align__(8) uint64_t mb;
+    if (threadIdx.x == 0) {
+        mbar_init(&mb, 1);   // one arrival expected; none is ever made
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait(&mb, 0, spin)) atomicCAS(mbar_status, 0, (int)GRMP_ERR_TIMEOUT);
+    __syncthreads();
+    if (blockIdx.x == 0) return;   // the block that never arrives
+    grid_barrier(bar, gridDim.x, grid_status, spin);
+}
+}  // namespace
+
+extern "C" int grmp_selftest_wait_timeout(grmp_context ctx, int64_t polls, int32_t *grid_status,
+                                          int32_t *mbar_status) {
+    if (!ctx || !ctx->stream || polls < 0 || !grid_status || !mbar_status) return GRMP_ERR_INVALID_ARG;
+    cudaError_t se = cudaSetDevice(ctx->device);
+    if (se != cudaSuccess) return grmp_cuda_fail(ctx, se, "wait self-test: cudaSetDevice");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    struct Words {
+        GridBarrier bar;
+        int grid_status, mbar_status;
+    };
+    Words *d = nullptr;
+    int rc = grmp_alloc(ctx, (void **)&d, sizeof(Words));
+    if (rc) return rc;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wait_selftest, 128, 0);
+    const int grid = std::max(2, std::min(2, per_sm) * ctx->num_sms);
+    GridBarrier *bar = &d->bar;
+    int *gs = &d->grid_status, *ms = &d->mbar_status;
+    long long spin = (long long)polls;
+    void *args[] = {&bar, &gs, &ms, &spin};
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(Words), ctx->stream);
+    if (e == cudaSuccess) e = cudaLaunchCooperativeKernel((void *)k_wait_selftest, grid, 128, args, 0, ctx->stream);
+    GRMP_LAUNCHED(ctx);
+    Words h;
+    std::memset(&h, 0, sizeof(h));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    grmp_free(ctx, d, sizeof(Words));
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "wait self-test launch");
+    *grid_status = h.grid_status;
+    *mbar_status = h.mbar_status;
+    return GRMP_OK;
+}
+
+// ---------------------------------------------------------------------------
 // FP64 PCG without device allocation (grmp_solve_fp64_noalloc).
 //
 // The work arrays are a file-scope device array sized for
@@ -1329,10 +1394,10 @@ int noalloc_scratch(grmp_context ctx, char **out) {
 
 template <int TPR, int U, bool PIPE>
 cudaError_t launch_pcg64_static(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
-                                char *work, int *grid_out) {
+                                int grid_blocks, char *work, int *grid_out) {
     grmp_context ctx = A->space->mesh->ctx;
     auto kern = k_pcg64<TPR, U, PIPE>;
-    int grid = coop_grid(ctx, kern, A->nrows, p->grid_blocks);
+    int grid = coop_grid(ctx, kern, A->nrows, grid_blocks);
     double *dinv = (double *)work, *r = (double *)(work + kNaVec), *z = (double *)(work + 2 * kNaVec);
     double *pp = (double *)(work + 3 * kNaVec), *q = (double *)(work + 4 * kNaVec);
     double *part = (double *)(work + 5 * kNaVec);
@@ -1342,7 +1407,8 @@ cudaError_t launch_pcg64_static(grmp_matrix A, const double *bvec, double *xvec,
     const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
     const double *vv = A->d_vals64, *bb = bvec;
     double *xx = xvec;
-    void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess};
+    long long spin = ctx->wait_limit;
+    void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess, &spin};
     *grid_out = grid;
     cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
     GRMP_LAUNCHED(ctx);
@@ -1361,13 +1427,15 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
     if (b->n != A->nrows || x->n != A->nrows) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: size mismatch");
     if (p->mode != GRMP_SOLVE_FP64)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "noalloc solve: only mode GRMP_SOLVE_FP64");
-    if (!(p->reltol >= 0) || !(p->abstol >= 0) || p->maxiter <= 0) return GRMP_ERR_INVALID_ARG;
+    if (!(p->reltol >= 0) || !(p->abstol >= 0) || p->maxiter <= 0)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: invalid tolerance or maxiter");
     if (A->nrows > GRMP_NOALLOC_MAX_ROWS)
         return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: %d rows exceed the fixed scratch limit of %d rows",
                          A->nrows, GRMP_NOALLOC_MAX_ROWS);
     if (!A->has64) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: FP64 values not assembled");
     const auto t0 = std::chrono::steady_clock::now();
-    cudaSetDevice(ctx->device);
+    cudaError_t se = cudaSetDevice(ctx->device);
+    if (se != cudaSuccess) return grmp_cuda_fail(ctx, se, "noalloc solve: cudaSetDevice");
     std::lock_guard<std::mutex> lk(ctx->mu);
     char *work = nullptr;
     int rc = noalloc_scratch(ctx, &work);
@@ -1386,20 +1454,27 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "noalloc solve: jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "noalloc solve: non-positive or non-finite diagonal entry");
-    int cfg = p->spmv_config > 0 ? p->spmv_config : (A->tuned_cfg ? A->tuned_cfg : heuristic_config(A, false));
+    // spmv_config 0 takes grmp_solve's tuned configuration and grid when there are
+    // any (so both entry points run the same launch), else the heuristic
+    int cfg = p->spmv_config;
+    int gb = p->grid_blocks;
+    if (cfg <= 0) {
+        cfg = A->tuned_cfg ? A->tuned_cfg : heuristic_config(A, false);
+        if (A->tuned_cfg && gb <= 0) gb = A->tuned_grid;
+    }
     int grid = 0;
     switch (cfg) {
-        case 208: e = launch_pcg64_static<2, 8, false>(A, b->d, x->d, p, work, &grid); break;
-        case 404: e = launch_pcg64_static<4, 4, false>(A, b->d, x->d, p, work, &grid); break;
-        case 408: e = launch_pcg64_static<4, 8, false>(A, b->d, x->d, p, work, &grid); break;
-        case 804: e = launch_pcg64_static<8, 4, false>(A, b->d, x->d, p, work, &grid); break;
-        case 1602: e = launch_pcg64_static<16, 2, false>(A, b->d, x->d, p, work, &grid); break;
-        case 10204: e = launch_pcg64_static<2, 4, true>(A, b->d, x->d, p, work, &grid); break;
-        case 10404: e = launch_pcg64_static<4, 4, true>(A, b->d, x->d, p, work, &grid); break;
-        case 10408: e = launch_pcg64_static<4, 8, true>(A, b->d, x->d, p, work, &grid); break;
-        case 10804: e = launch_pcg64_static<8, 4, true>(A, b->d, x->d, p, work, &grid); break;
-        case 10402: e = launch_pcg64_static<4, 2, true>(A, b->d, x->d, p, work, &grid); break;
-        case 10802: e = launch_pcg64_static<8, 2, true>(A, b->d, x->d, p, work, &grid); break;
+        case 208: e = launch_pcg64_static<2, 8, false>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 404: e = launch_pcg64_static<4, 4, false>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 408: e = launch_pcg64_static<4, 8, false>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 804: e = launch_pcg64_static<8, 4, false>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 1602: e = launch_pcg64_static<16, 2, false>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 10204: e = launch_pcg64_static<2, 4, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 10404: e = launch_pcg64_static<4, 4, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 10408: e = launch_pcg64_static<4, 8, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 10804: e = launch_pcg64_static<8, 4, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 10402: e = launch_pcg64_static<4, 2, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 10802: e = launch_pcg64_static<8, 2, true>(A, b->d, x->d, p, gb, work, &grid); break;
         default: return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_config: unknown configuration %d", cfg);
     }
     SolveState hs;

@@ -69,6 +69,21 @@ int grmp_synchronize(grmp_context ctx);
 int grmp_context_memory(grmp_context ctx, size_t *bytes_in_use);
 /* Number of kernels this context has launched so far (instrumentation). */
 int grmp_context_launches(grmp_context ctx, uint64_t *launches);
+/* Polls (about 64 ns each) after which a bounded device-side wait of this
+ * context's iterative solves gives up and the solve returns GRMP_ERR_TIMEOUT
+ * (grid barriers of the persistent kernels, mbarrier waits of the staged
+ * SpMV); 0 restores the default of 2^24.  No reference counterpart (the
+ * reference has no device waits); it lets a caller bound how long a stalled
+ * solve holds the GPU, and lets a test make a wait run out. */
+int grmp_context_set_wait_limit(grmp_context ctx, int64_t polls);
+/* Failure-detection check of the bounded waits: one cooperative launch in
+ * which every block waits on a shared-memory mbarrier that nothing
+ * completes, then block 0 leaves while the other blocks wait at a grid
+ * barrier it never reaches.  Both waits give up after `polls` polls; the
+ * statuses the waiting blocks recorded are returned in *grid_status and
+ * *mbar_status (GRMP_ERR_TIMEOUT when the bounds work).  Nothing faults or
+ * hangs and the context stays usable.  No reference counterpart. */
+int grmp_selftest_wait_timeout(grmp_context ctx, int64_t polls, int32_t *grid_status, int32_t *mbar_status);
 /* Device address of a vector's FP64 data (for coef_on_device inputs). */
 int grmp_vector_device_ptr(grmp_vector v, void **dptr);
 

@@ -19,14 +19,46 @@
  * that the drop-exact-zero sparsity rule (src/fematrix.jl:54-65) sees the same
  * floating-point zeros.  Build with -ffp-contract=off (no fused multiply-add),
  * which is what Julia does for plain `a*b + c`.
+ *
+ * Threads: the global assembly loops are run by OpenMP threads that each own
+ * a contiguous range of rows (DoFs).  Every thread walks all cells in
+ * ascending order and applies only the updates whose row it owns, so each row
+ * receives exactly the additions of the sequential loop, in the same order:
+ * the result is bit-identical to the single-threaded reference loop for any
+ * thread count (cells spanning several row ranges are evaluated by each of
+ * their owners).
  */
+
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define OR_MAXQ 128
 #define OR_MAXD 32
+
+/* Row range [lo, hi) of the calling thread (the whole range outside a
+ * parallel region). */
+static void or_row_range(int n, int *lo, int *hi)
+{
+#ifdef _OPENMP
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+#else
+    const int t = 0, nt = 1;
+#endif
+    *lo = (int)((long long)n * t / nt);
+    *hi = (int)((long long)n * (t + 1) / nt);
+}
+
+static int or_touches(const int *dofs, int nd, int lo, int hi)
+{
+    for (int i = 0; i < nd; i++)
+        if (dofs[i] >= lo && dofs[i] < hi) return 1;
+    return 0;
+}
 
 /* ------------------------------------------------------------------------- */
 /* Quadrature (src/quadrature.jl)                                            */
@@ -462,23 +494,32 @@ static int cmp_colval(const void *a, const void *b)
     return (ca > cb) - (ca < cb);
 }
 
-/* Export as CSR with columns ascending. */
+/* Export as CSR with columns ascending (rows sorted independently, in
+ * parallel). */
 void oracle_mat_csr(void *h, long long *rowptr, int *cols, double *vals)
 {
     omat *m = (omat *)h;
-    long long p = 0;
     typedef struct { int c; double v; } cv;
+    long long p = 0;
+    for (int i = 0; i < m->nrows; i++) {
+        rowptr[i] = p;
+        p += m->rows[i].n;
+    }
+    rowptr[m->nrows] = p;
+#pragma omp parallel
+    {
     cv *buf = NULL; int bcap = 0;
+#pragma omp for schedule(static)
     for (int i = 0; i < m->nrows; i++) {
         orow *r = &m->rows[i];
-        rowptr[i] = p;
         if (r->n > bcap) { bcap = r->n; buf = (cv *)realloc(buf, sizeof(cv) * (size_t)bcap); }
         for (int k = 0; k < r->n; k++) { buf[k].c = r->col[k]; buf[k].v = r->val[k]; }
         qsort(buf, (size_t)r->n, sizeof(cv), cmp_colval);
-        for (int k = 0; k < r->n; k++) { cols[p] = buf[k].c; vals[p] = buf[k].v; p++; }
+        long long q = rowptr[i];
+        for (int k = 0; k < r->n; k++) { cols[q] = buf[k].c; vals[q] = buf[k].v; q++; }
     }
-    rowptr[m->nrows] = p;
     free(buf);
+    }
 }
 
 /* apply_penalties! (src/fematrix.jl:349-355): A[d,d] = penalty. */
@@ -605,10 +646,15 @@ int oracle_assemble_bilinear(void *h, int dim, int nverts, const double *coords,
     double *vals = (double *)malloc(sizeof(double) * (size_t)nq * nb);
     double *derivs = (double *)malloc(sizeof(double) * (size_t)nq * nb * dim);
     oracle_basis_tables(fe, dim, nq, xref, vals, derivs);
+#pragma omp parallel
+    {
+    int lo, hi;
+    or_row_range(m->nrows, &lo, &hi);
     double *cv = (double *)malloc(sizeof(double) * (size_t)nq * nd * 6 * 3);
     double *loc = (double *)malloc(sizeof(double) * (size_t)nd * nd);
     double X[4 * 3];
     for (int cell = 0; cell < ncells; cell++) {
+        if (!or_touches(&celldofs[(size_t)cell * nd], nd, lo, hi)) continue;
         for (int v = 0; v <= dim; v++)
             for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cellnodes[(size_t)cell * (dim + 1) + v] * dim + k];
         double A[3][3], G[3][3], det, vol;
@@ -641,19 +687,25 @@ int oracle_assemble_bilinear(void *h, int dim, int nverts, const double *coords,
             }
         double itemfactor = vol * factor;
         const int *dofs = &celldofs[(size_t)cell * nd];
+#define OR_MINE(r) ((r) >= lo && (r) < hi)
         if (symmetric) {
             for (int i = 0; i < nd; i++)
                 for (int j = i + 1; j < nd; j++) {
-                    omat_addnz(m, dofs[i], dofs[j], loc[i * nd + j] * itemfactor, 1.0);
-                    omat_addnz(m, dofs[j], dofs[i], loc[i * nd + j] * itemfactor, 1.0);
+                    if (OR_MINE(dofs[i])) omat_addnz(m, dofs[i], dofs[j], loc[i * nd + j] * itemfactor, 1.0);
+                    if (OR_MINE(dofs[j])) omat_addnz(m, dofs[j], dofs[i], loc[i * nd + j] * itemfactor, 1.0);
                 }
-            for (int i = 0; i < nd; i++) omat_addnz(m, dofs[i], dofs[i], loc[i * nd + i] * itemfactor, 1.0);
+            for (int i = 0; i < nd; i++)
+                if (OR_MINE(dofs[i])) omat_addnz(m, dofs[i], dofs[i], loc[i * nd + i] * itemfactor, 1.0);
         } else {
             for (int i = 0; i < nd; i++)
-                for (int j = 0; j < nd; j++) omat_addnz(m, dofs[i], dofs[j], loc[i * nd + j] * itemfactor, 1.0);
+                if (OR_MINE(dofs[i]))
+                    for (int j = 0; j < nd; j++) omat_addnz(m, dofs[i], dofs[j], loc[i * nd + j] * itemfactor, 1.0);
         }
+#undef OR_MINE
     }
-    free(vals); free(derivs); free(cv); free(loc);
+    free(cv); free(loc);
+    }
+    free(vals); free(derivs);
     return nq;
 }
 
@@ -730,11 +782,19 @@ int oracle_assemble_linear(double *b, int dim, int nverts, const double *coords,
     double *vals = (double *)malloc(sizeof(double) * (size_t)nq * nb);
     double *derivs = (double *)malloc(sizeof(double) * (size_t)nq * nb * dim);
     oracle_basis_tables(fe, dim, nq, xref, vals, derivs);
+    int ndofs = 0;   /* rows: one past the largest DoF */
+    for (size_t k = 0; k < (size_t)ncells * nd; k++)
+        if (celldofs[k] + 1 > ndofs) ndofs = celldofs[k] + 1;
+#pragma omp parallel
+    {
+    int lo, hi;
+    or_row_range(ndofs, &lo, &hi);
     double G[3][3];
     double *cv = (double *)malloc(sizeof(double) * (size_t)nq * nd * 6);
     double *locb = (double *)malloc(sizeof(double) * (size_t)nd);
     double X[12];
     for (int cell = 0; cell < ncells; cell++) {
+        if (!or_touches(&celldofs[(size_t)cell * nd], nd, lo, hi)) continue;
         for (int v = 0; v <= dim; v++)
             for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cellnodes[(size_t)cell * (dim + 1) + v] * dim + k];
         double A[3][3], det, vol;
@@ -755,9 +815,14 @@ int oracle_assemble_linear(double *b, int dim, int nverts, const double *coords,
             }
         }
         double itemfactor = factor * vol;
-        for (int i = 0; i < nd; i++) b[celldofs[(size_t)cell * nd + i]] += locb[i] * itemfactor;
+        for (int i = 0; i < nd; i++) {
+            const int r = celldofs[(size_t)cell * nd + i];
+            if (r >= lo && r < hi) b[r] += locb[i] * itemfactor;
+        }
     }
-    free(vals); free(derivs); free(cv); free(locb);
+    free(cv); free(locb);
+    }
+    free(vals); free(derivs);
     return nq;
 }
 
@@ -904,6 +969,31 @@ int oracle_cg(int n, const long long *rp, const int *ci, const double *v, const 
     if (final_relres) *final_relres = rn / bn;
     free(r); free(z); free(p); free(q); free(dinv);
     return it;
+}
+
+/* r = b - A x with each row's sum carried in double-double and rounded once:
+ * products split exactly by fma (Dekker's TwoProduct), sums by Knuth's TwoSum,
+ * the low parts accumulated separately (the compensated dot product of Ogita,
+ * Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26,
+ * 2005).  The residual of iterative refinement in twice the working
+ * precision. */
+void oracle_resid_dd(int n, const long long *rp, const int *ci, const double *v, const double *x, const double *b,
+                     double *r)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        double hi = b[i], lo = 0.0;
+        for (long long k = rp[i]; k < rp[i + 1]; k++) {
+            const double p = -v[k] * x[ci[k]];
+            const double pe = fma(-v[k], x[ci[k]], -p);
+            const double s = hi + p;
+            const double bv = s - hi;
+            const double se = (hi - (s - bv)) + (p - bv);
+            hi = s;
+            lo += se + pe;
+        }
+        r[i] = hi + lo;
+    }
 }
 
 /* ------------------------------------------------------------------------- */

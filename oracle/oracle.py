@@ -84,6 +84,8 @@ def lib():
         L.oracle_item_l2error_br.restype = ctypes.c_int
         L.oracle_cg.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
         L.oracle_cg.restype = ctypes.c_int
+        L.oracle_resid_dd.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, dp]
+        L.oracle_resid_dd.restype = None
         sp = ctypes.POINTER(ctypes.c_byte)
         brm = [ctypes.c_int, dp, ip, ip, dp, dp, sp, ip]
         L.oracle_br_assemble.argtypes = [ctypes.c_void_p] + brm + [ctypes.c_double, dp, ctypes.c_double]
@@ -321,6 +323,49 @@ def solve_cg(A, b, reltol=1e-14, maxit=100000):
     rr = ctypes.c_double(0)
     it = lib().oracle_cg(n, _llp(rp), _ip(ci), _dp(v), _dp(bb), _dp(x), reltol, maxit, ctypes.byref(rr))
     return x, it, rr.value
+
+
+def resid_dd(A, x, b):
+    """b - A x with every row sum carried in double-double (grmp_oracle.c
+    oracle_resid_dd), rounded once to FP64."""
+    A = A.tocsr()
+    rp = np.ascontiguousarray(A.indptr, dtype=np.int64)
+    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+    v = np.ascontiguousarray(A.data, dtype=np.float64)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    r = np.empty(A.shape[0])
+    lib().oracle_resid_dd(A.shape[0], _llp(rp), _ip(ci), _dp(v), _dp(xx), _dp(bb), _dp(r))
+    return r
+
+
+def solve_refined(A, b, inner_reltol=1e-10, max_refine=8, maxit=200000, x0=None):
+    """FP64 solution of A x = b accurate to about the FP64 rounding of x, for
+    systems too large for a sparse-direct factorisation here: iterative
+    refinement whose residual is computed in double-double (resid_dd) and
+    whose corrections come from the FP64 Jacobi-CG of grmp_oracle.c, until a
+    correction is below 2 ulp of the solution norm.  With an extra-precise
+    residual the limiting accuracy does not grow with the condition number
+    (it needs only cond(A) * inner_reltol < 1).  x0: a starting solution
+    (e.g. an FP64 CG solve of the same system).  Returns (x, info) with
+    info = {"refinements", "cg_iterations", "last_correction", "relres"};
+    last_correction is ||dx|| / ||x|| of the final step, an estimate of the
+    remaining relative error."""
+    A = A.tocsr()
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(A.shape[0]) if x0 is None else np.array(x0, dtype=np.float64)
+    bn = max(np.linalg.norm(b), 1e-300)
+    its, corr, k = [], 1.0, 0
+    for k in range(1, max_refine + 1):
+        r = resid_dd(A, x, b)
+        d, it, _ = solve_cg(A, r, inner_reltol, maxit)
+        its.append(it)
+        x = x + d
+        corr = float(np.linalg.norm(d) / max(np.linalg.norm(x), 1e-300))
+        if corr <= 4.5e-16:
+            break
+    relres = float(np.linalg.norm(resid_dd(A, x, b)) / bn)
+    return x, {"refinements": k, "cg_iterations": its, "last_correction": corr, "relres": relres}
 
 
 if __name__ == "__main__":  # pragma: no cover - manual build helper

@@ -87,15 +87,6 @@ def test_invalid_handles_rejected(lib):
     assert p.reltol == 1e-12 and p.abstol == 1e-12
 
 
-def test_integration_notes_bind_every_symbol():
-    """The Julia-side bindings (the reference-side FFI a maintainer adds)
-    name every entry point the header declares."""
-    names = header_symbols()
-    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    missing = [n for n in names if n not in txt]
-    assert not missing, missing
-
-
 def test_build_compiles_every_source():
     """Every translation unit under csrc/ is in the build list (a file left
     out would not exist on a machine that builds from source)."""

@@ -48,6 +48,7 @@ def test_noalloc_matches_solve_on_two_calls(G, ctx, n):
         assert rc == 0, ctx.lib.grmp_last_error(ctx.h)
         assert st.status == 0
         assert st.spmv_config == ref_stats["spmv_config"]
+        assert st.grid_blocks == ref_stats["grid_blocks"]   # the tuned grid too: the same launch
         assert st.final_relres <= max(1e-10, 2.0 * ref_stats["final_relres"])
         x = sysd.x.entries
         err = np.linalg.norm(x - xref) / np.linalg.norm(xref)
@@ -65,3 +66,6 @@ def test_noalloc_rejects_oversize_and_mixed(G, ctx):
     small = _system(G, ctx, 8)
     rc, _ = _noalloc(ctx, small, G.GB300PCG(mode="mixed", reltol=1e-8))
     assert rc == L.ERR_UNSUPPORTED
+    rc, _ = _noalloc(ctx, small, G.GB300PCG(mode="fp64", reltol=-1.0))
+    assert rc == L.ERR_INVALID_ARG
+    assert b"invalid tolerance" in ctx.lib.grmp_last_error(ctx.h)
