@@ -91,6 +91,19 @@ struct grmp_matrix_s {
     int32_t *d_stg_row0 = nullptr;  // [nwin+1] first row of each window
     char *d_stg_rec = nullptr;      // [nwin] window records
     size_t stg_rec_bytes = 0;
+    // two-run 16-bit column copy of the FP32 values for mixed solves (duo
+    // records; state 0 = not built, 1 = built, -1 = a run spans more than
+    // 65535 columns)
+    int duo_state = 0;
+    int duo_span = 0;
+    int64_t duo_nduo = 0;
+    void *d_duo_meta = nullptr;     // [nrows+1] int4 {first duo, base1, base2, split | duos << 16}
+    uint32_t *d_duo_off = nullptr;  // [nduo] two 16-bit column offsets
+    int32_t *d_duo_src = nullptr;   // [nduo] CSR position of the first entry (-1 - pos: second is padding)
+    void *d_duo_val = nullptr;      // [nduo] float2 values
+    // the FP32 copies (packed pairs / staged windows, duo values) hold the
+    // values of the current solve
+    bool pack_fresh = false, duo_fresh = false;
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;
@@ -100,6 +113,7 @@ struct grmp_matrix_s {
     struct MfCache *mf = nullptr;
 };
 
+void grmp_duo_free(grmp_matrix A);   // duo copy of mixed solves (solve.cu)
 void grmp_direct_cache_free(grmp_matrix A);
 void grmp_mf_cache_free(grmp_matrix A);
 int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st);

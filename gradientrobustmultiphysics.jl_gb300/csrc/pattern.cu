@@ -562,6 +562,7 @@ extern "C" int grmp_matrix_destroy(grmp_matrix A) {
     grmp_free(ctx, A->d_pack32, (size_t)A->nnz * 8);
     grmp_free(ctx, A->d_stg_row0, ((size_t)A->stg_nwin + 1) * 4);
     grmp_free(ctx, A->d_stg_rec, A->stg_rec_bytes);
+    grmp_duo_free(A);
     grmp_free(ctx, A->d_fixed, (size_t)A->nrows);
     grmp_free(ctx, A->d_work, A->work_bytes);
     grmp_free(ctx, A->d_cellfac, A->cellfac_bytes);

@@ -25,6 +25,7 @@
 #include <cmath>
 #include <type_traits>
 
+#include "duo.h"
 #include "grmp_internal.h"
 
 namespace {
@@ -575,6 +576,160 @@ __global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) :
                    guess, spin);
 }
 
+// ------------------------------------------------------------ duo mixed PCG
+// FP32 SpMV fused with the search-direction update over the two-run 16-bit
+// column copy (duo records, the matrix's own numbering): groups of TPR lanes
+// per row as in spmv_rows, each lane with U duos (2U entries: one float2 and
+// one 32-bit offset word per duo) in flight, software pipelined over the
+// grid-strided rows (the next row's first chunk and the record of the row
+// after it are loaded before the current row's gathers).  Per row one int4
+// record {first duo, base1, base2, split | duos << 16}; entry e of the row has
+// column (e < split ? base1 : base2) + its offset.  Summation order per row:
+// chunk by chunk, duo u = 0..U-1, entry 0 then 1, then the lane reduction.
+struct DuoRow {
+    int kb, e, b1, b2, split;
+};
+
+__device__ __forceinline__ DuoRow duo_row(const int4 *__restrict__ meta, int r, int n) {
+    DuoRow d{0, 0, 0, 0, 0};
+    if (r < n) {
+        const int4 m = __ldg(meta + r);
+        d.kb = m.x;
+        d.e = m.x + (m.w >> 16);
+        d.b1 = m.y;
+        d.b2 = m.z;
+        d.split = m.w & 0xffff;
+    }
+    return d;
+}
+
+template <int U, int TPR>
+__device__ __forceinline__ void duo_chunk(const float2 *__restrict__ val, const uint32_t *__restrict__ off,
+                                          const DuoRow &d, int k, float2 *v, uint32_t *o) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int idx = k + u * TPR;
+        if (idx < d.e) {
+            v[u] = __ldg(val + idx);
+            o[u] = __ldg(off + idx);
+        } else {
+            v[u] = make_float2(0.f, 0.f);
+            o[u] = 0u;
+        }
+    }
+}
+
+// columns of duo idx (entries 2 (idx - kb) and 2 (idx - kb) + 1 of the row)
+__device__ __forceinline__ void duo_cols(const DuoRow &d, int idx, uint32_t o, int &c0, int &c1) {
+    const int e0 = 2 * (idx - d.kb);
+    c0 = (e0 < d.split ? d.b1 : d.b2) + (int)(o & 0xffffu);
+    c1 = (e0 + 1 < d.split ? d.b1 : d.b2) + (int)(o >> 16);
+}
+
+template <int TPR, int U>
+__device__ __forceinline__ float duo_fused_zp(int n, const int4 *__restrict__ meta, const uint32_t *__restrict__ off,
+                                              const float2 *__restrict__ val, const float2 *cur, float2 *nxt,
+                                              float *q, float beta) {
+    constexpr int RPW = 32 / TPR;
+    constexpr int CH = TPR * U;   // duos of a row per chunk
+    const int lane = threadIdx.x & (TPR - 1);
+    const int gin = (threadIdx.x & 31) / TPR;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int stride = ((gridDim.x * blockDim.x) >> 5) * RPW;
+    auto gp = [&](int c) {
+        const float2 g = cur[c];
+        return __fmaf_rn(beta, g.y, g.x);
+    };
+    float dacc = 0.f;
+    int r = warp * RPW + gin;
+    DuoRow d = duo_row(meta, r, n);
+    DuoRow dn = duo_row(meta, r + stride, n);
+    float2 v[U];
+    uint32_t o[U];
+    duo_chunk<U, TPR>(val, off, d, d.kb + lane, v, o);
+    for (int base = warp * RPW; base < n; base += stride) {
+        float2 vn[U];
+        uint32_t on[U];
+        duo_chunk<U, TPR>(val, off, dn, dn.kb + lane, vn, on);
+        const DuoRow d2 = duo_row(meta, r + 2 * stride, n);
+        float s = 0.f;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int c0, c1;
+            duo_cols(d, d.kb + lane + u * TPR, o[u], c0, c1);
+            s += v[u].x * gp(c0);
+            s += v[u].y * gp(c1);
+        }
+        for (int k = d.kb + lane + CH; k < d.e; k += CH) {   // rows longer than one chunk
+            float2 v2[U];
+            uint32_t o2[U];
+            duo_chunk<U, TPR>(val, off, d, k, v2, o2);
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                int c0, c1;
+                duo_cols(d, k + u * TPR, o2[u], c0, c1);
+                s += v2[u].x * gp(c0);
+                s += v2[u].y * gp(c1);
+            }
+        }
+#pragma unroll
+        for (int w = TPR / 2; w > 0; w >>= 1) s += __shfl_xor_sync(0xffffffffu, s, w);
+        if (r < n && lane == 0) {
+            const float2 me = cur[r];
+            const float pn = __fmaf_rn(beta, me.y, me.x);
+            nxt[r] = make_float2(me.x, pn);
+            q[r] = s;
+            dacc += pn * s;
+        }
+        r += stride;
+        d = dn;
+        dn = d2;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            v[u] = vn[u];
+            o[u] = on[u];
+        }
+    }
+    return dacc;
+}
+
+// SpMV policy over the duo copy; the FP64 residual from the CSR arrays.
+template <int TPR, int U>
+struct DuoSpmv {
+    int n;
+    const int32_t *rowptr, *cols;
+    const double *vals64;
+    const int4 *meta;
+    const uint32_t *off;
+    const float2 *val;
+    __device__ __forceinline__ float fused_zp(const float2 *cur, float2 *nxt, float *q, float beta) {
+        return duo_fused_zp<TPR, U>(n, meta, off, val, cur, nxt, q, beta);
+    }
+    __device__ __forceinline__ double resid64(const double *x, double *r64, const double *b) {
+        return spmv_grid<4, 4, true, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+    }
+};
+
+template <int TPR, int U>
+__global__ void __launch_bounds__(PTPB, U >= 4 ? 3 : 4) k_pcg_mixed_duo(
+    int n, const int32_t *rowptr, const int32_t *cols, const double *vals64, const int4 *meta, const uint32_t *off,
+    const float2 *val, const double *b, double *x, const float *dinv, float *r, float *q, float *xc, float2 *zp0,
+    float2 *zp1, double *r64, double *partial, SolveState *st, double abstol, double reltol, double delta, int maxit,
+    int maxouter, int guess, long long spin) {
+    DuoSpmv<TPR, U> sp{n, rowptr, cols, vals64, meta, off, val};
+    pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
+                   guess, spin);
+}
+
+// values of the duo copy from the CSR FP32 values (one thread per duo)
+__global__ void k_duo_fill(long long nduo, const int32_t *src, const float *vals32, float2 *val) {
+    const long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= nduo) return;
+    const int s = __ldg(src + d);
+    const int k = s >= 0 ? s : -1 - s;
+    val[d] = make_float2(__ldg(vals32 + k), s >= 0 ? __ldg(vals32 + k + 1) : 0.f);
+}
+
 // ------------------------------------------------------------ staged mixed PCG
 // The FP32 matrix re-laid out in fixed-size row windows (kStgRec bytes each):
 //   int row0, int nrows | uint16 local row offsets [nrows + 1] | pad to 16 B |
@@ -872,10 +1027,11 @@ void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, co
 // flight per lane), encoded 100*TPR + U; + 10000: software-pipelined row
 // loop; + 20000: staged windows, 512 threads x 3 stages per block; + 30000:
 // staged windows, 1024 threads x 6 stages (the staged ones: mixed solves only).
-constexpr int kConfigs[] = {208,   404,   408,   804,   1602,  10204, 10404, 10408,
-                            10804, 10402, 10802, 20204, 20408, 20804, 30408, 30804};
+constexpr int kConfigs[] = {208,   404,   408,   804,   1602,  10204, 10404, 10408, 10804, 10402,
+                            10802, 20204, 20408, 20804, 30408, 30804, 60404, 60208, 60802, 60408};
 
-inline bool staged_config(int cfg) { return cfg >= 20000; }
+inline bool staged_config(int cfg) { return cfg >= 20000 && cfg < 60000; }
+inline bool duo_config(int cfg) { return cfg >= 60000; }
 
 // Window layout of the staged SpMV, built once per matrix pattern from the
 // row pointers (greedy: whole rows while header + entries fit one record).
@@ -938,6 +1094,77 @@ void stage_fill(grmp_matrix A) {
     k_stage_fill<<<A->stg_nwin, 256, 0, ctx->stream>>>(A->d_stg_row0, A->d_rowptr, (const int2 *)A->d_pack32,
                                                        A->d_stg_rec);
     GRMP_LAUNCHED(ctx);
+}
+
+// The packed (column, FP32 value) pairs (and the staged windows copied from
+// them) for the values of the current solve.
+int ensure_pack32(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    if (A->pack_fresh) return GRMP_OK;
+    if (!A->d_pack32) {
+        int rc = grmp_alloc(ctx, &A->d_pack32, (size_t)A->nnz * 8);
+        if (rc) return rc;
+    }
+    k_pack32<<<(unsigned)((A->nnz + 255) / 256), 256, 0, ctx->stream>>>(A->nnz, A->d_cols, A->d_vals32,
+                                                                       (int2 *)A->d_pack32);
+    GRMP_LAUNCHED(ctx);
+    if (A->stg_state == 1) stage_fill(A);   // the staged windows hold a copy of the pairs
+    A->pack_fresh = true;
+    return GRMP_OK;
+}
+
+// The duo copy: layout once per pattern (host), values per solve (device).
+int duo_build_dev(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int n = A->nrows;
+    std::vector<int32_t> rp((size_t)n + 1), ci((size_t)A->nnz);
+    cudaError_t e = cudaMemcpyAsync(rp.data(), A->d_rowptr, rp.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ci.data(), A->d_cols, ci.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "duo layout: pattern download");
+    DuoLayout L;
+    if (duo_build(n, rp.data(), ci.data(), &L)) {
+        A->duo_state = -1;
+        A->duo_span = L.max_span;
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "duo layout: a column run spans %d columns (more than 65535)",
+                         L.max_span);
+    }
+    A->duo_nduo = L.nduo;
+    int rc = grmp_upload(ctx, (int32_t **)&A->d_duo_meta, L.meta.data(), L.meta.size());
+    if (!rc) rc = grmp_upload(ctx, &A->d_duo_off, L.off.data(), L.off.size());
+    if (!rc) rc = grmp_upload(ctx, &A->d_duo_src, L.src.data(), L.src.size());
+    if (!rc) rc = grmp_alloc(ctx, &A->d_duo_val, (size_t)L.nduo * 8);
+    if (!rc) {
+        e = cudaStreamSynchronize(ctx->stream);   // the host vectors are freed on return
+        if (e != cudaSuccess) rc = grmp_cuda_fail(ctx, e, "duo layout: upload");
+    }
+    if (rc) {
+        grmp_duo_free(A);
+        return rc;
+    }
+    A->duo_span = L.max_span;
+    A->duo_state = 1;
+    return GRMP_OK;
+}
+
+int ensure_duo(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    if (A->duo_state == 0) {
+        int rc = duo_build_dev(A);
+        if (rc) return rc;
+    }
+    if (A->duo_state < 0)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "duo layout: a column run spans %d columns (more than 65535)",
+                         A->duo_span);
+    if (!A->duo_fresh) {
+        k_duo_fill<<<(unsigned)((A->duo_nduo + 255) / 256), 256, 0, ctx->stream>>>(A->duo_nduo, A->d_duo_src,
+                                                                                   A->d_vals32,
+                                                                                   (float2 *)A->d_duo_val);
+        GRMP_LAUNCHED(ctx);
+        A->duo_fresh = true;
+    }
+    return GRMP_OK;
 }
 
 int heuristic_tpr(grmp_matrix A) {
@@ -1005,6 +1232,12 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         GRMP_LAUNCHED(ctx);
         cudaEventRecord(e1, ctx->stream);
     } else {
+        const int prc = ensure_pack32(A);
+        if (prc) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return prc;
+        }
         auto kern = k_pcg_mixed<TPR, U, PIPE>;
         grid = coop_grid(ctx, kern, n, p->grid_blocks);
         float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
@@ -1055,6 +1288,8 @@ int launch_pcg_staged(grmp_matrix A, const double *bvec, double *xvec, const grm
     const int cfg = (NT == 512 ? 20000 : 30000) + 100 * TPR + U;
     if (p->mode != GRMP_SOLVE_MIXED)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: staged configurations are for mixed solves", cfg);
+    const int prc = ensure_pack32(A);
+    if (prc) return prc;
     if (A->stg_state == 0) {
         int rc = stage_build(A);
         if (rc) return rc;
@@ -1119,9 +1354,74 @@ int launch_pcg_staged(grmp_matrix A, const double *bvec, double *xvec, const grm
     return hs.status;
 }
 
+// Mixed solve over the duo copy (configurations 60000 + 100 * lanes + duos in flight).
+template <int TPR, int U>
+int launch_pcg_duo(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p, grmp_solve_stats *out,
+                   char *work, SolveState *dst, WorkLayout lay) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int cfg = 60000 + 100 * TPR + U;
+    if (p->mode != GRMP_SOLVE_MIXED)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: duo configurations are for mixed solves", cfg);
+    int rc = ensure_duo(A);
+    if (rc) return rc;
+    const int n = A->nrows;
+    auto kern = k_pcg_mixed_duo<TPR, U>;
+    const int grid = coop_grid(ctx, kern, n, p->grid_blocks);
+    float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
+    float *xc = (float *)(work + 3 * lay.vec);
+    float2 *zp0 = (float2 *)(work + 4 * lay.vec), *zp1 = (float2 *)(work + 6 * lay.vec);
+    double *r64 = (double *)(work + lay.off_r64);
+    double *part = (double *)(work + lay.off_part);
+    int nn = n, mi = p->maxiter, mo = p->max_outer > 0 ? p->max_outer : 1000;
+    int guess = p->use_initial_guess ? 1 : 0;
+    double at = p->abstol, rt = p->reltol, dl = p->inner_reltol > 0 && p->inner_reltol < 1 ? p->inner_reltol : 0.1;
+    const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+    const int4 *mt = (const int4 *)A->d_duo_meta;
+    const uint32_t *of = A->d_duo_off;
+    const float2 *vl = (const float2 *)A->d_duo_val;
+    const double *v64 = A->d_vals64, *bb = bvec;
+    double *xx = xvec;
+    long long spin = ctx->wait_limit;
+    void *args[] = {&nn, &rp, &ci, &v64, &mt, &of, &vl, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
+                    &at, &rt, &dl, &mi, &mo, &guess, &spin};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
+    cudaEventRecord(e0, ctx->stream);
+    cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+    GRMP_LAUNCHED(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    SolveState hs;
+    std::memset(&hs, 0, sizeof(hs));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "duo PCG launch");
+    out->status = hs.status;
+    out->iterations = hs.iters;
+    out->outer_iterations = hs.outer;
+    out->final_relres = hs.relres;
+    out->spmv_config = cfg;
+    out->grid_blocks = grid;
+    out->solve_ms = ms;
+    if (hs.status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, GRMP_ERR_NOT_CONVERGED, "PCG: %d iterations, relative residual %.3e", hs.iters, hs.relres);
+    if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a grid barrier wait timed out");
+    if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
+    return hs.status;
+}
+
 int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_solve_params *p, grmp_solve_stats *st,
                  char *work, SolveState *dst, WorkLayout lay) {
     switch (cfg) {
+        case 60404: return launch_pcg_duo<4, 4>(A, b, x, p, st, work, dst, lay);
+        case 60208: return launch_pcg_duo<2, 8>(A, b, x, p, st, work, dst, lay);
+        case 60802: return launch_pcg_duo<8, 2>(A, b, x, p, st, work, dst, lay);
+        case 60408: return launch_pcg_duo<4, 8>(A, b, x, p, st, work, dst, lay);
         case 20204: return launch_pcg_staged<2, 4, 512, 3>(A, b, x, p, st, work, dst, lay);
         case 20408: return launch_pcg_staged<4, 8, 512, 3>(A, b, x, p, st, work, dst, lay);
         case 20804: return launch_pcg_staged<8, 4, 512, 3>(A, b, x, p, st, work, dst, lay);
@@ -1175,6 +1475,7 @@ int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_para
     double bt = 1e30;
     for (int cfg : kConfigs) {
         if (staged_config(cfg) && (p->mode != GRMP_SOLVE_MIXED || A->stg_state < 0)) continue;
+        if (duo_config(cfg) && (p->mode != GRMP_SOLVE_MIXED || A->duo_state < 0)) continue;
         const double per = trial(cfg);
         if (per < bt) {
             bt = per;
@@ -1241,17 +1542,11 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     grmp_free(ctx, bad, 4);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
-    if (mixed) {   // refresh the packed FP32 copy (values may have been reassembled)
-        const size_t pb = (size_t)A->nnz * 8;
-        if (!A->d_pack32) {
-            int prc = grmp_alloc(ctx, &A->d_pack32, pb);
-            if (prc) return prc;
-        }
-        k_pack32<<<(unsigned)((A->nnz + 255) / 256), 256, 0, ctx->stream>>>(A->nnz, A->d_cols, A->d_vals32,
-                                                                           (int2 *)A->d_pack32);
-        GRMP_LAUNCHED(ctx);
-        if (A->stg_state == 1) stage_fill(A);   // the staged windows hold a copy of the pairs
-    }
+    // the FP32 copies (packed pairs and staged windows, duo values) are
+    // refreshed by the first launch that reads them: the values may have been
+    // reassembled since the last solve
+    A->pack_fresh = false;
+    A->duo_fresh = false;
     int cfg = p->spmv_config;
     grmp_solve_params q = *p;
     if (cfg == 0) {   // autotuned once per matrix and solver mode (configuration and grid)
@@ -1494,4 +1789,19 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
     if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a grid barrier wait timed out");
     if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
     return hs.status;
+}
+
+// Frees the duo copy of a matrix (any part of it may be absent).
+void grmp_duo_free(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const size_t nd = (size_t)A->duo_nduo;
+    grmp_free(ctx, A->d_duo_meta, ((size_t)A->nrows + 1) * 16);
+    grmp_free(ctx, A->d_duo_off, nd * 4);
+    grmp_free(ctx, A->d_duo_src, nd * 4);
+    grmp_free(ctx, A->d_duo_val, nd * 8);
+    A->d_duo_meta = A->d_duo_val = nullptr;
+    A->d_duo_off = nullptr;
+    A->d_duo_src = nullptr;
+    A->duo_state = 0;
+    A->duo_fresh = false;
 }

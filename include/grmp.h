@@ -325,7 +325,11 @@ typedef struct {
                                1602, 10204, 10404, 10408, 10804, 10402, 10802; MIXED only,
                                rows streamed through shared memory in 32 KB windows by bulk
                                async copies: 20204, 20408, 20804 (512 threads, 3 stages per
-                               block), 30408, 30804 (1024 threads, 6 stages); 0 = autotuned
+                               block), 30408, 30804 (1024 threads, 6 stages); MIXED only,
+                               the FP32 values with two-run 16-bit columns (two entries per
+                               8-byte value load and 4-byte column load; rows whose columns
+                               fall in two windows of 65536): 60404, 60208, 60802, 60408
+                               (100*lanes + entry pairs in flight); 0 = autotuned
                                per matrix and mode (timed trial solves); -1 = chosen from the
                                mean row length
                                (no timing, so the choice does not depend on concurrent GPU work) */
