@@ -11,7 +11,7 @@ from .fespace import (FESpace, FEType, H1P1, H1P2, H1BR, L2P0, HDIVRT0, HDIVBDM1
 from . import _lib  # noqa: F401
 from .api import (GB300Context, Operator, CellCoefficient, LaplaceOperator, ReactionOperator,  # noqa: F401
                   HookStiffnessOperator2D, HookStiffnessOperator3D, BilinearForm, LinearForm, DataFunction,
-                  FEMatrix, FEVector, assemble, apply_dirichlet, GB300PCG, spmv,
+                  FEMatrix, FEVector, ImportedMatrix, assemble, apply_dirichlet, GB300PCG, spmv,
                   Identity, Gradient, SymmetricGradient, Divergence, ReconstructionIdentity,
                   ReconstructionDivergence, APT_BilinearForm, APT_SymmetricBilinearForm,
                   ItemIntegrator, L2ErrorIntegrator, L2NormIntegrator, L2DifferenceIntegrator)

@@ -121,6 +121,10 @@ SIGNATURES = {
     "grmp_pattern_build": ([_vp, ctypes.c_int, ctypes.POINTER(BilinearTerm), ctypes.POINTER(_vp)], ctypes.c_int),
     "grmp_matrix_destroy": ([_vp], ctypes.c_int),
     "grmp_matrix_info": ([_vp, _pi32, ctypes.POINTER(ctypes.c_int64), _pi32], ctypes.c_int),
+    "grmp_matrix_from_csc": ([_vp, _i32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), _pd,
+                              ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_vp)], ctypes.c_int),
+    "grmp_matrix_update_values": ([_vp, _pd], ctypes.c_int),
+    "grmp_matrix_penalty_rows": ([_vp, _pi32], ctypes.c_int),
     "grmp_assemble_bilinear": ([_vp, ctypes.c_int, ctypes.POINTER(BilinearTerm), ctypes.c_int], ctypes.c_int),
     "grmp_matrix_download": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64), _pi32, _pd], ctypes.c_int),
     "grmp_assemble_linear": ([_vp, ctypes.POINTER(Rhs), _vp], ctypes.c_int),

@@ -431,6 +431,57 @@ class FEMatrix:
             pass
 
 
+class ImportedMatrix:
+    """A matrix handed over as compressed sparse columns -- what LinearSolve
+    receives from solve_direct! (SparseMatrixCSC{Float64,Int64},
+    src/solvers.jl:89-101) -- imported with grmp_matrix_from_csc.  `A` is a
+    scipy sparse matrix (converted to CSC) or a (colptr, rowval, nzval) triple
+    with the given index base.  Rows with a diagonal >= penalty_threshold are
+    the reference's penalised Dirichlet rows (eliminated for the solvers,
+    grmp_solve maps b accordingly).  Solved with GB300PCG like an FEMatrix."""
+
+    def __init__(self, ctx: GB300Context, A, symmetric: bool = True, penalty_threshold: float = 1e30,
+                 index_base: int = 0):
+        self.ctx = ctx
+        if isinstance(A, tuple):
+            colptr, rowval, nzval = A
+        else:
+            C = A.tocsc()
+            C.sort_indices()
+            colptr, rowval, nzval = C.indptr + index_base, C.indices + index_base, C.data
+        self.colptr = np.ascontiguousarray(colptr, dtype=np.int64)
+        rowval = np.ascontiguousarray(rowval, dtype=np.int64)
+        nzval = np.ascontiguousarray(nzval, dtype=np.float64)
+        self.n = self.colptr.size - 1
+        self.h = ctypes.c_void_p()
+        ctx.check(ctx.lib.grmp_matrix_from_csc(
+            ctx.h, self.n, self.colptr.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            rowval.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _dp(nzval), index_base, int(symmetric),
+            float(penalty_threshold), ctypes.byref(self.h)))
+
+    def update_values(self, nzval):
+        """cache.A = A with the same pattern (values in the import's CSC order)."""
+        v = np.ascontiguousarray(nzval, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grmp_matrix_update_values(self.h, _dp(v)))
+
+    def penalty_rows(self) -> int:
+        c = ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.grmp_matrix_penalty_rows(self.h, ctypes.byref(c)))
+        return c.value
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.grmp_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            if self.ctx.h:
+                self.free()
+        except Exception:
+            pass
+
+
 def assemble(target, operators, precision: int = L.FP64):
     """assemble!(A, operators) / assemble!(b, LinearForm): device assembly.
 

@@ -315,6 +315,9 @@ int grmp_pattern_build(grmp_space space, int nterms, const grmp_bilinear_term *t
 
 int grmp_assemble_bilinear(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision) {
     if (!A || nterms <= 0 || nterms > GRMP_MAX_TERMS || !terms) return GRMP_ERR_INVALID_ARG;
+    if (A->imported)
+        return grmp_fail(A->space->mesh->ctx, GRMP_ERR_INVALID_ARG,
+                         "assemble: the matrix was imported from a CSC (no assembly space); use grmp_matrix_update_values");
     if (precision != GRMP_FP64 && precision != GRMP_FP32 && precision != GRMP_FP64_FP32) return GRMP_ERR_INVALID_ARG;
     cudaSetDevice(A->space->mesh->ctx->device);
     std::lock_guard<std::mutex> lk(A->space->mesh->ctx->mu);
@@ -377,8 +380,13 @@ int grmp_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     grmp_solve_stats local;
     if (!st) st = &local;
     std::memset(st, 0, sizeof(*st));
-    if (p->mode == GRMP_SOLVE_DIRECT || p->mode == GRMP_SOLVE_MIXED_DIRECT) return grmp_mf_solve(A, b, x, p, st);
-    return grmp_solve_impl(A, b, x, p, st);
+    // an imported matrix with penalty rows solves its eliminated system
+    grmp_vector_s bt;
+    grmp_vector bb = b;
+    int rc = grmp_import_rhs(A, b, &bt, &bb);
+    if (rc) return rc;
+    if (p->mode == GRMP_SOLVE_DIRECT || p->mode == GRMP_SOLVE_MIXED_DIRECT) return grmp_mf_solve(A, bb, x, p, st);
+    return grmp_solve_impl(A, bb, x, p, st);
 }
 
 int grmp_spmv(grmp_matrix A, int precision, grmp_vector x, grmp_vector y) {

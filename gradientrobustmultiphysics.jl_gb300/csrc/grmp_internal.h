@@ -104,6 +104,18 @@ struct grmp_matrix_s {
     // the FP32 copies (packed pairs / staged windows, duo values) hold the
     // values of the current solve
     bool pack_fresh = false, duo_fresh = false;
+    // imported from a host CSC (grmp_matrix_from_csc): no assembly space; the
+    // caller's values in CSR order, penalty rows (diagonal >= threshold)
+    // eliminated from the FP64 / FP32 values the solvers use
+    bool imported = false;
+    double imp_threshold = 0.0;
+    int imp_npen = 0;                  // penalty rows of the current values
+    double *d_imp_orig = nullptr;      // [nnz] the caller's values, CSR order
+    int64_t *d_imp_src = nullptr;      // [nnz] CSC position of each CSR entry (transposed imports)
+    uint8_t *d_imp_flag = nullptr;     // [nrows] 1 = penalty row
+    double *d_imp_diag = nullptr;      // [nrows] the caller's diagonal
+    double *d_imp_b = nullptr;         // [nrows] right-hand side of the eliminated system
+    int *d_imp_count = nullptr;
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;
@@ -114,6 +126,10 @@ struct grmp_matrix_s {
 };
 
 void grmp_duo_free(grmp_matrix A);   // duo copy of mixed solves (solve.cu)
+void grmp_import_free(grmp_matrix A);   // arrays of a CSC import (import.cu)
+// right-hand side of the eliminated system of an imported matrix with penalty
+// rows (into A's scratch, described by *tmp); *out = b otherwise
+int grmp_import_rhs(grmp_matrix A, grmp_vector b, struct grmp_vector_s *tmp, grmp_vector *out);
 void grmp_direct_cache_free(grmp_matrix A);
 void grmp_mf_cache_free(grmp_matrix A);
 int grmp_mf_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st);

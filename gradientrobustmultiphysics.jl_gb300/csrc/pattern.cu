@@ -568,7 +568,12 @@ extern "C" int grmp_matrix_destroy(grmp_matrix A) {
     grmp_free(ctx, A->d_cellfac, A->cellfac_bytes);
     grmp_direct_cache_free(A);
     grmp_mf_cache_free(A);
+    grmp_import_free(A);
     cudaStreamSynchronize(ctx->stream);
+    if (A->imported) {   // the placeholder mesh / space of a CSC import belong to the matrix
+        delete A->space->mesh;
+        delete A->space;
+    }
     delete A;
     return GRMP_OK;
 }

@@ -217,6 +217,36 @@ int grmp_matrix_info(grmp_matrix A, int32_t *nrows, int64_t *nnz, int32_t *max_r
  * nonzero is the sum of its cell contributions in ascending cell order. */
 int grmp_assemble_bilinear(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
 
+/* A matrix from the caller's compressed sparse column arrays: the matrix
+ * LinearSolve receives from solve_direct!, a SparseMatrixCSC{Float64,Int64}
+ * (init(LinearProblem(A, b), alg), src/solvers.jl:89-101, :658-661;
+ * FEMatrix entries, src/fematrix.jl:148-150).  colptr [n+1], rowval and
+ * nzval [colptr[n] - index_base]; index_base 1 for Julia's arrays (0 for
+ * C); row indices strictly increasing within a column.  symmetric = 1: the
+ * matrix is symmetric and its CSC arrays are used as the CSR arrays (no
+ * transpose); 0: the host transposes them once.  Rows whose diagonal is >=
+ * penalty_threshold (> 0; e.g. 1e30 for the reference's 1e60 Dirichlet
+ * penalty, src/solvers.jl:640-652) are penalty rows: the solvers work on the
+ * matrix with those rows and columns eliminated (FP64, and rounded to FP32
+ * for the mixed and FP32-factor solvers -- 1e60 overflows FP32), and
+ * grmp_solve maps the caller's b accordingly (x_d = b_d / a_dd, b_i -= a_id
+ * x_d), which reproduces the penalised system's solution up to O(1 / a_dd)
+ * relative.  0 = no penalty rows.  The handle has no assembly space
+ * (grmp_assemble_bilinear refuses it); its values are replaced with
+ * grmp_matrix_update_values.  Iterative solves need a symmetric positive
+ * definite matrix (after elimination). */
+int grmp_matrix_from_csc(grmp_context ctx, int32_t n, const int64_t *colptr, const int64_t *rowval,
+                         const double *nzval, int index_base, int symmetric, double penalty_threshold,
+                         grmp_matrix *out);
+/* New values for an imported matrix with the same pattern: nzval [nnz] in
+ * the CSC order of the import (cache.A = A in the fixpoint loops,
+ * src/solvers.jl:906-911, :1160-1165).  Penalty rows are detected again;
+ * symbolic analyses and tuned SpMV configurations are kept. */
+int grmp_matrix_update_values(grmp_matrix A, const double *nzval);
+/* Number of penalty rows of an imported matrix's current values (0 for an
+ * assembled matrix). */
+int grmp_matrix_penalty_rows(grmp_matrix A, int32_t *count);
+
 /* Copy the CSR arrays (rowptr [nrows+1] int64, cols [nnz], vals [nnz] FP64)
  * to host memory; any pointer may be NULL.  `precision` selects which values. */
 int grmp_matrix_download(grmp_matrix A, int precision, int64_t *rowptr, int32_t *cols, double *vals);
