@@ -53,14 +53,19 @@ def dist_env():
 
 
 class Dist:
-    def __init__(self):
-        self.ws, self.rank, self.local = dist_env()
+    def __init__(self, single: bool = False):
+        self.ws, self.rank, self.local = (1, 0, dist_env()[2]) if single else dist_env()
         self.pg = None
         if self.ws > 1:
             import torch.distributed as td
             os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
             td.init_process_group("gloo")
             self.td = td
+
+    @classmethod
+    def single(cls):
+        """This process alone (the bounded summaries the headline run adds)."""
+        return cls(single=True)
 
     def barrier(self):
         if self.ws > 1:
@@ -261,15 +266,22 @@ def run_reference(args):
 # k_pcg_mixed launch on the 48^3 case divided by pcg_bytes() of the same
 # launch: 180.78 GB / 185.73 GB (summary under profiles/).
 TRAFFIC_PER_ALGORITHMIC_BYTE = (163.612 + 17.166) / 185.732
+# the same for k_pcg_mixed_duo (two-run 16-bit columns); None until captured
+TRAFFIC_PER_ALGORITHMIC_BYTE_DUO = None
 
 
-def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool) -> float:
+def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool, nduo: int = 0) -> float:
     """Algorithmic DRAM bytes of one persistent PCG launch: per inner
-    iteration the matrix once (values + column indices) and the vector
-    traffic of the update phase; per FP64 refinement one FP64 residual."""
+    iteration the matrix once (values + column indices: 8 bytes per entry as
+    packed pairs; 12 bytes per pair of entries plus a 16-byte row record in
+    the two-run 16-bit column form, spmv_config 60xxx) and the vector traffic
+    of the update phase; per FP64 refinement one FP64 residual."""
     it, outer = stats["iterations"], stats["outer_iterations"]
     if mixed:
-        per_it = 8.0 * nnz + 56.0 * n
+        if stats.get("spmv_config", 0) >= 60000:
+            per_it = 12.0 * nduo + 16.0 * n + 56.0 * n
+        else:
+            per_it = 8.0 * nnz + 56.0 * n
         per_outer = 12.0 * nnz + 64.0 * n
         return it * per_it + (outer + 1) * per_outer
     return it * (12.0 * nnz + 108.0 * n) + 2 * (12.0 * nnz + 36.0 * n)
@@ -353,6 +365,8 @@ def run_ours(args):
     b = G.FEVector(ctx, FES)
     x = G.FEVector(ctx, FES)
     nnz = A.nnz
+    rp_host, _ = A.pattern()
+    nduo = int(np.sum((np.diff(rp_host) + 1) // 2))   # entry pairs of the two-run 16-bit column form
 
     direct = args.solver == "direct"
 
@@ -400,7 +414,7 @@ def run_ours(args):
             # iteration counts let a capture's DRAM bytes be set against the algorithmic bytes
             print(json.dumps({"profile_step": k, "ndofs": ndofs, "nnz": nnz, "iterations": st["iterations"],
                               "outer": st["outer_iterations"], "spmv_config": st["spmv_config"],
-                              "algorithmic_bytes": pcg_bytes(st, ndofs, nnz, True)}), flush=True)
+                              "algorithmic_bytes": pcg_bytes(st, ndofs, nnz, True, nduo)}), flush=True)
         torch.cuda.synchronize()
         ctx.close()
         dist.close()
@@ -452,16 +466,19 @@ def run_ours(args):
     plain_value = world_dofs / plain["total_s"]
     # roofline of the dominant kernel (persistent mixed PCG)
     st_last = mixed["stats"][-1]
-    kb = pcg_bytes(st_last, ndofs, nnz, True)
+    kb = pcg_bytes(st_last, ndofs, nnz, True, nduo)
+    duo = st_last["spmv_config"] >= 60000
     kms = statistics.mean([s["solve_ms"] for s in mixed["stats"]])
     achieved = kb / (kms / 1e3) / 1e9
     pk = peaks()
     peak = float(pk["hbm_gbs"]) if pk else 6800.0
+    tpab = TRAFFIC_PER_ALGORITHMIC_BYTE_DUO if duo else TRAFFIC_PER_ALGORITHMIC_BYTE
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": kb * TRAFFIC_PER_ALGORITHMIC_BYTE,
-                "traffic_source": "ncu dram__bytes_read+write of k_pcg_mixed on the 48^3 case "
-                                  "(0.973 x its algorithmic bytes), scaled to this launch",
-                "kernel": "k_pcg_mixed (persistent)",
+                "frac": achieved / peak, "traffic": kb * tpab if tpab else None,
+                "traffic_source": (f"ncu dram__bytes_read+write of {'k_pcg_mixed_duo' if duo else 'k_pcg_mixed'} "
+                                   f"on the 48^3 case ({tpab:.3f} x its algorithmic bytes), scaled to this launch"
+                                   if tpab else "not captured for this configuration"),
+                "kernel": "k_pcg_mixed_duo (persistent)" if duo else "k_pcg_mixed (persistent)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"}
     if direct:
         roofline = None   # factorisation-bound (FP32 / FP64 pipes), no HBM roofline line for this solver
@@ -517,19 +534,124 @@ def run_ours(args):
             "gpu_launches": mixed["launches"],
             "clocks": mixed["clocks"],
             "setup_ms": setup_ms}
+    ctx.close()
+    if dist.rank == 0 and not args.no_extras and args.workload == "poisson3d":
+        # the other configurations, bounded, on the same run's record
+        line["configs"] = run_extras(args)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     dist.close()
     return 0
 
 
-def run_stokes(args):
+def _timed(stream, fn, steps: int, warmup: int):
+    """warmup + steps calls of fn, each step bracketed by CUDA events on the
+    library's stream; returns (ms per step, last result)."""
+    import torch
+    r = None
+    for _ in range(warmup):
+        r = fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms, r
+
+
+def summary_linear(G, P, prob, modes, reltol: float, steps: int, warmup: int, reference: str, cpu: bool):
+    """One LinearProblem in a plain and a mixed solver mode (assembly + rhs +
+    Dirichlet + solve per step); errors against the oracle's sparse-direct
+    FP64 solve of the penalised system (reference "oracle"), or against the
+    library's FP64 multifrontal solve refined to 1e-14 ("gpu_direct", for
+    near-incompressible elasticity, whose Jacobi-CG the oracle cannot
+    converge and whose sparse-direct solve does not fit the time bound)."""
+    import torch
+    ctx = G.GB300Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=0)
+    sysd = P.DeviceSystem(ctx, prob, mixed=True)
+    ndofs = prob.FES.ndofs
+    out = {"ndofs": ndofs, "steps": steps, "warmup": warmup, "reltol": reltol}
+    sols = {}
+    for mode in modes:
+        sysd.mixed = mode == "mixed"   # FP32 element matrices only for the FP32 PCG
+        solver = G.GB300PCG(mode=mode, reltol=reltol, abstol=0.0)
+        ms, st = _timed(stream, lambda: sysd.assemble_and_solve(solver), steps, warmup)
+        sols[mode] = sysd.x.entries
+        out[mode] = {"value": ndofs / (statistics.mean(ms) / 1e3), "ms_per_step": statistics.mean(ms),
+                     "iterations": st["iterations"], "spmv_config": st["spmv_config"]}
+    plain, mixed = modes
+    out["mixed_vs_plain"] = out[mixed]["value"] / out[plain]["value"]
+    uref, desc = None, None
+    if reference == "gpu_direct":
+        sysd.mixed = False
+        sysd.assemble_and_solve(G.GB300PCG(mode="direct", reltol=1e-14, abstol=0.0))
+        uref, desc = sysd.x.entries, "GPU FP64 multifrontal direct solve refined to 1e-14"
+    ctx.close()
+    if cpu or reference == "oracle":
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        d, dt, ta, ts, it, A, bb, _ = cpu_port_step(prob, reltol)
+        if cpu:
+            out["cpu_baseline"] = {"value": d / dt, "unit": "DoF/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                   "sample": f"full problem: oracle assembly {ta:.2f}s + FP64 Jacobi-CG {ts:.2f}s"}
+        if reference == "oracle":
+            uref, desc = O.solve_direct(A, bb), "oracle sparse-direct (SuperLU) FP64 solve of the penalised system"
+    out["rel_err_vs_fp64"] = {m: float(np.linalg.norm(sols[m] - uref) / np.linalg.norm(uref)) for m in modes}
+    out["rel_err_vs_fp64"]["reference"] = desc
+    return out
+
+
+def run_extras(args) -> dict:
+    """Bounded summaries of the other configurations, attached to the
+    headline line so that one default run records them: 2D P2 Poisson 128^2
+    (FP64 vs mixed PCG), 2D P2 elasticity 256^2 with lambda = 1e3 (FP64 vs
+    FP32-factor multifrontal), the 2048-problem batched Stokes solve, and the
+    serving loop (Poisson arrivals, then the same requests at saturation in
+    mixed and plain FP64 mode).  Each entry records its own wall time."""
+    import copy
+    G = _package()
+    from grmp_gb300 import problems as P
+    out = {}
+    t0 = time.perf_counter()
+    out["poisson2d_P2_128x128"] = summary_linear(G, P, P.poisson2d(128), ("fp64", "mixed"), 1e-11, 5, 3, "oracle",
+                                                 True)
+    out["poisson2d_P2_128x128"]["wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    out["elasticity2d_P2vec_256x256_lambda1e3"] = summary_linear(
+        G, P, P.elasticity2d(256, seed=args.seed), ("direct", "mixed_direct"), 1e-12, 3, 3, "gpu_direct", False)
+    out["elasticity2d_P2vec_256x256_lambda1e3"]["wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a = copy.copy(args)
+    a.workload, a.steps, a.warmup, a.dim, a.nprob = "stokes-batch", 3, 3, 2, 2048
+    st = run_stokes(a, emit=False)
+    out["stokes_BR_P0_batch2048"] = {k: st[k] for k in ("value", "unit", "ms_per_step", "config", "solver",
+                                                        "rel_err_vs_oracle", "cpu_baseline", "latency_ms")}
+    out["stokes_BR_P0_batch2048"]["wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a = copy.copy(args)
+    a.workload = "serve"
+    sv = run_serve(a, emit=False)
+    out["serve_64_requests"] = {k: sv[k] for k in ("value", "unit", "config", "latency_ms", "failed", "run_ms_p50",
+                                                   "queue_ms_p50", "saturated", "mixed_vs_plain",
+                                                   "max_rel_diff_mixed_vs_fp64")}
+    out["serve_64_requests"]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
+def run_stokes(args, emit: bool = True):
     """Batched gradient-robust Stokes: 2048 BR/P0 problems (8x8 .. 96x96
     squares, nu log-uniform in [1e-4, 1], penalty 1e4), iterated penalty with
     one FP64 multifrontal factorisation per problem; a step = FP64 assembly
-    of all problems + reconstructed rhs + Dirichlet + the batched solve."""
-    dist = Dist()
+    of all problems + reconstructed rhs + Dirichlet + the batched solve.
+    The error is measured against the oracle's sparse-direct sweeps on the
+    problems the CPU baseline samples."""
+    dist = Dist() if emit else Dist.single()
     G = _package()
     from grmp_gb300 import build as B
     from grmp_gb300 import stokes as S
@@ -579,11 +701,22 @@ def run_stokes(args):
         sample = np.argsort(prob.sizes)[::max(1, len(prob.sizes) // 8)][:8]
         t0 = time.perf_counter()
         dd = 0
+        uo_s = {}
         for k in sample:
             g = prob.mesh.parts[k]
-            O.stokes_iterated_penalty(g, prob.nus[k], prob.lam, prob.terms[k], sweeps=args.sweeps)
+            uo_s[k] = O.stokes_iterated_penalty(g, prob.nus[k], prob.lam, prob.terms[k], sweeps=args.sweeps)
             dd += (prob.V.row_offsets[k + 1] - prob.V.row_offsets[k]) + g.ncells
         dt = time.perf_counter() - t0
+        u_g, p_g = sysd.velocity(), sysd.pressure()
+        eu, ep = [], []
+        for k, (uo, po, _) in uo_s.items():
+            r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
+            c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
+            eu.append(float(np.linalg.norm(u_g[r0:r1] - uo) / np.linalg.norm(uo)))
+            ep.append(float(np.linalg.norm(p_g[c0:c1] - po) / np.linalg.norm(po)))
+        err = {"velocity_max": max(eu), "pressure_max": max(ep), "problems": len(eu),
+               "nu_range": [float(min(prob.nus[k] for k in uo_s)), float(max(prob.nus[k] for k in uo_s))],
+               "reference": f"oracle sparse-direct (SuperLU) iterated-penalty sweeps ({args.sweeps})"}
         cpu = {"value": dd / dt, "unit": "DoF/s", "cores": 1, "kind": "port",
                "sample": f"{len(sample)} problems of the batch (every {max(1, len(prob.sizes) // 8)}th by size), "
                          f"{dd} DoFs: oracle assembly + SuperLU sparse-direct sweeps ({args.sweeps})"}
@@ -598,22 +731,25 @@ def run_stokes(args):
                        "solver": "FP64 multifrontal Cholesky per problem, factored once per step"},
             "latency_ms": {"p50": p[len(p) // 2], "p99": p[min(len(p) - 1, int(0.99 * len(p)))]},
             "solver": {k: st[k] for k in ("max_iterations", "max_sweeps", "failed", "max_relres", "solve_ms")},
+            "rel_err_vs_oracle": err if dist.rank == 0 and not args.no_cpu else None,
             "cpu_baseline": cpu, "clocks": clocks}
+    ctx.close()
+    if not emit:
+        return line
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     dist.close()
     return 0
 
 
-def run_serve(args):
+def run_serve(args, emit: bool = True):
     """Serving loop: Poisson-process arrivals of 2D/3D Poisson and
     reaction-diffusion requests (H1P1/H1P2, 1e3..2e6 DoFs), 4 slots, HBM
     budget 150 GB, mixed-precision solves; DoF/s and p50/p99 latency.  The
     same requests are then submitted all at once in mixed and in plain FP64
     mode (serving capacity of each, and the largest relative difference
     between the two solutions of a request)."""
-    dist = Dist()
+    dist = Dist() if emit else Dist.single()
     G = _package()
     from grmp_gb300 import build as B
     from grmp_gb300 import serve as SV
@@ -647,6 +783,8 @@ def run_serve(args):
             "queue_ms_p50": float(np.percentile([s["queue_ms"] for s in sts], 50)),
             "saturated": sat, "mixed_vs_plain": sat["mixed"]["dof_per_s"] / sat["fp64"]["dof_per_s"],
             "max_rel_diff_mixed_vs_fp64": max(rel), "clocks": clocks}
+    if not emit:
+        return line
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
@@ -668,6 +806,8 @@ def main():
                     help="SpMV configuration of the mixed solver (0: autotuned per matrix)")
     ap.add_argument("--cpu-n", type=int, default=0, help="CPU sample mesh size (0: the workload's own)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline only: skip the bounded summaries of the other configurations")
     ap.add_argument("--profile", action="store_true", help="mixed path only, no timing output (for ncu)")
     ap.add_argument("--workload", default="poisson3d",
                     choices=["poisson3d", "poisson2d", "elasticity2d", "stokes-batch", "serve"],

@@ -10,6 +10,8 @@ with sparse-direct solves, and bit-identical results alone and in a batch.
 import numpy as np
 import pytest
 
+from parity_helpers import stokes_tolerance
+
 
 def _poly_terms(rng):
     from grmp_gb300 import stokes as S
@@ -115,10 +117,12 @@ def test_br_assembly_parity(G, O, ctx, recon):
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["fp64", "mixed", "direct"])
 def test_batch_matches_oracle(G, O, ctx, mode):
-    """Iterated-penalty result against the oracle's sparse-direct sweeps.  The
+    """Iterated-penalty result against the oracle's sparse-direct sweeps, per
+    problem within max(1e-10, 10 cond eps) (stokes_tolerance: the condition
+    number of each problem's velocity system is computed and stated).  The
     FP32 inner solve (mixed) only resolves moderate lambda/nu: with lambda =
-    1e4 and nu = 0.05 its PCG needs ~1e5 iterations and stops short of 1e-8,
-    so the mixed case uses nu >= 0.2."""
+    1e4 and nu = 0.05 its PCG needs ~1e5 iterations, so the mixed case uses
+    nu >= 0.2."""
     from grmp_gb300 import stokes as S
     sizes, nus = [5, 9, 6], ([1.0, 0.2, 0.5] if mode == "mixed" else [1.0, 0.2, 0.05])
     prob = _small_batch(G, sizes, nus)
@@ -132,7 +136,8 @@ def test_batch_matches_oracle(G, O, ctx, mode):
         c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
         eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
         ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
-        assert eu < 1e-8 and ep < 1e-8, (k, eu, ep, st)
+        tol, cond = stokes_tolerance(O, g, nus[k], prob.lam, 1)
+        assert eu <= tol and ep <= tol, (k, eu, ep, tol, cond, st)
 
 
 @pytest.mark.gpu
@@ -151,7 +156,8 @@ def test_batch_bdm1_matches_oracle(G, O, ctx):
         c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
         eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
         ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
-        assert eu < 1e-8 and ep < 1e-8, (k, eu, ep, st)
+        tol, cond = stokes_tolerance(O, g, nus[k], prob.lam, 2)
+        assert eu <= tol and ep <= tol, (k, eu, ep, tol, cond, st)
 
 
 @pytest.mark.gpu

@@ -14,6 +14,8 @@ sparse-direct solve of the oracle's system.
 import numpy as np
 import pytest
 
+from parity_helpers import stokes_tolerance
+
 # phi = x^2 + 2 y^2 - z^2 + x y;  grad phi = (2x + y, x + 4y, -2z)
 GRAD_PHI = np.array([(0, 2.0, 1, 0, 0), (0, 1.0, 0, 1, 0), (1, 1.0, 1, 0, 0), (1, 4.0, 0, 1, 0),
                      (2, -2.0, 0, 0, 1)], dtype=np.float64)
@@ -275,8 +277,9 @@ def test_batch3d_matches_oracle(G, O, ctx, mode):
     """3D batched iterated penalty (H1BR{3} / P0, RT0-reconstructed load of
     order 3 + 2) against the oracle's sparse-direct sweeps per problem.  The
     FP32 inner solve (mixed) resolves moderate lambda/nu only; in 3D it
-    needs ~2e5 iterations per problem at lambda/nu = 2e4 and stops short of
-    1e-8 there, so the mixed case runs lambda = 1e3."""
+    needs ~2e5 iterations per problem at lambda/nu = 2e4, so the mixed case
+    runs lambda = 1e3.  Tolerance per problem: max(1e-10, 10 cond eps) with
+    the velocity system's condition number (stokes_tolerance)."""
     from grmp_gb300 import stokes as S
     sizes = [2, 3, 2]
     nus = [1.0, 0.5, 0.3] if mode == "mixed" else [1.0, 0.2, 0.05]
@@ -292,7 +295,8 @@ def test_batch3d_matches_oracle(G, O, ctx, mode):
         c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
         eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
         ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
-        assert eu < 1e-8 and ep < 1e-8, (k, eu, ep, st)
+        tol, cond = stokes_tolerance(O, g, nus[k], prob.lam, 1)
+        assert eu <= tol and ep <= tol, (k, eu, ep, tol, cond, st)
 
 
 @pytest.mark.gpu
