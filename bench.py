@@ -266,8 +266,9 @@ def run_reference(args):
 # k_pcg_mixed launch on the 48^3 case divided by pcg_bytes() of the same
 # launch: 180.78 GB / 185.73 GB (summary under profiles/).
 TRAFFIC_PER_ALGORITHMIC_BYTE = (163.612 + 17.166) / 185.732
-# the same for k_pcg_mixed_duo (two-run 16-bit columns); None until captured
-TRAFFIC_PER_ALGORITHMIC_BYTE_DUO = None
+# the same for k_pcg_mixed_duo (two-run 16-bit columns, configuration 60208):
+# 153.315 GB / 163.833 GB on the 48^3 case (summary under profiles/)
+TRAFFIC_PER_ALGORITHMIC_BYTE_DUO = (137.023 + 16.292) / 163.833
 
 
 def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool, nduo: int = 0) -> float:
