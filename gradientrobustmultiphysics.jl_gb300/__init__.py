@@ -13,6 +13,7 @@ from .api import (GB300Context, Operator, CellCoefficient, LaplaceOperator, Reac
                   HookStiffnessOperator2D, HookStiffnessOperator3D, BilinearForm, LinearForm, DataFunction,
                   FEMatrix, FEVector, ImportedMatrix, assemble, apply_dirichlet, GB300PCG, spmv,
                   Identity, Gradient, SymmetricGradient, Divergence, ReconstructionIdentity,
+                  ReconstructionIdentityBDM1,
                   ReconstructionDivergence, APT_BilinearForm, APT_SymmetricBilinearForm,
                   ItemIntegrator, L2ErrorIntegrator, L2NormIntegrator, L2DifferenceIntegrator)
 from .fespace import interpolate  # noqa: F401

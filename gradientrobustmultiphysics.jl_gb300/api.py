@@ -27,7 +27,8 @@ Identity = "Identity"
 Gradient = "Gradient"
 SymmetricGradient = "SymmetricGradient"
 Divergence = "Divergence"
-ReconstructionIdentity = "ReconstructionIdentity"
+ReconstructionIdentity = "ReconstructionIdentity"          # ReconstructionIdentity{HDIVRT0{d}}
+ReconstructionIdentityBDM1 = "ReconstructionIdentity{HDIVBDM1}"   # ReconstructionIdentity{HDIVBDM1{d}}
 ReconstructionDivergence = "ReconstructionDivergence"
 
 APT_BilinearForm = "APT_BilinearForm"
@@ -318,7 +319,7 @@ class LinearFormOp:
         r.nparams = self._p.size
         r.factor = float(self.factor)
         r.bonus_quadorder = int(self.f.bonus_quadorder)
-        r.test_operator = 1 if self.test_operator == ReconstructionIdentity else 0
+        r.test_operator = {ReconstructionIdentity: 1, ReconstructionIdentityBDM1: 2}.get(self.test_operator, 0)
         return r
 
 

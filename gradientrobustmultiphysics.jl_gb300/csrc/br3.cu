@@ -1,7 +1,9 @@
-// Bernardi-Raugel H1BR{3} velocity element on tetrahedra with the RT0
-// reconstruction: drop-zero mask (reference operation order), fast assembly
-// of nu (grad u, grad v) + lambda (div R u, div R v), and the reconstructed
-// right-hand side (f, R v).
+// Bernardi-Raugel H1BR{3} velocity element on tetrahedra with the RT0 and
+// BDM1 reconstructions: drop-zero mask (reference operation order), fast
+// assembly of nu (grad u, grad v) + lambda (div R u, div R v) (the same for
+// both reconstructions: the BDM1 functions beyond RT0 carry no flux, so the
+// divergence is the RT0 one), and the reconstructed right-hand side
+// (f, R v).
 //
 // Local DoFs of a tetrahedron (src/fedefs/h1v_br.jl:33 pattern "N1f1"):
 // 0-11 the P1 functions, component-major (4 c + node), 12-15 the face
@@ -265,11 +267,64 @@ __global__ void __launch_bounds__(128) k_br3_rows(int32_t nrows, const int32_t *
 }
 
 // ------------------------------------------------------------------ reconstructed rhs (FP64)
+// BR -> BDM1 reconstruction (src/reconstructions.jl:493-535): R phi is the
+// linear vector field whose normal-flux moments against P1 on every face
+// equal those of phi (the functionals the reference's coefficients
+// _P1_INTO_BDM1_COEFFS_3D encode; its orientation-dependent choice of two
+// linear moments per face only selects a basis of the same space).  On face
+// f with vertices V and moments m_a = int_F (phi . n_F) lambda_a, the
+// field's normal components at the face's vertices are
+// s_a = (12 / |F|) (m_a - (m_0 + m_1 + m_2) / 4); its value at vertex i
+// solves n_F . w_i = s over the three faces at i.  W[dof][vertex][component].
+__device__ void br3_bdm1_fields(const double fv[4], const double nrm[4][3], double W[16][4][3]) {
+    for (int dof = 0; dof < 16; dof++) {
+        double s[4][3];
+        for (int f = 0; f < 4; f++) {
+            double m[3] = {0.0, 0.0, 0.0};
+            for (int a = 0; a < 3; a++) {
+                const int va = kFaces3[f][a];
+                if (dof < 12) {
+                    const int k = dof / 4, p = dof % 4;
+                    const bool on = kFaces3[f][0] == p || kFaces3[f][1] == p || kFaces3[f][2] == p;
+                    if (on) m[a] = nrm[f][k] * fv[f] * (va == p ? 2.0 : 1.0) / 12.0;
+                } else if (dof - 12 == f) {
+                    m[a] = (nrm[f][0] * nrm[f][0] + nrm[f][1] * nrm[f][1] + nrm[f][2] * nrm[f][2]) * fv[f] / 3.0;
+                }
+            }
+            const double mean = (m[0] + m[1] + m[2]) / 4.0;
+            for (int a = 0; a < 3; a++) s[f][a] = (12.0 / fv[f]) * (m[a] - mean);
+        }
+        for (int i = 0; i < 4; i++) {
+            double N[3][3], r[3];
+            int row = 0;
+            for (int f = 0; f < 4; f++)
+                for (int a = 0; a < 3; a++)
+                    if (kFaces3[f][a] == i) {
+                        for (int k = 0; k < 3; k++) N[row][k] = nrm[f][k];
+                        r[row++] = s[f][a];
+                    }
+            const double det = N[0][0] * (N[1][1] * N[2][2] - N[1][2] * N[2][1]) -
+                               N[0][1] * (N[1][0] * N[2][2] - N[1][2] * N[2][0]) +
+                               N[0][2] * (N[1][0] * N[2][1] - N[1][1] * N[2][0]);
+            for (int c = 0; c < 3; c++) {   // Cramer's rule
+                double M[3][3];
+                for (int x = 0; x < 3; x++)
+                    for (int y = 0; y < 3; y++) M[x][y] = (y == c) ? r[x] : N[x][y];
+                W[dof][i][c] = (M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                                M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                                M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0])) /
+                               det;
+            }
+        }
+    }
+}
+
 struct Br3Rhs {
     const double *par;   // [ngroups][nt][5] polynomial terms (component, coef, e1, e2, e3)
     const int32_t *group;   // [ncells] group of each cell, or nullptr (one group)
     int nt;
     double factor;
+    int bdm1;            // 0: RT0 reconstruction, 1: BDM1
     int nq;
     double xref[64][3];
     double w[64];
@@ -289,6 +344,38 @@ __global__ void k_br3_rhs_cells(int ncells, Br3MeshDev m, Br3Rhs r, double *loc)
     br3_rt0(fv, nrm, R, false);
     double lb[16];
     for (int i = 0; i < 16; i++) lb[i] = 0.0;
+    if (r.bdm1) {
+        double W[16][4][3];
+        br3_bdm1_fields(fv, nrm, W);
+        for (int q = 0; q < r.nq; q++) {
+            const double lam[4] = {1.0 - r.xref[q][0] - r.xref[q][1] - r.xref[q][2], r.xref[q][0], r.xref[q][1],
+                                   r.xref[q][2]};
+            double x[3];
+            for (int k = 0; k < 3; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 3; j++) x[k] += A[k][j] * r.xref[q][j];
+            }
+            double fq[3] = {0, 0, 0};
+            const double *gpar = r.par + (r.group ? (size_t)r.group[cell] * r.nt * 5 : 0);
+            for (int t = 0; t < r.nt; t++) {
+                const double *pt = gpar + 5 * t;
+                double v = pt[1];
+                for (int j = 0; j < 3; j++)
+                    if (pt[2 + j] != 0) v *= poly_pow(x[j], pt[2 + j]);
+                fq[(int)pt[0]] += v;
+            }
+            for (int i = 0; i < 16; i++) {
+                double t = 0;
+                for (int k = 0; k < 3; k++)
+                    t += fq[k] * (lam[0] * W[i][0][k] + lam[1] * W[i][1][k] + lam[2] * W[i][2][k] +
+                                  lam[3] * W[i][3][k]);
+                lb[i] += t * r.w[q];
+            }
+        }
+        const double itemfactor = r.factor * vol;
+        for (int i = 0; i < 16; i++) loc[(size_t)cell * 16 + i] = lb[i] * itemfactor;
+        return;
+    }
     for (int q = 0; q < r.nq; q++) {
         const double x0 = r.xref[q][0], y0 = r.xref[q][1], z0 = r.xref[q][2];
         const double rt[4][3] = {{2 * x0, 2 * y0, 2 * (z0 - 1)}, {2 * x0, 2 * (y0 - 1), 2 * z0},
@@ -504,8 +591,8 @@ int grmp_br3_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms
 int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
     grmp_mesh m = s->mesh;
     grmp_context ctx = m->ctx;
-    if (rhs->test_operator != 1)
-        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR{3} right-hand sides: the RT0 reconstruction only");
+    if (rhs->test_operator != 1 && rhs->test_operator != 2)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR{3} right-hand sides: the RT0 or BDM1 reconstruction only");
     if (rhs->kind != GRMP_RHS_POLY || rhs->ncomponents != 3)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "H1BR{3} reconstructed rhs: 3-component polynomial data only");
     const long long ng = rhs->cell_group ? rhs->ngroups : 1;
@@ -535,6 +622,7 @@ int grmp_br3_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b) {
     delete rt;
     r.nt = nt;
     r.factor = rhs->factor;
+    r.bdm1 = rhs->test_operator == 2;
     double *dpar = nullptr;
     int32_t *dgrp = nullptr;
     rc = grmp_upload(ctx, &dpar, rhs->params, (size_t)rhs->nparams);

@@ -269,9 +269,11 @@ typedef struct {
     double factor;          /* LinearForm factor                                     */
     int bonus_quadorder;    /* DataFunction bonus_quadorder                          */
     int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0{d}};
-                               2 = ReconstructionIdentity{HDIVBDM1{2}} (1, 2: H1BR only,
-                               2 in 2D only; src/feevaluator_h1.jl:342-381,
-                               src/reconstructions.jl:351-491)                          */
+                               2 = ReconstructionIdentity{HDIVBDM1{d}} (1, 2: H1BR only;
+                               src/feevaluator_h1.jl:342-381, src/reconstructions.jl:351-535;
+                               in 3D the BDM1 function matching the P1 normal-flux moments of
+                               each face, which the reference's orientation-selected basis
+                               spans)                                                     */
     const int32_t *cell_group; /* optional [ncells]: POLY data per cell group (one DataFunction
                                   per independent problem of a batch); params then hold
                                   [ngroups][nterms][5]                                 */

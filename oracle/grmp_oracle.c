@@ -1557,6 +1557,205 @@ int oracle_br3_rhs(double *b, int ncells, const double *coords, const int *cells
     return nq;
 }
 
+/* H1BR{3} -> HDIVBDM1{3} reconstruction (src/reconstructions.jl:493-535):
+ * R phi is the BDM1 function (a linear vector field on the tetrahedron)
+ * whose normal-flux moments against P1 on every face equal those of phi --
+ * the functionals the reference's coefficients encode: for a P1 function
+ * lambda_p e_k the constant moment |F| n_k / 3 (its RT0 coefficient) and the
+ * linear moments int_F lambda_p (lambda_a - 1/3) n_k = |F| n_k (1/18 if
+ * a = p, -1/36 otherwise) (_P1_INTO_BDM1_COEFFS_3D), for a face bubble its
+ * flux |F| and vanishing linear moments.  The reference's choice of two of
+ * the three linear moments per face by CellFaceOrientations only selects a
+ * basis; R phi does not depend on it, so it is computed here from the
+ * moments themselves.  On face f with vertices V and moments m_a = int_F
+ * (phi . n_F) lambda_a (a in V), the normal components of the linear field
+ * at the face's vertices are s_i = (12/|F|) (m_i - (m_0 + m_1 + m_2)/4)
+ * (the inverse of the P1 mass matrix of the face); the field's value w_i at
+ * vertex i solves n_F . w_i = s_i^F over the three faces at i.  Output
+ * W[dof][vertex][component]. */
+static void br3_bdm1_fields(const double *fvol, const double *nrm, double W[16][4][3])
+{
+    for (int dof = 0; dof < 16; dof++) {
+        double s[4][3];   /* [face][position in BR3_FACES[face]] */
+        for (int f = 0; f < 4; f++) {
+            const double *nf = &nrm[f * 3];
+            double m[3] = {0, 0, 0};
+            for (int a = 0; a < 3; a++) {
+                const int va = BR3_FACES[f][a];
+                if (dof < 12) {
+                    const int k = dof / 4, p = dof % 4;
+                    int onface = 0;
+                    for (int b = 0; b < 3; b++) onface |= BR3_FACES[f][b] == p;
+                    if (onface) m[a] = nf[k] * fvol[f] * (va == p ? 2.0 : 1.0) / 12.0;
+                } else if (dof - 12 == f) {
+                    const double nn = nf[0] * nf[0] + nf[1] * nf[1] + nf[2] * nf[2];
+                    m[a] = nn * fvol[f] / 3.0;   /* 60 int_F l_i l_j l_k l_a = |F| / 3 */
+                }
+            }
+            const double mean = (m[0] + m[1] + m[2]) / 4.0;
+            for (int a = 0; a < 3; a++) s[f][a] = (12.0 / fvol[f]) * (m[a] - mean);
+        }
+        for (int i = 0; i < 4; i++) {
+            double N[3][3], r[3];
+            int row = 0;
+            for (int f = 0; f < 4; f++)
+                for (int a = 0; a < 3; a++)
+                    if (BR3_FACES[f][a] == i) {
+                        for (int k = 0; k < 3; k++) N[row][k] = nrm[f * 3 + k];
+                        r[row++] = s[f][a];
+                    }
+            /* Cramer's rule on the 3 x 3 system N w = r */
+            const double det = N[0][0] * (N[1][1] * N[2][2] - N[1][2] * N[2][1]) -
+                               N[0][1] * (N[1][0] * N[2][2] - N[1][2] * N[2][0]) +
+                               N[0][2] * (N[1][0] * N[2][1] - N[1][1] * N[2][0]);
+            for (int c = 0; c < 3; c++) {
+                double M[3][3];
+                for (int x = 0; x < 3; x++)
+                    for (int y = 0; y < 3; y++) M[x][y] = (y == c) ? r[x] : N[x][y];
+                const double dc = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                                  M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                                  M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+                W[dof][i][c] = dc / det;
+            }
+        }
+    }
+}
+
+/* b += LinearForm(ReconstructionIdentity{HDIVRT0{3}} (recon 1) or
+ * {HDIVBDM1{3}} (recon 2), f) on H1BR{3}: the RT0 case as oracle_br3_rhs,
+ * the BDM1 case with R phi from br3_bdm1_fields (linear in the barycentric
+ * coordinates: R phi(x_q) = sum_i lambda_i(x_q) w_i). */
+int oracle_br3_rhs_recon(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                         const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                         const double *par, int npar, double factor, int bonus_quadorder, int recon)
+{
+    if (recon == 1)
+        return oracle_br3_rhs(b, ncells, coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs, par, npar,
+                              factor, bonus_quadorder);
+    if (recon != 2) return -1;
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(3, 3 + bonus_quadorder, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], nrm[12], fv[4], sg[4];
+        br3_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(3, X, A, G, &det, &vol);
+        double W[16][4][3];
+        br3_bdm1_fields(fv, nrm, W);
+        double locb[16] = {0};
+        for (int q = 0; q < nq; q++) {
+            const double *xr = &xref[3 * q];
+            const double lam[4] = {1.0 - xr[0] - xr[1] - xr[2], xr[0], xr[1], xr[2]};
+            double x[3], f[3];
+            for (int k = 0; k < 3; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 3; j++) x[k] += A[k][j] * xr[j];
+            }
+            rhs_eval(OR_RHS_POLY, 3, 3, par, npar, cell, x, f);
+            for (int i = 0; i < 16; i++) {
+                double t = 0;
+                for (int k = 0; k < 3; k++) {
+                    double rv = 0;
+                    for (int v = 0; v < 4; v++) rv += lam[v] * W[i][v][k];
+                    t += f[k] * rv;
+                }
+                locb[i] += t * w[q];
+            }
+        }
+        const double itemfactor = factor * vol;
+        for (int i = 0; i < 16; i++) b[celldofs[(size_t)cell * 16 + i]] += locb[i] * itemfactor;
+    }
+    return nq;
+}
+
+/* L2ErrorIntegrator(data, ReconstructionIdentity{HDIVRT0{3}} (recon 1) /
+ * {HDIVBDM1{3}} (recon 2)) of an H1BR{3} function u (the velocity error of
+ * the reference's p-robust tests, test/runtests.jl:627-638): sum over cells
+ * of int_T |R u - f|^2 with f polynomial data (params as rhs_eval's POLY),
+ * quadrature of order `order`.  Returns the sum (the squared error). */
+double oracle_br3_recon_l2error(int ncells, const double *coords, const int *cells, const int *cell_faces,
+                                const double *fnormals, const double *fvolumes, const signed char *signs,
+                                const int *celldofs, const double *u, const double *par, int npar, int recon,
+                                int order)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(3, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1.0;
+    double total = 0;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], nrm[12], fv[4], sg[4];
+        br3_cell(&m, cell, X, nrm, fv, sg);
+        double A[3][3], G[3][3], det, vol;
+        oracle_geometry(3, X, A, G, &det, &vol);
+        double W[16][4][3], R[16][4];
+        if (recon == 2) br3_bdm1_fields(fv, nrm, W);
+        else br3_rt0_coeffs(fv, nrm, R);
+        const int *dofs = &celldofs[(size_t)cell * 16];
+        double e = 0;
+        for (int q = 0; q < nq; q++) {
+            const double *xr = &xref[3 * q];
+            const double lam[4] = {1.0 - xr[0] - xr[1] - xr[2], xr[0], xr[1], xr[2]};
+            double ru[3] = {0, 0, 0};
+            if (recon == 2) {
+                for (int j = 0; j < 16; j++)
+                    for (int v = 0; v < 4; v++)
+                        for (int k = 0; k < 3; k++) ru[k] += u[dofs[j]] * lam[v] * W[j][v][k];
+            } else {
+                double rt[4][3];
+                rt03_ref_basis(xr[0], xr[1], xr[2], rt);
+                for (int f = 0; f < 4; f++) {
+                    double cf = 0;
+                    for (int j = 0; j < 16; j++) cf += u[dofs[j]] * R[j][f];
+                    for (int k = 0; k < 3; k++) {
+                        double t = 0;
+                        for (int l = 0; l < 3; l++) t += A[k][l] * rt[f][l];
+                        ru[k] += cf * t * sg[f] / fabs(det);
+                    }
+                }
+            }
+            double x[3], f[3];
+            for (int k = 0; k < 3; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 3; j++) x[k] += A[k][j] * xr[j];
+            }
+            rhs_eval(OR_RHS_POLY, 3, 3, par, npar, cell, x, f);
+            double r2 = 0;
+            for (int k = 0; k < 3; k++) r2 += (ru[k] - f[k]) * (ru[k] - f[k]);
+            e += r2 * w[q];
+        }
+        total += e * vol;
+    }
+    return total;
+}
+
+/* Linear face moments of the BDM1 reconstruction of the P1 function
+ * lambda_p e_k on face f, int_F (R phi . n_F)(lambda_a - 1/3) for the face's
+ * three vertices a, divided by |F| n_F[k] (the entries of the reference's
+ * _P1_INTO_BDM1_COEFFS_3D when p lies on the face); for checking the
+ * reconstruction against that table. */
+void oracle_br3_bdm1_moments(const double *fvol, const double *nrm, int p, int k, int f, double out[3])
+{
+    double W[16][4][3];
+    br3_bdm1_fields(fvol, nrm, W);
+    const double *nf = &nrm[f * 3];
+    double sn[3];   /* normal component of R phi at the face's vertices */
+    for (int a = 0; a < 3; a++) {
+        const int v = BR3_FACES[f][a];
+        sn[a] = W[4 * k + p][v][0] * nf[0] + W[4 * k + p][v][1] * nf[1] + W[4 * k + p][v][2] * nf[2];
+    }
+    /* int_F (sum_b sn_b l_b)(l_a - 1/3) = |F| (sum_b sn_b (1 + d_ab)/12 - (sum_b sn_b)/9) */
+    const double tot = sn[0] + sn[1] + sn[2];
+    for (int a = 0; a < 3; a++) {
+        const double ma = (tot + sn[a]) / 12.0 - tot / 9.0;
+        out[a] = ma / nf[k];
+    }
+}
+
 /* Divergence of H1BR{3} functions with coefficients on the rule of order 2
  * (polyorder 3 - 1 + 0 for (div u, q_P0); exact for the quadratic divergence
  * of the bubbles): divu[cell] = (1/|T|) int_T div u and

@@ -100,6 +100,11 @@ def lib():
         L.oracle_br3_rhs.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.oracle_br3_rhs.restype = ctypes.c_int
         L.oracle_br3_div.argtypes = brm + [dp, dp, dp, dp]
+        L.oracle_br3_rhs_recon.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.oracle_br3_rhs_recon.restype = ctypes.c_int
+        L.oracle_br3_bdm1_moments.argtypes = [dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+        L.oracle_br3_recon_l2error.argtypes = brm + [dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_br3_recon_l2error.restype = ctypes.c_double
     return _lib
 
 
@@ -401,10 +406,12 @@ RECON_RT0, RECON_BDM1 = 1, 2
 
 
 def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, recon: int = RECON_RT0):
-    # (2D: H1BR{2} with RT0 or BDM1; 3D: H1BR{3} with RT0)
+    # (2D: H1BR{2} with RT0 or BDM1; 3D: H1BR{3} with RT0 or BDM1)
     """(A (penalised), bf, fixed, celldofs) of the velocity update system:
     nu (grad u, grad v) + lam (div R u, div R v) = (f, R_rhs v), R_rhs the
-    BR->RT0 (recon 1) or BR->BDM1 (recon 2) reconstruction."""
+    BR->RT0 (recon 1) or BR->BDM1 (recon 2) reconstruction (the penalty uses
+    the RT0 divergence: the BDM1 functions beyond RT0 carry no flux, so the
+    divergence of either reconstruction is the same cell constant)."""
     fn, cf = g.faces()
     cd, nd = br_celldofs(g.nverts, g.cells, cf)
     arrs, ptrs = _br_args(g, cd)
@@ -412,10 +419,8 @@ def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, 
     bf = np.zeros(nd)
     par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
     if g.dim == 3:
-        if recon != RECON_RT0:
-            raise ValueError("H1BR{3}: the RT0 reconstruction only")
         lib().oracle_br3_assemble(M.h, *ptrs, float(nu), None, float(lam))
-        if lib().oracle_br3_rhs(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder)) < 0:
+        if lib().oracle_br3_rhs_recon(_dp(bf), *ptrs, _dp(par), par.size, 1.0, int(bonus_quadorder), int(recon)) < 0:
             raise RuntimeError("oracle: no tetrahedral rule of that order")
     else:
         lib().oracle_br_assemble(M.h, *ptrs, float(nu), None, float(lam))
@@ -426,6 +431,20 @@ def br_stokes_system(g, nu: float, lam: float, terms, bonus_quadorder: int = 2, 
     fixed = np.unique(np.concatenate([bnodes + c * g.nverts for c in range(g.dim)] +
                                      [bf_ids + g.dim * g.nverts])).astype(np.int32)
     return M, bf, fixed, cd, (arrs, ptrs)
+
+
+def br3_recon_l2error(g, u, terms, recon: int = RECON_BDM1, order: int = 4) -> float:
+    """L2 error ||R u - f|| of an H1BR{3} function's reconstruction (RT0 or
+    BDM1) against polynomial data f (terms (component, coef, e1, e2, e3))."""
+    fn, cf = g.faces()
+    cd, nd = br_celldofs(g.nverts, g.cells, cf)
+    _, ptrs = _br_args(g, cd)
+    par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
+    uu = np.ascontiguousarray(u, dtype=np.float64)
+    e2 = lib().oracle_br3_recon_l2error(*ptrs, _dp(uu), _dp(par), par.size, int(recon), int(order))
+    if e2 < 0:
+        raise RuntimeError("oracle: no tetrahedral rule of that order")
+    return float(np.sqrt(e2))
 
 
 def br_div(g, cd_args, u=None, p=None):
