@@ -195,10 +195,10 @@ def test_br3_refusals_and_high_orders(G, ctx):
     g = G.grid_unitcube_kuhn(2)
     FES = F.FESpace(F.H1BR(3), g)
     b = api.FEVector(ctx, FES)
-    with pytest.raises(G.GrmpError) as ei:   # BDM1 is the 2D reconstruction only
+    with pytest.raises(G.GrmpError) as ei:   # reconstructions into RT0 and BDM1 only
         lf = api.LinearForm(api.ReconstructionIdentity, api.DataFunction.polynomial(GRAD_PHI, 3))
         r = lf.rhs()
-        r.test_operator = 2
+        r.test_operator = 3
         import ctypes
         ctx.check(ctx.lib.grmp_assemble_linear(ctx.space(FES), ctypes.byref(r), b.h))
     assert ei.value.code == L.ERR_UNSUPPORTED
