@@ -106,7 +106,7 @@ __global__ void k_cell_factors(int ncells, const double *coords, const int32_t *
 // owns blockDim.x consecutive rows; their values (contiguous in the CSR) are
 // accumulated in shared memory, each thread adding its row's contributions in
 // incidence order, and written out once with coalesced stores.
-template <int DIM, int NB, int NC, typename T, typename S>
+template <int DIM, int NB, int NC, typename T, typename S, bool LAP1 = false>
 __global__ void __launch_bounds__(128) k_assemble_rows(int32_t nrows, const int32_t *__restrict__ inc_ptr,
                                                        const int32_t *__restrict__ inc_cell,
                                                        const uint8_t *__restrict__ inc_loc,
@@ -134,6 +134,25 @@ __global__ void __launch_bounds__(128) k_assemble_rows(int32_t nrows, const int3
             const int c1 = A / NB, a = A - c1 * NB;
             const T *cf = fac + (size_t)cell * ft.nf_total;
             const S *sl = slot + (size_t)p * LD;
+            if (LAP1) {   // one Laplace term: its DIM(DIM+1)/2 factors in registers
+                constexpr int NT = DIM * (DIM + 1) / 2;
+                T fl[NT];
+#pragma unroll
+                for (int q = 0; q < NT; q++) fl[q] = cf[q];
+#pragma unroll
+                for (int B = 0; B < LD; B++) {
+                    const S s = sl[B];
+                    if (s == DROP) continue;
+                    const int c2 = B / NB, b = B - c2 * NB;
+                    if (c1 != c2) continue;
+                    const T *tt = tens + a * NB + b;
+                    T v = 0;
+#pragma unroll
+                    for (int q = 0; q < NT; q++) v += fl[q] * tt[q * NB * NB];
+                    rv[s] += v;
+                }
+                continue;
+            }
             T f[GRMP_MAX_TERMS * 16];
             for (int i = 0; i < ft.nf_total && i < GRMP_MAX_TERMS * 16; i++) f[i] = cf[i];
 #pragma unroll
@@ -165,7 +184,7 @@ __global__ void __launch_bounds__(128) k_assemble_rows(int32_t nrows, const int3
 // Both precisions in one walk: the FP64 and the FP32 contribution of every
 // (row, cell, DoF) triple, each from its own factors and reference tensors in
 // its own arithmetic, accumulated into two shared-memory row blocks.
-template <int DIM, int NB, int NC, typename S>
+template <int DIM, int NB, int NC, typename S, bool LAP1 = false>
 __global__ void __launch_bounds__(128) k_assemble_rows2(int32_t nrows, const int32_t *__restrict__ inc_ptr,
                                                         const int32_t *__restrict__ inc_cell,
                                                         const uint8_t *__restrict__ inc_loc,
@@ -174,12 +193,12 @@ __global__ void __launch_bounds__(128) k_assemble_rows2(int32_t nrows, const int
                                                         const double *__restrict__ gtens64,
                                                         const float *__restrict__ gtens32, FastTerms ft,
                                                         double *__restrict__ vals64, float *__restrict__ vals32,
-                                                        int max_row_nnz) {
+                                                        int block_nnz) {
     constexpr int LD = NB * NC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *tens64 = reinterpret_cast<double *>(smem_raw);
     double *acc64 = tens64 + ft.tens_total;
-    float *tens32 = reinterpret_cast<float *>(acc64 + (size_t)blockDim.x * max_row_nnz);
+    float *tens32 = reinterpret_cast<float *>(acc64 + block_nnz);
     float *acc32 = tens32 + ((ft.tens_total + 1) & ~1);
     const int row0 = blockIdx.x * blockDim.x;
     const int row1 = min(row0 + (int)blockDim.x, nrows);
@@ -206,6 +225,34 @@ __global__ void __launch_bounds__(128) k_assemble_rows2(int32_t nrows, const int
             const double *cf64 = fac64 + (size_t)cell * ft.nf_total;
             const float *cf32 = fac32 + (size_t)cell * ft.nf_total;
             const S *sl = slot + (size_t)p * LD;
+            if (LAP1) {   // one Laplace term: both precisions' factors in registers
+                constexpr int NT = DIM * (DIM + 1) / 2;
+                double g64[NT];
+                float g32[NT];
+#pragma unroll
+                for (int q = 0; q < NT; q++) {
+                    g64[q] = cf64[q];
+                    g32[q] = cf32[q];
+                }
+#pragma unroll
+                for (int B = 0; B < LD; B++) {
+                    const S s = sl[B];
+                    if (s == DROP) continue;
+                    const int c2 = B / NB, b = B - c2 * NB;
+                    if (c1 != c2) continue;
+                    const int to = a * NB + b;
+                    double v = 0;
+                    float w = 0;
+#pragma unroll
+                    for (int q = 0; q < NT; q++) {
+                        v += g64[q] * tens64[to + q * NB * NB];
+                        w += g32[q] * tens32[to + q * NB * NB];
+                    }
+                    rv64[s] += v;
+                    rv32[s] += w;
+                }
+                continue;
+            }
             double f64[GRMP_MAX_TERMS * 16];
             float f32[GRMP_MAX_TERMS * 16];
             for (int i = 0; i < ft.nf_total && i < GRMP_MAX_TERMS * 16; i++) {
@@ -247,6 +294,27 @@ __global__ void __launch_bounds__(128) k_assemble_rows2(int32_t nrows, const int
         vals32[v0 + i] = acc32[i];
     }
 }
+
+// Largest number of values a block of `tpb` consecutive rows holds (the
+// shared-memory accumulator is sized by it, not by tpb x the longest row).
+int block_nnz_max(grmp_matrix A, int tpb, int *out) {
+    grmp_context ctx = A->space->mesh->ctx;
+    if (A->blk_tpb != tpb) {
+        std::vector<int32_t> rp((size_t)A->nrows + 1);
+        cudaError_t e = cudaMemcpyAsync(rp.data(), A->d_rowptr, rp.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "assembly: row pointer download");
+        int mx = 0;
+        for (int r0 = 0; r0 < A->nrows; r0 += tpb) mx = std::max(mx, rp[std::min(A->nrows, r0 + tpb)] - rp[r0]);
+        A->blk_tpb = tpb;
+        A->blk_nnz = mx;
+    }
+    *out = A->blk_nnz;
+    return GRMP_OK;
+}
+
+// a single Laplace term: the register-resident kernel variants
+inline bool single_laplace(const FastTerms &ft) { return ft.n == 1 && ft.t[0].op == GRMP_OP_LAPLACE; }
 
 template <int DIM, int NB, int NC>
 int run_assembly_dual(grmp_matrix A, const FastTerms &ft, const std::vector<double> &tens64) {
@@ -293,25 +361,34 @@ int run_assembly_dual(grmp_matrix A, const FastTerms &ft, const std::vector<doub
         return rc;
     }
     const size_t tens_b = tens64.size() * 8 + ((tens32.size() + 1) & ~(size_t)1) * 4;
-    int tpb = 128;
-    while (tpb > 32 && tens_b + (size_t)tpb * A->max_row_nnz * 12 > 100 * 1024) tpb /= 2;
-    const size_t shm = tens_b + (size_t)tpb * A->max_row_nnz * 12 + 16;
+    int tpb = 128, bnz = 0;
+    rc = block_nnz_max(A, tpb, &bnz);
+    while (!rc && tpb > 32 && tens_b + (size_t)bnz * 12 > 100 * 1024) {
+        tpb /= 2;
+        rc = block_nnz_max(A, tpb, &bnz);
+    }
+    if (rc) {
+        release();
+        return rc;
+    }
+    const size_t shm = tens_b + (size_t)bnz * 12 + 16;
     if (shm > 220 * 1024) {
         release();
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
     }
+    auto launch = [&](auto kern, const auto *slot) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, slot,
+                                                            A->d_rowptr, fac64, fac32, dt64, dt32, ft, A->d_vals64,
+                                                            A->d_vals32, bnz);
+    };
+    const bool lap1 = single_laplace(ft);
     if (A->slot_bytes == 1) {
-        auto kern = k_assemble_rows2<DIM, NB, NC, uint8_t>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
-                                                            (const uint8_t *)A->d_slot, A->d_rowptr, fac64, fac32,
-                                                            dt64, dt32, ft, A->d_vals64, A->d_vals32, A->max_row_nnz);
+        if (lap1) launch(k_assemble_rows2<DIM, NB, NC, uint8_t, true>, (const uint8_t *)A->d_slot);
+        else launch(k_assemble_rows2<DIM, NB, NC, uint8_t, false>, (const uint8_t *)A->d_slot);
     } else {
-        auto kern = k_assemble_rows2<DIM, NB, NC, uint16_t>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
-                                                            (const uint16_t *)A->d_slot, A->d_rowptr, fac64, fac32,
-                                                            dt64, dt32, ft, A->d_vals64, A->d_vals32, A->max_row_nnz);
+        if (lap1) launch(k_assemble_rows2<DIM, NB, NC, uint16_t, true>, (const uint16_t *)A->d_slot);
+        else launch(k_assemble_rows2<DIM, NB, NC, uint16_t, false>, (const uint16_t *)A->d_slot);
     }
     GRMP_LAUNCHED(ctx);
     cudaError_t e = cudaGetLastError();
@@ -359,25 +436,34 @@ int run_assembly(grmp_matrix A, const FastTerms &ft, const std::vector<double> &
         }
         vals = (T *)A->d_vals32;
     }
-    // rows per block: their values (at most rows x longest row) and the
+    // rows per block: their values (the largest block's count) and the
     // reference tensors in shared memory, at most ~100 KB so that two blocks fit an SM
     const size_t tens_b = ((tens.size() + 1) & ~(size_t)1) * sizeof(T);
-    int tpb = 128;
-    while (tpb > 32 && tens_b + (size_t)tpb * A->max_row_nnz * sizeof(T) > 100 * 1024) tpb /= 2;
-    size_t shm = tens_b + (size_t)tpb * A->max_row_nnz * sizeof(T);
+    int tpb = 128, bnz = 0;
+    rc = block_nnz_max(A, tpb, &bnz);
+    while (!rc && tpb > 32 && tens_b + (size_t)bnz * sizeof(T) > 100 * 1024) {
+        tpb /= 2;
+        rc = block_nnz_max(A, tpb, &bnz);
+    }
+    if (rc) {
+        grmp_free(ctx, dtens, tens.size() * sizeof(T));
+        return rc;
+    }
+    size_t shm = tens_b + (size_t)bnz * sizeof(T);
     if (shm > 220 * 1024) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
+    auto launch = [&](auto kern, const auto *slot) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, slot,
+                                                            A->d_rowptr, fac, dtens, ft, vals);
+        GRMP_LAUNCHED(ctx);
+    };
+    const bool lap1 = single_laplace(ft);
     if (A->slot_bytes == 1) {
-        auto kern = k_assemble_rows<DIM, NB, NC, T, uint8_t>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
-                                                            (const uint8_t *)A->d_slot, A->d_rowptr, fac, dtens, ft, vals);
-        GRMP_LAUNCHED(ctx);
+        if (lap1) launch(k_assemble_rows<DIM, NB, NC, T, uint8_t, true>, (const uint8_t *)A->d_slot);
+        else launch(k_assemble_rows<DIM, NB, NC, T, uint8_t, false>, (const uint8_t *)A->d_slot);
     } else {
-        auto kern = k_assemble_rows<DIM, NB, NC, T, uint16_t>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
-                                                            (const uint16_t *)A->d_slot, A->d_rowptr, fac, dtens, ft, vals);
-        GRMP_LAUNCHED(ctx);
+        if (lap1) launch(k_assemble_rows<DIM, NB, NC, T, uint16_t, true>, (const uint16_t *)A->d_slot);
+        else launch(k_assemble_rows<DIM, NB, NC, T, uint16_t, false>, (const uint16_t *)A->d_slot);
     }
     cudaError_t e = cudaGetLastError();
     grmp_free(ctx, dtens, tens.size() * sizeof(T));

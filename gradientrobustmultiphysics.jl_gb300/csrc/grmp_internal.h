@@ -116,6 +116,9 @@ struct grmp_matrix_s {
     double *d_imp_diag = nullptr;      // [nrows] the caller's diagonal
     double *d_imp_b = nullptr;         // [nrows] right-hand side of the eliminated system
     int *d_imp_count = nullptr;
+    // largest value count of a block of blk_tpb consecutive rows (assembly's
+    // shared-memory accumulator; 0 = not computed)
+    int blk_tpb = 0, blk_nnz = 0;
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;
