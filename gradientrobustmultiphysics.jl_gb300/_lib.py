@@ -78,13 +78,14 @@ class Request(ctypes.Structure):
                 ("ncomponents", ctypes.c_int), ("ndofs", ctypes.c_int32),
                 ("celldofs", ctypes.POINTER(ctypes.c_int32)), ("nterms", ctypes.c_int),
                 ("terms", ctypes.POINTER(BilinearTerm)), ("rhs", Rhs), ("nfixed", ctypes.c_int32),
-                ("fixed", ctypes.POINTER(ctypes.c_int32)), ("solve", SolveParams)]
+                ("fixed", ctypes.POINTER(ctypes.c_int32)), ("solve", SolveParams), ("mesh_key", ctypes.c_uint64)]
 
 
 class RequestStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("slot", ctypes.c_int32), ("iterations", ctypes.c_int32),
                 ("outer_iterations", ctypes.c_int32), ("final_relres", ctypes.c_double), ("queue_ms", ctypes.c_double),
-                ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+                ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("solve_ms", ctypes.c_double),
+                ("ndofs", ctypes.c_int32), ("resident", ctypes.c_int32)]
 
 
 # every symbol of include/grmp.h with (argtypes, restype)

@@ -10,6 +10,14 @@
 // only on the request (launch shapes are chosen from its own sizes), so its
 // result is bit-identical whether it runs alone or in the mix.
 //
+// Residency: a request with a non-zero mesh_key leaves its mesh, DoF map,
+// sparsity pattern (with the solver workspace and tuned state) and vectors
+// on the device, in the slot that ran it (an LRU list of kSlotResident
+// entries per slot); a later request with the same key and operator
+// structure runs there and skips the upload and setup.  Resident entries
+// count against the budget; when the head of the queue does not fit, the
+// admission loop drops least recently used entries of idle slots.
+//
 // No counterpart in the reference (it is single-process, one solve at a time);
 // each request is one solve_direct! (src/solvers.jl:622-686) of a linear
 // problem with the operators of include/grmp.h.
@@ -26,6 +34,8 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+constexpr int kSlotResident = 4;   // resident problems kept per slot
+
 struct Request {
     int64_t id = 0;
     // copies of the caller's data
@@ -33,6 +43,9 @@ struct Request {
     int32_t nverts = 0, ncells = 0, ndofs = 0;
     std::vector<double> coords;
     std::vector<int32_t> cells, celldofs, fixed;
+    bool device_dofmap = false;     // celldofs built on the device
+    bool all_boundary = false;      // fixed = every boundary DoF (device)
+    uint64_t key = 0, sig = 0;      // residency key and operator-structure signature
     std::vector<grmp_bilinear_term> terms;
     std::vector<std::vector<double>> term_coef;
     grmp_rhs rhs{};
@@ -46,11 +59,35 @@ struct Request {
     Clock::time_point t_submit, t_start, t_end;
 };
 
+// Device data of one problem, reused by later requests with its key.
+struct Resident {
+    uint64_t key = 0, sig = 0;
+    grmp_mesh mesh = nullptr;
+    grmp_space space = nullptr;
+    grmp_matrix A = nullptr;
+    grmp_vector b = nullptr, x = nullptr;
+    std::vector<int32_t> fixed;
+    int32_t ndofs = 0;
+    size_t bytes = 0;        // counted against the budget
+    uint64_t last_use = 0;
+};
+
+void destroy_resident(Resident &r) {
+    if (r.x) grmp_vector_destroy(r.x);
+    if (r.b) grmp_vector_destroy(r.b);
+    if (r.A) grmp_matrix_destroy(r.A);
+    if (r.space) grmp_space_destroy(r.space);
+    if (r.mesh) grmp_mesh_destroy(r.mesh);
+    r = Resident();
+}
+
 struct Worker {
     grmp_context ctx = nullptr;
     std::thread th;
     std::shared_ptr<Request> job;
     bool has_job = false;
+    bool hit = false;                 // the job's key is resident here
+    std::vector<Resident> cache;      // touched by the worker while it has a job, by the admitter otherwise
 };
 
 }  // namespace
@@ -64,6 +101,7 @@ struct grmp_server_s {
     std::map<int64_t, std::shared_ptr<Request>> all;
     std::vector<Worker> workers;
     int64_t next_id = 1;
+    uint64_t clock = 0;      // LRU stamps
     bool stop = false;
     std::thread admitter;
     std::string last_error;
@@ -77,54 +115,147 @@ size_t estimate_bytes(const Request &r) {
     int ld = grmp_fe_ldofs(r.fe, r.dim, r.ncomp);
     double nnz_per_row = r.fe == GRMP_FE_H1P1 ? (r.dim == 2 ? 8 : 16) : (r.dim == 2 ? 14 : 30);
     nnz_per_row *= r.ncomp;
-    double nnz = nnz_per_row * r.ndofs;
+    // a device-built DoF map: vertices plus (P2) edges / faces, bounded from the cell count
+    const double nd = r.ndofs > 0 ? (double)r.ndofs
+                                  : (double)r.ncomp * (r.nverts + (r.fe == GRMP_FE_H1P2
+                                                                       ? (r.dim == 2 ? 1.5 : 1.25) * r.ncells + r.nverts
+                                                                       : 0.0));
+    double nnz = nnz_per_row * nd;
     double b = nnz * (8 + 4 + 4) + (double)r.ncells * ld * (4 + 1 + 4 + 2 * ld + 8) +
-               (double)r.nverts * r.dim * 8 + (double)r.ncells * (r.dim + 1) * 4 + (double)r.ndofs * 120.0 +
+               (double)r.nverts * r.dim * 8 + (double)r.ncells * (r.dim + 1) * 4 + nd * 120.0 +
                (double)r.ncells * 16 * 8;
     return (size_t)(1.25 * b) + (16u << 20);
 }
 
-// One request, synchronously, on a worker's context.
-int run_request(grmp_context ctx, Request &r) {
-    grmp_mesh mesh = nullptr;
-    grmp_space space = nullptr;
-    grmp_matrix A = nullptr;
-    grmp_vector b = nullptr, x = nullptr;
-    int rc = grmp_mesh_upload(ctx, r.dim, r.nverts, r.coords.data(), r.ncells, r.cells.data(), &mesh);
-    if (!rc) rc = grmp_space_create(mesh, r.fe, r.ncomp, r.celldofs.data(), r.ndofs, &space);
+// Mesh, DoF map, pattern, vectors and Dirichlet DoFs of a request.
+int build_resident(grmp_context ctx, Request &r, Resident &res) {
+    int rc = grmp_mesh_upload(ctx, r.dim, r.nverts, r.coords.data(), r.ncells, r.cells.data(), &res.mesh);
+    if (!rc) {
+        if (r.device_dofmap) {
+            rc = grmp_space_create_on_device(res.mesh, r.fe, r.ncomp, &res.space, &res.ndofs);
+        } else {
+            rc = grmp_space_create(res.mesh, r.fe, r.ncomp, r.celldofs.data(), r.ndofs, &res.space);
+            res.ndofs = r.ndofs;
+        }
+    }
+    if (!rc) {
+        // A resident pattern serves later coefficients too: it is built with
+        // unit factors and no cell coefficients, so it drops only the entries
+        // whose contributions vanish for the operator kinds themselves (the
+        // reference likewise keeps a matrix's pattern when it refills it with
+        // zeros and assembles again, src/fematrix.jl:220-232,
+        // src/solvers.jl:556).  A one-off request uses its own coefficients.
+        std::vector<grmp_bilinear_term> pt = r.terms;
+        if (r.key != 0)
+            for (auto &t : pt) {
+                t.factor = 1.0;
+                t.cell_coef = nullptr;
+                t.coef_on_device = 0;
+                if (t.op_kind == GRMP_OP_HOOKE) {
+                    t.param[0] = 1.0;
+                    t.param[1] = 1.6180339887498949;   // no coincidental cancellation of mu and lambda parts
+                }
+            }
+        else
+            for (size_t i = 0; i < pt.size(); i++)
+                pt[i].cell_coef = r.term_coef[i].empty() ? nullptr : r.term_coef[i].data();
+        rc = grmp_pattern_build(res.space, (int)pt.size(), pt.data(), &res.A);
+    }
+    if (!rc) rc = grmp_vector_create(ctx, res.ndofs, &res.b);
+    if (!rc) rc = grmp_vector_create(ctx, res.ndofs, &res.x);
+    if (!rc) {
+        if (r.all_boundary) {
+            int32_t nb = 0;
+            rc = grmp_space_boundary_dofs(res.space, 0, nullptr, &nb);
+            if (!rc) {
+                res.fixed.resize(nb);
+                rc = grmp_space_boundary_dofs(res.space, nb, res.fixed.data(), &nb);
+            }
+        } else {
+            res.fixed = r.fixed;
+        }
+    }
+    res.key = r.key;
+    res.sig = r.sig;
+    res.bytes = r.bytes;
+    if (rc) destroy_resident(res);
+    return rc;
+}
+
+// Assembly with the request's coefficients, its right-hand side, Dirichlet
+// elimination and the solve on resident (or freshly built) data.
+int run_on(grmp_context ctx, Request &r, Resident &res) {
     for (size_t i = 0; i < r.terms.size(); i++)
         r.terms[i].cell_coef = r.term_coef[i].empty() ? nullptr : r.term_coef[i].data();
     r.rhs.params = r.rhs_params.data();
     r.rhs.cell_group = nullptr;
-    if (!rc) rc = grmp_pattern_build(space, (int)r.terms.size(), r.terms.data(), &A);
     const bool mixed = r.solve.mode == GRMP_SOLVE_MIXED;
     // one walk of the incidence lists fills both precisions (bit-identical to two passes)
-    if (!rc) rc = grmp_assemble_bilinear(A, (int)r.terms.size(), r.terms.data(), mixed ? GRMP_FP64_FP32 : GRMP_FP64);
-    if (!rc) rc = grmp_vector_create(ctx, r.ndofs, &b);
-    if (!rc) rc = grmp_vector_create(ctx, r.ndofs, &x);
-    if (!rc) rc = grmp_assemble_linear(space, &r.rhs, b);
+    int rc = grmp_assemble_bilinear(res.A, (int)r.terms.size(), r.terms.data(), mixed ? GRMP_FP64_FP32 : GRMP_FP64);
+    if (!rc) rc = grmp_vector_fill(res.b, 0.0);
+    if (!rc) rc = grmp_vector_fill(res.x, 0.0);   // the same zero start as a fresh request
+    if (!rc) rc = grmp_assemble_linear(res.space, &r.rhs, res.b);
     if (!rc)
-        rc = grmp_apply_dirichlet(A, b, (int32_t)r.fixed.size(), r.fixed.empty() ? nullptr : r.fixed.data(), nullptr,
-                                  GRMP_DIRICHLET_ELIMINATE, 1e60);
+        rc = grmp_apply_dirichlet(res.A, res.b, (int32_t)res.fixed.size(), res.fixed.empty() ? nullptr : res.fixed.data(),
+                                  nullptr, GRMP_DIRICHLET_ELIMINATE, 1e60);
     grmp_solve_stats st{};
     // the SpMV configuration comes from the request's own sizes, never from
     // timings taken while other requests share the GPU
     if (r.solve.spmv_config == 0) r.solve.spmv_config = -1;
-    if (!rc) rc = grmp_solve(A, b, x, &r.solve, &st);
+    if (!rc) rc = grmp_solve(res.A, res.b, res.x, &r.solve, &st);
     if (!rc || rc == GRMP_ERR_NOT_CONVERGED) {
-        r.x.resize(r.ndofs);
-        int rc2 = grmp_vector_download(x, r.x.data());
+        r.x.resize(res.ndofs);
+        int rc2 = grmp_vector_download(res.x, r.x.data());
         if (!rc) rc = rc2;
     }
     r.stats.iterations = st.iterations;
     r.stats.outer_iterations = st.outer_iterations;
     r.stats.final_relres = st.final_relres;
     r.stats.solve_ms = st.solve_ms;
-    if (x) grmp_vector_destroy(x);
-    if (b) grmp_vector_destroy(b);
-    if (A) grmp_matrix_destroy(A);
-    if (space) grmp_space_destroy(space);
-    if (mesh) grmp_mesh_destroy(mesh);
+    r.stats.ndofs = res.ndofs;
+    return rc;
+}
+
+// One request, synchronously, on a worker's context: on its resident entry
+// (a hit), or on data built for it and then kept (key != 0, least recently
+// used entry of the slot dropped when full) or freed.  *freed receives the
+// bytes released from the budget.
+int run_request(grmp_server srv, Worker &me, Request &r, size_t *freed) {
+    grmp_context ctx = me.ctx;
+    *freed = 0;
+    if (me.hit) {
+        for (auto &e : me.cache)
+            if (e.key == r.key && e.sig == r.sig) {
+                r.stats.resident = 1;
+                if (!r.all_boundary) e.fixed = r.fixed;   // the request's own Dirichlet DoFs
+                {
+                    std::lock_guard<std::mutex> lk(srv->mu);
+                    e.last_use = ++srv->clock;
+                }
+                int rc = run_on(ctx, r, e);
+                grmp_synchronize(ctx);
+                return rc;
+            }
+    }
+    Resident res;
+    int rc = build_resident(ctx, r, res);
+    if (!rc) rc = run_on(ctx, r, res);
+    if (!rc && r.key != 0) {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        if ((int)me.cache.size() >= kSlotResident) {   // drop the slot's least recently used entry
+            size_t lru = 0;
+            for (size_t i = 1; i < me.cache.size(); i++)
+                if (me.cache[i].last_use < me.cache[lru].last_use) lru = i;
+            *freed += me.cache[lru].bytes;
+            destroy_resident(me.cache[lru]);
+            me.cache.erase(me.cache.begin() + lru);
+        }
+        res.last_use = ++srv->clock;
+        me.cache.push_back(res);   // its bytes stay counted
+    } else {
+        destroy_resident(res);
+        *freed += r.bytes;
+    }
     grmp_synchronize(ctx);
     return rc;
 }
@@ -140,7 +271,8 @@ void worker_loop(grmp_server srv, int w) {
             job = me.job;
         }
         job->t_start = Clock::now();
-        int rc = run_request(me.ctx, *job);
+        size_t freed = 0;
+        int rc = run_request(srv, me, *job, &freed);
         job->t_end = Clock::now();
         {
             std::lock_guard<std::mutex> lk(srv->mu);
@@ -150,13 +282,52 @@ void worker_loop(grmp_server srv, int w) {
             job->stats.run_ms = std::chrono::duration<double, std::milli>(job->t_end - job->t_start).count();
             job->stats.latency_ms = std::chrono::duration<double, std::milli>(job->t_end - job->t_submit).count();
             job->done = true;
-            srv->in_use -= job->bytes;
+            srv->in_use -= freed;
             me.job.reset();
             me.has_job = false;
+            me.hit = false;
         }
         srv->cv_done.notify_all();
         srv->cv_admit.notify_all();
     }
+}
+
+// the idle slot holding the request's key, or -1
+int resident_slot(grmp_server srv, const Request &q) {
+    if (q.key == 0) return -1;
+    for (size_t w = 0; w < srv->workers.size(); w++) {
+        const Worker &wk = srv->workers[w];
+        if (wk.has_job) continue;
+        for (const auto &e : wk.cache)
+            if (e.key == q.key && e.sig == q.sig) return (int)w;
+    }
+    return -1;
+}
+
+// Drops the least recently used resident entry of an idle slot (not the one
+// `keep` names); false when there is none.  Called with srv->mu held.
+bool evict_one(grmp_server srv, int keep_w, uint64_t keep_key) {
+    int bw = -1;
+    size_t bi = 0;
+    uint64_t best = UINT64_MAX;
+    for (size_t w = 0; w < srv->workers.size(); w++) {
+        Worker &wk = srv->workers[w];
+        if (wk.has_job) continue;
+        for (size_t i = 0; i < wk.cache.size(); i++) {
+            if ((int)w == keep_w && wk.cache[i].key == keep_key) continue;
+            if (wk.cache[i].last_use < best) {
+                best = wk.cache[i].last_use;
+                bw = (int)w;
+                bi = i;
+            }
+        }
+    }
+    if (bw < 0) return false;
+    Worker &wk = srv->workers[bw];
+    srv->in_use -= wk.cache[bi].bytes;
+    destroy_resident(wk.cache[bi]);   // the slot is idle: its context is not in use
+    wk.cache.erase(wk.cache.begin() + bi);
+    return true;
 }
 
 void admit_loop(grmp_server srv) {
@@ -167,19 +338,30 @@ void admit_loop(grmp_server srv) {
             if (srv->queue.empty()) return false;
             bool idle = false;
             for (auto &w : srv->workers) idle = idle || !w.has_job;
-            return idle && (srv->in_use + srv->queue.front()->bytes <= srv->budget || srv->in_use == 0);
+            if (!idle) return false;
+            const auto &q = *srv->queue.front();
+            if (resident_slot(srv, q) >= 0) return true;   // runs on its resident data: no new memory
+            while (srv->in_use + q.bytes > srv->budget && evict_one(srv, -1, 0)) {
+            }
+            return srv->in_use + q.bytes <= srv->budget || srv->in_use == 0;
         });
         if (srv->stop) return;
         // first come, first served; the head waits for memory (no starvation)
         auto job = srv->queue.front();
         srv->queue.pop_front();
-        for (auto &w : srv->workers)
-            if (!w.has_job) {
-                w.job = job;
-                w.has_job = true;
-                srv->in_use += job->bytes;
-                break;
-            }
+        const int rw = resident_slot(srv, *job);
+        int chosen = rw;
+        if (chosen < 0)
+            for (size_t w = 0; w < srv->workers.size(); w++)
+                if (!srv->workers[w].has_job) {
+                    chosen = (int)w;
+                    break;
+                }
+        Worker &wk = srv->workers[chosen];
+        wk.job = job;
+        wk.has_job = true;
+        wk.hit = rw >= 0;
+        if (rw < 0) srv->in_use += job->bytes;
         srv->cv_work.notify_all();
     }
 }
@@ -212,8 +394,9 @@ int grmp_server_create(int device, size_t hbm_budget_bytes, int nslots, grmp_ser
 
 int grmp_server_request_bytes(const grmp_request *q, size_t *bytes) {
     if (!q || !bytes) return GRMP_ERR_INVALID_ARG;
-    if ((q->dim != 2 && q->dim != 3) || q->nverts <= 0 || q->ncells <= 0 || q->ndofs <= 0) return GRMP_ERR_INVALID_ARG;
+    if ((q->dim != 2 && q->dim != 3) || q->nverts <= 0 || q->ncells <= 0 || q->ndofs < 0) return GRMP_ERR_INVALID_ARG;
     if (grmp_fe_ldofs(q->fe_kind, q->dim, q->ncomponents) <= 0) return GRMP_ERR_UNSUPPORTED;
+    if (q->ndofs == 0 && q->fe_kind != GRMP_FE_H1P1 && q->fe_kind != GRMP_FE_H1P2) return GRMP_ERR_INVALID_ARG;
     Request r;
     r.dim = q->dim;
     r.fe = q->fe_kind;
@@ -226,11 +409,13 @@ int grmp_server_request_bytes(const grmp_request *q, size_t *bytes) {
 }
 
 int grmp_server_submit(grmp_server srv, const grmp_request *q, int64_t *id) {
-    if (!srv || !q || !id || !q->coords || !q->cells || !q->celldofs || q->nterms <= 0 || q->nterms > GRMP_MAX_TERMS ||
-        !q->terms)
+    if (!srv || !q || !id || !q->coords || !q->cells || q->nterms <= 0 || q->nterms > GRMP_MAX_TERMS || !q->terms)
         return GRMP_ERR_INVALID_ARG;
-    if ((q->dim != 2 && q->dim != 3) || q->nverts <= 0 || q->ncells <= 0 || q->ndofs <= 0 || q->nfixed < 0)
+    if ((q->dim != 2 && q->dim != 3) || q->nverts <= 0 || q->ncells <= 0 || q->nfixed < -1)
         return GRMP_ERR_INVALID_ARG;
+    if (q->celldofs ? q->ndofs <= 0 : (q->fe_kind != GRMP_FE_H1P1 && q->fe_kind != GRMP_FE_H1P2))
+        return GRMP_ERR_INVALID_ARG;   // a device-built DoF map: H1P1 / H1P2
+    if (q->nfixed > 0 && !q->fixed) return GRMP_ERR_INVALID_ARG;
     int ld = grmp_fe_ldofs(q->fe_kind, q->dim, q->ncomponents);
     if (ld <= 0) return GRMP_ERR_UNSUPPORTED;
     auto r = std::make_shared<Request>();
@@ -242,8 +427,29 @@ int grmp_server_submit(grmp_server srv, const grmp_request *q, int64_t *id) {
     r->ndofs = q->ndofs;
     r->coords.assign(q->coords, q->coords + (size_t)q->nverts * q->dim);
     r->cells.assign(q->cells, q->cells + (size_t)q->ncells * (q->dim + 1));
-    r->celldofs.assign(q->celldofs, q->celldofs + (size_t)q->ncells * ld);
-    if (q->nfixed) r->fixed.assign(q->fixed, q->fixed + q->nfixed);
+    r->device_dofmap = q->celldofs == nullptr;
+    if (q->celldofs) r->celldofs.assign(q->celldofs, q->celldofs + (size_t)q->ncells * ld);
+    else r->ndofs = 0;
+    r->all_boundary = q->nfixed == -1;
+    if (q->nfixed > 0) r->fixed.assign(q->fixed, q->fixed + q->nfixed);
+    r->key = q->mesh_key;
+    // operator structure: the pattern depends on it (and on the mesh / element the key stands for)
+    uint64_t sig = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { sig = (sig ^ v) * 1099511628211ull; };
+    mix((uint64_t)q->dim);
+    mix((uint64_t)q->fe_kind);
+    mix((uint64_t)q->ncomponents);
+    mix((uint64_t)q->nverts);
+    mix((uint64_t)q->ncells);
+    mix((uint64_t)(q->celldofs != nullptr));
+    mix((uint64_t)q->ndofs);
+    mix((uint64_t)q->nterms);
+    for (int i = 0; i < q->nterms; i++) {
+        mix((uint64_t)q->terms[i].op_kind);
+        mix((uint64_t)q->terms[i].symmetric);
+        mix((uint64_t)q->terms[i].bonus_quadorder);
+    }
+    r->sig = sig;
     r->terms.assign(q->terms, q->terms + q->nterms);
     r->term_coef.resize(q->nterms);
     for (int i = 0; i < q->nterms; i++) {
@@ -283,8 +489,9 @@ int grmp_server_wait(grmp_server srv, int64_t id, double timeout_s, double *x_ou
     } else {
         srv->cv_done.wait(lk, pred);
     }
-    if (x_out && !r->x.empty()) std::memcpy(x_out, r->x.data(), r->x.size() * sizeof(double));
     if (stats) *stats = r->stats;
+    if (!x_out) return r->stats.status;   // a query: the result stays for a later wait
+    if (!r->x.empty()) std::memcpy(x_out, r->x.data(), r->x.size() * sizeof(double));
     srv->all.erase(it);
     return r->stats.status;
 }
@@ -300,7 +507,11 @@ int grmp_server_destroy(grmp_server srv) {
     if (srv->admitter.joinable()) srv->admitter.join();
     for (auto &w : srv->workers)
         if (w.th.joinable()) w.th.join();
-    for (auto &w : srv->workers) grmp_destroy_context(w.ctx);
+    for (auto &w : srv->workers) {
+        for (auto &e : w.cache) destroy_resident(e);
+        w.cache.clear();
+        grmp_destroy_context(w.ctx);
+    }
     delete srv;
     return GRMP_OK;
 }

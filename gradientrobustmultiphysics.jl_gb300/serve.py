@@ -9,6 +9,12 @@ boundary.  Requests are served by the library's serving engine
 (grmp_server_*): slots with their own streams, admission by an HBM budget,
 mixed-precision solves to a relative residual that gives <= 1e-10 relative
 error against FP64.
+
+Pooled workload (make_pooled_workload): the requests draw their mesh from a
+small pool and vary the coefficients and right-hand side, like the
+reference's parameter sweeps and time steps on one grid; with a mesh key the
+server keeps each mesh's DoF map, pattern and solver workspace resident and
+such requests run only assembly and solve.
 """
 from __future__ import annotations
 
@@ -39,6 +45,8 @@ class ServeRequest:
     fixed: np.ndarray
     arrival_s: float = 0.0
     meta: dict = field(default_factory=dict)
+    mesh_key: int = 0            # non-zero: data stay resident in the server under this key
+    device_dofmap: bool = False  # DoF map and boundary DoFs built on the device (no host arrays)
 
     @property
     def ndofs(self) -> int:
@@ -61,6 +69,8 @@ def mesh_size_for(dofs: float, dim: int, order: int) -> int:
     return max(2, int(round((side - 1) / order)))
 
 
+STATUS_TIMEOUT = 7   # GRMP_ERR_TIMEOUT
+
 _grid_cache: dict = {}
 _space_cache: dict = {}
 
@@ -82,6 +92,45 @@ def build_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=2e6, dim=None
     alpha = float(rng.uniform(0, 10)) if rng.random() < 0.5 else 0.0
     amp, k = fourier_modes(rng, dim)
     return ServeRequest(dim, order, n, FES, kappa, alpha, amp, k, FES.boundary_dofs())
+
+
+def mesh_key(dim: int, n: int, order: int) -> int:
+    """Residency key of the unit square / Kuhn cube grid with n subdivisions and element order."""
+    return (dim << 40) | (order << 32) | n
+
+
+def make_pooled_workload(nrequests: int, nmeshes: int = 8, seed: int = 0, mean_interarrival_s: float = 0.05,
+                         dofs_min=1e3, dofs_max=2e6, device_dofmap: bool = False):
+    """Requests on a pool of `nmeshes` problems (dimension, element, size and
+    whether a reaction term is present drawn as in make_workload), with fresh
+    kappa, reaction coefficient and right-hand side per request and the pool
+    entry's residency key."""
+    rng = np.random.default_rng(seed)
+    pool = []
+    for _ in range(nmeshes):
+        dim, order = int(rng.integers(2, 4)), int(rng.integers(1, 3))
+        target = math.exp(rng.uniform(math.log(dofs_min), math.log(dofs_max)))
+        pool.append((dim, order, mesh_size_for(target, dim, order), bool(rng.random() < 0.5)))
+    reqs, t = [], 0.0
+    for _ in range(nrequests):
+        dim, order, n, reaction = pool[int(rng.integers(0, nmeshes))]
+        key = (dim, n)
+        if key not in _grid_cache:
+            _grid_cache[key] = grid_unitsquare(n) if dim == 2 else grid_unitcube_kuhn(n)
+        g = _grid_cache[key]
+        skey = (dim, n, order)
+        if skey not in _space_cache:
+            _space_cache[skey] = FESpace(H1P1(1) if order == 1 else H1P2(1, dim), g)
+        FES = _space_cache[skey]
+        kappa = np.exp(rng.standard_normal(g.ncells))
+        alpha = float(rng.uniform(0.1, 10)) if reaction else 0.0
+        amp, k = fourier_modes(rng, dim)
+        r = ServeRequest(dim, order, n, FES, kappa, alpha, amp, k, FES.boundary_dofs(),
+                         mesh_key=mesh_key(dim, n, order), device_dofmap=device_dofmap)
+        t += float(rng.exponential(mean_interarrival_s))
+        r.arrival_s = t
+        reqs.append(r)
+    return reqs
 
 
 def make_workload(nrequests: int, seed: int = 0, mean_interarrival_s: float = 0.05, dofs_max=2e6):
@@ -114,14 +163,22 @@ class Server:
             raise L.GrmpError(rc, "grmp_server_submit")
         return rid.value
 
-    def wait(self, rid: int, ndofs: int, timeout_s: float = -1.0):
-        x = np.empty(ndofs)
+    def wait(self, rid: int, ndofs: int | None = None, timeout_s: float = -1.0):
+        """(status, solution, stats) of request rid; ndofs None asks the server
+        for the solution's length first (a device-built DoF map)."""
         st = L.RequestStats()
+        if ndofs is None:
+            rc = self.lib.grmp_server_wait(self.h, rid, timeout_s, None, ctypes.byref(st))
+            if rc == STATUS_TIMEOUT:
+                return rc, None, None
+            ndofs = st.ndofs   # 0 for a request that failed before its DoF map
+        x = np.empty(ndofs)
         rc = self.lib.grmp_server_wait(self.h, rid, timeout_s, x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                        ctypes.byref(st))
         return rc, x, {"status": st.status, "slot": st.slot, "iterations": st.iterations,
                        "outer": st.outer_iterations, "relres": st.final_relres, "queue_ms": st.queue_ms,
-                       "run_ms": st.run_ms, "latency_ms": st.latency_ms, "solve_ms": st.solve_ms}
+                       "run_ms": st.run_ms, "latency_ms": st.latency_ms, "solve_ms": st.solve_ms,
+                       "ndofs": st.ndofs, "resident": st.resident}
 
     def close(self):
         if self.h:
@@ -164,8 +221,12 @@ def make_request(r: ServeRequest, mode: str = "mixed", reltol: float = 1e-11):
     q.cells = arr(g.cells, np.int32)
     q.fe_kind = FES.FEType.kind
     q.ncomponents = FES.FEType.ncomponents
-    q.ndofs = FES.ndofs
-    q.celldofs = arr(FES.celldofs, np.int32)
+    if r.device_dofmap:
+        q.ndofs = 0
+        q.celldofs = None
+    else:
+        q.ndofs = FES.ndofs
+        q.celldofs = arr(FES.celldofs, np.int32)
     ops = r.operators()
     terms = (L.BilinearTerm * len(ops))()
     for i, o in enumerate(ops):
@@ -176,10 +237,15 @@ def make_request(r: ServeRequest, mode: str = "mixed", reltol: float = 1e-11):
     lf = r.rhs()
     q.rhs = lf.rhs()
     keep.append(lf)
-    q.nfixed = r.fixed.size
-    q.fixed = arr(r.fixed, np.int32)
+    if r.device_dofmap:
+        q.nfixed = -1
+        q.fixed = None
+    else:
+        q.nfixed = r.fixed.size
+        q.fixed = arr(r.fixed, np.int32)
     s = api.GB300PCG(mode=mode, reltol=reltol, abstol=0.0)
     q.solve = s.params()
+    q.mesh_key = r.mesh_key
     return q, keep
 
 
@@ -199,7 +265,7 @@ def run(reqs, nslots: int = 4, hbm_budget_bytes: int = 150 << 30, mode: str = "m
             ids.append(srv.submit(r, mode, reltol))
         xs, sts = [], []
         for r, rid in zip(reqs, ids):
-            rc, x, st = srv.wait(rid, r.ndofs)
+            rc, x, st = srv.wait(rid, None if r.device_dofmap else r.ndofs)
             st["rc"] = rc
             xs.append(x)
             sts.append(st)
@@ -215,4 +281,5 @@ def summarize(reqs, sts, makespan):
     return {"requests": len(reqs), "dofs": int(dofs), "makespan_s": makespan, "dof_per_s": dofs / makespan,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(lat.max())},
-            "failed": int(sum(1 for s in sts if s["rc"] != 0))}
+            "failed": int(sum(1 for s in sts if s["rc"] != 0)),
+            "resident_hits": int(sum(1 for s in sts if s.get("resident")))}

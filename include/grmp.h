@@ -211,7 +211,9 @@ int grmp_matrix_info(grmp_matrix A, int32_t *nrows, int64_t *nnz, int32_t *max_r
 /* Assemble the sum of `terms` into the matrix values in the given precision
  * (FP64 values and/or FP32 values are held separately in the handle;
  * GRMP_FP64_FP32 fills both from one walk of the incidence lists, the FP32
- * values computed in FP32 arithmetic exactly as a GRMP_FP32 assembly would).
+ * values computed in FP32 arithmetic exactly as a GRMP_FP32 assembly would;
+ * an assembly in one precision leaves the other precision's values as they
+ * were, so a MIXED solve after new coefficients wants GRMP_FP64_FP32).
  * Stands in for assemble!(A::FEMatrixBlock, AP::AssemblyPattern{<:APT_BilinearForm})
  * (src/assemblypatterns/bilinearform.jl:92-400).  Deterministic: each
  * nonzero is the sum of its cell contributions in ascending cell order. */
@@ -485,19 +487,34 @@ typedef struct grmp_server_s *grmp_server;
 typedef struct {
     int dim;
     int32_t nverts;
-    const double *coords;       /* [nverts][dim]          */
+    const double *coords;       /* [nverts][dim]                                                  */
     int32_t ncells;
-    const int32_t *cells;       /* [ncells][dim+1]        */
+    const int32_t *cells;       /* [ncells][dim+1]                                                */
     int fe_kind;
     int ncomponents;
-    int32_t ndofs;
-    const int32_t *celldofs;    /* [ncells][ndofs4cell]   */
+    int32_t ndofs;              /* 0 with celldofs == NULL: counted on the device                 */
+    const int32_t *celldofs;    /* [ncells][ndofs4cell], or NULL: the DoF map is built on the
+                                   device from the mesh (H1P1 / H1P2, grmp_space_create_on_device) */
     int nterms;
     const grmp_bilinear_term *terms;
-    grmp_rhs rhs;               /* cell_group not allowed */
-    int32_t nfixed;
-    const int32_t *fixed;       /* homogeneous Dirichlet DoFs (eliminated) */
+    grmp_rhs rhs;               /* cell_group not allowed                                          */
+    int32_t nfixed;             /* -1: every boundary DoF, found on the device                     */
+    const int32_t *fixed;       /* homogeneous Dirichlet DoFs (eliminated)                         */
     grmp_solve_params solve;
+    uint64_t mesh_key;          /* 0: nothing stays on the device after the request.  Otherwise the
+                                   request's mesh, DoF map, sparsity pattern, solver workspace and
+                                   vectors stay resident in the slot that ran it, and a later
+                                   request with the same key and operator structure (term kinds,
+                                   symmetry, quadrature bonus) reuses them: only its coefficients,
+                                   right-hand side and solve run.  A resident pattern is built
+                                   with unit factors and no cell coefficients, so that it holds
+                                   every later coefficient field (as the reference's refill of a
+                                   kept matrix, src/fematrix.jl:220-232); a one-off request's
+                                   pattern drops its own exact zeros.  The caller promises the same
+                                   mesh and element under one key (the reference reuses a solver
+                                   cache the same way, src/solvers.jl:906-911).  Resident data
+                                   count against the budget; the least recently used entries of
+                                   idle slots are dropped when a request would not fit.           */
 } grmp_request;
 
 typedef struct {
@@ -509,6 +526,8 @@ typedef struct {
     double run_ms;              /* admission -> result                       */
     double latency_ms;          /* submit -> result                          */
     double solve_ms;            /* device time of the solve                  */
+    int32_t ndofs;              /* DoFs of the solution (x_out's length)     */
+    int32_t resident;           /* 1: the request reused resident data       */
 } grmp_request_stats;
 
 /* A serving loop with `nslots` concurrent slots (one stream each) on device
@@ -524,7 +543,8 @@ int grmp_server_request_bytes(const grmp_request *q, size_t *bytes);
  * can never fit. */
 int grmp_server_submit(grmp_server srv, const grmp_request *req, int64_t *id);
 /* Wait for a request (timeout_s < 0: forever); x_out [ndofs] receives the
- * solution.  Returns the request's status (GRMP_ERR_TIMEOUT if still
+ * solution (with a device-built DoF map, query stats->ndofs first: x_out may
+ * be NULL).  Returns the request's status (GRMP_ERR_TIMEOUT if still
  * running after timeout_s; it can be waited for again). */
 int grmp_server_wait(grmp_server srv, int64_t id, double timeout_s, double *x_out, grmp_request_stats *stats);
 /* Stop the workers (running requests finish first) and free the server. */

@@ -67,3 +67,69 @@ def test_budget_serialises_and_refuses(G):
             tiny.close()
     finally:
         srv.close()
+
+
+def _cold(reqs):
+    import dataclasses
+    return [dataclasses.replace(r, mesh_key=0, device_dofmap=False) for r in reqs]
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_resident_results_match_cold_requests(G):
+    """Requests on a pool of three meshes: with residency most of them reuse
+    a slot's mesh, DoF map, pattern and solver workspace.  A resident pattern
+    is built with unit coefficients (it serves every later coefficient field),
+    so it may hold a few stored entries whose cold pattern drops as exact
+    zeros of that request's coefficients: the solutions agree with the cold
+    requests' to the serving tolerance, and a replay of the same sequence on
+    one slot is bit-identical."""
+    from grmp_gb300 import serve as SV
+    reqs = SV.make_pooled_workload(12, nmeshes=3, seed=11, dofs_max=5e4)
+    xs_res, sts_res, _ = SV.run(reqs, nslots=2, realtime=False)
+    assert all(s["rc"] == 0 for s in sts_res), [s["rc"] for s in sts_res]
+    assert sum(s["resident"] for s in sts_res) >= 12 - 2 * 3   # at most one cold start per mesh and slot
+    xs_cold, sts_cold, _ = SV.run(_cold(reqs), nslots=2, realtime=False)
+    assert not any(s["resident"] for s in sts_cold)
+    for xr, xc in zip(xs_res, xs_cold):
+        assert _rel(xr, xc) <= 1e-10
+    xa, sa, _ = SV.run(reqs, nslots=1, realtime=False)
+    xb, sb, _ = SV.run(reqs, nslots=1, realtime=False)
+    assert [s["resident"] for s in sa] == [s["resident"] for s in sb]
+    for a, b in zip(xa, xb):
+        assert np.array_equal(a, b)
+
+
+def test_device_dofmap_requests_equal_host_dofmap(G):
+    """Requests without CellDofs and Dirichlet lists (both built on the
+    device) give the host-numbered requests' solutions bit for bit, and with
+    residency the same to the serving tolerance."""
+    import dataclasses
+    from grmp_gb300 import serve as SV
+    reqs = SV.make_pooled_workload(8, nmeshes=4, seed=12, dofs_max=4e4, device_dofmap=True)
+    one_off = [dataclasses.replace(r, mesh_key=0) for r in reqs]
+    xs_dev, sts_dev, _ = SV.run(one_off, nslots=2, realtime=False)
+    assert all(s["rc"] == 0 for s in sts_dev)
+    xs_host, _, _ = SV.run(_cold(reqs), nslots=2, realtime=False)
+    for r, xd, xh, st in zip(reqs, xs_dev, xs_host, sts_dev):
+        assert st["ndofs"] == r.ndofs
+        assert np.array_equal(xd, xh)
+    xs_res, sts_res, _ = SV.run(reqs, nslots=2, realtime=False)
+    assert all(s["rc"] == 0 for s in sts_res) and any(s["resident"] for s in sts_res)
+    for xr, xh in zip(xs_res, xs_host):
+        assert _rel(xr, xh) <= 1e-10
+
+
+def test_resident_entries_are_evicted_under_budget(G):
+    """A budget that holds about two requests: resident entries of idle slots
+    are dropped as new meshes arrive, and every request completes."""
+    from grmp_gb300 import serve as SV
+    reqs = SV.make_pooled_workload(10, nmeshes=5, seed=13, dofs_max=3e4)
+    budget = int(2.2 * max(SV.estimate_bytes(r) for r in reqs))
+    xs, sts, _ = SV.run(reqs, nslots=2, hbm_budget_bytes=budget, realtime=False)
+    assert all(s["rc"] == 0 for s in sts), [s["rc"] for s in sts]
+    xs_cold, _, _ = SV.run(_cold(reqs), nslots=1, realtime=False)
+    for a, b in zip(xs, xs_cold):
+        assert _rel(a, b) <= 1e-10
