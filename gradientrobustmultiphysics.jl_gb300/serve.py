@@ -75,7 +75,8 @@ _grid_cache: dict = {}
 _space_cache: dict = {}
 
 
-def build_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=2e6, dim=None, order=None) -> ServeRequest:
+def build_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=2e6, dim=None, order=None,
+                  resident: bool = True) -> ServeRequest:
     dim = int(rng.integers(2, 4)) if dim is None else dim
     order = int(rng.integers(1, 3)) if order is None else order
     target = math.exp(rng.uniform(math.log(dofs_min), math.log(dofs_max)))
@@ -91,7 +92,8 @@ def build_request(rng: np.random.Generator, dofs_min=1e3, dofs_max=2e6, dim=None
     kappa = np.exp(rng.standard_normal(g.ncells))
     alpha = float(rng.uniform(0, 10)) if rng.random() < 0.5 else 0.0
     amp, k = fourier_modes(rng, dim)
-    return ServeRequest(dim, order, n, FES, kappa, alpha, amp, k, FES.boundary_dofs())
+    return ServeRequest(dim, order, n, FES, kappa, alpha, amp, k, FES.boundary_dofs(),
+                        mesh_key=mesh_key(dim, n, order) if resident else 0)
 
 
 def mesh_key(dim: int, n: int, order: int) -> int:
@@ -133,12 +135,15 @@ def make_pooled_workload(nrequests: int, nmeshes: int = 8, seed: int = 0, mean_i
     return reqs
 
 
-def make_workload(nrequests: int, seed: int = 0, mean_interarrival_s: float = 0.05, dofs_max=2e6):
-    """Requests with Poisson-process arrival times (exponential gaps)."""
+def make_workload(nrequests: int, seed: int = 0, mean_interarrival_s: float = 0.05, dofs_max=2e6,
+                  resident: bool = True):
+    """Requests with Poisson-process arrival times (exponential gaps); with
+    `resident` each carries the residency key of its grid and element, so
+    requests that land on an already served mesh size reuse its device data."""
     rng = np.random.default_rng(seed)
     reqs, t = [], 0.0
     for _ in range(nrequests):
-        r = build_request(rng, dofs_max=dofs_max)
+        r = build_request(rng, dofs_max=dofs_max, resident=resident)
         t += float(rng.exponential(mean_interarrival_s))
         r.arrival_s = t
         reqs.append(r)
