@@ -19,7 +19,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib as L
-from .fespace import FESpace, FE_H1BR
+from .fespace import FESpace, FE_H1BR, FE_H1P2B
 from .mesh import SimplexMesh
 
 # operator tags of src/functionoperators.jl
@@ -29,6 +29,8 @@ SymmetricGradient = "SymmetricGradient"
 Divergence = "Divergence"
 ReconstructionIdentity = "ReconstructionIdentity"          # ReconstructionIdentity{HDIVRT0{d}}
 ReconstructionIdentityBDM1 = "ReconstructionIdentity{HDIVBDM1}"   # ReconstructionIdentity{HDIVBDM1{d}}
+ReconstructionIdentityRT1 = "ReconstructionIdentity{HDIVRT1}"     # ReconstructionIdentity{HDIVRT1{2}} (H1P2B)
+ReconstructionIdentityBDM2 = "ReconstructionIdentity{HDIVBDM2}"   # ReconstructionIdentity{HDIVBDM2{2}} (H1P2B)
 ReconstructionDivergence = "ReconstructionDivergence"
 
 APT_BilinearForm = "APT_BilinearForm"
@@ -106,7 +108,7 @@ class GB300Context:
         key = id(FES)
         ent = self._spaces.get(key)
         if ent is None or ent[0] is not FES:
-            mh = self.mesh(FES.xgrid, with_faces=(FES.FEType.kind == FE_H1BR))
+            mh = self.mesh(FES.xgrid, with_faces=(FES.FEType.kind in (FE_H1BR, FE_H1P2B)))
             h = ctypes.c_void_p()
             cd = np.ascontiguousarray(FES.celldofs, dtype=np.int32)
             self.check(self.lib.grmp_space_create(mh, FES.FEType.kind, FES.FEType.ncomponents, _ip(cd), FES.ndofs,
@@ -319,7 +321,8 @@ class LinearFormOp:
         r.nparams = self._p.size
         r.factor = float(self.factor)
         r.bonus_quadorder = int(self.f.bonus_quadorder)
-        r.test_operator = {ReconstructionIdentity: 1, ReconstructionIdentityBDM1: 2}.get(self.test_operator, 0)
+        r.test_operator = {ReconstructionIdentity: 1, ReconstructionIdentityBDM1: 2, ReconstructionIdentityRT1: 3,
+                           ReconstructionIdentityBDM2: 4}.get(self.test_operator, 0)
         return r
 
 

@@ -207,12 +207,13 @@ int grmp_space_create(grmp_mesh mesh, int fe_kind, int ncomponents, const int32_
     bool ok = (fe_kind == GRMP_FE_H1P1 && ncomponents >= 1 && ncomponents <= 3) ||
               (fe_kind == GRMP_FE_H1P2 && ncomponents >= 1 && ncomponents <= 3) ||
               (fe_kind == GRMP_FE_H1BR && ncomponents == dim) ||
+              (fe_kind == GRMP_FE_H1P2B && ncomponents == 2 && dim == 2) ||
               (fe_kind == GRMP_FE_L2P0 && ncomponents >= 1 && ncomponents <= 3);
     if (!ok)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "space: element %d with %d components in %dD is not built", fe_kind,
                          ncomponents, dim);
-    if (fe_kind == GRMP_FE_H1BR && mesh->nfaces == 0)
-        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "space: H1BR needs grmp_mesh_set_faces first");
+    if ((fe_kind == GRMP_FE_H1BR || fe_kind == GRMP_FE_H1P2B) && mesh->nfaces == 0)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "space: H1BR / H1P2B need grmp_mesh_set_faces first");
     int ldofs = grmp_fe_ldofs(fe_kind, dim, ncomponents);
     if (ldofs <= 0 || ldofs > GRMP_MAX_LDOFS) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "space: %d local dofs", ldofs);
     size_t n = (size_t)mesh->ncells * ldofs;

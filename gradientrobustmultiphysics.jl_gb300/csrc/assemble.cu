@@ -571,6 +571,7 @@ __global__ void k_dirichlet_rows(int32_t nrows, const int32_t *rowptr, const int
 // ---------------------------------------------------------------------- bilinear
 int grmp_br_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
 int grmp_br_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b);
+int grmp_p2b_rhs(grmp_space s, const grmp_rhs *rhs, grmp_vector b);
 
 int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision) {
     grmp_space s = A->space;
@@ -674,6 +675,7 @@ int grmp_assemble_linear_impl(grmp_space s, const grmp_rhs *rhs, grmp_vector b) 
                              "H1BR right-hand sides use a reconstruction test operator (1 = RT0, 2 = BDM1)");
         return grmp_br_rhs(s, rhs, b);
     }
+    if (s->fe == GRMP_FE_H1P2B) return grmp_p2b_rhs(s, rhs, b);
     if (rhs->test_operator != 0) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "reconstruction test operator needs H1BR");
     if (s->fe != GRMP_FE_H1P1 && s->fe != GRMP_FE_H1P2)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "linear form on element %d", s->fe);

@@ -372,7 +372,8 @@ int grmp_prepare_terms(grmp_space s, int nterms, const grmp_bilinear_term *terms
     grmp_context ctx = s->mesh->ctx;
     int dim = s->mesh->dim;
     if (s->fe != GRMP_FE_H1P1 && s->fe != GRMP_FE_H1P2)
-        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "bilinear terms on element %d use the dedicated BR path", s->fe);
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED,
+                         "bilinear terms on element %d are not built here (H1BR has its own path)", s->fe);
     td->n = nterms;
     for (int i = 0; i < nterms; i++) {
         const grmp_bilinear_term &t = terms[i];

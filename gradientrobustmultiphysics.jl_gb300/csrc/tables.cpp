@@ -293,6 +293,9 @@ int grmp_fe_polyorder(int fe, int dim) {
         case GRMP_FE_L2P0: return 0;
         case GRMP_FE_HDIVRT0: return 1;
         case GRMP_FE_HDIVBDM1: return 1;
+        case GRMP_FE_H1P2B: return dim == 2 ? 3 : -1;   // src/fedefs/h1_p2b.jl:24-26
+        case GRMP_FE_HDIVRT1: return 2;
+        case GRMP_FE_HDIVBDM2: return 2;
     }
     return -1;
 }
@@ -303,6 +306,7 @@ int grmp_fe_nb(int fe, int dim) {
         case GRMP_FE_H1P2: return dim == 2 ? 6 : 10;
         case GRMP_FE_H1BR: return dim == 2 ? 6 : 8;
         case GRMP_FE_L2P0: return 1;
+        case GRMP_FE_H1P2B: return dim == 2 ? 7 : 0;
     }
     return 0;
 }
@@ -314,6 +318,7 @@ int grmp_fe_ldofs(int fe, int dim, int ncomp) {
         case GRMP_FE_H1BR: return dim == 2 ? 9 : 16;
         case GRMP_FE_L2P0: return ncomp;
         case GRMP_FE_HDIVRT0: return dim + 1;
+        case GRMP_FE_H1P2B: return dim == 2 ? 7 * ncomp : 0;
     }
     return 0;
 }

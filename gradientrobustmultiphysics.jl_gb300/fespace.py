@@ -29,6 +29,9 @@ FE_H1BR = 3
 FE_HDIVRT0 = 4
 FE_HDIVBDM1 = 5
 FE_L2P0 = 6
+FE_H1P2B = 7
+FE_HDIVRT1 = 8
+FE_HDIVBDM2 = 9
 
 
 @dataclass(frozen=True)
@@ -51,6 +54,22 @@ def H1P2(ncomponents: int = 1, edim: int = 2) -> FEType:
 
 def H1BR(edim: int = 2) -> FEType:
     return FEType(FE_H1BR, edim, f"H1BR{{{edim}}}")
+
+
+def H1P2B(ncomponents: int = 2, edim: int = 2) -> FEType:
+    """P2 plus a cell bubble per component (src/fedefs/h1_p2b.jl; 2D vector
+    fields, the reference's H1P2B{2,2})."""
+    if ncomponents != 2 or edim != 2:
+        raise ValueError("H1P2B is built for H1P2B{2,2}")
+    return FEType(FE_H1P2B, ncomponents, f"H1P2B{{{ncomponents},{edim}}}")
+
+
+def HDIVRT1(edim: int = 2) -> FEType:
+    return FEType(FE_HDIVRT1, edim, f"HDIVRT1{{{edim}}}")
+
+
+def HDIVBDM2(edim: int = 2) -> FEType:
+    return FEType(FE_HDIVBDM2, edim, f"HDIVBDM2{{{edim}}}")
 
 
 def L2P0(ncomponents: int = 1) -> FEType:
@@ -79,6 +98,10 @@ def polynomial_order(fe: FEType, dim: int) -> int:
         return 1
     if fe.kind == FE_HDIVBDM1:
         return 1
+    if fe.kind == FE_H1P2B:
+        return 3                             # src/fedefs/h1_p2b.jl:24-26
+    if fe.kind in (FE_HDIVRT1, FE_HDIVBDM2):
+        return 2
     raise ValueError(fe)
 
 
@@ -121,6 +144,18 @@ class FESpace:
             per = [g.cells.astype(np.int64) + c * nn for c in range(nc)]
             per.append(cfaces.astype(np.int64) + nc * nn)
             self.celldofs = np.concatenate(per, axis=1).astype(np.int32)
+        elif fe.kind == FE_H1P2B:
+            # "N1F1I1" per component: nodes, faces, then the cell bubble
+            fnodes, cfaces = g.faces()
+            self.coffset = nn + fnodes.shape[0] + g.ncells
+            self.ndofs = self.coffset * nc
+            per = []
+            for c in range(nc):
+                off = c * self.coffset
+                per.append(g.cells.astype(np.int64) + off)
+                per.append(cfaces.astype(np.int64) + off + nn)
+                per.append((np.arange(g.ncells, dtype=np.int64) + off + nn + fnodes.shape[0])[:, None])
+            self.celldofs = np.concatenate(per, axis=1).astype(np.int32)
         elif fe.kind == FE_L2P0:
             self.coffset = g.ncells
             self.ndofs = g.ncells * nc
@@ -150,10 +185,10 @@ class FESpace:
         fnodes = g.faces()[0][bf]                          # (nb, dim)
         nn = g.nverts
         out = []
-        if fe.kind in (FE_H1P1, FE_H1P2, FE_H1BR):
+        if fe.kind in (FE_H1P1, FE_H1P2, FE_H1BR, FE_H1P2B):
             for c in range(fe.ncomponents):
                 out.append(fnodes.ravel().astype(np.int64) + c * self.coffset)
-            if fe.kind == FE_H1P2:
+            if fe.kind in (FE_H1P2, FE_H1P2B):
                 if g.dim == 2:
                     for c in range(fe.ncomponents):
                         out.append(bf.astype(np.int64) + nn + c * self.coffset)

@@ -123,7 +123,11 @@ typedef enum {
     GRMP_FE_H1BR = 3,     /* src/fedefs/h1v_br.jl (2D and 3D)       */
     GRMP_FE_HDIVRT0 = 4,  /* reconstruction target only            */
     GRMP_FE_HDIVBDM1 = 5, /* reconstruction target only            */
-    GRMP_FE_L2P0 = 6      /* src/fedefs/l2_p0.jl                    */
+    GRMP_FE_L2P0 = 6,     /* src/fedefs/l2_p0.jl                    */
+    GRMP_FE_H1P2B = 7,    /* src/fedefs/h1_p2b.jl: H1P2B{2,2} (P2 + cell bubble, 2D vector);
+                             reconstructed right-hand sides only    */
+    GRMP_FE_HDIVRT1 = 8,  /* reconstruction target only (src/fedefs/hdiv_rt1.jl)  */
+    GRMP_FE_HDIVBDM2 = 9  /* reconstruction target only (src/fedefs/hdiv_bdm2.jl) */
 } grmp_fe_kind;
 
 /* FESpace{FEType}(xgrid) (src/finiteelements.jl:72-119) with the cell DoF
@@ -272,6 +276,9 @@ typedef struct {
     int bonus_quadorder;    /* DataFunction bonus_quadorder                          */
     int test_operator;      /* 0 = Identity; 1 = ReconstructionIdentity{HDIVRT0{d}};
                                2 = ReconstructionIdentity{HDIVBDM1{d}} (1, 2: H1BR only;
+                               3 = ReconstructionIdentity{HDIVRT1{2}},
+                               4 = ReconstructionIdentity{HDIVBDM2{2}} (3, 4: H1P2B only,
+                               src/reconstructions.jl:43-330, :405-469);
                                src/feevaluator_h1.jl:342-381, src/reconstructions.jl:351-535;
                                in 3D the BDM1 function matching the P1 normal-flux moments of
                                each face, which the reference's orientation-selected basis

@@ -1845,3 +1845,454 @@ void oracle_br_div(int ncells, const double *coords, const int *cells, const int
             for (int i = 0; i < 9; i++) b[dofs[i]] += lb[i] * vol;
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* H1P2B{2,2} with the RT1 / BDM2 reconstructions, 2D triangles              */
+/* ------------------------------------------------------------------------- */
+
+/* Local DoFs (src/fedefs/h1_p2b.jl:33 "N1F1I1", components blocked): 7k + s,
+ * s = 0-2 nodes, 3-5 faces (face f joins nodes f and f+1 mod 3), 6 the cell
+ * bubble.  Scalar basis on duals: the P2 functions of src/fedefs/h1_p2.jl:
+ * 134-144 and the bubble 60 (1-x-y) x y of src/fedefs/h1_p2b.jl:126-137. */
+static void p2b_basis_dual(double xi, double eta, dual o[7])
+{
+    dual x = dvar(xi, 0), y = dvar(eta, 1);
+    dual l = dsub(dcsub(1.0, x), y);
+    o[0] = dmul(dscale(2.0, l), dsubc(l, 0.5));
+    o[1] = dmul(dscale(2.0, x), dsubc(x, 0.5));
+    o[2] = dmul(dscale(2.0, y), dsubc(y, 0.5));
+    o[3] = dmul(dscale(4.0, l), x);
+    o[4] = dmul(dscale(4.0, x), y);
+    o[5] = dmul(dscale(4.0, y), l);
+    o[6] = dmul(dmul(dscale(60.0, dsub(dcsub(1.0, x), y)), x), y);
+}
+
+/* HDIVRT1{2} reference basis (src/fedefs/hdiv_rt1.jl:106-121): RT0 of face
+ * f at 2f, its linear-flux partner at 2f+1, interior functions 6, 7. */
+static void rt1_ref_basis(double x, double y, double o[8][2])
+{
+    o[0][0] = x; o[0][1] = y - 1;
+    o[2][0] = x; o[2][1] = y;
+    o[4][0] = x - 1; o[4][1] = y;
+    for (int k = 0; k < 2; k++) {
+        o[1][k] = -12 * (0.5 - x - y) * o[0][k];
+        o[3][k] = -(12 * (x - 0.5)) * o[2][k];
+        o[5][k] = -(12 * (y - 0.5)) * o[4][k];
+        o[6][k] = 12 * y * o[0][k];
+        o[7][k] = 12 * x * o[4][k];
+    }
+}
+
+/* HDIVBDM2{2} reference basis (src/fedefs/hdiv_bdm2.jl:171-194): per face f
+ * the RT0 function (3f), the linear BDM1 function (3f+1) and the quadratic
+ * one (3f+2); interior functions 9-11. */
+static void bdm2_ref_basis(double x, double y, double o[12][2])
+{
+    const double l = 1 - x - y;
+    o[0][0] = x; o[0][1] = y - 1;
+    o[3][0] = x; o[3][1] = y;
+    o[6][0] = x - 1; o[6][1] = y;
+    o[1][0] = 6 * x; o[1][1] = 6 - 12 * x - 6 * y;
+    o[4][0] = -6 * x; o[4][1] = 6 * y;
+    o[7][0] = 6 * (x - 1) + 12 * y; o[7][1] = -6 * y;
+    for (int k = 0; k < 2; k++) {
+        o[2][k] = -15 * ((l - 0.5) * o[1][k] + o[0][k]);
+        o[5][k] = -15 * ((x - 0.5) * o[4][k] + o[3][k]);
+        o[8][k] = -15 * ((y - 0.5) * o[7][k] + o[6][k]);
+        o[9][k] = y * o[1][k];
+        o[10][k] = l * o[4][k];
+        o[11][k] = x * o[7][k];
+    }
+}
+
+/* Number of reconstruction functions and the element coefficients (face
+ * signs): RT1 (hdiv_rt1.jl:124-135) signs the RT0 functions 2f, BDM2
+ * (hdiv_bdm2.jl:197-210) the functions 3f and 3f+2. */
+static int p2b_recon_target(int recon, const double sg[3], double coef[12])
+{
+    const int nr = recon == 4 ? 12 : 8;
+    for (int j = 0; j < nr; j++) coef[j] = 1.0;
+    for (int f = 0; f < 3; f++) {
+        if (recon == 4) { coef[3 * f] = sg[f]; coef[3 * f + 2] = sg[f]; }
+        else coef[2 * f] = sg[f];
+    }
+    return nr;
+}
+
+static void p2b_recon_basis(int recon, double x, double y, double o[12][2])
+{
+    if (recon == 4) bdm2_ref_basis(x, y, o);
+    else {
+        double t[8][2];
+        rt1_ref_basis(x, y, t);
+        for (int j = 0; j < 8; j++) { o[j][0] = t[j][0]; o[j][1] = t[j][1]; }
+    }
+}
+
+/* Face part of the reconstruction coefficients R[14][nr]
+ * (src/reconstructions.jl:405-469): for the two nodes n of face f and each
+ * component k, RT0 column (1/6)|F| n_k, linear column c_n |F| n_k s_f with
+ * c = (-1/12, 1/12), BDM2's quadratic column (1/90)|F| n_k; the face DoF
+ * gets (2/3)|F| n_k in the RT0 column and BDM2's quadratic column -(1/45)|F| n_k. */
+static void p2b_face_coeffs(int recon, const double fv[3], const double nrm[6], const double sg[3], double R[14][12])
+{
+    const double c[2] = {-1.0 / 12.0, 1.0 / 12.0};
+    const int w = recon == 4 ? 3 : 2;
+    memset(R, 0, sizeof(double) * 14 * 12);
+    for (int f = 0; f < 3; f++) {
+        const int nodes[2] = {f, (f + 1) % 3};
+        for (int n = 0; n < 2; n++)
+            for (int k = 0; k < 2; k++) {
+                R[7 * k + nodes[n]][w * f] = (1.0 / 6.0) * fv[f] * nrm[f * 2 + k];
+                R[7 * k + nodes[n]][w * f + 1] = c[n] * fv[f] * nrm[f * 2 + k] * sg[f];
+                if (recon == 4) R[7 * k + nodes[n]][w * f + 2] = (1.0 / 90.0) * fv[f] * nrm[f * 2 + k];
+            }
+        for (int k = 0; k < 2; k++) {
+            R[7 * k + 3 + f][w * f] = (2.0 / 3.0) * fv[f] * nrm[f * 2 + k];
+            if (recon == 4) R[7 * k + 3 + f][w * f + 2] = (-1.0 / 45.0) * fv[f] * nrm[f * 2 + k];
+        }
+    }
+}
+
+/* Interior RT1 coefficients (columns 6, 7; src/reconstructions.jl:43-161):
+ * the integrals of the face RT1 functions over the cell from closed forms in
+ * the vertices C, edge midpoints E and centroid M, the inverse of the 2x2
+ * integral matrix of the interior functions, and for every P2B function the
+ * interior pair that restores its cell integral (node functions 0, face
+ * functions |T|/3, bubble |T| in its own component). */
+static void p2b_rt1_interior(const double X[6], const double sg[3], double vol, double R[14][12])
+{
+    double M[2] = {0, 0}, E[2][3] = {{0, 0, 0}, {0, 0, 0}}, A[2][8];
+    for (int n = 0; n < 3; n++)
+        for (int k = 0; k < 2; k++) M[k] += X[n * 2 + k] / 3;
+    for (int f = 0; f < 3; f++)
+        for (int n = 0; n < 2; n++)
+            for (int k = 0; k < 2; k++) E[k][f] += X[((f + n) % 3) * 2 + k] / 2;
+    for (int k = 0; k < 2; k++) {
+        A[k][0] = (M[k] - X[2 * 2 + k]) / 2 * sg[0];
+        A[k][1] = X[1 * 2 + k] - E[k][1];
+        A[k][2] = (M[k] - X[0 * 2 + k]) / 2 * sg[1];
+        A[k][3] = X[2 * 2 + k] - E[k][2];
+        A[k][4] = (M[k] - X[1 * 2 + k]) / 2 * sg[2];
+        A[k][5] = X[0 * 2 + k] - E[k][0];
+    }
+    A[1][7] = (E[0][0] - X[2 * 2 + 0]);
+    A[1][6] = -(E[1][0] - X[2 * 2 + 1]);
+    A[0][7] = -(E[0][2] - X[1 * 2 + 0]);
+    A[0][6] = (E[1][2] - X[1 * 2 + 1]);
+    const double det = A[0][6] * A[1][7] - A[1][6] * A[0][7];
+    A[0][6] /= det; A[0][7] /= det; A[1][6] /= det; A[1][7] /= det;
+    for (int k = 0; k < 2; k++) {
+        for (int n = 0; n < 3; n++) {
+            for (int pass = 0; pass < 2; pass++) {   /* node function, then face function */
+                const int dof = 7 * k + n + 3 * pass;
+                double b[2] = {0, 0};
+                if (pass == 1) b[k] = vol / 3;
+                for (int c = 0; c < 2; c++)
+                    for (int j = 0; j < 6; j++) b[c] -= R[dof][j] * A[c][j];
+                for (int kk = 0; kk < 2; kk++) R[dof][6 + kk] = A[kk][6] * b[0] + A[kk][7] * b[1];
+            }
+        }
+        const int dof = 7 * k + 6;
+        double b[2] = {0, 0};
+        b[k] = vol;
+        for (int kk = 0; kk < 2; kk++) R[dof][6 + kk] = A[kk][6] * b[0] + A[kk][7] * b[1];
+    }
+}
+
+/* x = M^{-1} b for a 3x3 matrix: LU with partial pivoting (the factorisation
+ * lu() computes for a small dense matrix), then the two triangular solves. */
+static void p2b_lu3(double M[3][3], int piv[3])
+{
+    for (int j = 0; j < 3; j++) {
+        int p = j;
+        for (int i = j + 1; i < 3; i++)
+            if (fabs(M[i][j]) > fabs(M[p][j])) p = i;
+        piv[j] = p;
+        if (p != j)
+            for (int c = 0; c < 3; c++) { double t = M[j][c]; M[j][c] = M[p][c]; M[p][c] = t; }
+        for (int i = j + 1; i < 3; i++) {
+            M[i][j] /= M[j][j];
+            for (int c = j + 1; c < 3; c++) M[i][c] -= M[i][j] * M[j][c];
+        }
+    }
+}
+
+static void p2b_lu3_solve(const double M[3][3], const int piv[3], const double b[3], double x[3])
+{
+    double y[3] = {b[0], b[1], b[2]};
+    for (int j = 0; j < 3; j++)
+        if (piv[j] != j) { double t = y[j]; y[j] = y[piv[j]]; y[piv[j]] = t; }
+    for (int i = 1; i < 3; i++)
+        for (int j = 0; j < i; j++) y[i] -= M[i][j] * y[j];
+    for (int i = 2; i >= 0; i--) {
+        for (int j = i + 1; j < 3; j++) y[i] -= M[i][j] * y[j];
+        y[i] /= M[i][i];
+    }
+    x[0] = y[0]; x[1] = y[1]; x[2] = y[2];
+}
+
+/* Interior BDM2 coefficients (columns 9-11; src/reconstructions.jl:164-330):
+ * on the order-4 rule, the moments of the interior BDM2 functions, of the
+ * face BDM2 functions and of every P2B function against grad(P1 functions
+ * 1, 2) and curl(cell bubble), then per P2B function the 3x3 solve that makes
+ * the reconstruction keep those moments. */
+static void p2b_bdm2_interior(const double A[3][3], const double G[3][3], double det, double vol, const double sg[3],
+                              double R[14][12])
+{
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(2, 4, xref, w);
+    if (nq < 0) nq = -nq;
+    double coef[12];
+    p2b_recon_target(4, sg, coef);
+    double IMM[3][3] = {{0}}, IMMf[3][9] = {{0}};
+    double b1[OR_MAXQ][14][2], b2[OR_MAXQ][12][2], b3[2][2], b4[OR_MAXQ][2];
+    /* grad of the P1 functions 1 - x - y and x (constant) */
+    const double dp1[2][2] = {{-1, -1}, {1, 0}};
+    for (int a = 0; a < 2; a++)
+        for (int k = 0; k < 2; k++) {
+            double s = 0;
+            for (int j = 0; j < 2; j++) s += G[k][j] * dp1[a][j];
+            b3[a][k] = s;
+        }
+    for (int q = 0; q < nq; q++) {
+        const double xi = xref[3 * q], eta = xref[3 * q + 1];
+        dual o[7];
+        p2b_basis_dual(xi, eta, o);
+        for (int dof = 0; dof < 14; dof++) {
+            const int k = dof / 7, s = dof % 7;
+            b1[q][dof][k] = o[s].v;
+            b1[q][dof][1 - k] = 0.0;
+        }
+        double rb[12][2];
+        bdm2_ref_basis(xi, eta, rb);
+        for (int j = 0; j < 12; j++)
+            for (int k = 0; k < 2; k++) {
+                double s = 0;
+                for (int l = 0; l < 2; l++) s += A[k][l] * rb[j][l];
+                s *= coef[j] / det;
+                b2[q][j][k] = s;
+            }
+        /* CurlScalar of the bubble (src/feevaluator_h1.jl:270-285): (-d/dy, d/dx) */
+        double cu[2] = {0, 0};
+        for (int j = 0; j < 2; j++) {
+            cu[0] -= G[1][j] * o[6].d[j];
+            cu[1] += G[0][j] * o[6].d[j];
+        }
+        b4[q][0] = cu[0];
+        b4[q][1] = cu[1];
+    }
+    for (int q = 0; q < nq; q++)
+        for (int dof = 0; dof < 3; dof++) {
+            for (int d2 = 0; d2 < 2; d2++) {
+                double t = 0;
+                for (int k = 0; k < 2; k++) t += b2[q][9 + dof][k] * b3[d2][k];
+                IMM[d2][dof] += t * vol * w[q];
+            }
+            double t = 0;
+            for (int k = 0; k < 2; k++) t += b2[q][9 + dof][k] * b4[q][k];
+            IMM[2][dof] += t * vol * w[q];
+            for (int d2 = 0; d2 < 9; d2++) {
+                double u = 0;
+                for (int k = 0; k < 2; k++) u += (dof < 2 ? b3[dof][k] : b4[q][k]) * b2[q][d2][k];
+                IMMf[dof][d2] += u * vol * w[q];
+            }
+        }
+    int piv[3];
+    p2b_lu3(IMM, piv);
+    for (int d1 = 0; d1 < 14; d1++) {
+        double lb[3] = {0, 0, 0};
+        for (int q = 0; q < nq; q++) {
+            for (int id = 0; id < 2; id++) {
+                double t = 0;
+                for (int k = 0; k < 2; k++) t += b1[q][d1][k] * b3[id][k];
+                lb[id] += t * vol * w[q];
+            }
+            double t = 0;
+            for (int k = 0; k < 2; k++) t += b1[q][d1][k] * b4[q][k];
+            lb[2] += t * vol * w[q];
+        }
+        for (int id = 0; id < 3; id++)
+            for (int d2 = 0; d2 < 9; d2++) lb[id] -= R[d1][d2] * IMMf[id][d2];
+        double x[3];
+        p2b_lu3_solve(IMM, piv, lb, x);
+        for (int id = 0; id < 3; id++) R[d1][9 + id] = x[id];
+    }
+}
+
+/* All reconstruction coefficients R[14][nr] of one cell (recon 3 = RT1,
+ * 4 = BDM2; get_rcoefficients!, src/reconstructions.jl:34-40). */
+static int p2b_coeffs(int recon, const double X[6], const double A[3][3], const double G[3][3], double det,
+                      double vol, const double fv[3], const double nrm[6], const double sg[3], double R[14][12])
+{
+    p2b_face_coeffs(recon, fv, nrm, sg, R);
+    if (recon == 4) p2b_bdm2_interior(A, G, det, vol, sg, R);
+    else p2b_rt1_interior(X, sg, vol, R);
+    return recon == 4 ? 12 : 8;
+}
+
+/* Coefficients of every cell: out[ncells][14][12] (columns past nr zero). */
+void oracle_p2b_coeffs(int ncells, const double *coords, const int *cells, const int *cell_faces,
+                       const double *fnormals, const double *fvolumes, const signed char *signs, int recon,
+                       double *out)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, NULL};
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], nrm[6], fv[3], sg[3], A[3][3], G[3][3], det, vol, R[14][12];
+        br_cell(&m, cell, X, nrm, fv, sg);
+        oracle_geometry(2, X, A, G, &det, &vol);
+        p2b_coeffs(recon, X, A, G, det, vol, fv, nrm, sg, R);
+        memcpy(out + (size_t)cell * 168, R, sizeof(R));
+    }
+}
+
+/* b += factor * (f, R v) over H1P2B{2,2}, R = ReconstructionIdentity{HDIVRT1{2}}
+ * (recon 3) or {HDIVBDM2{2}} (recon 4), f polynomial with 2 components
+ * (src/feevaluator_h1.jl:342-381, src/assemblypatterns/linearform.jl:181-220);
+ * quadrature order polyorder(H1P2B) = 3 plus bonus. */
+int oracle_p2b_rhs_recon(double *b, int ncells, const double *coords, const int *cells, const int *cell_faces,
+                         const double *fnormals, const double *fvolumes, const signed char *signs, const int *celldofs,
+                         const double *par, int npar, double factor, int bonus_quadorder, int recon)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(2, 3 + bonus_quadorder, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], nrm[6], fv[3], sg[3], A[3][3], G[3][3], det, vol, R[14][12];
+        br_cell(&m, cell, X, nrm, fv, sg);
+        oracle_geometry(2, X, A, G, &det, &vol);
+        const int nr = p2b_coeffs(recon, X, A, G, det, vol, fv, nrm, sg, R);
+        double coef[12];
+        p2b_recon_target(recon, sg, coef);
+        double locb[14] = {0};
+        for (int q = 0; q < nq; q++) {
+            double rb[12][2], te[12][2];
+            p2b_recon_basis(recon, xref[3 * q], xref[3 * q + 1], rb);
+            for (int j = 0; j < nr; j++)
+                for (int k = 0; k < 2; k++) {
+                    double s = 0;
+                    for (int l = 0; l < 2; l++) s += A[k][l] * rb[j][l];
+                    s *= coef[j] / det;
+                    te[j][k] = s;
+                }
+            double x[2], f[2];
+            for (int k = 0; k < 2; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 2; j++) x[k] += A[k][j] * xref[3 * q + j];
+            }
+            rhs_eval(OR_RHS_POLY, 2, 2, par, npar, cell, x, f);
+            for (int i = 0; i < 14; i++) {
+                double cv[2] = {0, 0};
+                for (int j = 0; j < nr; j++)
+                    if (R[i][j] != 0)
+                        for (int k = 0; k < 2; k++) cv[k] += R[i][j] * te[j][k];
+                double t = 0;
+                for (int k = 0; k < 2; k++) t += f[k] * cv[k];
+                locb[i] += t * w[q];
+            }
+        }
+        const double itemfactor = factor * vol;
+        for (int i = 0; i < 14; i++) b[celldofs[(size_t)cell * 14 + i]] += locb[i] * itemfactor;
+    }
+    return nq;
+}
+
+/* Velocity-pressure blocks of the P2B / P1-broken Stokes system:
+ * nu (grad u, grad v) into the sparse accumulator (order 4), and
+ * Bloc[cell][l][i] = int_T lambda_l div phi_i for the three barycentric
+ * pressure functions (order 3). */
+int oracle_p2b_stokes(void *h, int ncells, const double *coords, const int *cells, const int *celldofs, double nu,
+                      double *Bloc)
+{
+    omat *M = (omat *)h;
+    double xa[3 * OR_MAXQ], wa[OR_MAXQ], xb[3 * OR_MAXQ], wb[OR_MAXQ];
+    int na = oracle_qrule(2, 4, xa, wa), nb = oracle_qrule(2, 3, xb, wb);
+    if (na < 0) na = -na;
+    if (nb < 0) nb = -nb;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], A[3][3], G[3][3], det, vol;
+        for (int v = 0; v < 3; v++)
+            for (int k = 0; k < 2; k++) X[v * 2 + k] = coords[(size_t)cells[(size_t)cell * 3 + v] * 2 + k];
+        oracle_geometry(2, X, A, G, &det, &vol);
+        const int *dofs = &celldofs[(size_t)cell * 14];
+        double K[7][7] = {{0}};
+        for (int q = 0; q < na; q++) {
+            dual o[7];
+            p2b_basis_dual(xa[3 * q], xa[3 * q + 1], o);
+            double g[7][2];
+            for (int s = 0; s < 7; s++)
+                for (int k = 0; k < 2; k++) {
+                    double t = 0;
+                    for (int j = 0; j < 2; j++) t += G[k][j] * o[s].d[j];
+                    g[s][k] = t;
+                }
+            for (int a = 0; a < 7; a++)
+                for (int bb = 0; bb < 7; bb++) K[a][bb] += (g[a][0] * g[bb][0] + g[a][1] * g[bb][1]) * wa[q];
+        }
+        for (int c = 0; c < 2; c++)
+            for (int a = 0; a < 7; a++)
+                for (int bb = 0; bb < 7; bb++) omat_addnz(M, dofs[7 * c + a], dofs[7 * c + bb], K[a][bb] * vol * nu, 1.0);
+        double *Bl = Bloc + (size_t)cell * 42;
+        for (int i = 0; i < 42; i++) Bl[i] = 0.0;
+        for (int q = 0; q < nb; q++) {
+            const double xi = xb[3 * q], eta = xb[3 * q + 1];
+            const double lam[3] = {1 - xi - eta, xi, eta};
+            dual o[7];
+            p2b_basis_dual(xi, eta, o);
+            for (int i = 0; i < 14; i++) {
+                const int c = i / 7, s = i % 7;
+                double dv = 0;
+                for (int j = 0; j < 2; j++) dv += G[c][j] * o[s].d[j];
+                for (int l = 0; l < 3; l++) Bl[l * 14 + i] += lam[l] * dv * wb[q] * vol;
+            }
+        }
+    }
+    return na;
+}
+
+/* sum over cells of int_T |R u - f|^2 (quadrature order `order`), u an
+ * H1P2B{2,2} vector, f polynomial data (2 components). */
+double oracle_p2b_recon_l2error(int ncells, const double *coords, const int *cells, const int *cell_faces,
+                                const double *fnormals, const double *fvolumes, const signed char *signs,
+                                const int *celldofs, const double *u, const double *par, int npar, int recon,
+                                int order)
+{
+    br_mesh m = {coords, cells, cell_faces, fnormals, fvolumes, signs, celldofs};
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(2, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1.0;
+    double total = 0.0;
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[6], nrm[6], fv[3], sg[3], A[3][3], G[3][3], det, vol, R[14][12], coef[12];
+        br_cell(&m, cell, X, nrm, fv, sg);
+        oracle_geometry(2, X, A, G, &det, &vol);
+        const int nr = p2b_coeffs(recon, X, A, G, det, vol, fv, nrm, sg, R);
+        p2b_recon_target(recon, sg, coef);
+        double acc = 0.0;
+        for (int q = 0; q < nq; q++) {
+            double rb[12][2], v[2] = {0, 0};
+            p2b_recon_basis(recon, xref[3 * q], xref[3 * q + 1], rb);
+            for (int i = 0; i < 14; i++) {
+                const double ui = u[celldofs[(size_t)cell * 14 + i]];
+                for (int j = 0; j < nr; j++)
+                    for (int k = 0; k < 2; k++) {
+                        double s = 0;
+                        for (int l = 0; l < 2; l++) s += A[k][l] * rb[j][l];
+                        v[k] += ui * R[i][j] * (s * (coef[j] / det));
+                    }
+            }
+            double x[2], f[2];
+            for (int k = 0; k < 2; k++) {
+                x[k] = X[k];
+                for (int j = 0; j < 2; j++) x[k] += A[k][j] * xref[3 * q + j];
+            }
+            rhs_eval(OR_RHS_POLY, 2, 2, par, npar, cell, x, f);
+            acc += ((v[0] - f[0]) * (v[0] - f[0]) + (v[1] - f[1]) * (v[1] - f[1])) * w[q];
+        }
+        total += acc * vol;
+    }
+    return total;
+}

@@ -105,6 +105,15 @@ def lib():
         L.oracle_br3_bdm1_moments.argtypes = [dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.oracle_br3_recon_l2error.argtypes = brm + [dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_br3_recon_l2error.restype = ctypes.c_double
+        brm_nocd = brm[:-1]
+        L.oracle_p2b_coeffs.argtypes = brm_nocd + [ctypes.c_int, dp]
+        L.oracle_p2b_coeffs.restype = None
+        L.oracle_p2b_rhs_recon.argtypes = [dp] + brm + [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.oracle_p2b_rhs_recon.restype = ctypes.c_int
+        L.oracle_p2b_stokes.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ip, ip, ctypes.c_double, dp]
+        L.oracle_p2b_stokes.restype = ctypes.c_int
+        L.oracle_p2b_recon_l2error.argtypes = brm + [dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_p2b_recon_l2error.restype = ctypes.c_double
     return _lib
 
 
@@ -487,3 +496,110 @@ def stokes_iterated_penalty(g, nu: float, lam: float, terms, sweeps: int = 6, re
         p = p - lam * divu
         p -= np.dot(vol, p) / vol.sum()
     return u, p, fixed
+
+
+# --------------------------------------------------------------------------
+# H1P2B{2,2} with the RT1 / BDM2 reconstructions (2D)
+# --------------------------------------------------------------------------
+
+RECON_RT1, RECON_BDM2 = 3, 4
+
+
+def p2b_celldofs(g):
+    """H1P2B{2,2} cell DoFs, pattern "N1F1I1" per component
+    (src/fedefs/h1_p2b.jl:33), components blocked as in src/dofmaps.jl:201-330:
+    nodes, faces, then the cell of component 1, then those of component 2."""
+    fn, cf = g.faces()
+    nf = fn.shape[0]
+    nd1 = g.nverts + nf + g.ncells
+    one = np.concatenate([g.cells, cf + g.nverts, (np.arange(g.ncells) + g.nverts + nf)[:, None]], axis=1)
+    cd = np.concatenate([one, one + nd1], axis=1).astype(np.int32)
+    return np.ascontiguousarray(cd), 2 * nd1
+
+
+def p2b_coefficients(g, recon: int = RECON_RT1):
+    """Reconstruction coefficients [ncells][14][12] (columns past 8 zero for RT1)."""
+    fn, cf = g.faces()
+    cd, _ = p2b_celldofs(g)
+    _, ptrs = _br_args(g, cd)
+    out = np.zeros((g.ncells, 14, 12))
+    lib().oracle_p2b_coeffs(*ptrs[:-1], int(recon), _dp(out))
+    return out
+
+
+def p2b_rhs(g, terms, recon: int = RECON_RT1, bonus_quadorder: int = 0, factor: float = 1.0):
+    """(f, R v) over H1P2B{2,2} with R = RT1 (recon 3) or BDM2 (recon 4)."""
+    cd, nd = p2b_celldofs(g)
+    _, ptrs = _br_args(g, cd)
+    b = np.zeros(nd)
+    par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
+    if lib().oracle_p2b_rhs_recon(_dp(b), *ptrs, _dp(par), par.size, float(factor), int(bonus_quadorder),
+                                  int(recon)) < 0:
+        raise RuntimeError("oracle: no triangle rule of that order")
+    return b
+
+
+def p2b_recon_l2error(g, u, terms, recon: int = RECON_RT1, order: int = 6) -> float:
+    """||R u - f||_L2 of an H1P2B{2,2} vector against polynomial data."""
+    cd, _ = p2b_celldofs(g)
+    _, ptrs = _br_args(g, cd)
+    par = np.ascontiguousarray(terms, dtype=np.float64).ravel()
+    uu = np.ascontiguousarray(u, dtype=np.float64)
+    e2 = lib().oracle_p2b_recon_l2error(*ptrs, _dp(uu), _dp(par), par.size, int(recon), int(order))
+    if e2 < 0:
+        raise RuntimeError("oracle: no triangle rule of that order")
+    return float(np.sqrt(max(e2, 0.0)))
+
+
+def p2b_stokes(g, nu: float, terms, recon: int, u_boundary, bonus_quadorder: int = 0):
+    """Stokes with H1P2B{2,2} velocity and broken P1 pressure (the
+    reference's p-robust catalogue entries, test/runtests.jl:684-723):
+    nu (grad u, grad v) - (p, div v) = (f, R v), (q, div u) = 0, mean(p) = 0,
+    velocity Dirichlet data u_boundary on every boundary DoF (nodes and edge
+    midpoints of boundary faces); sparse LU of the saddle-point matrix.
+    Returns (u, p)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    cd, nd = p2b_celldofs(g)
+    M = Matrix(nd)
+    Bloc = np.zeros((g.ncells, 3, 14))
+    lib().oracle_p2b_stokes(M.h, g.ncells, _dp(np.ascontiguousarray(g.coords, dtype=np.float64)),
+                            _ip(np.ascontiguousarray(g.cells, dtype=np.int32)), _ip(cd), float(nu), _dp(Bloc))
+    A = M.csr()
+    npres = 3 * g.ncells
+    rows = np.repeat(np.arange(npres), 14)
+    cols = np.tile(cd, (1, 3)).reshape(g.ncells, 3, 14).reshape(-1)
+    B = sp.csr_matrix((Bloc.reshape(-1), (rows, cols)), shape=(npres, nd))
+    vol = g.cell_volumes()
+    mean = sp.csr_matrix(np.repeat(vol / 3.0, 3)[None, :])       # int of each barycentric function
+    K = sp.bmat([[A, -B.T, None], [-B, None, mean.T], [None, mean, None]], format="csr")
+    rhs = np.concatenate([p2b_rhs(g, terms, recon, bonus_quadorder), np.zeros(npres + 1)])
+    fn, cf = g.faces()
+    bfaces = np.nonzero(np.bincount(cf.ravel(), minlength=fn.shape[0]) == 1)[0]
+    bnodes = np.unique(fn[bfaces].ravel())
+    nd1 = nd // 2
+    fixed = np.unique(np.concatenate([bnodes + c * nd1 for c in range(2)] +
+                                     [bfaces + g.nverts + c * nd1 for c in range(2)]))
+    ub = np.asarray(u_boundary, dtype=np.float64)
+    free = np.setdiff1d(np.arange(K.shape[0]), fixed)
+    x = np.zeros(K.shape[0])
+    x[fixed] = ub[fixed]
+    rr = rhs - K @ x
+    Kff = K[free][:, free].tocsc()
+    x[free] = spla.splu(Kff).solve(rr[free])
+    return x[:nd], x[nd:nd + npres]
+
+
+def p2b_interpolant(g, field):
+    """P2B DoF vector of a vector field with values at the vertices and edge
+    midpoints (its P2 Lagrange interpolant) and zero bubbles; exact for
+    quadratic fields up to the bubble part."""
+    fn, cf = g.faces()
+    nd1 = g.nverts + fn.shape[0] + g.ncells
+    vv = field(g.coords)
+    mid = field(0.5 * (g.coords[fn[:, 0]] + g.coords[fn[:, 1]]))
+    u = np.zeros(2 * nd1)
+    for c in range(2):
+        u[c * nd1: c * nd1 + g.nverts] = vv[:, c]
+        u[c * nd1 + g.nverts: c * nd1 + g.nverts + fn.shape[0]] = mid[:, c]
+    return u
