@@ -18,11 +18,12 @@ ITEM_IDENTITY, ITEM_GRADIENT = 0, 1
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "DEVICE", 4: "NOT_CONVERGED",
                 5: "UNSUPPORTED", 6: "BUDGET", 7: "TIMEOUT", 8: "NAN", 9: "NO_DEVICE"}
 
-OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV = 1, 2, 3, 4
+OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV, OP_STRUCTURAL = 1, 2, 3, 4, 5
+NL_DIFFUSION, NL_GRAD_DIFFUSION, NL_CONVECTION = 1, 2, 3
 FP64, FP32, FP64_FP32 = 0, 1, 2
 RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
 DIRICHLET_PENALTY, DIRICHLET_ELIMINATE = 0, 1
-SOLVE_FP64, SOLVE_MIXED, SOLVE_DIRECT, SOLVE_MIXED_DIRECT = 0, 1, 2, 3
+SOLVE_FP64, SOLVE_MIXED, SOLVE_DIRECT, SOLVE_MIXED_DIRECT, SOLVE_BICGSTAB = 0, 1, 2, 3, 4
 NOALLOC_MAX_ROWS = 262144   # GRMP_NOALLOC_MAX_ROWS
 
 
@@ -36,6 +37,11 @@ class BilinearTerm(ctypes.Structure):
     _fields_ = [("op_kind", ctypes.c_int), ("symmetric", ctypes.c_int), ("factor", ctypes.c_double),
                 ("cell_coef", ctypes.POINTER(ctypes.c_double)), ("param", ctypes.c_double * 4),
                 ("bonus_quadorder", ctypes.c_int), ("coef_on_device", ctypes.c_int)]
+
+
+class NonlinearTerm(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("factor", ctypes.c_double), ("param", ctypes.c_double * 4),
+                ("bonus_quadorder", ctypes.c_int)]
 
 
 class Rhs(ctypes.Structure):
@@ -127,6 +133,8 @@ SIGNATURES = {
     "grmp_matrix_update_values": ([_vp, _pd], ctypes.c_int),
     "grmp_matrix_penalty_rows": ([_vp, _pi32], ctypes.c_int),
     "grmp_assemble_bilinear": ([_vp, ctypes.c_int, ctypes.POINTER(BilinearTerm), ctypes.c_int], ctypes.c_int),
+    "grmp_assemble_nonlinear": ([_vp, _vp, _vp, ctypes.POINTER(NonlinearTerm), ctypes.c_int, ctypes.c_int],
+                                ctypes.c_int),
     "grmp_matrix_download": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64), _pi32, _pd], ctypes.c_int),
     "grmp_assemble_linear": ([_vp, ctypes.POINTER(Rhs), _vp], ctypes.c_int),
     "grmp_item_l2error": ([_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(Rhs), ctypes.c_double, ctypes.c_int, _pd, _pd],

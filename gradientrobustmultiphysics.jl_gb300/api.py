@@ -255,6 +255,14 @@ def HookStiffnessOperator3D(mu: float, lam: float, *, name: str = "auto") -> Ope
     return Operator(L.OP_HOOKE, False, 1.0, params=(mu, lam, 0.0, 0.0), name=name)
 
 
+def StructuralCoupling() -> Operator:
+    """Pattern-only term that couples every local pair of a cell: include it
+    in an FEMatrix's operators when a NonlinearForm's Jacobian is assembled
+    into it (the Jacobian fills every local pair); it adds nothing to
+    assembled values."""
+    return Operator(L.OP_STRUCTURAL, False, 1.0, name="structural coupling")
+
+
 def BilinearForm(operators: Sequence[str], action=None, *, APT: str = APT_BilinearForm, factor: float = 1.0,
                  name: str = "auto") -> Operator:
     """BilinearForm([op, op], action) for the operator pairs on the hot path."""
@@ -505,6 +513,84 @@ def assemble(target, operators, precision: int = L.FP64):
     raise TypeError("assemble target must be an FEMatrix or FEVector")
 
 
+# ----------------------------------------------------------------------- nonlinear forms
+@dataclass
+class NonlinearForm:
+    """NonlinearForm(test, [operators of the iterate], kernel) for the closed
+    set of kernels the device has (src/pdeoperators.jl:590-636):
+    "diffusion" ((kappa + beta u^2) grad u, grad v) -- Example205's first
+    form with kappa = beta = 1; "grad_diffusion" ((kappa + |grad u|^2) grad u,
+    grad v) -- Example205's second form; "convection" ((u . grad) u, v) on a
+    vector space -- the Navier-Stokes convection term.  Newton is the only
+    linearisation, as in the reference (newton = true)."""
+    kind: str = "diffusion"
+    kappa: float = 1.0
+    beta: float = 1.0
+    factor: float = 1.0
+    bonus_quadorder: int = 0
+
+    def term(self) -> L.NonlinearTerm:
+        t = L.NonlinearTerm()
+        t.kind = {"diffusion": L.NL_DIFFUSION, "grad_diffusion": L.NL_GRAD_DIFFUSION,
+                  "convection": L.NL_CONVECTION}[self.kind]
+        t.factor = float(self.factor)
+        t.param[0] = float(self.kappa)
+        t.param[1] = float(self.beta)
+        t.bonus_quadorder = int(self.bonus_quadorder)
+        return t
+
+
+def assemble_nonlinear(A: "FEMatrix", b: "FEVector", u: "FEVector", form: NonlinearForm, precision: int = L.FP64,
+                       add: bool = True):
+    """The Newton terms of `form` at the iterate u: DG(u) into A and
+    DG(u) u - G(u) into b (added to the current values, or overwriting them
+    with add=False) -- grmp_assemble_nonlinear."""
+    t = form.term()
+    A.ctx.check(A.ctx.lib.grmp_assemble_nonlinear(A.h, b.h, u.h, ctypes.byref(t), precision, 1 if add else 0))
+
+
+def solve_nonlinear(ctx: "GB300Context", FES, operators, form: NonlinearForm, rhs, fixed, *, maxiterations: int = 20,
+                    target_change: float = 1e-12, reltol: float = 1e-13, u0=None):
+    """The Newton loop of solve! for a problem with linear `operators`, one
+    NonlinearForm and a right-hand side, homogeneous Dirichlet DoFs `fixed`
+    (src/solvers.jl:519-566, :887-990): per step the linear operators are
+    assembled, the Newton terms added at the current iterate, the Dirichlet
+    DoFs eliminated and the non-symmetric system solved by BiCGStab; stops when
+    ||u_next - u|| <= target_change ||u_next||.  Returns (u, per-step stats)."""
+    ops = list(operators)
+    A = FEMatrix(ctx, FES, ops + [StructuralCoupling()])
+    f = FEVector(ctx, FES)
+    b = FEVector(ctx, FES)
+    u = FEVector(ctx, FES)
+    x = FEVector(ctx, FES)
+    f.fill(0.0)
+    if rhs is not None:
+        assemble(f, rhs)
+    fh = f.entries
+    u.upload(np.zeros(FES.ndofs) if u0 is None else np.asarray(u0, dtype=np.float64))
+    solver = GB300PCG(mode="bicgstab", reltol=reltol, abstol=0.0)
+    stats = []
+    fixed = np.ascontiguousarray(fixed, dtype=np.int32)
+    try:
+        for _ in range(maxiterations):
+            assemble(A, ops + [StructuralCoupling()], L.FP64)
+            b.upload(fh)
+            assemble_nonlinear(A, b, u, form, L.FP64, add=True)
+            apply_dirichlet(A, b, fixed, None, L.DIRICHLET_ELIMINATE)
+            st = solver.solve(A, b, x)
+            xn, un = x.entries, u.entries
+            change = float(np.linalg.norm(xn - un) / max(np.linalg.norm(xn), 1e-300))
+            st = dict(st, change=change)
+            stats.append(st)
+            u.upload(xn)
+            if change <= target_change:
+                break
+        return u.entries, stats
+    finally:
+        for v in (A, f, b, u, x):
+            v.free()
+
+
 # ----------------------------------------------------------------------- item integrators
 @dataclass
 class ItemIntegrator:
@@ -584,7 +670,8 @@ class GB300PCG:
     mode "direct": FP64 multifrontal Cholesky + residual refinement (the
     counterpart of the reference's sparse-direct default).  mode
     "mixed_direct": FP32 multifrontal Cholesky as the preconditioner of FP64
-    conjugate gradients."""
+    conjugate gradients.  mode "bicgstab": FP64 Jacobi-preconditioned
+    BiCGStab for non-symmetric matrices (Newton steps of a NonlinearForm)."""
     mode: str = "fp64"
     abstol: float = 1e-12
     reltol: float = 1e-12
@@ -602,7 +689,7 @@ class GB300PCG:
         p.reltol = self.reltol
         p.maxiter = self.maxiter
         p.mode = {"fp64": L.SOLVE_FP64, "mixed": L.SOLVE_MIXED, "direct": L.SOLVE_DIRECT,
-                  "mixed_direct": L.SOLVE_MIXED_DIRECT}[self.mode]
+                  "mixed_direct": L.SOLVE_MIXED_DIRECT, "bicgstab": L.SOLVE_BICGSTAB}[self.mode]
         p.inner_reltol = self.inner_reltol
         p.max_outer = self.max_outer
         p.spmv_config = self.spmv_config

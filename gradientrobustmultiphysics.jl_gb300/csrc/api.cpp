@@ -325,6 +325,17 @@ int grmp_assemble_bilinear(grmp_matrix A, int nterms, const grmp_bilinear_term *
     return grmp_assemble_bilinear_impl(A, nterms, terms, precision);
 }
 
+int grmp_assemble_nonlinear(grmp_matrix A, grmp_vector b, grmp_vector u, const grmp_nonlinear_term *term,
+                            int precision, int add) {
+    if (!A || !b || !u || !term || (add != 0 && add != 1)) return GRMP_ERR_INVALID_ARG;
+    grmp_context ctx = A->space->mesh->ctx;
+    if (b->n != A->nrows || u->n != A->nrows || b->ctx != ctx || u->ctx != ctx)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "nonlinear form: vector length or context mismatch");
+    cudaSetDevice(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return grmp_assemble_nonlinear_impl(A, b, u, term, precision, add);
+}
+
 int grmp_assemble_linear(grmp_space space, const grmp_rhs *rhs, grmp_vector b) {
     if (!space || !rhs || !b) return GRMP_ERR_INVALID_ARG;
     if (b->n != space->ndofs)
@@ -374,7 +385,7 @@ int grmp_solve(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_par
     if (!A || !b || !x || !p) return GRMP_ERR_INVALID_ARG;
     grmp_context ctx = A->space->mesh->ctx;
     if (b->n != A->nrows || x->n != A->nrows) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: size mismatch");
-    if (p->mode < GRMP_SOLVE_FP64 || p->mode > GRMP_SOLVE_MIXED_DIRECT) return GRMP_ERR_INVALID_ARG;
+    if (p->mode < GRMP_SOLVE_FP64 || p->mode > GRMP_SOLVE_BICGSTAB) return GRMP_ERR_INVALID_ARG;
     if (!(p->reltol >= 0) || !(p->abstol >= 0) || p->maxiter <= 0) return GRMP_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     std::lock_guard<std::mutex> lk(ctx->mu);

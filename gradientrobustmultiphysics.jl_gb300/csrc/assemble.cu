@@ -584,6 +584,26 @@ int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_t
         return rc;
     }
     int dim = s->mesh->dim, nb = s->nb, nc = s->ncomp;
+    // pattern-only terms contribute nothing to the values
+    std::vector<grmp_bilinear_term> kept;
+    for (int i = 0; i < nterms; i++)
+        if (terms[i].op_kind != GRMP_OP_STRUCTURAL) kept.push_back(terms[i]);
+    nterms = (int)kept.size();
+    terms = kept.data();
+    if (nterms == 0) {   // only pattern terms: every value is zero
+        int rz = GRMP_OK;
+        const bool want64 = precision != GRMP_FP32, want32 = precision != GRMP_FP64;
+        if (want64 && !A->d_vals64) rz = grmp_alloc(ctx, (void **)&A->d_vals64, (size_t)A->nnz * 8);
+        if (!rz && want32 && !A->d_vals32) rz = grmp_alloc(ctx, (void **)&A->d_vals32, (size_t)A->nnz * 4);
+        if (rz) return rz;
+        if (want64) cudaMemsetAsync(A->d_vals64, 0, (size_t)A->nnz * 8, ctx->stream);
+        if (want32) cudaMemsetAsync(A->d_vals32, 0, (size_t)A->nnz * 4, ctx->stream);
+        GRMP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (want64) A->has64 = true;
+        if (want32) A->has32 = true;
+        A->eliminated = false;
+        return GRMP_OK;
+    }
     TermsDev td;
     std::vector<std::pair<void *, size_t>> keep;
     int rc = grmp_prepare_terms(s, nterms, terms, &td, keep);

@@ -182,6 +182,8 @@ int grmp_scan_i32(grmp_context ctx, const int32_t *d_in, int32_t *d_out_excl, in
 // pattern / assembly / solve implementations (pattern.cu, assemble.cu, solve.cu)
 int grmp_pattern_build_impl(grmp_space space, int nterms, const grmp_bilinear_term *terms, grmp_matrix *out);
 int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
+int grmp_assemble_nonlinear_impl(grmp_matrix A, grmp_vector b, grmp_vector u, const grmp_nonlinear_term *term,
+                                 int precision, int add);
 int grmp_assemble_linear_impl(grmp_space space, const grmp_rhs *rhs, grmp_vector b);
 int grmp_item_l2error_impl(grmp_space s, grmp_vector u, grmp_vector v, int op, const grmp_rhs *data, double factor,
                            int quadorder, double *cell_values, double *total);

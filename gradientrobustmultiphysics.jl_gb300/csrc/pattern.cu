@@ -198,6 +198,10 @@ __global__ void k_nzmask(int ncells, const double *coords, const int32_t *cells,
     double cv[16][LD][RD];
     for (int ti = 0; ti < terms.n; ti++) {
         const TermDev &t = terms.t[ti];
+        if (t.op == GRMP_OP_STRUCTURAL) {   // every local pair
+            for (int i = 0; i < LD; i++) m[i] = LD >= 32 ? ~0u : ((1u << LD) - 1u);
+            continue;
+        }
         int opv = t.op == GRMP_OP_MASS ? OPV_IDENTITY : (t.op == GRMP_OP_LAPLACE ? OPV_GRADIENT : OPV_SYMGRAD);
         int rdim = opv == OPV_IDENTITY ? NC : (opv == OPV_GRADIENT ? DIM * NC : (DIM == 2 ? 3 : 6));
         ref_cvals<DIM, NB, NC>(opv, t.tab, G, cv);
@@ -386,7 +390,7 @@ int grmp_prepare_terms(grmp_space s, int nterms, const grmp_bilinear_term *terms
         d.cell_coef = nullptr;
         int deriv;
         if (t.op_kind == GRMP_OP_LAPLACE) deriv = 1;
-        else if (t.op_kind == GRMP_OP_MASS) deriv = 0;
+        else if (t.op_kind == GRMP_OP_MASS || t.op_kind == GRMP_OP_STRUCTURAL) deriv = 0;
         else if (t.op_kind == GRMP_OP_HOOKE) {
             deriv = 1;
             if (s->ncomp != dim)

@@ -356,6 +356,125 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
     }
 }
 
+// ------------------------------------------------------------------ FP64 BiCGStab
+// Jacobi right-preconditioned BiCGStab (van der Vorst 1992) for the
+// non-symmetric systems of a Newton step (the Jacobian of a NonlinearForm),
+// where the reference hands the matrix to a sparse LU.  Per iteration:
+//   p = r + beta (p - omega v), ph = D^-1 p;  v = A ph;  alpha = rho / (rh, v)
+//   s = r - alpha v, sh = D^-1 s;  t = A sh;  omega = (t, s) / (t, t)
+//   x += alpha ph + omega sh;  r = s - omega t;  rho' = (rh, r)
+// Five grid-wide synchronisations; every wait is bounded (`spin`).
+template <int TPR, int U>
+__global__ void __launch_bounds__(PTPB, 4) k_bicgstab64(int n, const int32_t *rowptr, const int32_t *cols,
+                                                         const double *vals, const double *b, double *x,
+                                                         const double *dinv, double *r, double *rh, double *p,
+                                                         double *v, double *s, double *t, double *ph, double *shv,
+                                                         double *partial, SolveState *st, double abstol,
+                                                         double reltol, int maxit, int guess, long long spin) {
+    __shared__ double sh[32 * 4];
+    int round = 0;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsz = gridDim.x * blockDim.x;
+    if (guess) spmv_grid<TPR, U, false, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+    double w3[3] = {0, 0, 0};
+    for (int i = gtid; i < n; i += gsz) {
+        const double ri = guess ? r[i] : b[i];
+        if (!guess) {
+            r[i] = ri;
+            x[i] = 0.0;
+        }
+        rh[i] = ri;
+        p[i] = 0.0;
+        v[i] = 0.0;
+        w3[0] += ri * ri;
+        w3[1] += ri * ri;
+        w3[2] += b[i] * b[i];
+    }
+    if (!grid_sum<3>(w3, partial, sh, st, round, spin)) return;
+    double rho = w3[0], rr = w3[1];
+    const double bn = sqrt(w3[2]);
+    const double tol = fmax(abstol, reltol * bn);
+    double alpha = 1.0, omega = 1.0, beta = 0.0;
+    int it = 0;
+    bool conv = sqrt(rr) <= tol;
+    while (!conv && it < maxit) {
+        for (int i = gtid; i < n; i += gsz) {
+            const double pi = r[i] + beta * (p[i] - omega * v[i]);
+            p[i] = pi;
+            ph[i] = dinv[i] * pi;
+        }
+        if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+        double d[1];
+        d[0] = spmv_grid<TPR, U, false, double, double, double, true, false>(n, rowptr, cols, vals, ph, v, rh, nullptr);
+        if (!grid_sum<1>(d, partial, sh, st, round, spin)) return;
+        if (!(d[0] != 0.0) || !isfinite(d[0])) {
+            if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
+            break;
+        }
+        alpha = rho / d[0];
+        double ss[1] = {0};
+        for (int i = gtid; i < n; i += gsz) {
+            const double si = r[i] - alpha * v[i];
+            s[i] = si;
+            shv[i] = dinv[i] * si;
+            ss[0] += si * si;
+        }
+        if (!grid_sum<1>(ss, partial, sh, st, round, spin)) return;
+        if (sqrt(ss[0]) <= tol) {   // converged on the half step
+            for (int i = gtid; i < n; i += gsz) {
+                x[i] += alpha * ph[i];
+                r[i] = s[i];
+            }
+            it++;
+            conv = true;
+            break;
+        }
+        double ts[2] = {0, 0};
+        spmv_rows<TPR, U, false, double>(
+            n, rowptr, CsrSource<double>{cols, vals}, [&](int c) { return shv[c]; },
+            [&](int row, double tv) {
+                t[row] = tv;
+                ts[0] += tv * s[row];
+                ts[1] += tv * tv;
+            });
+        if (!grid_sum<2>(ts, partial, sh, st, round, spin)) return;
+        if (!(ts[1] > 0.0) || !isfinite(ts[1])) {
+            if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
+            break;
+        }
+        omega = ts[0] / ts[1];
+        double w2[2] = {0, 0};
+        for (int i = gtid; i < n; i += gsz) {
+            x[i] += alpha * ph[i] + omega * shv[i];
+            const double ri = s[i] - omega * t[i];
+            r[i] = ri;
+            w2[0] += rh[i] * ri;
+            w2[1] += ri * ri;
+        }
+        if (!grid_sum<2>(w2, partial, sh, st, round, spin)) return;
+        it++;
+        rr = w2[1];
+        conv = sqrt(rr) <= tol;
+        if (!conv && (!(w2[0] != 0.0) || !(omega != 0.0))) {   // breakdown
+            if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
+            break;
+        }
+        beta = (w2[0] / rho) * (alpha / omega);
+        rho = w2[0];
+    }
+    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+    double tr[1];
+    tr[0] = spmv_grid<TPR, U, false, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
+    if (!grid_sum<1>(tr, partial, sh, st, round, spin)) return;
+    if (gtid == 0) {
+        st->iters = it;
+        st->outer = 0;
+        st->relres = sqrt(tr[0]) / (bn > 0 ? bn : 1.0);
+        if (st->status == 0 && !(sqrt(tr[0]) <= fmax(tol, 0.0) || conv)) st->status = GRMP_ERR_NOT_CONVERGED;
+    }
+}
+
 // ------------------------------------------------------------------ mixed PCG
 // FP32 SpMV fused with the search-direction update.  The preconditioned
 // residual z and the search direction p are stored interleaved (float2) and
@@ -1495,6 +1614,65 @@ int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_para
     return best;
 }
 
+template <int TPR, int U>
+int launch_bicgstab_t(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
+                      grmp_solve_stats *out, char *work, SolveState *dst, WorkLayout lay) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int n = A->nrows;
+    auto kern = k_bicgstab64<TPR, U>;
+    const int grid = coop_grid(ctx, kern, n, p->grid_blocks);
+    double *dinv = (double *)work;
+    double *vv[8];
+    for (int k = 0; k < 8; k++) vv[k] = (double *)(work + (size_t)(k + 1) * lay.vec);
+    double *part = (double *)(work + lay.off_part);
+    int nn = n, mi = p->maxiter, guess = p->use_initial_guess ? 1 : 0;
+    double at = p->abstol, rt = p->reltol;
+    const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+    const double *vals = A->d_vals64, *bb = bvec;
+    double *xx = xvec;
+    long long spin = ctx->wait_limit;
+    void *args[] = {&nn, &rp, &ci, &vals, &bb, &xx, &dinv, &vv[0], &vv[1], &vv[2], &vv[3], &vv[4], &vv[5], &vv[6],
+                    &vv[7], &part, &dst, &at, &rt, &mi, &guess, &spin};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
+    cudaEventRecord(e0, ctx->stream);
+    cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+    GRMP_LAUNCHED(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    SolveState hs;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "persistent BiCGStab launch");
+    out->status = hs.status;
+    out->iterations = hs.iters;
+    out->final_relres = hs.relres;
+    out->spmv_config = 100 * TPR + U;
+    out->grid_blocks = grid;
+    out->solve_ms = ms;
+    if (hs.status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, GRMP_ERR_NOT_CONVERGED, "BiCGStab: %d iterations, relative residual %.3e", hs.iters,
+                         hs.relres);
+    if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "BiCGStab: a grid barrier wait timed out");
+    if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "BiCGStab: breakdown");
+    return hs.status;
+}
+
+int launch_bicgstab(grmp_matrix A, const double *b, double *x, const grmp_solve_params *p, grmp_solve_stats *st,
+                    char *work, SolveState *dst, WorkLayout lay) {
+    switch (heuristic_tpr(A)) {
+        case 2: return launch_bicgstab_t<2, 4>(A, b, x, p, st, work, dst, lay);
+        case 4: return launch_bicgstab_t<4, 4>(A, b, x, p, st, work, dst, lay);
+        case 8: return launch_bicgstab_t<8, 4>(A, b, x, p, st, work, dst, lay);
+        default: return launch_bicgstab_t<16, 2>(A, b, x, p, st, work, dst, lay);
+    }
+}
+
 }  // namespace
 
 int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solve_params *p, grmp_solve_stats *st) {
@@ -1510,7 +1688,9 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     size_t pbytes = (size_t)2 * kPartStride * 8;   // two alternating partial-sum buffers
     size_t vec = mixed ? al((size_t)n * 4) : al((size_t)n * 8);
-    size_t nvec = mixed ? 8 : 5;   // MIXED: dinv, r, q, xc (float) + two (z, p) float2 pair buffers
+    const bool bicg = p->mode == GRMP_SOLVE_BICGSTAB;
+    // MIXED: dinv, r, q, xc (float) + two (z, p) float2 pair buffers; BICGSTAB: dinv r rh p v s t ph sh
+    size_t nvec = mixed ? 8 : (bicg ? 9 : 5);
     size_t off_r64 = nvec * vec;
     size_t off_part = off_r64 + (mixed ? al((size_t)n * 8) : 0);
     size_t off_state = off_part + al(pbytes);
@@ -1542,6 +1722,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     grmp_free(ctx, bad, 4);
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
     if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
+    if (bicg) return launch_bicgstab(A, b->d, x->d, p, st, work, dst, lay);
     // the FP32 copies (packed pairs and staged windows, duo values) are
     // refreshed by the first launch that reads them: the values may have been
     // reassembled since the last solve

@@ -175,10 +175,12 @@ typedef enum {
     GRMP_OP_MASS = 2,      /* (Identity u, Identity v): ReactionOperator, src/pdeoperators.jl:176-203     */
     GRMP_OP_HOOKE = 3,     /* (C eps(u), eps(v)) with SymmetricGradient{1}: HookStiffnessOperator2D/3D
                               src/pdeoperators.jl:256-315; param[0] = mu, param[1] = lambda            */
-    GRMP_OP_RDIVRDIV = 4   /* (div R u, div R v), R = BR -> RT0 reconstruction (ReconstructionDivergence,
+    GRMP_OP_RDIVRDIV = 4,  /* (div R u, div R v), R = BR -> RT0 reconstruction (ReconstructionDivergence,
                               src/feevaluator_h1.jl:409-437); iterated-penalty term.  In 3D the RT0
                               basis is mapped with A phi / |det A| (times the cell-face sign), so
                               div R u is the cell mean of div u on tetrahedra of either orientation */
+    GRMP_OP_STRUCTURAL = 5 /* pattern only: couples every local pair of a cell (the Jacobian of a
+                              NonlinearForm fills them all); contributes nothing to assembled values */
 } grmp_op_kind;
 
 /* One operator term.  Assembly of a list of terms adds them into one matrix,
@@ -222,6 +224,46 @@ int grmp_matrix_info(grmp_matrix A, int32_t *nrows, int64_t *nnz, int32_t *max_r
  * (src/assemblypatterns/bilinearform.jl:92-400).  Deterministic: each
  * nonzero is the sum of its cell contributions in ascending cell order. */
 int grmp_assemble_bilinear(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
+
+/* ---------------------------------------------------------- nonlinear forms */
+
+/* NonlinearForm kernels (the reference takes a user kernel and differentiates
+ * it with ForwardDiff; here a closed set with its Jacobian written out). */
+typedef enum {
+    GRMP_NL_DIFFUSION = 1,      /* ((kappa + beta u^2) grad u, grad v), scalar: NonlinearForm(Gradient,
+                                   [Identity, Gradient], ...), examples/Example205_NonlinearPoisson2D.jl:114
+                                   (kappa = beta = 1), Example206, ExampleA04, ExampleA05              */
+    GRMP_NL_GRAD_DIFFUSION = 2, /* ((kappa + |grad u|^2) grad u, grad v), scalar: NonlinearForm(Gradient,
+                                   [Gradient], ...), examples/Example205_NonlinearPoisson2D.jl:116       */
+    GRMP_NL_CONVECTION = 3      /* ((u . grad) u, v), vector with ncomponents = dim: NonlinearForm(
+                                   Identity, [Identity, Gradient], ...), the Navier-Stokes convection
+                                   (examples/ExampleA11_NavierStokesFixpointIterations.jl:78,
+                                   src/pdeoperators.jl:493)                                             */
+} grmp_nl_kind;
+
+typedef struct {
+    int kind;                /* grmp_nl_kind                                          */
+    double factor;           /* NonlinearForm factor                                  */
+    double param[4];         /* DIFFUSION: kappa, beta; GRAD_DIFFUSION: kappa          */
+    int bonus_quadorder;     /* added to the quadrature order                          */
+} grmp_nonlinear_term;
+
+/* Newton linearisation at the iterate u (full_assemble!,
+ * src/assemblypatterns/nonlinearform.jl:44-240): with K the kernel, J its
+ * Jacobian and input(.) the operator evaluations,
+ *   A[j][i] (+)= vol factor sum_q w_q (J input(phi_i)) . test(phi_j)
+ *   b[j]    (+)= vol factor sum_q w_q (J input(u) - K) . test(phi_j),
+ * i.e. DG(u) into A and DG(u) u - G(u) into b, so that A x = b is the
+ * Newton step's system for the next iterate x (the reference adds the same to
+ * the PDE's matrix and right-hand side, src/solvers.jl:519-566).  add = 1
+ * adds to A's values and b (after grmp_assemble_bilinear / _linear of the
+ * linear operators), add = 0 overwrites them.  A's pattern must hold every
+ * local pair: build it with a GRMP_OP_STRUCTURAL term (GRMP_ERR_INVALID_ARG
+ * otherwise).  precision GRMP_FP64, or GRMP_FP64_FP32 (the FP32 values get
+ * the FP64 contributions rounded).  The Jacobian is not symmetric: solve with
+ * GRMP_SOLVE_BICGSTAB.  H1P1 / H1P2 spaces. */
+int grmp_assemble_nonlinear(grmp_matrix A, grmp_vector b, grmp_vector u, const grmp_nonlinear_term *term,
+                            int precision, int add);
 
 /* A matrix from the caller's compressed sparse column arrays: the matrix
  * LinearSolve receives from solve_direct!, a SparseMatrixCSC{Float64,Int64}
@@ -349,9 +391,12 @@ typedef enum {
                               refinement against the assembled FP64 matrix; in
                               grmp_stokes_batch_solve one factorisation per problem, reused by
                               every sweep.  SPD matrices (Dirichlet eliminated or penalised).     */
-    GRMP_SOLVE_MIXED_DIRECT = 3 /* grmp_solve only: FP32 multifrontal Cholesky used as the
+    GRMP_SOLVE_MIXED_DIRECT = 3, /* grmp_solve only: FP32 multifrontal Cholesky used as the
                               preconditioner of FP64 conjugate gradients on the FP64 matrix
                               (Dirichlet rows must be eliminated: 1e60 overflows FP32)           */
+    GRMP_SOLVE_BICGSTAB = 4 /* grmp_solve only: FP64 Jacobi-preconditioned BiCGStab in one
+                              persistent launch, for non-symmetric matrices (the Jacobian of a
+                              NonlinearForm's Newton step, where the reference calls a sparse LU) */
 } grmp_solve_mode;
 
 typedef struct {

@@ -2296,3 +2296,156 @@ double oracle_p2b_recon_l2error(int ncells, const double *coords, const int *cel
     }
     return total;
 }
+
+/* ------------------------------------------------------------------------- */
+/* NonlinearForm: Newton terms (src/assemblypatterns/nonlinearform.jl:44-240) */
+/* ------------------------------------------------------------------------- */
+
+enum { OR_NL_DIFFUSION = 1, OR_NL_GRAD_DIFFUSION = 2, OR_NL_CONVECTION = 3 };
+
+/* Kernel value K and Jacobian J (row-major, nin columns) of the closed set of
+ * nonlinear kernels:  DIFFUSION ((kappa + beta u^2) grad u, input [u, grad u]),
+ * GRAD_DIFFUSION ((kappa + |grad u|^2) grad u, input [grad u]), CONVECTION
+ * ((u . grad) u, input [u, grad u] with grad u component-major). */
+static void nl_kernel(int kind, int dim, double kappa, double beta, const double *in, double *K, double *J, int nin)
+{
+    for (int i = 0; i < dim * nin; i++) J[i] = 0.0;
+    if (kind == OR_NL_DIFFUSION) {
+        const double u = in[0], c = kappa + beta * (u * u);
+        for (int k = 0; k < dim; k++) {
+            K[k] = c * in[1 + k];
+            J[k * nin + 0] = (beta * (2.0 * u)) * in[1 + k];
+            J[k * nin + 1 + k] = c;
+        }
+    } else if (kind == OR_NL_GRAD_DIFFUSION) {
+        double g2 = 0.0;
+        for (int k = 0; k < dim; k++) g2 += in[k] * in[k];
+        const double c = kappa + g2;
+        for (int k = 0; k < dim; k++) {
+            K[k] = c * in[k];
+            for (int l = 0; l < dim; l++) J[k * nin + l] = (2.0 * in[l]) * in[k];
+            J[k * nin + k] += c;
+        }
+    } else {
+        for (int c = 0; c < dim; c++) {
+            double s = 0.0;
+            for (int l = 0; l < dim; l++) s += in[l] * in[dim + c * dim + l];
+            K[c] = s;
+            for (int m = 0; m < dim; m++) J[c * nin + m] = in[dim + c * dim + m];
+            for (int l = 0; l < dim; l++) J[c * nin + dim + c * dim + l] = in[l];
+        }
+    }
+}
+
+/* Adds the Newton terms of one NonlinearForm at the iterate u: DG(u) into M
+ * (row = test DoF, column = ansatz DoF: transposed_assembly, skipping exact
+ * zeros as _addnz does) and DG(u) u - G(u) into b.  Quadrature order: bonus
+ * plus, per operator, polyorder + shift (src/assemblypatterns.jl:558-565). */
+int oracle_nl_assemble(void *h, double *b, int dim, const double *coords, int ncells, const int *cellnodes, int fe,
+                       int ncomp, const int *celldofs, const double *u, int kind, double factor, double kappa,
+                       double beta, int bonus_quadorder)
+{
+    omat *M = (omat *)h;
+    const int nb = (fe == OR_FE_P1) ? dim + 1 : (dim == 2 ? 6 : 10);
+    const int ld = nb * ncomp, p = (fe == OR_FE_P1) ? 1 : 2;
+    int order = bonus_quadorder;
+    if (kind == OR_NL_DIFFUSION) order += p + 2 * (p - 1);
+    else if (kind == OR_NL_GRAD_DIFFUSION) order += 2 * (p - 1);
+    else order += 2 * p + (p - 1);
+    if (order < 0) order = 0;
+    double xref[3 * OR_MAXQ], w[OR_MAXQ];
+    int nq = oracle_qrule(dim, order, xref, w);
+    if (nq < 0) nq = -nq;
+    if (nq == 0) return -1;
+    double *vals = (double *)malloc(sizeof(double) * (size_t)nq * nb);
+    double *derivs = (double *)malloc(sizeof(double) * (size_t)nq * nb * dim);
+    oracle_basis_tables(fe, dim, nq, xref, vals, derivs);
+    const int nin = (kind == OR_NL_CONVECTION) ? dim + dim * dim : (kind == OR_NL_GRAD_DIFFUSION ? dim : 1 + dim);
+    double *in = (double *)malloc(sizeof(double) * (size_t)nq * nin);
+    double *cvid = (double *)malloc(sizeof(double) * (size_t)nq * ld * nin);   /* input(phi_i) per q */
+    double *cvt = (double *)malloc(sizeof(double) * (size_t)nq * ld * dim);    /* test(phi_j) per q */
+    double *lm = (double *)malloc(sizeof(double) * (size_t)ld * ld);
+    double *lb = (double *)malloc(sizeof(double) * (size_t)ld);
+    double K[3], J[3 * 12], ar[3];
+    for (int cell = 0; cell < ncells; cell++) {
+        double X[12], A[3][3], G[3][3], det, vol;
+        for (int v = 0; v <= dim; v++)
+            for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cellnodes[(size_t)cell * (dim + 1) + v] * dim + k];
+        oracle_geometry(dim, X, A, G, &det, &vol);
+        const int *dofs = &celldofs[(size_t)cell * ld];
+        /* operator evaluations of every local basis function */
+        for (int q = 0; q < nq; q++)
+            for (int i = 0; i < ld; i++) {
+                const int c = i / nb, a = i % nb;
+                double gr[3];
+                for (int k = 0; k < dim; k++) {
+                    double s = 0;
+                    for (int j = 0; j < dim; j++) s += G[k][j] * derivs[(q * nb + a) * dim + j];
+                    gr[k] = s;
+                }
+                double *ci = cvid + ((size_t)q * ld + i) * nin;
+                double *ct = cvt + ((size_t)q * ld + i) * dim;
+                for (int m = 0; m < nin; m++) ci[m] = 0.0;
+                if (kind == OR_NL_CONVECTION) {
+                    ci[c] = vals[q * nb + a];
+                    for (int k = 0; k < dim; k++) ci[dim + c * dim + k] = gr[k];
+                    for (int k = 0; k < dim; k++) ct[k] = (k == c) ? vals[q * nb + a] : 0.0;
+                } else {
+                    if (kind == OR_NL_DIFFUSION) {
+                        ci[0] = vals[q * nb + a];
+                        for (int k = 0; k < dim; k++) ci[1 + k] = gr[k];
+                    } else {
+                        for (int k = 0; k < dim; k++) ci[k] = gr[k];
+                    }
+                    for (int k = 0; k < dim; k++) ct[k] = gr[k];
+                }
+            }
+        /* current iterate: eval_febe! over the DoFs in order */
+        for (int q = 0; q < nq; q++) {
+            double *iq = in + (size_t)q * nin;
+            for (int m = 0; m < nin; m++) iq[m] = 0.0;
+            for (int i = 0; i < ld; i++) {
+                const double ui = u[dofs[i]];
+                const double *ci = cvid + ((size_t)q * ld + i) * nin;
+                for (int m = 0; m < nin; m++) iq[m] += ui * ci[m];
+            }
+        }
+        for (int i = 0; i < ld * ld; i++) lm[i] = 0.0;
+        for (int j = 0; j < ld; j++) lb[j] = 0.0;
+        for (int q = 0; q < nq; q++) {
+            const double *iq = in + (size_t)q * nin;
+            nl_kernel(kind, dim, kappa, beta, iq, K, J, nin);
+            for (int i = 0; i < ld; i++) {
+                const double *ci = cvid + ((size_t)q * ld + i) * nin;
+                for (int k = 0; k < dim; k++) {
+                    double s = 0;
+                    for (int m = 0; m < nin; m++) s += J[k * nin + m] * ci[m];
+                    ar[k] = s;
+                }
+                for (int j = 0; j < ld; j++) {
+                    const double *ct = cvt + ((size_t)q * ld + j) * dim;
+                    double t = 0;
+                    for (int k = 0; k < dim; k++) t += ar[k] * ct[k];
+                    lm[i * ld + j] += t * w[q];
+                }
+            }
+            for (int k = 0; k < dim; k++) {
+                double s = 0;
+                for (int m = 0; m < nin; m++) s += J[k * nin + m] * iq[m];
+                ar[k] = s;
+            }
+            for (int j = 0; j < ld; j++) {
+                const double *ct = cvt + ((size_t)q * ld + j) * dim;
+                double t = 0;
+                for (int k = 0; k < dim; k++) t += (ar[k] - K[k]) * ct[k];
+                lb[j] += t * w[q];
+            }
+        }
+        const double itemfactor = vol * factor;
+        for (int i = 0; i < ld; i++)
+            for (int j = 0; j < ld; j++) omat_addnz(M, dofs[j], dofs[i], lm[i * ld + j], itemfactor);
+        for (int j = 0; j < ld; j++) b[dofs[j]] += lb[j] * itemfactor;
+    }
+    free(vals); free(derivs); free(in); free(cvid); free(cvt); free(lm); free(lb);
+    return nq;
+}

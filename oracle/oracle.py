@@ -114,6 +114,10 @@ def lib():
         L.oracle_p2b_stokes.restype = ctypes.c_int
         L.oracle_p2b_recon_l2error.argtypes = brm + [dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_p2b_recon_l2error.restype = ctypes.c_double
+        L.oracle_nl_assemble.argtypes = [ctypes.c_void_p, dp, ctypes.c_int, dp, ctypes.c_int, ip, ctypes.c_int,
+                                         ctypes.c_int, ip, dp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int]
+        L.oracle_nl_assemble.restype = ctypes.c_int
     return _lib
 
 
@@ -603,3 +607,54 @@ def p2b_interpolant(g, field):
         u[c * nd1: c * nd1 + g.nverts] = vv[:, c]
         u[c * nd1 + g.nverts: c * nd1 + g.nverts + fn.shape[0]] = mid[:, c]
     return u
+
+
+# --------------------------------------------------------------------------
+# NonlinearForm Newton terms and the Newton loop (src/solvers.jl:519-566)
+# --------------------------------------------------------------------------
+
+NL_DIFFUSION, NL_GRAD_DIFFUSION, NL_CONVECTION = 1, 2, 3
+
+
+def nl_assemble(M, b, coords, cells, fe, ncomp, cdofs, u, kind, factor=1.0, kappa=1.0, beta=1.0,
+                bonus_quadorder=0):
+    """Adds DG(u) into the accumulator M and DG(u) u - G(u) into b."""
+    dim = coords.shape[1]
+    uu = np.ascontiguousarray(u, dtype=np.float64)
+    nq = lib().oracle_nl_assemble(M.h, _dp(b), dim, _dp(np.ascontiguousarray(coords, dtype=np.float64)),
+                                  cells.shape[0], _ip(np.ascontiguousarray(cells, dtype=np.int32)), int(fe), int(ncomp),
+                                  _ip(np.ascontiguousarray(cdofs, dtype=np.int32)), _dp(uu), int(kind), float(factor),
+                                  float(kappa), float(beta), int(bonus_quadorder))
+    if nq < 0:
+        raise RuntimeError("oracle: no rule of that order")
+    return b
+
+
+def newton_nonlinear_poisson(coords, cells, fe, cdofs, nd, f_terms, fixed, kind=NL_DIFFUSION, kappa=1.0, beta=1.0,
+                             bonus_quadorder=2, rhs_bonus=0, maxit=20, tol=1e-12, u0=None):
+    """Newton iteration of G(u) = (f, v) with homogeneous Dirichlet DoFs
+    `fixed`: each step assembles DG(u), DG(u) u - G(u) + (f, v), imposes the
+    Dirichlet DoFs in the reference's penalty form and solves with a sparse
+    LU (the reference's default linear solver); stops when the update's
+    norm drops below tol times the iterate's.  Returns (u, iterates)."""
+    import scipy.sparse.linalg as spla
+    dim = coords.shape[1]
+    f = np.zeros(nd)
+    assemble_linear(f, coords, cells, fe, 1, cdofs, RHS_POLY, np.asarray(f_terms, dtype=np.float64).ravel(), 1.0,
+                    rhs_bonus)
+    u = np.zeros(nd) if u0 is None else np.array(u0, dtype=np.float64)
+    its = []
+    for _ in range(maxit):
+        M = Matrix(nd)
+        b = f.copy()
+        nl_assemble(M, b, coords, cells, fe, 1, cdofs, u, kind, 1.0, kappa, beta, bonus_quadorder)
+        M.penalize(fixed)
+        A = M.csr().tocsc()
+        b[fixed] = 0.0
+        un = spla.spsolve(A, b)
+        its.append(un)
+        done = np.linalg.norm(un - u) <= tol * max(np.linalg.norm(un), 1e-300)
+        u = un
+        if done:
+            break
+    return u, its
