@@ -16,7 +16,8 @@ from .api import (GB300Context, Operator, CellCoefficient, LaplaceOperator, Reac
                   ReconstructionIdentityBDM1, ReconstructionIdentityRT1, ReconstructionIdentityBDM2,
                   ReconstructionDivergence, APT_BilinearForm, APT_SymmetricBilinearForm,
                   ItemIntegrator, L2ErrorIntegrator, L2NormIntegrator, L2DifferenceIntegrator,
-                  NonlinearForm, StructuralCoupling, assemble_nonlinear, solve_nonlinear)
+                  NonlinearForm, StructuralCoupling, assemble_nonlinear, solve_nonlinear,
+                  Jump, ON_CELLS, ON_IFACES, FaceVolumePower, FaceJumpIntegrator)
 from .fespace import interpolate  # noqa: F401
 from ._lib import FP64, FP32, FP64_FP32, DIRICHLET_PENALTY, DIRICHLET_ELIMINATE, GrmpError  # noqa: F401
 

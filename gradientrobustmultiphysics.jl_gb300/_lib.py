@@ -18,7 +18,7 @@ ITEM_IDENTITY, ITEM_GRADIENT = 0, 1
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "DEVICE", 4: "NOT_CONVERGED",
                 5: "UNSUPPORTED", 6: "BUDGET", 7: "TIMEOUT", 8: "NAN", 9: "NO_DEVICE"}
 
-OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV, OP_STRUCTURAL = 1, 2, 3, 4, 5
+OP_LAPLACE, OP_MASS, OP_HOOKE, OP_RDIVRDIV, OP_STRUCTURAL, OP_JUMPGRAD = 1, 2, 3, 4, 5, 6
 NL_DIFFUSION, NL_GRAD_DIFFUSION, NL_CONVECTION = 1, 2, 3
 FP64, FP32, FP64_FP32 = 0, 1, 2
 RHS_CONST, RHS_CELL, RHS_FOURIER, RHS_POLY = 0, 1, 2, 3
@@ -135,6 +135,8 @@ SIGNATURES = {
     "grmp_assemble_bilinear": ([_vp, ctypes.c_int, ctypes.POINTER(BilinearTerm), ctypes.c_int], ctypes.c_int),
     "grmp_assemble_nonlinear": ([_vp, _vp, _vp, ctypes.POINTER(NonlinearTerm), ctypes.c_int, ctypes.c_int],
                                 ctypes.c_int),
+    "grmp_item_face_jumps": ([_vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _pd, _pd],
+                             ctypes.c_int),
     "grmp_matrix_download": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64), _pi32, _pd], ctypes.c_int),
     "grmp_assemble_linear": ([_vp, ctypes.POINTER(Rhs), _vp], ctypes.c_int),
     "grmp_item_l2error": ([_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(Rhs), ctypes.c_double, ctypes.c_int, _pd, _pd],

@@ -33,6 +33,16 @@ ReconstructionIdentityRT1 = "ReconstructionIdentity{HDIVRT1}"     # Reconstructi
 ReconstructionIdentityBDM2 = "ReconstructionIdentity{HDIVBDM2}"   # ReconstructionIdentity{HDIVBDM2{2}} (H1P2B)
 ReconstructionDivergence = "ReconstructionDivergence"
 
+
+def Jump(op: str) -> str:
+    """Jump(op) of src/functionoperators.jl:187: op|T1 - op|T2 across a face."""
+    return f"Jump({op})"
+
+
+# assembly types (src/assemblypatterns.jl)
+ON_CELLS = "ON_CELLS"
+ON_IFACES = "ON_IFACES"
+
 APT_BilinearForm = "APT_BilinearForm"
 APT_SymmetricBilinearForm = "APT_SymmetricBilinearForm"
 
@@ -224,6 +234,14 @@ class Operator:
 
 
 @dataclass
+class FaceVolumePower:
+    """The item-dependent action input .* |F|^power of a face form
+    (Action((result, input, item) -> result .= input .* xFaceVolumes[item]^power),
+    examples/Example203_ReactionConvectionDiffusion2D.jl:89-91)."""
+    power: float = 2.0
+
+
+@dataclass
 class CellCoefficient:
     """An Action with "I" dependency: result = coef[cell] * input
     (the reference's Action(kernel, [d, d]; dependencies = "I"))."""
@@ -264,9 +282,21 @@ def StructuralCoupling() -> Operator:
 
 
 def BilinearForm(operators: Sequence[str], action=None, *, APT: str = APT_BilinearForm, factor: float = 1.0,
-                 name: str = "auto") -> Operator:
-    """BilinearForm([op, op], action) for the operator pairs on the hot path."""
+                 AT: str = ON_CELLS, bonus_quadorder: int = 0, name: str = "auto") -> Operator:
+    """BilinearForm([op, op], action) for the operator pairs on the hot path;
+    AT = ON_IFACES with [Jump(Gradient), Jump(Gradient)] and a FaceVolumePower
+    action (or none: power 0) is the interior-face gradient-jump form."""
     ops = tuple(operators)
+    if AT == ON_IFACES:
+        if ops != (Jump(Gradient), Jump(Gradient)):
+            raise ValueError(f"face form {ops} is not on the GPU path")
+        if action is not None and not isinstance(action, FaceVolumePower):
+            raise ValueError("face forms take a FaceVolumePower action")
+        power = action.power if action is not None else 0.0
+        return Operator(L.OP_JUMPGRAD, True, factor, params=(power, 0.0, 0.0, 0.0), bonus_quadorder=bonus_quadorder,
+                        name=name)
+    if AT != ON_CELLS:
+        raise ValueError(f"assembly type {AT} is not on the GPU path")
     sym = APT == APT_SymmetricBilinearForm
     cc = action.values if isinstance(action, CellCoefficient) else None
     bonus = action.bonus_quadorder if isinstance(action, CellCoefficient) else 0
@@ -398,6 +428,8 @@ class FEMatrix:
         self.operators = list(operators)
         self.name = name
         sh = ctx.space(FES)
+        if any(o.op_kind == L.OP_JUMPGRAD for o in self.operators):
+            ctx.mesh(FES.xgrid, with_faces=True)   # face terms need the mesh's faces
         self.h = ctypes.c_void_p()
         ctx.check(ctx.lib.grmp_pattern_build(sh, len(self.operators), _terms(self.operators), ctypes.byref(self.h)))
 
@@ -589,6 +621,36 @@ def solve_nonlinear(ctx: "GB300Context", FES, operators, form: NonlinearForm, rh
     finally:
         for v in (A, f, b, u, x):
             v.free()
+
+
+# ----------------------------------------------------------------------- face integrators
+@dataclass
+class FaceJumpIntegrator:
+    """ItemIntegrator([Jump(Gradient)], action; AT = ON_IFACES): per interior
+    face factor |F| |F|^power int_F g with g = ([grad u].n_F)^2 (normal=True,
+    the jump part of the estimator of
+    examples/Example210_PoissonLshapeAdaptive2D.jl:58-75, power 1) or
+    |[grad u]|^2 -- grmp_item_face_jumps."""
+    normal: bool = True
+    power: float = 1.0
+    factor: float = 1.0
+    bonus_quadorder: int = 0
+
+    def evaluate_faces(self, u: "FEVector") -> np.ndarray:
+        ctx = u.ctx
+        g = u.FES.xgrid
+        ctx.mesh(g, with_faces=True)
+        out = np.zeros(g.faces()[0].shape[0])
+        tot = ctypes.c_double()
+        ctx.check(ctx.lib.grmp_item_face_jumps(ctx.space(u.FES), u.h, 1 if self.normal else 0, float(self.power),
+                                               float(self.factor), int(self.bonus_quadorder), _dp(out),
+                                               ctypes.byref(tot)))
+        self.last_total = tot.value
+        return out
+
+    def evaluate(self, u: "FEVector") -> float:
+        self.evaluate_faces(u)
+        return self.last_total
 
 
 # ----------------------------------------------------------------------- item integrators

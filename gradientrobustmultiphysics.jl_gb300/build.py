@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libgrmp_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cpp", "tables.cpp", "server.cpp", "nd_symbolic.cpp", "pattern.cu", "assemble.cu", "br.cu", "solve.cu",
            "batch.cu", "multifrontal.cu", "integrate.cu", "br3.cu", "topology.cu", "duo.cpp", "import.cu",
-           "p2b.cu", "nonlinear.cu"]
+           "p2b.cu", "nonlinear.cu", "faces.cu"]
 
 
 def nvcc() -> str:

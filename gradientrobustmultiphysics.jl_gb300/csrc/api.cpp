@@ -172,6 +172,9 @@ int grmp_mesh_set_faces(grmp_mesh m, int32_t nfaces, const int32_t *cell_faces, 
     grmp_free(ctx, m->d_face_normals, (size_t)m->nfaces * m->dim * 8);
     grmp_free(ctx, m->d_face_volumes, (size_t)m->nfaces * 8);
     grmp_free(ctx, m->d_cell_face_signs, nl);
+    grmp_free(ctx, m->d_cell_nbr, nl * 4);
+    grmp_free(ctx, m->d_face_cells, (size_t)m->nfaces * 8);
+    m->d_cell_nbr = m->d_face_cells = nullptr;
     m->nfaces = nfaces;
     int rc = grmp_upload(ctx, &m->d_cell_faces, cell_faces, nl);
     if (!rc) rc = grmp_upload(ctx, &m->d_face_normals, face_normals, (size_t)nfaces * m->dim);
@@ -192,6 +195,8 @@ int grmp_mesh_destroy(grmp_mesh m) {
     grmp_free(ctx, m->d_face_normals, (size_t)m->nfaces * m->dim * 8);
     grmp_free(ctx, m->d_face_volumes, (size_t)m->nfaces * 8);
     grmp_free(ctx, m->d_cell_face_signs, nl);
+    grmp_free(ctx, m->d_cell_nbr, nl * 4);
+    grmp_free(ctx, m->d_face_cells, (size_t)m->nfaces * 8);
     cudaStreamSynchronize(ctx->stream);
     delete m;
     return GRMP_OK;

@@ -585,9 +585,17 @@ int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_t
     }
     int dim = s->mesh->dim, nb = s->nb, nc = s->ncomp;
     // pattern-only terms contribute nothing to the values
-    std::vector<grmp_bilinear_term> kept;
-    for (int i = 0; i < nterms; i++)
-        if (terms[i].op_kind != GRMP_OP_STRUCTURAL) kept.push_back(terms[i]);
+    // (and face terms are added after the cell terms)
+    std::vector<grmp_bilinear_term> kept, faceterms;
+    for (int i = 0; i < nterms; i++) {
+        if (terms[i].op_kind == GRMP_OP_JUMPGRAD) faceterms.push_back(terms[i]);
+        else if (terms[i].op_kind != GRMP_OP_STRUCTURAL) kept.push_back(terms[i]);
+    }
+    if (!faceterms.empty()) {
+        const int rc0 = grmp_assemble_bilinear_impl(A, (int)kept.size(), kept.data(), precision);
+        if (rc0) return rc0;
+        return grmp_face_assemble(A, (int)faceterms.size(), faceterms.data(), precision);
+    }
     nterms = (int)kept.size();
     terms = kept.data();
     if (nterms == 0) {   // only pattern terms: every value is zero

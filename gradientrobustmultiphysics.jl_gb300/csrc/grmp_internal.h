@@ -45,6 +45,9 @@ struct grmp_mesh_s {
     double *d_face_normals = nullptr;
     double *d_face_volumes = nullptr;
     int8_t *d_cell_face_signs = nullptr;
+    // cell adjacency across faces (built on first use by face terms)
+    int32_t *d_cell_nbr = nullptr;    // [ncells][dim+1] cell across local face f, -1 on the boundary
+    int32_t *d_face_cells = nullptr;  // [nfaces][2] adjacent cells (lower id first), -1 if none
 };
 
 struct grmp_space_s {
@@ -184,6 +187,8 @@ int grmp_pattern_build_impl(grmp_space space, int nterms, const grmp_bilinear_te
 int grmp_assemble_bilinear_impl(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
 int grmp_assemble_nonlinear_impl(grmp_matrix A, grmp_vector b, grmp_vector u, const grmp_nonlinear_term *term,
                                  int precision, int add);
+int grmp_mesh_neighbors(grmp_mesh m);   // d_cell_nbr / d_face_cells (needs face data)
+int grmp_face_assemble(grmp_matrix A, int nterms, const grmp_bilinear_term *terms, int precision);
 int grmp_assemble_linear_impl(grmp_space space, const grmp_rhs *rhs, grmp_vector b);
 int grmp_item_l2error_impl(grmp_space s, grmp_vector u, grmp_vector v, int op, const grmp_rhs *data, double factor,
                            int quadorder, double *cell_values, double *total);

@@ -198,7 +198,7 @@ __global__ void k_nzmask(int ncells, const double *coords, const int32_t *cells,
     double cv[16][LD][RD];
     for (int ti = 0; ti < terms.n; ti++) {
         const TermDev &t = terms.t[ti];
-        if (t.op == GRMP_OP_STRUCTURAL) {   // every local pair
+        if (t.op == GRMP_OP_STRUCTURAL || t.op == GRMP_OP_JUMPGRAD) {   // every local pair
             for (int i = 0; i < LD; i++) m[i] = LD >= 32 ? ~0u : ((1u << LD) - 1u);
             continue;
         }
@@ -228,9 +228,37 @@ __global__ void k_nzmask(int ncells, const double *coords, const int32_t *cells,
 
 // ------------------------------------------------------------------ rows
 // Sorted unique column list of one row from its incidences and the mask.
+// With face terms (nbr != nullptr) the row also holds every DoF of the cells
+// across the faces of its cells.
+__device__ __forceinline__ bool list_insert(int32_t *list, int &n, int32_t col, int *overflow) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (list[mid] < col) lo = mid + 1; else hi = mid;
+    }
+    if (lo < n && list[lo] == col) return true;
+    if (n >= GRMP_MAX_ROW_NNZ) {
+        *overflow = 1;
+        return false;
+    }
+    for (int k = n; k > lo; k--) list[k] = list[k - 1];
+    list[lo] = col;
+    n++;
+    return true;
+}
+
 __device__ int row_columns(int row, const int32_t *inc_ptr, const int32_t *inc_cell, const uint8_t *inc_loc,
-                           const uint32_t *mask, const int32_t *celldofs, int ld, int32_t *list, int *overflow) {
+                           const uint32_t *mask, const int32_t *celldofs, int ld, const int32_t *nbr, int nf,
+                           int32_t *list, int *overflow) {
     int n = 0;
+    if (nbr)
+        for (int p = inc_ptr[row]; p < inc_ptr[row + 1]; p++)
+            for (int f = 0; f < nf; f++) {
+                const int c2 = nbr[(size_t)inc_cell[p] * nf + f];
+                if (c2 < 0) continue;
+                for (int b = 0; b < ld; b++)
+                    if (!list_insert(list, n, celldofs[(size_t)c2 * ld + b], overflow)) return n;
+            }
     for (int p = inc_ptr[row]; p < inc_ptr[row + 1]; p++) {
         int cell = inc_cell[p], a = inc_loc[p];
         uint32_t bits = mask[(size_t)cell * ld + a];
@@ -258,24 +286,24 @@ __device__ int row_columns(int row, const int32_t *inc_ptr, const int32_t *inc_c
 }
 
 __global__ void k_row_count(int32_t nrows, const int32_t *inc_ptr, const int32_t *inc_cell, const uint8_t *inc_loc,
-                            const uint32_t *mask, const int32_t *celldofs, int ld, int32_t *cnt, int32_t *maxcnt,
-                            int *overflow) {
+                            const uint32_t *mask, const int32_t *celldofs, int ld, const int32_t *nbr, int nf,
+                            int32_t *cnt, int32_t *maxcnt, int *overflow) {
     int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= nrows) return;
     int32_t list[GRMP_MAX_ROW_NNZ];
-    int n = row_columns(row, inc_ptr, inc_cell, inc_loc, mask, celldofs, ld, list, overflow);
+    int n = row_columns(row, inc_ptr, inc_cell, inc_loc, mask, celldofs, ld, nbr, nf, list, overflow);
     cnt[row] = n;
     atomicMax(maxcnt, n);
 }
 
 template <typename S>
 __global__ void k_row_fill(int32_t nrows, const int32_t *inc_ptr, const int32_t *inc_cell, const uint8_t *inc_loc,
-                           const uint32_t *mask, const int32_t *celldofs, int ld, const int32_t *rowptr, int32_t *cols,
-                           S *slot, int *overflow) {
+                           const uint32_t *mask, const int32_t *celldofs, int ld, const int32_t *nbr, int nf,
+                           const int32_t *rowptr, int32_t *cols, S *slot, int *overflow) {
     int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= nrows) return;
     int32_t list[GRMP_MAX_ROW_NNZ];
-    int n = row_columns(row, inc_ptr, inc_cell, inc_loc, mask, celldofs, ld, list, overflow);
+    int n = row_columns(row, inc_ptr, inc_cell, inc_loc, mask, celldofs, ld, nbr, nf, list, overflow);
     int32_t base = rowptr[row];
     for (int k = 0; k < n; k++) cols[base + k] = list[k];
     const S DROP = (S)~(S)0;
@@ -389,7 +417,7 @@ int grmp_prepare_terms(grmp_space s, int nterms, const grmp_bilinear_term *terms
         d.lambda = t.param[1];
         d.cell_coef = nullptr;
         int deriv;
-        if (t.op_kind == GRMP_OP_LAPLACE) deriv = 1;
+        if (t.op_kind == GRMP_OP_LAPLACE || t.op_kind == GRMP_OP_JUMPGRAD) deriv = 1;
         else if (t.op_kind == GRMP_OP_MASS || t.op_kind == GRMP_OP_STRUCTURAL) deriv = 0;
         else if (t.op_kind == GRMP_OP_HOOKE) {
             deriv = 1;
@@ -493,6 +521,20 @@ int grmp_pattern_build_impl(grmp_space s, int nterms, const grmp_bilinear_term *
         grmp_release(ctx, keep);
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "pattern: element layout dim=%d nb=%d nc=%d", dim, nb, nc);
     }
+    // face terms couple the DoFs of face neighbours
+    const int32_t *nbr = nullptr;
+    bool faces = false;
+    for (int i = 0; i < nterms; i++) faces = faces || terms[i].op_kind == GRMP_OP_JUMPGRAD;
+    if (faces) {
+        if (s->fe == GRMP_FE_H1BR || s->ncomp != 1) rc = grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "face terms: scalar H1P1 / H1P2");
+        if (!rc) rc = grmp_mesh_neighbors(s->mesh);
+        if (rc) {
+            grmp_free(ctx, mask, ncl * 4);
+            grmp_release(ctx, keep);
+            return rc;
+        }
+        nbr = s->mesh->d_cell_nbr;
+    }
     grmp_matrix A = new grmp_matrix_s();
     A->space = s;
     A->nrows = s->ndofs;
@@ -509,7 +551,8 @@ int grmp_pattern_build_impl(grmp_space s, int nterms, const grmp_bilinear_term *
         cudaMemsetAsync(dmax, 0, 4, ctx->stream);
         cudaMemsetAsync(dovf, 0, 4, ctx->stream);
         k_row_count<<<nblk(A->nrows, 128), 128, 0, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
-                                                                 mask, s->d_celldofs, ld, cnt, dmax, dovf);
+                                                                 mask, s->d_celldofs, ld, nbr, dim + 1, cnt, dmax,
+                                                                 dovf);
         GRMP_LAUNCHED(ctx);
         rc = grmp_scan_i32(ctx, cnt, A->d_rowptr, A->nrows + 1, &total);
     }
@@ -530,12 +573,12 @@ int grmp_pattern_build_impl(grmp_space s, int nterms, const grmp_bilinear_term *
     if (!rc) {
         if (A->slot_bytes == 1)
             k_row_fill<uint8_t><<<nblk(A->nrows, 128), 128, 0, ctx->stream>>>(
-                A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, mask, s->d_celldofs, ld, A->d_rowptr, A->d_cols,
-                (uint8_t *)A->d_slot, dovf);
+                A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, mask, s->d_celldofs, ld, nbr, dim + 1,
+                A->d_rowptr, A->d_cols, (uint8_t *)A->d_slot, dovf);
         else
             k_row_fill<uint16_t><<<nblk(A->nrows, 128), 128, 0, ctx->stream>>>(
-                A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, mask, s->d_celldofs, ld, A->d_rowptr, A->d_cols,
-                (uint16_t *)A->d_slot, dovf);
+                A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, mask, s->d_celldofs, ld, nbr, dim + 1,
+                A->d_rowptr, A->d_cols, (uint16_t *)A->d_slot, dovf);
         GRMP_LAUNCHED(ctx);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

@@ -326,6 +326,28 @@ int grmp_fe_ldofs(int fe, int dim, int ncomp) {
 int grmp_quadrature(int dim, int order, double (*x)[3], double *w) {
     std::memset(x, 0, sizeof(double) * 3 * GRMP_MAXQ);
     if (order < 0) order = 0;
+    if (dim == 1) {   // src/quadrature.jl:130-148: midpoint, Simpson, then Gauss-Legendre
+        if (order <= 1) {
+            x[0][0] = 0.5;
+            w[0] = 1.0;
+            return 1;
+        }
+        if (order == 2) {
+            x[0][0] = 0.0, x[1][0] = 0.5, x[2][0] = 1.0;
+            w[0] = 1.0 / 6.0, w[1] = 2.0 / 3.0, w[2] = 1.0 / 6.0;
+            return 3;
+        }
+        const int n = order / 2 + 1;
+        if (n > 16) return 0;
+        double dg[16] = {0}, of[16], r[16], v1[16];
+        for (int i = 1; i < n; i++) of[i - 1] = i / std::sqrt(4.0 * i * i - 1.0);
+        tridiag_eig(n, dg, of, r, v1);
+        for (int i = 0; i < n; i++) {
+            x[i][0] = 0.5 * r[i] + 0.5;
+            w[i] = 0.5 * (2.0 * v1[i] * v1[i]);
+        }
+        return n;
+    }
     if (dim == 2) {
         if (order <= 1) {
             x[0][0] = x[0][1] = 1.0 / 3.0;

@@ -371,6 +371,9 @@ int grmp_mesh_build_faces(grmp_mesh m) {
     grmp_free(ctx, m->d_face_normals, (size_t)m->nfaces * dim * 8);
     grmp_free(ctx, m->d_face_volumes, (size_t)m->nfaces * 8);
     grmp_free(ctx, m->d_cell_face_signs, (size_t)n);
+    grmp_free(ctx, m->d_cell_nbr, (size_t)n * 4);
+    grmp_free(ctx, m->d_face_cells, (size_t)m->nfaces * 8);
+    m->d_cell_nbr = m->d_face_cells = nullptr;
     m->nfaces = nf;
     m->d_cell_faces = cf;
     m->d_face_normals = nrm;

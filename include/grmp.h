@@ -179,8 +179,15 @@ typedef enum {
                               src/feevaluator_h1.jl:409-437); iterated-penalty term.  In 3D the RT0
                               basis is mapped with A phi / |det A| (times the cell-face sign), so
                               div R u is the cell mean of div u on tetrahedra of either orientation */
-    GRMP_OP_STRUCTURAL = 5 /* pattern only: couples every local pair of a cell (the Jacobian of a
+    GRMP_OP_STRUCTURAL = 5, /* pattern only: couples every local pair of a cell (the Jacobian of a
                               NonlinearForm fills them all); contributes nothing to assembled values */
+    GRMP_OP_JUMPGRAD = 6   /* BilinearForm([Jump(Gradient), Jump(Gradient)], Action(input |F|^param[0]);
+                              AT = ON_IFACES) times factor: factor |F| |F|^p int_F [grad u].[grad v]
+                              summed over interior faces (the interior-penalty stabilisation of
+                              examples/Example203_ReactionConvectionDiffusion2D.jl:89-92; jumps as in
+                              update_dii4op!, src/assemblypatterns.jl:103-153).  Scalar H1P1 / H1P2;
+                              needs the mesh's faces; the pattern then holds the DoFs of face
+                              neighbours; added after the cell terms, FP64 (FP32 values rounded) */
 } grmp_op_kind;
 
 /* One operator term.  Assembly of a list of terms adds them into one matrix,
@@ -359,6 +366,15 @@ typedef enum { GRMP_ITEM_IDENTITY = 0, GRMP_ITEM_GRADIENT = 1 } grmp_item_operat
  * reproducible run to run (fixed summation order). */
 int grmp_item_l2error(grmp_space space, grmp_vector u, grmp_vector v, int op, const grmp_rhs *data, double factor,
                       int quadorder, double *cell_values, double *total);
+
+/* ItemIntegrator([Jump(Gradient)], action; AT = ON_IFACES): per interior face
+ * factor |F| |F|^power int_F g, g = |[grad u]|^2 (kind 0) or ([grad u].n_F)^2
+ * (kind 1, the jump term of examples/Example210_PoissonLshapeAdaptive2D.jl:58-75
+ * with power 1); boundary faces give 0.  face_values [nfaces] (optional,
+ * host) and their sum in ascending face order (optional).  Scalar H1P1 /
+ * H1P2; needs the mesh's faces. */
+int grmp_item_face_jumps(grmp_space space, grmp_vector u, int kind, double power, double factor, int bonus_quadorder,
+                         double *face_values, double *total);
 
 /* -------------------------------------------------------------- vectors */
 

@@ -2449,3 +2449,205 @@ int oracle_nl_assemble(void *h, double *b, int dim, const double *coords, int nc
     free(vals); free(derivs); free(in); free(cvid); free(cvt); free(lm); free(lb);
     return nq;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Interior-face terms with Jump(Gradient) (src/assemblypatterns.jl:103-153)  */
+/* ------------------------------------------------------------------------- */
+
+/* Local vertices of face f of a simplex (the mesh module's numbering). */
+static int or_face_vertex(int dim, int f, int k)
+{
+    static const int t3[4][3] = {{0, 1, 2}, {0, 1, 3}, {1, 2, 3}, {0, 2, 3}};
+    return dim == 2 ? (f + k) % 3 : t3[f][k];
+}
+
+/* Face quadrature points as reference coordinates of `cell`: barycentric
+ * weights over the face's vertices in ascending global vertex order. */
+static void or_face_points(int dim, const int *cells, int cell, int f, int nq, const double *lam, double *xh)
+{
+    int loc[3], gid[3];
+    for (int k = 0; k < dim; k++) { loc[k] = or_face_vertex(dim, f, k); gid[k] = cells[(size_t)cell * (dim + 1) + loc[k]]; }
+    for (int i = 1; i < dim; i++)
+        for (int j = i; j > 0 && gid[j] < gid[j - 1]; j--) {
+            int t = gid[j]; gid[j] = gid[j - 1]; gid[j - 1] = t;
+            t = loc[j]; loc[j] = loc[j - 1]; loc[j - 1] = t;
+        }
+    for (int q = 0; q < nq; q++)
+        for (int j = 0; j < dim; j++) {
+            double s = 0.0;
+            for (int k = 0; k < dim; k++) s += loc[k] == j + 1 ? lam[q * 3 + k] : 0.0;
+            xh[q * 3 + j] = s;
+        }
+}
+
+static int or_face_rule(int dim, int order, double *lam, double *w)
+{
+    double xr[3 * OR_MAXQ];
+    int nq = oracle_qrule(dim - 1, order, xr, w);
+    if (nq < 0) nq = -nq;
+    for (int q = 0; q < nq; q++) {
+        if (dim == 2) { lam[q * 3] = 1.0 - xr[3 * q]; lam[q * 3 + 1] = xr[3 * q]; lam[q * 3 + 2] = 0.0; }
+        else {
+            lam[q * 3] = 1.0 - xr[3 * q] - xr[3 * q + 1];
+            lam[q * 3 + 1] = xr[3 * q];
+            lam[q * 3 + 2] = xr[3 * q + 1];
+        }
+    }
+    return nq;
+}
+
+/* physical gradients g[a*3 + k] of the scalar basis at reference point xh */
+static int or_grads(int fe, int dim, const double *xh, double G[3][3], double *g)
+{
+    dual x[3], o[10];
+    for (int j = 0; j < 3; j++) x[j] = dvar(j < dim ? xh[j] : 0.0, j);
+    const int nb = h1_scalar_basis(fe, dim, x, o);
+    for (int a = 0; a < nb; a++)
+        for (int k = 0; k < dim; k++) {
+            double s = 0;
+            for (int j = 0; j < dim; j++) s += G[k][j] * o[a].d[j];
+            g[a * 3 + k] = s;
+        }
+    return nb;
+}
+
+/* face -> (lower cell, higher cell or -1), registered in ascending cell order */
+static void or_face_cells(int dim, int ncells, const int *cell_faces, int nfaces, int *fc)
+{
+    for (int F = 0; F < 2 * nfaces; F++) fc[F] = -1;
+    for (int c = 0; c < ncells; c++)
+        for (int f = 0; f <= dim; f++) {
+            const int F = cell_faces[(size_t)c * (dim + 1) + f];
+            if (fc[2 * F] < 0) fc[2 * F] = c; else fc[2 * F + 1] = c;
+        }
+}
+
+/* factor |F| |F|^power sum_q w_q [grad phi_a].[grad phi_b] over the 2 x ld
+ * functions of the two cells of every interior face (jump coefficient +1 on
+ * the lower cell, -1 on the other; ascending faces; exact zeros skipped). */
+int oracle_face_jumpgrad(void *h, int dim, const double *coords, int ncells, const int *cells, const int *cell_faces,
+                         int nfaces, int fe, const int *celldofs, double factor, double power, int bonus_quadorder)
+{
+    omat *M = (omat *)h;
+    const int p = (fe == OR_FE_P1) ? 1 : 2;
+    const int nb = (fe == OR_FE_P1) ? dim + 1 : (dim == 2 ? 6 : 10);
+    int order = 2 * (p - 1) + bonus_quadorder;
+    double lam[3 * OR_MAXQ], w[OR_MAXQ];
+    const int nq = or_face_rule(dim, order < 0 ? 0 : order, lam, w);
+    if (nq <= 0) return -1;
+    int *fc = (int *)malloc(sizeof(int) * 2 * (size_t)nfaces);
+    or_face_cells(dim, ncells, cell_faces, nfaces, fc);
+    double *xh = (double *)malloc(sizeof(double) * 3 * (size_t)nq);
+    double *g = (double *)malloc(sizeof(double) * (size_t)nq * 2 * nb * 3);
+    for (int F = 0; F < nfaces; F++) {
+        const int c[2] = {fc[2 * F], fc[2 * F + 1]};
+        if (c[1] < 0) continue;
+        double fvol = 0;
+        for (int side = 0; side < 2; side++) {
+            int f = 0;
+            for (int k = 0; k <= dim; k++) if (cell_faces[(size_t)c[side] * (dim + 1) + k] == F) f = k;
+            double X[12], A[3][3], G[3][3], det, vol;
+            for (int v = 0; v <= dim; v++)
+                for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cells[(size_t)c[side] * (dim + 1) + v] * dim + k];
+            oracle_geometry(dim, X, A, G, &det, &vol);
+            or_face_points(dim, cells, c[side], f, nq, lam, xh);
+            const double sgn = side == 0 ? 1.0 : -1.0;
+            for (int q = 0; q < nq; q++) {
+                double gq[30];
+                or_grads(fe, dim, xh + 3 * q, G, gq);
+                for (int a = 0; a < nb; a++)
+                    for (int k = 0; k < 3; k++) g[((size_t)q * 2 * nb + side * nb + a) * 3 + k] = k < dim ? sgn * gq[a * 3 + k] : 0.0;
+            }
+            if (side == 0) {
+                /* face measure from the face's vertices */
+                double P[3][3];
+                for (int k = 0; k < dim; k++)
+                    for (int j = 0; j < dim; j++) P[k][j] = coords[(size_t)cells[(size_t)c[0] * (dim + 1) + or_face_vertex(dim, f, k)] * dim + j];
+                if (dim == 2) fvol = sqrt((P[1][0] - P[0][0]) * (P[1][0] - P[0][0]) + (P[1][1] - P[0][1]) * (P[1][1] - P[0][1]));
+                else {
+                    double u[3], v[3];
+                    for (int j = 0; j < 3; j++) { u[j] = P[1][j] - P[0][j]; v[j] = P[2][j] - P[0][j]; }
+                    double cx = u[1] * v[2] - u[2] * v[1], cy = u[2] * v[0] - u[0] * v[2], cz = u[0] * v[1] - u[1] * v[0];
+                    fvol = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+                }
+            }
+        }
+        double act = 1.0;
+        for (int i = 0; i < (int)power; i++) act *= fvol;
+        if ((double)(int)power != power) act = pow(fvol, power);
+        const double itemfactor = fvol * factor;
+        for (int a = 0; a < 2 * nb; a++)
+            for (int b = 0; b < 2 * nb; b++) {
+                double lm = 0;
+                for (int q = 0; q < nq; q++) {
+                    double t = 0;
+                    for (int k = 0; k < dim; k++) t += (act * g[((size_t)q * 2 * nb + a) * 3 + k]) * g[((size_t)q * 2 * nb + b) * 3 + k];
+                    lm += t * w[q];
+                }
+                const int ra = celldofs[(size_t)c[a / nb] * nb + a % nb], rb = celldofs[(size_t)c[b / nb] * nb + b % nb];
+                omat_addnz(M, ra, rb, lm, itemfactor);
+            }
+    }
+    free(fc); free(xh); free(g);
+    return nq;
+}
+
+/* per interior face: factor |F| |F|^power sum_q w_q g(q), g = |[grad u]|^2
+ * (kind 0) or ([grad u].n)^2 (kind 1); boundary faces 0.  fnormals /
+ * fvolumes: the mesh's face data. */
+int oracle_face_jumps(int dim, const double *coords, int ncells, const int *cells, const int *cell_faces, int nfaces,
+                      const double *fnormals, const double *fvolumes, int fe, const int *celldofs, const double *u,
+                      int kind, double power, double factor, int bonus_quadorder, double *out)
+{
+    const int p = (fe == OR_FE_P1) ? 1 : 2;
+    const int nb = (fe == OR_FE_P1) ? dim + 1 : (dim == 2 ? 6 : 10);
+    int order = 2 * (p - 1) + bonus_quadorder;
+    double lam[3 * OR_MAXQ], w[OR_MAXQ];
+    const int nq = or_face_rule(dim, order < 0 ? 0 : order, lam, w);
+    if (nq <= 0) return -1;
+    int *fc = (int *)malloc(sizeof(int) * 2 * (size_t)nfaces);
+    or_face_cells(dim, ncells, cell_faces, nfaces, fc);
+    double *xh = (double *)malloc(sizeof(double) * 3 * (size_t)nq);
+    double *J = (double *)malloc(sizeof(double) * 3 * (size_t)nq);
+    for (int F = 0; F < nfaces; F++) {
+        out[F] = 0.0;
+        const int c[2] = {fc[2 * F], fc[2 * F + 1]};
+        if (c[1] < 0) continue;
+        for (int i = 0; i < 3 * nq; i++) J[i] = 0.0;
+        for (int side = 0; side < 2; side++) {
+            int f = 0;
+            for (int k = 0; k <= dim; k++) if (cell_faces[(size_t)c[side] * (dim + 1) + k] == F) f = k;
+            double X[12], A[3][3], G[3][3], det, vol;
+            for (int v = 0; v <= dim; v++)
+                for (int k = 0; k < dim; k++) X[v * dim + k] = coords[(size_t)cells[(size_t)c[side] * (dim + 1) + v] * dim + k];
+            oracle_geometry(dim, X, A, G, &det, &vol);
+            or_face_points(dim, cells, c[side], f, nq, lam, xh);
+            for (int q = 0; q < nq; q++) {
+                double gq[30];
+                or_grads(fe, dim, xh + 3 * q, G, gq);
+                for (int a = 0; a < nb; a++) {
+                    const double ua = u[celldofs[(size_t)c[side] * nb + a]];
+                    for (int k = 0; k < dim; k++) J[3 * q + k] += (side == 0 ? ua : -ua) * gq[a * 3 + k];
+                }
+            }
+        }
+        double acc = 0.0;
+        for (int q = 0; q < nq; q++) {
+            double val = 0.0;
+            if (kind == 1) {
+                double jn = 0.0;
+                for (int k = 0; k < dim; k++) jn += J[3 * q + k] * fnormals[(size_t)F * dim + k];
+                val = jn * jn;
+            } else
+                for (int k = 0; k < dim; k++) val += J[3 * q + k] * J[3 * q + k];
+            acc += w[q] * val;
+        }
+        const double fv = fvolumes[F];
+        double act = 1.0;
+        for (int i = 0; i < (int)power; i++) act *= fv;
+        if ((double)(int)power != power) act = pow(fv, power);
+        out[F] = acc * act * fv * factor;
+    }
+    free(fc); free(xh); free(J);
+    return nq;
+}

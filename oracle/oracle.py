@@ -118,6 +118,12 @@ def lib():
                                          ctypes.c_int, ip, dp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_int]
         L.oracle_nl_assemble.restype = ctypes.c_int
+        L.oracle_face_jumpgrad.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_int, ip, ip, ctypes.c_int,
+                                           ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.oracle_face_jumpgrad.restype = ctypes.c_int
+        L.oracle_face_jumps.argtypes = [ctypes.c_int, dp, ctypes.c_int, ip, ip, ctypes.c_int, dp, dp, ctypes.c_int,
+                                        ip, dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, dp]
+        L.oracle_face_jumps.restype = ctypes.c_int
     return _lib
 
 
@@ -658,3 +664,37 @@ def newton_nonlinear_poisson(coords, cells, fe, cdofs, nd, f_terms, fixed, kind=
         if done:
             break
     return u, its
+
+
+# --------------------------------------------------------------------------
+# Interior-face terms with Jump(Gradient)
+# --------------------------------------------------------------------------
+
+def face_jumpgrad(M, g, fe, cdofs, factor=1.0, power=2.0, bonus_quadorder=0):
+    """Adds factor |F| |F|^power int_F [grad u].[grad v] over interior faces to M."""
+    fn, cf = g.faces()
+    nq = lib().oracle_face_jumpgrad(M.h, g.dim, _dp(np.ascontiguousarray(g.coords, dtype=np.float64)), g.ncells,
+                                    _ip(np.ascontiguousarray(g.cells, dtype=np.int32)),
+                                    _ip(np.ascontiguousarray(cf, dtype=np.int32)), fn.shape[0], int(fe),
+                                    _ip(np.ascontiguousarray(cdofs, dtype=np.int32)), float(factor), float(power),
+                                    int(bonus_quadorder))
+    if nq < 0:
+        raise RuntimeError("oracle: no face rule of that order")
+
+
+def face_jumps(g, fe, cdofs, u, kind=1, power=1.0, factor=1.0, bonus_quadorder=0):
+    """Per-face values of the Jump(Gradient) ItemIntegrator (0 on boundary faces)."""
+    fn, cf = g.faces()
+    nrm, fv, sg = g.face_geometry()
+    out = np.zeros(fn.shape[0])
+    nq = lib().oracle_face_jumps(g.dim, _dp(np.ascontiguousarray(g.coords, dtype=np.float64)), g.ncells,
+                                 _ip(np.ascontiguousarray(g.cells, dtype=np.int32)),
+                                 _ip(np.ascontiguousarray(cf, dtype=np.int32)), fn.shape[0],
+                                 _dp(np.ascontiguousarray(nrm, dtype=np.float64)),
+                                 _dp(np.ascontiguousarray(fv, dtype=np.float64)), int(fe),
+                                 _ip(np.ascontiguousarray(cdofs, dtype=np.int32)),
+                                 _dp(np.ascontiguousarray(u, dtype=np.float64)), int(kind), float(power), float(factor),
+                                 int(bonus_quadorder), _dp(out))
+    if nq < 0:
+        raise RuntimeError("oracle: no face rule of that order")
+    return out
