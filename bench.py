@@ -633,7 +633,8 @@ def run_extras(args) -> dict:
     a.workload, a.steps, a.warmup, a.dim, a.nprob = "stokes-batch", 3, 3, 2, 2048
     st = run_stokes(a, emit=False)
     out["stokes_BR_P0_batch2048"] = {k: st[k] for k in ("value", "unit", "ms_per_step", "config", "solver",
-                                                        "rel_err_vs_oracle", "cpu_baseline", "latency_ms")}
+                                                        "rel_err_vs_oracle", "cpu_baseline", "latency_ms",
+                                                        "mixed_direct", "mixed_vs_plain")}
     out["stokes_BR_P0_batch2048"]["wall_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     a = copy.copy(args)
@@ -695,6 +696,31 @@ def run_stokes(args, emit: bool = True):
     clocks = clk.stop()
     tot = dist.max(sum(ms) / 1e3)
     value = ndofs * dist.ws * args.steps / tot
+    u_direct, p_direct = sysd.velocity().copy(), sysd.pressure().copy()
+    # the mixed option: an FP32 factor per problem preconditioning FP64 CG
+    # (FP64 factor as the per-problem fallback), one warm-up and one timed step
+    sysm = S.StokesBatchSystem(ctx, prob, solver="mixed_direct")
+    mixed_line = None
+    for rep in range(2):
+        sysm.assemble()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stm = sysm.solve(sweeps=args.sweeps, reltol=args.stokes_reltol, maxiter=1, sweep_tol=0.0,
+                         raise_on_error=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ctx.check(stm["rc"])
+        mms = e0.elapsed_time(e1)
+    um, pm = sysm.velocity(), sysm.pressure()
+    ro, co = prob.V.row_offsets, prob.mesh.cell_offsets
+    dmax = max(max(np.linalg.norm(um[ro[k]:ro[k + 1]] - u_direct[ro[k]:ro[k + 1]]) /
+                   max(np.linalg.norm(u_direct[ro[k]:ro[k + 1]]), 1e-300),
+                   np.linalg.norm(pm[co[k]:co[k + 1]] - p_direct[co[k]:co[k + 1]]) /
+                   max(np.linalg.norm(p_direct[co[k]:co[k + 1]]), 1e-300)) for k in range(prob.nproblems))
+    mixed_line = {"value": ndofs / (mms / 1e3), "ms_per_step": mms, "fp64_fallbacks": stm["fp64_fallbacks"],
+                  "cg_iterations_total": int(stm["total_iterations"]), "max_rel_diff_vs_fp64_direct": float(dmax),
+                  "solver": "FP32 multifrontal factor per problem preconditioning FP64 CG (FP64 factor fallback)"}
+    del sysm
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -709,7 +735,7 @@ def run_stokes(args, emit: bool = True):
             uo_s[k] = O.stokes_iterated_penalty(g, prob.nus[k], prob.lam, prob.terms[k], sweeps=args.sweeps)
             dd += (prob.V.row_offsets[k + 1] - prob.V.row_offsets[k]) + g.ncells
         dt = time.perf_counter() - t0
-        u_g, p_g = sysd.velocity(), sysd.pressure()
+        u_g, p_g = u_direct, p_direct
         eu, ep = [], []
         for k, (uo, po, _) in uo_s.items():
             r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
@@ -733,6 +759,8 @@ def run_stokes(args, emit: bool = True):
                        "solver": "FP64 multifrontal Cholesky per problem, factored once per step"},
             "latency_ms": {"p50": p[len(p) // 2], "p99": p[min(len(p) - 1, int(0.99 * len(p)))]},
             "solver": {k: st[k] for k in ("max_iterations", "max_sweeps", "failed", "max_relres", "solve_ms")},
+            "mixed_direct": mixed_line,
+            "mixed_vs_plain": (mixed_line["value"] / value) if mixed_line else None,
             "rel_err_vs_oracle": err if dist.rank == 0 and not args.no_cpu else None,
             "cpu_baseline": cpu, "clocks": clocks}
     ctx.close()

@@ -618,6 +618,12 @@ struct DNode {
 // is then the exact solution of a system within this relative distance.
 constexpr double kDirectBackwardMax = 1e-13;
 
+// MIXED_DIRECT: CG iterations a sweep may take with the FP32 factor before
+// the problem is refactored in FP64 (the penalty systems that an FP32
+// factor still resolves need 3-25 per sweep; slower convergence means the
+// FP32 factor is too inexact for the problem's conditioning)
+constexpr int kMixedCgCap = 100;
+
 struct DirectDev {
     const DNode *node;
     const int32_t *front, *child, *ent_rel, *ent_pos, *ext;
@@ -638,7 +644,8 @@ constexpr int kGroupFront = 96;
 // fronts up to this size are solved by one warp (forward and backward)
 constexpr int kWarpFront = 96;
 
-__device__ __forceinline__ double warp_sum64(double v) {
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
@@ -648,19 +655,20 @@ __device__ __forceinline__ double warp_sum64(double v) {
 // DoFs (blocked right-looking dense Cholesky), keep the factor columns and
 // the update matrix.  Returns false on a non-positive pivot.  Every entry's
 // arithmetic is independent of the group's size.
-__device__ bool mf_factor_node(const BatchDev &d, const DirectDev &m, const DNode &nd, long long nnz0, double *F,
-                               double *U, double *L, double *colk, double *P, ThreadGroup g) {
+template <typename T>
+__device__ bool mf_factor_node(const BatchDev &d, const DirectDev &m, const DNode &nd, long long nnz0, T *F,
+                               T *U, T *L, T *colk, T *P, ThreadGroup g) {
     const int lane = threadIdx.x & 31, gw = g.tid >> 5, gnw = g.size >> 5;
     const int f = nd.f, s = nd.s;
     for (long long q = g.tid; q < (long long)f * f; q += g.size) F[q] = 0.0;
     g.sync();
     for (int e = g.tid; e < nd.nentry; e += g.size)
-        F[m.ent_pos[nd.entry_off + e]] = d.v64[nnz0 + m.ent_rel[nd.entry_off + e]];
+        F[m.ent_pos[nd.entry_off + e]] = (T)d.v64[nnz0 + m.ent_rel[nd.entry_off + e]];
     g.sync();
     for (int q = 0; q < nd.nchild; q++) {
         const DNode cn = m.node[m.child[nd.child_off + q]];
         const int sc = cn.f - cn.s;
-        const double *Uc = U + cn.U_off;
+        const T *Uc = U + cn.U_off;
         const int32_t *ex = m.ext + cn.ext_off;
         for (int a = gw; a < sc; a += gnw) {
             const long long pa = (long long)ex[a] * f;
@@ -668,14 +676,14 @@ __device__ bool mf_factor_node(const BatchDev &d, const DirectDev &m, const DNod
         }
         g.sync();
     }
-    if (!front_cholesky<double>(F, f, s, colk, P, kPanelStride, g)) return false;
-    double *Lt = L + nd.L_off;
+    if (!front_cholesky<T>(F, f, s, colk, P, kPanelStride, g)) return false;
+    T *Lt = L + nd.L_off;
     for (long long q = g.tid; q < (long long)f * s; q += g.size) {
         const int i = (int)(q / s), j = (int)(q - (long long)i * s);
         Lt[q] = j <= i ? F[(long long)i * f + j] : 0.0;
     }
     const int sc = f - s;
-    double *Ut = U + nd.U_off;
+    T *Ut = U + nd.U_off;
     for (long long q = g.tid; q < (long long)sc * sc; q += g.size) {
         const int a = (int)(q / sc), b = (int)(q - (long long)a * sc);
         if (b <= a) Ut[q] = F[(long long)(s + a) * f + s + b];
@@ -688,14 +696,15 @@ __device__ bool mf_factor_node(const BatchDev &d, const DirectDev &m, const DNod
 // fronts of at most kGroupFront rows by m.fact_groups groups of warps in
 // parallel (each with its own front scratch Fg, pivot column and panel
 // shares of colk and P), larger fronts by the whole block one after another.
-__device__ bool mf_factor_lv(const BatchDev &d, const DirectDev &m, int lv0, int nlev, long long nnz0, double *F,
-                             double *U, double *L, double *colk, double *P, double *Fg, int *fail) {
+template <typename T>
+__device__ bool mf_factor_lv(const BatchDev &d, const DirectDev &m, int lv0, int nlev, long long nnz0, T *F,
+                             T *U, T *L, T *colk, T *P, T *Fg, int *fail) {
     const int ng = m.fact_groups;
     const int gsize = blockDim.x / ng, gid = threadIdx.x / gsize;
     const ThreadGroup grp{(int)threadIdx.x - gid * gsize, gsize, 1 + gid};
-    double *gF = Fg + (long long)gid * kGroupFront * kGroupFront;
-    double *gcolk = colk + gid * kGroupFront;
-    double *gP = P + (long long)gid * kGroupFront * kPanelStride;
+    T *gF = Fg + (long long)gid * kGroupFront * kGroupFront;
+    T *gcolk = colk + gid * kGroupFront;
+    T *gP = P + (long long)gid * kGroupFront * kPanelStride;
     if (threadIdx.x == 0) *fail = 0;
     __syncthreads();
     for (int l = 0; l < nlev; l++) {
@@ -726,25 +735,26 @@ __device__ bool mf_factor_lv(const BatchDev &d, const DirectDev &m, int lv0, int
 // fronts of at most kWarpFront rows go one per warp in parallel and the
 // larger ones through the whole block; one block barrier per level.  Fixed
 // order everywhere, no atomics: bit-reproducible.
-__device__ void mf_fwd_warp(const DirectDev &m, const DNode &nd, double *w, const double *L, double *uv, double *v,
+template <typename T>
+__device__ void mf_fwd_warp(const DirectDev &m, const DNode &nd, T *w, const T *L, T *uv, T *v,
                             int lane) {
     const int f = nd.f, s = nd.s;
     const int32_t *fr = m.front + nd.front_off;
-    const double *Lt = L + nd.L_off;
+    const T *Lt = L + nd.L_off;
     for (int k = lane; k < f; k += 32) v[k] = k < s ? w[fr[k]] : 0.0;
     __syncwarp();
     for (int q = 0; q < nd.nchild; q++) {
         const DNode cn = m.node[m.child[nd.child_off + q]];
         const int sc = cn.f - cn.s;
         const int32_t *ex = m.ext + cn.ext_off;
-        const double *uc = uv + cn.uv_off;
+        const T *uc = uv + cn.uv_off;
         for (int a = lane; a < sc; a += 32) v[ex[a]] += uc[a];
         __syncwarp();
     }
     // column-oriented elimination; the next column of L (rows below its
     // diagonal, up to three per lane) and its diagonal entry are loaded
     // while the current column is applied
-    double lc[3], ln[3], dk = s > 0 ? Lt[0] : 1.0, dn = 1.0;
+    T lc[3], ln[3], dk = s > 0 ? Lt[0] : 1.0, dn = 1.0;
 #pragma unroll
     for (int t = 0; t < 3; t++) {
         const int j = 1 + lane + 32 * t;
@@ -758,7 +768,7 @@ __device__ void mf_fwd_warp(const DirectDev &m, const DNode &nd, double *w, cons
             ln[t] = (more && j < f) ? Lt[(long long)j * s + k + 1] : 0.0;
         }
         if (more) dn = Lt[(long long)(k + 1) * s + k + 1];
-        const double yk = v[k] / dk;
+        const T yk = v[k] / dk;
 #pragma unroll
         for (int t = 0; t < 3; t++) {
             const int j = k + 1 + lane + 32 * t;
@@ -772,27 +782,28 @@ __device__ void mf_fwd_warp(const DirectDev &m, const DNode &nd, double *w, cons
         dk = dn;
     }
     for (int k = lane; k < s; k += 32) w[fr[k]] = v[k];
-    double *uo = uv + nd.uv_off;
+    T *uo = uv + nd.uv_off;
     for (int j = lane; j < f - s; j += 32) uo[j] = v[s + j];
     __syncwarp();
 }
 
-__device__ void mf_bwd_warp(const DirectDev &m, const DNode &nd, double *w, const double *L, double *v, int lane) {
+template <typename T>
+__device__ void mf_bwd_warp(const DirectDev &m, const DNode &nd, T *w, const T *L, T *v, int lane) {
     const int f = nd.f, s = nd.s, sc = f - s;
     const int32_t *fr = m.front + nd.front_off;
-    const double *Lt = L + nd.L_off;
-    double *xs = v + s;
+    const T *Lt = L + nd.L_off;
+    T *xs = v + s;
     for (int i = lane; i < sc; i += 32) xs[i] = w[fr[s + i]];
     __syncwarp();
     for (int k = lane; k < s; k += 32) {
-        double acc = w[fr[k]];
+        T acc = w[fr[k]];
         for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
         v[k] = acc;
     }
     __syncwarp();
     // row k of L11 (entries left of its diagonal, up to three per lane since
     // s <= kWarpFront) and the next diagonal are loaded one step ahead
-    double rc[3], rn[3], dk = s > 0 ? Lt[(long long)(s - 1) * s + s - 1] : 1.0, dn = 1.0;
+    T rc[3], rn[3], dk = s > 0 ? Lt[(long long)(s - 1) * s + s - 1] : 1.0, dn = 1.0;
 #pragma unroll
     for (int t = 0; t < 3; t++) {
         const int j = lane + 32 * t;
@@ -806,7 +817,7 @@ __device__ void mf_bwd_warp(const DirectDev &m, const DNode &nd, double *w, cons
             rn[t] = (more && j < k - 1) ? Lt[(long long)(k - 1) * s + j] : 0.0;
         }
         if (more) dn = Lt[(long long)(k - 1) * s + k - 1];
-        const double xk = v[k] / dk;
+        const T xk = v[k] / dk;
 #pragma unroll
         for (int t = 0; t < 3; t++) {
             const int j = lane + 32 * t;
@@ -824,19 +835,20 @@ __device__ void mf_bwd_warp(const DirectDev &m, const DNode &nd, double *w, cons
 }
 
 // one large front by the whole block (fv: shared front vector, max_f)
-__device__ void mf_fwd_block(const DirectDev &m, const DNode &nd, double *w, const double *L, double *uv, double *fv,
-                             double *tile) {
+template <typename T>
+__device__ void mf_fwd_block(const DirectDev &m, const DNode &nd, T *w, const T *L, T *uv, T *fv,
+                             T *tile) {
     const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
     const int f = nd.f, s = nd.s;
     const int32_t *fr = m.front + nd.front_off;
-    const double *Lt = L + nd.L_off;
+    const T *Lt = L + nd.L_off;
     for (int k = tid; k < f; k += bs) fv[k] = k < s ? w[fr[k]] : 0.0;
     __syncthreads();
     for (int q = 0; q < nd.nchild; q++) {
         const DNode cn = m.node[m.child[nd.child_off + q]];
         const int sc = cn.f - cn.s;
         const int32_t *ex = m.ext + cn.ext_off;
-        const double *uc = uv + cn.uv_off;
+        const T *uc = uv + cn.uv_off;
         for (int a = tid; a < sc; a += bs) fv[ex[a]] += uc[a];
         __syncthreads();
     }
@@ -844,10 +856,10 @@ __device__ void mf_fwd_block(const DirectDev &m, const DNode &nd, double *w, con
         const int nbk = min(32, s - kb);
         if (kb > 0)
             for (int r = warp; r < nbk; r += nw) {
-                const double *Li = Lt + (long long)(kb + r) * s;
-                double acc = 0.0;
+                const T *Li = Lt + (long long)(kb + r) * s;
+                T acc = 0.0;
                 for (int j = lane; j < kb; j += 32) acc += Li[j] * fv[j];
-                acc = warp_sum64(acc);
+                acc = warp_sum_t(acc);
                 if (lane == 0) fv[kb + r] -= acc;
             }
         for (int q = tid; q < nbk * nbk; q += bs) {
@@ -856,9 +868,9 @@ __device__ void mf_fwd_block(const DirectDev &m, const DNode &nd, double *w, con
         }
         __syncthreads();
         if (warp == 0) {
-            double vv = lane < nbk ? fv[kb + lane] : 0.0;
+            T vv = lane < nbk ? fv[kb + lane] : 0.0;
             for (int c = 0; c < nbk; c++) {
-                const double yc = __shfl_sync(0xffffffffu, vv, c) / tile[c * 33 + c];
+                const T yc = __shfl_sync(0xffffffffu, vv, c) / tile[c * 33 + c];
                 if (lane == c) vv = yc;
                 else if (lane > c && lane < nbk) vv -= tile[lane * 33 + c] * yc;
             }
@@ -867,27 +879,28 @@ __device__ void mf_fwd_block(const DirectDev &m, const DNode &nd, double *w, con
         __syncthreads();
     }
     for (int k = tid; k < s; k += bs) w[fr[k]] = fv[k];
-    double *uo = uv + nd.uv_off;
+    T *uo = uv + nd.uv_off;
     for (int i = s + warp; i < f; i += nw) {
-        const double *Li = Lt + (long long)i * s;
-        double acc = 0.0;
+        const T *Li = Lt + (long long)i * s;
+        T acc = 0.0;
         for (int k = lane; k < s; k += 32) acc += Li[k] * fv[k];
-        acc = warp_sum64(acc);
+        acc = warp_sum_t(acc);
         if (lane == 0) uo[i - s] = fv[i] - acc;
     }
     __syncthreads();
 }
 
-__device__ void mf_bwd_block(const DirectDev &m, const DNode &nd, double *w, const double *L, double *ys, double *xs,
-                             double *tile) {
+template <typename T>
+__device__ void mf_bwd_block(const DirectDev &m, const DNode &nd, T *w, const T *L, T *ys, T *xs,
+                             T *tile) {
     const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int f = nd.f, s = nd.s, sc = f - s;
     const int32_t *fr = m.front + nd.front_off;
-    const double *Lt = L + nd.L_off;
+    const T *Lt = L + nd.L_off;
     for (int i = tid; i < sc; i += bs) xs[i] = w[fr[s + i]];
     __syncthreads();
     for (int k = tid; k < s; k += bs) {
-        double acc = w[fr[k]];
+        T acc = w[fr[k]];
         for (int i = 0; i < sc; i++) acc -= Lt[(long long)(s + i) * s + k] * xs[i];
         ys[k] = acc;
     }
@@ -900,9 +913,9 @@ __device__ void mf_bwd_block(const DirectDev &m, const DNode &nd, double *w, con
         }
         __syncthreads();
         if (warp == 0) {
-            double vv = lane < nbk ? ys[kb + lane] : 0.0;
+            T vv = lane < nbk ? ys[kb + lane] : 0.0;
             for (int c = nbk - 1; c >= 0; c--) {
-                const double xc = __shfl_sync(0xffffffffu, vv, c) / tile[c * 33 + c];
+                const T xc = __shfl_sync(0xffffffffu, vv, c) / tile[c * 33 + c];
                 if (lane == c) vv = xc;
                 else if (lane < c) vv -= tile[c * 33 + lane] * xc;
             }
@@ -910,7 +923,7 @@ __device__ void mf_bwd_block(const DirectDev &m, const DNode &nd, double *w, con
         }
         __syncthreads();
         for (int k = tid; k < kb; k += bs) {
-            double acc = 0.0;
+            T acc = 0.0;
             for (int r = 0; r < nbk; r++) acc += Lt[(long long)(kb + r) * s + k] * ys[kb + r];
             ys[k] -= acc;
         }
@@ -920,10 +933,11 @@ __device__ void mf_bwd_block(const DirectDev &m, const DNode &nd, double *w, con
     __syncthreads();
 }
 
-__device__ void mf_solve_lv(const DirectDev &m, int lv0, int nlev, double *w, const double *L, double *uv,
-                            double *fv, double *ys, double *xs, double *tile, double *wbuf) {
+template <typename T>
+__device__ void mf_solve_lv(const DirectDev &m, int lv0, int nlev, T *w, const T *L, T *uv,
+                            T *fv, T *ys, T *xs, T *tile, T *wbuf) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    double *v = wbuf + warp * kWarpFront;
+    T *v = wbuf + warp * kWarpFront;
     for (int l = 0; l < nlev; l++) {
         const int a = m.lvl_ptr[lv0 + l], b = m.lvl_ptr[lv0 + l + 1];
         for (int i = a + warp; i < b; i += nw) {
@@ -950,7 +964,26 @@ __device__ void mf_solve_lv(const DirectDev &m, int lv0, int nlev, double *w, co
     }
 }
 
-template <int TPR>
+// z = M^{-1} r for rows [r0, r1) with the FP32 factor: r rounded into the
+// problem's FP32 work vector, the level-scheduled FP32 solve, z back in FP64.
+__device__ void mf_prec32(const BatchDev &d, const DirectDev &m, int pid, int r0, int r1, const double *r, double *z,
+                          const float *L, float *uv, float *fv, float *ys, float *xs, float *tile, float *wbuf) {
+    float *w = d.r32 + r0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) w[i - r0] = (float)r[i];
+    __syncthreads();
+    mf_solve_lv<float>(m, m.prob_lvl0[pid], m.prob_nlev[pid], w, L, uv, fv, ys, xs, tile, wbuf);
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) z[i] = (double)w[i - r0];
+    __syncthreads();
+}
+
+// MIXED = false: FP64 factorisation, each sweep refined against the FP64
+// matrix.  MIXED = true: FP32 factorisation (GB300's FP32 rate is ~64x its
+// FP64 rate), each sweep solved by FP64 conjugate gradients on the FP64
+// matrix preconditioned by the FP32 factor, warm-started from the previous
+// sweep's velocity; a problem whose FP32 factorisation meets a non-positive
+// pivot, or whose preconditioned CG stalls above the tolerance, is factored
+// again in FP64 and finishes in the FP64 mode (counted in fallbacks).
+template <int TPR, bool MIXED>
 __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev m) {
     extern __shared__ double dsm[];
     __shared__ double sh[32 * 4];
@@ -976,8 +1009,21 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
         for (int i = r0 + tid; i < r1; i += bs) d.u[i] = 0.0;
         for (int c = c0 + tid; c < c1; c += bs) d.p[c] = 0.0;
         __syncthreads();
-        const bool fact_ok = mf_factor_lv(d, m, m.prob_lvl0[pid], m.prob_nlev[pid], (long long)d.rowptr[r0], F, U, L,
-                                          colk, P, Fg, &fail_flag);
+        bool use32 = MIXED;
+        int nfall = 0;
+        bool fact_ok = false;
+        if (MIXED) {
+            fact_ok = mf_factor_lv<float>(d, m, m.prob_lvl0[pid], m.prob_nlev[pid], (long long)d.rowptr[r0], (float *)F,
+                                          (float *)U, (float *)L, (float *)colk, (float *)P, (float *)Fg, &fail_flag);
+            __syncthreads();
+            if (!fact_ok) {
+                use32 = false;
+                nfall = 1;
+            }
+        }
+        if (!use32)
+            fact_ok = mf_factor_lv<double>(d, m, m.prob_lvl0[pid], m.prob_nlev[pid], (long long)d.rowptr[r0], F, U, L,
+                                           colk, P, Fg, &fail_flag);
         __syncthreads();
         // ||A||_inf of the problem (for the normwise backward error of a solve)
         double an[1] = {0.0};
@@ -1000,27 +1046,110 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
                 const double bn = sqrt(bb[0]);
                 double rel = 0.0, prev = INFINITY, eta = 0.0;
                 bool floor = false;
-                for (int ref = 0;; ref++) {
-                    // r = rhs - A u (FP64, assembled matrix); stop at reltol or when the
-                    // residual stops falling (the FP64 floor of an ill-conditioned
-                    // system), else u += A^{-1} r
-                    double v[2] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, d.r64, nullptr, d.rhs),
-                                   0.0};
-                    for (int i = r0 + tid; i < r1; i += bs) v[1] += d.u[i] * d.u[i];
-                    bsum<2>(v, sh);
+                bool done32 = false;
+                if (MIXED && use32) {
+                    // FP64 CG preconditioned by the FP32 factor (x = u, r = rhs - A u)
+                    double *z = d.w64a, *pp = d.w64b, *q = d.w64c, *r = d.r64;
+                    double v[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, r, nullptr, d.rhs)};
+                    bsum<1>(v, sh);
                     rel = bn > 0 ? sqrt(v[0]) / bn : 0.0;
-                    eta = sqrt(v[0]) / (anorm * sqrt(v[1]) + bn + 1e-300);   // normwise backward error
-                    if (rel <= d.reltol) break;
-                    if (ref > 0 && rel > 0.5 * prev) {
-                        floor = true;
-                        break;
+                    if (rel <= d.reltol) done32 = true;
+                    double rz = 0.0, best = rel;
+                    int since = 0, restarts = 0;
+                    int cg_its = 0;
+                    for (int it = 0; !done32 && cg_its < kMixedCgCap; it++, cg_its++) {
+                        mf_prec32(d, m, pid, r0, r1, r, z, (const float *)L, (float *)uvw, (float *)colk, (float *)ys,
+                                  (float *)P, (float *)tile, (float *)wbuf);
+                        double w1[1] = {0.0};
+                        for (int i = r0 + tid; i < r1; i += bs) w1[0] += r[i] * z[i];
+                        bsum<1>(w1, sh);
+                        const double beta = it == 0 ? 0.0 : w1[0] / rz;
+                        rz = w1[0];
+                        for (int i = r0 + tid; i < r1; i += bs) pp[i] = z[i] + beta * (it == 0 ? 0.0 : pp[i]);
+                        __syncthreads();
+                        double pq[1] = {block_spmv<TPR, double, double, false>(d, r0, r1, d.v64, pp, q, pp, nullptr)};
+                        bsum<1>(pq, sh);
+                        if (!(pq[0] > 0.0) || !isfinite(pq[0])) break;
+                        const double alpha = rz / pq[0];
+                        double w2[1] = {0.0};
+                        for (int i = r0 + tid; i < r1; i += bs) {
+                            d.u[i] += alpha * pp[i];
+                            const double ri = r[i] - alpha * q[i];
+                            r[i] = ri;
+                            w2[0] += ri * ri;
+                        }
+                        bsum<1>(w2, sh);
+                        nsolve++;
+                        rel = bn > 0 ? sqrt(w2[0]) / bn : 0.0;
+                        if (rel <= d.reltol) {   // confirm with the true residual
+                            double t[1] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, r, nullptr,
+                                                                                 d.rhs)};
+                            bsum<1>(t, sh);
+                            rel = bn > 0 ? sqrt(t[0]) / bn : 0.0;
+                            if (rel <= d.reltol) {
+                                done32 = true;
+                                break;
+                            }
+                            if (++restarts > 3) break;
+                            it = -1;   // restart from the true residual
+                        }
+                        if (rel < 0.5 * best) {
+                            best = rel;
+                            since = 0;
+                        } else if (++since >= 20) {
+                            break;   // stalled
+                        }
                     }
-                    if (ref >= m.max_solves) break;
-                    prev = rel;
-                    mf_solve_lv(m, m.prob_lvl0[pid], m.prob_nlev[pid], d.r64 + r0, L, uvw, colk, ys, P, tile, wbuf);
-                    for (int i = r0 + tid; i < r1; i += bs) d.u[i] += d.r64[i];
-                    __syncthreads();
-                    nsolve++;
+                    if (!done32 && cg_its < kMixedCgCap) {
+                        // a stall at the FP64 floor of an ill-conditioned system is accepted by backward error
+                        double t[2] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, r, nullptr, d.rhs),
+                                       0.0};
+                        for (int i = r0 + tid; i < r1; i += bs) t[1] += d.u[i] * d.u[i];
+                        bsum<2>(t, sh);
+                        rel = bn > 0 ? sqrt(t[0]) / bn : 0.0;
+                        eta = sqrt(t[0]) / (anorm * sqrt(t[1]) + bn + 1e-300);
+                        if (eta <= kDirectBackwardMax) {
+                            floor = true;
+                            done32 = true;
+                        }
+                    }
+                    if (!done32) {
+                        // fall back: factor in FP64 and finish this problem in the FP64 mode
+                        use32 = false;
+                        nfall = 1;
+                        fact_ok = mf_factor_lv<double>(d, m, m.prob_lvl0[pid], m.prob_nlev[pid],
+                                                       (long long)d.rowptr[r0], F, U, L, colk, P, Fg, &fail_flag);
+                        __syncthreads();
+                        if (!fact_ok) {
+                            all_ok = false;
+                            break;
+                        }
+                    }
+                }
+                if (!done32) {
+                    for (int ref = 0;; ref++) {
+                        // r = rhs - A u (FP64, assembled matrix); stop at reltol or when the
+                        // residual stops falling (the FP64 floor of an ill-conditioned
+                        // system), else u += A^{-1} r
+                        double v[2] = {block_spmv<TPR, double, double, true>(d, r0, r1, d.v64, d.u, d.r64, nullptr, d.rhs),
+                                       0.0};
+                        for (int i = r0 + tid; i < r1; i += bs) v[1] += d.u[i] * d.u[i];
+                        bsum<2>(v, sh);
+                        rel = bn > 0 ? sqrt(v[0]) / bn : 0.0;
+                        eta = sqrt(v[0]) / (anorm * sqrt(v[1]) + bn + 1e-300);   // normwise backward error
+                        if (rel <= d.reltol) break;
+                        if (ref > 0 && rel > 0.5 * prev) {
+                            floor = true;
+                            break;
+                        }
+                        if (ref >= m.max_solves) break;
+                        prev = rel;
+                        mf_solve_lv<double>(m, m.prob_lvl0[pid], m.prob_nlev[pid], d.r64 + r0, L, uvw, colk, ys, P, tile,
+                                            wbuf);
+                        for (int i = r0 + tid; i < r1; i += bs) d.u[i] += d.r64[i];
+                        __syncthreads();
+                        nsolve++;
+                    }
                 }
                 worst = fmax(worst, rel);
                 all_ok = all_ok && (rel <= d.reltol || (floor && eta <= kDirectBackwardMax));
@@ -1033,7 +1162,7 @@ __global__ void __launch_bounds__(512, 1) k_stokes_direct(BatchDev d, DirectDev 
             d.iters[pid] = nsolve;
             d.sweeps_done[pid] = sweep;
             d.relres[pid] = fact_ok ? worst : INFINITY;
-            d.fallbacks[pid] = 0;
+            d.fallbacks[pid] = nfall;
             d.status[pid] = !fact_ok ? (int)GRMP_ERR_NAN : (all_ok ? 0 : (int)GRMP_ERR_NOT_CONVERGED);
         }
         __syncthreads();
@@ -1339,6 +1468,8 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
         return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: assemble FP64 (and FP32 for MIXED) and eliminate Dirichlet rows first");
     if (prm->sweeps <= 0 || prm->maxiter <= 0 || !(prm->reltol > 0))
         return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: sweeps, maxiter and reltol must be positive");
+    if (prm->mode < GRMP_SOLVE_FP64 || prm->mode > GRMP_SOLVE_MIXED_DIRECT)
+        return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "batch: mode %d", prm->mode);
     const int n = A->nrows, nc = m->ncells;
     // problem order: largest first (longest processing time first)
     std::vector<int32_t> order(np);
@@ -1457,7 +1588,8 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     cudaEventCreate(&e1);
     void *dwork = nullptr;
     size_t dwork_bytes = 0;
-    if (prm->mode == GRMP_SOLVE_DIRECT) {
+    const bool direct = prm->mode == GRMP_SOLVE_DIRECT || prm->mode == GRMP_SOLVE_MIXED_DIRECT;
+    if (direct) {
         // symbolic analysis once per distinct local pattern, cached in the matrix
         if (!A->direct || A->direct->row_offsets != std::vector<int32_t>(prm->row_offsets, prm->row_offsets + np + 1)) {
             grmp_direct_cache_free(A);
@@ -1494,7 +1626,10 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
         }
         const size_t smem =
             ((size_t)m.max_f + m.max_s + 32 * 33 + (size_t)m.max_f * kPanelStride + 16 * (size_t)kWarpFront) * 8;
-        auto kern = tpr == 4 ? k_stokes_direct<4> : (tpr == 8 ? k_stokes_direct<8> : k_stokes_direct<16>);
+        const bool mx = prm->mode == GRMP_SOLVE_MIXED_DIRECT;
+        auto kern = mx ? (tpr == 4 ? k_stokes_direct<4, true> : (tpr == 8 ? k_stokes_direct<8, true> : k_stokes_direct<16, true>))
+                       : (tpr == 4 ? k_stokes_direct<4, false>
+                                   : (tpr == 8 ? k_stokes_direct<8, false> : k_stokes_direct<16, false>));
         if (!rc && smem > 220 * 1024)
             rc = grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "batch direct: front of %d DoFs too large", m.max_f);
         if (!rc) {
@@ -1566,7 +1701,7 @@ extern "C" int grmp_stokes_batch_solve(grmp_matrix A, grmp_vector bf, grmp_vecto
     stats->status = stats->failed_problems ? GRMP_ERR_NOT_CONVERGED : GRMP_OK;
     if (stats->status)
         return grmp_fail(ctx, stats->status,
-                         prm->mode == GRMP_SOLVE_DIRECT
+                         direct
                              ? "batch: %d of %d problems failed (non-positive pivot or residual above reltol, worst %.2e)"
                              : "batch: %d of %d problems hit the iteration cap (worst relres %.2e)",
                          stats->failed_problems, np, stats->max_relres);

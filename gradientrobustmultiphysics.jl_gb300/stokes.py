@@ -218,12 +218,17 @@ class StokesBatchSystem:
     """Device-resident batched system: pattern, assembly, reconstructed rhs."""
 
     def __init__(self, ctx: api.GB300Context, prob: StokesBatchProblem, mixed: bool = True,
-                 split_penalty: bool = True, direct: bool = False, reconstruction: str = "RT0"):
+                 split_penalty: bool = True, direct: bool = False, reconstruction: str = "RT0",
+                 solver: str = ""):
         """mixed: FP32 inner solves inside FP64 refinement.  split_penalty
         (mixed only): the FP32 matrix holds the viscous term alone and the
         inner operator applies the penalty per cell in factored form.
         direct: FP64 multifrontal Cholesky per problem (the reference's
         sparse-direct sweep solves), factored once for all sweeps.
+        solver (overrides mixed / direct): "fp64" or "mixed" (block PCG),
+        "direct", or "mixed_direct" (an FP32 factor per problem
+        preconditioning FP64 CG, with the FP64 factor as the per-problem
+        fallback).
         reconstruction: "RT0" or "BDM1", the H(div) space of the
         right-hand side's ReconstructionIdentity test operator."""
         if reconstruction not in ("RT0", "BDM1"):
@@ -231,6 +236,12 @@ class StokesBatchSystem:
         self.reconstruction = reconstruction
         self.ctx = ctx
         self.prob = prob
+        if solver:
+            if solver not in ("fp64", "mixed", "direct", "mixed_direct"):
+                raise ValueError(f"solver {solver}")
+            direct = solver in ("direct", "mixed_direct")
+            mixed = solver == "mixed"
+        self.mixed_direct = solver == "mixed_direct"
         self.direct = bool(direct)
         mixed = mixed and not self.direct
         self.mixed = mixed
@@ -277,7 +288,8 @@ class StokesBatchSystem:
         P.lam = self.prob.lam
         P.sweeps = sweeps
         P.sweep_tol = sweep_tol
-        P.mode = L.SOLVE_DIRECT if self.direct else (L.SOLVE_MIXED if self.mixed else L.SOLVE_FP64)
+        P.mode = (L.SOLVE_MIXED_DIRECT if self.mixed_direct else
+                  L.SOLVE_DIRECT if self.direct else (L.SOLVE_MIXED if self.mixed else L.SOLVE_FP64))
         P.reltol = reltol
         P.inner_reltol = inner_reltol
         P.maxiter = maxiter

@@ -501,7 +501,11 @@ typedef struct {
     double lambda;               /* iterated-penalty parameter                                        */
     int32_t sweeps;              /* maximum iterated-penalty sweeps                                   */
     double sweep_tol;            /* stop a problem when ||p_new - p|| <= sweep_tol ||p_new|| (0: all)  */
-    int32_t mode;                /* inner solver: GRMP_SOLVE_FP64 or GRMP_SOLVE_MIXED                 */
+    int32_t mode;                /* velocity solver: GRMP_SOLVE_FP64 / MIXED (block PCG), DIRECT (FP64
+                                    multifrontal factor per problem, residual refinement) or
+                                    MIXED_DIRECT (FP32 factor per problem preconditioning FP64 CG,
+                                    FP64 factor as the per-problem fallback; maxiter bounds the CG
+                                    iterations of a sweep with 4 maxiter + 200)                     */
     double reltol;               /* inner solve: ||rhs - A u|| <= reltol ||rhs|| per sweep             */
     double inner_reltol;         /* MIXED: refinement trigger                                          */
     int32_t maxiter;             /* inner iteration cap per sweep                                       */
@@ -524,7 +528,9 @@ typedef struct {
     double max_relres;           /* worst final inner relative residual       */
     double solve_ms;
     int32_t fp64_fallbacks;      /* MIXED: inner solves that stalled in FP32 and
-                                    were finished by FP64 PCG from the same iterate */
+                                    were finished by FP64 PCG from the same iterate;
+                                    MIXED_DIRECT: problems refactored in FP64 (a
+                                    non-positive FP32 pivot or a stalled CG) */
 } grmp_stokes_batch_stats;
 
 /* Iterated-penalty Stokes solve of many independent Bernardi-Raugel / P0

@@ -34,7 +34,7 @@ def oracle_system(G, O, prob, penalty=True):
     return A0, M.csr(), b, O.penalized_rhs(b, prob.fixed)
 
 
-def stokes_tolerance(O, g, nu, lam, recon=1):
+def stokes_tolerance(O, g, nu, lam, recon=1, cap=1e-8):
     """Relative-error bound for one problem of a batched iterated-penalty
     result against the oracle's sparse-direct sweeps: 1e-10, or 10 * cond *
     eps where the velocity matrix's condition number makes that larger, but
@@ -43,10 +43,12 @@ def stokes_tolerance(O, g, nu, lam, recon=1):
     h^2: its smallest eigenvalues belong to divergence-free fields, scaled by
     nu, its largest to the penalty); both solutions carry rounding errors of
     cond * eps, so no tighter agreement is meaningful.  cond is computed here
-    (2-norm, dense, free DoFs) and returned with the bound."""
+    (2-norm, dense, free DoFs) and returned with the bound; cap=None gives
+    the plain conditioning bound."""
     import numpy as np
     M, _, fixed, _, _ = O.br_stokes_system(g, nu, lam, np.zeros((1, 5)), recon=recon)
     A = M.csr().toarray()
     free = np.setdiff1d(np.arange(A.shape[0]), fixed)
     cond = float(np.linalg.cond(A[np.ix_(free, free)]))
-    return max(1e-10, min(1e-8, 10.0 * cond * np.finfo(float).eps)), cond
+    b = 10.0 * cond * np.finfo(float).eps
+    return max(1e-10, b if cap is None else min(cap, b)), cond

@@ -141,6 +141,33 @@ def test_batch_matches_oracle(G, O, ctx, mode):
 
 
 @pytest.mark.gpu
+def test_batch_mixed_direct_matches_oracle(G, O, ctx):
+    """FP32 factor per problem preconditioning FP64 CG, with the FP64 factor
+    as the fallback, against the oracle's sparse-direct sweeps over nu from 1
+    down to 1e-4.  Problems whose CG reaches the tolerance meet the same
+    bound as the FP64 direct mode; a problem solved to the FP64 floor of its
+    conditioning (accepted, as in the FP64 mode, by a normwise backward error
+    <= 1e-13) is held to the conditioning bound 10 cond eps itself (measured
+    2.4e-8 at cond 2.1e9, within that bound of 4.6e-6)."""
+    from grmp_gb300 import stokes as S
+    sizes, nus = [5, 9, 6, 8], [1.0, 0.05, 1e-3, 1e-4]
+    prob = _small_batch(G, sizes, nus, seed=7)
+    sysd = S.StokesBatchSystem(ctx, prob, solver="mixed_direct")
+    sysd.assemble()
+    st = sysd.solve(sweeps=8, reltol=1e-13)
+    assert 0 <= st["fp64_fallbacks"] <= len(sizes)
+    u, p = sysd.velocity(), sysd.pressure()
+    for k, g in enumerate(prob.mesh.parts):
+        uo, po, _ = O.stokes_iterated_penalty(g, nus[k], prob.lam, prob.terms[k], sweeps=8)
+        r0, r1 = prob.V.row_offsets[k], prob.V.row_offsets[k + 1]
+        c0, c1 = prob.mesh.cell_offsets[k], prob.mesh.cell_offsets[k + 1]
+        eu = np.linalg.norm(u[r0:r1] - uo) / np.linalg.norm(uo)
+        ep = np.linalg.norm(p[c0:c1] - po) / np.linalg.norm(po)
+        tol, cond = stokes_tolerance(O, g, nus[k], prob.lam, 1, cap=None if nus[k] < 1e-3 else 1e-8)
+        assert eu <= tol and ep <= tol, (k, eu, ep, tol, cond, st)
+
+
+@pytest.mark.gpu
 def test_batch_bdm1_matches_oracle(G, O, ctx):
     """Direct batch with the BR -> BDM1 reconstructed right-hand side."""
     from grmp_gb300 import stokes as S
@@ -161,21 +188,21 @@ def test_batch_bdm1_matches_oracle(G, O, ctx):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["mixed", "direct"])
+@pytest.mark.parametrize("mode", ["mixed", "direct", "mixed_direct"])
 def test_batch_result_same_alone_and_in_the_mix(G, ctx, mode):
     """Each problem is owned by one thread block: its bits do not depend on
     the other problems of the batch."""
     from grmp_gb300 import stokes as S
     sizes, nus = [6, 12, 4, 9], [1.0, 1e-2, 0.3, 1e-3]
     big = _small_batch(G, sizes, nus, seed=11)
-    sb = S.StokesBatchSystem(ctx, big, mixed=(mode == "mixed"), direct=(mode == "direct"))
+    sb = S.StokesBatchSystem(ctx, big, solver=mode)
     sb.assemble()
     sb.solve(sweeps=5, reltol=1e-10)
     u, p = sb.velocity(), sb.pressure()
     k = 1
     alone = S.make_batch(sizes=np.array([sizes[k]]), nus=np.array([nus[k]]), seed=11)
     alone.terms = big.terms[k:k + 1].copy()
-    sa = S.StokesBatchSystem(ctx, alone, mixed=(mode == "mixed"), direct=(mode == "direct"))
+    sa = S.StokesBatchSystem(ctx, alone, solver=mode)
     sa.assemble()
     sa.solve(sweeps=5, reltol=1e-10)
     r0, r1 = big.V.row_offsets[k], big.V.row_offsets[k + 1]
