@@ -133,3 +133,24 @@ def test_resident_entries_are_evicted_under_budget(G):
     xs_cold, _, _ = SV.run(_cold(reqs), nslots=1, realtime=False)
     for a, b in zip(xs, xs_cold):
         assert _rel(a, b) <= 1e-10
+
+
+def test_large_request_near_two_million_dofs(G):
+    """One 3D P2 request of ~1.8M DoFs (60^3 Kuhn cubes) through the server:
+    the mixed result against the FP64 one (1e-10 relative, the serving
+    tolerance), then the same mesh resubmitted with new coefficients runs on
+    its resident data and equals a cold run of it."""
+    import dataclasses
+    from grmp_gb300 import serve as SV
+    rng = np.random.default_rng(21)
+    r = SV.build_request(rng, dofs_min=1.7e6, dofs_max=1.9e6, dim=3, order=2)
+    assert 1.5e6 <= r.ndofs <= 2.1e6
+    xs_m, st_m, _ = SV.run([r], nslots=1, mode="mixed", realtime=False)
+    xs_f, st_f, _ = SV.run([r], nslots=1, mode="fp64", realtime=False)
+    assert st_m[0]["rc"] == 0 and st_f[0]["rc"] == 0
+    assert np.linalg.norm(xs_m[0] - xs_f[0]) <= 1e-10 * np.linalg.norm(xs_f[0])
+    r2 = dataclasses.replace(r, kappa=np.exp(rng.standard_normal(r.kappa.size)))
+    xs2, st2, _ = SV.run([r, r2], nslots=1, realtime=False)
+    assert st2[1]["resident"] == 1
+    xc, _, _ = SV.run([r2], nslots=1, realtime=False)
+    assert np.array_equal(xs2[1], xc[0])
