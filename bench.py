@@ -585,7 +585,9 @@ def summary_linear(G, P, prob, modes, reltol: float, steps: int, warmup: int, re
         ms, st = _timed(stream, lambda: sysd.assemble_and_solve(solver), steps, warmup)
         sols[mode] = sysd.x.entries
         out[mode] = {"value": ndofs / (statistics.mean(ms) / 1e3), "ms_per_step": statistics.mean(ms),
-                     "iterations": st["iterations"], "spmv_config": st["spmv_config"]}
+                     "iterations": st["iterations"], "spmv_config": st["spmv_config"],
+                     "solve_ms": st["solve_ms"], "grid_blocks": st["grid_blocks"],
+                     "us_per_iteration": (1e3 * st["solve_ms"] / st["iterations"]) if st["iterations"] else None}
     plain, mixed = modes
     out["mixed_vs_plain"] = out[mixed]["value"] / out[plain]["value"]
     uref, desc = None, None
@@ -624,6 +626,12 @@ def run_extras(args) -> dict:
     out["poisson2d_P2_128x128"] = summary_linear(G, P, P.poisson2d(128), ("fp64", "mixed"), 1e-11, 5, 3, "oracle",
                                                  True)
     out["poisson2d_P2_128x128"]["wall_s"] = time.perf_counter() - t0
+    # which bound: the FP64 values + columns of this matrix (395,265 nonzeros,
+    # ~4.7 MB) and its vectors stay in the 129 MB L2 between iterations, so a
+    # solver iteration is bounded by its grid-wide synchronisations (three per
+    # FP64 iteration, two per mixed one) and the dependent gathers, not by HBM
+    out["poisson2d_P2_128x128"]["bound"] = ("latency: L2-resident system; per-iteration time set by the persistent "
+                                            "solver's grid barriers and dependent gathers, not by HBM bandwidth")
     t0 = time.perf_counter()
     out["elasticity2d_P2vec_256x256_lambda1e3"] = summary_linear(
         G, P, P.elasticity2d(256, seed=args.seed), ("direct", "mixed_direct"), 1e-12, 3, 3, "gpu_direct", False)
