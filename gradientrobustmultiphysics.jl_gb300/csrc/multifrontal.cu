@@ -95,29 +95,42 @@ __global__ void __launch_bounds__(kTB) k_mf_factor_level(MfDev m, int lb, int co
     }
 }
 
-// One large front by the whole grid (cooperative launch, bounded grid
-// barriers): assembly, then per panel of kPanel columns (a) block 0 factors
-// the diagonal block, (b) every thread solves rows below it against the
-// diagonal block (L21 = A21 L11^-T, also staged into the panel buffer P),
-// (c) the trailing lower triangle gets the rank-kPanel update from 4x4
-// register tiles spread over all blocks.  Same arithmetic per entry as
-// front_cholesky, spread over the GPU instead of one block.
+// Large fronts by a group of blocks of the whole grid (cooperative launch,
+// bounded grid barriers): group_factor_wide below.
 struct CoopState {
     GridBarrier bar;
     int status;   // GRMP_ERR_TIMEOUT if a barrier wait gave up
     int abort;    // non-positive pivot found
 };
 
-// Body of the grouped large-front factorisation: `grank` = this
-// block's rank in the group, `gblocks` = blocks in the group, `sync()` = the
-// group's barrier (returns false when a bounded wait gave up), `abort` = the
-// group's pivot-failure flag (global memory, zero on entry).
+// Body of the grouped large-front factorisation: `grank` = this block's
+// rank in the group, `gblocks` = blocks in the group, `sync()` = the group's
+// barrier (returns false when a bounded wait gave up), `abort` = the group's
+// pivot-failure flag (global memory, zero on entry).
+// Wide-panel variant for the grid-wide path (the fronts near the root of
+// the tree, up to a few thousand rows): panels of kWide columns, so that a
+// front of f rows takes f / kWide steps with two group barriers each.
+// (a) every block factors the kWide x kWide diagonal block itself in shared
+// memory (identical arithmetic in every block, so no barrier and no copy
+// are needed before (b)); (b) one thread per row below solves it against the
+// diagonal block (L21 = A21 L11^-T, kept in registers, written to F and to
+// the panel buffer P); (c) the trailing lower triangle is cut into
+// kWide x kWide tiles, one per block at a time, each computed from the two
+// panel slices staged in shared memory by 4x4 register tiles (16 FMAs per
+// 8 shared loads) and subtracted from F once.  Each entry's arithmetic is
+// fixed (sum over the panel's columns in order, then one subtraction), so
+// results do not depend on the grid size.
+constexpr int kWide = 64;
+constexpr int kWideStride = kWide + 1;
+
 template <typename T, typename Sync>
-__device__ void group_factor(MfDev m, int t, const double *vals, T *L, T *U, T *F, T *P, int grank, int gblocks,
-                             Sync sync, int *abort, int *err) {
-    __shared__ T dt[kPanel][kPanel + 1];
+__device__ void group_factor_wide(MfDev m, int t, const double *vals, T *L, T *U, T *F, T *P, int grank, int gblocks,
+                                  Sync sync, int *abort, int *err, T *sm) {
+    T *Dg = sm;                          // diagonal block [kWide][kWideStride]
+    T *Ta = sm + kWide * kWideStride;    // panel rows of tile row bi
+    T *Tb = Ta + kWide * kWideStride;    // panel rows of tile column bj
     const long long gtid = (long long)grank * blockDim.x + threadIdx.x, gsz = (long long)gblocks * blockDim.x;
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31;
     const long long gwarp = gtid >> 5, nwarps = gsz >> 5;
     const MfNode nd = m.node[t];
     const int f = nd.f, s = nd.s;
@@ -136,106 +149,118 @@ __device__ void group_factor(MfDev m, int t, const double *vals, T *L, T *U, T *
         }
         if (!sync()) return;
     }
-    for (int k0 = 0; k0 < s; k0 += kPanel) {
-        const int kw = min(kPanel, s - k0), k1 = k0 + kw, mrows = f - k1;
-        if (grank == 0) {   // (a) diagonal block
-            for (int q = tid; q < kw * kw; q += blockDim.x) {
-                const int r = q / kw, c = q - r * kw;
-                dt[r][c] = c <= r ? F[(long long)(k0 + r) * f + k0 + c] : T(0);
-            }
-            __syncthreads();
-            bool bad = false;
-            for (int c = 0; c < kw; c++) {
-                const T dcc = dt[c][c];
-                if (!(dcc > T(0)) || !isfinite((double)dcc)) {
-                    bad = true;
-                    break;
-                }
-                const T dk = sqrt(dcc);
-                __syncthreads();
-                if (tid > c && tid < kw) dt[tid][c] /= dk;
-                if (tid == 0) dt[c][c] = dk;
-                __syncthreads();
-                const int r = c + 1 + tid / kw, cc = c + 1 + tid % kw;
-                if (tid < kw * kw && r < kw && cc <= r) dt[r][cc] -= dt[r][c] * dt[cc][c];
-                __syncthreads();
-            }
-            if (bad) {
-                if (tid == 0) {
-                    *(volatile int *)abort = 1;
-                    atomicCAS(err, 0, t + 1);
-                }
-            } else {
-                for (int q = tid; q < kw * kw; q += blockDim.x) {
-                    const int r = q / kw, c = q - r * kw;
-                    if (c <= r) F[(long long)(k0 + r) * f + k0 + c] = dt[r][c];
-                }
-            }
-        }
-        if (!sync()) return;
-        if (*(volatile int *)abort) return;
-        // (b) rows below the diagonal block
-        for (int q = tid; q < kw * kw; q += blockDim.x) {
-            const int r = q / kw, c = q - r * kw;
-            dt[r][c] = c <= r ? F[(long long)(k0 + r) * f + k0 + c] : T(0);
+    for (int k0 = 0; k0 < s; k0 += kWide) {
+        const int kw = min(kWide, s - k0), k1 = k0 + kw, mrows = f - k1;
+        // (a) the diagonal block, in every block
+        for (int q = tid; q < kWide * kWide; q += bs) {
+            const int r = q / kWide, c = q - r * kWide;
+            Dg[r * kWideStride + c] = (r < kw && c <= r) ? F[(long long)(k0 + r) * f + k0 + c] : T(0);
         }
         __syncthreads();
+        bool bad = false;
+        for (int c = 0; c < kw; c++) {
+            const T dcc = Dg[c * kWideStride + c];
+            if (!(dcc > T(0)) || !isfinite((double)dcc)) {   // the same value in every thread and block
+                bad = true;
+                break;
+            }
+            const T dk = sqrt(dcc);
+            __syncthreads();
+            for (int r = c + 1 + tid; r < kw; r += bs) Dg[r * kWideStride + c] /= dk;
+            if (tid == 0) Dg[c * kWideStride + c] = dk;
+            __syncthreads();
+            const int w = kw - c - 1;
+            for (int q = tid; q < w * w; q += bs) {
+                const int r = c + 1 + q / w, cc = c + 1 + q % w;
+                if (cc <= r) Dg[r * kWideStride + cc] -= Dg[r * kWideStride + c] * Dg[cc * kWideStride + c];
+            }
+            __syncthreads();
+        }
+        if (bad) {   // every block sees it: leave without a further barrier
+            if (tid == 0) {
+                *(volatile int *)abort = 1;
+                atomicCAS(err, 0, t + 1);
+            }
+            return;
+        }
+        // (b) rows below the diagonal block
         for (long long i = k1 + gtid; i < f; i += gsz) {
-            T xr[kPanel];
+            T x[kWide];
             T *Fi = F + i * f + k0;
 #pragma unroll
-            for (int j = 0; j < kPanel; j++) {
+            for (int j = 0; j < kWide; j++) {
                 if (j < kw) {
                     T a = Fi[j];
-                    for (int l = 0; l < j; l++) a -= xr[l] * dt[j][l];
-                    xr[j] = a / dt[j][j];
+#pragma unroll
+                    for (int l = 0; l < j; l++) a -= x[l] * Dg[j * kWideStride + l];
+                    x[j] = a / Dg[j * kWideStride + j];
+                } else {
+                    x[j] = T(0);
                 }
             }
+            T *Pi = P + (i - k1) * kWideStride;
 #pragma unroll
-            for (int j = 0; j < kPanel; j++)
+            for (int j = 0; j < kWide; j++)
                 if (j < kw) {
-                    Fi[j] = xr[j];
-                    P[(i - k1) * kPanelStride + j] = xr[j];
+                    Fi[j] = x[j];
+                    Pi[j] = x[j];
                 }
         }
         if (!sync()) return;
-        // (c) trailing update
-        const int nt = (mrows + 3) >> 2;
+        // the factored diagonal block goes back into F only now: before the
+        // barrier other blocks may still be reading the unfactored one in (a)
+        if (grank == 0)
+            for (int q = tid; q < kw * kw; q += bs) {
+                const int r = q / kw, c = q - r * kw;
+                if (c <= r) F[(long long)(k0 + r) * f + k0 + c] = Dg[r * kWideStride + c];
+            }
+        // (c) trailing update in kWide x kWide tiles of the lower triangle
+        const int nt = (mrows + kWide - 1) / kWide;
         const long long ntiles = (long long)nt * (nt + 1) / 2;
-        for (long long q = gtid; q < ntiles; q += gsz) {
+        const int ty = tid / 16, tx = tid % 16;   // 16 x 16 threads, 4 x 4 entries each
+        for (long long q = grank; q < ntiles; q += gblocks) {
             int bi = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
             while ((long long)(bi + 1) * (bi + 2) / 2 <= q) bi++;
             while ((long long)bi * (bi + 1) / 2 > q) bi--;
             const int bj = (int)(q - (long long)bi * (bi + 1) / 2);
-            const int i0 = bi * 4, j0 = bj * 4;
-            T acc[4][4];
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[a][b] = T(0);
-            for (int tt = 0; tt < kw; tt++) {
-                T x[4], y[4];
-#pragma unroll
-                for (int a = 0; a < 4; a++) {
-                    x[a] = i0 + a < mrows ? P[(long long)(i0 + a) * kPanelStride + tt] : T(0);
-                    y[a] = j0 + a < mrows ? P[(long long)(j0 + a) * kPanelStride + tt] : T(0);
-                }
+            for (int e = tid; e < kWide * kWide; e += bs) {
+                const int r = e / kWide, c = e - r * kWide;
+                const int ia = bi * kWide + r, ib = bj * kWide + r;
+                Ta[r * kWideStride + c] = (ia < mrows && c < kw) ? P[(long long)ia * kWideStride + c] : T(0);
+                Tb[r * kWideStride + c] = (ib < mrows && c < kw) ? P[(long long)ib * kWideStride + c] : T(0);
+            }
+            __syncthreads();
+            if (tid < 256) {
+                T acc[4][4];
 #pragma unroll
                 for (int a = 0; a < 4; a++)
 #pragma unroll
-                    for (int b = 0; b < 4; b++) acc[a][b] += x[a] * y[b];
-            }
+                    for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+                for (int tt = 0; tt < kw; tt++) {
+                    T xa[4], yb[4];
 #pragma unroll
-            for (int a = 0; a < 4; a++) {
-                const int i = i0 + a;
-                if (i >= mrows) break;
-                T *Fi = F + (long long)(k1 + i) * f + k1;
+                    for (int a = 0; a < 4; a++) {
+                        xa[a] = Ta[(ty * 4 + a) * kWideStride + tt];
+                        yb[a] = Tb[(tx * 4 + a) * kWideStride + tt];
+                    }
 #pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const int j = j0 + b;
-                    if (j <= i) Fi[j] -= acc[a][b];
+                    for (int a = 0; a < 4; a++)
+#pragma unroll
+                        for (int b = 0; b < 4; b++) acc[a][b] += xa[a] * yb[b];
+                }
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    const int i = bi * kWide + ty * 4 + a;
+                    if (i >= mrows) break;
+                    T *Fi = F + (long long)(k1 + i) * f + k1;
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        const int j = bj * kWide + tx * 4 + b;
+                        if (j <= i) Fi[j] -= acc[a][b];
+                    }
                 }
             }
+            __syncthreads();   // the tiles are reloaded next
         }
         if (!sync()) return;
     }
@@ -252,7 +277,6 @@ __device__ void group_factor(MfDev m, int t, const double *vals, T *L, T *U, T *
     }
 }
 
-
 // The large fronts of one level by the whole grid split into `ngroups`
 // groups (block b belongs to group b % ngroups, so every group spans all
 // SMs evenly); group g factors fronts g, g + ngroups, ... of the level, each
@@ -265,10 +289,12 @@ __global__ void __launch_bounds__(kTB) k_mf_group_factor(MfDev m, int lb, int co
     const int g = blockIdx.x % ngroups, grank = blockIdx.x / ngroups;
     const int gblocks = (gridDim.x - g + ngroups - 1) / ngroups;
     CoopState *c = cs + g;
+    extern __shared__ unsigned char mf_gsmem[];
+    T *sm = reinterpret_cast<T *>(mf_gsmem);
     auto sync = [&]() { return grid_barrier(&c->bar, gblocks, &c->status); };
     for (int q = g; q < count; q += ngroups) {
-        group_factor<T>(m, m.lvl_nodes[lb + q], vals, L, U, Fpool + g * fslot, Ppool + g * pslot, grank, gblocks, sync,
-                        &c->abort, err);
+        group_factor_wide<T>(m, m.lvl_nodes[lb + q], vals, L, U, Fpool + g * fslot, Ppool + g * pslot, grank, gblocks,
+                             sync, &c->abort, err, sm);
         if (*(volatile int *)&c->abort || *(volatile int *)&c->status) return;
         if (!sync()) return;   // buffers reused by the group's next front
     }
@@ -826,7 +852,7 @@ int mf_build(grmp_matrix A) {
         long long mf = 0;
         for (auto it2 = b0; it2 != b1; ++it2) mf = std::max<long long>(mf, S.node[*it2].f);
         C->fpool = std::max(C->fpool, g * mf * mf);
-        C->ppool = std::max(C->ppool, g * mf * kPanelStride);
+        C->ppool = std::max(C->ppool, g * mf * kWideStride);   // the grid-wide path's panels are kWide wide
     }
     C->level_nodes_host = order;
     std::vector<long long> qrow(S.nnodes + 1, 0), scol(S.nnodes + 1, 0), gpref(S.nnodes + 1, 0),
@@ -919,9 +945,11 @@ int mf_numeric(grmp_matrix A, int *grid_out) {
                 rc = grmp_alloc(ctx, (void **)&cs, (size_t)ncs * sizeof(CoopState));
                 if (rc) break;
             }
+            const size_t gsmem = (size_t)3 * kWide * kWideStride * sizeof(T);
             if (!coop_grid) {
                 int per_sm = 0;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_group_factor<T>, kTB, 0);
+                cudaFuncSetAttribute(k_mf_group_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_group_factor<T>, kTB, gsmem);
                 coop_grid = std::max(1, std::min(per_sm, 4)) * ctx->num_sms;
             }
             cudaMemsetAsync(cs, 0, (size_t)ng * sizeof(CoopState), ctx->stream);
@@ -929,9 +957,9 @@ int mf_numeric(grmp_matrix A, int *grid_out) {
             int lbb = lb + nsmall, cntb = nbig, ngv = ng;
             const double *vv = A->d_vals64;
             T *Lp = (T *)C.L, *Up = (T *)C.U, *Fp = (T *)C.F, *Pp = (T *)C.P;
-            long long mf = C.level_maxf[l], fs = mf * mf, ps = mf * kPanelStride;
+            long long mf = C.level_maxf[l], fs = mf * mf, ps = mf * kWideStride;
             void *args[] = {&dv, &lbb, &cntb, &ngv, &vv, &Lp, &Up, &Fp, &fs, &Pp, &ps, &cs, &derr};
-            e = cudaLaunchCooperativeKernel((void *)k_mf_group_factor<T>, coop_grid, kTB, args, 0, ctx->stream);
+            e = cudaLaunchCooperativeKernel((void *)k_mf_group_factor<T>, coop_grid, kTB, args, gsmem, ctx->stream);
             GRMP_LAUNCHED(ctx);
             gmax = std::max(gmax, coop_grid);
             if (e == cudaSuccess) {   // a timed-out barrier of any group fails the factorisation
