@@ -271,17 +271,41 @@ TRAFFIC_PER_ALGORITHMIC_BYTE = (163.612 + 17.166) / 185.732
 # the same for k_pcg_mixed_duo (two-run 16-bit columns, configuration 60208):
 # 153.315 GB / 163.833 GB on the 48^3 case (summary under profiles/)
 TRAFFIC_PER_ALGORITHMIC_BYTE_DUO = (137.023 + 16.292) / 163.833
+# the same for k_pcg_mixed_duo_keep (Jacobi-scaled two-run columns, A p kept
+# in shared memory, configuration 65208): 138.239 GB / 163.752 GB on the
+# 48^3 case (summary under profiles/)
+TRAFFIC_PER_ALGORITHMIC_BYTE_KEEP = (129.587 + 8.652) / 163.752
+# per persistent kernel
+TRAFFIC_RATIO = {"k_pcg_mixed": TRAFFIC_PER_ALGORITHMIC_BYTE, "k_pcg_mixed_duo": TRAFFIC_PER_ALGORITHMIC_BYTE_DUO,
+                 "k_pcg_mixed_duo_keep": TRAFFIC_PER_ALGORITHMIC_BYTE_KEEP}
+
+
+def duo_family(cfg: int) -> bool:
+    """spmv_config reads the two-run 16-bit column copy (60xxx-65xxx grid-wide,
+    80xxx one cluster)."""
+    return 60000 <= cfg < 70000 or 80000 <= cfg < 90000
+
+
+def pcg_kernel(cfg: int) -> str:
+    if 64000 <= cfg < 66000:
+        return "k_pcg_mixed_duo_keep"
+    if duo_family(cfg):
+        return "k_pcg_mixed_duo"
+    if 20000 <= cfg < 40000:
+        return "k_pcg_mixed_staged"
+    return "k_pcg_mixed"
 
 
 def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool, nduo: int = 0) -> float:
     """Algorithmic DRAM bytes of one persistent PCG launch: per inner
     iteration the matrix once (values + column indices: 8 bytes per entry as
     packed pairs; 12 bytes per pair of entries plus a 16-byte row record in
-    the two-run 16-bit column form, spmv_config 60xxx) and the vector traffic
-    of the update phase; per FP64 refinement one FP64 residual."""
+    the two-run 16-bit column form) and the vector traffic of the update
+    phase of Jacobi-PCG (seven 8-byte streams per row, whatever a kernel keeps
+    on chip); per FP64 refinement one FP64 residual."""
     it, outer = stats["iterations"], stats["outer_iterations"]
     if mixed:
-        if stats.get("spmv_config", 0) >= 60000:
+        if duo_family(stats.get("spmv_config", 0)):
             per_it = 12.0 * nduo + 16.0 * n + 56.0 * n
         else:
             per_it = 8.0 * nnz + 56.0 * n
@@ -470,18 +494,18 @@ def run_ours(args):
     # roofline of the dominant kernel (persistent mixed PCG)
     st_last = mixed["stats"][-1]
     kb = pcg_bytes(st_last, ndofs, nnz, True, nduo)
-    duo = st_last["spmv_config"] >= 60000
+    kname = pcg_kernel(st_last["spmv_config"])
     kms = statistics.mean([s["solve_ms"] for s in mixed["stats"]])
     achieved = kb / (kms / 1e3) / 1e9
     pk = peaks()
     peak = float(pk["hbm_gbs"]) if pk else 6800.0
-    tpab = TRAFFIC_PER_ALGORITHMIC_BYTE_DUO if duo else TRAFFIC_PER_ALGORITHMIC_BYTE
+    tpab = TRAFFIC_RATIO.get(kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": kb * tpab if tpab else None,
-                "traffic_source": (f"ncu dram__bytes_read+write of {'k_pcg_mixed_duo' if duo else 'k_pcg_mixed'} "
+                "traffic_source": (f"ncu dram__bytes_read+write of {kname} "
                                    f"on the 48^3 case ({tpab:.3f} x its algorithmic bytes), scaled to this launch"
                                    if tpab else "not captured for this configuration"),
-                "kernel": "k_pcg_mixed_duo (persistent)" if duo else "k_pcg_mixed (persistent)",
+                "kernel": f"{kname} (persistent)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6800 GB/s"}
     if direct:
         roofline = None   # factorisation-bound (FP32 / FP64 pipes), no HBM roofline line for this solver

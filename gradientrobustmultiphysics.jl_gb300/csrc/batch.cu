@@ -80,11 +80,18 @@ __device__ __forceinline__ void bsum(double *v, double *sh) {
     if (lane == 0)
         for (int k = 0; k < NV; k++) sh[wid * NV + k] = v[k];
     __syncthreads();
-    for (int k = 0; k < NV; k++) {
-        double s = 0;
-        for (int w = 0; w < nw; w++) s += sh[w * NV + k];
-        v[k] = s;
+    // warp 0 adds the per-warp values (fixed shuffle tree) and publishes the
+    // totals; the other threads do not repeat those FP64 additions
+    if (wid == 0) {
+        double a[NV];
+        for (int k = 0; k < NV; k++) a[k] = lane < nw ? sh[lane * NV + k] : 0.0;
+        for (int k = 0; k < NV; k++)
+            for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+        if (lane == 0)
+            for (int k = 0; k < NV; k++) sh[k] = a[k];
     }
+    __syncthreads();
+    for (int k = 0; k < NV; k++) v[k] = sh[k];
     __syncthreads();
 }
 
@@ -94,9 +101,13 @@ __device__ __forceinline__ void bmax1(double *v, double *sh) {
     __syncthreads();
     if (lane == 0) sh[wid] = v[0];
     __syncthreads();
-    double mx = 0.0;
-    for (int w = 0; w < nw; w++) mx = fmax(mx, sh[w]);
-    v[0] = mx;
+    if (wid == 0) {
+        double a = lane < nw ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+        if (lane == 0) sh[0] = a;
+    }
+    __syncthreads();
+    v[0] = sh[0];
     __syncthreads();
 }
 

@@ -104,9 +104,13 @@ struct grmp_matrix_s {
     uint32_t *d_duo_off = nullptr;  // [nduo] two 16-bit column offsets
     int32_t *d_duo_src = nullptr;   // [nduo] CSR position of the first entry (-1 - pos: second is padding)
     void *d_duo_val = nullptr;      // [nduo] float2 values
-    // the FP32 copies (packed pairs / staged windows, duo values) hold the
-    // values of the current solve
-    bool pack_fresh = false, duo_fresh = false;
+    // Jacobi-scaled duo values a_ij / sqrt(a_ii a_jj) (rounded once from FP64)
+    // and the FP64 scale 1 / sqrt(a_ii) of each row, for the scaled solver
+    void *d_duo_sval = nullptr;     // [nduo] float2
+    double *d_duo_sc = nullptr;     // [nrows]
+    // the FP32 copies (packed pairs / staged windows, duo values, scaled duo
+    // values) hold the values of the current solve
+    bool pack_fresh = false, duo_fresh = false, duo_sfresh = false;
     // imported from a host CSC (grmp_matrix_from_csc): no assembly space; the
     // caller's values in CSR order, penalty rows (diagonal >= threshold)
     // eliminated from the FP64 / FP32 values the solvers use
@@ -209,12 +213,18 @@ int grmp_upload(grmp_context ctx, T **dst, const T *src, size_t count) {
 // ---------------------------------------------------------------- device helpers
 #ifdef __CUDACC__
 // Grid-wide barrier for a cooperative (co-resident) launch.  Every wait is
-// bounded: after `limit` polls (about 64 ns each) the waiting block records
-// GRMP_ERR_TIMEOUT in *status and leaves; callers check the return value
-// and exit their loops.
-struct GridBarrier {
-    unsigned int count;
-    unsigned int gen;
+// bounded: after `limit` polls (one L2 round trip plus 32 ns each) the
+// waiting block records GRMP_ERR_TIMEOUT in *status and leaves; callers
+// check the return value and exit their loops.
+//
+// One 64-bit arrival counter that only grows (zeroed before the launch):
+// block b's arrival at the k-th barrier returns a value in [k N, (k+1) N)
+// -- no block reaches barrier k+1 before all N have arrived at barrier k --
+// so the barrier is passed once the counter reaches (old / N + 1) N.  One
+// atomic per block and a poll of the same word: the last arrival releases
+// the waiters directly, with no reset or generation flip in between.
+struct alignas(8) GridBarrier {
+    unsigned long long arrived;
 };
 
 __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nblocks, int *status,
@@ -222,23 +232,17 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned int nbloc
     __shared__ int ok;   // one answer for the whole block, so its threads leave together
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int *vgen = &gb->gen;
-        unsigned int g = *vgen;
         __threadfence();
-        unsigned int arrived = atomicAdd(&gb->count, 1u) + 1u;
-        if (arrived == nblocks) {
-            atomicExch(&gb->count, 0u);
-            __threadfence();
-            atomicAdd(&gb->gen, 1u);
-        } else {
-            long long spins = 0;
-            while (*vgen == g) {
-                if (++spins > limit) {
-                    atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(64);
+        const unsigned long long old = atomicAdd(&gb->arrived, 1ull);
+        const unsigned long long target = (old / nblocks + 1ull) * nblocks;
+        volatile unsigned long long *va = &gb->arrived;
+        long long spins = 0;
+        while (*va < target) {
+            if (++spins > limit) {
+                atomicCAS(status, 0, (int)GRMP_ERR_TIMEOUT);
+                break;
             }
+            __nanosleep(32);
         }
         __threadfence();
         ok = *(volatile int *)status == 0;

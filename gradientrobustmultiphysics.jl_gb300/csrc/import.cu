@@ -112,7 +112,7 @@ int refresh_values(grmp_matrix A) {
     if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "CSC import: value refresh");
     A->imp_npen = cnt;
     A->has64 = A->has32 = true;
-    A->pack_fresh = A->duo_fresh = false;
+    A->pack_fresh = A->duo_fresh = A->duo_sfresh = false;
     return GRMP_OK;
 }
 

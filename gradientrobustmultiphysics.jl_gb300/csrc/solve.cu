@@ -11,10 +11,13 @@
 //    matrix and replaces the FP32 residual ("reliable updates"), keeping the
 //    FP32 search direction.  Convergence is decided on the FP64 residual only.
 //
-// The whole iteration runs in one cooperative launch: three grid barriers per
-// iteration (bounded waits, see grid_barrier), dot products reduced through
-// per-block partials summed in a fixed order by every block, so all blocks
-// take identical decisions and results are reproducible run to run.
+// The whole iteration runs in one persistent launch: a cooperative grid over
+// the GPU (three grid barriers per FP64 iteration, two per mixed one; bounded
+// waits, see grid_barrier) or, for the smallest systems, one thread-block
+// cluster (hardware cluster barriers, see ClusterSync).  Dot products are
+// reduced through per-block partials summed in a fixed order by every block,
+// so all blocks take identical decisions and results are reproducible run to
+// run.
 #include <cooperative_groups.h>
 
 #include <chrono>
@@ -52,21 +55,34 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// Sum NV values over the block; result valid in all threads.
-template <int NV>
-__device__ __forceinline__ void block_sum(double *v, double *sh /* [32*NV] */) {
+// Sum NV values over the block; result valid in all threads.  Warp sums,
+// then warp 0 sums the per-warp values with the same fixed shuffle tree and
+// publishes the totals: one thread's worth of additions per value instead of
+// every thread re-adding all warps' values (on GB300 that redundant work lands
+// on the narrow FP64 pipe).
+template <int NV, typename T>
+__device__ __forceinline__ void block_sum_t(T *v, T *sh /* [32*NV] */) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
     __syncthreads();
     if (lane == 0)
         for (int k = 0; k < NV; k++) sh[wid * NV + k] = v[k];
     __syncthreads();
-    for (int k = 0; k < NV; k++) {
-        double s = 0;
-        for (int w = 0; w < nw; w++) s += sh[w * NV + k];   // fixed order
-        v[k] = s;
+    if (wid == 0) {
+        T a[NV];
+        for (int k = 0; k < NV; k++) a[k] = lane < nw ? sh[lane * NV + k] : T(0);
+        for (int k = 0; k < NV; k++) a[k] = warp_sum(a[k]);
+        if (lane == 0)
+            for (int k = 0; k < NV; k++) sh[k] = a[k];
     }
     __syncthreads();
+    for (int k = 0; k < NV; k++) v[k] = sh[k];
+    __syncthreads();
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum(double *v, double *sh /* [32*NV] */) {
+    block_sum_t<NV, double>(v, sh);
 }
 
 // Write this block's partial sums, pass a grid barrier, then every block sums
@@ -101,18 +117,7 @@ __device__ __forceinline__ bool grid_sum(double *v, double *partial_area, double
 // summation order is fixed as in the FP64 versions.
 template <int NV>
 __device__ __forceinline__ void block_sum_f(float *v, float *sh /* [32*NV] */) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
-    __syncthreads();
-    if (lane == 0)
-        for (int k = 0; k < NV; k++) sh[wid * NV + k] = v[k];
-    __syncthreads();
-    for (int k = 0; k < NV; k++) {
-        float s = 0.f;
-        for (int w = 0; w < nw; w++) s += sh[w * NV + k];
-        v[k] = s;
-    }
-    __syncthreads();
+    block_sum_t<NV, float>(v, sh);
 }
 
 template <int NV>
@@ -131,6 +136,102 @@ __device__ __forceinline__ bool grid_sum_f(float *v, double *partial_area, float
     for (int k = 0; k < NV; k++) v[k] = acc[k];
     return true;
 }
+
+// Synchronisation policies of the persistent solvers.
+//
+// GridSync: a cooperative grid over the whole GPU; barriers and reductions
+// through global memory (grid_barrier, grid_sum), every wait bounded.
+//
+// ClusterSync: the whole solve in ONE thread-block cluster (8 or 16 CTAs on
+// one GPC) for problems whose matrix and vectors sit in L2: the barrier is
+// the hardware cluster barrier (barrier.cluster.arrive.release / wait.acquire,
+// the cluster's analogue of __syncthreads: it orders global and shared
+// memory at cluster scope), and reductions read each CTA's partial sums out
+// of that CTA's shared memory (distributed shared memory) instead of global
+// memory.  Every CTA executes the same sequence of barriers -- all decisions
+// come from sums that every CTA forms in the same fixed order -- so the
+// barrier cannot wait on a CTA that took another path; finish() is a last
+// barrier that keeps every CTA's shared memory alive until no CTA reads it.
+struct GridSync {
+    SolveState *st;
+    double *part;
+    long long spin;
+    int round;
+    __device__ __forceinline__ bool barrier() { return grid_barrier(&st->bar, gridDim.x, &st->status, spin); }
+    template <int NV>
+    __device__ __forceinline__ bool sum(double *v, double *sh) {
+        return grid_sum<NV>(v, part, sh, st, round, spin);
+    }
+    template <int NV>
+    __device__ __forceinline__ bool sumf(float *v, float *sh) {
+        return grid_sum_f<NV>(v, part, sh, st, round, spin);
+    }
+    __device__ __forceinline__ void finish() {}
+};
+
+namespace cg = cooperative_groups;
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// Sum NV values (already block-summed, valid in every thread) over the CTAs
+// of the cluster: thread 0 publishes them in `mine` (this reduction's buffer
+// of two, used alternately as in grid_sum), the cluster barrier, then warp 0
+// reads every CTA's copy in rank order and sums with a fixed shuffle tree.
+template <int NV, typename T>
+__device__ __forceinline__ void cluster_combine(T *v, T (*pub)[4], int par, T *sh) {
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NV; k++) pub[par][k] = v[k];
+    cluster_barrier();
+    cg::cluster_group cl = cg::this_cluster();
+    const int nb = (int)cl.num_blocks();
+    if (threadIdx.x < 32) {
+        T a[NV];
+        for (int k = 0; k < NV; k++) a[k] = T(0);
+        if ((int)threadIdx.x < nb) {
+            const T *rp = cl.map_shared_rank(&pub[par][0], (unsigned)threadIdx.x);
+            for (int k = 0; k < NV; k++) a[k] = rp[k];
+        }
+        for (int k = 0; k < NV; k++) a[k] = warp_sum(a[k]);
+        if (threadIdx.x == 0)
+            for (int k = 0; k < NV; k++) sh[k] = a[k];
+    }
+    __syncthreads();
+    for (int k = 0; k < NV; k++) v[k] = sh[k];
+    __syncthreads();
+}
+
+struct ClusterSync {
+    SolveState *st;
+    double *part;     // unused: partial sums live in shared memory
+    long long spin;   // unused: the cluster barrier is a hardware barrier
+    int round;
+    __device__ __forceinline__ bool barrier() {
+        cluster_barrier();
+        return true;
+    }
+    template <int NV>
+    __device__ __forceinline__ bool sum(double *v, double *sh) {
+        __shared__ double pub[2][4];
+        block_sum<NV>(v, sh);
+        cluster_combine<NV, double>(v, pub, round++ & 1, sh);
+        return true;
+    }
+    template <int NV>
+    __device__ __forceinline__ bool sumf(float *v, float *sh) {
+        __shared__ float pub[2][4];
+        block_sum_f<NV>(v, sh);
+        cluster_combine<NV, float>(v, pub, round++ & 1, sh);
+        return true;
+    }
+    __device__ __forceinline__ void finish() { cluster_barrier(); }
+};
+
+template <bool CL>
+using SyncOf = typename std::conditional<CL, ClusterSync, GridSync>::type;
+
+constexpr int kClT = 1024;   // threads per CTA of the cluster solvers
 
 // Row loop shared by the SpMV variants: groups of TPR lanes per row, each
 // lane with U independent (column, value) loads per chunk.  With PIPE the
@@ -283,19 +384,19 @@ __device__ __forceinline__ double spmv_grid(int n, const int32_t *__restrict__ r
 }
 
 // ------------------------------------------------------------------ FP64 PCG
-template <int TPR, int U, bool PIPE>
-__global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
+template <int TPR, int U, bool PIPE, bool CL = false>
+__global__ void __launch_bounds__(CL ? kClT : PTPB, CL ? 1 : (PIPE && U >= 8 ? 2 : 4)) k_pcg64(int n, const int32_t *rowptr, const int32_t *cols,
                                                 const double *vals, const double *b, double *x, const double *dinv,
                                                 double *r, double *z, double *p, double *q, double *partial,
                                                 SolveState *st, double abstol, double reltol, int maxit, int guess,
                                                 long long spin) {
     __shared__ double sh[32 * 4];
-    int round = 0;
+    SyncOf<CL> sy{st, partial, spin, 0};
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // r = b - A x  (or b)
     if (guess) spmv_grid<TPR, U, PIPE, double, double, double, false, true>(n, rowptr, cols, vals, x, r, nullptr, b);
-    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+    if (!sy.barrier()) return;
     double v[3] = {0, 0, 0};
     for (int i = gtid; i < n; i += gsz) {
         double ri = guess ? r[i] : b[i];
@@ -307,7 +408,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
         v[1] += ri * ri;
         v[2] += b[i] * b[i];
     }
-    if (!grid_sum<3>(v, partial, sh, st, round, spin)) return;
+    if (!sy.template sum<3>(v, sh)) return;
     double rz = v[0], rr = v[1];
     const double bn = sqrt(v[2]);
     const double tol = fmax(abstol, reltol * bn);
@@ -316,7 +417,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
     while (!conv && it < maxit) {
         double d[1];
         d[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, false>(n, rowptr, cols, vals, p, q, p, nullptr);
-        if (!grid_sum<1>(d, partial, sh, st, round, spin)) return;
+        if (!sy.template sum<1>(d, sh)) return;
         const double pq = d[0];
         if (!(pq > 0) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
@@ -333,7 +434,7 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
             w[0] += ri * zi;
             w[1] += ri * ri;
         }
-        if (!grid_sum<2>(w, partial, sh, st, round, spin)) return;
+        if (!sy.template sum<2>(w, sh)) return;
         it++;
         rr = w[1];
         conv = sqrt(rr) <= tol;
@@ -341,19 +442,20 @@ __global__ void __launch_bounds__(PTPB, PIPE && U >= 8 ? 2 : 4) k_pcg64(int n, c
         const double beta = w[0] / rz;
         rz = w[0];
         for (int i = gtid; i < n; i += gsz) p[i] = z[i] + beta * p[i];
-        if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+        if (!sy.barrier()) return;
     }
     // true residual in FP64
-    if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+    if (!sy.barrier()) return;
     double t[1];
     t[0] = spmv_grid<TPR, U, PIPE, double, double, double, true, true>(n, rowptr, cols, vals, x, r, nullptr, b);
-    if (!grid_sum<1>(t, partial, sh, st, round, spin)) return;
+    if (!sy.template sum<1>(t, sh)) return;
     if (gtid == 0) {
         st->iters = it;
         st->outer = 0;
         st->relres = sqrt(t[0]) / (bn > 0 ? bn : 1.0);
         if (st->status == 0 && !(sqrt(t[0]) <= fmax(tol, 0.0) || conv)) st->status = GRMP_ERR_NOT_CONVERGED;
     }
+    sy.finish();
 }
 
 // ------------------------------------------------------------------ FP64 BiCGStab
@@ -527,14 +629,13 @@ struct RowsSpmv {
 // the fly, the owner of row i stores the pair (z_k, p_k) into nxt[i]; the
 // vector phase (four rows per thread, 16-byte loads) reads p_k from nxt[i],
 // updates x, r and writes z_{k+1} over the pair's first half.
-template <class SP>
-__device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, double *x, const float *dinv, float *r,
-                                               float *q, float *xc, float2 *zp0, float2 *zp1, double *r64,
-                                               double *partial, SolveState *st, double abstol, double reltol,
-                                               double delta, int maxit, int maxouter, int guess, long long spin) {
+template <class SP, class SY>
+__device__ __forceinline__ void pcg_mixed_body(SP &sp, SY &sy, int n, const double *b, double *x, const float *dinv,
+                                               float *r, float *q, float *xc, float2 *zp0, float2 *zp1, double *r64,
+                                               SolveState *st, double abstol, double reltol, double delta, int maxit,
+                                               int maxouter, int guess) {
     __shared__ double sh[32 * 4];
     __shared__ float shf[32 * 4];
-    int round = 0;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
     // FP64 residual of the initial guess
@@ -549,7 +650,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
         }
     }
     for (int i = gtid; i < n; i += gsz) v[1] += b[i] * b[i];
-    if (!grid_sum<2>(v, partial, sh, st, round, spin)) return;
+    if (!sy.template sum<2>(v, sh)) return;
     const double bn = sqrt(v[1]);
     const double tol = fmax(abstol, reltol * bn);
     double rn64 = sqrt(v[0]);
@@ -566,7 +667,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
         wf += ri * zi;
     }
     float w[1] = {wf};
-    if (!grid_sum_f<1>(w, partial, shf, st, round, spin)) return;
+    if (!sy.template sumf<1>(w, shf)) return;
     // inner-iteration scalars in FP32 (the FP64 pipe is scarce)
     float rz = w[0];
     float rmax = (float)rn64;
@@ -578,7 +679,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
     const int n4 = n >> 2;
     while (!conv && it < maxit && outer < maxouter) {
         float d[1] = {sp.fused_zp(cur, nxt, q, beta)};
-        if (!grid_sum_f<1>(d, partial, shf, st, round, spin)) return;   // barrier 1
+        if (!sy.template sumf<1>(d, shf)) return;   // barrier 1
         const float pq = d[0];
         if (!(pq > 0.f) || !isfinite(pq)) {
             if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
@@ -628,7 +729,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
             }
         }
         float u[2] = {uf0, uf1};
-        if (!grid_sum_f<2>(u, partial, shf, st, round, spin)) return;   // barrier 2
+        if (!sy.template sumf<2>(u, shf)) return;   // barrier 2
         it++;
         float rz_new = u[0];
         const float rn32 = sqrtf(u[1]);
@@ -639,10 +740,10 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
                 x[i] += (double)xc[i];
                 xc[i] = 0.0f;
             }
-            if (!grid_barrier(&st->bar, gridDim.x, &st->status, spin)) return;
+            if (!sy.barrier()) return;
             double t[1];
             t[0] = sp.resid64(x, r64, b);
-            if (!grid_sum<1>(t, partial, sh, st, round, spin)) return;
+            if (!sy.template sum<1>(t, sh)) return;
             outer++;
             rn64 = sqrt(t[0]);
             conv = rn64 <= tol;
@@ -665,7 +766,7 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
                 yf += ri * zi;
             }
             float y[1] = {yf};
-            if (!grid_sum_f<1>(y, partial, shf, st, round, spin)) return;
+            if (!sy.template sumf<1>(y, shf)) return;
             rz_new = y[0];
             rmax = (float)rn64;
         }
@@ -683,16 +784,17 @@ __device__ __forceinline__ void pcg_mixed_body(SP &sp, int n, const double *b, d
     }
 }
 
-template <int TPR, int U, bool PIPE>
-__global__ void __launch_bounds__(PTPB, PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) : (U >= 8 ? 4 : 5)) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
+template <int TPR, int U, bool PIPE, bool CL = false>
+__global__ void __launch_bounds__(CL ? kClT : PTPB, CL ? 1 : (PIPE ? (U >= 8 ? 3 : (U >= 4 ? 4 : 6)) : (U >= 8 ? 4 : 5))) k_pcg_mixed(int n, const int32_t *rowptr, const int32_t *cols,
                                                     const double *vals64, const int2 *pack32, const double *b,
                                                     double *x, const float *dinv, float *r, float *q, float *xc,
                                                     float2 *zp0, float2 *zp1, double *r64, double *partial,
                                                     SolveState *st, double abstol, double reltol, double delta,
                                                     int maxit, int maxouter, int guess, long long spin) {
     RowsSpmv<TPR, U, PIPE> sp{n, rowptr, cols, vals64, pack32};
-    pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
-                   guess, spin);
+    SyncOf<CL> sy{st, partial, spin, 0};
+    pcg_mixed_body(sp, sy, n, b, x, dinv, r, q, xc, zp0, zp1, r64, st, abstol, reltol, delta, maxit, maxouter, guess);
+    sy.finish();
 }
 
 // ------------------------------------------------------------ duo mixed PCG
@@ -829,15 +931,252 @@ struct DuoSpmv {
     }
 };
 
-template <int TPR, int U>
-__global__ void __launch_bounds__(PTPB, U >= 4 ? 3 : 4) k_pcg_mixed_duo(
+template <int TPR, int U, bool CL = false>
+__global__ void __launch_bounds__(CL ? kClT : PTPB, CL ? 1 : (U >= 4 ? 3 : 4)) k_pcg_mixed_duo(
     int n, const int32_t *rowptr, const int32_t *cols, const double *vals64, const int4 *meta, const uint32_t *off,
     const float2 *val, const double *b, double *x, const float *dinv, float *r, float *q, float *xc, float2 *zp0,
     float2 *zp1, double *r64, double *partial, SolveState *st, double abstol, double reltol, double delta, int maxit,
     int maxouter, int guess, long long spin) {
     DuoSpmv<TPR, U> sp{n, rowptr, cols, vals64, meta, off, val};
-    pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
-                   guess, spin);
+    SyncOf<CL> sy{st, partial, spin, 0};
+    pcg_mixed_body(sp, sy, n, b, x, dinv, r, q, xc, zp0, zp1, r64, st, abstol, reltol, delta, maxit, maxouter, guess);
+    sy.finish();
+}
+
+// ------------------------------------------------ scaled duo mixed PCG (keep)
+// The mixed solver on the Jacobi-scaled system  S A S y = S b,  x = S y,
+// S = diag(1 / sqrt(a_ii)): unpreconditioned CG on S A S is Jacobi-PCG on A,
+// with z = r, so the (z, p) pair is (r, p) and neither a separate residual
+// array nor the inverse diagonal is streamed.  The row loop gives every row
+// group a fixed list of rows (first row + j * stride, j < J); the SpMV phase
+// keeps each row's r, p and (S A S p) in shared memory ([3][J][groups of the
+// block]) and the vector phase, run by the same group after the p.q
+// reduction, updates the row from there.  Per row and iteration the vector
+// streams left are the own pair (read), the FP32 correction (read, write) and
+// the next pair (write) -- against nine 4-byte words of the unscaled solver.
+// The FP64 refinement is unchanged: x += S xc, r64 = b - A x with the FP64
+// matrix, the scaled FP32 residual S r64.
+template <int TPR, int U, bool ALL>
+__device__ __forceinline__ float duo_zp_keep(int n, const int4 *__restrict__ meta, const uint32_t *__restrict__ off,
+                                             const float2 *__restrict__ val, const float2 *cur, float beta, float *kr,
+                                             float *kp, float *kq) {
+    constexpr int RPW = 32 / TPR;
+    constexpr int CH = TPR * U;
+    constexpr int G = PTPB / TPR;
+    const int lane = threadIdx.x & (TPR - 1);
+    const int gin = (threadIdx.x & 31) / TPR;
+    const int g = threadIdx.x / TPR;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int stride = ((gridDim.x * blockDim.x) >> 5) * RPW;
+    auto gp = [&](int c) {
+        const float2 v = cur[c];
+        return __fmaf_rn(beta, v.y, v.x);
+    };
+    float dacc = 0.f;
+    int r = warp * RPW + gin;
+    int j = 0;
+    DuoRow d = duo_row(meta, r, n);
+    DuoRow dn = duo_row(meta, r + stride, n);
+    float2 v[U];
+    uint32_t o[U];
+    duo_chunk<U, TPR>(val, off, d, d.kb + lane, v, o);
+    for (int base = warp * RPW; base < n; base += stride, j++) {
+        float2 vn[U];
+        uint32_t on[U];
+        duo_chunk<U, TPR>(val, off, dn, dn.kb + lane, vn, on);
+        const DuoRow d2 = duo_row(meta, r + 2 * stride, n);
+        float s = 0.f;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int c0, c1;
+            duo_cols(d, d.kb + lane + u * TPR, o[u], c0, c1);
+            s += v[u].x * gp(c0);
+            s += v[u].y * gp(c1);
+        }
+        for (int k = d.kb + lane + CH; k < d.e; k += CH) {   // rows longer than one chunk
+            float2 v2[U];
+            uint32_t o2[U];
+            duo_chunk<U, TPR>(val, off, d, k, v2, o2);
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                int c0, c1;
+                duo_cols(d, k + u * TPR, o2[u], c0, c1);
+                s += v2[u].x * gp(c0);
+                s += v2[u].y * gp(c1);
+            }
+        }
+#pragma unroll
+        for (int w = TPR / 2; w > 0; w >>= 1) s += __shfl_xor_sync(0xffffffffu, s, w);
+        if (r < n && lane == 0) {
+            const float2 me = cur[r];
+            const float pn = __fmaf_rn(beta, me.y, me.x);
+            const int k = j * G + g;
+            if (ALL) {
+                kr[k] = me.x;
+                kp[k] = pn;
+            }
+            kq[k] = s;
+            dacc += pn * s;
+        }
+        r += stride;
+        d = dn;
+        dn = d2;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            v[u] = vn[u];
+            o[u] = on[u];
+        }
+    }
+    return dacc;
+}
+
+template <int TPR, int U, bool ALL>
+__global__ void __launch_bounds__(PTPB, U >= 4 ? 3 : 4) k_pcg_mixed_duo_keep(
+    int n, const int32_t *rowptr, const int32_t *cols, const double *vals64, const int4 *meta, const uint32_t *off,
+    const float2 *sval, const double *b, double *x, const double *sc, float *xc, float2 *zp0, float2 *zp1,
+    double *r64, double *partial, SolveState *st, double abstol, double reltol, double delta, int maxit,
+    int maxouter, int guess, long long spin, int J) {
+    extern __shared__ float keep[];
+    constexpr int G = PTPB / TPR, RPW = 32 / TPR, VB = 8;
+    // ALL: r, p and A p per slot; else A p only (r and p from the pair)
+    float *kq = keep, *kr = keep + (size_t)J * G, *kp = keep + 2 * (size_t)J * G;
+    __shared__ double sh[32 * 4];
+    __shared__ float shf[32 * 4];
+    GridSync sy{st, partial, spin, 0};
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsz = gridDim.x * blockDim.x;
+    // slot k = j * G + g of this block holds row  blockIdx.x * G + g + j * stride
+    // (group g's j-th row in the SpMV row loop)
+    const int stride = (gsz >> 5) * RPW;
+    const int rbase = blockIdx.x * G;
+    const int nslot = J * G;
+    auto resid64 = [&]() {
+        return spmv_grid<4, 4, true, double, double, double, true, true>(n, rowptr, cols, vals64, x, r64, nullptr, b);
+    };
+    // FP64 residual of the initial guess
+    double v[2] = {0, 0};
+    if (guess) {
+        v[0] = resid64();
+    } else {
+        for (int i = gtid; i < n; i += gsz) {
+            x[i] = 0.0;
+            r64[i] = b[i];
+            v[0] += b[i] * b[i];
+        }
+    }
+    for (int i = gtid; i < n; i += gsz) v[1] += b[i] * b[i];
+    if (!sy.template sum<2>(v, sh)) return;
+    const double bn = sqrt(v[1]);
+    const double tol = fmax(abstol, reltol * bn);
+    double rn64 = sqrt(v[0]);
+    int it = 0, outer = 0;
+    bool conv = rn64 <= tol;
+    // scaled FP32 residual S r64; p_{-1} = 0
+    float wf = 0.f;
+    for (int i = gtid; i < n; i += gsz) {
+        const float ri = (float)(sc[i] * r64[i]);
+        zp0[i] = make_float2(ri, 0.f);
+        xc[i] = 0.0f;
+        wf += ri * ri;
+    }
+    float w[1] = {wf};
+    if (!sy.template sumf<1>(w, shf)) return;
+    float rz = w[0];
+    float rmax = sqrtf(rz);
+    // the refinement also runs once the unscaled residual, estimated from the
+    // scaled one with the ratio seen at the last refinement, is below tol
+    float ratio = rmax > 0.f ? (float)(rn64 / (double)rmax) : 1.f;
+    const float tolf = (float)tol;
+    const float deltaf = (float)delta;
+    double prev_rn64 = rn64;
+    int stall = 0;
+    float beta = 0.f;
+    float2 *cur = zp0, *nxt = zp1;
+    while (!conv && it < maxit && outer < maxouter) {
+        float d[1] = {duo_zp_keep<TPR, U, ALL>(n, meta, off, sval, cur, beta, kr, kp, kq)};
+        if (!sy.template sumf<1>(d, shf)) return;   // barrier 1
+        const float pq = d[0];
+        if (!(pq > 0.f) || !isfinite(pq)) {
+            if (gtid == 0) atomicCAS(&st->status, 0, (int)GRMP_ERR_NAN);
+            break;
+        }
+        const float alpha = rz / pq;
+        float uf = 0.f;
+        // the block's slots over all its threads (consecutive threads,
+        // consecutive rows), VB independent correction loads in flight
+        for (int k0 = threadIdx.x; k0 < nslot; k0 += PTPB * VB) {
+            float xv[VB];
+            float2 cv[VB];
+            int rr[VB];
+#pragma unroll
+            for (int t = 0; t < VB; t++) {
+                const int k = k0 + t * PTPB;
+                rr[t] = k < nslot ? rbase + (k % G) + (k / G) * stride : n;
+                xv[t] = rr[t] < n ? xc[rr[t]] : 0.f;
+                if (!ALL) cv[t] = rr[t] < n ? cur[rr[t]] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int t = 0; t < VB; t++) {
+                if (rr[t] < n) {
+                    const int k = k0 + t * PTPB;
+                    // p_k as the SpMV formed it (same fmaf): identical values
+                    const float pk = ALL ? kp[k] : __fmaf_rn(beta, cv[t].y, cv[t].x);
+                    const float rn = (ALL ? kr[k] : cv[t].x) - alpha * kq[k];
+                    xc[rr[t]] = xv[t] + alpha * pk;
+                    nxt[rr[t]] = make_float2(rn, pk);
+                    uf += rn * rn;
+                }
+            }
+        }
+        float u[1] = {uf};
+        if (!sy.template sumf<1>(u, shf)) return;   // barrier 2
+        it++;
+        float rz_new = u[0];
+        const float rn32 = sqrtf(rz_new);
+        bool restart = false;
+        if (rn32 <= deltaf * rmax || ratio * rn32 <= tolf || it >= maxit) {
+            // refinement: fold S xc into x, recompute b - A x in FP64
+            for (int i = gtid; i < n; i += gsz) {
+                x[i] += sc[i] * (double)xc[i];
+                xc[i] = 0.0f;
+            }
+            if (!sy.barrier()) return;
+            double t[1] = {resid64()};
+            if (!sy.template sum<1>(t, sh)) return;
+            outer++;
+            rn64 = sqrt(t[0]);
+            conv = rn64 <= tol;
+            if (conv || it >= maxit) break;
+            // as in pcg_mixed_body: restart the inner CG when the true residual
+            // stops falling, give up after 16 refinements without progress
+            restart = rn64 > 0.5 * prev_rn64;
+            stall = (rn64 > 0.9 * prev_rn64) ? stall + 1 : 0;
+            prev_rn64 = rn64;
+            if (stall >= 16) break;
+            float yf = 0.f;
+            for (int i = gtid; i < n; i += gsz) {
+                const float ri = (float)(sc[i] * r64[i]);
+                nxt[i].x = ri;
+                yf += ri * ri;
+            }
+            float y[1] = {yf};
+            if (!sy.template sumf<1>(y, shf)) return;
+            rz_new = y[0];
+            rmax = sqrtf(rz_new);
+            ratio = rmax > 0.f ? (float)(rn64 / (double)rmax) : 1.f;
+        }
+        beta = restart ? 0.0f : rz_new / rz;
+        rz = rz_new;
+        float2 *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    if (gtid == 0) {
+        st->iters = it;
+        st->outer = outer;
+        st->relres = rn64 / (bn > 0 ? bn : 1.0);
+        if (st->status == 0 && !conv) st->status = GRMP_ERR_NOT_CONVERGED;
+    }
 }
 
 // values of the duo copy from the CSR FP32 values (one thread per duo)
@@ -1069,8 +1408,8 @@ __global__ void __launch_bounds__(NT, 2048 / NT / 2) k_pcg_mixed_staged(int n, c
     }
     __syncthreads();
     sp.prologue();
-    pcg_mixed_body(sp, n, b, x, dinv, r, q, xc, zp0, zp1, r64, partial, st, abstol, reltol, delta, maxit, maxouter,
-                   guess, spin);
+    GridSync sy{st, partial, spin, 0};
+    pcg_mixed_body(sp, sy, n, b, x, dinv, r, q, xc, zp0, zp1, r64, st, abstol, reltol, delta, maxit, maxouter, guess);
     sp.drain();
 }
 
@@ -1146,11 +1485,16 @@ void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, co
 // flight per lane), encoded 100*TPR + U; + 10000: software-pipelined row
 // loop; + 20000: staged windows, 512 threads x 3 stages per block; + 30000:
 // staged windows, 1024 threads x 6 stages (the staged ones: mixed solves only).
+// (The cluster configurations 7xxxx / 8xxxx are not timed: on systems of
+// 20,000 rows and more, where the autotuner runs, the grid-wide solvers are
+// faster; the row-length heuristic uses them for the smallest mixed solves.)
 constexpr int kConfigs[] = {208,   404,   408,   804,   1602,  10204, 10404, 10408, 10804, 10402,
-                            10802, 20204, 20408, 20804, 30408, 30804, 60404, 60208, 60802, 60408};
+                            10802, 20204, 20408, 20804, 30408, 30804, 60404, 60208, 60802, 60408, 64208, 64404,
+                            65208, 65404};
 
 inline bool staged_config(int cfg) { return cfg >= 20000 && cfg < 60000; }
-inline bool duo_config(int cfg) { return cfg >= 60000; }
+inline bool duo_config(int cfg) { return (cfg >= 60000 && cfg < 70000) || cfg >= 80000; }
+inline bool cluster_config(int cfg) { return cfg >= 70000; }
 
 // Window layout of the staged SpMV, built once per matrix pattern from the
 // row pointers (greedy: whole rows while header + entries fit one record).
@@ -1286,6 +1630,78 @@ int ensure_duo(grmp_matrix A) {
     return GRMP_OK;
 }
 
+// The Jacobi-scaled duo values of the current FP64 values (scaled solver):
+// the FP64 row scales 1 / sqrt(a_ii), then each duo's two values
+// a_ij * s_i * s_j rounded once to FP32.  *bad is set for a non-positive or
+// non-finite diagonal entry.
+__global__ void k_duo_scales(int n, const int32_t *rowptr, const int32_t *cols, const double *vals, double *sc,
+                             int *bad) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double d = 0.0;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; k++)
+        if (cols[k] == r) d = vals[k];
+    if (!(d > 0.0) || !isfinite(d)) {
+        atomicExch(bad, 1);
+        sc[r] = 0.0;
+        return;
+    }
+    sc[r] = 1.0 / sqrt(d);
+}
+
+// one thread per row: the row's duos (their source positions are the row's
+// CSR entries in order)
+__global__ void k_duo_fill_scaled(int n, const int4 *meta, const int32_t *src, const int32_t *cols,
+                                  const double *vals, const double *sc, float2 *sval) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int4 m = meta[r];
+    const double sr = sc[r];
+    const int d0 = m.x, d1 = m.x + (m.w >> 16);
+    for (int d = d0; d < d1; d++) {
+        const int s = src[d];
+        const int k = s >= 0 ? s : -1 - s;
+        const float v0 = (float)(vals[k] * sr * sc[cols[k]]);
+        const float v1 = s >= 0 ? (float)(vals[k + 1] * sr * sc[cols[k + 1]]) : 0.f;
+        sval[d] = make_float2(v0, v1);
+    }
+}
+
+int ensure_duo_scaled(grmp_matrix A) {
+    grmp_context ctx = A->space->mesh->ctx;
+    int rc = ensure_duo(A);
+    if (rc) return rc;
+    if (!A->d_duo_sval) {
+        rc = grmp_alloc(ctx, &A->d_duo_sval, (size_t)A->duo_nduo * 8);
+        if (!rc) rc = grmp_alloc(ctx, (void **)&A->d_duo_sc, (size_t)A->nrows * 8);
+        if (rc) {
+            grmp_free(ctx, A->d_duo_sval, (size_t)A->duo_nduo * 8);
+            A->d_duo_sval = nullptr;
+            return rc;
+        }
+    }
+    if (!A->duo_sfresh) {
+        const int n = A->nrows;
+        int *bad = nullptr;
+        rc = grmp_alloc(ctx, (void **)&bad, 4);
+        if (rc) return rc;
+        cudaMemsetAsync(bad, 0, 4, ctx->stream);
+        k_duo_scales<<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, A->d_duo_sc, bad);
+        GRMP_LAUNCHED(ctx);
+        k_duo_fill_scaled<<<nblk(n), 256, 0, ctx->stream>>>(n, (const int4 *)A->d_duo_meta, A->d_duo_src, A->d_cols,
+                                                             A->d_vals64, A->d_duo_sc, (float2 *)A->d_duo_sval);
+        GRMP_LAUNCHED(ctx);
+        int hbad = 0;
+        cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        grmp_free(ctx, bad, 4);
+        if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "scaled duo values");
+        if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
+        A->duo_sfresh = true;
+    }
+    return GRMP_OK;
+}
+
 int heuristic_tpr(grmp_matrix A) {
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
     if (avg <= 3) return 2;
@@ -1297,9 +1713,16 @@ int heuristic_tpr(grmp_matrix A) {
 
 // Configuration from the mean row length alone (no timing): the autotuner's
 // usual choices on FEM matrices -- plain row loops for FP64 (FP64-pipe bound,
-// more loads in flight do not help), the pipelined row loop for FP32.
+// more loads in flight do not help), the pipelined row loop for FP32 -- and,
+// for mixed solves of at most kClusterRows rows, the one-cluster solver
+// (measured on 2D P1 systems of 1,089 and 4,225 rows: 6.8 and 7.5 us per
+// iteration against 7.8 and 8.2 for the best grid-wide configuration; on
+// 15,625 rows of 3D P2 the grid-wide solver is faster).
+constexpr int kClusterRows = 8192;
+
 int heuristic_config(grmp_matrix A, bool mixed) {
     double avg = (double)A->nnz / (double)std::max(1, A->nrows);
+    if (mixed && A->nrows <= kClusterRows) return avg <= 10 ? 70204 : 70404;
     if (mixed) {
         if (avg <= 8) return 10204;
         if (avg <= 20) return 10404;
@@ -1320,7 +1743,75 @@ int coop_grid(grmp_context ctx, K kern, int n, int want) {
     return std::max(1, g);
 }
 
-template <int TPR, int U, bool PIPE>
+// Cluster size of a cluster solver: 16 CTAs (non-portable size) where such
+// a cluster fits on this GPU, else the portable 8.  Returns 0 when neither
+// fits.  (Sets the kernel's non-portable-size attribute, which a launch with
+// 16 CTAs needs.)
+template <typename K>
+int cluster_ctas(K kern) {
+    int c = 0;
+    for (int want : {16, 8}) {
+        if (want > 8 &&
+            cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t lc{};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)want;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        lc.gridDim = dim3((unsigned)want);
+        lc.blockDim = dim3(kClT);
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        int ncl = 0;
+        if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)kern, &lc) != cudaSuccess) {
+            cudaGetLastError();
+            ncl = 0;
+        }
+        if (ncl >= 1) {
+            c = want;
+            break;
+        }
+    }
+    return c;
+}
+
+// One cluster of `ctas` CTAs of kClT threads on the context's stream.
+template <typename K>
+cudaError_t launch_cluster(grmp_context ctx, K kern, int ctas, void **args) {
+    cudaLaunchConfig_t lc{};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)ctas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3((unsigned)ctas);
+    lc.blockDim = dim3(kClT);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = ctx->stream;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelExC(&lc, (const void *)kern, args);
+}
+
+// Persistent launch of a solver kernel: a cooperative grid (CL false) or one
+// cluster (CL true).  *grid receives the number of CTAs.
+template <bool CL, typename K>
+cudaError_t launch_persistent(grmp_context ctx, K kern, int n, int want, void **args, int *grid) {
+    if (CL) {
+        const int c = cluster_ctas(kern);
+        *grid = c;
+        if (c < 1) return cudaErrorInvalidConfiguration;
+        return launch_cluster(ctx, kern, c, args);
+    }
+    *grid = coop_grid(ctx, kern, n, want);
+    return cudaLaunchCooperativeKernel((void *)kern, *grid, PTPB, args, 0, ctx->stream);
+}
+
+template <int TPR, int U, bool PIPE, bool CL = false>
 int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p, grmp_solve_stats *out,
                char *work, SolveState *dst, WorkLayout lay) {
     grmp_context ctx = A->space->mesh->ctx;
@@ -1334,8 +1825,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
     cudaEventCreate(&e1);
     cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
     if (!mixed) {
-        auto kern = k_pcg64<TPR, U, PIPE>;
-        grid = coop_grid(ctx, kern, n, p->grid_blocks);
+        auto kern = k_pcg64<TPR, U, PIPE, CL>;
         double *dinv = (double *)work, *r = (double *)(work + lay.vec), *z = (double *)(work + 2 * lay.vec);
         double *pp = (double *)(work + 3 * lay.vec), *q = (double *)(work + 4 * lay.vec);
         double *part = (double *)(work + lay.off_part);
@@ -1347,7 +1837,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         long long spin = ctx->wait_limit;
         void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess, &spin};
         cudaEventRecord(e0, ctx->stream);
-        e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+        e = launch_persistent<CL>(ctx, kern, n, p->grid_blocks, args, &grid);
         GRMP_LAUNCHED(ctx);
         cudaEventRecord(e1, ctx->stream);
     } else {
@@ -1357,8 +1847,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
             cudaEventDestroy(e1);
             return prc;
         }
-        auto kern = k_pcg_mixed<TPR, U, PIPE>;
-        grid = coop_grid(ctx, kern, n, p->grid_blocks);
+        auto kern = k_pcg_mixed<TPR, U, PIPE, CL>;
         float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
         float *xc = (float *)(work + 3 * lay.vec);
         float2 *zp0 = (float2 *)(work + 4 * lay.vec), *zp1 = (float2 *)(work + 6 * lay.vec);
@@ -1374,7 +1863,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
         void *args[] = {&nn, &rp, &ci, &v64, &v32, &bb, &xx, &dinv, &r, &q, &xc, &zp0, &zp1, &r64, &part, &dst,
                         &at, &rt, &dl, &mi, &mo, &guess, &spin};
         cudaEventRecord(e0, ctx->stream);
-        e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+        e = launch_persistent<CL>(ctx, kern, n, p->grid_blocks, args, &grid);
         GRMP_LAUNCHED(ctx);
         cudaEventRecord(e1, ctx->stream);
     }
@@ -1390,7 +1879,7 @@ int launch_pcg(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve
     out->iterations = hs.iters;
     out->outer_iterations = hs.outer;
     out->final_relres = hs.relres;
-    out->spmv_config = 100 * TPR + U + (PIPE ? 10000 : 0);
+    out->spmv_config = 100 * TPR + U + (CL ? 70000 : (PIPE ? 10000 : 0));
     out->grid_blocks = grid;
     out->solve_ms = ms;
     if (hs.status == GRMP_ERR_NOT_CONVERGED)
@@ -1474,18 +1963,18 @@ int launch_pcg_staged(grmp_matrix A, const double *bvec, double *xvec, const grm
 }
 
 // Mixed solve over the duo copy (configurations 60000 + 100 * lanes + duos in flight).
-template <int TPR, int U>
+template <int TPR, int U, bool CL = false>
 int launch_pcg_duo(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p, grmp_solve_stats *out,
                    char *work, SolveState *dst, WorkLayout lay) {
     grmp_context ctx = A->space->mesh->ctx;
-    const int cfg = 60000 + 100 * TPR + U;
+    const int cfg = (CL ? 80000 : 60000) + 100 * TPR + U;
     if (p->mode != GRMP_SOLVE_MIXED)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: duo configurations are for mixed solves", cfg);
     int rc = ensure_duo(A);
     if (rc) return rc;
     const int n = A->nrows;
-    auto kern = k_pcg_mixed_duo<TPR, U>;
-    const int grid = coop_grid(ctx, kern, n, p->grid_blocks);
+    auto kern = k_pcg_mixed_duo<TPR, U, CL>;
+    int grid = 0;
     float *dinv = (float *)work, *r = (float *)(work + lay.vec), *q = (float *)(work + 2 * lay.vec);
     float *xc = (float *)(work + 3 * lay.vec);
     float2 *zp0 = (float2 *)(work + 4 * lay.vec), *zp1 = (float2 *)(work + 6 * lay.vec);
@@ -1508,7 +1997,7 @@ int launch_pcg_duo(grmp_matrix A, const double *bvec, double *xvec, const grmp_s
     cudaEventCreate(&e1);
     cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
     cudaEventRecord(e0, ctx->stream);
-    cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+    cudaError_t e = launch_persistent<CL>(ctx, kern, n, p->grid_blocks, args, &grid);
     GRMP_LAUNCHED(ctx);
     cudaEventRecord(e1, ctx->stream);
     SolveState hs;
@@ -1534,9 +2023,112 @@ int launch_pcg_duo(grmp_matrix A, const double *bvec, double *xvec, const grmp_s
     return hs.status;
 }
 
+// Mixed solve over the Jacobi-scaled duo copy with the row state kept in
+// shared memory (configurations 64000 + 100 * lanes + duos in flight).  Each
+// block keeps 12 bytes per row of its rows: about 12 n / (number of SMs)
+// bytes per SM whatever the grid, so systems beyond about 2.8 M rows do not
+// fit (GRMP_ERR_UNSUPPORTED).
+template <int TPR, int U, bool ALL>
+int launch_pcg_duo_keep(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
+                        grmp_solve_stats *out, char *work, SolveState *dst, WorkLayout lay) {
+    grmp_context ctx = A->space->mesh->ctx;
+    const int cfg = (ALL ? 64000 : 65000) + 100 * TPR + U;
+    constexpr int KW = ALL ? 3 : 1;   // words kept per row
+    if (p->mode != GRMP_SOLVE_MIXED)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: duo configurations are for mixed solves", cfg);
+    int rc = ensure_duo_scaled(A);
+    if (rc) return rc;
+    const int n = A->nrows;
+    constexpr int G = PTPB / TPR;
+    auto kern = k_pcg_mixed_duo_keep<TPR, U, ALL>;
+    int dev_max = 0;
+    cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PTPB, 0);
+    int grid = 0, J = 0;
+    size_t smem = 0;
+    for (int bps = std::max(1, per_sm); bps >= 1 && !grid; bps--) {
+        int gtry = bps * ctx->num_sms;
+        if (p->grid_blocks > 0) gtry = std::min(gtry, p->grid_blocks);
+        const long long stride = (long long)gtry * G;
+        const int jt = (int)((n + stride - 1) / stride);
+        const size_t sb = (size_t)KW * jt * G * 4;
+        if ((long long)sb > dev_max) continue;
+        if (cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, PTPB, sb);
+        if ((long long)occ * ctx->num_sms >= gtry) {
+            grid = gtry;
+            J = jt;
+            smem = sb;
+        }
+    }
+    if (!grid)
+        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: %d rows of row state do not fit shared memory",
+                         cfg, n);
+    float *xc = (float *)(work + 3 * lay.vec);
+    float2 *zp0 = (float2 *)(work + 4 * lay.vec), *zp1 = (float2 *)(work + 6 * lay.vec);
+    double *r64 = (double *)(work + lay.off_r64);
+    double *part = (double *)(work + lay.off_part);
+    int nn = n, mi = p->maxiter, mo = p->max_outer > 0 ? p->max_outer : 1000;
+    int guess = p->use_initial_guess ? 1 : 0;
+    double at = p->abstol, rt = p->reltol, dl = p->inner_reltol > 0 && p->inner_reltol < 1 ? p->inner_reltol : 0.1;
+    const int32_t *rp = A->d_rowptr, *ci = A->d_cols;
+    const int4 *mt = (const int4 *)A->d_duo_meta;
+    const uint32_t *of = A->d_duo_off;
+    const float2 *vl = (const float2 *)A->d_duo_sval;
+    const double *v64 = A->d_vals64, *bb = bvec, *scl = A->d_duo_sc;
+    double *xx = xvec;
+    long long spin = ctx->wait_limit;
+    void *args[] = {&nn, &rp, &ci, &v64, &mt, &of, &vl, &bb, &xx, &scl, &xc, &zp0, &zp1, &r64, &part, &dst,
+                    &at, &rt, &dl, &mi, &mo, &guess, &spin, &J};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
+    cudaEventRecord(e0, ctx->stream);
+    cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, smem, ctx->stream);
+    GRMP_LAUNCHED(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    SolveState hs;
+    std::memset(&hs, 0, sizeof(hs));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "scaled duo PCG launch");
+    out->status = hs.status;
+    out->iterations = hs.iters;
+    out->outer_iterations = hs.outer;
+    out->final_relres = hs.relres;
+    out->spmv_config = cfg;
+    out->grid_blocks = grid;
+    out->solve_ms = ms;
+    if (hs.status == GRMP_ERR_NOT_CONVERGED)
+        return grmp_fail(ctx, GRMP_ERR_NOT_CONVERGED, "PCG: %d iterations, relative residual %.3e", hs.iters, hs.relres);
+    if (hs.status == GRMP_ERR_TIMEOUT) return grmp_fail(ctx, GRMP_ERR_TIMEOUT, "PCG: a grid barrier wait timed out");
+    if (hs.status == GRMP_ERR_NAN) return grmp_fail(ctx, GRMP_ERR_NAN, "PCG: breakdown (non-positive or non-finite p.Ap)");
+    return hs.status;
+}
+
 int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_solve_params *p, grmp_solve_stats *st,
                  char *work, SolveState *dst, WorkLayout lay) {
     switch (cfg) {
+        case 64208: return launch_pcg_duo_keep<2, 8, true>(A, b, x, p, st, work, dst, lay);
+        case 64404: return launch_pcg_duo_keep<4, 4, true>(A, b, x, p, st, work, dst, lay);
+        case 65208: return launch_pcg_duo_keep<2, 8, false>(A, b, x, p, st, work, dst, lay);
+        case 65404: return launch_pcg_duo_keep<4, 4, false>(A, b, x, p, st, work, dst, lay);
+        case 70204: return launch_pcg<2, 4, true, true>(A, b, x, p, st, work, dst, lay);
+        case 70404: return launch_pcg<4, 4, true, true>(A, b, x, p, st, work, dst, lay);
+        case 70802: return launch_pcg<8, 2, true, true>(A, b, x, p, st, work, dst, lay);
+        case 80204: return launch_pcg_duo<2, 4, true>(A, b, x, p, st, work, dst, lay);
+        case 80404: return launch_pcg_duo<4, 4, true>(A, b, x, p, st, work, dst, lay);
         case 60404: return launch_pcg_duo<4, 4>(A, b, x, p, st, work, dst, lay);
         case 60208: return launch_pcg_duo<2, 8>(A, b, x, p, st, work, dst, lay);
         case 60802: return launch_pcg_duo<8, 2>(A, b, x, p, st, work, dst, lay);
@@ -1578,17 +2170,23 @@ int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_para
     double *xs = nullptr;
     if (grmp_alloc(ctx, (void **)&xs, (size_t)A->nrows * 8)) return heuristic_config(A, mixed);
     grmp_solve_params q = *p;
-    q.maxiter = 24;
+    q.maxiter = 48;
     q.use_initial_guess = 0;
     q.reltol = 0.0;
     q.abstol = 0.0;
     q.grid_blocks = 0;
+    // per configuration: one untimed launch (first launch of the
+    // instantiation), then the faster of two timed ones
     auto trial = [&](int cfg) {
         grmp_solve_stats s{};
-        dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);   // warm-up: first launch of this instantiation
-        s = grmp_solve_stats{};
         dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);
-        return s.iterations > 0 ? s.solve_ms / s.iterations : 1e30;
+        double best = 1e30;
+        for (int rep = 0; rep < 2; rep++) {
+            s = grmp_solve_stats{};
+            dispatch_pcg(cfg, A, b->d, xs, &q, &s, work, dst, lay);
+            if (s.iterations > 0) best = std::min(best, (double)s.solve_ms / s.iterations);
+        }
+        return best;
     };
     int best = heuristic_config(A, mixed);
     double bt = 1e30;
@@ -1602,6 +2200,7 @@ int autotune_config(grmp_matrix A, const grmp_vector_s *b, const grmp_solve_para
         }
     }
     for (int g : {ctx->num_sms, 2 * ctx->num_sms}) {
+        if (cluster_config(best)) break;   // one cluster: no grid size to choose
         q.grid_blocks = g;
         const double per = trial(best);
         if (per < 0.97 * bt) {   // keep the default unless a smaller grid is clearly faster
@@ -1728,6 +2327,7 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     // reassembled since the last solve
     A->pack_fresh = false;
     A->duo_fresh = false;
+    A->duo_sfresh = false;
     int cfg = p->spmv_config;
     grmp_solve_params q = *p;
     if (cfg == 0) {   // autotuned once per matrix and solver mode (configuration and grid)
@@ -1868,12 +2468,11 @@ int noalloc_scratch(grmp_context ctx, char **out) {
     return GRMP_OK;
 }
 
-template <int TPR, int U, bool PIPE>
+template <int TPR, int U, bool PIPE, bool CL = false>
 cudaError_t launch_pcg64_static(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
                                 int grid_blocks, char *work, int *grid_out) {
     grmp_context ctx = A->space->mesh->ctx;
-    auto kern = k_pcg64<TPR, U, PIPE>;
-    int grid = coop_grid(ctx, kern, A->nrows, grid_blocks);
+    auto kern = k_pcg64<TPR, U, PIPE, CL>;
     double *dinv = (double *)work, *r = (double *)(work + kNaVec), *z = (double *)(work + 2 * kNaVec);
     double *pp = (double *)(work + 3 * kNaVec), *q = (double *)(work + 4 * kNaVec);
     double *part = (double *)(work + 5 * kNaVec);
@@ -1885,8 +2484,7 @@ cudaError_t launch_pcg64_static(grmp_matrix A, const double *bvec, double *xvec,
     double *xx = xvec;
     long long spin = ctx->wait_limit;
     void *args[] = {&nn, &rp, &ci, &vv, &bb, &xx, &dinv, &r, &z, &pp, &q, &part, &dst, &at, &rt, &mi, &guess, &spin};
-    *grid_out = grid;
-    cudaError_t e = cudaLaunchCooperativeKernel((void *)kern, grid, PTPB, args, 0, ctx->stream);
+    cudaError_t e = launch_persistent<CL>(ctx, kern, A->nrows, grid_blocks, args, grid_out);
     GRMP_LAUNCHED(ctx);
     return e;
 }
@@ -1951,6 +2549,9 @@ extern "C" int grmp_solve_fp64_noalloc(grmp_matrix A, grmp_vector b, grmp_vector
         case 10804: e = launch_pcg64_static<8, 4, true>(A, b->d, x->d, p, gb, work, &grid); break;
         case 10402: e = launch_pcg64_static<4, 2, true>(A, b->d, x->d, p, gb, work, &grid); break;
         case 10802: e = launch_pcg64_static<8, 2, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 70204: e = launch_pcg64_static<2, 4, true, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 70404: e = launch_pcg64_static<4, 4, true, true>(A, b->d, x->d, p, gb, work, &grid); break;
+        case 70802: e = launch_pcg64_static<8, 2, true, true>(A, b->d, x->d, p, gb, work, &grid); break;
         default: return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "spmv_config: unknown configuration %d", cfg);
     }
     SolveState hs;
@@ -1980,9 +2581,13 @@ void grmp_duo_free(grmp_matrix A) {
     grmp_free(ctx, A->d_duo_off, nd * 4);
     grmp_free(ctx, A->d_duo_src, nd * 4);
     grmp_free(ctx, A->d_duo_val, nd * 8);
-    A->d_duo_meta = A->d_duo_val = nullptr;
+    grmp_free(ctx, A->d_duo_sval, nd * 8);
+    grmp_free(ctx, A->d_duo_sc, (size_t)A->nrows * 8);
+    A->d_duo_meta = A->d_duo_val = A->d_duo_sval = nullptr;
+    A->d_duo_sc = nullptr;
     A->d_duo_off = nullptr;
     A->d_duo_src = nullptr;
     A->duo_state = 0;
     A->duo_fresh = false;
+    A->duo_sfresh = false;
 }

@@ -69,7 +69,8 @@ int grmp_synchronize(grmp_context ctx);
 int grmp_context_memory(grmp_context ctx, size_t *bytes_in_use);
 /* Number of kernels this context has launched so far (instrumentation). */
 int grmp_context_launches(grmp_context ctx, uint64_t *launches);
-/* Polls (about 64 ns each) after which a bounded device-side wait of this
+/* Polls (a grid-barrier poll is one L2 round trip, under a microsecond;
+ * an mbarrier poll a few tens of ns) after which a bounded device-side wait of this
  * context's iterative solves gives up and the solve returns GRMP_ERR_TIMEOUT
  * (grid barriers of the persistent kernels, mbarrier waits of the staged
  * SpMV); 0 restores the default of 2^24.  No reference counterpart (the
@@ -431,7 +432,12 @@ typedef struct {
                                the FP32 values with two-run 16-bit columns (two entries per
                                8-byte value load and 4-byte column load; rows whose columns
                                fall in two windows of 65536): 60404, 60208, 60802, 60408
-                               (100*lanes + entry pairs in flight); 0 = autotuned
+                               (100*lanes + entry pairs in flight); the whole solve in one
+                               thread-block cluster of 8 or 16 blocks of 1024 threads
+                               (hardware cluster barriers, reductions through distributed
+                               shared memory; for systems that sit in L2): 70204, 70404,
+                               70802 (pipelined row loop, both modes), 80204, 80404 (MIXED
+                               only, two-run 16-bit columns); 0 = autotuned
                                per matrix and mode (timed trial solves); -1 = chosen from the
                                mean row length
                                (no timing, so the choice does not depend on concurrent GPU work) */

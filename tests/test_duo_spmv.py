@@ -18,7 +18,8 @@ def _solve_oracle(G, O, prob):
 
 
 @pytest.mark.parametrize("which,cfg", [("p2_128", 60404), ("p2_128", 60208), ("p1_96", 60802),
-                                       ("p1_96", 60404)])
+                                       ("p1_96", 60404), ("p2_128", 64208), ("p1_96", 64404),
+                                       ("p2_128", 65404), ("p1_96", 65208)])
 def test_duo_2d_matches_oracle(G, O, ctx, which, cfg):
     from grmp_gb300 import problems as P
     prob = P.poisson2d(128) if which == "p2_128" else P.poisson2d(96, order=1)

@@ -7,6 +7,7 @@ scratch is then reused, not fresh).  Results are compared with the ordinary
 grmp_solve entry point on the same system, on two calls in a row.
 """
 import ctypes
+import gc
 
 import numpy as np
 import pytest
@@ -41,6 +42,7 @@ def test_noalloc_matches_solve_on_two_calls(G, ctx, n):
     solver = G.GB300PCG(mode="fp64", reltol=1e-11, abstol=0.0)
     ref_stats = solver.solve(sysd.A, sysd.b, sysd.x)
     xref = sysd.x.entries
+    gc.collect()   # handles of earlier tests freed now, not during the calls below
     mem0 = ctx.memory_in_use()
     for call in range(2):
         sysd.x.fill(123.0)   # overwritten: use_initial_guess = 0
@@ -53,6 +55,7 @@ def test_noalloc_matches_solve_on_two_calls(G, ctx, n):
         x = sysd.x.entries
         err = np.linalg.norm(x - xref) / np.linalg.norm(xref)
         assert err <= REL_TOL, (call, err)
+    gc.collect()
     assert ctx.memory_in_use() == mem0   # nothing was allocated through the context
 
 
