@@ -287,7 +287,7 @@ def duo_family(cfg: int) -> bool:
 
 
 def pcg_kernel(cfg: int) -> str:
-    if 64000 <= cfg < 66000:
+    if 64000 <= cfg < 67000:
         return "k_pcg_mixed_duo_keep"
     if duo_family(cfg):
         return "k_pcg_mixed_duo"

@@ -1030,8 +1030,8 @@ __device__ __forceinline__ float duo_zp_keep(int n, const int4 *__restrict__ met
     return dacc;
 }
 
-template <int TPR, int U, bool ALL>
-__global__ void __launch_bounds__(PTPB, U >= 4 ? 3 : 4) k_pcg_mixed_duo_keep(
+template <int TPR, int U, bool ALL, int MINB = (U >= 4 ? 3 : 4)>
+__global__ void __launch_bounds__(PTPB, MINB) k_pcg_mixed_duo_keep(
     int n, const int32_t *rowptr, const int32_t *cols, const double *vals64, const int4 *meta, const uint32_t *off,
     const float2 *sval, const double *b, double *x, const double *sc, float *xc, float2 *zp0, float2 *zp1,
     double *r64, double *partial, SolveState *st, double abstol, double reltol, double delta, int maxit,
@@ -1490,11 +1490,12 @@ void launch_spmv(int tpr, int grid, cudaStream_t s, int n, const int32_t *rp, co
 // faster; the row-length heuristic uses them for the smallest mixed solves.)
 constexpr int kConfigs[] = {208,   404,   408,   804,   1602,  10204, 10404, 10408, 10804, 10402,
                             10802, 20204, 20408, 20804, 30408, 30804, 60404, 60208, 60802, 60408, 64208, 64404,
-                            65208, 65404};
+                            65208, 65404, 66404};
 
 inline bool staged_config(int cfg) { return cfg >= 20000 && cfg < 60000; }
 inline bool duo_config(int cfg) { return (cfg >= 60000 && cfg < 70000) || cfg >= 80000; }
 inline bool cluster_config(int cfg) { return cfg >= 70000; }
+inline bool scaled_config(int cfg) { return cfg >= 64000 && cfg < 67000; }
 
 // Window layout of the staged SpMV, built once per matrix pattern from the
 // row pointers (greedy: whole rows while header + entries fit one record).
@@ -1611,7 +1612,9 @@ int duo_build_dev(grmp_matrix A) {
     return GRMP_OK;
 }
 
-int ensure_duo(grmp_matrix A) {
+// The duo layout (once per pattern); with `values`, also the unscaled FP32
+// values of the current solve.
+int ensure_duo(grmp_matrix A, bool values = true) {
     grmp_context ctx = A->space->mesh->ctx;
     if (A->duo_state == 0) {
         int rc = duo_build_dev(A);
@@ -1620,7 +1623,7 @@ int ensure_duo(grmp_matrix A) {
     if (A->duo_state < 0)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "duo layout: a column run spans %d columns (more than 65535)",
                          A->duo_span);
-    if (!A->duo_fresh) {
+    if (values && !A->duo_fresh) {
         k_duo_fill<<<(unsigned)((A->duo_nduo + 255) / 256), 256, 0, ctx->stream>>>(A->duo_nduo, A->d_duo_src,
                                                                                    A->d_vals32,
                                                                                    (float2 *)A->d_duo_val);
@@ -1649,16 +1652,18 @@ __global__ void k_duo_scales(int n, const int32_t *rowptr, const int32_t *cols, 
     sc[r] = 1.0 / sqrt(d);
 }
 
-// one thread per row: the row's duos (their source positions are the row's
-// CSR entries in order)
+// 16 lanes per row over the row's duos (contiguous in the duo arrays and,
+// through their source positions, in the CSR arrays): coalesced loads and
+// stores
 __global__ void k_duo_fill_scaled(int n, const int4 *meta, const int32_t *src, const int32_t *cols,
                                   const double *vals, const double *sc, float2 *sval) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 4);
+    const int l = threadIdx.x & 15;
     if (r >= n) return;
     const int4 m = meta[r];
     const double sr = sc[r];
-    const int d0 = m.x, d1 = m.x + (m.w >> 16);
-    for (int d = d0; d < d1; d++) {
+    const int d1 = m.x + (m.w >> 16);
+    for (int d = m.x + l; d < d1; d += 16) {
         const int s = src[d];
         const int k = s >= 0 ? s : -1 - s;
         const float v0 = (float)(vals[k] * sr * sc[cols[k]]);
@@ -1669,7 +1674,7 @@ __global__ void k_duo_fill_scaled(int n, const int4 *meta, const int32_t *src, c
 
 int ensure_duo_scaled(grmp_matrix A) {
     grmp_context ctx = A->space->mesh->ctx;
-    int rc = ensure_duo(A);
+    int rc = ensure_duo(A, false);
     if (rc) return rc;
     if (!A->d_duo_sval) {
         rc = grmp_alloc(ctx, &A->d_duo_sval, (size_t)A->duo_nduo * 8);
@@ -1688,8 +1693,9 @@ int ensure_duo_scaled(grmp_matrix A) {
         cudaMemsetAsync(bad, 0, 4, ctx->stream);
         k_duo_scales<<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, A->d_duo_sc, bad);
         GRMP_LAUNCHED(ctx);
-        k_duo_fill_scaled<<<nblk(n), 256, 0, ctx->stream>>>(n, (const int4 *)A->d_duo_meta, A->d_duo_src, A->d_cols,
-                                                             A->d_vals64, A->d_duo_sc, (float2 *)A->d_duo_sval);
+        k_duo_fill_scaled<<<nblk((long long)n * 16), 256, 0, ctx->stream>>>(
+            n, (const int4 *)A->d_duo_meta, A->d_duo_src, A->d_cols, A->d_vals64, A->d_duo_sc,
+            (float2 *)A->d_duo_sval);
         GRMP_LAUNCHED(ctx);
         int hbad = 0;
         cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
@@ -2028,11 +2034,13 @@ int launch_pcg_duo(grmp_matrix A, const double *bvec, double *xvec, const grmp_s
 // block keeps 12 bytes per row of its rows: about 12 n / (number of SMs)
 // bytes per SM whatever the grid, so systems beyond about 2.8 M rows do not
 // fit (GRMP_ERR_UNSUPPORTED).
-template <int TPR, int U, bool ALL>
+template <int TPR, int U, bool ALL, int MINB = (U >= 4 ? 3 : 4)>
 int launch_pcg_duo_keep(grmp_matrix A, const double *bvec, double *xvec, const grmp_solve_params *p,
                         grmp_solve_stats *out, char *work, SolveState *dst, WorkLayout lay) {
     grmp_context ctx = A->space->mesh->ctx;
-    const int cfg = (ALL ? 64000 : 65000) + 100 * TPR + U;
+    // 64xxx: r, p, A p kept, 3 blocks/SM; 65xxx / 66xxx: A p kept, at least
+    // 3 / 4 blocks per SM (registers capped to match: 80 / 64)
+    const int cfg = (ALL ? 64000 : 62000 + 1000 * MINB) + 100 * TPR + U;
     constexpr int KW = ALL ? 3 : 1;   // words kept per row
     if (p->mode != GRMP_SOLVE_MIXED)
         return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "spmv_config %d: duo configurations are for mixed solves", cfg);
@@ -2040,7 +2048,7 @@ int launch_pcg_duo_keep(grmp_matrix A, const double *bvec, double *xvec, const g
     if (rc) return rc;
     const int n = A->nrows;
     constexpr int G = PTPB / TPR;
-    auto kern = k_pcg_mixed_duo_keep<TPR, U, ALL>;
+    auto kern = k_pcg_mixed_duo_keep<TPR, U, ALL, MINB>;
     int dev_max = 0;
     cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     int per_sm = 0;
@@ -2124,6 +2132,7 @@ int dispatch_pcg(int cfg, grmp_matrix A, const double *b, double *x, const grmp_
         case 64404: return launch_pcg_duo_keep<4, 4, true>(A, b, x, p, st, work, dst, lay);
         case 65208: return launch_pcg_duo_keep<2, 8, false>(A, b, x, p, st, work, dst, lay);
         case 65404: return launch_pcg_duo_keep<4, 4, false>(A, b, x, p, st, work, dst, lay);
+        case 66404: return launch_pcg_duo_keep<4, 4, false, 4>(A, b, x, p, st, work, dst, lay);
         case 70204: return launch_pcg<2, 4, true, true>(A, b, x, p, st, work, dst, lay);
         case 70404: return launch_pcg<4, 4, true, true>(A, b, x, p, st, work, dst, lay);
         case 70802: return launch_pcg<8, 2, true, true>(A, b, x, p, st, work, dst, lay);
@@ -2305,22 +2314,27 @@ int grmp_solve_impl(grmp_matrix A, grmp_vector b, grmp_vector x, const grmp_solv
     SolveState *dst = (SolveState *)(work + off_state);
     WorkLayout lay{vec, off_r64, off_part};
     cudaMemsetAsync(dst, 0, sizeof(SolveState), ctx->stream);
-    // Jacobi preconditioner
-    int *bad = nullptr;
-    int rc = grmp_alloc(ctx, (void **)&bad, 4);
-    if (rc) return rc;
-    cudaMemsetAsync(bad, 0, 4, ctx->stream);
-    if (mixed)
-        k_dinv<float><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals32, (float *)work, bad);
-    else
-        k_dinv<double><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, (double *)work, bad);
-    GRMP_LAUNCHED(ctx);
-    int hbad = 0;
-    cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    grmp_free(ctx, bad, 4);
-    if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
-    if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
+    // Jacobi preconditioner (not for the Jacobi-scaled configurations, which
+    // form and check their own row scales)
+    const int known = p->spmv_config != 0 ? p->spmv_config : (mixed ? A->tuned_cfg32 : A->tuned_cfg);
+    if (!(mixed && scaled_config(known))) {
+        int *bad = nullptr;
+        int rc = grmp_alloc(ctx, (void **)&bad, 4);
+        if (rc) return rc;
+        cudaMemsetAsync(bad, 0, 4, ctx->stream);
+        if (mixed)
+            k_dinv<float><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals32, (float *)work, bad);
+        else
+            k_dinv<double><<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, (double *)work,
+                                                             bad);
+        GRMP_LAUNCHED(ctx);
+        int hbad = 0;
+        cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        grmp_free(ctx, bad, 4);
+        if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "jacobi diagonal");
+        if (hbad) return grmp_fail(ctx, GRMP_ERR_INVALID_ARG, "solve: non-positive or non-finite diagonal entry");
+    }
     if (bicg) return launch_bicgstab(A, b->d, x->d, p, st, work, dst, lay);
     // the FP32 copies (packed pairs and staged windows, duo values) are
     // refreshed by the first launch that reads them: the values may have been

@@ -432,7 +432,13 @@ typedef struct {
                                the FP32 values with two-run 16-bit columns (two entries per
                                8-byte value load and 4-byte column load; rows whose columns
                                fall in two windows of 65536): 60404, 60208, 60802, 60408
-                               (100*lanes + entry pairs in flight); the whole solve in one
+                               (100*lanes + entry pairs in flight); MIXED only, the same
+                               columns with the Jacobi-scaled values a_ij/sqrt(a_ii a_jj)
+                               (unpreconditioned inner CG, no residual or inverse-diagonal
+                               stream) and each row's A p kept in shared memory between the
+                               SpMV and the vector phase: 64208, 64404 (r and p kept too),
+                               65208, 65404, 66404 (A p only; 66xxx at 4 blocks per SM);
+                               up to about 2.8 M rows; the whole solve in one
                                thread-block cluster of 8 or 16 blocks of 1024 threads
                                (hardware cluster barriers, reductions through distributed
                                shared memory; for systems that sit in L2): 70204, 70404,

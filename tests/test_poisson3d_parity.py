@@ -9,8 +9,8 @@ double-double residuals, itself pinned against SuperLU in
 test_oracle_reference.py).  Each GPU solve -- plain FP64 Jacobi-PCG and the
 mixed FP32-inner / FP64-outer solver, in the row-loop (10408, 408),
 staged-window (20204, 20408) and two-run 16-bit column (604xx, 60208,
-60802; 64208 / 64404 / 65208 / 65404 on the Jacobi-scaled copy with the
-row state in shared memory) SpMV forms the autotuner picks among on the 64^3 matrix -- must be
+60802; 64208 / 64404 / 65208 / 65404 / 66404 on the Jacobi-scaled copy
+with the row state in shared memory) SpMV forms the autotuner picks among on the 64^3 matrix -- must be
 within 1e-10 relative 2-norm error.  The FP64 matrix is
 also checked against the oracle's per nonzero (1e-12 relative, floored at
 1e-3 of the row maximum).
@@ -24,7 +24,8 @@ pytestmark = pytest.mark.gpu
 
 CONFIGS = [("fp64", 408), ("fp64", 208), ("mixed", 10408), ("mixed", 10404), ("mixed", 20204), ("mixed", 20408),
            ("mixed", 60404), ("mixed", 60208), ("mixed", 60802), ("mixed", 60408), ("mixed", 64208),
-           ("mixed", 64404), ("mixed", 65208), ("mixed", 65404)]
+           ("mixed", 64404), ("mixed", 65208), ("mixed", 65404),
+           ("mixed", 66404)]
 
 
 def _reference(G, O, n):
