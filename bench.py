@@ -265,19 +265,16 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ GPU arm
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one
-# k_pcg_mixed launch on the 48^3 case divided by pcg_bytes() of the same
-# launch: 180.78 GB / 185.73 GB (summary under profiles/).
-TRAFFIC_PER_ALGORITHMIC_BYTE = (163.612 + 17.166) / 185.732
-# the same for k_pcg_mixed_duo (two-run 16-bit columns, configuration 60208):
-# 153.315 GB / 163.833 GB on the 48^3 case (summary under profiles/)
-TRAFFIC_PER_ALGORITHMIC_BYTE_DUO = (137.023 + 16.292) / 163.833
-# the same for k_pcg_mixed_duo_keep (Jacobi-scaled two-run columns, A p kept
-# in shared memory, configuration 65208): 138.239 GB / 163.752 GB on the
-# 48^3 case (summary under profiles/)
-TRAFFIC_PER_ALGORITHMIC_BYTE_KEEP = (129.587 + 8.652) / 163.752
-# per persistent kernel
-TRAFFIC_RATIO = {"k_pcg_mixed": TRAFFIC_PER_ALGORITHMIC_BYTE, "k_pcg_mixed_duo": TRAFFIC_PER_ALGORITHMIC_BYTE_DUO,
-                 "k_pcg_mixed_duo_keep": TRAFFIC_PER_ALGORITHMIC_BYTE_KEEP}
+# persistent-solver launch on the 48^3 case divided by pcg_bytes() of the
+# same launch (summaries under profiles/):
+#   k_pcg_mixed (packed pairs, 10408): 180.78 GB / 185.73 GB
+#   k_pcg_mixed_duo (two-run 16-bit columns, 60208; 768 iterations, 11
+#     refinements): 153.315 GB / 185.260 GB
+#   k_pcg_mixed_duo_keep (Jacobi-scaled two-run columns, A p kept on chip,
+#     65208; 766 iterations, 12 refinements): 138.241 GB / 185.124 GB
+TRAFFIC_RATIO = {"k_pcg_mixed": (163.612 + 17.166) / 185.732,
+                 "k_pcg_mixed_duo": (137.023 + 16.292) / 185.260,
+                 "k_pcg_mixed_duo_keep": (129.587 + 8.652) / 185.124}
 
 
 def duo_family(cfg: int) -> bool:
@@ -296,19 +293,16 @@ def pcg_kernel(cfg: int) -> str:
     return "k_pcg_mixed"
 
 
-def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool, nduo: int = 0) -> float:
-    """Algorithmic DRAM bytes of one persistent PCG launch: per inner
-    iteration the matrix once (values + column indices: 8 bytes per entry as
-    packed pairs; 12 bytes per pair of entries plus a 16-byte row record in
-    the two-run 16-bit column form) and the vector traffic of the update
-    phase of Jacobi-PCG (seven 8-byte streams per row, whatever a kernel keeps
-    on chip); per FP64 refinement one FP64 residual."""
+def pcg_bytes(stats: dict, n: int, nnz: int, mixed: bool) -> float:
+    """Algorithmic DRAM bytes of one persistent PCG launch, by the CSR
+    definition (int32 column indices) whatever the storage format: per inner
+    FP32 iteration the matrix once (4-byte value + 4-byte column per entry)
+    and the vector traffic of Jacobi-PCG's update phase (seven 8-byte streams
+    per row); per FP64 refinement one FP64 residual.  A format or kernel that
+    moves fewer bytes shows as DRAM traffic below these bytes."""
     it, outer = stats["iterations"], stats["outer_iterations"]
     if mixed:
-        if duo_family(stats.get("spmv_config", 0)):
-            per_it = 12.0 * nduo + 16.0 * n + 56.0 * n
-        else:
-            per_it = 8.0 * nnz + 56.0 * n
+        per_it = 8.0 * nnz + 56.0 * n
         per_outer = 12.0 * nnz + 64.0 * n
         return it * per_it + (outer + 1) * per_outer
     return it * (12.0 * nnz + 108.0 * n) + 2 * (12.0 * nnz + 36.0 * n)
@@ -392,8 +386,6 @@ def run_ours(args):
     b = G.FEVector(ctx, FES)
     x = G.FEVector(ctx, FES)
     nnz = A.nnz
-    rp_host, _ = A.pattern()
-    nduo = int(np.sum((np.diff(rp_host) + 1) // 2))   # entry pairs of the two-run 16-bit column form
 
     direct = args.solver == "direct"
 
@@ -441,7 +433,7 @@ def run_ours(args):
             # iteration counts let a capture's DRAM bytes be set against the algorithmic bytes
             print(json.dumps({"profile_step": k, "ndofs": ndofs, "nnz": nnz, "iterations": st["iterations"],
                               "outer": st["outer_iterations"], "spmv_config": st["spmv_config"],
-                              "algorithmic_bytes": pcg_bytes(st, ndofs, nnz, True, nduo)}), flush=True)
+                              "algorithmic_bytes": pcg_bytes(st, ndofs, nnz, True)}), flush=True)
         torch.cuda.synchronize()
         ctx.close()
         dist.close()
@@ -493,7 +485,7 @@ def run_ours(args):
     plain_value = world_dofs / plain["total_s"]
     # roofline of the dominant kernel (persistent mixed PCG)
     st_last = mixed["stats"][-1]
-    kb = pcg_bytes(st_last, ndofs, nnz, True, nduo)
+    kb = pcg_bytes(st_last, ndofs, nnz, True)
     kname = pcg_kernel(st_last["spmv_config"])
     kms = statistics.mean([s["solve_ms"] for s in mixed["stats"]])
     achieved = kb / (kms / 1e3) / 1e9
