@@ -271,10 +271,11 @@ def run_reference(args):
 #   k_pcg_mixed_duo (two-run 16-bit columns, 60208; 768 iterations, 11
 #     refinements): 153.315 GB / 185.260 GB
 #   k_pcg_mixed_duo_keep (Jacobi-scaled two-run columns, A p kept on chip,
-#     65208; 766 iterations, 12 refinements): 138.241 GB / 185.124 GB
+#     66404, the autotuner's choice at 64^3; 763 iterations, 13
+#     refinements): 141.091 GB / 184.752 GB (65208: 138.241 / 185.124)
 TRAFFIC_RATIO = {"k_pcg_mixed": (163.612 + 17.166) / 185.732,
                  "k_pcg_mixed_duo": (137.023 + 16.292) / 185.260,
-                 "k_pcg_mixed_duo_keep": (129.587 + 8.652) / 185.124}
+                 "k_pcg_mixed_duo_keep": (131.944 + 9.147) / 184.752}
 
 
 def duo_family(cfg: int) -> bool:
