@@ -104,8 +104,9 @@ struct grmp_matrix_s {
     uint32_t *d_duo_off = nullptr;  // [nduo] two 16-bit column offsets
     int32_t *d_duo_src = nullptr;   // [nduo] CSR position of the first entry (-1 - pos: second is padding)
     void *d_duo_val = nullptr;      // [nduo] float2 values
-    // Jacobi-scaled duo values a_ij / sqrt(a_ii a_jj) (rounded once from FP64)
-    // and the FP64 scale 1 / sqrt(a_ii) of each row, for the scaled solver
+    // Jacobi-scaled duo values a32_ij / sqrt(a32_ii a32_jj) of the FP32-assembled
+    // values (formed in FP64, rounded once) and the FP64 scale
+    // 1 / sqrt(a32_ii) of each row, for the scaled solver
     void *d_duo_sval = nullptr;     // [nduo] float2
     double *d_duo_sc = nullptr;     // [nrows]
     // the FP32 copies (packed pairs / staged windows, duo values, scaled duo

@@ -944,18 +944,20 @@ __global__ void __launch_bounds__(CL ? kClT : PTPB, CL ? 1 : (U >= 4 ? 3 : 4)) k
 }
 
 // ------------------------------------------------ scaled duo mixed PCG (keep)
-// The mixed solver on the Jacobi-scaled system  S A S y = S b,  x = S y,
-// S = diag(1 / sqrt(a_ii)): unpreconditioned CG on S A S is Jacobi-PCG on A,
+// The mixed solver's inner iteration on the Jacobi-scaled FP32 system
+// S A32 S y = S r,  S = diag(1 / sqrt(a32_ii)) (A32: the FP32-assembled
+// matrix): unpreconditioned CG on S A32 S is Jacobi-PCG on A32,
 // with z = r, so the (z, p) pair is (r, p) and neither a separate residual
 // array nor the inverse diagonal is streamed.  The row loop gives every row
 // group a fixed list of rows (first row + j * stride, j < J); the SpMV phase
-// keeps each row's r, p and (S A S p) in shared memory ([3][J][groups of the
-// block]) and the vector phase, run by the same group after the p.q
-// reduction, updates the row from there.  Per row and iteration the vector
-// streams left are the own pair (read), the FP32 correction (read, write) and
-// the next pair (write) -- against nine 4-byte words of the unscaled solver.
-// The FP64 refinement is unchanged: x += S xc, r64 = b - A x with the FP64
-// matrix, the scaled FP32 residual S r64.
+// keeps each row's S A32 S p (ALL: also r and p) in shared memory, in slots
+// [J][groups of the block], and the vector phase, run over all threads of
+// the block after the p.q reduction, updates the rows from there (p
+// recomputed from the pair with the SpMV's own fmaf).  Per row and iteration
+// the vector streams left are the own pair (read), the FP32 correction (read,
+// write) and the next pair (write) -- against nine 4-byte words of the
+// unscaled solver.  The FP64 refinement is unchanged: x += S xc, r64 = b - A x
+// with the FP64 matrix, the scaled FP32 residual S r64.
 template <int TPR, int U, bool ALL>
 __device__ __forceinline__ float duo_zp_keep(int n, const int4 *__restrict__ meta, const uint32_t *__restrict__ off,
                                              const float2 *__restrict__ val, const float2 *cur, float beta, float *kr,
@@ -1633,17 +1635,18 @@ int ensure_duo(grmp_matrix A, bool values = true) {
     return GRMP_OK;
 }
 
-// The Jacobi-scaled duo values of the current FP64 values (scaled solver):
-// the FP64 row scales 1 / sqrt(a_ii), then each duo's two values
-// a_ij * s_i * s_j rounded once to FP32.  *bad is set for a non-positive or
-// non-finite diagonal entry.
-__global__ void k_duo_scales(int n, const int32_t *rowptr, const int32_t *cols, const double *vals, double *sc,
+// The Jacobi-scaled duo values of the FP32-assembled values (scaled
+// solver: the inner iteration is Jacobi-PCG on the FP32 matrix, run as CG on
+// S A32 S): the row scales s_i = 1 / sqrt(a32_ii) in FP64, then each duo's
+// two values a32_ij * s_i * s_j formed in FP64 and rounded once to FP32.
+// *bad is set for a non-positive or non-finite diagonal entry.
+__global__ void k_duo_scales(int n, const int32_t *rowptr, const int32_t *cols, const float *vals, double *sc,
                              int *bad) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     double d = 0.0;
     for (int k = rowptr[r]; k < rowptr[r + 1]; k++)
-        if (cols[k] == r) d = vals[k];
+        if (cols[k] == r) d = (double)vals[k];
     if (!(d > 0.0) || !isfinite(d)) {
         atomicExch(bad, 1);
         sc[r] = 0.0;
@@ -1656,7 +1659,7 @@ __global__ void k_duo_scales(int n, const int32_t *rowptr, const int32_t *cols, 
 // through their source positions, in the CSR arrays): coalesced loads and
 // stores
 __global__ void k_duo_fill_scaled(int n, const int4 *meta, const int32_t *src, const int32_t *cols,
-                                  const double *vals, const double *sc, float2 *sval) {
+                                  const float *vals, const double *sc, float2 *sval) {
     const int r = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 4);
     const int l = threadIdx.x & 15;
     if (r >= n) return;
@@ -1666,8 +1669,8 @@ __global__ void k_duo_fill_scaled(int n, const int4 *meta, const int32_t *src, c
     for (int d = m.x + l; d < d1; d += 16) {
         const int s = src[d];
         const int k = s >= 0 ? s : -1 - s;
-        const float v0 = (float)(vals[k] * sr * sc[cols[k]]);
-        const float v1 = s >= 0 ? (float)(vals[k + 1] * sr * sc[cols[k + 1]]) : 0.f;
+        const float v0 = (float)((double)vals[k] * sr * sc[cols[k]]);
+        const float v1 = s >= 0 ? (float)((double)vals[k + 1] * sr * sc[cols[k + 1]]) : 0.f;
         sval[d] = make_float2(v0, v1);
     }
 }
@@ -1691,10 +1694,10 @@ int ensure_duo_scaled(grmp_matrix A) {
         rc = grmp_alloc(ctx, (void **)&bad, 4);
         if (rc) return rc;
         cudaMemsetAsync(bad, 0, 4, ctx->stream);
-        k_duo_scales<<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals64, A->d_duo_sc, bad);
+        k_duo_scales<<<nblk(n), 256, 0, ctx->stream>>>(n, A->d_rowptr, A->d_cols, A->d_vals32, A->d_duo_sc, bad);
         GRMP_LAUNCHED(ctx);
         k_duo_fill_scaled<<<nblk((long long)n * 16), 256, 0, ctx->stream>>>(
-            n, (const int4 *)A->d_duo_meta, A->d_duo_src, A->d_cols, A->d_vals64, A->d_duo_sc,
+            n, (const int4 *)A->d_duo_meta, A->d_duo_src, A->d_cols, A->d_vals32, A->d_duo_sc,
             (float2 *)A->d_duo_sval);
         GRMP_LAUNCHED(ctx);
         int hbad = 0;

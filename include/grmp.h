@@ -433,7 +433,7 @@ typedef struct {
                                8-byte value load and 4-byte column load; rows whose columns
                                fall in two windows of 65536): 60404, 60208, 60802, 60408
                                (100*lanes + entry pairs in flight); MIXED only, the same
-                               columns with the Jacobi-scaled values a_ij/sqrt(a_ii a_jj)
+                               columns with the Jacobi-scaled FP32 values a_ij/sqrt(a_ii a_jj)
                                (unpreconditioned inner CG, no residual or inverse-diagonal
                                stream) and each row's A p kept in shared memory between the
                                SpMV and the vector phase: 64208, 64404 (r and p kept too),
