@@ -299,17 +299,99 @@ __global__ void __launch_bounds__(128) k_assemble_rows2(int32_t nrows, const int
 // shared-memory accumulator is sized by it, not by tpb x the longest row).
 int block_nnz_max(grmp_matrix A, int tpb, int *out) {
     grmp_context ctx = A->space->mesh->ctx;
-    if (A->blk_tpb != tpb) {
+    const int k = tpb >= 128 ? 2 : (tpb >= 64 ? 1 : 0);
+    if (A->blk_nnz[k] < 0) {   // all three block sizes from one download of the row pointers
         std::vector<int32_t> rp((size_t)A->nrows + 1);
         cudaError_t e = cudaMemcpyAsync(rp.data(), A->d_rowptr, rp.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) return grmp_cuda_fail(ctx, e, "assembly: row pointer download");
-        int mx = 0;
-        for (int r0 = 0; r0 < A->nrows; r0 += tpb) mx = std::max(mx, rp[std::min(A->nrows, r0 + tpb)] - rp[r0]);
-        A->blk_tpb = tpb;
-        A->blk_nnz = mx;
+        for (int q = 0; q < 3; q++) {
+            const int b = 32 << q;
+            int mx = 0;
+            for (int r0 = 0; r0 < A->nrows; r0 += b) mx = std::max(mx, rp[std::min(A->nrows, r0 + b)] - rp[r0]);
+            A->blk_nnz[q] = mx;
+        }
     }
-    *out = A->blk_nnz;
+    *out = A->blk_nnz[k];
+    return GRMP_OK;
+}
+
+// Rows per block of a row-assembly kernel (128, 64 or 32: the kernels are
+// built for at most 128 threads) and its shared memory: the reference tensors
+// (tens_b bytes) and the block's values (per_nnz bytes each, the largest
+// block's count).  The first assembly of a matrix of at least kAsmTuneRows
+// rows times every candidate that fits once with CUDA events and keeps the
+// fastest in *cached; smaller matrices, and matrices whose *cached is
+// negative (served requests), take the largest block within 100 KB (two
+// blocks per SM).  The assembled values do not depend on the choice:
+// every row is summed by one thread in incidence order.  go(tpb, shm)
+// enqueues the kernel; on return it has run with the chosen shape.
+constexpr int kAsmTuneRows = 20000;
+
+template <typename L>
+int assemble_rows_tuned(grmp_matrix A, size_t tens_b, size_t per_nnz, int *cached, L go) {
+    grmp_context ctx = A->space->mesh->ctx;
+    auto shm_of = [&](int tpb, size_t *shm) {
+        int bnz = 0;
+        const int rc = block_nnz_max(A, tpb, &bnz);
+        *shm = tens_b + (size_t)bnz * per_nnz + 16;
+        return rc;
+    };
+    if (*cached > 0) {
+        size_t shm = 0;
+        int rc = shm_of(*cached, &shm);
+        if (rc) return rc;
+        go(*cached, shm);
+        return GRMP_OK;
+    }
+    if (*cached < 0 || A->nrows < kAsmTuneRows) {   // negative: the caller asked for the rule, not timing
+        int tpb = 128;
+        size_t shm = 0;
+        int rc = shm_of(tpb, &shm);
+        while (!rc && tpb > 32 && shm > 100 * 1024) {
+            tpb /= 2;
+            rc = shm_of(tpb, &shm);
+        }
+        if (rc) return rc;
+        if (shm > 220 * 1024) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
+        if (*cached == 0) *cached = tpb;
+        go(tpb, shm);
+        return GRMP_OK;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = 0;
+    float best_ms = 0.f;
+    for (int tpb : {128, 64, 32}) {
+        size_t shm = 0;
+        int rc = shm_of(tpb, &shm);
+        if (rc) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+        }
+        if (shm > 220 * 1024) continue;
+        cudaEventRecord(e0, ctx->stream);
+        go(tpb, shm);
+        cudaEventRecord(e1, ctx->stream);
+        float ms = 0.f;
+        if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+            (best == 0 || ms < best_ms)) {
+            best = tpb;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best == 0) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
+    *cached = best;
+    if (best != 32) {   // the values in place are the last candidate's (identical); keep the chosen launch last
+        size_t shm = 0;
+        int rc = shm_of(best, &shm);
+        if (rc) return rc;
+        go(best, shm);
+    }
     return GRMP_OK;
 }
 
@@ -361,36 +443,30 @@ int run_assembly_dual(grmp_matrix A, const FastTerms &ft, const std::vector<doub
         return rc;
     }
     const size_t tens_b = tens64.size() * 8 + ((tens32.size() + 1) & ~(size_t)1) * 4;
-    int tpb = 128, bnz = 0;
-    rc = block_nnz_max(A, tpb, &bnz);
-    while (!rc && tpb > 32 && tens_b + (size_t)bnz * 12 > 100 * 1024) {
-        tpb /= 2;
-        rc = block_nnz_max(A, tpb, &bnz);
-    }
+    const bool lap1 = single_laplace(ft);
+    auto go = [&](int tpb, size_t shm) {
+        int bnz = 0;
+        block_nnz_max(A, tpb, &bnz);   // counted by the caller already: no download here
+        auto launch = [&](auto kern, const auto *slot) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+            kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
+                                                                slot, A->d_rowptr, fac64, fac32, dt64, dt32, ft,
+                                                                A->d_vals64, A->d_vals32, bnz);
+            GRMP_LAUNCHED(ctx);
+        };
+        if (A->slot_bytes == 1) {
+            if (lap1) launch(k_assemble_rows2<DIM, NB, NC, uint8_t, true>, (const uint8_t *)A->d_slot);
+            else launch(k_assemble_rows2<DIM, NB, NC, uint8_t, false>, (const uint8_t *)A->d_slot);
+        } else {
+            if (lap1) launch(k_assemble_rows2<DIM, NB, NC, uint16_t, true>, (const uint16_t *)A->d_slot);
+            else launch(k_assemble_rows2<DIM, NB, NC, uint16_t, false>, (const uint16_t *)A->d_slot);
+        }
+    };
+    rc = assemble_rows_tuned(A, tens_b, 12, &A->asm_tpb[2], go);
     if (rc) {
         release();
         return rc;
     }
-    const size_t shm = tens_b + (size_t)bnz * 12 + 16;
-    if (shm > 220 * 1024) {
-        release();
-        return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
-    }
-    auto launch = [&](auto kern, const auto *slot) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, slot,
-                                                            A->d_rowptr, fac64, fac32, dt64, dt32, ft, A->d_vals64,
-                                                            A->d_vals32, bnz);
-    };
-    const bool lap1 = single_laplace(ft);
-    if (A->slot_bytes == 1) {
-        if (lap1) launch(k_assemble_rows2<DIM, NB, NC, uint8_t, true>, (const uint8_t *)A->d_slot);
-        else launch(k_assemble_rows2<DIM, NB, NC, uint8_t, false>, (const uint8_t *)A->d_slot);
-    } else {
-        if (lap1) launch(k_assemble_rows2<DIM, NB, NC, uint16_t, true>, (const uint16_t *)A->d_slot);
-        else launch(k_assemble_rows2<DIM, NB, NC, uint16_t, false>, (const uint16_t *)A->d_slot);
-    }
-    GRMP_LAUNCHED(ctx);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // the tensor uploads are released next
     release();
@@ -436,34 +512,29 @@ int run_assembly(grmp_matrix A, const FastTerms &ft, const std::vector<double> &
         }
         vals = (T *)A->d_vals32;
     }
-    // rows per block: their values (the largest block's count) and the
-    // reference tensors in shared memory, at most ~100 KB so that two blocks fit an SM
+    // rows per block (autotuned per matrix and precision): their values (the
+    // largest block's count) and the reference tensors in shared memory
     const size_t tens_b = ((tens.size() + 1) & ~(size_t)1) * sizeof(T);
-    int tpb = 128, bnz = 0;
-    rc = block_nnz_max(A, tpb, &bnz);
-    while (!rc && tpb > 32 && tens_b + (size_t)bnz * sizeof(T) > 100 * 1024) {
-        tpb /= 2;
-        rc = block_nnz_max(A, tpb, &bnz);
-    }
+    const bool lap1 = single_laplace(ft);
+    auto go = [&](int tpb, size_t shm) {
+        auto launch = [&](auto kern, const auto *slot) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+            kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc,
+                                                                slot, A->d_rowptr, fac, dtens, ft, vals);
+            GRMP_LAUNCHED(ctx);
+        };
+        if (A->slot_bytes == 1) {
+            if (lap1) launch(k_assemble_rows<DIM, NB, NC, T, uint8_t, true>, (const uint8_t *)A->d_slot);
+            else launch(k_assemble_rows<DIM, NB, NC, T, uint8_t, false>, (const uint8_t *)A->d_slot);
+        } else {
+            if (lap1) launch(k_assemble_rows<DIM, NB, NC, T, uint16_t, true>, (const uint16_t *)A->d_slot);
+            else launch(k_assemble_rows<DIM, NB, NC, T, uint16_t, false>, (const uint16_t *)A->d_slot);
+        }
+    };
+    rc = assemble_rows_tuned(A, tens_b, sizeof(T), &A->asm_tpb[sizeof(T) == 8 ? 0 : 1], go);
     if (rc) {
         grmp_free(ctx, dtens, tens.size() * sizeof(T));
         return rc;
-    }
-    size_t shm = tens_b + (size_t)bnz * sizeof(T);
-    if (shm > 220 * 1024) return grmp_fail(ctx, GRMP_ERR_UNSUPPORTED, "assembly: rows too long for shared memory");
-    auto launch = [&](auto kern, const auto *slot) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        kern<<<nblk(A->nrows, tpb), tpb, shm, ctx->stream>>>(A->nrows, s->d_inc_ptr, s->d_inc_cell, s->d_inc_loc, slot,
-                                                            A->d_rowptr, fac, dtens, ft, vals);
-        GRMP_LAUNCHED(ctx);
-    };
-    const bool lap1 = single_laplace(ft);
-    if (A->slot_bytes == 1) {
-        if (lap1) launch(k_assemble_rows<DIM, NB, NC, T, uint8_t, true>, (const uint8_t *)A->d_slot);
-        else launch(k_assemble_rows<DIM, NB, NC, T, uint8_t, false>, (const uint8_t *)A->d_slot);
-    } else {
-        if (lap1) launch(k_assemble_rows<DIM, NB, NC, T, uint16_t, true>, (const uint16_t *)A->d_slot);
-        else launch(k_assemble_rows<DIM, NB, NC, T, uint16_t, false>, (const uint16_t *)A->d_slot);
     }
     cudaError_t e = cudaGetLastError();
     grmp_free(ctx, dtens, tens.size() * sizeof(T));

@@ -124,9 +124,12 @@ struct grmp_matrix_s {
     double *d_imp_diag = nullptr;      // [nrows] the caller's diagonal
     double *d_imp_b = nullptr;         // [nrows] right-hand side of the eliminated system
     int *d_imp_count = nullptr;
-    // largest value count of a block of blk_tpb consecutive rows (assembly's
-    // shared-memory accumulator; 0 = not computed)
-    int blk_tpb = 0, blk_nnz = 0;
+    // largest value count of a block of 32 / 64 / 128 consecutive rows (the
+    // row-assembly kernels' shared-memory accumulator; -1 = not counted yet)
+    int blk_nnz[3] = {-1, -1, -1};
+    // rows per block of the row-assembly kernels, autotuned at the first
+    // assembly: [0] FP64, [1] FP32, [2] both precisions in one walk (0 = not yet)
+    int asm_tpb[3] = {0, 0, 0};
     // per-cell geometric factors (scratch for assembly)
     void *d_cellfac = nullptr;
     size_t cellfac_bytes = 0;

@@ -160,6 +160,11 @@ int build_resident(grmp_context ctx, Request &r, Resident &res) {
             for (size_t i = 0; i < pt.size(); i++)
                 pt[i].cell_coef = r.term_coef[i].empty() ? nullptr : r.term_coef[i].data();
         rc = grmp_pattern_build(res.space, (int)pt.size(), pt.data(), &res.A);
+        // no timed choice of the assembly's block shape for served requests:
+        // a request's latency must not pay trial launches (nor depend on the
+        // other requests sharing the GPU while they run)
+        if (!rc)
+            for (int &t : res.A->asm_tpb) t = -1;
     }
     if (!rc) rc = grmp_vector_create(ctx, res.ndofs, &res.b);
     if (!rc) rc = grmp_vector_create(ctx, res.ndofs, &res.x);
