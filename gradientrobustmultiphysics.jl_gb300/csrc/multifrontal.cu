@@ -560,38 +560,42 @@ __global__ void __launch_bounds__(kTB) k_mf_qmul_level(MfDev m, const long long 
     }
 }
 
-// backward: x_k = sum_j Q[j][k] y_j - sum_i G[i][k] x_struct_i.  A block
-// takes 32 consecutive own columns of the level (tx = column) and splits
-// the rows over 8 groups (ty); the 8 partial sums are added in a fixed order.
+// backward: x_k = sum_j Q[j][k] y_j - sum_i G[i][k] x_struct_i over the
+// level's tiles of 32 consecutive own columns of one front (`bcol`: the
+// prefix of tiles per front in level order).  A block of 32 x 32 threads
+// takes a tile: lane tx = column kb + tx, warp ty = rows kb + ty, kb + ty +
+// 32, ...; all lanes of a warp read the same row of Q (32 consecutive
+// columns: one coalesced line) and the same right-hand value, skipping rows
+// above their column's diagonal; the 32 partial sums of a column are added in
+// a fixed order.
+constexpr int kQtT = 1024;
+
 template <typename T>
-__global__ void __launch_bounds__(kTB) k_mf_qtmul_level(MfDev m, const long long *scol, int lb, int cnt, const T *Q,
-                                                        const T *wy, T *wx) {
-    __shared__ T part[8][33];
-    const long long c0 = scol[lb], ncols = scol[lb + cnt] - c0;
+__global__ void __launch_bounds__(kQtT) k_mf_qtmul_level(MfDev m, const long long *bcol, int lb, int cnt, const T *Q,
+                                                         const T *wy, T *wx) {
+    __shared__ T part[32][33];
+    const long long t0 = bcol[lb], ntiles = bcol[lb + cnt] - t0;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (long long base = (long long)blockIdx.x * 32; base < ncols; base += (long long)gridDim.x * 32) {
-        const long long it = base + tx;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int idx = find_seg(bcol, lb, lb + cnt, t0 + t);
+        const MfNode nd = m.node[m.lvl_nodes[idx]];
+        const int s = nd.s, f = nd.f;
+        const int kb = (int)(t0 + t - bcol[idx]) * 32;
+        const int k = kb + tx;
+        const int32_t *fr = m.front + nd.front_off;
+        const T *Qk = Q + nd.L_off + k;
         T acc = T(0);
-        int k = 0, idx = lb;
-        if (it < ncols) {
-            idx = find_seg(scol, lb, lb + cnt, c0 + it);
-            const MfNode nd = m.node[m.lvl_nodes[idx]];
-            const int s = nd.s, f = nd.f;
-            k = (int)(c0 + it - scol[idx]);
-            const int32_t *fr = m.front + nd.front_off;
-            const T *Qt = Q + nd.L_off;
-            for (int j = k + ty; j < f; j += 8) {
+        if (k < s)
+            for (int j = kb + ty; j < f; j += 32) {
                 const T v = j < s ? wy[fr[j]] : -wx[fr[j]];
-                acc += Qt[(long long)j * s + k] * v;
+                if (j >= k) acc += Qk[(long long)j * s] * v;
             }
-        }
         part[ty][tx] = acc;
         __syncthreads();
-        if (ty == 0 && it < ncols) {
+        if (ty == 0 && k < s) {
             T sum = T(0);
-            for (int g = 0; g < 8; g++) sum += part[g][tx];
-            const MfNode nd = m.node[m.lvl_nodes[idx]];
-            wx[m.front[nd.front_off + k]] = sum;
+            for (int g = 0; g < 32; g++) sum += part[g][tx];
+            wx[fr[k]] = sum;
         }
         __syncthreads();
     }
@@ -760,6 +764,7 @@ struct MfCache {
     size_t Qb = 0;
     // prefixes over fronts in level order: rows (f), own columns (s), G entries (sc * s)
     const long long *qrow = nullptr, *scol = nullptr, *gpref = nullptr, *bcol = nullptr;
+    std::vector<long long> bcol_host;   // the same prefix of 32-column tiles, for launch sizes
     long long total_cols = 0, total_g = 0, total_bcols = 0;
     // the preconditioner's level launches (w -> wx), captured once per numeric storage
     cudaGraphExec_t apply_graph = nullptr;
@@ -867,6 +872,7 @@ int mf_build(grmp_matrix A) {
     C->total_cols = scol[S.nnodes];
     C->total_g = gpref[S.nnodes];
     C->total_bcols = bcol[S.nnodes];
+    C->bcol_host = bcol;
     A->mf = C;
     int rc = mf_upload(ctx, *C, node, &C->dev.node);
     if (!rc) rc = mf_upload(ctx, *C, S.front, &C->dev.front);
@@ -1034,8 +1040,10 @@ int mf_enqueue_inverse(grmp_matrix A) {
     }
     for (int l = nl - 1; l >= 0; l--) {
         const int lb = C.level_ptr[l], cnt = C.level_ptr[l + 1] - lb;
-        k_mf_qtmul_level<T><<<grid, kTB, 0, ctx->stream>>>(C.dev, C.scol, lb, cnt, (const T *)C.Q, (const T *)C.wy,
-                                                          (T *)C.wx);
+        const long long tiles = C.bcol_host[lb + cnt] - C.bcol_host[lb];
+        const int tgrid = (int)std::max<long long>(1, std::min<long long>(tiles, 2LL * ctx->num_sms));
+        k_mf_qtmul_level<T><<<tgrid, kQtT, 0, ctx->stream>>>(C.dev, C.bcol, lb, cnt, (const T *)C.Q, (const T *)C.wy,
+                                                            (T *)C.wx);
         k++;
     }
     return k;
