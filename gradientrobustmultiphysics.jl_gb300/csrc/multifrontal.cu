@@ -491,21 +491,65 @@ __global__ void __launch_bounds__(kTB) k_mf_invert(MfDev m, const long long *bco
     }
 }
 
-// G = L21 L11^-1, one thread per entry (i, k)
+// G = L21 L11^-1 of every front, as tiles of 64 x 64 entries (rows i of the
+// structure part, columns k): a 256-thread block per tile, the product over
+// m in 32-wide slabs of L21 (64 x 32) and L11^-1 (32 x 64) staged in shared
+// memory, 4 x 4 outputs per thread.  L11^-1 is lower triangular and only
+// its blocks on or below the diagonal are stored, so entries with m < k are
+// read as zero.  Tiles: {level-order front index, first row, first column}.
+constexpr int kGmT = 64, kGmK = 32;
+
 template <typename T>
-__global__ void k_mf_gmat(MfDev m, const long long *gpref, int nn, long long total, const T *L, T *Q) {
-    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (item >= total) return;
-    const int idx = find_seg(gpref, 0, nn, item);
-    const MfNode nd = m.node[m.lvl_nodes[idx]];
-    const int s = nd.s;
-    const long long e = item - gpref[idx];
-    const int i = (int)(e / s), k = (int)(e - (long long)i * s);
-    const T *Lr = L + nd.L_off + (long long)(s + i) * s;
-    const T *Qt = Q + nd.L_off;
-    T acc = T(0);
-    for (int mm = k; mm < s; mm++) acc += Lr[mm] * Qt[(long long)mm * s + k];
-    Q[nd.L_off + (long long)(s + i) * s + k] = acc;
+__global__ void __launch_bounds__(256) k_mf_gmat(MfDev m, const int4 *tiles, long long ntiles, const T *L, T *Q) {
+    __shared__ T As[kGmK][kGmT + 1];   // As[mm][i]
+    __shared__ T Bs[kGmK][kGmT + 1];   // Bs[mm][k]
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 4 x 4 outputs each
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int4 tl = tiles[t];
+        const MfNode nd = m.node[m.lvl_nodes[tl.x]];
+        const int s = nd.s, sc = nd.f - nd.s, i0 = tl.y, k0 = tl.z;
+        const T *L21 = L + nd.L_off + (long long)s * s;   // row i of the structure part: L21 + i * s
+        const T *Qt = Q + nd.L_off;
+        T acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+        for (int m0 = k0; m0 < s; m0 += kGmK) {
+            for (int q = threadIdx.x; q < kGmK * kGmT; q += 256) {
+                const int mm = q % kGmK, ii = q / kGmK;   // A: consecutive threads along m (row-major L21)
+                const int gi = i0 + ii, gm = m0 + mm;
+                As[mm][ii] = (gi < sc && gm < s) ? L21[(long long)gi * s + gm] : T(0);
+                const int kk = q % kGmT, m2 = q / kGmT;    // B: consecutive threads along k (row-major Q)
+                const int gk = k0 + kk, gm2 = m0 + m2;
+                Bs[m2][kk] = (gk < s && gm2 < s && gm2 >= gk) ? Qt[(long long)gm2 * s + gk] : T(0);
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int mm = 0; mm < kGmK; mm++) {
+                T av[4], bv[4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) av[a] = As[mm][ty * 4 + a];
+#pragma unroll
+                for (int b = 0; b < 4; b++) bv[b] = Bs[mm][tx * 4 + b];
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[a][b] += av[a] * bv[b];
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const int gi = i0 + ty * 4 + a;
+            if (gi >= sc) continue;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const int gk = k0 + tx * 4 + b;
+                if (gk < s) Q[nd.L_off + (long long)(s + gi) * s + gk] = acc[a][b];
+            }
+        }
+    }
 }
 
 // forward, part 1 (block per front): the children's update entries, own ones
@@ -763,9 +807,10 @@ struct MfCache {
     void *Q = nullptr, *wy = nullptr, *wx = nullptr;
     size_t Qb = 0;
     // prefixes over fronts in level order: rows (f), own columns (s), G entries (sc * s)
-    const long long *qrow = nullptr, *scol = nullptr, *gpref = nullptr, *bcol = nullptr;
+    const long long *qrow = nullptr, *scol = nullptr, *bcol = nullptr;
     std::vector<long long> bcol_host;   // the same prefix of 32-column tiles, for launch sizes
-    long long total_cols = 0, total_g = 0, total_bcols = 0;
+    const int4 *gtiles = nullptr;       // 64 x 64 tiles of every front's L21 L11^-1
+    long long total_cols = 0, total_gtiles = 0, total_bcols = 0;
     // the preconditioner's level launches (w -> wx), captured once per numeric storage
     cudaGraphExec_t apply_graph = nullptr;
     int apply_kernels = 0;
@@ -860,17 +905,18 @@ int mf_build(grmp_matrix A) {
         C->ppool = std::max(C->ppool, g * mf * kWideStride);   // the grid-wide path's panels are kWide wide
     }
     C->level_nodes_host = order;
-    std::vector<long long> qrow(S.nnodes + 1, 0), scol(S.nnodes + 1, 0), gpref(S.nnodes + 1, 0),
-        bcol(S.nnodes + 1, 0);
+    std::vector<long long> qrow(S.nnodes + 1, 0), scol(S.nnodes + 1, 0), bcol(S.nnodes + 1, 0);
+    std::vector<int4> gtiles;
     for (int i = 0; i < S.nnodes; i++) {
         const NdNode &q = S.node[order[i]];
         qrow[i + 1] = qrow[i] + q.f;
         scol[i + 1] = scol[i] + q.s;
-        gpref[i + 1] = gpref[i] + (long long)(q.f - q.s) * q.s;
         bcol[i + 1] = bcol[i] + (q.s + 31) / 32;
+        for (int i0 = 0; i0 < q.f - q.s; i0 += kGmT)
+            for (int k0 = 0; k0 < q.s; k0 += kGmT) gtiles.push_back(make_int4(i, i0, k0, 0));
     }
     C->total_cols = scol[S.nnodes];
-    C->total_g = gpref[S.nnodes];
+    C->total_gtiles = (long long)gtiles.size();
     C->total_bcols = bcol[S.nnodes];
     C->bcol_host = bcol;
     A->mf = C;
@@ -883,7 +929,7 @@ int mf_build(grmp_matrix A) {
     if (!rc) rc = mf_upload(ctx, *C, order, &C->dev.lvl_nodes);
     if (!rc) rc = mf_upload(ctx, *C, qrow, &C->qrow);
     if (!rc) rc = mf_upload(ctx, *C, scol, &C->scol);
-    if (!rc) rc = mf_upload(ctx, *C, gpref, &C->gpref);
+    if (!rc) rc = mf_upload(ctx, *C, gtiles, &C->gtiles);
     if (!rc) rc = mf_upload(ctx, *C, bcol, &C->bcol);
     if (!rc) {
         e = cudaStreamSynchronize(ctx->stream);
@@ -1005,16 +1051,14 @@ int mf_build_inverse(grmp_matrix A) {
         if (!rc) rc = grmp_alloc(ctx, &C.wx, C.wb);
         if (rc) return rc;
     }
-    const int tb = 256;
     if (C.total_bcols > 0) {
         k_mf_invert<T><<<(unsigned)C.total_bcols, kTB, 0, ctx->stream>>>(C.dev, C.bcol, C.nnodes, (const T *)C.L,
                                                                         (T *)C.Q);
         GRMP_LAUNCHED(ctx);
     }
-    if (C.total_g > 0) {
-        k_mf_gmat<T><<<(unsigned)((C.total_g + tb - 1) / tb), tb, 0, ctx->stream>>>(C.dev, C.gpref, C.nnodes,
-                                                                                   C.total_g, (const T *)C.L,
-                                                                                   (T *)C.Q);
+    if (C.total_gtiles > 0) {
+        const int gg = (int)std::min<long long>(C.total_gtiles, 8LL * ctx->num_sms);
+        k_mf_gmat<T><<<gg, 256, 0, ctx->stream>>>(C.dev, C.gtiles, C.total_gtiles, (const T *)C.L, (T *)C.Q);
         GRMP_LAUNCHED(ctx);
     }
     cudaError_t e = cudaGetLastError();
