@@ -448,6 +448,8 @@ template <typename T>
 __global__ void __launch_bounds__(kTB) k_mf_invert(MfDev m, const long long *bcol, int nn, const T *L, T *Q) {
     __shared__ T Lbb[32][33];
     __shared__ T Tb[32][33];
+    __shared__ T Ls[32][33];   // slab of L_b,[k0, k0+32)
+    __shared__ T Xs[32][33];   // slab of X_[k0, k0+32),c
     const long long item = blockIdx.x;
     const int idx = find_seg(bcol, 0, nn, item);
     const MfNode nd = m.node[m.lvl_nodes[idx]];
@@ -459,20 +461,31 @@ __global__ void __launch_bounds__(kTB) k_mf_invert(MfDev m, const long long *bco
     const int c0 = c * 32, cw = min(32, s - c0);
     for (int b = c; b < nbk; b++) {
         const int b0 = b * 32, bw = min(32, s - b0);
-        // Tb = (b == c ? I : -sum_m L_bm X_mc), Lbb = L_bb
+        // Tb = (b == c ? I : -sum_m L_bm X_mc), Lbb = L_bb.  The sum runs over
+        // k in [c0, b0) (whole 32-slabs) with both factors staged in shared
+        // memory, k ascending as a plain loop would take it.
         for (int q = tid; q < 32 * 32; q += blockDim.x) {
             const int r = q >> 5, cc = q & 31;
-            T acc = T(0);
-            if (r < bw && cc < cw) {
-                if (b == c) {
-                    acc = r == cc ? T(1) : T(0);
-                } else {
-                    const T *Lr = Lt + (long long)(b0 + r) * s;
-                    for (int k = c0; k < b0; k++) acc -= Lr[k] * Qt[(long long)k * s + c0 + cc];
+            Tb[r][cc] = (b == c && r == cc && r < bw) ? T(1) : T(0);
+            Lbb[r][cc] = (r < bw && cc <= r) ? Lt[(long long)(b0 + r) * s + b0 + cc] : T(0);
+        }
+        if (b > c) {
+            for (int k0 = c0; k0 < b0; k0 += 32) {
+                __syncthreads();
+                for (int q = tid; q < 32 * 32; q += blockDim.x) {
+                    const int r = q >> 5, cc = q & 31;
+                    Ls[r][cc] = r < bw ? Lt[(long long)(b0 + r) * s + k0 + cc] : T(0);
+                    Xs[r][cc] = cc < cw ? Qt[(long long)(k0 + r) * s + c0 + cc] : T(0);
+                }
+                __syncthreads();
+                for (int q = tid; q < 32 * 32; q += blockDim.x) {
+                    const int r = q >> 5, cc = q & 31;
+                    T acc = Tb[r][cc];
+#pragma unroll 8
+                    for (int kk = 0; kk < 32; kk++) acc -= Ls[r][kk] * Xs[kk][cc];
+                    Tb[r][cc] = acc;
                 }
             }
-            Tb[r][cc] = acc;
-            Lbb[r][cc] = (r < bw && cc <= r) ? Lt[(long long)(b0 + r) * s + b0 + cc] : T(0);
         }
         __syncthreads();
         if (warp == 0 && lane < cw) {   // forward substitution, column `lane`
