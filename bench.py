@@ -201,6 +201,29 @@ def cpu_port_step(prob, reltol: float):
     return FES.ndofs, t2 - t0, t1 - t0, t2 - t1, it, A, bb, x
 
 
+# sample of the single-core CPU baseline per workload (bounded to a few seconds
+# of one core; the all-core baseline runs the full workload)
+SINGLE_CORE_N = {"poisson3d": 24, "poisson2d": 128, "elasticity2d": 16}
+
+
+def cpu_single_core(P, args, n: int = None) -> dict:
+    """The oracle port on ONE host core (the reference assembles in one Julia
+    task, src/assemblypatterns/bilinearform.jl:226), on a bounded sample of
+    the workload: assembly in the reference's item-loop order + FP64
+    Jacobi-CG to the workload's tolerance."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    n = n or SINGLE_CORE_N[args.workload]
+    O.set_threads(1)
+    try:
+        d, dt, ta, ts, it, _, _, _ = cpu_port_step(make_problem(P, args, args.seed, n), args.reltol)
+    finally:
+        O.set_threads(0)
+    return {"value": d / dt, "unit": "DoF/s", "cores": 1, "kind": "port",
+            "sample": f"{WORKLOADS[args.workload][0].format(n=n)}, {d} DoFs: oracle assembly {ta:.2f}s + "
+                      f"1-thread FP64 Jacobi-CG {ts:.2f}s ({it} it)"}
+
+
 def oracle_reference(prob, reltol: float) -> dict:
     """The CPU baseline and the independent FP64 reference solution of the
     workload, from the oracle alone (nothing of the GPU library): one timed
@@ -525,7 +548,8 @@ def run_ours(args):
         cpu = {"value": d / dt, "unit": "DoF/s", "cores": cores, "kind": "port",
                "sample": f"{WORKLOADS[args.workload][0].format(n=args.cpu_n if direct else args.n)}, {d} DoFs: "
                          f"oracle assembly (reference item loop, rows over {cores} threads) {ta:.2f}s + "
-                         f"{cores}-thread FP64 Jacobi-CG {ts:.2f}s ({it} it)"}
+                         f"{cores}-thread FP64 Jacobi-CG {ts:.2f}s ({it} it)",
+               "single_core": cpu_single_core(P, args)}
     errs = {}
     for mode in ("mixed", "fp64"):
         errs[mode] = (float(np.linalg.norm(results[mode]["u"] - uref) / np.linalg.norm(uref))

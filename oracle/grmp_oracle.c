@@ -40,6 +40,18 @@
 #define OR_MAXQ 128
 #define OR_MAXD 32
 
+/* Threads of the OpenMP regions that follow (assembly rows, CG): n > 0
+ * threads, n <= 0 all processors.  Lets the CPU baseline be timed on one
+ * core (the reference assembles in one Julia task) beside all cores. */
+void oracle_set_threads(int n)
+{
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+#else
+    (void)n;
+#endif
+}
+
 /* Row range [lo, hi) of the calling thread (the whole range outside a
  * parallel region). */
 static void or_row_range(int n, int *lo, int *hi)

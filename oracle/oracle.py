@@ -84,6 +84,8 @@ def lib():
         L.oracle_item_l2error_br.restype = ctypes.c_int
         L.oracle_cg.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
         L.oracle_cg.restype = ctypes.c_int
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_set_threads.restype = None
         L.oracle_resid_dd.argtypes = [ctypes.c_int, llp, ip, dp, dp, dp, dp]
         L.oracle_resid_dd.restype = None
         sp = ctypes.POINTER(ctypes.c_byte)
@@ -333,6 +335,11 @@ def solve_direct(A, b):
     """FP64 sparse-direct solve (SuperLU standing in for UMFPACK)."""
     import scipy.sparse.linalg as spla
     return spla.spsolve(A.tocsc(), b)
+
+
+def set_threads(n: int):
+    """Threads of the oracle's OpenMP regions (n <= 0: all processors)."""
+    lib().oracle_set_threads(int(n))
 
 
 def solve_cg(A, b, reltol=1e-14, maxit=100000):

@@ -61,3 +61,15 @@ def test_roofline_kernel_names_and_traffic_ratios():
     assert B.pcg_kernel(80204) == "k_pcg_mixed_duo"
     for k in ("k_pcg_mixed", "k_pcg_mixed_duo", "k_pcg_mixed_duo_keep"):
         assert 0.5 < B.TRAFFIC_RATIO[k] < 1.0
+
+
+def test_single_core_cpu_baseline():
+    """The one-core CPU baseline runs the oracle port with one OpenMP thread
+    and restores all threads afterwards."""
+    import types
+    B = _bench_module()
+    import grmp_gb300.problems as P
+    args = types.SimpleNamespace(workload="poisson3d", seed=0, reltol=1e-11, n=None)
+    out = B.cpu_single_core(P, args, n=4)
+    assert out["cores"] == 1 and out["value"] > 0 and out["kind"] == "port"
+    assert "729 DoFs" in out["sample"]
